@@ -1,0 +1,502 @@
+"""CPU oracle for the synaptogenesis per-timestep cycle (TEST INFRASTRUCTURE).
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
+this module, and only as the checker.  The product never imports it.
+
+It restates, in Python plus the C file ``sg_oracle.c``:
+  * the JSON network schema with the reference's defaults and quirks
+    (network/connection_config.cpp:8-45, 112-134, 207-257;
+    network/layer_config.cpp:11-33; network/connection.cpp:7-61),
+  * the state each neural model allocates (state/attributes.cpp:16-37,
+    state/impl/izhikevich_attributes.cpp:587-757), in the reference's host
+    layout, under the reference's variable names,
+  * the engine's synchronous step order for "parallel" structures
+    (engine/engine.cpp:226-315, engine/cluster/parallel_cluster.cpp:27-131,
+    engine/cluster/cluster_node.cpp:7-212, engine/instruction.cpp:3-30).
+Random initialisers of the reference are unseedable (util/tools.h:8); the
+oracle draws them from a seeded numpy generator instead, and parity runs
+inject every random quantity explicitly.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_BUILD = os.path.join(HERE, "_build")
+_LIB_PATH = os.path.join(_BUILD, "libsgoracle.so")
+
+FLOAT, BIT, INT = 0, 1, 2
+CONN_TYPES = {"fully connected": 0, "subset": 1, "one to one": 2, "convergent": 3, "divergent": 4}
+OPCODES = {"add": 0, "sub": 1, "mult": 2, "div": 3, "pool": 4, "reward": 5, "modulate": 6,
+           "gap": 7, "add_heaviside": 8, "sub_heaviside": 9, "mult_heaviside": 10}
+MODELS = {"izhikevich": BIT, "relay": FLOAT, "game_of_life": BIT, "rate_encoding": FLOAT}
+IZ_PARAMS = {  # izhikevich_attributes.cpp:28-35
+    "default": (0.02, 0.2, -70.0, 2), "regular": (0.02, 0.2, -65.0, 8),
+    "bursting": (0.02, 0.2, -55.0, 4), "chattering": (0.02, 0.2, -50.0, 2),
+    "fast": (0.1, 0.2, -65.0, 2), "low_threshold": (0.02, 0.25, -65.0, 2),
+    "thalamo_cortical": (0.02, 0.25, -65.0, 0.05), "resonator": (0.1, 0.26, -65.0, 2)}
+
+
+def build_lib():
+    os.makedirs(_BUILD, exist_ok=True)
+    src = os.path.join(HERE, "sg_oracle.c")
+    if not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
+                        "-o", _LIB_PATH, src, "-lm"], check=True)
+    return _LIB_PATH
+
+
+class _Conn(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in (
+        "type", "opcode", "convolutional", "num_weights",
+        "from_rows", "from_cols", "to_rows", "to_cols",
+        "row_field", "col_field", "row_stride", "col_stride",
+        "row_spacing", "col_spacing", "row_offset", "col_offset", "wrap",
+        "fr0", "fr1", "fc0", "fc1", "tr0", "tr1", "tc0", "tc1")]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build_lib())
+        _lib.sg_visits.restype = ctypes.c_long
+        _lib.sg_istdp_src.restype = ctypes.c_float
+        _lib.sg_istdp_dst.restype = ctypes.c_float
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+# ---------------------------------------------------------------------------
+# Property semantics: values are strings (builder.cpp:15-39); the Python
+# front-end converts bool -> "true"/"false" and everything else with str().
+# ---------------------------------------------------------------------------
+class Props:
+    def __init__(self, d):
+        self.d = {}
+        self.children = {}
+        self.arrays = {}
+        self.child_arrays = {}
+        for k, v in (d or {}).items():
+            if v is None:
+                continue
+            if isinstance(v, dict):
+                self.children[k] = Props(v)
+            elif isinstance(v, list):
+                for x in v:
+                    if isinstance(x, dict):
+                        self.child_arrays.setdefault(k, []).append(Props(x))
+                    else:
+                        self.arrays.setdefault(k, []).append(
+                            ("true" if x else "false") if isinstance(x, bool) else str(x))
+            else:
+                self.d[k] = ("true" if v else "false") if isinstance(v, bool) else str(v)
+
+    def has(self, k):
+        return k in self.d
+
+    def get(self, k, default=""):
+        return self.d.get(k, default)
+
+    def get_int(self, k, default):  # std::stoi: leading integer
+        if k not in self.d:
+            return default
+        s = self.d[k].strip()
+        i = 0
+        if i < len(s) and s[i] in "+-":
+            i += 1
+        while i < len(s) and s[i].isdigit():
+            i += 1
+        return int(s[:i])
+
+    def get_float(self, k, default):
+        return float(np.float32(float(self.d[k]))) if k in self.d else float(np.float32(default))
+
+    def get_bool(self, k, default):
+        return self.d[k] == "true" if k in self.d else default
+
+    def child(self, k):
+        return self.children.get(k)
+
+
+class Layer:
+    def __init__(self, structure, p):
+        self.structure = structure
+        self.p = p
+        self.name = p.get("name")
+        self.model = p.get("neural model")
+        if self.model not in MODELS:
+            raise ValueError("oracle: unsupported neural model " + self.model)
+        self.rows = p.get_int("rows", 0)
+        self.cols = p.get_int("columns", 0)
+        if self.rows <= 0 or self.cols <= 0:
+            raise ValueError("invalid layer dimensions")
+        self.size = self.rows * self.cols
+        self.output_type = MODELS[self.model]
+        self.inputs, self.outputs = [], []
+        if p.child_arrays.get("dendrites"):
+            raise ValueError("oracle: dendritic trees are not restated")
+
+
+class Conn:
+    def __init__(self, p, frm, to):
+        self.p = p
+        self.name = p.get("name", "")
+        self.frm, self.to = frm, to
+        self.plastic = p.get_bool("plastic", True)            # connection_config.cpp:213
+        self.delay = p.get_int("delay", 0)
+        self.max_weight = p.get_float("max weight", 1.0)
+        self.type = CONN_TYPES[p.get("type", "fully connected")]
+        self.opcode = OPCODES[p.get("opcode", "add")]
+        self.convolutional = p.get_bool("convolutional", False)
+        if p.get_bool("sparse", False) or p.get_bool("randomized projection", False):
+            raise ValueError("oracle: sparse / randomized projections are not restated")
+        c = _Conn()
+        c.type, c.opcode, c.convolutional = self.type, self.opcode, int(self.convolutional)
+        c.from_rows, c.from_cols, c.to_rows, c.to_cols = frm.rows, frm.cols, to.rows, to.cols
+        if self.type in (3, 4):
+            a = p.child("arborized config")
+            rf = a.get_int("row field size", 0)
+            cf = a.get_int("column field size", 0)
+            rs = a.get_int("row stride", 1)
+            cs = a.get_int("column stride", 1)
+            rsp = a.get_int("row spacing", 1)
+            csp = a.get_int("column spacing", 1)
+            ro = a.get_int("row offset", 0)
+            co = a.get_int("row offset", 0)      # quirk: connection_config.cpp:16
+            wrap = a.get_bool("wrap", False)
+            if a.has("field size"):
+                rf = cf = a.get_int("field size", 0)
+            if a.has("stride"):
+                rs = cs = a.get_int("stride", 0)
+            if a.has("spacing"):
+                rsp = csp = a.get_int("spacing", 0)
+            if a.has("offset"):
+                ro = co = a.get_int("offset", 0)
+            if rf <= 0 or cf <= 0 or rs < 0 or cs < 0 or rsp < 1 or csp < 1:
+                raise ValueError("invalid arborized config")
+            if not a.has("row offset") and not a.has("offset"):
+                ro = int(-rf / 2)
+            if not a.has("column offset") and not a.has("offset"):
+                co = int(-cf / 2)
+            if self.type == 4 and (rs == 0 or cs == 0):
+                raise ValueError("divergent connections cannot have zero stride")
+            (c.row_field, c.col_field, c.row_stride, c.col_stride, c.row_spacing,
+             c.col_spacing, c.row_offset, c.col_offset, c.wrap) = rf, cf, rs, cs, rsp, csp, ro, co, int(wrap)
+            self.num_weights = rf * cf if self.convolutional else to.size * rf * cf
+        elif self.type == 1:
+            s = p.child("subset config")
+            c.fr0, c.fr1 = s.get_int("from row start", 0), s.get_int("from row end", 0)
+            c.tr0, c.tr1 = s.get_int("to row start", 0), s.get_int("to row end", 0)
+            c.fc0, c.fc1 = s.get_int("from column start", 0), s.get_int("from column end", 0)
+            c.tc0, c.tc1 = s.get_int("to column start", 0), s.get_int("to column end", 0)
+            self.num_weights = (c.fr1 - c.fr0) * (c.fc1 - c.fc0) * (c.tr1 - c.tr0) * (c.tc1 - c.tc0)
+        elif self.type == 2:
+            if frm.rows != to.rows or frm.cols != to.cols:
+                raise ValueError("one to one between differently sized layers")
+            self.num_weights = to.size
+        else:
+            self.num_weights = frm.size * to.size
+        c.num_weights = self.num_weights
+        self.c = c
+        self._visits()
+
+    def _visits(self):
+        L = lib()
+        rows = ctypes.c_int()
+        n = L.sg_visits(ctypes.byref(self.c), ctypes.byref(rows), None, None, None, None, None, None)
+        nrows = max(self.to.size, 1) + 1
+        self.dst = np.zeros(nrows, np.int32)
+        self.ptr = np.zeros(nrows + 1, np.int64)
+        self.from_idx = np.zeros(max(n, 1), np.int32)
+        self.w_idx = np.zeros(max(n, 1), np.int32)
+        self.pre_row = np.zeros(max(n, 1), np.int32)
+        self.pre_col = np.zeros(max(n, 1), np.int32)
+        L.sg_visits(ctypes.byref(self.c), ctypes.byref(rows), _p(self.dst), _p(self.ptr),
+                    _p(self.from_idx), _p(self.w_idx), _p(self.pre_row), _p(self.pre_col))
+        self.rows = rows.value
+        self.nvisits = n
+
+    def matrix_rows_cols(self):  # connection.cpp:229-248
+        if self.convolutional:
+            rows = 1
+        elif self.type == 1:
+            rows = (self.c.tr1 - self.c.tr0) * (self.c.tc1 - self.c.tc0)
+        else:
+            rows = self.to.size
+        if self.type == 1:
+            cols = (self.c.fr1 - self.c.fr0) * (self.c.fc1 - self.c.fc0)
+        elif self.type in (3, 4):
+            cols = self.c.row_field * self.c.col_field
+        elif self.type == 2:
+            cols = 1
+        else:
+            cols = self.frm.size
+        return rows, cols
+
+
+class OracleNetwork:
+    """Builds the network and its state from a reference-schema dict."""
+
+    def __init__(self, net, seed=0):
+        self.rng = np.random.default_rng(seed)
+        top = Props(net)
+        self.layers, self.conns, self.structures = [], [], []
+        for sp in top.child_arrays.get("structures", []):
+            sname = sp.get("name")
+            if sp.get("type", "parallel") != "parallel":
+                raise ValueError("oracle: only parallel structures are restated")
+            self.structures.append(sname)
+            for lp in sp.child_arrays.get("layers", []):
+                self.layers.append(Layer(sname, lp))
+        for cp in top.child_arrays.get("connections", []):
+            frm = self._find(cp.get("from layer"), cp.get("from structure", None))
+            to = self._find(cp.get("to layer"), cp.get("to structure", None))
+            conn = Conn(cp, frm, to)
+            frm.outputs.append(conn)
+            to.inputs.append(conn)
+            self.conns.append(conn)
+        self._build_state()
+
+    def _find(self, name, structure):
+        hits = [l for l in self.layers if l.name == name and (structure is None or l.structure == structure)]
+        if len(hits) != 1:
+            raise ValueError("cannot resolve layer " + str(name))
+        return hits[0]
+
+    # -- state ------------------------------------------------------------
+    def _build_state(self):
+        self.neuron = {}
+        self.matrix = {}
+        L = lib()
+        for l in self.layers:
+            max_delay = max([c.delay for c in l.outputs] + [0])
+            l.history = 1 + (max_delay // 32 if l.output_type == BIT else max_delay)
+            st = {"input": np.zeros(l.size, np.float32),
+                  "output": np.zeros(l.history * l.size, np.uint32)}
+            if l.model == "izhikevich":
+                for k in ("ampa", "nmda", "gabaa", "gabab", "mult", "dopamine",
+                          "voltage", "recovery", "post trace"):
+                    st[k] = np.zeros(l.size, np.float32)
+                st["time since spike"] = np.full(l.size, 32, np.int32)
+                a, b, c, d = IZ_PARAMS[l.p.get("params", "regular")]
+                for k, v in zip("abcd", (a, b, c, d)):
+                    st[k] = np.full(l.size, v, np.float32)
+                L.sg_iz_init(l.size, _p(st["a"]), _p(st["b"]), _p(st["c"]),
+                             _p(st["voltage"]), _p(st["recovery"]))
+            self.neuron[l] = st
+        for c in self.conns:
+            self.matrix[c] = m = {"weights": self._init_weights(c)}
+            if c.to.model == "izhikevich":
+                n = c.num_weights
+                m["short trace"] = np.zeros(n, np.float32)
+                m["long trace"] = np.zeros(n, np.float32)
+                m["presyn trace"] = np.zeros(n, np.float32)
+                m["short term R"] = np.ones(n, np.float32)
+                # quirk F4: compares the ConnectionType with the ADD/SUB opcodes
+                # (izhikevich_attributes.cpp:723-728)
+                m["short term w"] = np.full(n, 0.5 if c.type == 0 else (0.2 if c.type == 1 else 0.0),
+                                            np.float32)
+                m["weight derivatives"] = np.full(n, 0.000001, np.float32)
+                m["time since spike"] = np.full(n, 32, np.int32)
+                if "delays" not in m:
+                    m["delays"] = self._default_delays(c)
+                c.baseline_conductance = c.p.get_float("conductance", 1.0)
+                c.learning_rate = c.p.get_float("learning rate", 0.1)
+                c.stp_flag = c.p.get("short term plasticity", "true") == "true"
+
+    def _init_weights(self, c):
+        wc = c.p.child("weight config") or Props({})
+        n = c.num_weights
+        t = wc.get("type", "flat")
+        if t == "flat":
+            w = np.full(n, wc.get_float("weight", 1.0), np.float32)
+            frac = wc.get_float("fraction", 1.0)
+            if frac != 1.0:
+                w = np.where(self.rng.random(n) < frac, w, 0).astype(np.float32)
+        elif t == "random":
+            w = self.rng.uniform(wc.get_float("min weight", 0.0),
+                                 wc.get_float("max weight", c.max_weight), n).astype(np.float32)
+        elif t == "specified":
+            vals = [float(x) for x in wc.get("weight string").split()]
+            w = np.array(vals[:n], np.float32)
+        else:
+            raise ValueError("oracle: weight config " + t)
+        if not wc.get_bool("diagonal", True):   # weight_matrix.cpp:951-977
+            if c.type == 0:
+                w[np.arange(c.frm.size) * c.frm.size + np.arange(c.frm.size)] = 0
+            elif c.type == 1:
+                fs = (c.c.fr1 - c.c.fr0) * (c.c.fc1 - c.c.fc0)
+                w[np.arange(fs) * fs + np.arange(fs)] = 0
+            elif c.type == 3:
+                self._circular_mask(c, w, radius=0.5, invert=True, value=0.0)
+        return w
+
+    @staticmethod
+    def _circular_mask(c, w, radius, invert, value):  # weight_matrix.cpp:749-824
+        rf, cf = c.c.row_field, c.c.col_field
+        rr = cr = np.float32(radius)
+        rc, cc = np.float32(rf) / np.float32(2), np.float32(cf) / np.float32(2)
+        rsq, csq = np.float32(rr * rr), np.float32(cr * cr)
+        sq_mult = np.float32(rsq * csq)
+        K = rf * cf
+        reps = 1 if c.convolutional else c.to.size
+        for kr in range(rf):
+            for kc in range(cf):
+                a = np.float32(np.float64(kr) + 0.5 - np.float64(rc))
+                b = np.float32(np.float64(kc) + 0.5 - np.float64(cc))
+                term = np.float32(np.float32(a * a) * csq) + np.float32(np.float32(b * b) * rsq)
+                if invert == (term <= sq_mult):
+                    w[np.arange(reps) * K + kr * cf + kc] = value
+
+    def _default_delays(self, c):  # izhikevich_attributes.cpp:732-751
+        n = c.num_weights
+        if c.p.get("myelinated", "false") == "true":
+            return np.full(n, c.delay, np.int32)
+        if c.p.has("random delay"):
+            raise ValueError("oracle: 'random delay' crashes the reference (unallocated delays)")
+        fr = np.full(n, -1, np.int32)
+        fcol = np.full(n, -1, np.int32)
+        tr = np.full(n, -1, np.int32)
+        tcol = np.full(n, -1, np.int32)
+        dst_of_visit = np.repeat(c.dst[:c.rows], np.diff(c.ptr[:c.rows + 1]))
+        wi = c.w_idx[:c.nvisits]
+        fr[wi] = c.pre_row[:c.nvisits]
+        fcol[wi] = c.pre_col[:c.nvisits]
+        tr[wi] = dst_of_visit // c.to.cols
+        tcol[wi] = dst_of_visit % c.to.cols
+        dist = np.zeros(n, np.float32)
+        delays = np.zeros(n, np.int32)
+        rc = lib().sg_distance_delays(
+            ctypes.c_long(n), _p(fr), _p(fcol), _p(tr), _p(tcol),
+            ctypes.c_float(c.frm.p.get_float("neuron spacing", 0.1)),
+            ctypes.c_float(c.to.p.get_float("neuron spacing", 0.1)),
+            ctypes.c_float(c.p.get_float("x offset", 0.0)),
+            ctypes.c_float(c.p.get_float("y offset", 0.0)),
+            ctypes.c_float(0.15), int(c.p.get("cap delay", "false") == "true"),
+            c.delay, _p(dist), _p(delays))
+        if rc != 0:
+            raise ValueError("BIT delays cannot be greater than 31")
+        return delays
+
+    # -- accessors mirroring the reference's getters -------------------------
+    def layer(self, name):
+        return self._find(name, None)
+
+    def connection(self, name):
+        hits = [c for c in self.conns if c.name == name]
+        return hits[-1]
+
+    def get_neuron_data(self, layer, key):
+        return self.neuron[self.layer(layer)][key]
+
+    def get_weight_matrix(self, conn, key="weights"):
+        return self.matrix[self.connection(conn)][key]
+
+    # -- one timestep ------------------------------------------------------
+    def step(self, inputs=None, learning=True):
+        """inputs: {layer name: float32 array} for layers fed by an input module."""
+        inputs = inputs or {}
+        L = lib()
+        # init / input transfer (instruction.cpp:3-30, instruction.h:474-489)
+        for l in self.layers:
+            st = self.neuron[l]
+            init = l.p.child("init config")
+            is_input = l.name in inputs
+            if is_input:
+                st["input"][:] = np.asarray(inputs[l.name], np.float32)
+            if init is not None:
+                if init.get("type", "normal") != "flat":
+                    raise ValueError("oracle: only flat init configs are restated")
+                v = np.float32(init.get_float("value", 1.0))
+                if is_input:
+                    st["input"] += v
+                else:
+                    st["input"][:] = v
+            elif not is_input:
+                st["input"][:] = 0.0
+        # synaptic activation: every connection reads outputs of step t-1
+        for l in self.layers:
+            for c in l.inputs:
+                self._activate(L, c)
+        # neuron updates
+        for l in self.layers:
+            self._update(L, l)
+        # plasticity
+        if learning:
+            for l in self.layers:
+                for c in l.inputs:
+                    if c.plastic and c.to.model == "izhikevich":
+                        self._learn(L, c)
+
+    def run(self, steps, input_fn=None, learning=True, record=None):
+        """record: list of (layer, key) recorded after every step."""
+        trace = {k: [] for k in (record or [])}
+        for t in range(steps):
+            self.step(input_fn(t) if input_fn else None, learning)
+            for k in trace:
+                trace[k].append(self.neuron[self.layer(k[0])][k[1]].copy())
+        return {k: np.stack(v) for k, v in trace.items()}
+
+    def _src_words(self, c):
+        out = self.neuron[c.frm]["output"]
+        w = c.delay // 32 if c.frm.output_type == BIT else c.delay
+        return out[w * c.frm.size:(w + 1) * c.frm.size]
+
+    def _activate(self, L, c):
+        st, m = self.neuron[c.to], self.matrix[c]
+        src = self._src_words(c)
+        geo = (c.rows, _p(c.dst), _p(c.ptr), _p(c.from_idx), _p(c.w_idx))
+        if c.to.model == "izhikevich" and c.p.get("direct", "false") != "true":
+            if c.opcode == OPCODES["gap"]:
+                L.sg_act_gap(*geo, _p(st["voltage"]), _p(m["weights"]), _p(st["input"]))
+                return
+            targets = {0: ("ampa", 0.8, "nmda", 0.993), 1: ("gabaa", 0.833, "gabab", 0.993),
+                       2: ("mult", 0.95, None, -1.0), 5: ("dopamine", 0.95, None, -1.0)}
+            if c.opcode not in targets:
+                raise ValueError("Unimplemented connection type!")
+            sname, stau, lname, ltau = targets[c.opcode]
+            L.sg_act_iz(*geo, _p(src), c.frm.output_type, _p(m["weights"]), _p(m["short term R"]),
+                        _p(m["short term w"]), _p(m["delays"]), _p(m["time since spike"]),
+                        _p(m["short trace"]), _p(m["long trace"]),
+                        ctypes.c_float(c.baseline_conductance), ctypes.c_float(stau),
+                        ctypes.c_float(ltau), _p(st[sname]), _p(st[lname] if lname else st[sname]))
+        else:
+            L.sg_act_base(*geo, _p(src), c.frm.output_type, c.delay, c.opcode,
+                          _p(m["weights"]), _p(st["input"]))
+
+    def _update(self, L, l):
+        st = self.neuron[l]
+        if l.model == "izhikevich":
+            L.sg_iz_neurons(l.size, l.history, _p(st["input"]), _p(st["output"]),
+                            *[_p(st[k]) for k in ("ampa", "nmda", "gabaa", "gabab", "mult",
+                                                  "dopamine", "voltage", "recovery", "post trace",
+                                                  "time since spike", "a", "b", "c", "d")])
+        elif l.model == "relay":
+            L.sg_relay(l.size, l.history, _p(st["input"]), _p(st["output"]),
+                       int(l.p.get("ramp", "false") == "true"))
+        elif l.model == "rate_encoding":
+            L.sg_rate(l.size, l.history, _p(st["input"]), _p(st["output"]))
+        elif l.model == "game_of_life":
+            L.sg_gol(l.size, l.history, _p(st["input"]), _p(st["output"]),
+                     l.p.get_int("survival_min", 2), l.p.get_int("survival_max", 3),
+                     l.p.get_int("birth_min", 3), l.p.get_int("birth_max", 3))
+
+    def _learn(self, L, c):
+        if c.convolutional:
+            raise ValueError("Unimplemented connection type!")
+        if c.opcode not in (0, 1):
+            raise ValueError("Unimplemented connection type!")
+        st, m, ft = self.neuron[c.to], self.matrix[c], self.matrix[c]["time since spike"]
+        L.sg_upd_iz(c.rows, _p(c.dst), _p(c.ptr), _p(c.from_idx), _p(c.w_idx),
+                    c.frm.output_type, int(c.opcode == 1), ctypes.c_float(c.learning_rate), int(c.stp_flag),
+                    ctypes.c_float(c.max_weight), _p(st["post trace"]), _p(st["time since spike"]),
+                    _p(st["output"][:c.to.size]), _p(ft), _p(m["weights"]), _p(m["presyn trace"]),
+                    _p(m["weight derivatives"]), _p(m["short term R"]), _p(m["short term w"]))

@@ -1,0 +1,275 @@
+"""Seeded parity cases shared by the fixture generator and the tests.
+
+Each case is a network in the reference JSON schema plus every random quantity
+injected explicitly (the reference's own initialisers are unseedable): weights,
+Izhikevich per-synapse state, delays, initial outputs and per-step input
+currents.  ``make_golden.py`` runs the reference's CPU library on these cases
+and stores what it produced; tests rebuild the same inputs from the seeds.
+"""
+import numpy as np
+
+
+def _rng(seed):
+    return np.random.default_rng(seed)
+
+
+class Case:
+    def __init__(self, name, net, steps, seed, inject=None, inputs=None, record=(),
+                 final=(), learning=True, tol=None):
+        self.name = name
+        self.net = net
+        self.steps = steps
+        self.seed = seed
+        self.inject = inject or (lambda rng, sizes: {})
+        self.inputs = inputs or {}       # layer name -> fn(rng, step, size) -> float32
+        self.record = list(record)       # (structure, layer) output word 0 per step
+        self.final = list(final)         # ("neuron", structure, layer, key) / ("matrix", conn, key)
+        self.learning = learning
+        self.tol = tol or {}             # key -> relative tolerance (float paths with libm)
+
+    def input_arrays(self, sizes):
+        """Per-step input arrays, deterministic in the seed."""
+        rng = _rng(self.seed + 1000)
+        out = []
+        for t in range(self.steps):
+            out.append({name: fn(rng, t, sizes[name]).astype(np.float32)
+                        for name, fn in sorted(self.inputs.items())})
+        return out
+
+    def injections(self, sizes):
+        return self.inject(_rng(self.seed), sizes)
+
+
+def _layer(name, model, rows, cols, **kw):
+    d = {"name": name, "neural model": model, "rows": rows, "columns": cols}
+    d.update(kw)
+    return d
+
+
+def _gol_net(rows, cols, field=3, delay=None, **rule):
+    conn = {"name": "nbr", "from layer": "board", "to layer": "board", "type": "convergent",
+            "convolutional": True, "plastic": False, "opcode": "add",
+            "weight config": {"type": "flat", "weight": 1.0, "diagonal": False},
+            "arborized config": {"field size": field, "wrap": True}}
+    if delay is not None:
+        conn["delay"] = delay
+    return {"structures": [{"name": "g", "type": "parallel",
+                            "layers": [_layer("board", "game_of_life", rows, cols, **rule)]}],
+            "connections": [conn]}
+
+
+def _gol_inject(p):
+    def f(rng, sizes):
+        n = sizes["board"]
+        alive = (rng.random(n) < p).astype(np.uint32)
+        return {("neuron", "g", "board", "output"): alive << np.uint32(31)}
+    return f
+
+
+def _gol_inject_history(p, words):
+    def f(rng, sizes):
+        n = sizes["board"]
+        return {("neuron", "g", "board", "output"):
+                rng.integers(0, 2**32, n * words, dtype=np.uint64).astype(np.uint32)}
+    return f
+
+
+def cases():
+    out = []
+
+    # --- game of life ---------------------------------------------------
+    out.append(Case("gol_16x16", _gol_net(16, 16), 80, 11, inject=_gol_inject(0.3),
+                    record=[("g", "board")], final=[("neuron", "g", "board", "output"),
+                                                     ("neuron", "g", "board", "input")]))
+    out.append(Case("gol_12x20_field5_rules",
+                    _gol_net(12, 20, field=5, survival_min=3, survival_max=6,
+                             birth_min=4, birth_max=6),
+                    40, 12, inject=_gol_inject_history(0.5, 1),
+                    record=[("g", "board")], final=[("neuron", "g", "board", "output")]))
+    out.append(Case("gol_two_word_history", _gol_net(10, 14, delay=37), 40, 13,
+                    inject=_gol_inject_history(0.5, 2),
+                    record=[("g", "board")], final=[("neuron", "g", "board", "output")]))
+
+    # --- base activator over every connection type and opcode -----------
+    src = _layer("src", "relay", 6, 8)
+    net = {"structures": [{"name": "s", "type": "parallel", "layers": [
+        src,
+        _layer("fc", "relay", 4, 5),
+        _layer("sub", "relay", 5, 7, ramp=True),
+        _layer("one", "rate_encoding", 6, 8),
+        _layer("conv", "relay", 6, 8),
+        _layer("conv_s2", "relay", 3, 4),
+        _layer("div", "rate_encoding", 12, 16),
+        _layer("pool", "relay", 6, 8),
+    ]}], "connections": [
+        {"name": "c_fc_add", "from layer": "src", "to layer": "fc", "type": "fully connected",
+         "opcode": "add", "plastic": False},
+        {"name": "c_fc_mult", "from layer": "src", "to layer": "fc", "type": "fully connected",
+         "opcode": "mult", "plastic": False},
+        {"name": "c_sub_sub", "from layer": "src", "to layer": "sub", "type": "subset",
+         "opcode": "sub", "plastic": False,
+         "subset config": {"from row start": 1, "from row end": 5, "from column start": 2,
+                           "from column end": 7, "to row start": 1, "to row end": 4,
+                           "to column start": 0, "to column end": 6}},
+        {"name": "c_one_add", "from layer": "src", "to layer": "one", "type": "one to one",
+         "opcode": "add", "plastic": False},
+        {"name": "c_one_heavi", "from layer": "src", "to layer": "one", "type": "one to one",
+         "opcode": "add_heaviside", "plastic": False},
+        {"name": "c_conv_nowrap", "from layer": "src", "to layer": "conv", "type": "convergent",
+         "opcode": "add", "plastic": False,
+         "arborized config": {"field size": 3, "wrap": False}},
+        {"name": "c_conv_wrap_sp", "from layer": "src", "to layer": "conv", "type": "convergent",
+         "opcode": "sub_heaviside", "plastic": False,
+         "arborized config": {"field size": 3, "spacing": 2, "wrap": True}},
+        {"name": "c_conv_div", "from layer": "src", "to layer": "conv", "type": "convergent",
+         "opcode": "div", "plastic": False, "convolutional": True,
+         "arborized config": {"row field size": 2, "column field size": 3, "offset": -1,
+                              "wrap": True}},
+        {"name": "c_conv_stride2", "from layer": "src", "to layer": "conv_s2", "type": "convergent",
+         "opcode": "add", "plastic": False,
+         "arborized config": {"field size": 4, "stride": 2, "offset": -1, "wrap": False}},
+        {"name": "c_div", "from layer": "src", "to layer": "div", "type": "divergent",
+         "opcode": "add", "plastic": False,
+         "arborized config": {"field size": 3, "stride": 2, "wrap": False}},
+        {"name": "c_div_conv", "from layer": "src", "to layer": "div", "type": "divergent",
+         "opcode": "mult_heaviside", "plastic": False, "convolutional": True,
+         "arborized config": {"field size": 2, "stride": 2, "wrap": True}},
+        {"name": "c_pool", "from layer": "src", "to layer": "pool", "type": "convergent",
+         "opcode": "pool", "plastic": False,
+         "arborized config": {"field size": 3, "wrap": True}},
+    ]}
+    base_conns = [c["name"] for c in net["connections"]]
+
+    def inj_base(rng, sizes):
+        d = {}
+        for name in base_conns:
+            n = sizes["conn:" + name]
+            d[("matrix", name, "weights")] = rng.uniform(-1.0, 1.0, n).astype(np.float32)
+        return d
+    out.append(Case("base_all_types", net, 12, 21, inject=inj_base,
+                    inputs={"src": lambda rng, t, n: rng.normal(0.0, 1.0, n)},
+                    record=[("s", l) for l in ("fc", "sub", "one", "conv", "conv_s2", "div", "pool")],
+                    final=[("neuron", "s", l, "input") for l in
+                           ("fc", "sub", "one", "conv", "conv_s2", "div", "pool")],
+                    tol={"rate_encoding": 2e-7}))
+
+    # --- Izhikevich, the config-0 topology at small size ----------------
+    def iz_c0(side, steps, seed, rate, value):
+        n = side * side
+        net = {"structures": [{"name": "s", "type": "parallel", "layers": [
+            _layer("in", "relay", side, side),
+            _layer("iz", "izhikevich", side, side, params="regular")]}],
+            "connections": [
+                {"name": "c_in", "from layer": "in", "to layer": "iz", "type": "convergent",
+                 "plastic": False, "opcode": "add",
+                 "arborized config": {"field size": 5, "wrap": True}},
+                {"name": "c_rec", "from layer": "iz", "to layer": "iz",
+                 "type": "fully connected", "plastic": False, "opcode": "sub"}]}
+
+        def inj(rng, sizes):
+            nin = sizes["conn:c_in"]
+            nrec = sizes["conn:c_rec"]
+            v0 = np.full(n, -65.0, np.float32)
+            return {("matrix", "c_in", "weights"): rng.uniform(0, 0.5, nin).astype(np.float32),
+                    ("matrix", "c_in", "short term w"): np.full(nin, 0.5, np.float32),
+                    ("matrix", "c_rec", "weights"):
+                        (rng.uniform(0, 0.2, nrec) * (rng.random(nrec) < 0.2)).astype(np.float32),
+                    ("matrix", "c_rec", "delays"): rng.integers(0, 4, nrec).astype(np.int32),
+                    ("neuron", "s", "iz", "voltage"): v0,
+                    ("neuron", "s", "iz", "recovery"): (np.float32(0.2) * v0).astype(np.float32)}
+        return Case("iz_c0_%d" % side, net, steps, seed, inject=inj,
+                    inputs={"in": lambda rng, t, m: (rng.random(m) < rate) * value},
+                    record=[("s", "iz"), ("s", "in")],
+                    final=[("neuron", "s", "iz", k) for k in
+                           ("voltage", "recovery", "ampa", "nmda", "gabaa", "gabab",
+                            "post trace", "time since spike", "output", "dopamine")]
+                    + [("matrix", "c_in", k) for k in ("short trace", "long trace", "time since spike")]
+                    + [("matrix", "c_rec", k) for k in ("short trace", "long trace", "time since spike")])
+    out.append(iz_c0(8, 300, 31, 0.05, 1.0))
+    out.append(iz_c0(32, 120, 32, 0.01, 1.0))
+
+    # --- Izhikevich plasticity (STDP + STP), every plastic connection type --
+    net = {"structures": [{"name": "s", "type": "parallel", "layers": [
+        _layer("in", "relay", 8, 8),
+        _layer("e", "izhikevich", 8, 8, params="regular"),
+        _layer("i", "izhikevich", 6, 6, params="fast")]}],
+        "connections": [
+            {"name": "p_conv", "from layer": "in", "to layer": "e", "type": "convergent",
+             "opcode": "add", "arborized config": {"field size": 3, "wrap": True}},
+            {"name": "p_ee", "from layer": "e", "to layer": "e", "type": "fully connected",
+             "opcode": "add", "max weight": 0.5, "learning rate": 0.05},
+            {"name": "p_ie", "from layer": "i", "to layer": "e", "type": "fully connected",
+             "opcode": "sub"},
+            {"name": "p_ei", "from layer": "e", "to layer": "i", "type": "subset", "opcode": "add",
+             "subset config": {"from row start": 0, "from row end": 6, "from column start": 1,
+                               "from column end": 7, "to row start": 0, "to row end": 5,
+                               "to column start": 0, "to column end": 6}},
+            {"name": "p_div", "from layer": "i", "to layer": "e", "type": "divergent",
+             "opcode": "add", "arborized config": {"field size": 3, "stride": 1}},
+            {"name": "p_one", "from layer": "e", "to layer": "e", "type": "one to one",
+             "opcode": "sub", "short term plasticity": False}]}
+    pconns = ["p_conv", "p_ee", "p_ie", "p_ei", "p_div", "p_one"]
+
+    def inj_plastic(rng, sizes):
+        d = {}
+        for name in pconns:
+            n = sizes["conn:" + name]
+            d[("matrix", name, "weights")] = rng.uniform(0.0, 0.6, n).astype(np.float32)
+            d[("matrix", name, "short term w")] = rng.uniform(0.2, 0.6, n).astype(np.float32)
+            d[("matrix", name, "delays")] = rng.integers(0, 5, n).astype(np.int32)
+        return d
+    finals = []
+    for name in pconns:
+        finals += [("matrix", name, k) for k in ("weights", "presyn trace", "weight derivatives",
+                                                 "short term R", "short term w", "short trace",
+                                                 "long trace", "time since spike")]
+    finals += [("neuron", "s", l, k) for l in ("e", "i")
+               for k in ("voltage", "recovery", "post trace", "time since spike", "output")]
+    out.append(Case("iz_plastic", net, 150, 41, inject=inj_plastic,
+                    inputs={"in": lambda rng, t, m: (rng.random(m) < 0.15) * 2.0},
+                    record=[("s", "e"), ("s", "i")], final=finals,
+                    tol={"istdp": 0.0}))
+
+    # --- Izhikevich opcodes: mult, reward, gap, direct, default delays,
+    #     multi-word BIT history read by a FLOAT layer ----------------------
+    net = {"structures": [{"name": "s", "type": "parallel", "layers": [
+        _layer("in", "relay", 6, 6),
+        _layer("iz", "izhikevich", 6, 6, params="chattering", **{"neuron spacing": 0.3}),
+        _layer("ro", "relay", 6, 6)]}],
+        "connections": [
+            {"name": "o_drive", "from layer": "in", "to layer": "iz", "type": "one to one",
+             "opcode": "add", "plastic": False},
+            {"name": "o_direct", "from layer": "in", "to layer": "iz", "type": "convergent",
+             "opcode": "add", "plastic": False, "direct": True,
+             "arborized config": {"field size": 3, "wrap": True}},
+            {"name": "o_mult", "from layer": "iz", "to layer": "iz", "type": "fully connected",
+             "opcode": "mult", "plastic": False},
+            {"name": "o_reward", "from layer": "in", "to layer": "iz", "type": "fully connected",
+             "opcode": "reward", "plastic": False},
+            {"name": "o_gap", "from layer": "iz", "to layer": "iz", "type": "fully connected",
+             "opcode": "gap", "plastic": False},
+            {"name": "o_rec", "from layer": "iz", "to layer": "iz", "type": "fully connected",
+             "opcode": "add", "plastic": False},
+            {"name": "o_read", "from layer": "iz", "to layer": "ro", "type": "one to one",
+             "opcode": "add", "plastic": False, "delay": 45}]}
+
+    def inj_ops(rng, sizes):
+        d = {}
+        for name in ("o_drive", "o_mult", "o_reward", "o_rec"):
+            n = sizes["conn:" + name]
+            d[("matrix", name, "weights")] = rng.uniform(0.0, 0.3, n).astype(np.float32)
+            d[("matrix", name, "short term w")] = rng.uniform(0.3, 0.7, n).astype(np.float32)
+        d[("matrix", "o_drive", "weights")] = np.full(sizes["conn:o_drive"], 1.0, np.float32)
+        d[("matrix", "o_direct", "weights")] = rng.uniform(0.0, 2.0, sizes["conn:o_direct"]).astype(np.float32)
+        d[("matrix", "o_gap", "weights")] = rng.uniform(0.0, 0.02, sizes["conn:o_gap"]).astype(np.float32)
+        return d
+    out.append(Case("iz_opcodes", net, 200, 51, inject=inj_ops,
+                    inputs={"in": lambda rng, t, m: (rng.random(m) < 0.2) * 3.0},
+                    record=[("s", "iz"), ("s", "ro")],
+                    final=[("neuron", "s", "iz", k) for k in
+                           ("voltage", "recovery", "mult", "dopamine", "input", "output")]
+                    + [("neuron", "s", "ro", "output")]))
+    return out
+
+
+CASES = {c.name: c for c in cases()}

@@ -1,0 +1,148 @@
+"""Runs golden cases on the oracle or on the GB300 library and compares results."""
+import os
+
+import numpy as np
+
+from tests.golden.cases import CASES
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load_fixture(name):
+    with np.load(os.path.join(GOLDEN, name + ".npz")) as z:
+        return {k: z[k] for k in z.files}
+
+
+def case_sizes(case):
+    from oracle.oracle import OracleNetwork
+    onet = OracleNetwork(case.net)
+    sizes = {l.name: l.size for l in onet.layers}
+    sizes.update({"conn:" + c.name: c.num_weights for c in onet.conns})
+    return sizes
+
+
+def _as_u32(a):
+    a = np.asarray(a)
+    return a.view(np.uint32) if a.dtype == np.float32 else a
+
+
+def run_oracle(case, steps=None):
+    """Runs ``case`` on the CPU oracle; returns the fixture-shaped dict."""
+    from oracle.oracle import OracleNetwork
+    steps = case.steps if steps is None else steps
+    net = OracleNetwork(case.net)
+    sizes = case_sizes(case)
+    for key, arr in case.injections(sizes).items():
+        if key[0] == "neuron":
+            dst = net.get_neuron_data(key[2], key[3])
+        else:
+            dst = net.get_weight_matrix(key[1], key[2])
+        assert dst.size == arr.size, key
+        dst.view(arr.dtype)[:] = arr
+    inputs = case.input_arrays(sizes)
+    rec = {k: [] for k in case.record}
+    for t in range(steps):
+        net.step(inputs[t], learning=case.learning)
+        for (s, l) in case.record:
+            rec[(s, l)].append(net.get_neuron_data(l, "output")[:sizes[l]].copy())
+    out = {"rec/%s/%s" % k: np.stack(v) for k, v in rec.items()}
+    for key in case.final:
+        if key[0] == "neuron":
+            out["neuron/%s/%s/%s" % key[1:]] = _as_u32(net.get_neuron_data(key[2], key[3]).copy())
+        else:
+            out["matrix/%s/%s" % key[1:]] = _as_u32(net.get_weight_matrix(key[1], key[2]).copy())
+    return out
+
+
+def run_library(case, syngen, steps=None):
+    """Runs ``case`` through the drop-in front-end ``syngen`` (either library)."""
+    steps = case.steps if steps is None else steps
+    sizes = case_sizes(case)
+    injections = case.injections(sizes)
+    import copy
+    net_dict = copy.deepcopy(case.net)
+    delay_arrays = []
+    for c in net_dict["connections"]:
+        key = ("matrix", c["name"], "delays")
+        if key in injections:
+            wc = c.setdefault("weight config", {"type": "flat", "weight": 1.0})
+            wc["delay callback"] = "golden_delay"
+            wc["id"] = len(delay_arrays)
+            delay_arrays.append(injections.pop(key))
+
+    def delay_cb(ID, size, weights, delays):
+        syngen.IntArray(size, delays).to_np_array()[:] = delay_arrays[ID]
+
+    syngen.create_delay_weight_callback("golden_delay", delay_cb)
+    net = syngen.Network(net_dict)
+    net.build_state()
+    for key, arr in injections.items():
+        if key[0] == "neuron":
+            dst = net.get_neuron_data(key[1], key[2], key[3]).to_np_array()
+        else:
+            dst = net.get_weight_matrix(key[1], key[2]).to_np_array()
+        assert dst.size == arr.size, (key, dst.size, arr.size)
+        dst.view(arr.dtype)[:] = arr
+    inputs = case.input_arrays(sizes)
+    step = {"in": 0}
+    in_layers = sorted(case.inputs)
+    rec = {k: [] for k in case.record}
+
+    def in_cb(ID, size, ptr):
+        syngen.FloatArray(size, ptr).to_np_array()[:] = inputs[step["in"]][in_layers[ID]]
+        if ID == len(in_layers) - 1:
+            step["in"] += 1
+
+    def out_cb(ID, size, ptr):
+        rec[case.record[ID]].append(syngen.FloatArray(size, ptr).to_np_array().view(np.uint32).copy())
+
+    syngen.create_io_callback("golden_in", in_cb)
+    syngen.create_io_callback("golden_out", out_cb)
+    modules = []
+    structs = {l["name"]: st["name"] for st in case.net["structures"] for l in st["layers"]}
+    if in_layers:
+        modules.append({"type": "callback", "layers": [
+            {"structure": structs[l], "layer": l, "input": True, "function": "golden_in", "id": i}
+            for i, l in enumerate(in_layers)]})
+    if case.record:
+        modules.append({"type": "callback", "layers": [
+            {"structure": s, "layer": l, "output": True, "function": "golden_out", "id": i}
+            for i, (s, l) in enumerate(case.record)]})
+    report = net.run(syngen.Environment({"modules": modules}),
+                     {"iterations": steps, "multithreaded": False, "worker threads": 0,
+                      "learning flag": case.learning})
+    assert report is not None and report.obj is not None, "run failed"
+    out = {"rec/%s/%s" % k: np.stack(v) for k, v in rec.items()}
+    for key in case.final:
+        if key[0] == "neuron":
+            arr = net.get_neuron_data(key[1], key[2], key[3])
+            out["neuron/%s/%s/%s" % key[1:]] = _as_u32(arr.to_np_array().copy())
+        else:
+            arr = net.get_weight_matrix(key[1], key[2])
+            out["matrix/%s/%s" % key[1:]] = _as_u32(arr.to_np_array().copy())
+    return out
+
+
+def compare(got, want, steps=None, tol=None, float_keys=()):
+    """Bit-exact comparison; keys matching ``float_keys`` use relative tolerance ``tol``."""
+    problems = []
+    for k, w in want.items():
+        if k not in got:
+            problems.append("missing " + k)
+            continue
+        g = got[k]
+        if steps is not None and k.startswith("rec/"):
+            w = w[:steps]
+        if g.shape != w.shape:
+            problems.append("%s shape %s != %s" % (k, g.shape, w.shape))
+            continue
+        if tol is not None and any(f in k for f in float_keys):
+            gf, wf = g.view(np.float32), w.view(np.float32)
+            bad = ~np.isclose(gf, wf, rtol=tol, atol=tol)
+        else:
+            bad = g != w
+        if bad.any():
+            idx = np.argwhere(bad)[0]
+            problems.append("%s: %d mismatches, first at %s got %r want %r"
+                            % (k, int(bad.sum()), tuple(idx), g[tuple(idx)], w[tuple(idx)]))
+    return problems
