@@ -1,0 +1,141 @@
+/*
+ * syngen.h -- C-ABI of the GB300 synaptogenesis simulation-cycle library
+ * (libsyngen.so built from synaptogenesis_gb300/csrc).
+ *
+ * The first block is a drop-in for the reference's src/core/extern.h: same
+ * symbol names, argument meaning, ownership and error behaviour, so the
+ * reference front-end (lib/syngen.py) binds it unchanged.  Line numbers cite
+ * src/core/extern.h (declarations) and src/core/extern.cpp (behaviour).
+ *
+ * Errors: entry points never throw; on failure they return nullptr, false or
+ * an empty ARRAY{0, VOID_POINTER, NULL, false} (extern.cpp:151-279).  The
+ * message of the last failure on the calling thread is sg_last_error().
+ *
+ * Ownership: data getters return non-owning pointers into the live host copy
+ * of the state (they first move the state to the host; the next run moves it
+ * back, extern.cpp:214-258, state.cpp:706-764).  STRING / PROPS arrays are
+ * owned and are released with free_array / free_array_deep.
+ */
+#ifndef SYNGEN_GB300_H
+#define SYNGEN_GB300_H
+
+#ifdef __cplusplus
+#include <cstddef>
+extern "C" {
+#else
+#include <stdbool.h>
+#include <stddef.h>
+#endif
+
+#define SG_ABI_VERSION 1
+
+/* extern.h:6-12 */
+typedef enum {
+    FLOAT_POINTER = 1,
+    INT_POINTER = 2,
+    STRING_POINTER = 3,
+    PROPS_POINTER = 4,
+    VOID_POINTER = 5
+} POINTER_TYPE;
+
+/* extern.h:14-19 */
+typedef struct ARRAY {
+    int size;
+    POINTER_TYPE type;
+    void* data;
+    bool owner;
+} ARRAY;
+
+/* extern.h:25-28 */
+typedef void* NETWORK;
+typedef void* ENVIRONMENT;
+typedef void* STATE;
+typedef void* PROPS;
+
+/* extern.h:23-24 */
+void free_array(ARRAY arr);
+void free_array_deep(ARRAY arr);
+
+/* Properties, extern.h:30-45 */
+PROPS create_properties(void);
+void add_property(PROPS properties, char* key, char* val);
+void add_child(PROPS properties, char* key, PROPS child);
+void add_to_array(PROPS properties, char* key, char* val);
+void add_to_child_array(PROPS properties, char* key, PROPS props);
+ARRAY get_keys(PROPS properties);
+ARRAY get_child_keys(PROPS properties);
+ARRAY get_array_keys(PROPS properties);
+ARRAY get_child_array_keys(PROPS properties);
+const char* get_property(PROPS properties, char* key);
+PROPS get_child(PROPS properties, char* key);
+ARRAY get_array(PROPS properties, char* key);
+ARRAY get_child_array(PROPS properties, char* key);
+
+/* Environment / network objects, extern.h:47-53 */
+ENVIRONMENT create_environment(PROPS properties);
+ENVIRONMENT load_env(char* filename);
+bool save_env(ENVIRONMENT env, char* filename);
+NETWORK create_network(PROPS properties);
+NETWORK load_net(char* filename);
+bool save_net(NETWORK network, char* filename);
+
+/* State, extern.h:55-58 */
+STATE build_state(NETWORK net);
+STATE build_load_state(NETWORK net, char* filename);
+bool load_state(STATE state, char* filename);
+bool save_state(STATE state, char* filename);
+
+/* Data access, extern.h:60-65 (host layout views) */
+ARRAY get_neuron_data(STATE state, char* structure_name, char* layer_name, char* key);
+ARRAY get_layer_data(STATE state, char* structure_name, char* layer_name, char* key);
+ARRAY get_connection_data(STATE state, char* conn_name, char* key);
+ARRAY get_weight_matrix(STATE state, char* conn_name, char* key);
+
+/* One run of the simulation cycle, extern.h:67; returns the report */
+PROPS run(NETWORK net, ENVIRONMENT env, STATE state, PROPS args);
+
+/* Teardown, extern.h:69-73 */
+void destroy(void* obj);
+void destroy_network(NETWORK net);
+void destroy_environment(ENVIRONMENT env);
+void destroy_state(STATE state);
+void destroy_properties(PROPS props);
+
+/* Devices, extern.h:75-78 (the host id is the number of GPUs) */
+int get_num_gpus(void);
+int get_cpu(void);
+ARRAY get_gpus(void);
+ARRAY get_all_devices(void);
+
+/* Logging and control, extern.h:80-84 */
+void set_suppress_output(bool val);
+void set_warnings(bool val);
+void set_debug(bool val);
+void interrupt_engine(void);
+
+/* Named host callbacks, extern.h:86-90 */
+void add_io_callback(char* name, long long addr);
+void add_weight_callback(char* name, long long addr);
+void add_indices_weight_callback(char* name, long long addr);
+void add_distance_weight_callback(char* name, long long addr);
+void add_delay_weight_callback(char* name, long long addr);
+
+/* MPI, extern.h:92-95: single-process no-ops (rank 0 of 1) */
+void initialize_mpi(void);
+int get_mpi_rank(void);
+int get_mpi_size(void);
+void finalize_mpi(void);
+
+/* ---------------- Extensions (no counterpart in extern.h) ---------------- */
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* sg_last_error(void);
+/* Seed of the random weight / parameter / noise initialisers. */
+void sg_set_seed(unsigned long long seed);
+/* ABI version of this header. */
+int sg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,171 @@
+// Base activator (all connection types, every opcode) and the stateless
+// neural models: relay, rate_encoding, game_of_life.
+#include <cmath>
+
+#include "cuda_check.h"
+#include "models.h"
+#include "state.h"
+
+namespace sg {
+
+// ---------------------------------------------------------------------------
+// Model registry (neural_model_bank.cpp:21-83)
+// ---------------------------------------------------------------------------
+static std::map<std::string, const Model*>& registry() {
+    static std::map<std::string, const Model*> r;
+    return r;
+}
+
+const Model* find_model(const std::string& name) {
+    auto it = registry().find(name);
+    return it == registry().end() ? nullptr : it->second;
+}
+
+bool register_model(const Model* m) {
+    if (registry().count(m->name()))
+        throw SgError(std::string("Duplicate attributes neural model string: ") + m->name() + "!");
+    registry()[m->name()] = m;
+    return true;
+}
+
+std::vector<std::string> model_names() {
+    std::vector<std::string> out;
+    for (auto& kv : registry()) out.push_back(kv.first);
+    return out;
+}
+
+// ---------------------------------------------------------------------------
+// Base activator: one thread per destination, sources in serial order,
+// sequential fp32 sum (synapse_kernel.h:887-912).
+// ---------------------------------------------------------------------------
+template <int TY, int SR>
+__global__ void __launch_bounds__(256) k_activate_base(DGeom g, const uint32_t* __restrict__ src,
+                                                       int delay, int opcode,
+                                                       const float* __restrict__ w,
+                                                       float* __restrict__ inputs) {
+    int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= g.n_dest) return;
+    float sum = 0.0f;
+    for_each_source<TY>(g, d, [&](int from, int wi) {
+        float val = extract<SR>(src[from], delay) * w[wi];
+        sum += val;
+    });
+    int to = dest_of<TY>(g, d);
+    inputs[to] = aggregate(inputs[to], sum, opcode);
+}
+
+void launch_base_activator(State& st, ConnState& cs, float* inputs, cudaStream_t s) {
+    const Connection& c = *cs.conn;
+    const uint32_t* src = st.dev_output(c.from, word_index(c.delay, c.from->output_type));
+    const int threads = 128;
+    unsigned blocks = blocks_for(cs.geom.n_dest, threads);
+    SG_DISPATCH_TYPE_SRC((int)c.type, (int)c.from->output_type,
+        (k_activate_base<TY, SR><<<blocks, threads, 0, s>>>(cs.geom, src, c.delay, (int)c.opcode,
+                                                           cs.weights->df(), inputs)));
+    SG_LAUNCH_CHECK();
+}
+
+void Model::activate(State& st, ConnState& cs, const StepCtx& ctx) const {
+    launch_base_activator(st, cs, st.layer_state(cs.conn->to)->input->df(), ctx.stream);
+}
+
+// ---------------------------------------------------------------------------
+// Output history shifts (state/attributes.h:316-333)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t shift_bits(uint32_t* out, int size, int history, int nid,
+                                               uint32_t new_bit) {
+    uint32_t curr = out[(size_t)size * (history - 1) + nid];
+    for (int idx = history - 1; idx > 0; --idx) {
+        uint32_t prev = out[(size_t)size * (idx - 1) + nid];
+        out[(size_t)size * idx + nid] = (curr >> 1) | (prev << 31);
+        curr = prev;
+    }
+    out[nid] = (curr >> 1) | (new_bit << 31);
+    return curr >> 31;
+}
+
+__device__ __forceinline__ void shift_floats(float* out, int size, int history, int nid, float v) {
+    for (int idx = history - 1; idx > 0; --idx)
+        out[(size_t)size * idx + nid] = out[(size_t)size * (idx - 1) + nid];
+    out[nid] = v;
+}
+
+// relay_attributes.cpp:10-18 (the ramp is std::fmax on doubles, i.e. fmax)
+__global__ void k_relay(int size, int history, const float* __restrict__ in, float* out, int ramp) {
+    int nid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nid >= size) return;
+    float input = in[nid];
+    shift_floats(out, size, history, nid, ramp ? (float)fmax(0.0, (double)input) : input);
+}
+
+// rate_encoding_attributes.cpp:122-131 (tanh of a float is tanhf)
+__global__ void k_rate(int size, int history, const float* __restrict__ in, float* out) {
+    int nid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nid >= size) return;
+    float input = in[nid];
+    shift_floats(out, size, history, nid, (input > 0.0f) ? tanhf(input) : 0.0f);
+}
+
+// game_of_life_attributes.cpp:58-77: prev_live is bit 0 of word 0, i.e. the
+// cell 32 steps back, while neighbours are read at delay 0 (bit 31).
+__global__ void k_gol(int size, int history, const float* __restrict__ in, uint32_t* out,
+                      int smin, int smax, int bmin, int bmax) {
+    int nid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nid >= size) return;
+    int input = (int)in[nid];
+    bool prev_live = out[nid] & 1u;
+    bool live = prev_live ? (input >= smin && input <= smax) : (input >= bmin && input <= bmax);
+    shift_bits(out, size, history, nid, live ? 1u : 0u);
+}
+
+class RelayModel : public Model {
+  public:
+    const char* name() const override { return "relay"; }
+    OutputType output_type() const override { return OUT_FLOAT; }
+    void build_layer(State&, LayerState& ls) const override {
+        ls.params["ramp"] = ls.layer->parameter("ramp", "false") == "true" ? 1.0f : 0.0f;
+    }
+    void update(State&, LayerState& ls, const StepCtx& ctx) const override {
+        const Layer& l = *ls.layer;
+        k_relay<<<blocks_for(l.size, 256), 256, 0, ctx.stream>>>(
+            l.size, l.history(), ls.input->df(), ls.output->df(), (int)ls.params.at("ramp"));
+        SG_LAUNCH_CHECK();
+    }
+};
+SG_REGISTER_MODEL(RelayModel);
+
+class RateEncodingModel : public Model {
+  public:
+    const char* name() const override { return "rate_encoding"; }
+    OutputType output_type() const override { return OUT_FLOAT; }
+    void update(State&, LayerState& ls, const StepCtx& ctx) const override {
+        const Layer& l = *ls.layer;
+        k_rate<<<blocks_for(l.size, 256), 256, 0, ctx.stream>>>(l.size, l.history(), ls.input->df(),
+                                                                ls.output->df());
+        SG_LAUNCH_CHECK();
+    }
+};
+SG_REGISTER_MODEL(RateEncodingModel);
+
+class GameOfLifeModel : public Model {
+  public:
+    const char* name() const override { return "game_of_life"; }
+    OutputType output_type() const override { return OUT_BIT; }
+    void build_layer(State&, LayerState& ls) const override {
+        const Layer& l = *ls.layer;
+        ls.params["smin"] = (float)std::stoi(l.parameter("survival_min", "2"));
+        ls.params["smax"] = (float)std::stoi(l.parameter("survival_max", "3"));
+        ls.params["bmin"] = (float)std::stoi(l.parameter("birth_min", "3"));
+        ls.params["bmax"] = (float)std::stoi(l.parameter("birth_max", "3"));
+    }
+    void update(State&, LayerState& ls, const StepCtx& ctx) const override {
+        const Layer& l = *ls.layer;
+        k_gol<<<blocks_for(l.size, 256), 256, 0, ctx.stream>>>(
+            l.size, l.history(), ls.input->df(), ls.output->du(), (int)ls.params.at("smin"),
+            (int)ls.params.at("smax"), (int)ls.params.at("bmin"), (int)ls.params.at("bmax"));
+        SG_LAUNCH_CHECK();
+    }
+};
+SG_REGISTER_MODEL(GameOfLifeModel);
+
+}  // namespace sg

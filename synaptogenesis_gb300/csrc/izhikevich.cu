@@ -1,0 +1,445 @@
+// Izhikevich neural model: src/core/state/impl/izhikevich_attributes.cpp.
+//
+// Arithmetic follows the reference's mixed float/double expressions term by
+// term (IZ_* and STDP constants are double literals); the library is built
+// with --fmad=false so nothing is contracted.  powf(x, 2) is x * x, which is
+// what the reference's optimised build computes.
+#include <cmath>
+#include <cstdlib>
+#include <random>
+
+#include "cuda_check.h"
+#include "models.h"
+#include "state.h"
+#include "weight_init.h"
+
+namespace sg {
+
+namespace {
+
+struct IzParams { float a, b, c, d; };
+
+// izhikevich_attributes.cpp:28-35
+IzParams preset(const std::string& s) {
+    if (s == "default") return {0.02f, 0.2f, -70.0f, 2.0f};
+    if (s == "regular") return {0.02f, 0.2f, -65.0f, 8.0f};
+    if (s == "bursting") return {0.02f, 0.2f, -55.0f, 4.0f};
+    if (s == "chattering") return {0.02f, 0.2f, -50.0f, 2.0f};
+    if (s == "fast") return {0.1f, 0.2f, -65.0f, 2.0f};
+    if (s == "low_threshold") return {0.02f, 0.25f, -65.0f, 2.0f};
+    if (s == "thalamo_cortical") return {0.02f, 0.25f, -65.0f, 0.05f};
+    if (s == "resonator") return {0.1f, 0.26f, -65.0f, 2.0f};
+    throw SgError("Unrecognized parameter string: " + s);
+}
+
+// iSTDP kernels of STDP_SUB (izhikevich_attributes.cpp:454-472).  Their
+// arguments are integer times 1..31, so they are tabulated on the host with
+// the host C library, evaluating the reference's expression unchanged.
+float istdp_src(volatile int t) { return (float)(powf(t, 10) * 0.000001 * 2.29 * expf(-1.1 * t)); }
+float istdp_dst(volatile int t) { return (float)(powf(t, 10) * 0.0000001 * 2.6 * expf(-0.94 * t)); }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
+
+// Trace activators (izhikevich_attributes.cpp:228-352); the time-since-spike
+// bookkeeping of CALC_VAL_PREAMBLE runs in k_iz_time_since_spike.
+// `serial` runs every destination in one thread: convolutional matrices share
+// their per-synapse traces across destinations, which the reference updates in
+// destination order.
+template <int TY, int SR, bool LONG>
+__global__ void __launch_bounds__(128) k_iz_activate(
+    DGeom g, int serial, const uint32_t* __restrict__ src, const float* __restrict__ w,
+    const float* __restrict__ stp_r, const float* __restrict__ stp_w, const int* __restrict__ delays,
+    float* __restrict__ short_tr, float* __restrict__ long_tr, float gcond, float short_tau,
+    float long_tau, float* short_cond, float* long_cond) {
+    int d0 = blockIdx.x * blockDim.x + threadIdx.x;
+    int d1 = d0 + 1;
+    if (serial) { if (d0 != 0) return; d1 = g.n_dest; }
+    for (int d = d0; d < d1 && d < g.n_dest; ++d) {
+        float short_sum = 0.0f, long_sum = 0.0f;
+        for_each_source<TY>(g, d, [&](int from, int wi) {
+            float spike = extract<SR>(src[from], SR == S_BIT ? delays[wi] : 0);
+            float weight = w[wi] * (stp_r[wi] * stp_w[wi]);
+            float st = short_tr[wi] + (spike * weight * gcond);
+            short_sum += st;
+            short_tr[wi] = st * short_tau;
+            if (LONG) {
+                float lt = long_tr[wi] + (spike * weight * gcond);
+                long_sum += lt;
+                long_tr[wi] = lt * long_tau;
+            }
+        });
+        int to = dest_of<TY>(g, d);
+        short_cond[to] += short_sum;
+        if (LONG) long_cond[to] += long_sum;
+    }
+}
+
+// Gap junctions (izhikevich_attributes.cpp:354-366)
+template <int TY>
+__global__ void k_iz_gap(DGeom g, const float* __restrict__ voltage, const float* __restrict__ w,
+                         float* __restrict__ inputs) {
+    int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= g.n_dest) return;
+    int to = dest_of<TY>(g, d);
+    float v = voltage[to];
+    float sum = 0.0f;
+    for_each_source<TY>(g, d, [&](int from, int wi) { sum += (voltage[from] - v) * w[wi]; });
+    inputs[to] += sum;
+}
+
+// Time since the presynaptic spike, per source (CALC_VAL_PREAMBLE,
+// izhikevich_attributes.cpp:257-262).  The reference updates it once per
+// visit in serial order: t = spike ? 0 : min(32, t + 1).  The result depends
+// only on the last visit that saw a spike and on how many visits follow it,
+// so each source scans its last (at most 32) visits backwards.
+__global__ void k_iz_time_since_spike(int n_src, const int* __restrict__ counts,
+                                      const int* __restrict__ last, const int* __restrict__ delays,
+                                      const uint32_t* __restrict__ src, int src_type,
+                                      int* __restrict__ tss) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_src) return;
+    int n = counts[f];
+    if (n == 0) return;
+    uint32_t word = src[f];
+    int m = n < 32 ? n : 32;
+    const int* L = last + (size_t)f * 32;
+    for (int j = m - 1; j >= 0; --j) {
+        float spike = extract_rt(word, delays[L[j]], src_type);
+        if (spike > 0.0f) { tss[f] = m - 1 - j; return; }
+    }
+    int t = tss[f] + n;
+    tss[f] = t < 32 ? t : 32;
+}
+
+// Neuron update (izhikevich_attributes.cpp:102-213)
+__global__ void __launch_bounds__(256) k_iz_update(
+    int size, int history, const float* __restrict__ inputs, uint32_t* spikes, float* ampa,
+    float* nmda, float* gabaa, float* gabab, float* mult, float* dopamine, float* voltages,
+    float* recoveries, float* post_traces, int* tss, const float* __restrict__ as,
+    const float* __restrict__ bs, const float* __restrict__ cs, const float* __restrict__ ds) {
+    int nid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nid >= size) return;
+    float ampa_c = ampa[nid], nmda_c = nmda[nid], gabaa_c = gabaa[nid], gabab_c = gabab[nid];
+    float mf = mult[nid];
+    float voltage = voltages[nid];
+    float recovery = recoveries[nid];
+    float base_current = inputs[nid];
+    float a = as[nid], b = bs[nid];
+    for (int i = 0; (i < 10) && (voltage < 30.0); ++i) {
+        float current = -ampa_c * voltage;
+        float q = (voltage + 80) / 60;
+        float temp = q * q;
+        current -= nmda_c * (temp / (1 + temp)) * voltage;
+        current -= gabaa_c * (voltage + 70);
+        current -= gabab_c * (voltage + 90);
+        current *= 1 + mf;
+        current += base_current;
+        float delta_v = (0.04 * voltage * voltage) + (5 * voltage) + 140 - recovery + current;
+        float sum_c = ampa_c + nmda_c + gabaa_c + gabab_c;
+        voltage = (voltage + 0.1 * (delta_v + (gabaa_c * -70) + (gabab_c * -90))) /
+                  (1 + (0.1 * sum_c));
+        voltage = (voltage != voltage) ? 30.0 : voltage;
+        float adjusted_tau = (voltage > 30.0) ? delta_v / (30.0 - voltage + delta_v) * 0.1 : 0.1;
+        recovery += a * adjusted_tau * ((b * voltage) - recovery);
+    }
+    ampa[nid] = 0.0f;
+    nmda[nid] = 0.0f;
+    gabaa[nid] = 0.0f;
+    gabab[nid] = 0.0f;
+    mult[nid] = 0.0f;
+    dopamine[nid] *= 0.95;
+    unsigned int spike = voltage >= 30.0;
+    // SHIFT_BIT_OUTPUTS (state/attributes.h:321-333)
+    uint32_t curr = spikes[(size_t)size * (history - 1) + nid];
+    for (int idx = history - 1; idx > 0; --idx) {
+        uint32_t prev = spikes[(size_t)size * (idx - 1) + nid];
+        spikes[(size_t)size * idx + nid] = (curr >> 1) | (prev << 31);
+        curr = prev;
+    }
+    spikes[nid] = (curr >> 1) | (spike << 31);
+    bool prev_bit = curr >> 31;
+    post_traces[nid] = prev_bit ? 0.004 : (post_traces[nid] * 0.95);
+    int t = tss[nid] + 1;
+    tss[nid] = prev_bit ? 0 : (t < 32 ? t : 32);
+    voltages[nid] = spike ? cs[nid] : voltage;
+    recoveries[nid] = recovery + (spike * ds[nid]);
+}
+
+struct IzLut { float src[33]; float dst[33]; };
+
+// STDP + STP updaters (izhikevich_attributes.cpp:404-520).  The destination
+// spike goes through the connection's extractor, i.e. the SOURCE layer's
+// output type (izhikevich_attributes.cpp:426).
+template <int TY, int SR, bool SUB>
+__global__ void __launch_bounds__(128) k_iz_learn(
+    DGeom g, const uint32_t* __restrict__ dest_out, const float* __restrict__ to_exc,
+    const int* __restrict__ to_tss, const int* __restrict__ from_tss, float lr, int stp_flag,
+    float max_weight, float* w, float* presyn, float* wd, float* stp_r, float* stp_w, IzLut lut) {
+    int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= g.n_dest) return;
+    const double U = SUB ? 0.2 : 0.5;
+    const int F = SUB ? 20 : 1000;
+    const int D = SUB ? 700 : 800;
+    int to = dest_of<TY>(g, d);
+    float dest_exc_trace = to_exc[to];
+    int dest_tss = to_tss[to];
+    float dest_spike = extract<SR>(dest_out[to], 0);
+    for_each_source<TY>(g, d, [&](int from, int wi) {
+        float weight = w[wi];
+        if (weight >= 0.0001f) {
+            int src_tss = from_tss[from];
+            bool src_spike = src_tss == 0;
+            float src_trace, dest_trace;
+            if (!SUB) {
+                src_trace = (presyn[wi] = src_spike ? 0.004 : presyn[wi] * 0.933);
+                dest_trace = dest_exc_trace;
+            } else {
+                src_trace = (dest_spike > 0.0f && src_tss > 0 && src_tss < 32) ? lut.src[src_tss] : 0.0f;
+                dest_trace = (src_spike && dest_tss > 0 && dest_tss < 32) ? lut.dst[dest_tss] : 0.0f;
+            }
+            float weight_delta = wd[wi];
+            weight_delta = wd[wi] -= (weight_delta - 0.000001) * 0.0001 + (dest_spike * src_trace) -
+                                     (src_spike * dest_trace);
+            weight += lr * weight_delta;
+            w[wi] = fmaxf(0.0001f, fminf(max_weight, weight));
+            if (stp_flag) {
+                float r = stp_r[wi];
+                float sw = stp_w[wi];
+                stp_r[wi] += ((1 - r) / D) - (r * sw * src_spike);
+                stp_w[wi] += ((U - sw) / F) + (U * (1 - sw) * src_spike);
+            }
+        }
+    });
+}
+
+// ---------------------------------------------------------------------------
+// Model
+// ---------------------------------------------------------------------------
+class IzhikevichModel : public Model {
+  public:
+    const char* name() const override { return "izhikevich"; }
+    OutputType output_type() const override { return OUT_BIT; }
+
+    // Constructor of IzhikevichAttributes (izhikevich_attributes.cpp:587-662)
+    void build_layer(State& st, LayerState& ls) const override {
+        const Layer& l = *ls.layer;
+        for (const char* k : {"ampa", "nmda", "gabaa", "gabab", "mult", "dopamine", "voltage",
+                              "recovery", "post trace", "a", "b", "c", "d"})
+            ls.vars[k] = st.add_array(k, 'f', l.size);
+        ls.vars["time since spike"] = st.add_array("time since spike", 'i', l.size);
+        float *as = ls.vars["a"]->hf(), *bs = ls.vars["b"]->hf(), *cs = ls.vars["c"]->hf(),
+              *ds = ls.vars["d"]->hf();
+        std::string p = l.parameter("params", "regular");
+        if (p == "random positive" || p == "random negative") {
+            auto rng = make_rng(l.config, 7 + l.index);
+            std::uniform_real_distribution<float> u(0.0f, 1.0f);
+            for (int i = 0; i < l.size; ++i) {
+                if (p == "random positive") {
+                    as[i] = 0.02f; bs[i] = 0.2f;
+                    cs[i] = -65.0 + (15.0 * std::pow(u(rng), 2));
+                    ds[i] = 8.0 - (6.0 * std::pow(u(rng), 2));
+                } else {
+                    as[i] = 0.02 + (0.08 * u(rng)); bs[i] = 0.25 - (0.05 * u(rng));
+                    cs[i] = -65.0f; ds[i] = 2.0f;
+                }
+            }
+        } else {
+            IzParams q = preset(p);
+            for (int i = 0; i < l.size; ++i) { as[i] = q.a; bs[i] = q.b; cs[i] = q.c; ds[i] = q.d; }
+        }
+        float* v = ls.vars["voltage"]->hf();
+        float* r = ls.vars["recovery"]->hf();
+        int32_t* tss = ls.vars["time since spike"]->hi();
+        for (int j = 0; j < l.size; ++j) {
+            tss[j] = 32;
+            // settle to the resting state
+            float vv = cs[j], rr = bs[j] * cs[j], dv, dr, a = as[j], b = bs[j];
+            do {
+                dv = (0.04 * vv * vv) + (5 * vv) + 140 - rr;
+                vv += dv;
+                dr = a * ((b * vv) - rr);
+                rr += dr;
+            } while (std::fabs(dv) > 0.001 && std::fabs(dr) > 0.001);
+            v[j] = vv;
+            r[j] = rr;
+        }
+        for (Connection* c : l.inputs)
+            if (c->opcode == OP_GAP && c->from != c->to)
+                throw SgError("Error " + c->str() +
+                              "\nGap junctions must be between neurons of the same layer.");
+    }
+
+    // process_weight_matrix (izhikevich_attributes.cpp:692-757)
+    void build_matrix(State& st, ConnState& cs) const override {
+        Connection& c = *cs.conn;
+        size_t n = c.num_weights;
+        int R = c.matrix_rows, C = c.matrix_cols;
+        cs.params["conductance"] = std::stof(c.parameter("conductance", "1.0"));
+        cs.params["learning rate"] = std::stof(c.parameter("learning rate", "0.1"));
+        cs.params["stp"] = c.parameter("short term plasticity", "true") == "true" ? 1.0f : 0.0f;
+        for (const char* k : {"short trace", "long trace", "presyn trace", "short term R",
+                              "short term w", "weight derivatives"})
+            cs.vars[k] = st.add_array(k, 'f', n, LAYOUT_MATRIX, R, C);
+        size_t tss_n = std::max<size_t>(n, c.from->size);
+        cs.vars["time since spike"] = st.add_array("time since spike", 'i', tss_n, LAYOUT_SOURCE,
+                                                   1, 1, c.from->size);
+        float* stp_r = cs.vars["short term R"]->hf();
+        float* stp_w = cs.vars["short term w"]->hf();
+        float* wd = cs.vars["weight derivatives"]->hf();
+        // quirk: the ConnectionType is compared with the ADD/SUB opcodes
+        // (izhikevich_attributes.cpp:723-728)
+        float w0 = c.type == 0 ? 0.5f : (c.type == 1 ? 0.2f : 0.0f);
+        for (size_t i = 0; i < n; ++i) { stp_r[i] = 1.0f; stp_w[i] = w0; wd[i] = 0.000001f; }
+        int32_t* tss = cs.vars["time since spike"]->hi();
+        for (size_t i = 0; i < tss_n; ++i) tss[i] = 32;
+
+        if (!cs.delays) {
+            cs.delays = st.add_array("delays", 'i', n, LAYOUT_MATRIX, R, C);
+            int32_t* dl = cs.delays->hi();
+            if (c.parameter("myelinated", "false") == "true") {
+                for (size_t i = 0; i < n; ++i) dl[i] = c.delay;
+            } else if (c.config.has("random delay")) {
+                int mx = std::stoi(c.parameter("random delay", "0"));
+                if (mx > 31) throw SgError("Randomized axons cannot have delays greater than 31!");
+                auto rng = make_rng(c.config, 3000 + c.index);
+                std::uniform_int_distribution<int> u(0, mx);
+                for (size_t i = 0; i < n; ++i) dl[i] = u(rng);
+            } else {
+                std::vector<float> dist = cs.cached_distances;
+                if (dist.empty()) {
+                    Indices ix = compute_indices(c);
+                    dist = compute_distances(c, ix,
+                                             std::stof(c.from->parameter("neuron spacing", "0.1")),
+                                             std::stof(c.to->parameter("neuron spacing", "0.1")),
+                                             std::stof(c.parameter("x offset", "0.0")),
+                                             std::stof(c.parameter("y offset", "0.0")));
+                }
+                compute_delays(c, dist, 0.15f, c.parameter("cap delay", "false") == "true", dl);
+            }
+        }
+        cs.vars["delays"] = cs.delays;
+
+        // Last (up to 32) visits of each source in serial order, device indices.
+        int nsrc = c.from->size;
+        cs.visit_counts = st.add_array("visit counts", 'i', nsrc);
+        cs.last_visits = st.add_array("last visits", 'i', (size_t)nsrc * 32);
+        int32_t* cnt = cs.visit_counts->hi();
+        int32_t* last = cs.last_visits->hi();
+        const bool transposed = R > 1 && C > 1;
+        enumerate_visits(c, [&](int, int, int from, long wi, int, int) {
+            long dev = transposed ? (wi % C) * (long)R + wi / C : wi;
+            last[(size_t)from * 32 + (cnt[from] % 32)] = (int)dev;
+            cnt[from]++;
+        });
+        // unroll each ring so that entries 0..m-1 are in serial order
+        std::vector<int32_t> tmp(32);
+        for (int f = 0; f < nsrc; ++f) {
+            int m = std::min(cnt[f], 32);
+            if (cnt[f] <= 32) continue;
+            int start = cnt[f] % 32;
+            for (int j = 0; j < m; ++j) tmp[j] = last[(size_t)f * 32 + (start + j) % 32];
+            for (int j = 0; j < m; ++j) last[(size_t)f * 32 + j] = tmp[j];
+        }
+        if (c.parameter("direct", "false") != "true" && c.opcode != OP_ADD && c.opcode != OP_SUB &&
+            c.opcode != OP_MULT && c.opcode != OP_REWARD && c.opcode != OP_GAP)
+            throw SgError(c.str() + ": Unimplemented connection type!");
+    }
+
+    void activate(State& st, ConnState& cs, const StepCtx& ctx) const override {
+        Connection& c = *cs.conn;
+        LayerState& to = *st.layer_state(c.to);
+        if (c.parameter("direct", "false") == "true") {
+            launch_base_activator(st, cs, to.input->df(), ctx.stream);
+            return;
+        }
+        const int threads = 128;
+        unsigned blocks = blocks_for(cs.geom.n_dest, threads);
+        if (c.opcode == OP_GAP) {
+            switch (c.type) {
+                case 0: k_iz_gap<0><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), to.input->df()); break;
+                case 1: k_iz_gap<1><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), to.input->df()); break;
+                case 2: k_iz_gap<2><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), to.input->df()); break;
+                case 3: k_iz_gap<3><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), to.input->df()); break;
+                case 4: k_iz_gap<4><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), to.input->df()); break;
+            }
+            SG_LAUNCH_CHECK();
+            return;
+        }
+        const char *sname, *lname = nullptr;
+        float stau, ltau = 0.0f;
+        switch (c.opcode) {
+            case OP_ADD: sname = "ampa"; stau = 0.8f; lname = "nmda"; ltau = 0.993f; break;
+            case OP_SUB: sname = "gabaa"; stau = 0.833f; lname = "gabab"; ltau = 0.993f; break;
+            case OP_MULT: sname = "mult"; stau = 0.95f; break;
+            case OP_REWARD: sname = "dopamine"; stau = 0.95f; break;
+            default: throw SgError(c.str() + ": Unimplemented connection type!");
+        }
+        const uint32_t* src = st.dev_output(c.from, word_index(c.delay, c.from->output_type));
+        // time since spike, from the same (pre-update) source words
+        k_iz_time_since_spike<<<blocks_for(c.from->size, 256), 256, 0, ctx.stream>>>(
+            c.from->size, cs.visit_counts->di(), cs.last_visits->di(), cs.delays->di(), src,
+            (int)c.from->output_type, cs.var("time since spike")->di());
+        SG_LAUNCH_CHECK();
+        int serial = c.convolutional ? 1 : 0;
+        if (serial) blocks = 1;
+        float* sc = to.var(sname)->df();
+        float* lc = lname ? to.var(lname)->df() : sc;
+        float g = cs.params.at("conductance");
+#define SG_IZ_ACT(LONG)                                                                        \
+    SG_DISPATCH_TYPE_SRC((int)c.type, (int)c.from->output_type,                                \
+        (k_iz_activate<TY, SR, LONG><<<blocks, threads, 0, ctx.stream>>>(                      \
+            cs.geom, serial, src, cs.weights->df(), cs.var("short term R")->df(),              \
+            cs.var("short term w")->df(), cs.delays->di(), cs.var("short trace")->df(),        \
+            cs.var("long trace")->df(), g, stau, ltau, sc, lc)))
+        if (lname) { SG_IZ_ACT(true); } else { SG_IZ_ACT(false); }
+#undef SG_IZ_ACT
+        SG_LAUNCH_CHECK();
+    }
+
+    void update(State& st, LayerState& ls, const StepCtx& ctx) const override {
+        const Layer& l = *ls.layer;
+        k_iz_update<<<blocks_for(l.size, 256), 256, 0, ctx.stream>>>(
+            l.size, l.history(), ls.input->df(), ls.output->du(), ls.var("ampa")->df(),
+            ls.var("nmda")->df(), ls.var("gabaa")->df(), ls.var("gabab")->df(), ls.var("mult")->df(),
+            ls.var("dopamine")->df(), ls.var("voltage")->df(), ls.var("recovery")->df(),
+            ls.var("post trace")->df(), ls.var("time since spike")->di(), ls.var("a")->df(),
+            ls.var("b")->df(), ls.var("c")->df(), ls.var("d")->df());
+        SG_LAUNCH_CHECK();
+    }
+
+    bool learns(const Connection& c) const override { return true; }
+
+    // get_updaters (izhikevich_attributes.cpp:522-539)
+    void learn(State& st, ConnState& cs, const StepCtx& ctx) const override {
+        Connection& c = *cs.conn;
+        if (c.convolutional || (c.opcode != OP_ADD && c.opcode != OP_SUB))
+            throw SgError(c.str() + ": Unimplemented connection type!");
+        LayerState& to = *st.layer_state(c.to);
+        static IzLut lut = [] {
+            IzLut t{};
+            for (int i = 1; i < 32; ++i) { t.src[i] = istdp_src(i); t.dst[i] = istdp_dst(i); }
+            return t;
+        }();
+        const int threads = 128;
+        unsigned blocks = blocks_for(cs.geom.n_dest, threads);
+        bool sub = c.opcode == OP_SUB;
+#define SG_IZ_LEARN(SUBV)                                                                      \
+    SG_DISPATCH_TYPE_SRC((int)c.type, (int)c.from->output_type,                                \
+        (k_iz_learn<TY, SR, SUBV><<<blocks, threads, 0, ctx.stream>>>(                         \
+            cs.geom, st.dev_output(c.to, 0), to.var("post trace")->df(),                       \
+            to.var("time since spike")->di(), cs.var("time since spike")->di(),                \
+            cs.params.at("learning rate"), (int)cs.params.at("stp"), c.max_weight,             \
+            cs.weights->df(), cs.var("presyn trace")->df(), cs.var("weight derivatives")->df(), \
+            cs.var("short term R")->df(), cs.var("short term w")->df(), lut)))
+        if (sub) { SG_IZ_LEARN(true); } else { SG_IZ_LEARN(false); }
+#undef SG_IZ_LEARN
+        SG_LAUNCH_CHECK();
+    }
+};
+SG_REGISTER_MODEL(IzhikevichModel);
+
+}  // namespace sg

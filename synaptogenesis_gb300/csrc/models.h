@@ -1,0 +1,65 @@
+// Neural-model plugin API.
+//
+// The GB300 counterpart of the reference's Attributes plugin base
+// (src/core/state/attributes.h:24-129) and its registry
+// (src/core/state/neural_model_bank.cpp:21-83): a model registers under its
+// JSON name with its output type, declares its per-neuron and per-synapse
+// variables, initialises them on the host (the constructor and
+// process_weight_matrix of the reference), and launches its CUDA kernels for
+// synaptic input (get_activators), the neuron update (get_kernel) and
+// plasticity (get_updaters).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "network.h"
+
+namespace sg {
+
+class State;
+struct LayerState;
+struct ConnState;
+
+// Per-step launch context handed to model kernels.
+struct StepCtx {
+    cudaStream_t stream;
+    bool last_step;          // the step whose input registers stay observable
+};
+
+class Model {
+  public:
+    virtual ~Model() = default;
+    virtual const char* name() const = 0;
+    virtual OutputType output_type() const = 0;
+
+    // Allocate model variables (State::add_array) and set host initial values.
+    virtual void build_layer(State& st, LayerState& ls) const {}
+    // Allocate and initialise per-synapse variables after the weights.
+    virtual void build_matrix(State& st, ConnState& cs) const {}
+    // Called once the state is on the device (device-only tables).
+    virtual void prepare_device(State& st, ConnState& cs, cudaStream_t s) const {}
+
+    // Synaptic input of one incoming connection (default: base activator).
+    virtual void activate(State& st, ConnState& cs, const StepCtx& ctx) const;
+    // Neuron update of one layer.
+    virtual void update(State& st, LayerState& ls, const StepCtx& ctx) const = 0;
+    // Whether a plastic connection into this model has an updater.
+    virtual bool learns(const Connection& c) const { return false; }
+    virtual void learn(State& st, ConnState& cs, const StepCtx& ctx) const {}
+};
+
+const Model* find_model(const std::string& name);
+bool register_model(const Model* m);
+std::vector<std::string> model_names();
+
+// Register in the model's translation unit: SG_REGISTER_MODEL(MyModel);
+#define SG_REGISTER_MODEL(CLS) \
+    static const bool sg_registered_##CLS = ::sg::register_model(new CLS())
+
+// Base activator launch (ACTIVATE_ALL(activate_base), kernel.cpp:217):
+// inputs[to] = aggregate(inputs[to], sum_k extract(out[from], delay) * w).
+void launch_base_activator(State& st, ConnState& cs, float* inputs, cudaStream_t s);
+
+}  // namespace sg

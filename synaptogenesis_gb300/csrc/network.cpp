@@ -1,0 +1,258 @@
+#include "network.h"
+
+#include <algorithm>
+#include <map>
+
+#include "models.h"
+
+namespace sg {
+
+static const std::vector<std::pair<std::string, ConnType>> kConnTypes = {
+    {"fully connected", FULLY_CONNECTED}, {"subset", SUBSET}, {"one to one", ONE_TO_ONE},
+    {"convergent", CONVERGENT}, {"divergent", DIVERGENT}};
+static const std::vector<std::pair<std::string, Opcode>> kOpcodes = {
+    {"add", OP_ADD}, {"sub", OP_SUB}, {"mult", OP_MULT}, {"div", OP_DIV}, {"pool", OP_POOL},
+    {"reward", OP_REWARD}, {"modulate", OP_MODULATE}, {"gap", OP_GAP},
+    {"add_heaviside", OP_ADD_HEAVISIDE}, {"sub_heaviside", OP_SUB_HEAVISIDE},
+    {"mult_heaviside", OP_MULT_HEAVISIDE}};
+
+ConnType parse_conn_type(const std::string& s) {
+    for (auto& p : kConnTypes) if (p.first == s) return p.second;
+    throw SgError("Unrecognized ConnectionType: " + s);
+}
+Opcode parse_opcode(const std::string& s) {
+    for (auto& p : kOpcodes) if (p.first == s) return p.second;
+    throw SgError("Unrecognized Opcode: " + s);
+}
+const char* conn_type_name(ConnType t) {
+    for (auto& p : kConnTypes) if (p.second == t) return p.first.c_str();
+    return "?";
+}
+const char* opcode_name(Opcode o) {
+    for (auto& p : kOpcodes) if (p.second == o) return p.first.c_str();
+    return "?";
+}
+
+int Layer::max_delay() const {
+    int m = 0;
+    for (auto* c : outputs) m = std::max(m, c->delay);
+    return m;
+}
+
+std::string Layer::str() const {
+    return "[Layer: " + name + " (" + structure->name + ")]";
+}
+
+// Same text as the reference's Connection::str() (connection.cpp:251-259); it
+// also keys saved state records.
+std::string Connection::str() const {
+    return "[Connection: " + from->name + " (" + from->structure->name + ") -> " + to->name +
+           " (" + to->structure->name + ") {Node: root} name=" + name + "]";
+}
+
+// ArborizedConfig (connection_config.cpp:8-45), including the "column offset"
+// quirk: the column offset is first read from "row offset".
+static Arbor parse_arbor(const Props& a) {
+    Arbor r;
+    r.row_field = a.get_int("row field size", 0);
+    r.col_field = a.get_int("column field size", 0);
+    r.row_stride = a.get_int("row stride", 1);
+    r.col_stride = a.get_int("column stride", 1);
+    r.row_spacing = a.get_int("row spacing", 1);
+    r.col_spacing = a.get_int("column spacing", 1);
+    r.row_offset = a.get_int("row offset", 0);
+    r.col_offset = a.get_int("row offset", 0);
+    r.wrap = a.get_bool("wrap", false);
+    if (a.has("field size")) r.row_field = r.col_field = a.get_int("field size", 0);
+    if (a.has("stride")) r.row_stride = r.col_stride = a.get_int("stride", 0);
+    if (a.has("spacing")) r.row_spacing = r.col_spacing = a.get_int("spacing", 0);
+    if (a.has("offset")) r.row_offset = r.col_offset = a.get_int("offset", 0);
+    if (r.row_field <= 0 || r.col_field <= 0)
+        throw SgError("Unspecified field size for arborized config!");
+    if (r.row_stride < 0 || r.col_stride < 0)
+        throw SgError("Cannot have negative stride in arborized config!");
+    if (r.row_spacing < 1 || r.col_spacing < 1)
+        throw SgError("Cannot have zero or negative spacing in arborized config!");
+    if (!a.has("row offset") && !a.has("offset")) r.row_offset = -r.row_field / 2;
+    if (!a.has("column offset") && !a.has("offset")) r.col_offset = -r.col_field / 2;
+    return r;
+}
+
+static SubsetCfg parse_subset(const Props& s) {
+    SubsetCfg r;
+    r.fr0 = s.get_int("from row start", 0);
+    r.fr1 = s.get_int("from row end", 0);
+    r.tr0 = s.get_int("to row start", 0);
+    r.tr1 = s.get_int("to row end", 0);
+    r.fc0 = s.get_int("from column start", 0);
+    r.fc1 = s.get_int("from column end", 0);
+    r.tc0 = s.get_int("to column start", 0);
+    r.tc1 = s.get_int("to column end", 0);
+    if (r.fr1 - r.fr0 <= 0 || r.tr1 - r.tr0 <= 0 || r.fc1 - r.fc0 <= 0 || r.tc1 - r.tc0 <= 0)
+        throw SgError("Invalid subset dimensions!");
+    return r;
+}
+
+Network::Network(const Props& config) : config_(config) {
+    for (Props* sp : config.child_array("structures")) {
+        if (!sp->has("name")) throw SgError("Unspecified name for structure!");
+        for (auto& s : structures)
+            if (s->name == sp->get("name")) throw SgError("Repeated structure name: " + s->name);
+        auto st = std::make_unique<Structure>();
+        st->name = sp->get("name");
+        st->cluster_type = sp->get("type", "parallel");
+        if (st->cluster_type != "parallel" && st->cluster_type != "sequential" &&
+            st->cluster_type != "feedforward")
+            throw SgError("Unrecognized ClusterType: " + st->cluster_type);
+        if (st->cluster_type != "parallel")
+            throw SgError("Structure " + st->name + ": only \"parallel\" structures are supported");
+        for (Props* lp : sp->child_array("layers")) {
+            auto l = std::make_unique<Layer>();
+            l->config = *lp;
+            if (!lp->has("name")) throw SgError("Attempted to construct LayerConfig without name!");
+            if (!lp->has("neural model"))
+                throw SgError("Attempted to construct LayerConfig without neural model!");
+            if (lp->has("image")) throw SgError("image-sized layers are not supported");
+            l->name = lp->get("name");
+            l->model = lp->get("neural model");
+            l->rows = lp->get_int("rows", 0);
+            l->cols = lp->get_int("columns", 0);
+            if (l->rows <= 0 || l->cols <= 0)
+                throw SgError("Invalid dimensions for layer " + l->name);
+            l->size = l->rows * l->cols;
+            l->plastic = lp->get_bool("plastic", false);
+            if (lp->get_bool("ghost", false)) throw SgError("ghost layers are not supported");
+            if (!lp->child_array("dendrites").empty())
+                throw SgError("Layer " + l->name + ": dendritic trees are not supported");
+            const Model* m = find_model(l->model);
+            if (!m) throw SgError("Unrecognized neural model \"" + l->model + "\"");
+            l->output_type = m->output_type();
+            l->structure = st.get();
+            for (auto* other : st->layers)
+                if (other->name == l->name) throw SgError("Repeated layer name : \"" + l->name + "\"");
+            l->index = (int)layers.size();
+            st->layers.push_back(l.get());
+            layers.push_back(std::move(l));
+        }
+        structures.push_back(std::move(st));
+    }
+    for (Props* cp : config.child_array("connections")) add_connection(*cp);
+}
+
+Structure* Network::structure(const std::string& name) const {
+    Structure* found = nullptr;
+    for (auto& s : structures) if (s->name == name) found = s.get();
+    return found;
+}
+
+Layer* Network::layer(const std::string& sname, const std::string& name) const {
+    Structure* s = structure(sname);
+    if (!s) throw SgError("Could not find structure: " + sname);
+    for (auto* l : s->layers) if (l->name == name) return l;
+    throw SgError("Could not find layer \"" + name + "\"");
+}
+
+Layer* Network::find_layer(const std::string& name) const {
+    Layer* found = nullptr;
+    for (auto& l : layers)
+        if (l->name == name) {
+            if (found) throw SgError("Ambiguous layer name: " + name);
+            found = l.get();
+        }
+    if (!found) throw SgError("Could not find layer: " + name);
+    return found;
+}
+
+Connection* Network::connection(const std::string& name) const {
+    Connection* found = nullptr;
+    for (auto& c : connections) if (c->name == name) found = c.get();
+    if (!found) throw SgError("Could not find connection: " + name);
+    return found;
+}
+
+long Network::total_weights() const {
+    long n = 0;
+    for (auto& c : connections) n += c->num_weights;
+    return n;
+}
+
+int Network::max_layer_size() const {
+    int m = 0;
+    for (auto& l : layers) m = std::max(m, l->size);
+    return m;
+}
+
+void Network::add_connection(const Props& p) {
+    if (!p.has("from layer")) throw SgError("Attempted to construct ConnectionConfig without source layer!");
+    if (!p.has("to layer")) throw SgError("Attempted to construct ConnectionConfig without destination layer!");
+    auto c = std::make_unique<Connection>();
+    c->config = p;
+    c->name = p.get("name", "");
+    std::string fl = p.get("from layer"), tl = p.get("to layer");
+    if (structures.size() == 1) {
+        c->from = layer(structures[0]->name, fl);
+        c->to = layer(structures[0]->name, tl);
+    } else {
+        c->from = p.has("from structure") ? layer(p.get("from structure"), fl) : find_layer(fl);
+        c->to = p.has("to structure") ? layer(p.get("to structure"), tl) : find_layer(tl);
+    }
+    if (p.get("dendrite", "root") != "root")
+        throw SgError(c->str() + ": dendritic nodes are not supported");
+    c->plastic = p.get_bool("plastic", true);
+    c->delay = p.get_int("delay", 0);
+    c->max_weight = p.get_float("max weight", 1.0f);
+    c->type = parse_conn_type(p.get("type", "fully connected"));
+    c->opcode = parse_opcode(p.get("opcode", "add"));
+    c->convolutional = p.get_bool("convolutional", false);
+    if (c->delay < 0) throw SgError("Attempted to construct ConnectionConfig with negative delay!");
+    if (p.get_bool("sparse", false) || p.get_bool("randomized projection", false))
+        throw SgError(c->str() + ": sparse connections are not supported");
+    if (c->convolutional && c->type != CONVERGENT && c->type != DIVERGENT)
+        throw SgError("Only convergent/divergent connections can be convolutional!");
+    Layer *from = c->from, *to = c->to;
+    switch (c->type) {
+        case FULLY_CONNECTED:
+            c->num_weights = (long)from->size * to->size;
+            c->matrix_rows = to->size;
+            c->matrix_cols = from->size;
+            break;
+        case SUBSET: {
+            Props* s = p.child("subset config");
+            if (!s) throw SgError("Attempted to create SUBSET connection without specifying subset configuration!");
+            c->subset = parse_subset(*s);
+            auto& sc = c->subset;
+            if (!(sc.fr1 <= from->rows && sc.fc1 <= from->cols && sc.tr1 <= to->rows && sc.tc1 <= to->cols))
+                throw SgError(c->str() + ": Invalid connection config!");
+            c->num_weights = (long)sc.from_size() * sc.to_size();
+            c->matrix_rows = sc.to_size();
+            c->matrix_cols = sc.from_size();
+            break;
+        }
+        case ONE_TO_ONE:
+            if (from->rows != to->rows || from->cols != to->cols)
+                throw SgError(c->str() + ": Cannot connect differently sized layers one-to-one!");
+            c->num_weights = to->size;
+            c->matrix_rows = to->size;
+            c->matrix_cols = 1;
+            break;
+        case CONVERGENT:
+        case DIVERGENT: {
+            Props* a = p.child("arborized config");
+            if (!a) throw SgError("Attempted to create arborized connection without specifying arborized configuration!");
+            c->arbor = parse_arbor(*a);
+            if (c->type == DIVERGENT && (c->arbor.row_stride == 0 || c->arbor.col_stride == 0))
+                throw SgError(c->str() + ": Divergent connections cannot have zero stride!");
+            c->num_weights = c->convolutional ? c->arbor.kernel() : (long)to->size * c->arbor.kernel();
+            c->matrix_rows = c->convolutional ? 1 : to->size;
+            c->matrix_cols = c->arbor.kernel();
+            break;
+        }
+    }
+    if (c->num_weights >= (1L << 31)) throw SgError(c->str() + ": more than 2^31 weights");
+    c->index = (int)connections.size();
+    from->outputs.push_back(c.get());
+    to->inputs.push_back(c.get());
+    connections.push_back(std::move(c));
+}
+
+}  // namespace sg

@@ -1,0 +1,120 @@
+// Network / Structure / Layer / Connection built from the reference's JSON
+// schema.  Field meanings, defaults and quirks follow
+//   src/core/network/network.cpp:5-217      (structure resolution)
+//   src/core/network/layer_config.cpp:11-33 (layer fields)
+//   src/core/network/connection_config.cpp:8-45, 112-134, 207-257
+//   src/core/network/connection.cpp:7-61, 224-248 (weight counts, matrix shape)
+#pragma once
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "props.h"
+
+namespace sg {
+
+enum OutputType { OUT_FLOAT = 0, OUT_BIT = 1, OUT_INT = 2 };
+enum ConnType { FULLY_CONNECTED = 0, SUBSET = 1, ONE_TO_ONE = 2, CONVERGENT = 3, DIVERGENT = 4 };
+enum Opcode {
+    OP_ADD = 0, OP_SUB, OP_MULT, OP_DIV, OP_POOL, OP_REWARD, OP_MODULATE, OP_GAP,
+    OP_ADD_HEAVISIDE, OP_SUB_HEAVISIDE, OP_MULT_HEAVISIDE
+};
+
+ConnType parse_conn_type(const std::string& s);
+Opcode parse_opcode(const std::string& s);
+const char* conn_type_name(ConnType t);
+const char* opcode_name(Opcode o);
+
+// Words of output history needed to serve a delay (util/constants.h:24-37).
+inline int word_index(int delay, OutputType t) { return t == OUT_BIT ? delay / 32 : delay; }
+
+struct Arbor {
+    int row_field = 0, col_field = 0, row_stride = 0, col_stride = 0;
+    int row_spacing = 0, col_spacing = 0, row_offset = 0, col_offset = 0;
+    bool wrap = false;
+    int kernel() const { return row_field * col_field; }
+};
+
+struct SubsetCfg {
+    int fr0 = 0, fr1 = 0, fc0 = 0, fc1 = 0, tr0 = 0, tr1 = 0, tc0 = 0, tc1 = 0;
+    int from_size() const { return (fr1 - fr0) * (fc1 - fc0); }
+    int to_size() const { return (tr1 - tr0) * (tc1 - tc0); }
+};
+
+struct Structure;
+struct Connection;
+
+struct Layer {
+    Props config;
+    std::string name;
+    Structure* structure = nullptr;
+    std::string model;
+    int rows = 0, cols = 0, size = 0;
+    bool plastic = false;
+    OutputType output_type = OUT_FLOAT;
+    std::vector<Connection*> inputs;    // in JSON order (dendritic DFS order)
+    std::vector<Connection*> outputs;
+    int index = 0;                      // position in network order
+
+    int max_delay() const;
+    int history() const { return 1 + word_index(max_delay(), output_type); }
+    std::string parameter(const std::string& k, const std::string& def) const {
+        return config.get(k, def);
+    }
+    std::string str() const;
+};
+
+struct Connection {
+    Props config;
+    std::string name;
+    Layer* from = nullptr;
+    Layer* to = nullptr;
+    bool plastic = true;
+    int delay = 0;
+    float max_weight = 1.0f;
+    ConnType type = FULLY_CONNECTED;
+    Opcode opcode = OP_ADD;
+    bool convolutional = false;
+    Arbor arbor;
+    SubsetCfg subset;
+    long num_weights = 0;
+    int matrix_rows = 0, matrix_cols = 0;
+    int index = 0;
+
+    // Destinations the per-destination loop visits (subset: its window).
+    int dest_count() const { return type == SUBSET ? subset.to_size() : to->size; }
+    std::string parameter(const std::string& k, const std::string& def) const {
+        return config.get(k, def);
+    }
+    std::string str() const;
+};
+
+struct Structure {
+    std::string name;
+    std::string cluster_type;
+    std::vector<Layer*> layers;
+};
+
+class Network {
+  public:
+    explicit Network(const Props& config);
+    const Props& config() const { return config_; }
+
+    Structure* structure(const std::string& name) const;
+    Layer* layer(const std::string& structure, const std::string& name) const;
+    Layer* find_layer(const std::string& name) const;          // unique across structures
+    Connection* connection(const std::string& name) const;     // last match wins
+
+    std::vector<std::unique_ptr<Structure>> structures;
+    std::vector<std::unique_ptr<Layer>> layers;                 // network order
+    std::vector<std::unique_ptr<Connection>> connections;       // JSON order
+
+    long total_weights() const;
+    int max_layer_size() const;
+
+  private:
+    void add_connection(const Props& p);
+    Props config_;
+};
+
+}  // namespace sg

@@ -1,0 +1,241 @@
+#include "state.h"
+
+#include <algorithm>
+#include <cstring>
+#include <fstream>
+#include <functional>
+
+#include "cuda_check.h"
+#include "models.h"
+#include "weight_init.h"
+
+namespace sg {
+
+Array* LayerState::var(const std::string& k) const {
+    if (k == "input") return input;
+    if (k == "output") return output;
+    auto it = vars.find(k);
+    if (it == vars.end())
+        throw SgError("Failed to retrieve neuron data \"" + k + "\" in Attributes!");
+    return it->second;
+}
+
+Array* ConnState::var(const std::string& k) const {
+    if (k == "weights") return weights;
+    if (k == "delays" && delays) return delays;
+    auto it = vars.find(k);
+    if (it == vars.end())
+        throw SgError("Failed to retrieve data \"" + k + "\" in WeightMatrix for connection:" +
+                      conn->str());
+    return it->second;
+}
+
+DGeom make_geom(const Connection& c) {
+    DGeom g{};
+    g.type = (int)c.type;
+    g.conv = c.convolutional ? 1 : 0;
+    g.from_rows = c.from->rows; g.from_cols = c.from->cols; g.from_size = c.from->size;
+    g.to_rows = c.to->rows; g.to_cols = c.to->cols; g.to_size = c.to->size;
+    const Arbor& a = c.arbor;
+    g.rf = a.row_field; g.cf = a.col_field; g.rs = a.row_stride; g.cs = a.col_stride;
+    g.rsp = a.row_spacing; g.csp = a.col_spacing; g.ro = a.row_offset; g.co = a.col_offset;
+    g.wrap = a.wrap ? 1 : 0;
+    const SubsetCfg& s = c.subset;
+    g.fr0 = s.fr0; g.fr1 = s.fr1; g.fc0 = s.fc0; g.fc1 = s.fc1; g.tr0 = s.tr0; g.tc0 = s.tc0;
+    g.tk_cols = s.tc1 - s.tc0;
+    g.tk_size = s.to_size();
+    g.n_dest = c.dest_count();
+    return g;
+}
+
+State::State(Network* net) : network(net) { build(); }
+
+State::~State() {
+    if (arena_) cudaFree(arena_);
+}
+
+Array* State::add_array(const std::string& name, char dtype, size_t count, ArrayLayout layout,
+                        int rows, int cols, size_t dev_count) {
+    if (arena_) throw SgError("state arrays cannot be added after device allocation");
+    auto a = std::make_unique<Array>();
+    a->name = name;
+    a->dtype = dtype;
+    a->count = count;
+    a->dev_count = dev_count ? dev_count : count;
+    a->layout = layout;
+    a->rows = rows;
+    a->cols = cols;
+    a->host.assign(count, 0u);
+    arrays_.push_back(std::move(a));
+    return arrays_.back().get();
+}
+
+void State::build() {
+    for (auto& lp : network->layers) {
+        Layer* l = lp.get();
+        auto ls = std::make_unique<LayerState>();
+        ls->layer = l;
+        ls->input = add_array("input", 'f', l->size);
+        ls->output = add_array("output", 'u', (size_t)l->history() * l->size);
+        find_model(l->model)->build_layer(*this, *ls);
+        layers.push_back(std::move(ls));
+    }
+    for (auto& cp : network->connections) {
+        Connection* c = cp.get();
+        auto cs = std::make_unique<ConnState>();
+        cs->conn = c;
+        cs->geom = make_geom(*c);
+        cs->weights = add_array("weights", 'f', c->num_weights, LAYOUT_MATRIX, c->matrix_rows,
+                                c->matrix_cols);
+        conns.push_back(std::move(cs));
+    }
+    // Weight initialisation and model processing follow the reference's order:
+    // all matrices of a layer are created with the layer's attributes
+    // (attributes.cpp:31-36), then processed (state.cpp:98-106).
+    for (auto& lp : network->layers) {
+        for (Connection* c : lp->inputs) init_weights(*this, *conns[c->index]);
+        for (Connection* c : lp->inputs)
+            find_model(lp->model)->build_matrix(*this, *conns[c->index]);
+    }
+}
+
+size_t State::host_bytes() const {
+    size_t n = 0;
+    for (auto& a : arrays_) n += a->count * 4;
+    return n;
+}
+
+void State::allocate_device() {
+    size_t off = 0;
+    for (auto& a : arrays_) {
+        a->dev_offset = off;
+        off += (a->dev_count * 4 + 255) / 256 * 256;
+    }
+    arena_bytes_ = std::max<size_t>(off, 256);
+    SG_CUDA(cudaMalloc(&arena_, arena_bytes_));
+    SG_CUDA(cudaMemset(arena_, 0, arena_bytes_));
+    for (auto& a : arrays_) a->dev = static_cast<char*>(arena_) + a->dev_offset;
+}
+
+// Blocked transpose of a [rows][cols] matrix of 32-bit words.
+static void transpose(const uint32_t* in, uint32_t* out, int rows, int cols) {
+    const int B = 64;
+    for (int r0 = 0; r0 < rows; r0 += B)
+        for (int c0 = 0; c0 < cols; c0 += B) {
+            int r1 = std::min(rows, r0 + B), c1 = std::min(cols, c0 + B);
+            for (int r = r0; r < r1; ++r)
+                for (int c = c0; c < c1; ++c) out[(size_t)c * rows + r] = in[(size_t)r * cols + c];
+        }
+}
+
+static bool needs_transpose(const Array& a) {
+    return a.layout == LAYOUT_MATRIX && a.rows > 1 && a.cols > 1;
+}
+
+void State::to_device(cudaStream_t stream) {
+    if (!arena_) allocate_device();
+    if (!on_host_) return;
+    for (auto& a : arrays_) {
+        if (a->dev_count == 0) continue;
+        const uint32_t* src = a->host.data();
+        if (needs_transpose(*a)) {
+            scratch_.resize(a->count);
+            transpose(a->host.data(), scratch_.data(), a->rows, a->cols);
+            src = scratch_.data();
+        }
+        size_t n = std::min(a->dev_count, a->count);
+        SG_CUDA(cudaMemcpy(a->dev, src, n * 4, cudaMemcpyHostToDevice));
+    }
+    for (auto& cp : network->connections)
+        find_model(cp->to->model)->prepare_device(*this, *conns[cp->index], stream);
+    SG_CUDA(cudaStreamSynchronize(stream));
+    on_host_ = false;
+}
+
+void State::to_host(cudaStream_t stream) {
+    if (on_host_) return;
+    SG_CUDA(cudaStreamSynchronize(stream));
+    for (auto& a : arrays_) {
+        if (a->dev_count == 0) continue;
+        size_t n = std::min(a->dev_count, a->count);
+        if (needs_transpose(*a)) {
+            scratch_.resize(a->count);
+            SG_CUDA(cudaMemcpy(scratch_.data(), a->dev, n * 4, cudaMemcpyDeviceToHost));
+            // device [cols][rows] -> host [rows][cols]
+            transpose(scratch_.data(), a->host.data(), a->cols, a->rows);
+        } else {
+            SG_CUDA(cudaMemcpy(a->host.data(), a->dev, n * 4, cudaMemcpyDeviceToHost));
+        }
+    }
+    on_host_ = true;
+}
+
+// ---------------------------------------------------------------------------
+// Save / load: a sequence of records [hash, type-hash, bytes][bytes of data],
+// keyed like the reference (PointerKey, util/resources/pointer.h:9-30): the
+// owner hash is std::hash of "structure/layer" or of the connection's str(),
+// the type hash is std::hash of the variable name.
+// ---------------------------------------------------------------------------
+namespace {
+struct Rec {
+    size_t hash, type, bytes;
+    Array* arr;
+};
+}  // namespace
+
+static std::vector<Rec> records(State& st) {
+    std::hash<std::string> h;
+    std::vector<Rec> out;
+    for (auto& ls : st.layers) {
+        size_t owner = h(ls->layer->structure->name + "/" + ls->layer->name);
+        out.push_back({owner, h("input"), ls->input->count * 4, ls->input});
+        out.push_back({owner, h("output"), ls->output->count * 4, ls->output});
+        for (auto& kv : ls->vars) out.push_back({owner, h(kv.first), kv.second->count * 4, kv.second});
+    }
+    for (auto& cs : st.conns) {
+        size_t owner = h(cs->conn->str());
+        out.push_back({owner, h("weights"), cs->weights->count * 4, cs->weights});
+        if (cs->delays) out.push_back({owner, h("delays"), cs->delays->count * 4, cs->delays});
+        for (auto& kv : cs->vars) out.push_back({owner, h(kv.first), kv.second->count * 4, kv.second});
+    }
+    std::sort(out.begin(), out.end(), [](const Rec& a, const Rec& b) {
+        return a.hash == b.hash ? a.type < b.type : a.hash < b.hash;
+    });
+    return out;
+}
+
+void State::save(const std::string& path) {
+    to_host(0);
+    std::ofstream f(path, std::ios::binary);
+    if (!f) throw SgError("Error writing state to file!");
+    for (auto& r : records(*this)) {
+        if (r.bytes == 0) continue;
+        size_t key[3] = {r.hash, r.type, r.bytes};
+        f.write(reinterpret_cast<const char*>(key), sizeof(key));
+        f.write(reinterpret_cast<const char*>(r.arr->host.data()), r.bytes);
+        if (!f) throw SgError("Error writing state to file!");
+    }
+}
+
+void State::load(const std::string& path) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) throw SgError("Could not open file: " + path);
+    to_host(0);
+    auto recs = records(*this);
+    for (;;) {
+        size_t key[3];
+        if (!f.read(reinterpret_cast<char*>(key), sizeof(key))) break;
+        Array* target = nullptr;
+        for (auto& r : recs)
+            if (r.hash == key[0] && r.type == key[1] && r.bytes == key[2]) target = r.arr;
+        if (target) {
+            if (!f.read(reinterpret_cast<char*>(target->host.data()), key[2]))
+                throw SgError("Error reading data from file!");
+        } else {
+            f.ignore(key[2]);
+        }
+    }
+    on_host_ = true;
+}
+
+}  // namespace sg

@@ -1,0 +1,229 @@
+#include "weight_init.h"
+
+#include <cmath>
+#include <sstream>
+
+#include "callbacks.h"
+
+namespace sg {
+
+static uint64_t g_seed = 0x5eed5eedULL;
+
+void set_global_seed(uint64_t seed) { g_seed = seed; }
+uint64_t global_seed() { return g_seed; }
+
+std::mt19937_64 make_rng(const Props& cfg, uint64_t salt) {
+    uint64_t seed = cfg.has("seed") ? std::stoull(cfg.get("seed")) : g_seed;
+    return std::mt19937_64(seed ^ (salt * 0x9E3779B97F4A7C15ULL));
+}
+
+Indices compute_indices(const Connection& c) {
+    Indices ix;
+    size_t n = c.num_weights;
+    ix.from_row.assign(n, -1); ix.from_col.assign(n, -1); ix.from_index.assign(n, -1);
+    ix.to_row.assign(n, -1); ix.to_col.assign(n, -1); ix.to_index.assign(n, -1);
+    ix.used.assign(n, 0);
+    const bool arbor = c.type == CONVERGENT || c.type == DIVERGENT;
+    const int fcols = c.from->cols, tcols = c.to->cols;
+    enumerate_visits(c, [&](int, int to, int from, long wi, int pr, int pc) {
+        int r = arbor ? pr : from / fcols;
+        int cc = arbor ? pc : from % fcols;
+        ix.from_row[wi] = r;
+        ix.from_col[wi] = cc;
+        ix.from_index[wi] = r * fcols + cc;
+        ix.to_row[wi] = to / tcols;
+        ix.to_col[wi] = to % tcols;
+        ix.to_index[wi] = to;
+        ix.used[wi] = 1;
+    });
+    return ix;
+}
+
+std::vector<float> compute_distances(const Connection& c, const Indices& ix, float from_spacing,
+                                     float to_spacing, float x_offset, float y_offset) {
+    std::vector<float> d(c.num_weights, 0.0f);
+    for (size_t i = 0; i < d.size(); ++i) {
+        float f_y = ix.from_row[i] * from_spacing;
+        float f_x = ix.from_col[i] * from_spacing;
+        float t_y = ix.to_row[i] * to_spacing + y_offset;
+        float t_x = ix.to_col[i] * to_spacing + x_offset;
+        d[i] = std::pow(std::pow(t_x - f_x, 2) + std::pow(t_y - f_y, 2), 0.5);
+    }
+    return d;
+}
+
+void compute_delays(const Connection& c, const std::vector<float>& dist, float velocity,
+                    bool cap, int32_t* delays) {
+    for (size_t i = 0; i < dist.size(); ++i) {
+        int delay = c.delay + (dist[i] / velocity);
+        if (delay > 31 && !cap)
+            throw SgError(c.str() + ": BIT delays cannot be greater than 31!");
+        delays[i] = delay < 31 ? delay : 31;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Initialisers (weight_matrix.cpp:676-851)
+// ---------------------------------------------------------------------------
+static void set_fraction(float* w, size_t n, float val, float fraction, std::mt19937_64& rng) {
+    if (fraction == 1.0f) {
+        for (size_t i = 0; i < n; ++i) w[i] = val;
+    } else {
+        std::uniform_real_distribution<float> d(0.0f, 1.0f);
+        for (size_t i = 0; i < n; ++i)
+            if (d(rng) < fraction) w[i] = val;
+    }
+}
+
+static void circular_mask(const Connection& c, const Props& cfg, float* w) {
+    if (c.type != CONVERGENT)
+        throw SgError(c.str() + ": CircularMaskConfig can only be used on convergent arborized connections!");
+    int rf = c.arbor.row_field, cf = c.arbor.col_field, K = c.arbor.kernel();
+    float row_radius = cfg.get_float("row radius", 0), col_radius = cfg.get_float("column radius", 0);
+    float row_d = cfg.get_float("row diameter", 0), col_d = cfg.get_float("column diameter", 0);
+    float radius = cfg.get_float("radius", 0), diameter = cfg.get_float("diameter", 0);
+    bool invert = cfg.get_bool("invert", false);
+    float value = cfg.get_float("value", 0.0f);
+    if (row_radius <= 0)
+        row_radius = row_d > 0 ? row_d / 2 : radius > 0 ? radius : diameter > 0 ? diameter / 2 : float(rf) / 2;
+    if (col_radius <= 0)
+        col_radius = col_d > 0 ? col_d / 2 : radius > 0 ? radius : diameter > 0 ? diameter / 2 : float(cf) / 2;
+    if (row_radius <= 0 || col_radius <= 0)
+        throw SgError(c.str() + ": Circular mask weight config radii must be positive!");
+    float row_center = float(rf) / 2, col_center = float(cf) / 2;
+    float row_sq = row_radius * row_radius, col_sq = col_radius * col_radius;
+    float sq_mult = row_sq * col_sq;
+    long reps = c.convolutional ? 1 : c.to->size;
+    for (long idx = 0; idx < reps; ++idx)
+        for (int kr = 0; kr < rf; ++kr)
+            for (int kc = 0; kc < cf; ++kc) {
+                float a = (float)(kr + 0.5 - row_center);
+                float b = (float)(kc + 0.5 - col_center);
+                float term = (a * a * col_sq) + (b * b * row_sq);
+                if (invert == (term <= sq_mult)) w[idx * K + kr * cf + kc] = value;
+            }
+}
+
+static void clear_diagonal(const Connection& c, float* w) {
+    switch (c.type) {
+        case FULLY_CONNECTED: {
+            if (c.from->size != c.to->size)
+                throw SgError("Attempted to clear diagonal of non-square weight matrix!");
+            for (long i = 0; i < c.from->size; ++i) w[i * c.from->size + i] = 0.0f;
+            break;
+        }
+        case SUBSET: {
+            int fs = c.subset.from_size();
+            if (fs != c.subset.to_size())
+                throw SgError("Attempted to clear diagonal of non-square weight matrix!");
+            for (long i = 0; i < fs; ++i) w[i * fs + i] = 0.0f;
+            break;
+        }
+        case CONVERGENT: {
+            Props p;
+            p.set("radius", "0.5");
+            p.set("invert", "true");
+            circular_mask(c, p, w);
+            break;
+        }
+        default: break;
+    }
+}
+
+void init_weights(State& st, ConnState& cs) {
+    Connection& c = *cs.conn;
+    Props empty;
+    const Props& cfg = c.config.child("weight config") ? *c.config.child("weight config") : empty;
+    size_t n = c.num_weights;
+    float* w = cs.weights->hf();
+    auto rng = make_rng(cfg, 1000 + c.index);
+
+    if (cfg.has("fraction")) {
+        float f = cfg.get_float("fraction", 1.0f);
+        if (f < 0 || f > 1.0f) throw SgError(c.str() + ": Weight config fraction must be between 0 and 1!");
+    }
+    float fraction = cfg.get_float("fraction", 1.0f);
+    std::string type = cfg.get("type", "flat");
+    if (type == "flat") {
+        set_fraction(w, n, cfg.get_float("weight", 1.0f), fraction, rng);
+    } else if (type == "random") {
+        float mx = cfg.get_float("max weight", c.max_weight), mn = cfg.get_float("min weight", 0.0f);
+        std::uniform_real_distribution<float> d(mn, mx);
+        std::uniform_real_distribution<float> fd(0.0f, 1.0f);
+        for (size_t i = 0; i < n; ++i)
+            if (fraction == 1.0f || fd(rng) < fraction) w[i] = d(rng);
+    } else if (type == "gaussian" || type == "log normal") {
+        float mean = cfg.get_float("mean", 1.0f), sd = cfg.get_float("std dev", 0.3f);
+        if (sd < 0) throw SgError(c.str() + ": weight config std_dev must be positive!");
+        if (sd == 0.0f) {
+            set_fraction(w, n, mean, fraction, rng);
+        } else {
+            std::normal_distribution<double> nd(mean, sd);
+            std::lognormal_distribution<double> ld(mean, sd);
+            std::uniform_real_distribution<double> fd(0.0, 1.0);
+            bool logn = type == "log normal";
+            for (size_t i = 0; i < n; ++i) {
+                if (fraction != 1.0f && !(fd(rng) < fraction)) { w[i] = 0.0f; continue; }
+                double v = logn ? ld(rng) : nd(rng);
+                w[i] = (float)std::min((double)c.max_weight, std::max(0.0, v));
+            }
+        }
+    } else if (type == "power law") {
+        float ex = std::fabs(cfg.get_float("exponent", 1.5f));
+        float mx = cfg.get_float("max weight", c.max_weight), mn = cfg.get_float("min weight", 0.0f);
+        if (c.max_weight < 0) throw SgError(c.str() + ": Power law config max must be positive!");
+        std::uniform_real_distribution<float> d(0.0f, 1.0f);
+        float ca = std::pow(mx, 1.0 - ex);
+        float cb = std::pow(std::max(mn, 0.00001f), 1.0 - ex);
+        float coeff = ca - cb, pexp = 1.0 / (1.0 - ex);
+        for (size_t i = 0; i < n; ++i) {
+            if (fraction != 1.0f && !(d(rng) < fraction)) { w[i] = 0.0f; continue; }
+            w[i] = std::pow(coeff * d(rng) + cb, pexp);
+        }
+    } else if (type == "specified") {
+        std::string s = cfg.get("weight string", "");
+        if (s.empty()) throw SgError(c.str() + ": Missing weight string for specified weight config!");
+        std::stringstream ss(s);
+        float v = 0.0f;
+        for (long i = 0; i < (long)n; ++i) {
+            if (!(ss >> v)) throw SgError(c.str() + ": Insufficient number of weights specified!");
+            w[i] = v;
+        }
+    } else {
+        throw SgError(c.str() + ": Unrecognized weight config type: " + type);
+    }
+
+    auto& cb = Callbacks::get();
+    int id = cfg.get_int("id", 0);
+    if (cfg.has("callback"))
+        Callbacks::find(cb.weight, cfg.get("callback"), "weight")(id, (int)n, w);
+    if (cfg.has("indices callback")) {
+        Indices ix = compute_indices(c);
+        Callbacks::find(cb.indices, cfg.get("indices callback"), "indices")(
+            id, (int)n, w, ix.from_index.data(), ix.to_index.data(), ix.used.data());
+    }
+    if (cfg.has("distance callback")) {
+        float fs = cfg.has("from spacing") ? cfg.get_float("from spacing", 1.0f)
+                                           : c.from->config.get_float("neuron spacing", 1.0f);
+        float ts = cfg.has("to spacing") ? cfg.get_float("to spacing", 1.0f)
+                                         : c.to->config.get_float("neuron spacing", 1.0f);
+        Indices ix = compute_indices(c);
+        std::vector<float> dist = compute_distances(c, ix, fs, ts, cfg.get_float("x offset", 0.0f),
+                                                    cfg.get_float("y offset", 0.0f));
+        Callbacks::find(cb.distance, cfg.get("distance callback"), "distance")(id, (int)n, w, dist.data());
+        cs.params["__has_distances"] = 1.0f;
+        cs.cached_distances = std::move(dist);
+    }
+    if (cfg.has("delay callback")) {
+        if (!cs.delays) {
+            cs.delays = st.add_array("delays", 'i', n, LAYOUT_MATRIX, c.matrix_rows, c.matrix_cols);
+            for (size_t i = 0; i < n; ++i) cs.delays->hi()[i] = c.delay;
+        }
+        Callbacks::find(cb.delay, cfg.get("delay callback"), "delay")(id, (int)n, w, cs.delays->hi());
+    }
+    if (Props* m = cfg.child("circular mask")) circular_mask(c, *m, w);
+    for (Props* m : cfg.child_array("circular mask")) circular_mask(c, *m, w);
+    if (!cfg.get_bool("diagonal", true)) clear_diagonal(c, w);
+}
+
+}  // namespace sg

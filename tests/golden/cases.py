@@ -27,11 +27,11 @@ class Case:
         self.learning = learning
         self.tol = tol or {}             # key -> relative tolerance (float paths with libm)
 
-    def input_arrays(self, sizes):
+    def input_arrays(self, sizes, steps=None):
         """Per-step input arrays, deterministic in the seed."""
         rng = _rng(self.seed + 1000)
         out = []
-        for t in range(self.steps):
+        for t in range(self.steps if steps is None else steps):
             out.append({name: fn(rng, t, sizes[name]).astype(np.float32)
                         for name, fn in sorted(self.inputs.items())})
         return out

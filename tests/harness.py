@@ -39,7 +39,7 @@ def run_oracle(case, steps=None):
             dst = net.get_weight_matrix(key[1], key[2])
         assert dst.size == arr.size, key
         dst.view(arr.dtype)[:] = arr
-    inputs = case.input_arrays(sizes)
+    inputs = case.input_arrays(sizes, steps)
     rec = {k: [] for k in case.record}
     for t in range(steps):
         net.step(inputs[t], learning=case.learning)
@@ -83,7 +83,7 @@ def run_library(case, syngen, steps=None):
             dst = net.get_weight_matrix(key[1], key[2]).to_np_array()
         assert dst.size == arr.size, (key, dst.size, arr.size)
         dst.view(arr.dtype)[:] = arr
-    inputs = case.input_arrays(sizes)
+    inputs = case.input_arrays(sizes, steps)
     step = {"in": 0}
     in_layers = sorted(case.inputs)
     rec = {k: [] for k in case.record}
