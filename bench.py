@@ -1,0 +1,382 @@
+"""Benchmark of the GB300 simulation cycle (one JSON line on rank 0).
+
+Default workload: game of life on a 2048x2048 toroidal grid (3x3 convergent
+wrap connection, B3/S23, cells alive with p=0.3 from seed 1); one bench step is
+the full 10,000-timestep run of that grid.  Metric: synapse updates per second
+(a synapse update is one (destination, weight) visit in one timestep: 9 per
+cell, as the reference computes the zero centre weight too).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload gol|iz_plastic]
+  python bench.py --impl reference ...   # the reference's own CPU path
+
+Timing: each step is bracketed by CUDA events recorded on the stream the
+library launches every kernel on; L2 is flushed (a 256 MiB buffer is written)
+between steps, outside the events.  Under torchrun each rank runs an
+independent replica on its own GPU (the single-network cycle does not shard);
+value is the sum over ranks of units over the max over ranks of time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+REF_LIB = os.path.join(ROOT, "oracle", "_ref", "libsyngen.so")
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC = os.path.join(ROOT, "profiles", "traffic.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+# ---------------------------------------------------------------------------
+# Workloads (synthetic, seeded)
+# ---------------------------------------------------------------------------
+def gol_workload(side=2048):
+    import numpy as np
+    net = {"structures": [{"name": "g", "type": "parallel", "layers": [
+        {"name": "board", "neural model": "game_of_life", "rows": side, "columns": side,
+         "survival_min": 2, "survival_max": 3, "birth_min": 3, "birth_max": 3}]}],
+        "connections": [{"name": "nbr", "from layer": "board", "to layer": "board",
+                         "type": "convergent", "convolutional": True, "plastic": False,
+                         "opcode": "add",
+                         "weight config": {"type": "flat", "weight": 1.0, "diagonal": False},
+                         "arborized config": {"field size": 3, "wrap": True}}]}
+    n = side * side
+
+    def inject(net_obj):
+        rng = np.random.default_rng(1)
+        out = net_obj.get_neuron_data("g", "board", "output").to_np_array().view(np.uint32)
+        out[:] = (rng.random(n) < 0.3).astype(np.uint32) << np.uint32(31)
+
+    def result(net_obj):
+        return net_obj.get_neuron_data("g", "board", "output").to_np_array()
+
+    return {
+        "name": "gol",
+        "desc": "game_of_life %dx%d toroidal, 3x3 convergent wrap, B3/S23, p_alive=0.3 seed 1" % (side, side),
+        "net": net, "inject": inject, "result": result,
+        "timesteps": 10000,                  # per bench step: the full configured run
+        "units_per_timestep": 9 * n,
+        "unit": "synapse-updates/s",
+        "dtype": "u32",
+        "kernel": "game_of_life.update",     # launch group holding k_gol_fused
+        "bytes_per_launch": 8 * n,           # read + write the 32-bit history word
+        "state_bytes": 8 * n + 36,           # input + output + weights moved per e2e step
+        "cpu_seconds": 12.0,
+        "learning": False,
+    }
+
+
+WORKLOADS = {"gol": gol_workload}
+
+
+# ---------------------------------------------------------------------------
+# Helpers
+# ---------------------------------------------------------------------------
+def measured_peak():
+    try:
+        with open(PEAKS) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.rows = []
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "50"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def dist_setup():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def reduce_max(values, world):
+    if world == 1:
+        return values
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(values, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the reference's own library (or the oracle port) timed on the
+# host cores on a bounded sample of the workload.
+# ---------------------------------------------------------------------------
+def cpu_worker(args):
+    """Runs in a child process with SYNGEN_LIB set; prints one JSON object."""
+    wl = WORKLOADS[args.workload]()
+    from synaptogenesis_gb300 import syngen as sg
+    sg.set_warnings(False)
+    net = sg.Network(wl["net"])
+    net.build_state()
+    wl["inject"](net)
+    env = sg.Environment({"modules": []})
+    run_args = {"multithreaded": False, "worker threads": 0, "learning flag": wl["learning"]}
+    t0 = time.perf_counter()
+    net.run(env, dict(run_args, iterations=2))
+    per = max((time.perf_counter() - t0) / 2, 1e-6)
+    steps = max(2, int(args.cpu_seconds / per))
+    if args.cpu_timesteps:
+        steps = args.cpu_timesteps
+    t0 = time.perf_counter()
+    rep = net.run(env, dict(run_args, iterations=steps))
+    dt = time.perf_counter() - t0
+    assert rep.obj is not None, "reference run failed"
+    print(json.dumps({"value": wl["units_per_timestep"] * steps / dt, "seconds": dt,
+                      "timesteps": steps}))
+
+
+def cpu_baseline(workload, seconds, timesteps=0):
+    from oracle import build_ref
+    lib = build_ref.build()
+    cores = os.cpu_count() or 1
+    if lib is None:
+        return {"value": None, "unit": WORKLOADS[workload]()["unit"], "cores": 0, "kind": "reference",
+                "sample": "unavailable: reference sources absent"}
+    env = dict(os.environ, SYNGEN_LIB=lib, OMP_NUM_THREADS=str(cores))
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--cpu-worker", "--workload", workload,
+           "--cpu-seconds", str(seconds), "--cpu-timesteps", str(timesteps)]
+    r = subprocess.run(cmd, env=env, capture_output=True, text=True, timeout=900)
+    if r.returncode != 0:
+        return {"value": None, "unit": WORKLOADS[workload]()["unit"], "cores": cores,
+                "kind": "reference", "sample": "failed: " + r.stderr[-300:]}
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    return {"value": out["value"], "unit": WORKLOADS[workload]()["unit"], "cores": cores,
+            "kind": "reference",
+            "sample": "%d timesteps of the same workload, %.1f s wall, OMP_NUM_THREADS=%d"
+                      % (out["timesteps"], out["seconds"], cores),
+            "timesteps": out["timesteps"], "seconds": out["seconds"]}
+
+
+# ---------------------------------------------------------------------------
+# GB300 arm
+# ---------------------------------------------------------------------------
+def run_gb300(args, rank, world, local):
+    import torch
+    from synaptogenesis_gb300 import syngen as sg
+    sg.set_warnings(False)
+    wl = WORKLOADS[args.workload]()
+    T = args.timesteps or wl["timesteps"]
+    net = sg.Network(wl["net"])
+    net.build_state()
+    wl["inject"](net)
+    run_args = {"learning flag": wl["learning"], "graph steps": 16}
+
+    # -- device-resident throughput ------------------------------------------
+    eng = sg.Engine(net, None, run_args)
+    stream = torch.cuda.ExternalStream(eng.stream)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        eng.step(T)
+    rep0 = eng.report()
+    launches0 = int(rep0.properties["kernel launches"])
+    gpu_index = os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0]
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = ClockSampler(gpu_index)
+    evs = []
+    t_wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.add_(1.0)                       # L2 flush, outside the events
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        eng.step(T)
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    barrier(world)
+    clk = clocks.stop()
+    dev_ms = sum(a.elapsed_time(b) for a, b in evs)
+    rep1 = eng.report()
+    launches = int(rep1.properties["kernel launches"]) - launches0
+    eng.close()
+
+    # -- per-kernel timing of the dominant kernel (separate profiled pass) ----
+    prof_steps = min(T, 400)
+    with sg.Engine(net, None, dict(run_args, profile=True)) as peng:
+        peng.step(prof_steps)
+        prep = peng.report()
+    kern = {p.properties["name"]: p.properties for p in prep.child_arrays.get("kernel times", [])}
+    dom = kern.get(wl["kernel"])
+    mean_us = float(dom["mean us"]) if dom else None
+
+    # -- end to end through the public API with host buffers ----------------
+    env = sg.Environment({"modules": []})
+    net.get_neuron_data("g", "board", "output") if args.workload == "gol" else None
+    e2e_steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        rep = net.run(env, dict(run_args, iterations=T))      # H2D of the state, then T timesteps
+        assert rep.obj is not None, sg.last_error()
+        res = wl["result"](net)                               # D2H of the state
+        _ = int(res.view("uint32")[0])
+    e2e_s = time.perf_counter() - t0
+
+    secs = dev_ms / 1000.0
+    dev_max, = reduce_max([secs], world)
+    e2e_max, = reduce_max([e2e_s], world)
+    units = wl["units_per_timestep"] * T * args.steps
+    out = {
+        "dev_s": dev_max, "units": units * world, "wall_s": t_wall, "launches": launches,
+        "mean_us": mean_us, "clocks": clk, "kernels": kern,
+        "e2e_value": wl["units_per_timestep"] * T * e2e_steps * world / e2e_max,
+        "e2e_steps": e2e_steps, "wl": wl, "T": T,
+    }
+    return out
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default="gol", choices=sorted(WORKLOADS))
+    p.add_argument("--timesteps", type=int, default=0, help="timesteps per bench step")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-worker", action="store_true", help=argparse.SUPPRESS)
+    p.add_argument("--cpu-seconds", type=float, default=0.0, help=argparse.SUPPRESS)
+    p.add_argument("--cpu-timesteps", type=int, default=0, help=argparse.SUPPRESS)
+    args = p.parse_args()
+    if args.cpu_worker:
+        cpu_worker(args)
+        return
+
+    rank, world, local = dist_setup()
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = os.environ.get("CUDA_VISIBLE_DEVICES",
+                                                            ",".join(str(i) for i in range(world))
+                                                            ).split(",")[local]
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    wl = WORKLOADS[args.workload]()
+    metric = "synapse-updates/s (%s)" % wl["name"]
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from oracle import build_ref
+        if build_ref.build() is None:
+            print(json.dumps({"impl": "reference", "unavailable": "reference sources absent"}))
+            return
+        # each bench step: a bounded sample of the workload on all host cores
+        per_step_s = max(1.0, 60.0 / max(1, args.steps + args.warmup))
+        cb = cpu_baseline(args.workload, per_step_s * (args.steps + args.warmup))
+        if cb["value"] is None:
+            print(json.dumps({"impl": "reference", "unavailable": cb["sample"]}))
+            return
+        ts_per_step = max(1, cb["timesteps"] // max(1, args.steps + args.warmup))
+        ms_per_step = 1000.0 * cb["seconds"] / max(1, args.steps + args.warmup)
+        line = {"metric": metric, "value": cb["value"], "unit": wl["unit"], "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": wl["dtype"], "data": "synthetic", "impl": "reference",
+                "config": {"workload": wl["desc"], "timesteps_per_step": ts_per_step,
+                           "host_threads": cb["cores"]},
+                "cpu_baseline": dict(cb),
+                "e2e": {"value": cb["value"], "unit": wl["unit"], "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    r = run_gb300(args, rank, world, local)
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak()
+    achieved = None
+    if r["mean_us"]:
+        achieved = wl["bytes_per_launch"] / (r["mean_us"] * 1e-6) / 1e9
+    traffic = None
+    try:
+        with open(TRAFFIC) as f:
+            traffic = json.load(f).get(args.workload)
+    except Exception:
+        pass
+    cb = None
+    if not args.no_cpu_baseline:
+        cb = cpu_baseline(args.workload, wl["cpu_seconds"])
+    value = r["units"] / r["dev_s"]
+    line = {
+        "metric": metric, "value": value, "unit": wl["unit"], "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * r["dev_s"] / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": wl["dtype"], "data": "synthetic",
+        "config": {"workload": wl["desc"], "timesteps_per_step": r["T"],
+                   "ms_per_timestep": 1000.0 * r["dev_s"] / (args.steps * r["T"]),
+                   "l2": "flushed between steps (256 MiB write outside the timed events)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None,
+                     "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": wl["kernel"], "bytes_per_launch": wl["bytes_per_launch"],
+                     "mean_launch_us": r["mean_us"]},
+        "cpu_baseline": cb,
+        "e2e": {"value": r["e2e_value"], "unit": wl["unit"],
+                "h2d_bytes_per_step": wl["state_bytes"], "d2h_bytes_per_step": wl["state_bytes"],
+                "steps": r["e2e_steps"]},
+        "clocks": r["clocks"],
+        "gpu_launches": r["launches"],
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

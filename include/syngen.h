@@ -130,6 +130,21 @@ void finalize_mpi(void);
 
 /* Message of the last failed call on this thread ("" if none). */
 const char* sg_last_error(void);
+
+/* Persistent engine: run() split into create / step / report / destroy, so a
+ * caller can advance the same state repeatedly without rebuilding.  Behaves
+ * like run() (src/core/engine/engine.cpp:462-596): same args, same step order,
+ * same callbacks.  Without host callbacks, steps replay a captured CUDA graph.
+ * At most one engine exists at a time (engine.cpp:466-471). */
+typedef void* SG_ENGINE;
+SG_ENGINE sg_engine_create(NETWORK net, ENVIRONMENT env, STATE state, PROPS args);
+/* Runs `steps` (> 0) timesteps; returns the number run, or -1 on error. */
+long long sg_engine_step(SG_ENGINE engine, long long steps);
+/* The CUDA stream (cudaStream_t) every kernel of the engine is launched on. */
+void* sg_engine_stream(SG_ENGINE engine);
+/* Report of all steps so far (same keys as run()'s report), owned by caller. */
+PROPS sg_engine_report(SG_ENGINE engine);
+void sg_engine_destroy(SG_ENGINE engine);
 /* Seed of the random weight / parameter / noise initialisers. */
 void sg_set_seed(unsigned long long seed);
 /* ABI version of this header. */

@@ -67,6 +67,7 @@ void launch_base_activator(State& st, ConnState& cs, float* inputs, cudaStream_t
 
 void Model::activate(State& st, ConnState& cs, const StepCtx& ctx) const {
     launch_base_activator(st, cs, st.layer_state(cs.conn->to)->input->df(), ctx.stream);
+    ctx.count();
 }
 
 // ---------------------------------------------------------------------------
@@ -118,6 +119,34 @@ __global__ void k_gol(int size, int history, const float* __restrict__ in, uint3
     shift_bits(out, size, history, nid, live ? 1u : 0u);
 }
 
+// Fused game_of_life step for a layer whose only input is its own convergent
+// connection: the base activator's sequential weighted count (prior 0, "add"),
+// the life rule and the history shift in one pass.  Reads the output words of
+// step t-1 from `cur` and writes step t to `next` (ping-pong), so every other
+// reader of the layer still sees step t-1.  2-D blocks keep the neighbour
+// words of a block in L1.
+__global__ void __launch_bounds__(256) k_gol_fused(DGeom g, int delay, const uint32_t* __restrict__ cur,
+                                                   uint32_t* __restrict__ next,
+                                                   const float* __restrict__ w,
+                                                   float* __restrict__ input_out, int smin, int smax,
+                                                   int bmin, int bmax) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    int r = blockIdx.y * blockDim.y + threadIdx.y;
+    if (c >= g.to_cols || r >= g.to_rows) return;
+    int d = r * g.to_cols + c;
+    float sum = 0.0f;
+    for_each_source<T_CONV>(g, d, [&](int from, int wi) {
+        float val = extract<S_BIT>(__ldg(cur + from), delay) * __ldg(w + wi);
+        sum += val;
+    });
+    float input = 0.0f + sum;
+    if (input_out) input_out[d] = input;
+    int n = (int)input;
+    uint32_t word = cur[d];
+    bool live = (word & 1u) ? (n >= smin && n <= smax) : (n >= bmin && n <= bmax);
+    next[d] = (word >> 1) | ((live ? 1u : 0u) << 31);
+}
+
 class RelayModel : public Model {
   public:
     const char* name() const override { return "relay"; }
@@ -130,6 +159,7 @@ class RelayModel : public Model {
         k_relay<<<blocks_for(l.size, 256), 256, 0, ctx.stream>>>(
             l.size, l.history(), ls.input->df(), ls.output->df(), (int)ls.params.at("ramp"));
         SG_LAUNCH_CHECK();
+        ctx.count();
     }
 };
 SG_REGISTER_MODEL(RelayModel);
@@ -143,6 +173,7 @@ class RateEncodingModel : public Model {
         k_rate<<<blocks_for(l.size, 256), 256, 0, ctx.stream>>>(l.size, l.history(), ls.input->df(),
                                                                 ls.output->df());
         SG_LAUNCH_CHECK();
+        ctx.count();
     }
 };
 SG_REGISTER_MODEL(RateEncodingModel);
@@ -151,19 +182,51 @@ class GameOfLifeModel : public Model {
   public:
     const char* name() const override { return "game_of_life"; }
     OutputType output_type() const override { return OUT_BIT; }
-    void build_layer(State&, LayerState& ls) const override {
+    // The fused step applies to a layer whose only input is its own
+    // convergent "add" connection reading word 0, with no init config, no
+    // environment input and a one-word history.
+    static bool fusable_shape(const Layer& l) {
+        if (l.inputs.size() != 1) return false;
+        const Connection* c = l.inputs[0];
+        return c->from == &l && c->type == CONVERGENT && c->opcode == OP_ADD && c->delay < 32 &&
+               l.history() == 1 && !l.config.child("init config");
+    }
+    void build_layer(State& st, LayerState& ls) const override {
         const Layer& l = *ls.layer;
         ls.params["smin"] = (float)std::stoi(l.parameter("survival_min", "2"));
         ls.params["smax"] = (float)std::stoi(l.parameter("survival_max", "3"));
         ls.params["bmin"] = (float)std::stoi(l.parameter("birth_min", "3"));
         ls.params["bmax"] = (float)std::stoi(l.parameter("birth_max", "3"));
+        if (fusable_shape(l)) {
+            Array* swap = st.add_array("output swap", 'u', l.size);
+            swap->scratch = true;
+            ls.internal["output swap"] = swap;
+        }
     }
-    void update(State&, LayerState& ls, const StepCtx& ctx) const override {
+    bool fuses_input(State&, const Connection& c, const StepCtx& ctx) const override {
+        return fusable_shape(*c.to) && !ctx.is_input(*c.to);
+    }
+    void update(State& st, LayerState& ls, const StepCtx& ctx) const override {
         const Layer& l = *ls.layer;
-        k_gol<<<blocks_for(l.size, 256), 256, 0, ctx.stream>>>(
-            l.size, l.history(), ls.input->df(), ls.output->du(), (int)ls.params.at("smin"),
-            (int)ls.params.at("smax"), (int)ls.params.at("bmin"), (int)ls.params.at("bmax"));
+        int smin = (int)ls.params.at("smin"), smax = (int)ls.params.at("smax");
+        int bmin = (int)ls.params.at("bmin"), bmax = (int)ls.params.at("bmax");
+        if (fusable_shape(l) && !ctx.is_input(l)) {
+            ConnState& cs = *st.conn_state(l.inputs[0]);
+            Array* swap = ls.internal.at("output swap");
+            dim3 block(32, 8);
+            dim3 grid(blocks_for(l.cols, 32), blocks_for(l.rows, 8));
+            k_gol_fused<<<grid, block, 0, ctx.stream>>>(
+                cs.geom, cs.conn->delay, ls.output->du(), swap->du(), cs.weights->df(),
+                ctx.last_step ? ls.input->df() : nullptr, smin, smax, bmin, bmax);
+            SG_LAUNCH_CHECK();
+            std::swap(ls.output->dev, swap->dev);
+            ctx.count();
+            return;
+        }
+        k_gol<<<blocks_for(l.size, 256), 256, 0, ctx.stream>>>(l.size, l.history(), ls.input->df(),
+                                                               ls.output->du(), smin, smax, bmin, bmax);
         SG_LAUNCH_CHECK();
+        ctx.count();
     }
 };
 SG_REGISTER_MODEL(GameOfLifeModel);

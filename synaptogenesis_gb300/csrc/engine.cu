@@ -1,9 +1,7 @@
 #include "engine.h"
 
 #include <algorithm>
-#include <chrono>
 #include <cstring>
-#include <mutex>
 
 #include "cuda_check.h"
 #include "models.h"
@@ -24,8 +22,9 @@ cudaStream_t engine_stream() {
 }
 
 // ---------------------------------------------------------------------------
-// Input-register initialisation kernels (engine/kernel/kernel.cpp:14-158).
-// Noise uses a seeded counter-based generator (the reference's is unseedable).
+// Input-register initialisation (engine/kernel/kernel.cpp:14-158).  Noise is
+// drawn from a seeded counter-based generator keyed by (seed, step, neuron);
+// the step comes from a device counter so captured graphs stay valid.
 // ---------------------------------------------------------------------------
 __global__ void k_set_value(float* p, int n, float v, int overwrite) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -39,23 +38,24 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
     return x ^ (x >> 31);
 }
 
-__device__ __forceinline__ float uniform01(unsigned long long seed, long step, int i, int draw) {
-    unsigned long long h = mix64(seed ^ mix64((unsigned long long)step * 0x100000001B3ULL + draw) ^
-                                 ((unsigned long long)i << 20));
+__device__ __forceinline__ float uniform01(unsigned long long seed, long long step, int i, int draw) {
+    unsigned long long h =
+        mix64(seed ^ mix64((unsigned long long)step * 0x100000001B3ULL + draw) ^ ((unsigned long long)i << 20));
     return ((h >> 40) + 1) * (1.0f / 16777217.0f);   // (0, 1)
 }
 
-// kind 0 uniform(a, b), 1 normal(a=mean, b=std), 2 poisson(rate a -> value b)
+// kind 0 uniform(a, b), 1 normal(mean a, std b), 2 poisson(probability a, value b)
 __global__ void k_noise(float* p, int n, int kind, float a, float b, int overwrite,
-                        unsigned long long seed, long step) {
+                        unsigned long long seed, const long long* step) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    float u = uniform01(seed, step, i, 0);
+    long long t = *step;
+    float u = uniform01(seed, t, i, 0);
     float v;
     if (kind == 0) {
         v = u * (b - a) + a;
     } else if (kind == 1) {
-        float u2 = uniform01(seed, step, i, 1);
+        float u2 = uniform01(seed, t, i, 1);
         v = sqrtf(-2.0f * logf(u)) * cospif(2.0f * u2) * b + a;
     } else {
         if (overwrite) { p[i] = u < a ? b : 0.0f; return; }
@@ -65,8 +65,80 @@ __global__ void k_noise(float* p, int n, int kind, float a, float b, int overwri
     p[i] = overwrite ? v : p[i] + v;
 }
 
+__global__ void k_step_counter(long long* step) { *step += 1; }
+
+// ---------------------------------------------------------------------------
+Engine::Engine(Network* net, Environment* env, State* state, const Props& args)
+    : net_(net), env_(env), state_(state), args_(args), stream_(engine_stream()) {
+    bool expected = false;
+    if (!running.compare_exchange_strong(expected, true))
+        throw SgError("Cannot run more than one engine at once!");
+    try {
+        if (args.has("devices")) {
+            int d = args.get_int("devices", 0);
+            if (d != 0) throw SgError("Failed to extract devices from Engine args! (one GPU: device 0)");
+        }
+        verbose_ = args.get_bool("verbose", false);
+        learning_ = args.get_bool("learning flag", true);
+        suppress_ = args.get_bool("suppress output", false);
+        env_rate_ = std::max(1, args.get_int("environment rate", 1));
+        profile_ = args.get_bool("profile", false);
+        use_graphs_ = args.get_bool("graphs", true) && !profile_;
+        graph_steps_ = std::max(2, args.get_int("graph steps", 16) / 2 * 2);
+        build_modules();
+        if (!modules_.empty()) use_graphs_ = false;
+        for (auto& lp : net_->layers) {
+            Props* init = lp->config.child("init config");
+            if (init && init->get("type", "normal") != "flat") step_counter_ = true;
+        }
+        state_->to_device(stream_);
+        for (auto& lp : net_->layers) {
+            if (layer_io_[lp->index] & 1) input_layers_.push_back(lp.get());
+            if (layer_io_[lp->index] & 2) output_layers_.push_back(lp.get());
+        }
+        in_dirty_.assign(input_layers_.size(), 0);
+        for (Layer* l : input_layers_) {
+            void* h;
+            void* d;
+            SG_CUDA(cudaMallocHost(&h, (size_t)l->size * 4));
+            std::memset(h, 0, (size_t)l->size * 4);
+            SG_CUDA(cudaMalloc(&d, (size_t)l->size * 4));
+            SG_CUDA(cudaMemsetAsync(d, 0, (size_t)l->size * 4, stream_));
+            in_pinned_.push_back((float*)h);
+            in_staging_.push_back((float*)d);
+        }
+        for (Layer* l : output_layers_) {
+            void* h;
+            SG_CUDA(cudaMallocHost(&h, (size_t)l->size * 4));
+            out_pinned_.push_back((uint32_t*)h);
+        }
+        SG_CUDA(cudaMalloc(&d_step_, sizeof(long long)));
+        SG_CUDA(cudaMemsetAsync(d_step_, 0, sizeof(long long), stream_));
+        SG_CUDA(cudaStreamSynchronize(stream_));
+    } catch (...) {
+        for (float* p : in_pinned_) cudaFreeHost(p);
+        for (float* p : in_staging_) cudaFree(p);
+        for (uint32_t* p : out_pinned_) cudaFreeHost(p);
+        if (d_step_) cudaFree(d_step_);
+        running = false;
+        throw;
+    }
+}
+
+Engine::~Engine() {
+    cudaStreamSynchronize(stream_);
+    for (float* p : in_pinned_) cudaFreeHost(p);
+    for (float* p : in_staging_) cudaFree(p);
+    for (uint32_t* p : out_pinned_) cudaFreeHost(p);
+    if (d_step_) cudaFree(d_step_);
+    for (auto& g : graphs_) cudaGraphExecDestroy(g.exec);
+    for (auto& kv : prof_)
+        for (auto& e : kv.second.events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+    running = false;
+    interrupt_flag = false;
+}
+
 void Engine::build_modules() {
-    modules_.clear();
     layer_io_.assign(net_->layers.size(), 0);
     if (!env_) return;
     for (Props* mp : env_->config.child_array("modules")) {
@@ -107,23 +179,41 @@ void Engine::build_modules() {
     }
 }
 
-void Engine::enqueue_step(int step, bool last, bool learning) {
-    cudaStream_t s = engine_stream();
-    StepCtx ctx{s, last};
+template <class F>
+void Engine::timed(const std::string& name, long kernels, F&& f) {
+    if (!profile_) { f(); return; }
+    cudaEvent_t a, b;
+    SG_CUDA(cudaEventCreate(&a));
+    SG_CUDA(cudaEventCreate(&b));
+    SG_CUDA(cudaEventRecord(a, stream_));
+    f();
+    SG_CUDA(cudaEventRecord(b, stream_));
+    auto& p = prof_[name];
+    p.events.push_back({a, b});
+    p.launches += kernels;
+}
+
+void Engine::enqueue_step(bool last) {
+    StepCtx ctx{stream_, last, &layer_io_, &launches_};
     // 1. input registers
     for (auto& lp : net_->layers) {
         Layer* l = lp.get();
+        const Model* m = find_model(l->model);
         LayerState* ls = state_->layer_state(l);
         float* in = ls->input->df();
         bool is_input = (layer_io_[l->index] & 1) != 0;
+        bool all_fused = !l->inputs.empty();
+        for (Connection* c : l->inputs) all_fused = all_fused && m->fuses_input(*state_, *c, ctx);
+        if (all_fused && !is_input) continue;   // the fused update writes the register itself
         if (is_input) {
             size_t k = std::find(input_layers_.begin(), input_layers_.end(), l) - input_layers_.begin();
             if (in_dirty_[k]) {
-                SG_CUDA(cudaMemcpyAsync(in_staging_[k], in_pinned_[k], l->size * 4,
-                                        cudaMemcpyHostToDevice, s));
+                SG_CUDA(cudaMemcpyAsync(in_staging_[k], in_pinned_[k], (size_t)l->size * 4,
+                                        cudaMemcpyHostToDevice, stream_));
                 in_dirty_[k] = 0;
             }
-            SG_CUDA(cudaMemcpyAsync(in, in_staging_[k], l->size * 4, cudaMemcpyDeviceToDevice, s));
+            SG_CUDA(cudaMemcpyAsync(in, in_staging_[k], (size_t)l->size * 4, cudaMemcpyDeviceToDevice,
+                                    stream_));
         }
         Props* init = l->config.child("init config");
         if (init) {
@@ -132,195 +222,213 @@ void Engine::enqueue_step(int step, bool last, bool learning) {
             unsigned long long seed = init->has("seed") ? std::stoull(init->get("seed"))
                                                         : (global_seed() ^ (0xA5A5ULL * (l->index + 1)));
             unsigned blocks = blocks_for(l->size, 256);
-            if (t == "flat") {
-                k_set_value<<<blocks, 256, 0, s>>>(in, l->size, init->get_float("value", 1.0f), ow);
-            } else if (t == "uniform") {
-                k_noise<<<blocks, 256, 0, s>>>(in, l->size, 0, init->get_float("min", 0.0f),
-                                               init->get_float("max", 1.0f), ow, seed, step);
-            } else if (t == "normal") {
-                k_noise<<<blocks, 256, 0, s>>>(in, l->size, 1, init->get_float("mean", 1.0f),
-                                               init->get_float("std dev", 0.1f), ow, seed, step);
-            } else if (t == "poisson") {
-                if (init->get_bool("random", false))
-                    throw SgError("random per-neuron Poisson rates are not supported");
-                k_noise<<<blocks, 256, 0, s>>>(in, l->size, 2, 0.001f * init->get_float("rate", 1.0f),
-                                               init->get_float("value", 20.0f), ow, seed, step);
-            } else {
-                throw SgError("Error building cluster node for " + l->str() + ":\n  Unrecognized init type: " + t);
-            }
-            SG_LAUNCH_CHECK();
+            timed("init", 1, [&] {
+                if (t == "flat") {
+                    k_set_value<<<blocks, 256, 0, stream_>>>(in, l->size, init->get_float("value", 1.0f), ow);
+                } else if (t == "uniform") {
+                    k_noise<<<blocks, 256, 0, stream_>>>(in, l->size, 0, init->get_float("min", 0.0f),
+                                                         init->get_float("max", 1.0f), ow, seed, d_step_);
+                } else if (t == "normal") {
+                    k_noise<<<blocks, 256, 0, stream_>>>(in, l->size, 1, init->get_float("mean", 1.0f),
+                                                         init->get_float("std dev", 0.1f), ow, seed, d_step_);
+                } else if (t == "poisson") {
+                    if (init->get_bool("random", false))
+                        throw SgError("random per-neuron Poisson rates are not supported");
+                    k_noise<<<blocks, 256, 0, stream_>>>(in, l->size, 2,
+                                                         0.001f * init->get_float("rate", 1.0f),
+                                                         init->get_float("value", 20.0f), ow, seed, d_step_);
+                } else {
+                    throw SgError("Error building cluster node for " + l->str() +
+                                  ":\n  Unrecognized init type: " + t);
+                }
+                SG_LAUNCH_CHECK();
+            });
             ++launches_;
         } else if (!is_input) {
-            SG_CUDA(cudaMemsetAsync(in, 0, (size_t)l->size * 4, s));
+            SG_CUDA(cudaMemsetAsync(in, 0, (size_t)l->size * 4, stream_));
         }
     }
     // 2. synaptic input
     for (auto& lp : net_->layers) {
         const Model* m = find_model(lp->model);
         for (Connection* c : lp->inputs) {
-            m->activate(*state_, *state_->conn_state(c), ctx);
-            ++launches_;
+            if (m->fuses_input(*state_, *c, ctx)) continue;
+            timed(std::string(lp->model) + ".activate." + conn_type_name(c->type), 1, [&] {
+                m->activate(*state_, *state_->conn_state(c), ctx);
+            });
         }
     }
     // 3. neuron updates
     for (auto& lp : net_->layers) {
-        find_model(lp->model)->update(*state_, *state_->layer_state(lp.get()), ctx);
-        ++launches_;
+        const Model* m = find_model(lp->model);
+        timed(std::string(lp->model) + ".update", 1, [&] {
+            m->update(*state_, *state_->layer_state(lp.get()), ctx);
+        });
     }
     // 4. plasticity
-    if (learning)
+    if (learning_)
         for (auto& lp : net_->layers) {
             const Model* m = find_model(lp->model);
             for (Connection* c : lp->inputs)
                 if (c->plastic && m->learns(*c)) {
-                    m->learn(*state_, *state_->conn_state(c), ctx);
-                    ++launches_;
+                    timed(std::string(lp->model) + ".learn." + conn_type_name(c->type), 1, [&] {
+                        m->learn(*state_, *state_->conn_state(c), ctx);
+                    });
                 }
         }
+    if (step_counter_) {
+        k_step_counter<<<1, 1, 0, stream_>>>(d_step_);
+        SG_LAUNCH_CHECK();
+        ++launches_;
+    }
 }
 
-Props* Engine::run(const Props& args) {
-    bool expected = false;
-    if (!running.compare_exchange_strong(expected, true))
-        throw SgError("Cannot run more than one engine at once!");
-    struct Guard {
-        Engine* e;
-        std::vector<void*> pinned;
-        std::vector<void*> dev;
-        ~Guard() {
-            for (void* p : pinned) cudaFreeHost(p);
-            for (void* p : dev) cudaFree(p);
-            Engine::running = false;
-            Engine::interrupt_flag = false;
+void Engine::feed_input() {
+    // module.cpp:86-97: callbacks write the pinned buffers; they must not be
+    // overwritten while a copy from them is still queued.
+    bool synced = false;
+    for (auto& m : modules_) {
+        if (m.start_delay > 0) continue;
+        bool active = m.active();
+        bool cut = m.cutoff != 0 && m.curr == m.cutoff;
+        for (auto& ml : m.layers) {
+            if (!ml.input || (!active && !cut)) continue;
+            if (!synced) { SG_CUDA(cudaStreamSynchronize(stream_)); synced = true; }
+            size_t k = std::find(input_layers_.begin(), input_layers_.end(), ml.layer) - input_layers_.begin();
+            if (active) {
+                if (m.clear) std::memset(in_pinned_[k], 0, (size_t)ml.layer->size * 4);
+                ml.fn(ml.id, ml.layer->size, in_pinned_[k]);
+            } else {
+                std::memset(in_pinned_[k], 0, (size_t)ml.layer->size * 4);
+            }
+            in_dirty_[k] = 1;
         }
-    } guard{this, {}, {}};
-
-    if (args.has("devices")) {
-        int n = 0;
-        cudaGetDeviceCount(&n);
-        int d = args.get_int("devices", 0);
-        if (d != 0 && d != n) throw SgError("Failed to extract devices from Engine args!");
     }
-    const bool verbose = args.get_bool("verbose", false);
-    const bool learning = args.get_bool("learning flag", true);
-    const bool suppress = args.get_bool("suppress output", false);
-    const int env_rate = std::max(1, args.get_int("environment rate", 1));
-    long iterations = args.get_int("iterations", 0);
+}
 
-    build_modules();
-    cudaStream_t s = engine_stream();
-    state_->to_device(s);
+void Engine::report_output(long i) {
+    // module.cpp:99-104
+    if (i % env_rate_ != 0 || suppress_ || output_layers_.empty()) return;
+    for (size_t k = 0; k < output_layers_.size(); ++k)
+        SG_CUDA(cudaMemcpyAsync(out_pinned_[k], state_->dev_output(output_layers_[k], 0),
+                                (size_t)output_layers_[k]->size * 4, cudaMemcpyDeviceToHost, stream_));
+    SG_CUDA(cudaStreamSynchronize(stream_));
+    for (auto& m : modules_) {
+        if (!m.active()) continue;
+        for (auto& ml : m.layers)
+            if (ml.output) {
+                size_t k = std::find(output_layers_.begin(), output_layers_.end(), ml.layer) -
+                           output_layers_.begin();
+                ml.fn(ml.id, ml.layer->size, out_pinned_[k]);
+            }
+    }
+}
 
-    input_layers_.clear();
-    output_layers_.clear();
-    for (auto& lp : net_->layers) {
-        if (layer_io_[lp->index] & 1) input_layers_.push_back(lp.get());
-        if (layer_io_[lp->index] & 2) output_layers_.push_back(lp.get());
-    }
-    in_pinned_.clear(); in_staging_.clear(); out_pinned_.clear();
-    in_dirty_.assign(input_layers_.size(), 0);
-    for (Layer* l : input_layers_) {
-        void* h; void* d;
-        SG_CUDA(cudaMallocHost(&h, (size_t)l->size * 4));
-        std::memset(h, 0, (size_t)l->size * 4);
-        guard.pinned.push_back(h);
-        SG_CUDA(cudaMalloc(&d, (size_t)l->size * 4));
-        SG_CUDA(cudaMemsetAsync(d, 0, (size_t)l->size * 4, s));
-        guard.dev.push_back(d);
-        in_pinned_.push_back((float*)h);
-        in_staging_.push_back((float*)d);
-    }
-    for (Layer* l : output_layers_) {
-        void* h;
-        SG_CUDA(cudaMallocHost(&h, (size_t)l->size * 4));
-        guard.pinned.push_back(h);
-        out_pinned_.push_back((uint32_t*)h);
-    }
-    auto index_of = [](const std::vector<Layer*>& v, Layer* l) {
-        return (size_t)(std::find(v.begin(), v.end(), l) - v.begin());
-    };
+void Engine::launch_step(bool last) {
+    feed_input();
+    enqueue_step(last);
+}
 
+long Engine::step(long n) {
     cudaEvent_t ev0, ev1;
     SG_CUDA(cudaEventCreate(&ev0));
     SG_CUDA(cudaEventCreate(&ev1));
-    SG_CUDA(cudaStreamSynchronize(s));
     auto t0 = std::chrono::steady_clock::now();
-    SG_CUDA(cudaEventRecord(ev0, s));
-    launches_ = 0;
+    SG_CUDA(cudaEventRecord(ev0, stream_));
     long i = 0;
-    for (; iterations == 0 || i < iterations; ++i) {
-        // feed input (module.cpp:86-97): the callback writes the pinned
-        // buffer; it must not be overwritten while a copy from it is queued.
-        bool any_input_cb = false;
-        for (auto& m : modules_) {
-            if (m.start_delay > 0) continue;
-            bool active = (m.cutoff == 0 || m.curr < m.cutoff) && m.curr % m.rate == 0;
-            bool cut = m.cutoff != 0 && m.curr == m.cutoff;
-            for (auto& ml : m.layers) {
-                if (!ml.input) continue;
-                if (!any_input_cb) { SG_CUDA(cudaStreamSynchronize(s)); any_input_cb = true; }
-                size_t k = index_of(input_layers_, ml.layer);
-                if (active) {
-                    if (m.clear) std::memset(in_pinned_[k], 0, (size_t)ml.layer->size * 4);
-                    ml.fn(ml.id, ml.layer->size, in_pinned_[k]);
-                    in_dirty_[k] = 1;
-                } else if (cut) {
-                    std::memset(in_pinned_[k], 0, (size_t)ml.layer->size * 4);
-                    in_dirty_[k] = 1;
-                }
+    while (n == 0 || i < n) {
+        if (interrupt_flag) break;
+        if (use_graphs_ && n != 0 && n - i > graph_steps_) {
+            // Ping-pong outputs may sit in either buffer; a graph is only valid
+            // for the buffer placement it was captured with.
+            std::vector<void*> sig;
+            for (auto& ls : state_->layers) sig.push_back(ls->output->dev);
+            Graph* gr = nullptr;
+            for (auto& cand : graphs_)
+                if (cand.sig == sig) gr = &cand;
+            if (!gr) {
+                // Capture an even number of steps, so ping-pong buffers end
+                // where they started.
+                Graph ng;
+                ng.sig = sig;
+                long before = launches_;
+                cudaGraph_t g;
+                SG_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+                for (int k = 0; k < graph_steps_; ++k) enqueue_step(false);
+                SG_CUDA(cudaStreamEndCapture(stream_, &g));
+                SG_CUDA(cudaGraphInstantiate(&ng.exec, g, 0));
+                SG_CUDA(cudaGraphDestroy(g));
+                ng.launches = launches_ - before;
+                launches_ = before;
+                graphs_.push_back(ng);
+                gr = &graphs_.back();
             }
+            SG_CUDA(cudaGraphLaunch(gr->exec, stream_));
+            launches_ += gr->launches;
+            i += graph_steps_;
+            continue;
         }
-        bool last = iterations != 0 && i == iterations - 1;
-        enqueue_step((int)i, last, learning);
-        // report output (module.cpp:99-104)
-        if (i % env_rate == 0 && !suppress && !output_layers_.empty()) {
-            for (size_t k = 0; k < output_layers_.size(); ++k)
-                SG_CUDA(cudaMemcpyAsync(out_pinned_[k], state_->dev_output(output_layers_[k], 0),
-                                        (size_t)output_layers_[k]->size * 4,
-                                        cudaMemcpyDeviceToHost, s));
-            SG_CUDA(cudaStreamSynchronize(s));
-            for (auto& m : modules_) {
-                if (m.start_delay > 0 || !((m.cutoff == 0 || m.curr < m.cutoff) && m.curr % m.rate == 0))
-                    continue;
-                for (auto& ml : m.layers)
-                    if (ml.output)
-                        ml.fn(ml.id, ml.layer->size, out_pinned_[index_of(output_layers_, ml.layer)]);
-            }
-        }
+        bool last = (n != 0 && i == n - 1);
+        launch_step(last);
+        report_output(i);
         for (auto& m : modules_) {
             if (m.start_delay > 0) { --m.start_delay; continue; }
             if (m.cutoff == 0 || m.curr <= m.cutoff) ++m.curr;
         }
-        if (interrupt_flag) { ++i; break; }
+        ++i;
     }
-    SG_CUDA(cudaEventRecord(ev1, s));
+    SG_CUDA(cudaEventRecord(ev1, stream_));
     SG_CUDA(cudaEventSynchronize(ev1));
     auto t1 = std::chrono::steady_clock::now();
-    float dev_ms = 0.0f;
-    SG_CUDA(cudaEventElapsedTime(&dev_ms, ev0, ev1));
+    float ms = 0.0f;
+    SG_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
     SG_CUDA(cudaGetLastError());
     state_->mark_device_newer();
+    device_ms_ += ms;
+    wall_s_ += std::chrono::duration<double>(t1 - t0).count();
+    steps_ += i;
+    return i;
+}
 
-    double total = std::chrono::duration<double>(t1 - t0).count();
+void Engine::synchronize() { SG_CUDA(cudaStreamSynchronize(stream_)); }
+
+Props* Engine::report() {
+    synchronize();
     auto* r = new Props();
-    r->set("iterations", std::to_string(i));
-    r->set("total time", std::to_string((float)total));
-    r->set("average time", std::to_string((float)(i ? total / i : 0.0)));
-    r->set("fps", std::to_string((float)(total > 0 ? i / total : 0.0)));
+    r->set("iterations", std::to_string(steps_));
+    r->set("total time", std::to_string((float)wall_s_));
+    r->set("average time", std::to_string((float)(steps_ ? wall_s_ / steps_ : 0.0)));
+    r->set("fps", std::to_string((float)(wall_s_ > 0 ? steps_ / wall_s_ : 0.0)));
     r->set("network bytes", std::to_string(state_->device_bytes()));
     r->set("state buffer bytes", "0");
     size_t eb = 0;
     for (Layer* l : input_layers_) eb += (size_t)l->size * 4;
     for (Layer* l : output_layers_) eb += (size_t)l->size * 4;
     r->set("engine buffer bytes", std::to_string(eb));
-    r->set("device time", std::to_string(dev_ms / 1000.0f));
+    r->set("device time", std::to_string(device_ms_ / 1000.0f));
     r->set("kernel launches", std::to_string(launches_));
-    r->set_child("args", args);
+    r->set("graphs", use_graphs_ ? "true" : "false");
+    r->set_child("args", args_);
     r->set("interrupted", interrupt_flag ? "true" : "false");
-    if (verbose)
-        printf("Ran %ld iterations in %fs (device %fs)\n", i, total, dev_ms / 1000.0f);
+    for (auto& kv : prof_) {
+        double total = 0.0;
+        for (auto& e : kv.second.events) {
+            float ms = 0.0f;
+            SG_CUDA(cudaEventElapsedTime(&ms, e.first, e.second));
+            total += ms;
+        }
+        Props k;
+        k.set("name", kv.first);
+        k.set("groups", std::to_string(kv.second.events.size()));
+        k.set("launches", std::to_string(kv.second.launches));
+        k.set("total ms", std::to_string(total));
+        k.set("mean us", std::to_string(kv.second.events.empty() ? 0.0 : 1000.0 * total / kv.second.events.size()));
+        r->add_to_child_array("kernel times", k);
+    }
+    if (verbose_)
+        printf("Ran %ld iterations in %fs (device %fs)\n", steps_, wall_s_, device_ms_ / 1000.0f);
     return r;
 }
 

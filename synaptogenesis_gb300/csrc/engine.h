@@ -12,11 +12,14 @@
 //   5. output of the new step to the environment.
 // All kernels go to one CUDA stream.  Host callbacks (the "callback" module,
 // src/core/io/impl/callback_module.cpp:29-51) fill pinned input buffers and read
-// pinned output buffers between steps.
+// pinned output buffers between steps.  Without host callbacks, pairs of steps
+// are captured once into a CUDA graph and replayed.
 #pragma once
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <chrono>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -37,8 +40,14 @@ cudaStream_t engine_stream();
 
 class Engine {
   public:
-    Engine(Network* net, Environment* env, State* state) : net_(net), env_(env), state_(state) {}
-    Props* run(const Props& args);
+    Engine(Network* net, Environment* env, State* state, const Props& args);
+    ~Engine();
+
+    // Runs n steps (n == 0: until interrupted).  Returns steps run.
+    long step(long n);
+    void synchronize();
+    Props* report();
+    cudaStream_t stream() const { return stream_; }
 
     static std::atomic<bool> interrupt_flag;
     static std::atomic<bool> running;
@@ -54,22 +63,50 @@ class Engine {
         std::vector<ModLayer> layers;
         bool clear = false;
         int start_delay = 0, cutoff = 0, rate = 1, curr = 0;
+        bool active() const {
+            return start_delay <= 0 && (cutoff == 0 || curr < cutoff) && curr % rate == 0;
+        }
+    };
+    struct Prof {
+        std::vector<std::pair<cudaEvent_t, cudaEvent_t>> events;
+        long launches = 0;
     };
 
     void build_modules();
-    void enqueue_step(int step, bool last, bool learning);
+    void feed_input();
+    void report_output(long i);
+    void enqueue_step(bool last);
+    void launch_step(bool last);
+    template <class F>
+    void timed(const std::string& name, long kernels, F&& f);
 
     Network* net_;
     Environment* env_;
     State* state_;
+    Props args_;
+    cudaStream_t stream_;
+    bool learning_ = true, suppress_ = false, verbose_ = false, use_graphs_ = true;
+    bool profile_ = false;
+    int env_rate_ = 1;
     std::vector<Module> modules_;
-    std::vector<Layer*> input_layers_, output_layers_;
-    std::vector<float*> in_pinned_;      // per input layer (host)
-    std::vector<float*> in_staging_;     // per input layer (device)
-    std::vector<char> in_dirty_;
-    std::vector<uint32_t*> out_pinned_;  // per output layer (host)
     std::vector<int> layer_io_;          // per layer: bit0 input, bit1 output
-    long launches_ = 0;
+    std::vector<Layer*> input_layers_, output_layers_;
+    std::vector<float*> in_pinned_, in_staging_;
+    std::vector<char> in_dirty_;
+    std::vector<uint32_t*> out_pinned_;
+    long long* d_step_ = nullptr;        // device step counter (noise generators)
+    struct Graph {
+        std::vector<void*> sig;          // output buffers the graph was captured with
+        cudaGraphExec_t exec = nullptr;
+        long launches = 0;
+    };
+    std::vector<Graph> graphs_;          // one per ping-pong placement
+    int graph_steps_ = 16;               // steps per captured graph (even)
+    bool step_counter_ = false;          // a noise generator reads the step counter
+    long launches_ = 0, steps_ = 0;
+    double wall_s_ = 0.0;
+    float device_ms_ = 0.0f;
+    std::map<std::string, Prof> prof_;
 };
 
 }  // namespace sg

@@ -209,8 +209,10 @@ PROPS run(NETWORK net, ENVIRONMENT env, STATE st, PROPS args) {
     if (!net || !st) return nullptr;
     SG_TRY(nullptr)
     Props empty;
-    Engine e(((NetHandle*)net)->net, (Environment*)env, ((StateHandle*)st)->state);
-    return e.run(args ? *(Props*)args : empty);
+    const Props& a = args ? *(Props*)args : empty;
+    Engine e(((NetHandle*)net)->net, (Environment*)env, ((StateHandle*)st)->state, a);
+    e.step(a.get_int("iterations", 0));
+    return e.report();
     SG_CATCH(nullptr)
 }
 
@@ -277,6 +279,40 @@ void finalize_mpi() {}
 // Extensions
 // ---------------------------------------------------------------------------
 const char* sg_last_error(void) { return g_last_error.c_str(); }
+
+SG_ENGINE sg_engine_create(NETWORK net, ENVIRONMENT env, STATE st, PROPS args) {
+    if (!net || !st) return nullptr;
+    SG_TRY(nullptr)
+    Props empty;
+    return new Engine(((NetHandle*)net)->net, (Environment*)env, ((StateHandle*)st)->state,
+                      args ? *(Props*)args : empty);
+    SG_CATCH(nullptr)
+}
+
+long long sg_engine_step(SG_ENGINE eng, long long steps) {
+    if (!eng || steps <= 0) return -1;
+    SG_TRY(-1)
+    return ((Engine*)eng)->step((long)steps);
+    SG_CATCH(-1)
+}
+
+void* sg_engine_stream(SG_ENGINE eng) {
+    return eng ? (void*)((Engine*)eng)->stream() : nullptr;
+}
+
+PROPS sg_engine_report(SG_ENGINE eng) {
+    if (!eng) return nullptr;
+    SG_TRY(nullptr)
+    return ((Engine*)eng)->report();
+    SG_CATCH(nullptr)
+}
+
+void sg_engine_destroy(SG_ENGINE eng) {
+    try {
+        delete (Engine*)eng;
+    } catch (...) {
+    }
+}
 
 void sg_set_seed(unsigned long long seed) { set_global_seed(seed); }
 

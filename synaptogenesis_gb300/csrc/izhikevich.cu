@@ -354,6 +354,7 @@ class IzhikevichModel : public Model {
         LayerState& to = *st.layer_state(c.to);
         if (c.parameter("direct", "false") == "true") {
             launch_base_activator(st, cs, to.input->df(), ctx.stream);
+            ctx.count();
             return;
         }
         const int threads = 128;
@@ -367,6 +368,7 @@ class IzhikevichModel : public Model {
                 case 4: k_iz_gap<4><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), to.input->df()); break;
             }
             SG_LAUNCH_CHECK();
+            ctx.count();
             return;
         }
         const char *sname, *lname = nullptr;
@@ -384,6 +386,7 @@ class IzhikevichModel : public Model {
             c.from->size, cs.visit_counts->di(), cs.last_visits->di(), cs.delays->di(), src,
             (int)c.from->output_type, cs.var("time since spike")->di());
         SG_LAUNCH_CHECK();
+        ctx.count();
         int serial = c.convolutional ? 1 : 0;
         if (serial) blocks = 1;
         float* sc = to.var(sname)->df();
@@ -398,6 +401,7 @@ class IzhikevichModel : public Model {
         if (lname) { SG_IZ_ACT(true); } else { SG_IZ_ACT(false); }
 #undef SG_IZ_ACT
         SG_LAUNCH_CHECK();
+        ctx.count();
     }
 
     void update(State& st, LayerState& ls, const StepCtx& ctx) const override {
@@ -409,6 +413,7 @@ class IzhikevichModel : public Model {
             ls.var("post trace")->df(), ls.var("time since spike")->di(), ls.var("a")->df(),
             ls.var("b")->df(), ls.var("c")->df(), ls.var("d")->df());
         SG_LAUNCH_CHECK();
+        ctx.count();
     }
 
     bool learns(const Connection& c) const override { return true; }
@@ -438,6 +443,7 @@ class IzhikevichModel : public Model {
         if (sub) { SG_IZ_LEARN(true); } else { SG_IZ_LEARN(false); }
 #undef SG_IZ_LEARN
         SG_LAUNCH_CHECK();
+        ctx.count();
     }
 };
 SG_REGISTER_MODEL(IzhikevichModel);

@@ -25,7 +25,11 @@ struct ConnState;
 // Per-step launch context handed to model kernels.
 struct StepCtx {
     cudaStream_t stream;
-    bool last_step;          // the step whose input registers stay observable
+    bool last_step;                        // input registers stay observable after it
+    const std::vector<int>* layer_io;      // per layer: bit 0 input module, bit 1 output
+    long* launches;                        // kernel launch counter
+    bool is_input(const Layer& l) const { return layer_io && ((*layer_io)[l.index] & 1); }
+    void count(long n = 1) const { if (launches) *launches += n; }
 };
 
 class Model {
@@ -43,6 +47,11 @@ class Model {
 
     // Synaptic input of one incoming connection (default: base activator).
     virtual void activate(State& st, ConnState& cs, const StepCtx& ctx) const;
+    // True when the model's update computes this connection's input itself
+    // (fused kernel); the engine then skips activate() for it.
+    virtual bool fuses_input(State& st, const Connection& c, const StepCtx& ctx) const {
+        return false;
+    }
     // Neuron update of one layer.
     virtual void update(State& st, LayerState& ls, const StepCtx& ctx) const = 0;
     // Whether a plastic connection into this model has an updater.

@@ -45,6 +45,30 @@ DGeom make_geom(const Connection& c) {
     g.tk_cols = s.tc1 - s.tc0;
     g.tk_size = s.to_size();
     g.n_dest = c.dest_count();
+    // Range of source coordinates before wrapping, per axis.
+    g.wrap_fast = 0;
+    if (c.type == CONVERGENT || c.type == DIVERGENT) {
+        auto range = [&](int to_n, int stride, int spacing, int offset, int field, int from_n) {
+            long lo = 1L << 40, hi = -(1L << 40);
+            for (int t = 0; t < to_n; ++t) {
+                long a, b;
+                if (c.type == CONVERGENT) {
+                    a = (long)t * stride + (long)spacing * offset;
+                    b = a + (long)(field - 1) * spacing;
+                } else {
+                    a = (t + spacing * (-offset - field + stride)) / stride;
+                    b = a + (spacing * (field - stride) / stride);
+                }
+                lo = std::min(lo, a);
+                hi = std::max(hi, b);
+            }
+            return lo >= -(long)from_n && hi < 2L * from_n;
+        };
+        g.wrap_fast = range(c.to->rows, a.row_stride, a.row_spacing, a.row_offset, a.row_field,
+                            c.from->rows) &&
+                      range(c.to->cols, a.col_stride, a.col_spacing, a.col_offset, a.col_field,
+                            c.from->cols);
+    }
     return g;
 }
 
@@ -136,7 +160,7 @@ void State::to_device(cudaStream_t stream) {
     if (!arena_) allocate_device();
     if (!on_host_) return;
     for (auto& a : arrays_) {
-        if (a->dev_count == 0) continue;
+        if (a->dev_count == 0 || a->scratch) continue;
         const uint32_t* src = a->host.data();
         if (needs_transpose(*a)) {
             scratch_.resize(a->count);
@@ -156,7 +180,7 @@ void State::to_host(cudaStream_t stream) {
     if (on_host_) return;
     SG_CUDA(cudaStreamSynchronize(stream));
     for (auto& a : arrays_) {
-        if (a->dev_count == 0) continue;
+        if (a->dev_count == 0 || a->scratch) continue;
         size_t n = std::min(a->dev_count, a->count);
         if (needs_transpose(*a)) {
             scratch_.resize(a->count);

@@ -36,6 +36,7 @@ struct Array {
     std::vector<uint32_t> host;
     void* dev = nullptr;
     size_t dev_offset = 0;
+    bool scratch = false;    // device-only working buffer: never uploaded or downloaded
 
     float* hf() { return reinterpret_cast<float*>(host.data()); }
     int32_t* hi() { return reinterpret_cast<int32_t*>(host.data()); }
@@ -50,7 +51,8 @@ struct LayerState {
     Array* input = nullptr;
     Array* output = nullptr;
     std::map<std::string, Array*> vars;
-    std::map<std::string, float> params;   // model scalars (e.g. game_of_life rules)
+    std::map<std::string, Array*> internal;   // model buffers not exposed by the getters
+    std::map<std::string, float> params;      // model scalars (e.g. game_of_life rules)
     Array* var(const std::string& k) const;
 };
 

@@ -28,6 +28,9 @@ struct DGeom {
     int rf, cf, rs, cs, rsp, csp, ro, co, wrap;
     int fr0, fr1, fc0, fc1, tr0, tc0, tk_cols, tk_size;
     int n_dest;
+    // Every wrapped source coordinate lies in [-n, 2n): one conditional add or
+    // subtract gives the same result as ((x % n) + n) % n.
+    int wrap_fast;
 };
 
 enum { T_FC = 0, T_SUBSET = 1, T_ONE = 2, T_CONV = 3, T_DIV = 4 };
@@ -66,6 +69,11 @@ __device__ __forceinline__ float aggregate(float prior, float input, int opcode)
 
 __device__ __forceinline__ int wrap_idx(int x, int n) { return (x % n + n) % n; }
 
+__device__ __forceinline__ int wrap_coord(const DGeom& g, int x, int n) {
+    if (g.wrap_fast) return x < 0 ? x + n : (x >= n ? x - n : x);
+    return wrap_idx(x, n);
+}
+
 // Destination index of iteration d (subset iterates its window only).
 template <int TYPE>
 __device__ __forceinline__ int dest_of(const DGeom& g, int d) {
@@ -94,11 +102,11 @@ __device__ __forceinline__ void for_each_source(const DGeom& g, int d, F&& f) {
         for (int kr = 0; kr < g.rf; ++kr) {
             int fr = s_row + kr * g.rsp;
             bool row_ok = true;
-            if (g.wrap) fr = wrap_idx(fr, g.from_rows);
+            if (g.wrap) fr = wrap_coord(g, fr, g.from_rows);
             else row_ok = fr >= 0 && fr < g.from_rows;
             for (int kc = 0; kc < g.cf; ++kc, ++k) {
                 int fc = s_col + kc * g.csp;
-                if (g.wrap) fc = wrap_idx(fc, g.from_cols);
+                if (g.wrap) fc = wrap_coord(g, fc, g.from_cols);
                 else if (!row_ok || fc < 0 || fc >= g.from_cols) continue;
                 f(fr * g.from_cols + fc, g.conv ? k : k * g.to_size + d);
             }
@@ -113,11 +121,11 @@ __device__ __forceinline__ void for_each_source(const DGeom& g, int d, F&& f) {
         for (int sr = sr0; sr <= sr1; sr += g.rsp) {
             int fr = sr;
             bool row_ok = true;
-            if (g.wrap) fr = wrap_idx(fr, g.from_rows);
+            if (g.wrap) fr = wrap_coord(g, fr, g.from_rows);
             else row_ok = fr >= 0 && fr < g.from_rows;
             for (int sc = sc0; sc <= sc1; sc += g.csp, ++k) {
                 int fc = sc;
-                if (g.wrap) fc = wrap_idx(fc, g.from_cols);
+                if (g.wrap) fc = wrap_coord(g, fc, g.from_cols);
                 else if (!row_ok || fc < 0 || fc >= g.from_cols) continue;
                 f(fr * g.from_cols + fc, g.conv ? k : k * g.to_size + d);
             }

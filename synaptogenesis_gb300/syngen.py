@@ -146,6 +146,15 @@ def _load_library(path=None):
     if hasattr(lib, "sg_last_error"):
         lib.sg_last_error.restype = c_char_p
         lib.sg_set_seed.argtypes = (c_ulonglong,)
+        lib.sg_engine_create.argtypes = (c_void_p, c_void_p, c_void_p, c_void_p)
+        lib.sg_engine_create.restype = c_void_p
+        lib.sg_engine_step.argtypes = (c_void_p, c_longlong)
+        lib.sg_engine_step.restype = c_longlong
+        lib.sg_engine_stream.argtypes = (c_void_p,)
+        lib.sg_engine_stream.restype = c_void_p
+        lib.sg_engine_report.argtypes = (c_void_p,)
+        lib.sg_engine_report.restype = c_void_p
+        lib.sg_engine_destroy.argtypes = (c_void_p,)
     return lib, path
 
 
@@ -454,6 +463,48 @@ class Network:
         if report is None:
             print("Failed to run network!", last_error())
         return Properties(report)
+
+
+class Engine:
+    """A run that stays open: step it repeatedly on the same state (GB300
+    library extension, sg_engine_* in include/syngen.h)."""
+
+    def __init__(self, network, environment=None, args=None):
+        if network.state is None:
+            network.build_state()
+        self.network = network
+        self.environment = environment if isinstance(environment, Environment) else \
+            Environment(environment or {"modules": []})
+        self.args = args if isinstance(args, Properties) else Properties(args or {})
+        self.obj = _syn.sg_engine_create(network.obj, self.environment.obj, network.state,
+                                         self.args.obj)
+        if not self.obj:
+            raise RuntimeError("engine creation failed: " + last_error())
+
+    def step(self, n):
+        done = _syn.sg_engine_step(self.obj, int(n))
+        if done < 0:
+            raise RuntimeError("engine step failed: " + last_error())
+        return done
+
+    @property
+    def stream(self):
+        """cudaStream_t (as an int) that every kernel of this engine runs on."""
+        return _syn.sg_engine_stream(self.obj)
+
+    def report(self):
+        return Properties(_syn.sg_engine_report(self.obj))
+
+    def close(self):
+        if self.obj:
+            _syn.sg_engine_destroy(self.obj)
+            self.obj = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def fill_in(defaults, props):

@@ -123,8 +123,30 @@ def run_library(case, syngen, steps=None):
     return out
 
 
-def compare(got, want, steps=None, tol=None, float_keys=()):
-    """Bit-exact comparison; keys matching ``float_keys`` use relative tolerance ``tol``."""
+FLOAT_MODELS = ("relay", "rate_encoding")
+INT_KEYS = ("output", "time since spike", "delays")
+
+
+def float_like_keys(case):
+    """Result keys holding fp32 values (where any NaN payload counts as equal:
+    x86, Arm and the GPU produce different default NaNs)."""
+    models = {l["name"]: l["neural model"] for st in case.net["structures"] for l in st["layers"]}
+    keys = set()
+    for s, l in case.record:
+        if models[l] in FLOAT_MODELS:
+            keys.add("rec/%s/%s" % (s, l))
+    for key in case.final:
+        if key[0] == "neuron":
+            if key[3] not in INT_KEYS or (key[3] == "output" and models[key[2]] in FLOAT_MODELS):
+                keys.add("neuron/%s/%s/%s" % key[1:])
+        elif key[2] not in INT_KEYS:
+            keys.add("matrix/%s/%s" % key[1:])
+    return keys
+
+
+def compare(got, want, steps=None, tol=None, float_keys=(), nan_keys=()):
+    """Bit-exact comparison; keys matching ``float_keys`` use relative tolerance
+    ``tol``; in ``nan_keys`` two NaNs match whatever their payload."""
     problems = []
     for k, w in want.items():
         if k not in got:
@@ -138,9 +160,11 @@ def compare(got, want, steps=None, tol=None, float_keys=()):
             continue
         if tol is not None and any(f in k for f in float_keys):
             gf, wf = g.view(np.float32), w.view(np.float32)
-            bad = ~np.isclose(gf, wf, rtol=tol, atol=tol)
+            bad = ~np.isclose(gf, wf, rtol=tol, atol=tol, equal_nan=True)
         else:
             bad = g != w
+            if k in nan_keys:
+                bad &= ~(np.isnan(g.view(np.float32)) & np.isnan(w.view(np.float32)))
         if bad.any():
             idx = np.argwhere(bad)[0]
             problems.append("%s: %d mismatches, first at %s got %r want %r"

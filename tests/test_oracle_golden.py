@@ -7,10 +7,11 @@ same injected inputs.
 import pytest
 
 from tests.golden.cases import CASES
-from tests.harness import compare, load_fixture, run_oracle
+from tests.harness import compare, float_like_keys, load_fixture, run_oracle
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_oracle_matches_reference_fixture(name):
-    problems = compare(run_oracle(CASES[name]), load_fixture(name))
+    problems = compare(run_oracle(CASES[name]), load_fixture(name),
+                       nan_keys=float_like_keys(CASES[name]))
     assert not problems, problems
