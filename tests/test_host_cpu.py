@@ -1,0 +1,184 @@
+"""CPU tests of the library's host side (no GPU needed: device memory is only
+allocated when a run starts).
+
+* the C-ABI library loads and exports every function include/syngen.h declares;
+* building a state reproduces the oracle's initial state exactly (Izhikevich
+  resting state, distance-based delays, short-term-plasticity defaults, ...);
+* schema quirks and error behaviour of the reference;
+* JSON, property and state round trips.
+"""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def sg():
+    from synaptogenesis_gb300 import build
+    build.build()
+    from synaptogenesis_gb300 import syngen
+    syngen.set_warnings(False)
+    return syngen
+
+
+def header_functions():
+    text = open(os.path.join(ROOT, "include", "syngen.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^[A-Za-z_][\w\s\*]*?\b(\w+)\s*\([^;]*\)\s*;", text, flags=re.M)
+    return sorted(set(n for n in names if n not in ("if", "while")))
+
+
+def test_library_exports_every_header_function(sg):
+    lib = ctypes.CDLL(sg.LIB_PATH)
+    names = header_functions()
+    assert len(names) >= 60
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+@pytest.mark.parametrize("name", ["iz_opcodes", "iz_plastic", "base_all_types", "iz_c0_8",
+                                  "gol_two_word_history"])
+def test_initial_state_matches_oracle(sg, name):
+    from oracle.oracle import OracleNetwork
+    from tests.golden.cases import CASES
+    case = CASES[name]
+    net = sg.Network(case.net)
+    net.build_state()
+    assert net.state, sg.last_error()
+    onet = OracleNetwork(case.net)
+    for l in onet.layers:
+        for k, v in onet.neuron[l].items():
+            got = net.get_neuron_data(l.structure, l.name, k).to_np_array()
+            assert np.array_equal(got.view(np.uint32), v.view(np.uint32)), (l.name, k)
+    for c in onet.conns:
+        for k, v in onet.matrix[c].items():
+            got = net.get_weight_matrix(c.name, k).to_np_array()
+            assert got.size == v.size or k == "time since spike", (c.name, k)
+            if k != "weights":
+                assert np.array_equal(got.view(np.uint32)[:v.size], v.view(np.uint32)), (c.name, k)
+
+
+def test_column_offset_quirk_and_weight_counts(sg):
+    from oracle.oracle import OracleNetwork
+    net = {"structures": [{"name": "s", "layers": [
+        {"name": "a", "neural model": "relay", "rows": 7, "columns": 9},
+        {"name": "b", "neural model": "relay", "rows": 5, "columns": 6}]}],
+        "connections": [
+            {"name": "co", "from layer": "a", "to layer": "b", "type": "convergent",
+             "arborized config": {"row field size": 3, "column field size": 2,
+                                  "column offset": -3, "stride": 1}},
+            {"name": "dv", "from layer": "b", "to layer": "a", "type": "divergent",
+             "arborized config": {"field size": 3, "stride": 2}},
+            {"name": "ss", "from layer": "a", "to layer": "b", "type": "subset",
+             "subset config": {"from row start": 1, "from row end": 4, "from column start": 0,
+                               "from column end": 2, "to row start": 2, "to row end": 5,
+                               "to column start": 3, "to column end": 6}}]}
+    n = sg.Network(net)
+    n.build_state()
+    o = OracleNetwork(net)
+    for c in o.conns:
+        assert n.get_weight_matrix(c.name).size == c.num_weights
+    # "column offset" alone is ignored (read from "row offset"): it is 0, not -3.
+    assert o.connection("co").c.col_offset == 0
+
+
+@pytest.mark.parametrize("bad", [
+    {"structures": [{"name": "s", "layers": [{"name": "a", "neural model": "nope", "rows": 2, "columns": 2}]}]},
+    {"structures": [{"name": "s", "layers": [{"name": "a", "neural model": "relay", "rows": 0, "columns": 2}]}]},
+    {"structures": [{"name": "s", "layers": [
+        {"name": "a", "neural model": "relay", "rows": 2, "columns": 2},
+        {"name": "b", "neural model": "relay", "rows": 3, "columns": 2}]}],
+     "connections": [{"from layer": "a", "to layer": "b", "type": "one to one"}]},
+    {"structures": [{"name": "s", "layers": [
+        {"name": "a", "neural model": "relay", "rows": 2, "columns": 2}]}],
+     "connections": [{"from layer": "a", "to layer": "a", "type": "convergent"}]},
+])
+def test_invalid_networks_fail_like_the_reference(sg, bad):
+    n = sg.Network(bad)
+    assert n.obj is None          # create_network returns nullptr
+    assert sg.last_error()
+
+
+def test_izhikevich_gap_must_be_self_connection(sg):
+    net = {"structures": [{"name": "s", "layers": [
+        {"name": "a", "neural model": "izhikevich", "rows": 2, "columns": 2},
+        {"name": "b", "neural model": "izhikevich", "rows": 2, "columns": 2}]}],
+        "connections": [{"from layer": "a", "to layer": "b", "opcode": "gap"}]}
+    n = sg.Network(net)
+    n.build_state()
+    assert n.state is None and "Gap junctions" in sg.last_error()
+
+
+def test_large_distance_delays_are_rejected(sg):
+    net = {"structures": [{"name": "s", "layers": [
+        {"name": "a", "neural model": "izhikevich", "rows": 64, "columns": 64},
+        {"name": "b", "neural model": "izhikevich", "rows": 64, "columns": 64}]}],
+        "connections": [{"from layer": "a", "to layer": "b", "plastic": False}]}
+    n = sg.Network(net)
+    n.build_state()
+    assert n.state is None and "delays cannot be greater than 31" in sg.last_error()
+
+
+def test_weight_and_delay_callbacks(sg):
+    seen = {}
+
+    def wcb(ID, size, ptr):
+        arr = sg.FloatArray(size, ptr).to_np_array()
+        arr[:] = np.arange(size, dtype=np.float32) * (ID + 1)
+        seen["w"] = size
+
+    def dcb(ID, size, weights, delays):
+        sg.IntArray(size, delays).to_np_array()[:] = np.arange(size) % 7
+        seen["d"] = size
+
+    sg.create_weight_callback("t_w", wcb)
+    sg.create_delay_weight_callback("t_d", dcb)
+    net = {"structures": [{"name": "s", "layers": [
+        {"name": "a", "neural model": "relay", "rows": 3, "columns": 3},
+        {"name": "b", "neural model": "izhikevich", "rows": 3, "columns": 3}]}],
+        "connections": [{"name": "c", "from layer": "a", "to layer": "b",
+                         "weight config": {"type": "flat", "weight": 0.5, "callback": "t_w",
+                                           "delay callback": "t_d", "id": 1}}]}
+    n = sg.Network(net)
+    n.build_state()
+    w = n.get_weight_matrix("c").to_np_array()
+    assert np.array_equal(w, np.arange(81, dtype=np.float32) * 2)
+    assert np.array_equal(n.get_weight_matrix("c", "delays").to_np_array(), np.arange(81) % 7)
+    assert seen == {"w": 81, "d": 81}
+
+
+def test_properties_and_json_roundtrip(sg, tmp_path):
+    from tests.golden.cases import CASES
+    net_dict = CASES["iz_opcodes"].net
+    n = sg.Network(net_dict)
+    path = str(tmp_path / "net.json")
+    assert n.save(path)
+    n2 = sg.Network(path)
+    assert n2.obj
+    n2.build_state()
+    assert n2.get_weight_matrix("o_gap").size == 36 * 36
+    p = sg.Properties({"a": "1", "b": True, "c": {"d": "x"}, "e": ["p", "q"], "f": [{"g": "h"}]})
+    q = sg.Properties(p.obj).to_dict()
+    assert q == {"a": "1", "b": "true", "c": {"d": "x"}, "e": ["p", "q"], "f": [{"g": "h"}]}
+
+
+def test_state_save_load_roundtrip(sg, tmp_path):
+    from tests.golden.cases import CASES
+    net_dict = CASES["iz_plastic"].net
+    n = sg.Network(net_dict)
+    n.build_state()
+    v = n.get_neuron_data("s", "e", "voltage").to_np_array()
+    v[:] = np.linspace(-70, -50, v.size, dtype=np.float32)
+    w = n.get_weight_matrix("p_ee").to_np_array()
+    w[:] = np.random.default_rng(0).random(w.size).astype(np.float32)
+    path = str(tmp_path / "state.bin")
+    n.save_state(path)
+    m = sg.Network(net_dict)
+    m.build_state(path)
+    assert np.array_equal(m.get_neuron_data("s", "e", "voltage").to_np_array(), v)
+    assert np.array_equal(m.get_weight_matrix("p_ee").to_np_array(), w)
