@@ -150,6 +150,34 @@ void sg_set_seed(unsigned long long seed);
 /* ABI version of this header. */
 int sg_version(void);
 
+/* Allocation-free game_of_life stepping.  No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc: a host program whose device memory
+ * belongs to another allocator, or a loop that must not allocate between steps.
+ * Advances `steps` timesteps of a toroidal game_of_life board held in the
+ * caller's device buffers, with the semantics of a game_of_life layer whose only
+ * input is its own convergent, convolutional, wrapping "add" connection
+ * (field x field weights, stride 1, spacing 1, offset -field/2, delay 0):
+ *   words      device, rows*cols output-history words, updated in place
+ *   input_out  device, rows*cols floats receiving the last step's input
+ *              register (the weighted neighbour count), or NULL
+ *   weights    device, field*field floats (row-major kernel)
+ *   stream     cudaStream_t to launch on (NULL: the default stream)
+ * Allocates nothing: its only working memory is a static device array of
+ * SG_GOL_NOALLOC_MAX_CELLS words that every GPU loading the library holds until
+ * exit.  Boards larger than that are rejected (SG_NOALLOC_ETOOBIG).  The first
+ * call on a device looks up that array's device address; make that first call
+ * before any stream capture.  All calls share the array, so calls that overlap
+ * on the GPU race.  Returns 0, or a negative SG_NOALLOC_* code.  The work is
+ * asynchronous on `stream`. */
+#define SG_GOL_NOALLOC_MAX_CELLS (1 << 20)
+#define SG_NOALLOC_EINVAL (-1)
+#define SG_NOALLOC_ETOOBIG (-2)
+#define SG_NOALLOC_ECUDA (-3)
+int sg_gol_steps_noalloc(unsigned int* words, float* input_out, int rows, int cols,
+                         const float* weights, int field, int steps, int survival_min,
+                         int survival_max, int birth_min, int birth_max, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
