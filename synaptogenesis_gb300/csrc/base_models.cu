@@ -147,6 +147,127 @@ __global__ void __launch_bounds__(256) k_gol_fused(DGeom g, int delay, const uin
     next[d] = (word >> 1) | ((live ? 1u : 0u) << 31);
 }
 
+// Bit-sliced game_of_life step (same semantics as k_gol_fused) for a 3x3
+// kernel whose weights are all 0 or 1, stride 1, spacing 1, offset -1, and
+// rows of whole 32-cell segments.  With 0/1 weights the reference's fp32
+// sequential sum is an exact integer count, so counting bits is exact.
+// One thread owns one 32-cell segment of one row:
+//   * gathers bit (31 - delay) of its 32 history words (128-bit loads) into a
+//     plane word, for the rows above, itself and below, plus the boundary bits
+//     of the neighbouring segments (west / east shifts, wrap or zero);
+//   * adds the planes selected by the weight mask with a bit-sliced counter
+//     (c3 c2 c1 c0 per cell);
+//   * evaluates survival / birth as plane logic against bit 0 (the state 32
+//     steps back);
+//   * shifts the new bit into its 32 words and stores them.
+__device__ __forceinline__ uint32_t newest_bit(uint32_t w, int delay) { return (w << delay) >> 31; }
+
+__device__ __forceinline__ void csa_add(uint32_t& c0, uint32_t& c1, uint32_t& c2, uint32_t& c3,
+                                        uint32_t x) {
+    uint32_t t = c0 & x; c0 ^= x; x = t;
+    t = c1 & x; c1 ^= x; x = t;
+    t = c2 & x; c2 ^= x; x = t;
+    c3 ^= x;
+}
+
+__global__ void __launch_bounds__(256) k_gol_bits(int rows, int cols, int wrap, int delay,
+                                                  unsigned mask9, const uint32_t* __restrict__ cur,
+                                                  uint32_t* __restrict__ next,
+                                                  float* __restrict__ input_out, unsigned smask,
+                                                  unsigned bmask) {
+    const int segs = cols >> 5;
+    int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= rows * segs) return;
+    const int r = gid / segs, s = gid - r * segs;
+    uint32_t N[3], W[3], E[3];
+    uint4 own[8];
+    uint32_t O = 0;
+#pragma unroll
+    for (int dr = 0; dr < 3; ++dr) {
+        int rr = r + dr - 1;
+        bool valid = true;
+        if (wrap) rr = rr < 0 ? rr + rows : (rr >= rows ? rr - rows : rr);
+        else valid = rr >= 0 && rr < rows;
+        uint32_t P = 0, wb = 0, eb = 0;
+        if (valid) {
+            const uint32_t* row = cur + (size_t)rr * cols;
+            const uint4* p = reinterpret_cast<const uint4*>(row + (s << 5));
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                uint4 v = __ldg(p + q);
+                P |= (newest_bit(v.x, delay) << (4 * q)) | (newest_bit(v.y, delay) << (4 * q + 1)) |
+                     (newest_bit(v.z, delay) << (4 * q + 2)) | (newest_bit(v.w, delay) << (4 * q + 3));
+                if (dr == 1) {
+                    own[q] = v;
+                    O |= ((v.x & 1u) << (4 * q)) | ((v.y & 1u) << (4 * q + 1)) |
+                         ((v.z & 1u) << (4 * q + 2)) | ((v.w & 1u) << (4 * q + 3));
+                }
+            }
+            int cl = (s << 5) - 1, ce = (s << 5) + 32;
+            if (wrap) {
+                cl = cl < 0 ? cols - 1 : cl;
+                ce = ce >= cols ? 0 : ce;
+                wb = newest_bit(__ldg(row + cl), delay);
+                eb = newest_bit(__ldg(row + ce), delay);
+            } else {
+                wb = cl >= 0 ? newest_bit(__ldg(row + cl), delay) : 0u;
+                eb = ce < cols ? newest_bit(__ldg(row + ce), delay) : 0u;
+            }
+        }
+        N[dr] = P;
+        W[dr] = (P << 1) | wb;         // bit i: cell i-1 (kernel column 0)
+        E[dr] = (P >> 1) | (eb << 31); // bit i: cell i+1 (kernel column 2)
+    }
+    uint32_t c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+#pragma unroll
+    for (int kr = 0; kr < 3; ++kr) {
+        if (mask9 & (1u << (kr * 3 + 0))) csa_add(c0, c1, c2, c3, W[kr]);
+        if (mask9 & (1u << (kr * 3 + 1))) csa_add(c0, c1, c2, c3, N[kr]);
+        if (mask9 & (1u << (kr * 3 + 2))) csa_add(c0, c1, c2, c3, E[kr]);
+    }
+    uint32_t S = 0, B = 0;
+    for (int v = 0; v < 10; ++v) {
+        if (!(((smask | bmask) >> v) & 1u)) continue;
+        uint32_t e = ~((c0 ^ ((v & 1) ? ~0u : 0u)) | (c1 ^ ((v & 2) ? ~0u : 0u)) |
+                       (c2 ^ ((v & 4) ? ~0u : 0u)) | (c3 ^ ((v & 8) ? ~0u : 0u)));
+        if ((smask >> v) & 1u) S |= e;
+        if ((bmask >> v) & 1u) B |= e;
+    }
+    const uint32_t L = (O & S) | (~O & B);
+    uint4* out = reinterpret_cast<uint4*>(next + (size_t)r * cols + (s << 5));
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        uint4 v = own[q];
+        v.x = (v.x >> 1) | (((L >> (4 * q)) & 1u) << 31);
+        v.y = (v.y >> 1) | (((L >> (4 * q + 1)) & 1u) << 31);
+        v.z = (v.z >> 1) | (((L >> (4 * q + 2)) & 1u) << 31);
+        v.w = (v.w >> 1) | (((L >> (4 * q + 3)) & 1u) << 31);
+        out[q] = v;
+    }
+    if (input_out) {
+        float4* in = reinterpret_cast<float4*>(input_out + (size_t)r * cols + (s << 5));
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            float f[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                int i = 4 * q + k;
+                f[k] = (float)(((c0 >> i) & 1u) | (((c1 >> i) & 1u) << 1) | (((c2 >> i) & 1u) << 2) |
+                               (((c3 >> i) & 1u) << 3));
+            }
+            in[q] = make_float4(f[0], f[1], f[2], f[3]);
+        }
+    }
+}
+
+// Mask of counts in [lo, hi] (counts of a 3x3 kernel are 0..9).
+static unsigned count_mask(int lo, int hi) {
+    unsigned m = 0;
+    for (int v = 0; v < 10; ++v)
+        if (v >= lo && v <= hi) m |= 1u << v;
+    return m;
+}
+
 class RelayModel : public Model {
   public:
     const char* name() const override { return "relay"; }
@@ -206,6 +327,26 @@ class GameOfLifeModel : public Model {
     bool fuses_input(State&, const Connection& c, const StepCtx& ctx) const override {
         return fusable_shape(*c.to) && !ctx.is_input(*c.to);
     }
+    // After every upload: can the bit-sliced kernel run this layer?  (3x3
+    // convolutional kernel of 0/1 weights, stride and spacing 1, offset -1,
+    // whole 32-cell row segments.)
+    void prepare_device(State& st, ConnState& cs, cudaStream_t) const override {
+        const Connection& c = *cs.conn;
+        cs.params["bits mask"] = -1.0f;
+        if (!fusable_shape(*c.to) || !c.convolutional) return;
+        const Arbor& a = c.arbor;
+        if (a.row_field != 3 || a.col_field != 3 || a.row_stride != 1 || a.col_stride != 1 ||
+            a.row_spacing != 1 || a.col_spacing != 1 || a.row_offset != -1 || a.col_offset != -1 ||
+            c.to->cols % 32 != 0)
+            return;
+        const float* w = cs.weights->hf();
+        unsigned mask = 0;
+        for (int k = 0; k < 9; ++k) {
+            if (w[k] == 1.0f) mask |= 1u << k;
+            else if (!(w[k] == 0.0f && !std::signbit(w[k]))) return;
+        }
+        cs.params["bits mask"] = (float)mask;
+    }
     void update(State& st, LayerState& ls, const StepCtx& ctx) const override {
         const Layer& l = *ls.layer;
         int smin = (int)ls.params.at("smin"), smax = (int)ls.params.at("smax");
@@ -213,6 +354,19 @@ class GameOfLifeModel : public Model {
         if (fusable_shape(l) && !ctx.is_input(l)) {
             ConnState& cs = *st.conn_state(l.inputs[0]);
             Array* swap = ls.internal.at("output swap");
+            auto bm = cs.params.find("bits mask");
+            if (bm != cs.params.end() && bm->second >= 0.0f) {
+                int threads = l.rows * (l.cols / 32);
+                k_gol_bits<<<blocks_for(threads, 256), 256, 0, ctx.stream>>>(
+                    l.rows, l.cols, cs.conn->arbor.wrap ? 1 : 0, cs.conn->delay,
+                    (unsigned)bm->second, ls.output->du(), swap->du(),
+                    ctx.last_step ? ls.input->df() : nullptr, count_mask(smin, smax),
+                    count_mask(bmin, bmax));
+                SG_LAUNCH_CHECK();
+                std::swap(ls.output->dev, swap->dev);
+                ctx.count();
+                return;
+            }
             dim3 block(32, 8);
             dim3 grid(blocks_for(l.cols, 32), blocks_for(l.rows, 8));
             k_gol_fused<<<grid, block, 0, ctx.stream>>>(

@@ -15,15 +15,28 @@ def sg():
     return syngen
 
 
-def gol_net(rows, cols, field=3, **rule):
+def gol_net(rows, cols, field=3, wrap=True, delay=0, weight=1.0, diagonal=False, **rule):
     return {"structures": [{"name": "g", "type": "parallel", "layers": [
         dict({"name": "board", "neural model": "game_of_life", "rows": rows, "columns": cols},
              **rule)]}],
         "connections": [{"name": "nbr", "from layer": "board", "to layer": "board",
                          "type": "convergent", "convolutional": True, "plastic": False,
-                         "opcode": "add",
-                         "weight config": {"type": "flat", "weight": 1.0, "diagonal": False},
-                         "arborized config": {"field size": field, "wrap": True}}]}
+                         "opcode": "add", "delay": delay,
+                         "weight config": {"type": "flat", "weight": weight, "diagonal": diagonal},
+                         "arborized config": {"field size": field, "wrap": wrap}}]}
+
+
+@pytest.mark.parametrize("variant", [
+    dict(wrap=False), dict(delay=5), dict(diagonal=True, survival_min=3, survival_max=4),
+    dict(weight=2.0, survival_min=4, survival_max=6, birth_min=6, birth_max=6),
+    dict(wrap=False, delay=31, birth_min=2, birth_max=3)])
+def test_gol_kernel_variants_match_oracle(sg, variant):
+    """Bit-sliced path (0/1 weights) and its fallback (other weights)."""
+    rows, cols = 37, 128
+    words = np.random.default_rng(7).integers(0, 2**32, rows * cols, dtype=np.uint64).astype(np.uint32)
+    go, gi, oo, oi = run_both(sg, gol_net(rows, cols, **variant), words, [19, 22])
+    assert np.array_equal(go, oo)
+    assert np.array_equal(gi, oi)
 
 
 def run_both(sg, net_dict, words, chunks, graphs=True):
