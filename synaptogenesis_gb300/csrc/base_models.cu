@@ -260,6 +260,119 @@ __global__ void __launch_bounds__(256) k_gol_bits(int rows, int cols, int wrap, 
     }
 }
 
+// Coalesced variant of k_gol_bits.  A warp owns a strip of 32 segments
+// (1024 cells) and walks kGolRows rows down it, keeping a 3-row window of
+// planes.  Planes are gathered with one coalesced 128-byte load per segment
+// and __ballot_sync (lane t keeps the ballot of segment t); new words are
+// written back with coalesced stores, lane i writing cell i of each segment.
+constexpr int kGolRows = 4;
+
+struct GolPlanes { uint32_t n, w, e, o; };   // newest bit, west, east, bit 0
+
+__device__ __forceinline__ GolPlanes gol_gather(const uint32_t* __restrict__ cur, int rows, int cols,
+                                                int segs, int sx, int rr, int wrap, int delay,
+                                                bool bit0) {
+    const int lane = threadIdx.x & 31;
+    GolPlanes p{0u, 0u, 0u, 0u};
+    bool valid = true;
+    if (wrap) rr = rr < 0 ? rr + rows : (rr >= rows ? rr - rows : rr);
+    else valid = rr >= 0 && rr < rows;
+    if (!valid) return p;
+    const uint32_t* row = cur + (size_t)rr * cols;
+    const int seg = sx * 32 + lane;
+    uint32_t mine = 0, mine0 = 0;
+#pragma unroll 8
+    for (int t = 0; t < 32; ++t) {
+        int sg = sx * 32 + t;
+        uint32_t word = sg < segs ? __ldg(row + sg * 32 + lane) : 0u;
+        uint32_t b = __ballot_sync(0xffffffffu, newest_bit(word, delay));
+        if (lane == t) mine = b;
+        if (bit0) {
+            uint32_t b0 = __ballot_sync(0xffffffffu, word & 1u);
+            if (lane == t) mine0 = b0;
+        }
+    }
+    p.o = mine0;
+    uint32_t west = __shfl_up_sync(0xffffffffu, mine, 1) >> 31;
+    uint32_t east = __shfl_down_sync(0xffffffffu, mine, 1) & 1u;
+    if (seg < segs) {
+        if (lane == 0) {
+            int cl = seg * 32 - 1;
+            if (cl < 0) west = wrap ? newest_bit(__ldg(row + cols - 1), delay) : 0u;
+            else west = newest_bit(__ldg(row + cl), delay);
+        }
+        if (lane == 31 || seg + 1 >= segs) {
+            int ce = seg * 32 + 32;
+            if (ce >= cols) east = wrap ? newest_bit(__ldg(row), delay) : 0u;
+            else east = newest_bit(__ldg(row + ce), delay);
+        }
+    }
+    p.n = mine;
+    p.w = (mine << 1) | west;
+    p.e = (mine >> 1) | (east << 31);
+    return p;
+}
+
+__global__ void __launch_bounds__(256, 2) k_gol_bits_strip(int rows, int cols, int wrap, int delay,
+                                                        unsigned mask9, const uint32_t* __restrict__ cur,
+                                                        uint32_t* __restrict__ next,
+                                                        float* __restrict__ input_out, unsigned smask,
+                                                        unsigned bmask) {
+    const int segs = cols >> 5;
+    const int strips = (segs + 31) >> 5;
+    const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int sx = warp_id % strips;
+    const int r0 = (warp_id / strips) * kGolRows;
+    if (r0 >= rows) return;
+    const int r1 = min(rows, r0 + kGolRows);
+    GolPlanes up = gol_gather(cur, rows, cols, segs, sx, r0 - 1, wrap, delay, false);
+    GolPlanes mid = gol_gather(cur, rows, cols, segs, sx, r0, wrap, delay, true);
+    for (int r = r0; r < r1; ++r) {
+        GolPlanes down = gol_gather(cur, rows, cols, segs, sx, r + 1, wrap, delay, r + 1 < r1);
+        const uint32_t O = mid.o;
+        uint32_t c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+        auto add_row = [&](const GolPlanes& p, int kr) {
+            if (mask9 & (1u << (kr * 3 + 0))) csa_add(c0, c1, c2, c3, p.w);
+            if (mask9 & (1u << (kr * 3 + 1))) csa_add(c0, c1, c2, c3, p.n);
+            if (mask9 & (1u << (kr * 3 + 2))) csa_add(c0, c1, c2, c3, p.e);
+        };
+        add_row(up, 0);
+        add_row(mid, 1);
+        add_row(down, 2);
+        uint32_t S = 0, B = 0;
+        for (int v = 0; v < 10; ++v) {
+            if (!(((smask | bmask) >> v) & 1u)) continue;
+            uint32_t e = ~((c0 ^ ((v & 1) ? ~0u : 0u)) | (c1 ^ ((v & 2) ? ~0u : 0u)) |
+                           (c2 ^ ((v & 4) ? ~0u : 0u)) | (c3 ^ ((v & 8) ? ~0u : 0u)));
+            if ((smask >> v) & 1u) S |= e;
+            if ((bmask >> v) & 1u) B |= e;
+        }
+        const uint32_t L = (O & S) | (~O & B);
+        const uint32_t* src_row = cur + (size_t)r * cols;
+        uint32_t* dst_row = next + (size_t)r * cols;
+#pragma unroll 4
+        for (int t = 0; t < 32; ++t) {
+            int sg = sx * 32 + t;
+            uint32_t Lt = __shfl_sync(0xffffffffu, L, t);
+            if (sg < segs) {
+                uint32_t word = __ldg(src_row + sg * 32 + lane);
+                dst_row[sg * 32 + lane] = (word >> 1) | (((Lt >> lane) & 1u) << 31);
+            }
+            if (input_out) {
+                uint32_t a0 = __shfl_sync(0xffffffffu, c0, t), a1 = __shfl_sync(0xffffffffu, c1, t);
+                uint32_t a2 = __shfl_sync(0xffffffffu, c2, t), a3 = __shfl_sync(0xffffffffu, c3, t);
+                if (sg < segs)
+                    input_out[(size_t)r * cols + sg * 32 + lane] =
+                        (float)(((a0 >> lane) & 1u) | (((a1 >> lane) & 1u) << 1) |
+                                (((a2 >> lane) & 1u) << 2) | (((a3 >> lane) & 1u) << 3));
+            }
+        }
+        up = mid;
+        mid = down;
+    }
+}
+
 // Mask of counts in [lo, hi] (counts of a 3x3 kernel are 0..9).
 static unsigned count_mask(int lo, int hi) {
     unsigned m = 0;
@@ -356,8 +469,9 @@ class GameOfLifeModel : public Model {
             Array* swap = ls.internal.at("output swap");
             auto bm = cs.params.find("bits mask");
             if (bm != cs.params.end() && bm->second >= 0.0f) {
-                int threads = l.rows * (l.cols / 32);
-                k_gol_bits<<<blocks_for(threads, 256), 256, 0, ctx.stream>>>(
+                int strips = (l.cols / 32 + 31) / 32;
+                long threads = 32L * strips * ((l.rows + kGolRows - 1) / kGolRows);
+                k_gol_bits_strip<<<blocks_for(threads, 256), 256, 0, ctx.stream>>>(
                     l.rows, l.cols, cs.conn->arbor.wrap ? 1 : 0, cs.conn->delay,
                     (unsigned)bm->second, ls.output->du(), swap->du(),
                     ctx.last_step ? ls.input->df() : nullptr, count_mask(smin, smax),

@@ -4,6 +4,8 @@
 // term (IZ_* and STDP constants are double literals); the library is built
 // with --fmad=false so nothing is contracted.  powf(x, 2) is x * x, which is
 // what the reference's optimised build computes.
+#include <cuda_pipeline.h>
+
 #include <cmath>
 #include <cstdlib>
 #include <random>
@@ -75,6 +77,174 @@ __global__ void __launch_bounds__(128) k_iz_activate(
         int to = dest_of<TY>(g, d);
         short_cond[to] += short_sum;
         if (LONG) long_cond[to] += long_sum;
+    }
+}
+
+// Source index of matrix row `row` (FC: the source itself; subset: its window).
+template <bool SUBSET>
+__device__ __forceinline__ int row_source(const DGeom& g, int row) {
+    if (!SUBSET) return row;
+    int fkc = g.fc1 - g.fc0;
+    return (row / fkc + g.fr0) * g.from_cols + (row % fkc + g.fc0);
+}
+
+// Trace activator for fully connected and subset matrices, which have many
+// sources per destination and (in the device layout [source][destination])
+// rows of contiguous destinations.  One CTA owns 32 destination columns and
+// streams every source row through a 4-stage cp.async pipeline of 32-row
+// tiles (weights, short-term R and w, delays, short and long traces), so the
+// loads of later tiles are in flight while a tile is processed.  All 256
+// threads do the per-synapse work (one warp per row, one lane per column) and
+// write the decayed traces straight back; the pre-decay traces go to a
+// double-buffered shared tile from which one lane per column adds them in row
+// order, keeping the reference's sequential fp32 sum.  Needs ncols % 4 == 0.
+constexpr int kColsR = 32;       // rows per stage
+constexpr int kColsS = 4;        // stages
+
+template <int SR, bool LONG, bool SUBSET>
+__global__ void __launch_bounds__(256, 1) k_iz_activate_cols(
+    DGeom g, int nrows, int ncols, const uint32_t* __restrict__ src, const float* __restrict__ w,
+    const float* __restrict__ stp_r, const float* __restrict__ stp_w, const int* __restrict__ delays,
+    float* __restrict__ short_tr, float* __restrict__ long_tr, float gcond, float short_tau,
+    float long_tau, float* __restrict__ short_cond, float* __restrict__ long_cond) {
+    constexpr int R = kColsR, S = kColsS;
+    constexpr int HAS_D = SR == S_BIT ? 1 : 0;
+    constexpr int NA = 4 + HAS_D + (LONG ? 1 : 0);     // w, r, sw, [delay], st, [lt]
+    extern __shared__ float4 smem4[];
+    float* stage_mem = reinterpret_cast<float*>(smem4);
+    float* sums = stage_mem + S * NA * R * 32;         // [2 buffers][2 kinds][R][32]
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int col0 = blockIdx.x * 32;
+    const int col = col0 + lane;
+    const bool colok = col < ncols;
+    const int nchunks = (nrows + R - 1) / R;
+
+    auto src_array = [&](int a) -> const float* {
+        if (a == 0) return w;
+        if (a == 1) return stp_r;
+        if (a == 2) return stp_w;
+        if (HAS_D && a == 3) return reinterpret_cast<const float*>(delays);
+        if (a == 3 + HAS_D) return short_tr;
+        return long_tr;
+    };
+    auto issue = [&](int ch) {
+        if (ch < nchunks) {
+            float* st = stage_mem + (size_t)(ch % S) * NA * R * 32;
+            for (int e = tid; e < NA * R * 8; e += 256) {
+                int a = e / (R * 8), rem = e - a * (R * 8), j = rem >> 3, p = rem & 7;
+                int row = ch * R + j, c = col0 + p * 4;
+                if (row < nrows && c < ncols)
+                    __pipeline_memcpy_async(st + (a * R + j) * 32 + p * 4,
+                                            src_array(a) + (size_t)row * ncols + c, 16);
+            }
+        }
+        __pipeline_commit();
+    };
+
+    float short_sum = 0.0f, long_sum = 0.0f;
+    auto consume = [&](int ch) {
+        int nr = min(R, nrows - ch * R);
+        const float* sb = sums + (ch & 1) * 2 * R * 32;
+        if (warp == 0)
+            for (int j = 0; j < nr; ++j) short_sum += sb[j * 32 + lane];
+        else if (LONG && warp == 1)
+            for (int j = 0; j < nr; ++j) long_sum += sb[R * 32 + j * 32 + lane];
+    };
+
+    for (int s = 0; s < S - 1; ++s) issue(s);
+    for (int ch = 0; ch < nchunks; ++ch) {
+        __pipeline_wait_prior(S - 2);
+        __syncthreads();
+        issue(ch + S - 1);
+        if (ch > 0) consume(ch - 1);
+        const float* st = stage_mem + (size_t)(ch % S) * NA * R * 32;
+        float* sb = sums + (ch & 1) * 2 * R * 32;
+#pragma unroll
+        for (int i = 0; i < R / 8; ++i) {
+            int j = warp + 8 * i;
+            int row = ch * R + j;
+            float st_pre = 0.0f, lt_pre = 0.0f;
+            if (row < nrows && colok) {
+                int o = j * 32 + lane;
+                uint32_t word = __ldg(src + row_source<SUBSET>(g, row));
+                int delay = HAS_D ? __float_as_int(st[3 * R * 32 + o]) : 0;
+                float spike = extract<SR>(word, delay);
+                float weight = st[o] * (st[R * 32 + o] * st[2 * R * 32 + o]);
+                st_pre = st[(3 + HAS_D) * R * 32 + o] + (spike * weight * gcond);
+                size_t gi = (size_t)row * ncols + col;
+                short_tr[gi] = st_pre * short_tau;
+                if (LONG) {
+                    lt_pre = st[(4 + HAS_D) * R * 32 + o] + (spike * weight * gcond);
+                    long_tr[gi] = lt_pre * long_tau;
+                }
+            }
+            sb[j * 32 + lane] = st_pre;
+            if (LONG) sb[R * 32 + j * 32 + lane] = lt_pre;
+        }
+    }
+    __syncthreads();
+    if (nchunks > 0) consume(nchunks - 1);
+    if (colok) {
+        int to = dest_of<SUBSET ? T_SUBSET : T_FC>(g, col);
+        if (warp == 0) short_cond[to] += short_sum;
+        if (LONG && warp == 1) long_cond[to] += long_sum;
+    }
+}
+
+template <int SR, bool LONG, bool SUBSET>
+size_t iz_cols_smem() {
+    constexpr int NA = 4 + (SR == S_BIT ? 1 : 0) + (LONG ? 1 : 0);
+    return (size_t)(kColsS * NA * kColsR * 32 + 2 * 2 * kColsR * 32) * sizeof(float);
+}
+
+// Rows (sources) and columns (destinations) of a fully connected or subset
+// matrix in the device layout; false for the other connection types.
+static bool matrix_shape(const Connection& c, int& nrows, int& ncols) {
+    if (c.type == FULLY_CONNECTED) {
+        nrows = c.from->size;
+        ncols = c.to->size;
+        return true;
+    }
+    if (c.type == SUBSET) {
+        nrows = c.subset.from_size();
+        ncols = c.subset.to_size();
+        return true;
+    }
+    return false;
+}
+
+struct IzColsArgs {
+    DGeom g;
+    int nrows, ncols;
+    const uint32_t* src;
+    const float *w, *stp_r, *stp_w;
+    const int* delays;
+    float *short_tr, *long_tr;
+    float gcond, short_tau, long_tau;
+    float *short_cond, *long_cond;
+};
+
+template <int SR, bool LONG, bool SUBSET>
+static void launch_cols_t(const IzColsArgs& a, cudaStream_t s) {
+    static bool configured = false;
+    size_t smem = iz_cols_smem<SR, LONG, SUBSET>();
+    if (!configured) {
+        SG_CUDA(cudaFuncSetAttribute(k_iz_activate_cols<SR, LONG, SUBSET>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = true;
+    }
+    k_iz_activate_cols<SR, LONG, SUBSET><<<blocks_for(a.ncols, 32), 256, smem, s>>>(
+        a.g, a.nrows, a.ncols, a.src, a.w, a.stp_r, a.stp_w, a.delays, a.short_tr, a.long_tr,
+        a.gcond, a.short_tau, a.long_tau, a.short_cond, a.long_cond);
+    SG_LAUNCH_CHECK();
+}
+
+template <int SR>
+static void launch_cols(const IzColsArgs& a, bool long_trace, bool subset, cudaStream_t s) {
+    if (long_trace) {
+        if (subset) launch_cols_t<SR, true, true>(a, s); else launch_cols_t<SR, true, false>(a, s);
+    } else {
+        if (subset) launch_cols_t<SR, false, true>(a, s); else launch_cols_t<SR, false, false>(a, s);
     }
 }
 
@@ -214,6 +384,56 @@ __global__ void __launch_bounds__(128) k_iz_learn(
             }
         }
     });
+}
+
+// Updater for fully connected and subset matrices: every synapse is
+// independent, so a 2-D grid covers (column tile, row block); each thread
+// keeps its destination's activity in registers and walks a block of source
+// rows (coalesced along the destination axis).
+template <int SR, bool SUB, bool SUBSET>
+__global__ void __launch_bounds__(256) k_iz_learn_2d(
+    DGeom g, int nrows, int ncols, int rows_per_block, const uint32_t* __restrict__ dest_out,
+    const float* __restrict__ to_exc, const int* __restrict__ to_tss,
+    const int* __restrict__ from_tss, float lr, int stp_flag, float max_weight,
+    float* __restrict__ w, float* __restrict__ presyn, float* __restrict__ wd,
+    float* __restrict__ stp_r, float* __restrict__ stp_w, IzLut lut) {
+    int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= ncols) return;
+    const double U = SUB ? 0.2 : 0.5;
+    const int F = SUB ? 20 : 1000;
+    const int D = SUB ? 700 : 800;
+    int to = dest_of<SUBSET ? T_SUBSET : T_FC>(g, col);
+    float dest_exc_trace = to_exc[to];
+    int dest_tss = to_tss[to];
+    float dest_spike = extract<SR>(dest_out[to], 0);
+    int r0 = blockIdx.y * rows_per_block, r1 = min(nrows, r0 + rows_per_block);
+    for (int row = r0; row < r1; ++row) {
+        size_t wi = (size_t)row * ncols + col;
+        float weight = w[wi];
+        if (weight >= 0.0001f) {
+            int src_tss = __ldg(from_tss + row_source<SUBSET>(g, row));
+            bool src_spike = src_tss == 0;
+            float src_trace, dest_trace;
+            if (!SUB) {
+                src_trace = (presyn[wi] = src_spike ? 0.004 : presyn[wi] * 0.933);
+                dest_trace = dest_exc_trace;
+            } else {
+                src_trace = (dest_spike > 0.0f && src_tss > 0 && src_tss < 32) ? lut.src[src_tss] : 0.0f;
+                dest_trace = (src_spike && dest_tss > 0 && dest_tss < 32) ? lut.dst[dest_tss] : 0.0f;
+            }
+            float weight_delta = wd[wi];
+            weight_delta = wd[wi] -= (weight_delta - 0.000001) * 0.0001 + (dest_spike * src_trace) -
+                                     (src_spike * dest_trace);
+            weight += lr * weight_delta;
+            w[wi] = fmaxf(0.0001f, fminf(max_weight, weight));
+            if (stp_flag) {
+                float r = stp_r[wi];
+                float sw = stp_w[wi];
+                stp_r[wi] += ((1 - r) / D) - (r * sw * src_spike);
+                stp_w[wi] += ((U - sw) / F) + (U * (1 - sw) * src_spike);
+            }
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -392,6 +612,19 @@ class IzhikevichModel : public Model {
         float* sc = to.var(sname)->df();
         float* lc = lname ? to.var(lname)->df() : sc;
         float g = cs.params.at("conductance");
+        int nrows = 0, ncols = 0;
+        if (matrix_shape(c, nrows, ncols) && ncols % 4 == 0) {
+            IzColsArgs a{cs.geom, nrows, ncols, src, cs.weights->df(), cs.var("short term R")->df(),
+                         cs.var("short term w")->df(), cs.delays->di(), cs.var("short trace")->df(),
+                         cs.var("long trace")->df(), g, stau, ltau, sc, lc};
+            int sr = (int)c.from->output_type;
+            bool subset = c.type == SUBSET;
+            if (sr == S_FLOAT) launch_cols<S_FLOAT>(a, lname != nullptr, subset, ctx.stream);
+            else if (sr == S_BIT) launch_cols<S_BIT>(a, lname != nullptr, subset, ctx.stream);
+            else launch_cols<S_INT>(a, lname != nullptr, subset, ctx.stream);
+            ctx.count();
+            return;
+        }
 #define SG_IZ_ACT(LONG)                                                                        \
     SG_DISPATCH_TYPE_SRC((int)c.type, (int)c.from->output_type,                                \
         (k_iz_activate<TY, SR, LONG><<<blocks, threads, 0, ctx.stream>>>(                      \
@@ -432,7 +665,32 @@ class IzhikevichModel : public Model {
         const int threads = 128;
         unsigned blocks = blocks_for(cs.geom.n_dest, threads);
         bool sub = c.opcode == OP_SUB;
-#define SG_IZ_LEARN(SUBV)                                                                      \
+        int nrows = 0, ncols = 0;
+        if (matrix_shape(c, nrows, ncols)) {
+            int rpb = 32;
+            dim3 grid(blocks_for(ncols, 256), blocks_for(nrows, rpb));
+            bool subset = c.type == SUBSET;
+#define SG_IZ_LEARN2D(SRV, SUBV, SSV)                                                           \
+    k_iz_learn_2d<SRV, SUBV, SSV><<<grid, 256, 0, ctx.stream>>>(                                \
+        cs.geom, nrows, ncols, rpb, st.dev_output(c.to, 0), to.var("post trace")->df(),        \
+        to.var("time since spike")->di(), cs.var("time since spike")->di(),                    \
+        cs.params.at("learning rate"), (int)cs.params.at("stp"), c.max_weight,                 \
+        cs.weights->df(), cs.var("presyn trace")->df(), cs.var("weight derivatives")->df(),    \
+        cs.var("short term R")->df(), cs.var("short term w")->df(), lut)
+#define SG_IZ_LEARN2D_SR(SRV)                                                                   \
+    if (sub) { if (subset) SG_IZ_LEARN2D(SRV, true, true); else SG_IZ_LEARN2D(SRV, true, false); } \
+    else { if (subset) SG_IZ_LEARN2D(SRV, false, true); else SG_IZ_LEARN2D(SRV, false, false); }
+            int sr = (int)c.from->output_type;
+            if (sr == S_FLOAT) { SG_IZ_LEARN2D_SR(S_FLOAT) }
+            else if (sr == S_BIT) { SG_IZ_LEARN2D_SR(S_BIT) }
+            else { SG_IZ_LEARN2D_SR(S_INT) }
+#undef SG_IZ_LEARN2D_SR
+#undef SG_IZ_LEARN2D
+            SG_LAUNCH_CHECK();
+            ctx.count();
+            return;
+        }
+#define SG_IZ_LEARN(SUBV)                                                                   \
     SG_DISPATCH_TYPE_SRC((int)c.type, (int)c.from->output_type,                                \
         (k_iz_learn<TY, SR, SUBV><<<blocks, threads, 0, ctx.stream>>>(                         \
             cs.geom, st.dev_output(c.to, 0), to.var("post trace")->df(),                       \

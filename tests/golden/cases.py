@@ -230,6 +230,48 @@ def cases():
                     record=[("s", "e"), ("s", "i")], final=finals,
                     tol={"istdp": 0.0}))
 
+    # --- Izhikevich subset / fully connected matrices wide enough for the
+    #     column kernels (destination counts divisible by 4) ----------------
+    net = {"structures": [{"name": "s", "type": "parallel", "layers": [
+        _layer("in", "relay", 12, 16),
+        _layer("a", "izhikevich", 12, 16, params="regular"),
+        _layer("b", "izhikevich", 10, 20, params="fast")]}],
+        "connections": [
+            {"name": "q_in", "from layer": "in", "to layer": "a", "type": "fully connected",
+             "opcode": "add", "plastic": False},
+            {"name": "q_ab", "from layer": "a", "to layer": "b", "type": "subset", "opcode": "add",
+             "learning rate": 0.02,
+             "subset config": {"from row start": 2, "from row end": 10, "from column start": 3,
+                               "from column end": 15, "to row start": 1, "to row end": 9,
+                               "to column start": 4, "to column end": 16}},
+            {"name": "q_ba", "from layer": "b", "to layer": "a", "type": "subset", "opcode": "sub",
+             "subset config": {"from row start": 0, "from row end": 10, "from column start": 0,
+                               "from column end": 20, "to row start": 0, "to row end": 12,
+                               "to column start": 0, "to column end": 16}},
+            {"name": "q_bb", "from layer": "b", "to layer": "b", "type": "fully connected",
+             "opcode": "mult", "plastic": False}]}
+    qconns = ["q_in", "q_ab", "q_ba", "q_bb"]
+
+    def inj_q(rng, sizes):
+        d = {}
+        for name in qconns:
+            n = sizes["conn:" + name]
+            d[("matrix", name, "weights")] = rng.uniform(0.0, 0.12, n).astype(np.float32)
+            d[("matrix", name, "short term w")] = rng.uniform(0.3, 0.7, n).astype(np.float32)
+            d[("matrix", name, "delays")] = rng.integers(0, 6, n).astype(np.int32)
+        return d
+    qfinal = []
+    for name in qconns:
+        qfinal += [("matrix", name, k) for k in ("weights", "short trace", "long trace",
+                                                 "time since spike", "short term R",
+                                                 "short term w", "weight derivatives",
+                                                 "presyn trace")]
+    qfinal += [("neuron", "s", l, k) for l in ("a", "b")
+               for k in ("voltage", "recovery", "output", "mult", "time since spike")]
+    out.append(Case("iz_subset_columns", net, 120, 61, inject=inj_q,
+                    inputs={"in": lambda rng, t, m: (rng.random(m) < 0.1) * 1.0},
+                    record=[("s", "a"), ("s", "b")], final=qfinal))
+
     # --- Izhikevich opcodes: mult, reward, gap, direct, default delays,
     #     multi-word BIT history read by a FLOAT layer ----------------------
     net = {"structures": [{"name": "s", "type": "parallel", "layers": [
