@@ -72,7 +72,80 @@ def gol_workload(side=2048):
     }
 
 
-WORKLOADS = {"gol": gol_workload}
+def iz_plastic_workload(side=256):
+    """configs[2]: three 256x256 Izhikevich layers with STDP on the convergent
+    connection, a 4096x4096 subset projection and a 5 Hz Poisson drive."""
+    import numpy as np
+    n = side * side
+
+    def layer(name, drive=False):
+        d = {"name": name, "neural model": "izhikevich", "rows": side, "columns": side}
+        if drive:   # 5 Hz at 1 ms per step, seeded, generated on the device
+            d["init config"] = {"type": "poisson", "rate": 5, "value": 20, "seed": 11}
+        return d
+    lo, hi = side * 3 // 8, side * 3 // 8 + 64
+    net = {"structures": [{"name": "s", "type": "parallel", "layers": [
+        layer("L1", drive=True), layer("L2"), layer("L3")]}],
+        "connections": [
+            {"name": "c12", "from layer": "L1", "to layer": "L2", "type": "convergent",
+             "opcode": "add", "plastic": True, "learning rate": 0.004, "myelinated": True,
+             "arborized config": {"field size": 9, "wrap": True},
+             "weight config": {"type": "random", "min weight": 0.0, "max weight": 0.3, "seed": 21}},
+            {"name": "c23", "from layer": "L2", "to layer": "L3", "type": "divergent",
+             "opcode": "add", "plastic": False, "myelinated": True,
+             "arborized config": {"field size": 3, "stride": 2},
+             "weight config": {"type": "random", "min weight": 0.0, "max weight": 0.3, "seed": 22}},
+            {"name": "c31", "from layer": "L3", "to layer": "L1", "type": "one to one",
+             "opcode": "sub", "plastic": False, "myelinated": True,
+             "weight config": {"type": "flat", "weight": 0.5}},
+            {"name": "c23s", "from layer": "L2", "to layer": "L3", "type": "subset",
+             "opcode": "add", "plastic": False, "myelinated": True,
+             "subset config": {"from row start": lo, "from row end": hi, "from column start": lo,
+                               "from column end": hi, "to row start": lo, "to row end": hi,
+                               "to column start": lo, "to column end": hi},
+             "weight config": {"type": "gaussian", "mean": 0.0, "std dev": 0.05, "seed": 23}}]}
+
+    def inject(net_obj):
+        rng = np.random.default_rng(2)
+        for lname in ("L1", "L2", "L3"):
+            fast = rng.random(n) < 0.2           # 80% regular, 20% fast spiking
+            vals = {"a": np.where(fast, 0.1, 0.02), "b": np.full(n, 0.2),
+                    "c": np.full(n, -65.0), "d": np.where(fast, 2.0, 8.0)}
+            for k, v in vals.items():
+                net_obj.get_neuron_data("s", lname, k).to_np_array()[:] = v.astype(np.float32)
+            net_obj.get_neuron_data("s", lname, "voltage").to_np_array()[:] = -65.0
+            net_obj.get_neuron_data("s", lname, "recovery").to_np_array()[:] = (
+                np.float32(0.2) * np.float32(-65.0))
+        # short-term w of convergent / divergent / one-to-one connections is 0 in
+        # the reference (type compared with opcodes); give them the ADD value.
+        for cname in ("c12", "c23", "c31"):
+            net_obj.get_weight_matrix(cname, "short term w").to_np_array()[:] = 0.5
+
+    def result(net_obj):
+        return net_obj.get_neuron_data("s", "L3", "output").to_np_array()
+
+    conv, div, one, sub = n * 81, n, n, 4096 * 4096
+    activate = conv + div + one + sub
+    return {
+        "name": "iz_plastic",
+        "desc": "3x 256x256 Izhikevich (80% RS / 20% FS), L1->L2 convergent 9x9 STDP, "
+                "L2->L3 divergent 3x3 stride 2, L3->L1 one-to-one, L2->L3 subset 4096x4096, "
+                "5 Hz Poisson drive",
+        "net": net, "inject": inject, "result": result,
+        "timesteps": 1000,
+        "units_per_timestep": activate + conv,          # activator visits + updater visits
+        "unit": "synapse-updates/s",
+        "dtype": "f32",
+        "kernel": "izhikevich.activate.subset",
+        "bytes_per_launch": 32 * sub,                   # w, stp r/w, delay, 2 traces r+w
+        "bytes_per_timestep": 32 * activate + 40 * conv + 3 * n * 124,
+        "state_bytes": None,                            # taken from the run report
+        "cpu_seconds": 15.0,
+        "learning": True,
+    }
+
+
+WORKLOADS = {"gol": gol_workload, "iz_plastic": iz_plastic_workload}
 
 
 # ---------------------------------------------------------------------------
@@ -259,7 +332,8 @@ def run_gb300(args, rank, world, local):
 
     # -- end to end through the public API with host buffers ----------------
     env = sg.Environment({"modules": []})
-    net.get_neuron_data("g", "board", "output") if args.workload == "gol" else None
+    wl["result"](net)                                      # state now lives on the host
+    state_bytes = wl["state_bytes"] or int(rep1.properties["state bytes"])
     e2e_steps = max(1, min(args.steps, 3))
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
@@ -277,7 +351,7 @@ def run_gb300(args, rank, world, local):
         "dev_s": dev_max, "units": units * world, "wall_s": t_wall, "launches": launches,
         "mean_us": mean_us, "clocks": clk, "kernels": kern,
         "e2e_value": wl["units_per_timestep"] * T * e2e_steps * world / e2e_max,
-        "e2e_steps": e2e_steps, "wl": wl, "T": T,
+        "e2e_steps": e2e_steps, "wl": wl, "T": T, "state_bytes": state_bytes,
     }
     return out
 
@@ -370,7 +444,7 @@ def main():
                      "mean_launch_us": r["mean_us"]},
         "cpu_baseline": cb,
         "e2e": {"value": r["e2e_value"], "unit": wl["unit"],
-                "h2d_bytes_per_step": wl["state_bytes"], "d2h_bytes_per_step": wl["state_bytes"],
+                "h2d_bytes_per_step": r["state_bytes"], "d2h_bytes_per_step": r["state_bytes"],
                 "steps": r["e2e_steps"]},
         "clocks": r["clocks"],
         "gpu_launches": r["launches"],

@@ -373,6 +373,134 @@ __global__ void __launch_bounds__(256, 2) k_gol_bits_strip(int rows, int cols, i
     }
 }
 
+// Shared-memory tiled variant of k_gol_bits.  A CTA (8 warps) owns 8 rows of
+// a 1024-cell strip (32 segments).  It stages the 8 rows plus one halo row
+// above and below with coalesced 128-bit loads into shared memory, padded to
+// 33 words per segment so that lane j reading word i of its own segment hits
+// bank (j + i) mod 32 (conflict free).  Warp w then processes row w of the
+// tile with one lane per segment (plane gather, bit-sliced count, rule),
+// writes its new words back into the tile, and the CTA stores the tile with
+// coalesced 128-bit stores.
+constexpr int kTileRows = 8;
+constexpr int kSegPad = 33;
+
+__global__ void __launch_bounds__(256) k_gol_bits_tile(int rows, int cols, int wrap, int delay,
+                                                       unsigned mask9, const uint32_t* __restrict__ cur,
+                                                       uint32_t* __restrict__ next,
+                                                       float* __restrict__ input_out, unsigned smask,
+                                                       unsigned bmask) {
+    __shared__ uint32_t tile[kTileRows + 2][32 * kSegPad];
+    __shared__ uint32_t cnt[4][kTileRows][32];
+    const int segs = cols >> 5;
+    const int sx = blockIdx.x;                 // strip
+    const int r0 = blockIdx.y * kTileRows;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int strip_segs = min(32, segs - sx * 32);
+    const int strip_words = strip_segs * 32;
+    // stage rows r0-1 .. r0+kTileRows (wrapping or zero outside the board)
+    for (int e = tid; e < (kTileRows + 2) * 256; e += 256) {
+        int tr = e >> 8, q = e & 255;          // 256 uint4 per 1024-word row
+        int rr = r0 - 1 + tr;
+        bool valid = true;
+        if (wrap) rr = rr < 0 ? rr + rows : (rr >= rows ? rr - rows : rr);
+        else valid = rr >= 0 && rr < rows;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (valid && rr < rows && 4 * q < strip_words)
+            v = __ldg(reinterpret_cast<const uint4*>(cur + (size_t)rr * cols + sx * 1024) + q);
+        int word = 4 * q, sg = word >> 5, i = word & 31;
+        uint32_t* dst = &tile[tr][sg * kSegPad + i];
+        dst[0] = v.x; dst[1] = v.y; dst[2] = v.z; dst[3] = v.w;
+    }
+    __syncthreads();
+    const int r = r0 + warp;
+    const bool row_ok = r < rows;
+    const bool seg_ok = lane < strip_segs;
+    uint32_t N[3], W[3], E[3], O = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const uint32_t* t = &tile[warp + k][lane * kSegPad];
+        uint32_t P = 0;
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+            uint32_t wv = t[i];
+            P |= newest_bit(wv, delay) << i;
+            if (k == 1) O |= (wv & 1u) << i;
+        }
+        // Boundary cells of the neighbouring segments: in the tile within the
+        // strip, from the board across strips.
+        uint32_t west = __shfl_up_sync(0xffffffffu, P, 1) >> 31;
+        uint32_t east = __shfl_down_sync(0xffffffffu, P, 1) & 1u;
+        int rr = r + k - 1;
+        bool rvalid = true;
+        if (wrap) rr = rr < 0 ? rr + rows : (rr >= rows ? rr - rows : rr);
+        else rvalid = rr >= 0 && rr < rows;
+        if (seg_ok && row_ok) {
+            int seg = sx * 32 + lane;
+            if (lane == 0) {
+                int cl = seg * 32 - 1;
+                if (!rvalid) west = 0u;
+                else if (cl < 0) west = wrap ? newest_bit(__ldg(cur + (size_t)rr * cols + cols - 1), delay) : 0u;
+                else west = newest_bit(__ldg(cur + (size_t)rr * cols + cl), delay);
+            }
+            if (lane == strip_segs - 1) {
+                int ce = seg * 32 + 32;
+                if (!rvalid) east = 0u;
+                else if (ce >= cols) east = wrap ? newest_bit(__ldg(cur + (size_t)rr * cols), delay) : 0u;
+                else east = newest_bit(__ldg(cur + (size_t)rr * cols + ce), delay);
+            }
+        }
+        N[k] = P;
+        W[k] = (P << 1) | west;
+        E[k] = (P >> 1) | (east << 31);
+    }
+    uint32_t c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+#pragma unroll
+    for (int kr = 0; kr < 3; ++kr) {
+        if (mask9 & (1u << (kr * 3 + 0))) csa_add(c0, c1, c2, c3, W[kr]);
+        if (mask9 & (1u << (kr * 3 + 1))) csa_add(c0, c1, c2, c3, N[kr]);
+        if (mask9 & (1u << (kr * 3 + 2))) csa_add(c0, c1, c2, c3, E[kr]);
+    }
+    uint32_t S = 0, B = 0;
+    for (int v = 0; v < 10; ++v) {
+        if (!(((smask | bmask) >> v) & 1u)) continue;
+        uint32_t e = ~((c0 ^ ((v & 1) ? ~0u : 0u)) | (c1 ^ ((v & 2) ? ~0u : 0u)) |
+                       (c2 ^ ((v & 4) ? ~0u : 0u)) | (c3 ^ ((v & 8) ? ~0u : 0u)));
+        if ((smask >> v) & 1u) S |= e;
+        if ((bmask >> v) & 1u) B |= e;
+    }
+    const uint32_t L = (O & S) | (~O & B);
+    // new words of this warp's row, in place in the tile (row warp + 1)
+    uint32_t* own = &tile[warp + 1][lane * kSegPad];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) own[i] = (own[i] >> 1) | (((L >> i) & 1u) << 31);
+    if (input_out) {
+        cnt[0][warp][lane] = c0;
+        cnt[1][warp][lane] = c1;
+        cnt[2][warp][lane] = c2;
+        cnt[3][warp][lane] = c3;
+    }
+    __syncthreads();
+    for (int e = tid; e < kTileRows * 256; e += 256) {
+        int tr = e >> 8, q = e & 255;
+        int rr = r0 + tr;
+        if (rr >= rows || 4 * q >= strip_words) continue;
+        int word = 4 * q, sg = word >> 5, i = word & 31;
+        const uint32_t* s = &tile[tr + 1][sg * kSegPad + i];
+        reinterpret_cast<uint4*>(next + (size_t)rr * cols + sx * 1024)[q] = make_uint4(s[0], s[1], s[2], s[3]);
+        if (input_out) {
+            float f[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                int b = i + k;
+                f[k] = (float)(((cnt[0][tr][sg] >> b) & 1u) | (((cnt[1][tr][sg] >> b) & 1u) << 1) |
+                               (((cnt[2][tr][sg] >> b) & 1u) << 2) | (((cnt[3][tr][sg] >> b) & 1u) << 3));
+            }
+            reinterpret_cast<float4*>(input_out + (size_t)rr * cols + sx * 1024)[q] =
+                make_float4(f[0], f[1], f[2], f[3]);
+        }
+    }
+}
+
 // Mask of counts in [lo, hi] (counts of a 3x3 kernel are 0..9).
 static unsigned count_mask(int lo, int hi) {
     unsigned m = 0;
@@ -470,8 +598,8 @@ class GameOfLifeModel : public Model {
             auto bm = cs.params.find("bits mask");
             if (bm != cs.params.end() && bm->second >= 0.0f) {
                 int strips = (l.cols / 32 + 31) / 32;
-                long threads = 32L * strips * ((l.rows + kGolRows - 1) / kGolRows);
-                k_gol_bits_strip<<<blocks_for(threads, 256), 256, 0, ctx.stream>>>(
+                dim3 grid(strips, blocks_for(l.rows, kTileRows));
+                k_gol_bits_tile<<<grid, 256, 0, ctx.stream>>>(
                     l.rows, l.cols, cs.conn->arbor.wrap ? 1 : 0, cs.conn->delay,
                     (unsigned)bm->second, ls.output->du(), swap->du(),
                     ctx.last_step ? ls.input->df() : nullptr, count_mask(smin, smax),

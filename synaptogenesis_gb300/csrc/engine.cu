@@ -402,6 +402,7 @@ Props* Engine::report() {
     r->set("average time", std::to_string((float)(steps_ ? wall_s_ / steps_ : 0.0)));
     r->set("fps", std::to_string((float)(wall_s_ > 0 ? steps_ / wall_s_ : 0.0)));
     r->set("network bytes", std::to_string(state_->device_bytes()));
+    r->set("state bytes", std::to_string(state_->host_bytes()));   // moved by one upload / download
     r->set("state buffer bytes", "0");
     size_t eb = 0;
     for (Layer* l : input_layers_) eb += (size_t)l->size * 4;

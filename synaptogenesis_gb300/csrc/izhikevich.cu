@@ -42,6 +42,9 @@ float istdp_dst(volatile int t) { return (float)(powf(t, 10) * 0.0000001 * 2.6 *
 
 }  // namespace
 
+// iSTDP tables, indexed by the time since a spike (1..31).
+struct IzLut { float src[33]; float dst[33]; };
+
 // ---------------------------------------------------------------------------
 // Kernels
 // ---------------------------------------------------------------------------
@@ -197,6 +200,121 @@ size_t iz_cols_smem() {
     return (size_t)(kColsS * NA * kColsR * 32 + 2 * 2 * kColsR * 32) * sizeof(float);
 }
 
+// Source of kernel position k of destination d for a non-convolutional
+// convergent connection (synapse_kernel.h:384-421); -1 if it is skipped.
+__device__ __forceinline__ int conv_source(const DGeom& g, int d, int k) {
+    const int tr = d / g.to_cols, tc = d - (d / g.to_cols) * g.to_cols;
+    const int kr = k / g.cf, kc = k - (k / g.cf) * g.cf;
+    int fr = tr * g.rs + g.rsp * g.ro + kr * g.rsp;
+    int fc = tc * g.cs + g.csp * g.co + kc * g.csp;
+    if (g.wrap) {
+        fr = wrap_coord(g, fr, g.from_rows);
+        fc = wrap_coord(g, fc, g.from_cols);
+    } else if (fr < 0 || fr >= g.from_rows || fc < 0 || fc >= g.from_cols) {
+        return -1;
+    }
+    return fr * g.from_cols + fc;
+}
+
+// Trace activator for non-convolutional convergent connections.  A CTA owns
+// 32 consecutive destinations; its 8 warps take the kernel positions k in
+// turn (warp w: k = w, w+8, ...), one lane per destination, so every load is a
+// coalesced 128-byte row of the [k][destination] layout and each warp has
+// many independent loads in flight.  Pre-decay traces go to shared memory and
+// lanes of warps 0 / 1 add them in k order (the reference's sequential sum),
+// skipping positions outside a non-wrapping layer as the reference does.
+constexpr int kConvMaxK = 128;
+
+template <int SR, bool LONG>
+__global__ void __launch_bounds__(256) k_iz_activate_conv_tile(
+    DGeom g, int K, const uint32_t* __restrict__ src, const float* __restrict__ w,
+    const float* __restrict__ stp_r, const float* __restrict__ stp_w, const int* __restrict__ delays,
+    float* __restrict__ short_tr, float* __restrict__ long_tr, float gcond, float short_tau,
+    float long_tau, float* __restrict__ short_cond, float* __restrict__ long_cond) {
+    __shared__ float s_st[kConvMaxK][32];
+    __shared__ float s_lt[LONG ? kConvMaxK : 1][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int d = blockIdx.x * 32 + lane;
+    const bool ok = d < g.to_size;
+    for (int k = warp; k < K; k += 8) {
+        int from = ok ? conv_source(g, d, k) : -1;
+        float st_pre = 0.0f, lt_pre = 0.0f;
+        if (from >= 0) {
+            size_t wi = (size_t)k * g.to_size + d;
+            float spike = extract<SR>(__ldg(src + from), SR == S_BIT ? __ldg(delays + wi) : 0);
+            float weight = __ldg(w + wi) * (__ldg(stp_r + wi) * __ldg(stp_w + wi));
+            st_pre = short_tr[wi] + (spike * weight * gcond);
+            short_tr[wi] = st_pre * short_tau;
+            if (LONG) {
+                lt_pre = long_tr[wi] + (spike * weight * gcond);
+                long_tr[wi] = lt_pre * long_tau;
+            }
+        }
+        s_st[k][lane] = st_pre;
+        if (LONG) s_lt[k][lane] = lt_pre;
+    }
+    __syncthreads();
+    if (!ok) return;
+    if (warp == 0) {
+        float sum = 0.0f;
+        for (int k = 0; k < K; ++k)
+            if (g.wrap || conv_source(g, d, k) >= 0) sum += s_st[k][lane];
+        short_cond[d] += sum;
+    } else if (LONG && warp == 1) {
+        float sum = 0.0f;
+        for (int k = 0; k < K; ++k)
+            if (g.wrap || conv_source(g, d, k) >= 0) sum += s_lt[k][lane];
+        long_cond[d] += sum;
+    }
+}
+
+// Updater for non-convolutional convergent connections: one thread per
+// synapse (kernel position, destination), coalesced along destinations.
+template <int SR, bool SUB>
+__global__ void __launch_bounds__(256) k_iz_learn_conv_tile(
+    DGeom g, int K, const uint32_t* __restrict__ dest_out, const float* __restrict__ to_exc,
+    const int* __restrict__ to_tss, const int* __restrict__ from_tss, float lr, int stp_flag,
+    float max_weight, float* __restrict__ w, float* __restrict__ presyn, float* __restrict__ wd,
+    float* __restrict__ stp_r, float* __restrict__ stp_w, IzLut lut) {
+    const int d = blockIdx.x * 32 + (threadIdx.x & 31);
+    if (d >= g.to_size) return;
+    const double U = SUB ? 0.2 : 0.5;
+    const int F = SUB ? 20 : 1000;
+    const int D = SUB ? 700 : 800;
+    const float dest_exc_trace = __ldg(to_exc + d);
+    const int dest_tss = __ldg(to_tss + d);
+    const float dest_spike = extract<SR>(__ldg(dest_out + d), 0);
+    for (int k = (threadIdx.x >> 5) + blockIdx.y * 8; k < K; k += 8 * gridDim.y) {
+        int from = conv_source(g, d, k);
+        if (from < 0) continue;
+        size_t wi = (size_t)k * g.to_size + d;
+        float weight = w[wi];
+        if (weight >= 0.0001f) {
+            int src_tss = __ldg(from_tss + from);
+            bool src_spike = src_tss == 0;
+            float src_trace, dest_trace;
+            if (!SUB) {
+                src_trace = (presyn[wi] = src_spike ? 0.004 : presyn[wi] * 0.933);
+                dest_trace = dest_exc_trace;
+            } else {
+                src_trace = (dest_spike > 0.0f && src_tss > 0 && src_tss < 32) ? lut.src[src_tss] : 0.0f;
+                dest_trace = (src_spike && dest_tss > 0 && dest_tss < 32) ? lut.dst[dest_tss] : 0.0f;
+            }
+            float weight_delta = wd[wi];
+            weight_delta = wd[wi] -= (weight_delta - 0.000001) * 0.0001 + (dest_spike * src_trace) -
+                                     (src_spike * dest_trace);
+            weight += lr * weight_delta;
+            w[wi] = fmaxf(0.0001f, fminf(max_weight, weight));
+            if (stp_flag) {
+                float r = stp_r[wi];
+                float sw = stp_w[wi];
+                stp_r[wi] += ((1 - r) / D) - (r * sw * src_spike);
+                stp_w[wi] += ((U - sw) / F) + (U * (1 - sw) * src_spike);
+            }
+        }
+    }
+}
+
 // Rows (sources) and columns (destinations) of a fully connected or subset
 // matrix in the device layout; false for the other connection types.
 static bool matrix_shape(const Connection& c, int& nrows, int& ncols) {
@@ -339,7 +457,6 @@ __global__ void __launch_bounds__(256) k_iz_update(
     recoveries[nid] = recovery + (spike * ds[nid]);
 }
 
-struct IzLut { float src[33]; float dst[33]; };
 
 // STDP + STP updaters (izhikevich_attributes.cpp:404-520).  The destination
 // spike goes through the connection's extractor, i.e. the SOURCE layer's
@@ -612,6 +729,29 @@ class IzhikevichModel : public Model {
         float* sc = to.var(sname)->df();
         float* lc = lname ? to.var(lname)->df() : sc;
         float g = cs.params.at("conductance");
+        const int K = c.arbor.kernel();
+        if (c.type == CONVERGENT && !c.convolutional && K <= kConvMaxK) {
+            unsigned nb = blocks_for(c.to->size, 32);
+            int sr = (int)c.from->output_type;
+#define SG_CONV_TILE(SRV, LV)                                                                     \
+    k_iz_activate_conv_tile<SRV, LV><<<nb, 256, 0, ctx.stream>>>(                                 \
+        cs.geom, K, src, cs.weights->df(), cs.var("short term R")->df(),                        \
+        cs.var("short term w")->df(), cs.delays->di(), cs.var("short trace")->df(),             \
+        cs.var("long trace")->df(), g, stau, ltau, sc, lc)
+            if (lname) {
+                if (sr == S_FLOAT) SG_CONV_TILE(S_FLOAT, true);
+                else if (sr == S_BIT) SG_CONV_TILE(S_BIT, true);
+                else SG_CONV_TILE(S_INT, true);
+            } else {
+                if (sr == S_FLOAT) SG_CONV_TILE(S_FLOAT, false);
+                else if (sr == S_BIT) SG_CONV_TILE(S_BIT, false);
+                else SG_CONV_TILE(S_INT, false);
+            }
+#undef SG_CONV_TILE
+            SG_LAUNCH_CHECK();
+            ctx.count();
+            return;
+        }
         int nrows = 0, ncols = 0;
         if (matrix_shape(c, nrows, ncols) && ncols % 4 == 0) {
             IzColsArgs a{cs.geom, nrows, ncols, src, cs.weights->df(), cs.var("short term R")->df(),
@@ -665,6 +805,31 @@ class IzhikevichModel : public Model {
         const int threads = 128;
         unsigned blocks = blocks_for(cs.geom.n_dest, threads);
         bool sub = c.opcode == OP_SUB;
+        if (c.type == CONVERGENT) {
+            const int K = c.arbor.kernel();
+            dim3 grid(blocks_for(c.to->size, 32), std::max(1, (K + 23) / 24));
+            int sr = (int)c.from->output_type;
+#define SG_CONV_LEARN(SRV, SUBV)                                                                  \
+    k_iz_learn_conv_tile<SRV, SUBV><<<grid, 256, 0, ctx.stream>>>(                                \
+        cs.geom, K, st.dev_output(c.to, 0), to.var("post trace")->df(),                         \
+        to.var("time since spike")->di(), cs.var("time since spike")->di(),                     \
+        cs.params.at("learning rate"), (int)cs.params.at("stp"), c.max_weight,                  \
+        cs.weights->df(), cs.var("presyn trace")->df(), cs.var("weight derivatives")->df(),     \
+        cs.var("short term R")->df(), cs.var("short term w")->df(), lut)
+            if (sub) {
+                if (sr == S_FLOAT) SG_CONV_LEARN(S_FLOAT, true);
+                else if (sr == S_BIT) SG_CONV_LEARN(S_BIT, true);
+                else SG_CONV_LEARN(S_INT, true);
+            } else {
+                if (sr == S_FLOAT) SG_CONV_LEARN(S_FLOAT, false);
+                else if (sr == S_BIT) SG_CONV_LEARN(S_BIT, false);
+                else SG_CONV_LEARN(S_INT, false);
+            }
+#undef SG_CONV_LEARN
+            SG_LAUNCH_CHECK();
+            ctx.count();
+            return;
+        }
         int nrows = 0, ncols = 0;
         if (matrix_shape(c, nrows, ncols)) {
             int rpb = 32;

@@ -125,7 +125,8 @@ void State::build() {
 
 size_t State::host_bytes() const {
     size_t n = 0;
-    for (auto& a : arrays_) n += a->count * 4;
+    for (auto& a : arrays_)
+        if (!a->scratch) n += std::min(a->count, a->dev_count) * 4;
     return n;
 }
 
