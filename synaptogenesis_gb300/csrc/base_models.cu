@@ -469,6 +469,8 @@ __global__ void __launch_bounds__(256) k_gol_bits_tile(int rows, int cols, int w
         if ((bmask >> v) & 1u) B |= e;
     }
     const uint32_t L = (O & S) | (~O & B);
+    // Every warp has read its three tile rows; rows are now rewritten in place.
+    __syncthreads();
     // new words of this warp's row, in place in the tile (row warp + 1)
     uint32_t* own = &tile[warp + 1][lane * kSegPad];
 #pragma unroll
