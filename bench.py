@@ -327,6 +327,11 @@ def run_gb300(args, rank, world, local):
         peng.step(prof_steps)
         prep = peng.report()
     kern = {p.properties["name"]: p.properties for p in prep.child_arrays.get("kernel times", [])}
+    total_ms = sum(float(k["total ms"]) for k in kern.values()) or 1.0
+    for name, k in sorted(kern.items(), key=lambda kv: -float(kv[1]["total ms"])):
+        print("# %-36s groups %7s  mean %9.2f us  share %5.1f%%"
+              % (name, k["groups"], float(k["mean us"]), 100.0 * float(k["total ms"]) / total_ms),
+              file=sys.stderr)
     dom = kern.get(wl["kernel"])
     mean_us = float(dom["mean us"]) if dom else None
 

@@ -94,7 +94,7 @@ __device__ __forceinline__ int row_source(const DGeom& g, int row) {
 // Trace activator for fully connected and subset matrices, which have many
 // sources per destination and (in the device layout [source][destination])
 // rows of contiguous destinations.  One CTA owns 32 destination columns and
-// streams every source row through a 4-stage cp.async pipeline of 32-row
+// streams every source row through a 6-stage cp.async pipeline of 32-row
 // tiles (weights, short-term R and w, delays, short and long traces), so the
 // loads of later tiles are in flight while a tile is processed.  All 256
 // threads do the per-synapse work (one warp per row, one lane per column) and
@@ -102,7 +102,7 @@ __device__ __forceinline__ int row_source(const DGeom& g, int row) {
 // double-buffered shared tile from which one lane per column adds them in row
 // order, keeping the reference's sequential fp32 sum.  Needs ncols % 4 == 0.
 constexpr int kColsR = 32;       // rows per stage
-constexpr int kColsS = 4;        // stages
+constexpr int kColsS = 6;        // stages
 
 template <int SR, bool LONG, bool SUBSET>
 __global__ void __launch_bounds__(256, 1) k_iz_activate_cols(
