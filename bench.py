@@ -73,7 +73,7 @@ def gol_workload(side=2048):
 
 
 def iz_plastic_workload(side=256):
-    """configs[2]: three 256x256 Izhikevich layers with STDP on the convergent
+    """Large plastic Izhikevich network: three 256x256 Izhikevich layers with STDP on the convergent
     connection, a 4096x4096 subset projection and a 5 Hz Poisson drive."""
     import numpy as np
     n = side * side
@@ -145,7 +145,53 @@ def iz_plastic_workload(side=256):
     }
 
 
-WORKLOADS = {"gol": gol_workload, "iz_plastic": iz_plastic_workload}
+def batched_workload():
+    """Batched instances: 256 independent instances of the plain Izhikevich
+    configuration, sides uniform in 16..128 (seed 3), advanced together."""
+    return {
+        "name": "batched",
+        "desc": "256 Izhikevich instances (relay->Izhikevich convergent 5x5 wrap, recurrent "
+                "fully connected 20% density U(0,0.2), delays U{0..3}, 10 Hz relay drive), "
+                "sides U{16..128} seed 3, a/b/c/d within +-10% of regular spiking",
+        "timesteps": 100,
+        "unit": "instance-timesteps/s",
+        "dtype": "f32",
+        "kernel": "k_batch_step",
+        "cpu_seconds": 15.0,
+        "batched": True,
+    }
+
+
+WORKLOADS = {"gol": gol_workload, "iz_plastic": iz_plastic_workload, "batched": batched_workload}
+
+# Sides of the instances timed one at a time (plain GPU path / reference CPU
+# path); the per-timestep time is fitted as alpha + beta * (recurrent synapses)
+# and summed over the batch's instances.
+PLAIN_SAMPLE_SIDES = (16, 32, 48, 64, 80, 96)
+CPU_SAMPLE_SIDES = (16, 24, 32, 48, 64)
+
+
+def sample_network(side):
+    """One instance of the batch as an ordinary network, for timing only:
+    connections are myelinated (delay 0) since distance-based default delays
+    exceed 31 on large layers; a step's work does not depend on delay values."""
+    from synaptogenesis_gb300 import batching
+    net = batching.plain_network(batching.instance(side, 1))[0]
+    for c in net["connections"]:
+        c["myelinated"] = True
+    return net
+
+
+def fit_batch_seconds(samples, instances):
+    """Seconds per timestep of running ``instances`` one at a time, from
+    (side, seconds per timestep) samples fitted as alpha + beta * side**4."""
+    import numpy as np
+    x = np.array([float(s) ** 4 for s, _ in samples])
+    y = np.array([t for _, t in samples])
+    A = np.stack([np.ones_like(x), x], axis=1)
+    (alpha, beta), *_ = np.linalg.lstsq(A, y, rcond=None)
+    alpha, beta = max(alpha, 0.0), max(beta, 0.0)
+    return sum(alpha + beta * float(i["rows"] * i["cols"]) ** 2 for i in instances), alpha, beta
 
 
 # ---------------------------------------------------------------------------
@@ -234,6 +280,33 @@ def cpu_worker(args):
     wl = WORKLOADS[args.workload]()
     from synaptogenesis_gb300 import syngen as sg
     sg.set_warnings(False)
+    if wl.get("batched"):
+        # the reference runs one network at a time: time sample instances
+        from synaptogenesis_gb300 import batching
+        env = sg.Environment({"modules": []})
+        run_args = {"multithreaded": False, "worker threads": 0, "learning flag": False}
+        budget = args.cpu_seconds / len(CPU_SAMPLE_SIDES)
+        samples, total_steps, total_s = [], 0, 0.0
+        for side in CPU_SAMPLE_SIDES:
+            net = sg.Network(sample_network(side))
+            net.build_state()
+            t0 = time.perf_counter()
+            net.run(env, dict(run_args, iterations=2))
+            per = max((time.perf_counter() - t0) / 2, 1e-6)
+            steps = max(2, int(budget / per))
+            t0 = time.perf_counter()
+            rep = net.run(env, dict(run_args, iterations=steps))
+            dt = time.perf_counter() - t0
+            assert rep.obj is not None, "reference run failed"
+            samples.append((side, dt / steps))
+            total_steps += steps
+            total_s += dt
+            del net
+        insts = batching.batch_instances(256, 3)
+        secs, alpha, beta = fit_batch_seconds(samples, insts)
+        print(json.dumps({"value": len(insts) / secs, "seconds": total_s, "timesteps": total_steps,
+                          "samples": samples, "alpha": alpha, "beta": beta}))
+        return
     net = sg.Network(wl["net"])
     net.build_state()
     wl["inject"](net)
@@ -268,10 +341,17 @@ def cpu_baseline(workload, seconds, timesteps=0):
         return {"value": None, "unit": WORKLOADS[workload]()["unit"], "cores": cores,
                 "kind": "reference", "sample": "failed: " + r.stderr[-300:]}
     out = json.loads(r.stdout.strip().splitlines()[-1])
+    if "samples" in out:
+        sample = ("reference library run one instance at a time (dense recurrent matrix), "
+                  "sides %s timed for %d timesteps in all (%.1f s wall, OMP_NUM_THREADS=%d); "
+                  "per-timestep time fitted as %.3g s + %.3g s * side^4 and summed over the "
+                  "256 instances" % (list(CPU_SAMPLE_SIDES), out["timesteps"], out["seconds"],
+                                     cores, out["alpha"], out["beta"]))
+    else:
+        sample = ("%d timesteps of the same workload, %.1f s wall, OMP_NUM_THREADS=%d"
+                  % (out["timesteps"], out["seconds"], cores))
     return {"value": out["value"], "unit": WORKLOADS[workload]()["unit"], "cores": cores,
-            "kind": "reference",
-            "sample": "%d timesteps of the same workload, %.1f s wall, OMP_NUM_THREADS=%d"
-                      % (out["timesteps"], out["seconds"], cores),
+            "kind": "reference", "sample": sample,
             "timesteps": out["timesteps"], "seconds": out["seconds"]}
 
 
@@ -361,6 +441,139 @@ def run_gb300(args, rank, world, local):
     return out
 
 
+def run_batched(args, rank, world, local):
+    """The batch of instances (this rank's shard) on one GPU, plus the plain
+    layer-by-layer GPU path run one instance at a time on sample instances."""
+    import torch
+    from synaptogenesis_gb300 import batching
+    from synaptogenesis_gb300 import syngen as sg
+    sg.set_warnings(False)
+    wl = WORKLOADS[args.workload]()
+    T = args.timesteps or wl["timesteps"]
+    all_insts = batching.batch_instances(256, 3)
+    insts = [all_insts[i] for i in batching.shard_instances(all_insts, rank, world)]
+    b = sg.Batch(insts)
+    rep0 = b.report()
+    props = rep0.properties
+    tuning = [{k: c.properties[k] for k in ("tile rows", "tile colblocks", "ms per step")}
+              for c in rep0.child_arrays.get("autotune", [])]
+    stream = torch.cuda.ExternalStream(b.stream)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        b.step(T)
+    launches0 = int(b.report().properties["kernel launches"])
+    gpu_index = os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0]
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = ClockSampler(gpu_index)
+    evs = []
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.add_(1.0)                       # L2 flush, outside the events
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.step(T)
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    dev_s = sum(a.elapsed_time(c) for a, c in evs) / 1000.0
+    launches = int(b.report().properties["kernel launches"]) - launches0
+
+    # end to end: step through the C-ABI, then read every instance's output
+    # words into host memory
+    e2e_steps = max(1, min(args.steps, 3))
+    d2h = sum(i["rows"] * i["cols"] for i in insts) * 4
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        b.step(T)
+        outs = [b.read(i, "output") for i in range(len(insts))]
+        _ = int(outs[-1][0])
+    e2e_s = time.perf_counter() - t0
+    b.close()
+
+    # plain GPU path, one instance at a time (rank 0)
+    plain = None
+    if rank == 0:
+        samples = []
+        for side in PLAIN_SAMPLE_SIDES:
+            net = sg.Network(sample_network(side))
+            net.build_state()
+            with sg.Engine(net, None, {"learning flag": False, "graph steps": 16}) as eng:
+                pst = torch.cuda.ExternalStream(eng.stream)
+                eng.step(32)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(pst)
+                eng.step(64)
+                e1.record(pst)
+                torch.cuda.synchronize()
+                samples.append((side, e0.elapsed_time(e1) / 1000.0 / 64))
+            del net
+        secs, alpha, beta = fit_batch_seconds(samples, all_insts)
+        plain = {"value": len(all_insts) / secs, "unit": wl["unit"],
+                 "sample": "layer-by-layer GPU path (dense recurrent matrix), one instance at a "
+                           "time, sides %s x 64 timesteps each; per-timestep time fitted as "
+                           "%.3g s + %.3g s * side^4 and summed over the 256 instances"
+                           % (list(PLAIN_SAMPLE_SIDES), alpha, beta),
+                 "samples_s_per_timestep": samples}
+
+    dev_max, e2e_max = reduce_max([dev_s, e2e_s], world)
+    n_total = len(all_insts) if world > 1 else len(insts)
+    return {"dev_s": dev_max, "units": n_total * T * args.steps, "launches": launches,
+            "mean_us": dev_s * 1e6 / (T * args.steps), "clocks": clk, "T": T,
+            "e2e_value": n_total * T * e2e_steps / e2e_max, "e2e_steps": e2e_steps,
+            "d2h": d2h, "props": props, "tuning": tuning, "plain": plain,
+            "step_bytes": int(props["step bytes"]),
+            "syn_per_timestep": int(props["fc synapses"]) + int(props["conv synapses"])}
+
+
+def batched_line(args, world, r, wl, cb):
+    peak, peak_kind = measured_peak()
+    achieved = r["step_bytes"] / (r["mean_us"] * 1e-6) / 1e9
+    traffic = None
+    try:
+        with open(TRAFFIC) as f:
+            traffic = json.load(f).get(args.workload)
+    except Exception:
+        pass
+    p = r["props"]
+    value = r["units"] / r["dev_s"]
+    return {
+        "metric": "instance-timesteps/s (batched)", "value": value, "unit": wl["unit"],
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * r["dev_s"] / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": wl["dtype"], "data": "synthetic (counter-based generator, seeds per instance)",
+        "config": {"workload": wl["desc"], "timesteps_per_step": r["T"],
+                   "ms_per_timestep": 1000.0 * r["dev_s"] / (args.steps * r["T"]),
+                   "synapse_updates_per_s": r["syn_per_timestep"] * r["T"] * args.steps / r["dev_s"],
+                   "recurrent_synapses": int(p["fc synapses"]), "ell_slots": int(p["fc slots"]),
+                   "convergent_synapses": int(p["conv synapses"]),
+                   "device_bytes": int(p["device bytes"]),
+                   "tile": [int(p["tile rows"]), int(p["tile colblocks"])],
+                   "grid": int(p["grid"]), "threads": int(p["threads"]),
+                   "autotune_ms_per_timestep": r["tuning"],
+                   "l2": "flushed between steps (256 MiB write outside the timed events); "
+                         "per-step traffic ~%.0f GB >> L2" % (r["step_bytes"] / 1e9),
+                   "parallelism": "instances sharded over ranks" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": wl["kernel"], "bytes_per_launch": r["step_bytes"],
+                     "mean_launch_us": r["mean_us"]},
+        "plain_gpu_one_at_a_time": r["plain"],
+        "cpu_baseline": cb,
+        "e2e": {"value": r["e2e_value"], "unit": wl["unit"], "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": r["d2h"], "steps": r["e2e_steps"],
+                "note": "inputs are generated on the device from the instance seeds; every "
+                        "instance's output words are read back each step"},
+        "clocks": r["clocks"],
+        "gpu_launches": r["launches"],
+    }
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -386,7 +599,8 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("gloo")
     wl = WORKLOADS[args.workload]()
-    metric = "synapse-updates/s (%s)" % wl["name"]
+    metric = ("instance-timesteps/s (batched)" if wl.get("batched")
+              else "synapse-updates/s (%s)" % wl["name"])
 
     if args.impl == "reference":
         if rank != 0:
@@ -413,6 +627,14 @@ def main():
                 "e2e": {"value": cb["value"], "unit": wl["unit"], "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
+        return
+
+    if wl.get("batched"):
+        r = run_batched(args, rank, world, local)
+        if rank != 0:
+            return
+        cb = None if args.no_cpu_baseline else cpu_baseline(args.workload, wl["cpu_seconds"])
+        print(json.dumps(batched_line(args, world, r, wl, cb)))
         return
 
     r = run_gb300(args, rank, world, local)

@@ -178,6 +178,57 @@ int sg_gol_steps_noalloc(unsigned int* words, float* input_out, int rows, int co
                          const float* weights, int field, int steps, int survival_min,
                          int survival_max, int birth_min, int birth_max, void* stream);
 
+/* Batched Izhikevich instances.  No counterpart in the reference, which runs
+ * one network per engine (src/core/engine/engine.cpp:466-471); a batch
+ * replaces running that engine once per instance.
+ *
+ * Every instance is the plain Izhikevich topology: a relay layer of rows x cols
+ * (FLOAT output) whose input each step is `input_value` with probability
+ * `input_rate`, a convergent wrapping "add" connection (conv_field^2 kernel,
+ * stride 1, offset -field/2) into an Izhikevich layer of the same shape, and
+ * a recurrent fully connected "sub" connection on that layer.  Weights, delays
+ * and inputs are counter-based functions of `seed` (convergent weights
+ * U(0, conv_wmax); recurrent weights U(0, fc_wmax) kept with probability
+ * fc_density, delays U{0..fc_max_delay}); the effective weight of a synapse is
+ * weight x (short term R = 1) x (short term w = *_stp_w), as in the
+ * reference's activator.  Initial voltage v0 and recovery b * v0.  The same
+ * instance built as an ordinary network gives the same spike raster, bit for
+ * bit.  All instances need the same conv_field. */
+typedef struct SgBatchInstance {
+    int rows, cols;
+    float a, b, c, d;
+    float v0;
+    unsigned long long seed;
+    float input_rate, input_value;
+    int conv_field;
+    float conv_wmax, conv_stp_w, conv_conductance;
+    float fc_wmax, fc_density, fc_stp_w, fc_conductance;
+    int fc_max_delay;
+} SgBatchInstance;
+
+#define SG_BATCH_EINVAL (-1)
+#define SG_BATCH_ECUDA (-3)
+typedef void* SG_BATCH;
+
+/* Builds the batch on the current device.  tile_rows x tile_colblocks (rows x
+ * blocks of 32 columns, at most 8 warps) is the work unit of the step kernel;
+ * 0, 0 runs the autotuner, which times each candidate over real steps and
+ * then resets the state.  NULL on error (sg_last_error). */
+SG_BATCH sg_batch_create(const SgBatchInstance* instances, int count, int tile_rows,
+                         int tile_colblocks);
+/* Advances every instance by `steps` timesteps, one kernel launch per step
+ * (captured in CUDA graphs of 32 steps).  Asynchronous on sg_batch_stream. */
+int sg_batch_step(SG_BATCH batch, long long steps);
+/* Copies an instance's "voltage", "recovery" (float) or "output" (newest
+ * output-history word, uint32) to host memory of at least rows*cols values. */
+int sg_batch_read(SG_BATCH batch, int instance, const char* key, void* out, long long count);
+/* Sizes, chosen tile, autotuner timings and launch counts; owned by the
+ * caller (destroy_properties). */
+PROPS sg_batch_report(SG_BATCH batch);
+void* sg_batch_stream(SG_BATCH batch);
+int sg_batch_synchronize(SG_BATCH batch);
+void sg_batch_destroy(SG_BATCH batch);
+
 #ifdef __cplusplus
 }
 #endif

@@ -54,6 +54,11 @@ struct StateHandle {
 
 }  // namespace
 
+namespace sg {
+// Error text for sg_last_error from entry points defined in other files.
+void set_last_error(const char* what) { set_error(what); }
+}  // namespace sg
+
 #define SG_TRY(fail)                          \
     try {
 #define SG_CATCH(fail)                        \

@@ -1,0 +1,35 @@
+// Izhikevich neuron integration (src/core/state/impl/izhikevich_attributes.cpp:102-213),
+// shared by the per-layer update kernel and the batched instance runner so
+// both execute the same float/double expression sequence.
+#pragma once
+
+namespace sg {
+
+#ifdef __CUDACC__
+// Up to 10 hybrid-Euler substeps that stop once v >= 30 (NaN -> 30), with the
+// conductance-implicit voltage update and the recovery step whose time
+// constant is adjusted on the substep that crosses threshold.
+__device__ __forceinline__ void iz_integrate(float& voltage, float& recovery, float ampa_c,
+                                             float nmda_c, float gabaa_c, float gabab_c, float mf,
+                                             float base_current, float a, float b) {
+    for (int i = 0; (i < 10) && (voltage < 30.0); ++i) {
+        float current = -ampa_c * voltage;
+        float q = (voltage + 80) / 60;
+        float temp = q * q;
+        current -= nmda_c * (temp / (1 + temp)) * voltage;
+        current -= gabaa_c * (voltage + 70);
+        current -= gabab_c * (voltage + 90);
+        current *= 1 + mf;
+        current += base_current;
+        float delta_v = (0.04 * voltage * voltage) + (5 * voltage) + 140 - recovery + current;
+        float sum_c = ampa_c + nmda_c + gabaa_c + gabab_c;
+        voltage = (voltage + 0.1 * (delta_v + (gabaa_c * -70) + (gabab_c * -90))) /
+                  (1 + (0.1 * sum_c));
+        voltage = (voltage != voltage) ? 30.0 : voltage;
+        float adjusted_tau = (voltage > 30.0) ? delta_v / (30.0 - voltage + delta_v) * 0.1 : 0.1;
+        recovery += a * adjusted_tau * ((b * voltage) - recovery);
+    }
+}
+#endif
+
+}  // namespace sg

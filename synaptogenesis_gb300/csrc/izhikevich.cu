@@ -11,6 +11,7 @@
 #include <random>
 
 #include "cuda_check.h"
+#include "iz_neuron.cuh"
 #include "models.h"
 #include "state.h"
 #include "weight_init.h"
@@ -416,24 +417,8 @@ __global__ void __launch_bounds__(256) k_iz_update(
     float voltage = voltages[nid];
     float recovery = recoveries[nid];
     float base_current = inputs[nid];
-    float a = as[nid], b = bs[nid];
-    for (int i = 0; (i < 10) && (voltage < 30.0); ++i) {
-        float current = -ampa_c * voltage;
-        float q = (voltage + 80) / 60;
-        float temp = q * q;
-        current -= nmda_c * (temp / (1 + temp)) * voltage;
-        current -= gabaa_c * (voltage + 70);
-        current -= gabab_c * (voltage + 90);
-        current *= 1 + mf;
-        current += base_current;
-        float delta_v = (0.04 * voltage * voltage) + (5 * voltage) + 140 - recovery + current;
-        float sum_c = ampa_c + nmda_c + gabaa_c + gabab_c;
-        voltage = (voltage + 0.1 * (delta_v + (gabaa_c * -70) + (gabab_c * -90))) /
-                  (1 + (0.1 * sum_c));
-        voltage = (voltage != voltage) ? 30.0 : voltage;
-        float adjusted_tau = (voltage > 30.0) ? delta_v / (30.0 - voltage + delta_v) * 0.1 : 0.1;
-        recovery += a * adjusted_tau * ((b * voltage) - recovery);
-    }
+    iz_integrate(voltage, recovery, ampa_c, nmda_c, gabaa_c, gabab_c, mf, base_current, as[nid],
+                 bs[nid]);
     ampa[nid] = 0.0f;
     nmda[nid] = 0.0f;
     gabaa[nid] = 0.0f;

@@ -155,7 +155,31 @@ def _load_library(path=None):
         lib.sg_engine_report.argtypes = (c_void_p,)
         lib.sg_engine_report.restype = c_void_p
         lib.sg_engine_destroy.argtypes = (c_void_p,)
+    if hasattr(lib, "sg_batch_create"):
+        lib.sg_batch_create.argtypes = (POINTER(BatchInstance), c_int, c_int, c_int)
+        lib.sg_batch_create.restype = c_void_p
+        lib.sg_batch_step.argtypes = (c_void_p, c_longlong)
+        lib.sg_batch_step.restype = c_int
+        lib.sg_batch_read.argtypes = (c_void_p, c_int, c_char_p, c_void_p, c_longlong)
+        lib.sg_batch_read.restype = c_int
+        lib.sg_batch_report.argtypes = (c_void_p,)
+        lib.sg_batch_report.restype = c_void_p
+        lib.sg_batch_stream.argtypes = (c_void_p,)
+        lib.sg_batch_stream.restype = c_void_p
+        lib.sg_batch_synchronize.argtypes = (c_void_p,)
+        lib.sg_batch_synchronize.restype = c_int
+        lib.sg_batch_destroy.argtypes = (c_void_p,)
     return lib, path
+
+
+class BatchInstance(Structure):
+    """SgBatchInstance of include/syngen.h: one instance of a batch."""
+    _fields_ = [("rows", c_int), ("cols", c_int), ("a", c_float), ("b", c_float),
+                ("c", c_float), ("d", c_float), ("v0", c_float), ("seed", c_ulonglong),
+                ("input_rate", c_float), ("input_value", c_float), ("conv_field", c_int),
+                ("conv_wmax", c_float), ("conv_stp_w", c_float), ("conv_conductance", c_float),
+                ("fc_wmax", c_float), ("fc_density", c_float), ("fc_stp_w", c_float),
+                ("fc_conductance", c_float), ("fc_max_delay", c_int)]
 
 
 _syn, LIB_PATH = _load_library()
@@ -498,6 +522,61 @@ class Engine:
     def close(self):
         if self.obj:
             _syn.sg_engine_destroy(self.obj)
+            self.obj = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class Batch:
+    """Many independent Izhikevich instances advanced together (sg_batch_* in
+    include/syngen.h).  ``instances`` is a sequence of dicts with the fields of
+    ``BatchInstance``; ``tile`` = (rows, colblocks) fixes the step kernel's work
+    unit, None lets the autotuner choose."""
+
+    def __init__(self, instances, tile=None):
+        n = len(instances)
+        arr = (BatchInstance * n)()
+        for i, spec in enumerate(instances):
+            for k, v in spec.items():
+                setattr(arr[i], k, v)
+        self.sizes = [(s["rows"], s["cols"]) for s in instances]
+        tr, tc = tile if tile else (0, 0)
+        self.obj = _syn.sg_batch_create(arr, n, int(tr), int(tc))
+        if not self.obj:
+            raise RuntimeError("batch creation failed: " + last_error())
+
+    def step(self, n):
+        if _syn.sg_batch_step(self.obj, int(n)) != 0:
+            raise RuntimeError("batch step failed: " + last_error())
+
+    def read(self, instance, key):
+        """Host copy of "voltage", "recovery" (float32) or "output" (uint32)."""
+        import numpy as np
+        rows, cols = self.sizes[instance]
+        out = np.empty(rows * cols, np.uint32 if key == "output" else np.float32)
+        if _syn.sg_batch_read(self.obj, int(instance), key.encode("utf-8"),
+                              out.ctypes.data, out.size) != 0:
+            raise RuntimeError("batch read failed: " + last_error())
+        return out
+
+    @property
+    def stream(self):
+        return _syn.sg_batch_stream(self.obj)
+
+    def synchronize(self):
+        if _syn.sg_batch_synchronize(self.obj) != 0:
+            raise RuntimeError("batch synchronize failed")
+
+    def report(self):
+        return Properties(_syn.sg_batch_report(self.obj))
+
+    def close(self):
+        if self.obj:
+            _syn.sg_batch_destroy(self.obj)
             self.obj = None
 
     def __enter__(self):
