@@ -114,7 +114,7 @@ def plain_network(inst):
              "conductance": str(inst["conv_conductance"]),
              "arborized config": {"field size": inst["conv_field"], "wrap": True}},
             {"name": "c_rec", "from layer": "iz", "to layer": "iz", "type": "fully connected",
-             "plastic": False, "opcode": "sub",
+             "plastic": False, "opcode": "sub", "myelinated": True,
              "conductance": str(inst["fc_conductance"])}]}
     w, delays = fc_dense(inst)
     cw = conv_dense(inst)

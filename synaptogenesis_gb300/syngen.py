@@ -295,16 +295,19 @@ def _strings(arr_obj):
     return out
 
 
+_EMPTY = object()
+
+
 class Properties:
     """String-keyed property tree; built from a dict, or read from a C handle."""
 
-    def __init__(self, props=None):
+    def __init__(self, props=_EMPTY):
         self.properties = OrderedDict()
         self.children = OrderedDict()
         self.arrays = OrderedDict()
         self.child_arrays = OrderedDict()
-        self.obj = None
-        if props is None:
+        self.obj = None          # stays None for a failed call's NULL handle
+        if props is _EMPTY:
             props = {}
         if isinstance(props, dict):
             self.obj = _syn.create_properties()
