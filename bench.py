@@ -69,6 +69,7 @@ def gol_workload(side=2048):
         "state_bytes": 8 * n + 36,           # input + output + weights moved per e2e step
         "cpu_seconds": 12.0,
         "learning": False,
+        "single_kernel": True,               # every timed launch is the fused update
     }
 
 
@@ -414,6 +415,11 @@ def run_gb300(args, rank, world, local):
               file=sys.stderr)
     dom = kern.get(wl["kernel"])
     mean_us = float(dom["mean us"]) if dom else None
+    profiled_us = mean_us
+    if wl.get("single_kernel") and launches == T * args.steps:
+        # one launch per timestep, all of them the dominant kernel: its mean
+        # duration is the timed region's device time over its launches
+        mean_us = dev_ms * 1000.0 / launches
 
     # -- end to end through the public API with host buffers ----------------
     env = sg.Environment({"modules": []})
@@ -434,7 +440,7 @@ def run_gb300(args, rank, world, local):
     units = wl["units_per_timestep"] * T * args.steps
     out = {
         "dev_s": dev_max, "units": units * world, "wall_s": t_wall, "launches": launches,
-        "mean_us": mean_us, "clocks": clk, "kernels": kern,
+        "mean_us": mean_us, "profiled_us": profiled_us, "clocks": clk, "kernels": kern,
         "e2e_value": wl["units_per_timestep"] * T * e2e_steps * world / e2e_max,
         "e2e_steps": e2e_steps, "wl": wl, "T": T, "state_bytes": state_bytes,
     }
@@ -451,6 +457,9 @@ def run_batched(args, rank, world, local):
     wl = WORKLOADS[args.workload]()
     T = args.timesteps or wl["timesteps"]
     all_insts = batching.batch_instances(256, 3)
+    if args.instances:
+        # a smaller case of the same kernel (profiling): the largest instances
+        all_insts = sorted(all_insts, key=lambda i: -i["rows"] * i["cols"])[:args.instances]
     insts = [all_insts[i] for i in batching.shard_instances(all_insts, rank, world)]
     b = sg.Batch(insts)
     rep0 = b.report()
@@ -496,7 +505,7 @@ def run_batched(args, rank, world, local):
 
     # plain GPU path, one instance at a time (rank 0)
     plain = None
-    if rank == 0:
+    if rank == 0 and not args.no_plain:
         samples = []
         for side in PLAIN_SAMPLE_SIDES:
             net = sg.Network(sample_network(side))
@@ -583,6 +592,10 @@ def main():
     p.add_argument("--workload", default="gol", choices=sorted(WORKLOADS))
     p.add_argument("--timesteps", type=int, default=0, help="timesteps per bench step")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--instances", type=int, default=0,
+                   help="batched workload: only the N largest instances (profiling case)")
+    p.add_argument("--no-plain", action="store_true",
+                   help="batched workload: skip the one-instance-at-a-time plain GPU timing")
     p.add_argument("--cpu-worker", action="store_true", help=argparse.SUPPRESS)
     p.add_argument("--cpu-seconds", type=float, default=0.0, help=argparse.SUPPRESS)
     p.add_argument("--cpu-timesteps", type=int, default=0, help=argparse.SUPPRESS)
@@ -668,7 +681,8 @@ def main():
                      "frac": (achieved / peak) if achieved else None,
                      "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": wl["kernel"], "bytes_per_launch": wl["bytes_per_launch"],
-                     "mean_launch_us": r["mean_us"]},
+                     "mean_launch_us": r["mean_us"],
+                     "profiled_launch_us": r["profiled_us"]},
         "cpu_baseline": cb,
         "e2e": {"value": r["e2e_value"], "unit": wl["unit"],
                 "h2d_bytes_per_step": r["state_bytes"], "d2h_bytes_per_step": r["state_bytes"],
