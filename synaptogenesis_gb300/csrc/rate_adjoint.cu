@@ -1,0 +1,468 @@
+// Differentiable leaky-integrator rate network: forward cycle and its
+// hand-written adjoint (backpropagation through time with checkpoints).
+//
+// The reference has no differentiable model; its rate_encoding layer
+// (src/core/state/impl/rate_encoding_attributes.cpp:14-34) maps input to a
+// rate with no memory.  This model gives each neuron a leaky membrane:
+//
+//   layers l = 0..L-1 of rows x cols neurons (N), batch element b
+//   I_0[t]  = x[t]                                     (input sequence)
+//   I_l[t]  = sum_k W_l[i][k] * r_{l-1}[t-1][src(i,k)]  (l >= 1, convergent)
+//   d_l[t]  = -v_l[t-1] + I_l[t]
+//   v_l[t]  = v_l[t-1] + a_l * d_l[t],   a_l = dt / tau_l
+//   r_l[t]  = sigmoid(v_l[t]),           v_l[0] = 0
+//   y[t]    = R r_{L-1}[t]                             (readout, O outputs)
+//   loss    = sum_{t,b,o} (y[t][b][o] - target[b][o])^2 / (T B O)
+//
+// Convergent connections follow the reference's arborized geometry
+// (src/core/engine/kernel/synapse_kernel.h:384-421) with stride 1, spacing 1,
+// offset -field/2 and no wrap: out-of-range sources are skipped; weights are
+// in the CPU layout [destination][k], k = kernel row * field + kernel column.
+// Synchronous update as in the reference's cycle: every layer at t reads the
+// rates of t-1.
+//
+// Adjoint (lambda_l[t] = dloss/dv_l[t]):
+//   g_{L-1}[t] = R^T gy[t],  gy[t] = grad_loss * 2 (y[t] - target) / (T B O)
+//   g_l[t]     = sum over (j, k) with src(j,k) = i of W_{l+1}[j][k] a_{l+1} lambda_{l+1}[t+1][j]
+//   lambda_l[t] = r (1 - r) g_l[t] + (1 - a_l) lambda_l[t+1],  lambda[T+1] = 0
+//   dW_l[j][k] = a_l sum_{t,b} lambda_l[t][j] r_{l-1}[t-1][src(j,k)]
+//   dR[o][i]   = sum_{t,b} gy[t][o] r_{L-1}[t][i]
+//   dtau_l     = -(dt / tau_l^2) sum_{t,b,i} lambda_l[t][i] d_l[t][i]
+//   dx[t]      = a_0 lambda_0[t]
+// The forward pass stores v every `checkpoint` steps; the backward pass
+// recomputes each segment's states from its checkpoint (bit-identical: the
+// same kernel on the same inputs), then runs the adjoint back through it.
+// Every sum has a fixed order, so results are deterministic.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "../../include/syngen.h"
+#include "cuda_check.h"
+
+namespace sg {
+void set_last_error(const char* what);
+}
+
+namespace {
+using namespace sg;
+
+constexpr int kMaxOutputs = 16;
+constexpr int kTauBlocks = 64;
+
+struct Dims {
+    int L, rows, cols, N, field, h, K, O, B, T, k, nseg;
+    float dt;
+    long long S;   // L * B * N
+};
+
+__device__ __forceinline__ float sigmoid(float v) { return 1.0f / (1.0f + expf(-v)); }
+
+// One forward timestep of every layer and batch element.
+__global__ void __launch_bounds__(256) k_rate_step(Dims D, const float* __restrict__ x_t,
+                                                   const float* __restrict__ w,
+                                                   const float* __restrict__ tau,
+                                                   const float* __restrict__ v_prev,
+                                                   const float* __restrict__ r_prev,
+                                                   float* __restrict__ v_new,
+                                                   float* __restrict__ r_new,
+                                                   float* __restrict__ d_out) {
+    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= D.S) return;
+    const int l = (int)(idx / ((long long)D.B * D.N));
+    const int rem = (int)(idx - (long long)l * D.B * D.N);
+    const int b = rem / D.N, i = rem - b * D.N;
+    const float a = D.dt / __ldg(tau + l);
+    float I;
+    if (l == 0) {
+        I = __ldg(x_t + (long long)b * D.N + i);
+    } else {
+        const float* wr = w + ((long long)(l - 1) * D.N + i) * D.K;
+        const float* src = r_prev + ((long long)(l - 1) * D.B + b) * D.N;
+        const int ir = i / D.cols, ic = i - ir * D.cols;
+        I = 0.0f;
+        int k = 0;
+        for (int kr = 0; kr < D.field; ++kr) {
+            const int sr = ir - D.h + kr;
+            if (sr < 0 || sr >= D.rows) { k += D.field; continue; }
+            for (int kc = 0; kc < D.field; ++kc, ++k) {
+                const int sc = ic - D.h + kc;
+                if (sc < 0 || sc >= D.cols) continue;
+                I += __ldg(wr + k) * src[sr * D.cols + sc];
+            }
+        }
+    }
+    const float vp = v_prev[idx];
+    const float d = -vp + I;
+    const float vn = vp + a * d;
+    v_new[idx] = vn;
+    r_new[idx] = sigmoid(vn);
+    if (d_out) d_out[idx] = d;
+}
+
+// r = sigmoid(v) for a whole state (checkpoint reload / initial state).
+__global__ void k_rate_rates(long long S, const float* __restrict__ v, float* __restrict__ r) {
+    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < S) r[idx] = sigmoid(v[idx]);
+}
+
+// Readout of one timestep: one CTA per batch element; y[b][o] and the
+// element's squared error, each reduced in a fixed tree.
+__global__ void __launch_bounds__(256) k_rate_readout(Dims D, const float* __restrict__ r_last,
+                                                      const float* __restrict__ wo,
+                                                      const float* __restrict__ target,
+                                                      float* __restrict__ y_t,
+                                                      float* __restrict__ loss_t) {
+    __shared__ float part[kMaxOutputs][256];
+    const int b = blockIdx.x, tid = threadIdx.x;
+    const float* r = r_last + (long long)b * D.N;
+    float acc[kMaxOutputs];
+#pragma unroll
+    for (int o = 0; o < kMaxOutputs; ++o) acc[o] = 0.0f;
+    for (int i = tid; i < D.N; i += 256) {
+        const float ri = r[i];
+#pragma unroll
+        for (int o = 0; o < kMaxOutputs; ++o)
+            if (o < D.O) acc[o] += __ldg(wo + (long long)o * D.N + i) * ri;
+    }
+#pragma unroll
+    for (int o = 0; o < kMaxOutputs; ++o)
+        if (o < D.O) part[o][tid] = acc[o];
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (tid < s)
+            for (int o = 0; o < D.O; ++o) part[o][tid] += part[o][tid + s];
+        __syncthreads();
+    }
+    if (tid == 0) {
+        float e = 0.0f;
+        for (int o = 0; o < D.O; ++o) {
+            const float yo = part[o][0];
+            y_t[(long long)b * D.O + o] = yo;
+            const float diff = yo - target[(long long)b * D.O + o];
+            e += diff * diff;
+        }
+        loss_t[b] = e;
+    }
+}
+
+// loss = sum over (t, b) of the squared errors / (T B O), in (t, b) order.
+__global__ void k_rate_loss(Dims D, const float* __restrict__ loss_tb, float* __restrict__ loss) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    float s = 0.0f;
+    for (long long j = 0; j < (long long)D.T * D.B; ++j) s += loss_tb[j];
+    *loss = s / (float)((long long)D.T * D.B * D.O);
+}
+
+// Adjoint of one timestep for every layer and batch element: lambda[t] from
+// lambda[t+1] (the next layer's inputs at t+1 read the rates of t).
+__global__ void __launch_bounds__(256) k_rate_lambda(
+    Dims D, const float* __restrict__ w, const float* __restrict__ wo,
+    const float* __restrict__ tau, const float* __restrict__ y_t,
+    const float* __restrict__ target, float gscale, const float* __restrict__ r_t,
+    const float* __restrict__ lam_next, float* __restrict__ lam, float* __restrict__ dx_t) {
+    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= D.S) return;
+    const int l = (int)(idx / ((long long)D.B * D.N));
+    const int rem = (int)(idx - (long long)l * D.B * D.N);
+    const int b = rem / D.N, i = rem - b * D.N;
+    float g = 0.0f;
+    if (l == D.L - 1) {
+        for (int o = 0; o < D.O; ++o) {
+            const float gy = gscale * (__ldg(y_t + (long long)b * D.O + o) -
+                                       __ldg(target + (long long)b * D.O + o));
+            g += __ldg(wo + (long long)o * D.N + i) * gy;
+        }
+    } else {
+        // destinations j of layer l+1 whose window holds i: j = i + h - (kr, kc)
+        const float a1 = D.dt / __ldg(tau + l + 1);
+        const float* wl = w + (long long)l * D.N * D.K;        // weights into layer l+1
+        const float* ln = lam_next + ((long long)(l + 1) * D.B + b) * D.N;
+        const int ir = i / D.cols, ic = i - ir * D.cols;
+        for (int kr = 0; kr < D.field; ++kr) {
+            const int jr = ir + D.h - kr;
+            if (jr < 0 || jr >= D.rows) continue;
+            for (int kc = 0; kc < D.field; ++kc) {
+                const int jc = ic + D.h - kc;
+                if (jc < 0 || jc >= D.cols) continue;
+                const int j = jr * D.cols + jc;
+                g += __ldg(wl + (long long)j * D.K + kr * D.field + kc) * (a1 * ln[j]);
+            }
+        }
+    }
+    const float a = D.dt / __ldg(tau + l);
+    const float r = r_t[idx];
+    const float lv = r * (1.0f - r) * g + (1.0f - a) * lam_next[idx];
+    lam[idx] = lv;
+    if (l == 0 && dx_t) dx_t[(long long)b * D.N + i] = a * lv;
+}
+
+// dW over one segment: one thread per (layer >= 1, destination j, k); the
+// segment's timesteps (latest first) and batch elements in fixed order.
+__global__ void __launch_bounds__(256) k_rate_dw(Dims D, int nt, const float* __restrict__ tau,
+                                                 const float* __restrict__ seg_lam,
+                                                 const float* __restrict__ seg_r,
+                                                 float* __restrict__ dw) {
+    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long per = (long long)D.N * D.K;
+    if (idx >= (long long)(D.L - 1) * per) return;
+    const int l = 1 + (int)(idx / per);
+    const int rem = (int)(idx - (long long)(l - 1) * per);
+    const int j = rem / D.K, k = rem - j * D.K;
+    const int jr = j / D.cols, jc = j - jr * D.cols;
+    const int sr = jr - D.h + k / D.field, sc = jc - D.h + k % D.field;
+    if (sr < 0 || sr >= D.rows || sc < 0 || sc >= D.cols) return;
+    const int s = sr * D.cols + sc;
+    float acc = 0.0f;
+    for (int tt = nt - 1; tt >= 0; --tt) {
+        // lambda of step t = c + tt + 1 and the source rates of step t - 1
+        const float* lam = seg_lam + (long long)tt * D.S + (long long)l * D.B * D.N;
+        const float* r = seg_r + (long long)tt * D.S + (long long)(l - 1) * D.B * D.N;
+        for (int b = 0; b < D.B; ++b) acc += lam[(long long)b * D.N + j] * r[(long long)b * D.N + s];
+    }
+    dw[idx] += (D.dt / __ldg(tau + l)) * acc;
+}
+
+// dR over one segment: one thread per (output o, neuron i).
+__global__ void __launch_bounds__(256) k_rate_dwo(Dims D, int t0, int nt, const float* __restrict__ y,
+                                                  const float* __restrict__ target, float gscale,
+                                                  const float* __restrict__ seg_r,
+                                                  float* __restrict__ dwo) {
+    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)D.O * D.N) return;
+    const int o = (int)(idx / D.N), i = (int)(idx - (long long)o * D.N);
+    float acc = 0.0f;
+    for (int tt = nt - 1; tt >= 0; --tt) {
+        const int t = t0 + tt + 1;                      // 1-based step
+        const float* yt = y + (long long)(t - 1) * D.B * D.O;
+        const float* r = seg_r + (long long)(tt + 1) * D.S + (long long)(D.L - 1) * D.B * D.N;
+        for (int b = 0; b < D.B; ++b) {
+            const float gy = gscale * (yt[(long long)b * D.O + o] - target[(long long)b * D.O + o]);
+            acc += gy * r[(long long)b * D.N + i];
+        }
+    }
+    dwo[idx] += acc;
+}
+
+// Partial sums of lambda * d per layer over one segment: grid (kTauBlocks, L),
+// each block a fixed strided slice reduced in a fixed tree.
+__global__ void __launch_bounds__(256) k_rate_dtau_partial(Dims D, int seg, int nt,
+                                                           const float* __restrict__ seg_lam,
+                                                           const float* __restrict__ seg_d,
+                                                           float* __restrict__ part) {
+    __shared__ float sm[256];
+    const int l = blockIdx.y, tid = threadIdx.x;
+    const long long per = (long long)D.B * D.N;
+    const long long total = (long long)nt * per;
+    float acc = 0.0f;
+    for (long long e = (long long)blockIdx.x * 256 + tid; e < total; e += (long long)gridDim.x * 256) {
+        const long long tt = e / per, rem = e - tt * per;
+        const long long off = tt * D.S + (long long)l * per + rem;
+        acc += seg_lam[off] * seg_d[off];
+    }
+    sm[tid] = acc;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (tid < s) sm[tid] += sm[tid + s];
+        __syncthreads();
+    }
+    if (tid == 0) part[((long long)seg * D.L + l) * gridDim.x + blockIdx.x] = sm[0];
+}
+
+__global__ void k_rate_dtau_final(Dims D, const float* __restrict__ tau,
+                                  const float* __restrict__ part, float* __restrict__ dtau) {
+    const int l = threadIdx.x;
+    if (blockIdx.x != 0 || l >= D.L) return;
+    float s = 0.0f;
+    for (int seg = D.nseg - 1; seg >= 0; --seg)
+        for (int q = 0; q < kTauBlocks; ++q) s += part[((long long)seg * D.L + l) * kTauBlocks + q];
+    const float t = __ldg(tau + l);
+    dtau[l] = s * (-D.dt / (t * t));
+}
+
+Dims make_dims(const SgRateShape& s) {
+    if (s.layers < 1 || s.rows < 1 || s.cols < 1 || s.batch < 1 || s.steps < 1 ||
+        s.checkpoint < 1)
+        throw SgError("rate network: sizes must be positive");
+    if (s.outputs < 1 || s.outputs > kMaxOutputs)
+        throw SgError("rate network: outputs must lie in 1..16");
+    if (s.field < 1 || s.field % 2 == 0) throw SgError("rate network: field must be odd");
+    if (!(s.dt > 0.0f)) throw SgError("rate network: dt must be positive");
+    Dims D;
+    D.L = s.layers;
+    D.rows = s.rows;
+    D.cols = s.cols;
+    D.N = s.rows * s.cols;
+    D.field = s.field;
+    D.h = s.field / 2;
+    D.K = s.field * s.field;
+    D.O = s.outputs;
+    D.B = s.batch;
+    D.T = s.steps;
+    D.k = s.checkpoint;
+    D.nseg = (s.steps + s.checkpoint - 1) / s.checkpoint;
+    D.dt = s.dt;
+    D.S = (long long)D.L * D.B * D.N;
+    return D;
+}
+
+// Workspace layout (floats): checkpoints [nseg][S], segment states v, r
+// [k+1][S], drives d and adjoints lambda [k][S], the lambda carried across
+// segments [S], outputs y [T][B][O], squared errors [T][B], tau partials.
+struct Work {
+    float *ckpt, *seg_v, *seg_r, *seg_d, *seg_lam, *carry, *y, *loss_tb, *tau_part;
+    long long floats;
+};
+
+Work carve(const Dims& D, void* base) {
+    Work w{};
+    float* p = static_cast<float*>(base);
+    auto take = [&](long long n) {
+        float* q = p;
+        n = (n + 63) / 64 * 64;       // 256-byte aligned pieces
+        if (p) p += n;
+        w.floats += n;
+        return q;
+    };
+    w.ckpt = take((long long)D.nseg * D.S);
+    w.seg_v = take((long long)(D.k + 1) * D.S);
+    w.seg_r = take((long long)(D.k + 1) * D.S);
+    w.seg_d = take((long long)D.k * D.S);
+    w.seg_lam = take((long long)D.k * D.S);
+    w.carry = take(D.S);
+    w.y = take((long long)D.T * D.B * D.O);
+    w.loss_tb = take((long long)D.T * D.B);
+    w.tau_part = take((long long)D.nseg * D.L * kTauBlocks);
+    return w;
+}
+
+unsigned grid_of(long long n) { return (unsigned)((n + 255) / 256); }
+
+void forward(const Dims& D, const float* x, const float* w, const float* wo, const float* tau,
+             const float* target, float* y_out, float* loss, void* ws, cudaStream_t st) {
+    Work W = carve(D, ws);
+    float* v[2] = {W.seg_v, W.seg_v + D.S};
+    float* r[2] = {W.seg_r, W.seg_r + D.S};
+    SG_CUDA(cudaMemsetAsync(v[0], 0, D.S * sizeof(float), st));
+    k_rate_rates<<<grid_of(D.S), 256, 0, st>>>(D.S, v[0], r[0]);
+    SG_LAUNCH_CHECK();
+    SG_CUDA(cudaMemsetAsync(W.ckpt, 0, D.S * sizeof(float), st));
+    for (int t = 1; t <= D.T; ++t) {
+        const int p = (t - 1) & 1, q = t & 1;
+        k_rate_step<<<grid_of(D.S), 256, 0, st>>>(D, x + (long long)(t - 1) * D.B * D.N, w, tau,
+                                                  v[p], r[p], v[q], r[q], nullptr);
+        SG_LAUNCH_CHECK();
+        k_rate_readout<<<D.B, 256, 0, st>>>(D, r[q] + (long long)(D.L - 1) * D.B * D.N, wo,
+                                            target, W.y + (long long)(t - 1) * D.B * D.O,
+                                            W.loss_tb + (long long)(t - 1) * D.B);
+        SG_LAUNCH_CHECK();
+        if (t % D.k == 0 && t < D.T)
+            SG_CUDA(cudaMemcpyAsync(W.ckpt + (long long)(t / D.k) * D.S, v[q],
+                                    D.S * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    }
+    k_rate_loss<<<1, 32, 0, st>>>(D, W.loss_tb, loss);
+    SG_LAUNCH_CHECK();
+    if (y_out)
+        SG_CUDA(cudaMemcpyAsync(y_out, W.y, (size_t)D.T * D.B * D.O * sizeof(float),
+                                cudaMemcpyDeviceToDevice, st));
+}
+
+void backward(const Dims& D, const float* x, const float* w, const float* wo, const float* tau,
+              const float* target, float grad_loss, void* ws, float* dw, float* dwo,
+              float* dtau, float* dx, cudaStream_t st) {
+    Work W = carve(D, ws);
+    const float gscale = grad_loss * 2.0f / (float)((long long)D.T * D.B * D.O);
+    if (D.L > 1)
+        SG_CUDA(cudaMemsetAsync(dw, 0, (size_t)(D.L - 1) * D.N * D.K * sizeof(float), st));
+    SG_CUDA(cudaMemsetAsync(dwo, 0, (size_t)D.O * D.N * sizeof(float), st));
+    SG_CUDA(cudaMemsetAsync(W.carry, 0, D.S * sizeof(float), st));
+    for (int seg = D.nseg - 1; seg >= 0; --seg) {
+        const int c = seg * D.k, nt = std::min(D.k, D.T - c);
+        SG_CUDA(cudaMemcpyAsync(W.seg_v, W.ckpt + (long long)seg * D.S, D.S * sizeof(float),
+                                cudaMemcpyDeviceToDevice, st));
+        k_rate_rates<<<grid_of(D.S), 256, 0, st>>>(D.S, W.seg_v, W.seg_r);
+        SG_LAUNCH_CHECK();
+        for (int tt = 1; tt <= nt; ++tt) {
+            k_rate_step<<<grid_of(D.S), 256, 0, st>>>(
+                D, x + (long long)(c + tt - 1) * D.B * D.N, w, tau, W.seg_v + (tt - 1) * D.S,
+                W.seg_r + (tt - 1) * D.S, W.seg_v + tt * D.S, W.seg_r + tt * D.S,
+                W.seg_d + (tt - 1) * D.S);
+            SG_LAUNCH_CHECK();
+        }
+        for (int tt = nt; tt >= 1; --tt) {
+            const int t = c + tt;
+            const float* lam_next = tt == nt ? W.carry : W.seg_lam + (long long)tt * D.S;
+            k_rate_lambda<<<grid_of(D.S), 256, 0, st>>>(
+                D, w, wo, tau, W.y + (long long)(t - 1) * D.B * D.O, target, gscale,
+                W.seg_r + (long long)tt * D.S, lam_next, W.seg_lam + (long long)(tt - 1) * D.S,
+                dx ? dx + (long long)(t - 1) * D.B * D.N : nullptr);
+            SG_LAUNCH_CHECK();
+        }
+        SG_CUDA(cudaMemcpyAsync(W.carry, W.seg_lam, D.S * sizeof(float),
+                                cudaMemcpyDeviceToDevice, st));
+        if (D.L > 1) {
+            k_rate_dw<<<grid_of((long long)(D.L - 1) * D.N * D.K), 256, 0, st>>>(
+                D, nt, tau, W.seg_lam, W.seg_r, dw);
+            SG_LAUNCH_CHECK();
+        }
+        k_rate_dwo<<<grid_of((long long)D.O * D.N), 256, 0, st>>>(D, c, nt, W.y, target, gscale,
+                                                                  W.seg_r, dwo);
+        SG_LAUNCH_CHECK();
+        k_rate_dtau_partial<<<dim3(kTauBlocks, D.L), 256, 0, st>>>(D, seg, nt, W.seg_lam,
+                                                                   W.seg_d, W.tau_part);
+        SG_LAUNCH_CHECK();
+    }
+    k_rate_dtau_final<<<1, 32, 0, st>>>(D, tau, W.tau_part, dtau);
+    SG_LAUNCH_CHECK();
+}
+
+}  // namespace
+
+extern "C" {
+
+long long sg_rate_workspace_bytes(const SgRateShape* shape) {
+    if (!shape) return SG_RATE_EINVAL;
+    try {
+        return carve(make_dims(*shape), nullptr).floats * (long long)sizeof(float);
+    } catch (const std::exception& e) {
+        sg::set_last_error(e.what());
+    }
+    return SG_RATE_EINVAL;
+}
+
+int sg_rate_forward(const SgRateShape* shape, const float* x, const float* weights,
+                    const float* readout, const float* tau, const float* target, float* y,
+                    float* loss, void* workspace, void* stream) {
+    if (!shape || !x || !readout || !tau || !target || !loss || !workspace) return SG_RATE_EINVAL;
+    try {
+        Dims D = make_dims(*shape);
+        if (D.L > 1 && !weights) return SG_RATE_EINVAL;
+        forward(D, x, weights, readout, tau, target, y, loss, workspace,
+                static_cast<cudaStream_t>(stream));
+        return 0;
+    } catch (const std::exception& e) {
+        sg::set_last_error(e.what());
+    }
+    return SG_RATE_ECUDA;
+}
+
+int sg_rate_backward(const SgRateShape* shape, const float* x, const float* weights,
+                     const float* readout, const float* tau, const float* target,
+                     float grad_loss, void* workspace, float* d_weights, float* d_readout,
+                     float* d_tau, float* d_x, void* stream) {
+    if (!shape || !x || !readout || !tau || !target || !workspace || !d_readout || !d_tau)
+        return SG_RATE_EINVAL;
+    try {
+        Dims D = make_dims(*shape);
+        if (D.L > 1 && (!weights || !d_weights)) return SG_RATE_EINVAL;
+        backward(D, x, weights, readout, tau, target, grad_loss, workspace, d_weights, d_readout,
+                 d_tau, d_x, static_cast<cudaStream_t>(stream));
+        return 0;
+    } catch (const std::exception& e) {
+        sg::set_last_error(e.what());
+    }
+    return SG_RATE_ECUDA;
+}
+
+}  // extern "C"
