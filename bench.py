@@ -163,7 +163,40 @@ def batched_workload():
     }
 
 
-WORKLOADS = {"gol": gol_workload, "iz_plastic": iz_plastic_workload, "batched": batched_workload}
+def rate_workload():
+    """Differentiable rate network: forward pass and hand-written adjoint."""
+    return {
+        "name": "rate_adjoint",
+        "desc": "3 x 64x64 leaky-integrator rate layers (tau 10 ms learnable, dt 1 ms, sigmoid "
+                "rate), convergent 5x5 N(0,0.1), readout 4096->10 N(0,0.1), batch 64 x 100 "
+                "steps of N(0,1) input, MSE to U(0,1) targets (seed 4), checkpoint every 10",
+        "unit": "sequence-timesteps/s",
+        "dtype": "f32",
+        "kernel": "forward pass (k_rate_step + k_rate_readout per timestep)",
+        "cpu_seconds": 12.0,
+        "rate": True,
+    }
+
+
+RATE_CFG = dict(layers=3, rows=64, cols=64, field=5, outputs=10, batch=64, steps=100,
+                checkpoint=10)
+
+
+def rate_inputs(batch=64, seed=4):
+    """Seeded inputs and parameters of the rate workload (float32 numpy)."""
+    import numpy as np
+    c = RATE_CFG
+    N = c["rows"] * c["cols"]
+    rng = np.random.default_rng(seed)
+    return {"x": rng.normal(0, 1, (c["steps"], batch, N)).astype(np.float32),
+            "weights": rng.normal(0, 0.1, (c["layers"] - 1, N, c["field"] ** 2)).astype(np.float32),
+            "readout": rng.normal(0, 0.1, (c["outputs"], N)).astype(np.float32),
+            "tau": np.full(c["layers"], 10.0, np.float32),
+            "target": rng.uniform(0, 1, (batch, c["outputs"])).astype(np.float32)}
+
+
+WORKLOADS = {"gol": gol_workload, "iz_plastic": iz_plastic_workload, "batched": batched_workload,
+             "rate_adjoint": rate_workload}
 
 # Sides of the instances timed one at a time (plain GPU path / reference CPU
 # path); the per-timestep time is fitted as alpha + beta * (recurrent synapses)
@@ -279,6 +312,25 @@ def barrier(world):
 def cpu_worker(args):
     """Runs in a child process with SYNGEN_LIB set; prints one JSON object."""
     wl = WORKLOADS[args.workload]()
+    if wl.get("rate"):
+        # FP64 restatement (numpy, one thread): forward + adjoint of a sample of
+        # the batch, the same 100 steps
+        from oracle import rate_adjoint as ra
+        sample_b = 8
+        p = rate_inputs(batch=sample_b)
+        shape = dict(RATE_CFG, batch=sample_b, dt=1.0)
+        t0 = time.perf_counter()
+        reps = 0
+        while True:
+            ra.adjoint(shape, p["x"], p["weights"], p["readout"], p["tau"], p["target"])
+            reps += 1
+            if time.perf_counter() - t0 >= args.cpu_seconds:
+                break
+        dt = time.perf_counter() - t0
+        print(json.dumps({"value": sample_b * RATE_CFG["steps"] * reps / dt, "seconds": dt,
+                          "timesteps": RATE_CFG["steps"] * reps, "reps": reps,
+                          "sample_batch": sample_b}))
+        return
     from synaptogenesis_gb300 import syngen as sg
     sg.set_warnings(False)
     if wl.get("batched"):
@@ -328,6 +380,22 @@ def cpu_worker(args):
 
 
 def cpu_baseline(workload, seconds, timesteps=0):
+    if WORKLOADS[workload]().get("rate"):
+        env = dict(os.environ, OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1",
+                   MKL_NUM_THREADS="1")
+        cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--cpu-worker", "--workload",
+               workload, "--cpu-seconds", str(seconds)]
+        r = subprocess.run(cmd, env=env, capture_output=True, text=True, timeout=900)
+        if r.returncode != 0:
+            return {"value": None, "unit": "sequence-timesteps/s", "cores": 1, "kind": "port",
+                    "sample": "failed: " + r.stderr[-300:]}
+        out = json.loads(r.stdout.strip().splitlines()[-1])
+        return {"value": out["value"], "unit": "sequence-timesteps/s", "cores": 1, "kind": "port",
+                "sample": "FP64 numpy restatement (oracle/rate_adjoint.py; the reference has no "
+                          "differentiable model), forward + adjoint of %d sequences x 100 steps, "
+                          "%d repetitions in %.1f s, one thread"
+                          % (out["sample_batch"], out["reps"], out["seconds"]),
+                "timesteps": out["timesteps"], "seconds": out["seconds"]}
     from oracle import build_ref
     lib = build_ref.build()
     cores = os.cpu_count() or 1
@@ -583,6 +651,124 @@ def batched_line(args, world, r, wl, cb):
     }
 
 
+def run_rate(args, rank, world, local):
+    """Forward + adjoint of the rate workload, device-resident and end to end
+    through the torch.autograd wrapper with host tensors; also the forward
+    alone and the same work run one sequence at a time."""
+    import torch
+    from synaptogenesis_gb300 import syngen as sg
+    c = RATE_CFG
+    net = sg.RateNetwork(**c)
+    host = rate_inputs()
+    dev = {k: torch.tensor(v, device="cuda") for k, v in host.items()}
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+
+    def fwd_bwd(net_, d):
+        loss, ws = net_._forward(d["x"], d["weights"], d["readout"], d["tau"], d["target"])
+        net_._backward(ws, 1.0, d["x"], d["weights"], d["readout"], d["tau"], d["target"],
+                       want_dx=False)
+        return loss
+
+    def timed(fn, reps):
+        out = []
+        for _ in range(reps):
+            flush.add_(1.0)                       # L2 flush, outside the events
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            out.append((e0, e1))
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in out) / 1000.0
+
+    for _ in range(args.warmup):
+        fwd_bwd(net, dev)
+    torch.cuda.synchronize()
+    barrier(world)
+    gpu_index = os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0]
+    clocks = ClockSampler(gpu_index)
+    dev_s = timed(lambda: fwd_bwd(net, dev), args.steps)
+    barrier(world)
+    clk = clocks.stop()
+    fwd_s = timed(lambda: net._forward(dev["x"], dev["weights"], dev["readout"], dev["tau"],
+                                       dev["target"]), args.steps)
+
+    # one sequence at a time (batch 1, 64 calls) for the same work
+    one = sg.RateNetwork(**dict(c, batch=1))
+    singles = [{"x": dev["x"][:, b:b + 1].contiguous(), "weights": dev["weights"],
+                "readout": dev["readout"], "tau": dev["tau"],
+                "target": dev["target"][b:b + 1].contiguous()} for b in range(c["batch"])]
+    fwd_bwd(one, singles[0])
+    one_s = timed(lambda: [fwd_bwd(one, d) for d in singles], 1)
+
+    # end to end: host inputs and parameters in, loss and gradients out
+    e2e_steps = max(1, min(args.steps, 3))
+    h2d = sum(v.nbytes for v in host.values())
+    pinned = {k: torch.from_numpy(v).pin_memory() for k, v in host.items()}
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        t = {k: v.to("cuda", non_blocking=True) for k, v in pinned.items()}
+        for k in ("weights", "readout", "tau"):
+            t[k].requires_grad_(True)
+        loss = net.loss(t["x"], t["weights"], t["readout"], t["tau"], t["target"])
+        loss.backward()
+        grads = [t[k].grad.cpu() for k in ("weights", "readout", "tau")] + [loss.detach().cpu()]
+    e2e_s = time.perf_counter() - t0
+    d2h = sum(g.numel() * 4 for g in grads)
+
+    per_step = c["batch"] * c["steps"]
+    dev_max, e2e_max = reduce_max([dev_s, e2e_s], world)
+    S = c["layers"] * c["batch"] * c["rows"] * c["cols"]
+    N = c["rows"] * c["cols"]
+    fwd_bytes = 16 * S + 4 * c["batch"] * N + 4 * ((c["layers"] - 1) * N * c["field"] ** 2
+                                                   + c["outputs"] * N)
+    return {"dev_s": dev_max, "units": per_step * args.steps * world, "clocks": clk,
+            "fwd_s": fwd_s, "one_s": one_s, "e2e_value": per_step * e2e_steps * world / e2e_max,
+            "e2e_steps": e2e_steps, "h2d": h2d, "d2h": d2h,
+            "fwd_us_per_timestep": fwd_s * 1e6 / (args.steps * c["steps"]),
+            "fwd_bytes_per_timestep": fwd_bytes, "loss": float(loss)}
+
+
+def rate_line(args, world, r, wl, cb):
+    peak, peak_kind = measured_peak()
+    c = RATE_CFG
+    per_step = c["batch"] * c["steps"]
+    achieved = r["fwd_bytes_per_timestep"] / (r["fwd_us_per_timestep"] * 1e-6) / 1e9
+    # kernel launches per forward + adjoint: forward 2 per timestep (step,
+    # readout) + initial rates + loss; backward 2 per timestep (recompute,
+    # adjoint) + per segment rates, dW, dR, dtau partials + the dtau total
+    nseg = -(-c["steps"] // c["checkpoint"])
+    launches = (2 * c["steps"] + 2) + (2 * c["steps"] + 4 * nseg + 1)
+    return {
+        "metric": "sequence-timesteps/s (rate forward + adjoint)",
+        "value": r["units"] / r["dev_s"], "unit": wl["unit"], "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * r["dev_s"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": wl["dtype"],
+        "data": "synthetic (seeded numpy)",
+        "config": {"workload": wl["desc"], "sequence_timesteps_per_step": per_step,
+                   "forward_only_sequence_timesteps_per_s": per_step * args.steps / r["fwd_s"],
+                   "one_sequence_at_a_time_sequence_timesteps_per_s": per_step / r["one_s"],
+                   "loss": r["loss"],
+                   "l2": "flushed between steps (256 MiB write outside the timed events); the "
+                         "state (3 MB per timestep) is L2-resident within a step",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                     "kernel": wl["kernel"], "bytes_per_launch": r["fwd_bytes_per_timestep"],
+                     "mean_launch_us": r["fwd_us_per_timestep"]},
+        "cpu_baseline": cb,
+        "e2e": {"value": r["e2e_value"], "unit": wl["unit"], "h2d_bytes_per_step": r["h2d"],
+                "d2h_bytes_per_step": r["d2h"], "steps": r["e2e_steps"],
+                "note": "torch.autograd path: pinned host inputs and parameters copied in, "
+                        "loss.backward(), gradients and loss copied out"},
+        "clocks": r["clocks"],
+        "gpu_launches": launches * args.steps,
+    }
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -613,13 +799,14 @@ def main():
         dist.init_process_group("gloo")
     wl = WORKLOADS[args.workload]()
     metric = ("instance-timesteps/s (batched)" if wl.get("batched")
+              else "sequence-timesteps/s (rate forward + adjoint)" if wl.get("rate")
               else "synapse-updates/s (%s)" % wl["name"])
 
     if args.impl == "reference":
         if rank != 0:
             return
         from oracle import build_ref
-        if build_ref.build() is None:
+        if not wl.get("rate") and build_ref.build() is None:
             print(json.dumps({"impl": "reference", "unavailable": "reference sources absent"}))
             return
         # each bench step: a bounded sample of the workload on all host cores
@@ -642,6 +829,13 @@ def main():
         print(json.dumps(line))
         return
 
+    if wl.get("rate"):
+        r = run_rate(args, rank, world, local)
+        if rank != 0:
+            return
+        cb = None if args.no_cpu_baseline else cpu_baseline(args.workload, wl["cpu_seconds"])
+        print(json.dumps(rate_line(args, world, r, wl, cb)))
+        return
     if wl.get("batched"):
         r = run_batched(args, rank, world, local)
         if rank != 0:

@@ -229,6 +229,48 @@ void* sg_batch_stream(SG_BATCH batch);
 int sg_batch_synchronize(SG_BATCH batch);
 void sg_batch_destroy(SG_BATCH batch);
 
+/* Differentiable leaky-integrator rate network.  No counterpart in the
+ * reference, whose rate_encoding layer has no memory
+ * (src/core/state/impl/rate_encoding_attributes.cpp:14-34).
+ *
+ * `layers` layers of rows x cols neurons; layer 0 is driven by the input
+ * sequence x, layer l >= 1 by a convergent connection from layer l-1
+ * (field x field, stride 1, offset -field/2, no wrap: out-of-range sources are
+ * skipped); every layer integrates v += (dt / tau_l) (-v + I), rate
+ * sigmoid(v), v = 0 at the start; every layer reads the previous step's rates.
+ * A readout R (outputs x N) of the last layer's rates gives y[t]; the loss is
+ * the mean over (t, b, o) of (y[t][b][o] - target[b][o])^2.
+ * Device arrays, float32:
+ *   x        [steps][batch][rows*cols]
+ *   weights  [layers-1][rows*cols][field*field]  (destination-major, k row-major)
+ *   readout  [outputs][rows*cols]
+ *   tau      [layers]
+ *   target   [batch][outputs]
+ *   y        [steps][batch][outputs] (optional output)
+ *   loss     one float
+ * The workspace (sg_rate_workspace_bytes, device memory owned by the caller)
+ * keeps the forward pass's checkpoints (v every `checkpoint` steps) for the
+ * backward pass, which recomputes each segment from its checkpoint and runs
+ * the hand-written adjoint back through it.  d_weights, d_readout, d_tau (and
+ * d_x, or NULL) receive grad_loss * dloss/d(parameter).  Work is asynchronous
+ * on `stream` (a cudaStream_t; NULL = default stream).  Returns 0 or a
+ * negative SG_RATE_* code (sg_last_error). */
+typedef struct SgRateShape {
+    int layers, rows, cols, field, outputs, batch, steps, checkpoint;
+    float dt;
+} SgRateShape;
+
+#define SG_RATE_EINVAL (-1)
+#define SG_RATE_ECUDA (-3)
+long long sg_rate_workspace_bytes(const SgRateShape* shape);
+int sg_rate_forward(const SgRateShape* shape, const float* x, const float* weights,
+                    const float* readout, const float* tau, const float* target, float* y,
+                    float* loss, void* workspace, void* stream);
+int sg_rate_backward(const SgRateShape* shape, const float* x, const float* weights,
+                     const float* readout, const float* tau, const float* target,
+                     float grad_loss, void* workspace, float* d_weights, float* d_readout,
+                     float* d_tau, float* d_x, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

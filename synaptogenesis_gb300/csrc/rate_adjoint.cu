@@ -147,12 +147,21 @@ __global__ void __launch_bounds__(256) k_rate_readout(Dims D, const float* __res
     }
 }
 
-// loss = sum over (t, b) of the squared errors / (T B O), in (t, b) order.
-__global__ void k_rate_loss(Dims D, const float* __restrict__ loss_tb, float* __restrict__ loss) {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+// loss = sum over (t, b) of the squared errors / (T B O): 256 strided
+// partial sums reduced in a fixed tree.
+__global__ void __launch_bounds__(256) k_rate_loss(Dims D, const float* __restrict__ loss_tb,
+                                                   float* __restrict__ loss) {
+    __shared__ float sm[256];
+    const int tid = threadIdx.x;
     float s = 0.0f;
-    for (long long j = 0; j < (long long)D.T * D.B; ++j) s += loss_tb[j];
-    *loss = s / (float)((long long)D.T * D.B * D.O);
+    for (long long j = tid; j < (long long)D.T * D.B; j += 256) s += loss_tb[j];
+    sm[tid] = s;
+    __syncthreads();
+    for (int k = 128; k > 0; k >>= 1) {
+        if (tid < k) sm[tid] += sm[tid + k];
+        __syncthreads();
+    }
+    if (tid == 0) *loss = sm[0] / (float)((long long)D.T * D.B * D.O);
 }
 
 // Adjoint of one timestep for every layer and batch element: lambda[t] from
@@ -198,8 +207,9 @@ __global__ void __launch_bounds__(256) k_rate_lambda(
     if (l == 0 && dx_t) dx_t[(long long)b * D.N + i] = a * lv;
 }
 
-// dW over one segment: one thread per (layer >= 1, destination j, k); the
-// segment's timesteps (latest first) and batch elements in fixed order.
+// dW over one segment: one thread per (layer >= 1, destination j, k).  The
+// accumulator takes one timestep's batch sum at a time, latest step first, so
+// the result does not depend on where the segments start.
 __global__ void __launch_bounds__(256) k_rate_dw(Dims D, int nt, const float* __restrict__ tau,
                                                  const float* __restrict__ seg_lam,
                                                  const float* __restrict__ seg_r,
@@ -214,14 +224,17 @@ __global__ void __launch_bounds__(256) k_rate_dw(Dims D, int nt, const float* __
     const int sr = jr - D.h + k / D.field, sc = jc - D.h + k % D.field;
     if (sr < 0 || sr >= D.rows || sc < 0 || sc >= D.cols) return;
     const int s = sr * D.cols + sc;
-    float acc = 0.0f;
+    const float a = D.dt / __ldg(tau + l);
+    float acc = dw[idx];
     for (int tt = nt - 1; tt >= 0; --tt) {
         // lambda of step t = c + tt + 1 and the source rates of step t - 1
         const float* lam = seg_lam + (long long)tt * D.S + (long long)l * D.B * D.N;
         const float* r = seg_r + (long long)tt * D.S + (long long)(l - 1) * D.B * D.N;
-        for (int b = 0; b < D.B; ++b) acc += lam[(long long)b * D.N + j] * r[(long long)b * D.N + s];
+        float st = 0.0f;
+        for (int b = 0; b < D.B; ++b) st += lam[(long long)b * D.N + j] * r[(long long)b * D.N + s];
+        acc += a * st;
     }
-    dw[idx] += (D.dt / __ldg(tau + l)) * acc;
+    dw[idx] = acc;
 }
 
 // dR over one segment: one thread per (output o, neuron i).
@@ -232,53 +245,57 @@ __global__ void __launch_bounds__(256) k_rate_dwo(Dims D, int t0, int nt, const 
     long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)D.O * D.N) return;
     const int o = (int)(idx / D.N), i = (int)(idx - (long long)o * D.N);
-    float acc = 0.0f;
+    float acc = dwo[idx];
     for (int tt = nt - 1; tt >= 0; --tt) {
         const int t = t0 + tt + 1;                      // 1-based step
         const float* yt = y + (long long)(t - 1) * D.B * D.O;
         const float* r = seg_r + (long long)(tt + 1) * D.S + (long long)(D.L - 1) * D.B * D.N;
+        float st = 0.0f;
         for (int b = 0; b < D.B; ++b) {
             const float gy = gscale * (yt[(long long)b * D.O + o] - target[(long long)b * D.O + o]);
-            acc += gy * r[(long long)b * D.N + i];
+            st += gy * r[(long long)b * D.N + i];
         }
+        acc += st;
     }
-    dwo[idx] += acc;
+    dwo[idx] = acc;
 }
 
-// Partial sums of lambda * d per layer over one segment: grid (kTauBlocks, L),
-// each block a fixed strided slice reduced in a fixed tree.
-__global__ void __launch_bounds__(256) k_rate_dtau_partial(Dims D, int seg, int nt,
+// Partial sums of lambda * d per (timestep, layer): grid (kTauBlocks, L, nt),
+// each block a fixed strided slice of the batch x neurons reduced in a fixed
+// tree, written to part[t][l][block].
+__global__ void __launch_bounds__(256) k_rate_dtau_partial(Dims D, int t0,
                                                            const float* __restrict__ seg_lam,
                                                            const float* __restrict__ seg_d,
                                                            float* __restrict__ part) {
     __shared__ float sm[256];
-    const int l = blockIdx.y, tid = threadIdx.x;
+    const int l = blockIdx.y, tt = blockIdx.z, tid = threadIdx.x;
     const long long per = (long long)D.B * D.N;
-    const long long total = (long long)nt * per;
+    const long long off = (long long)tt * D.S + (long long)l * per;
     float acc = 0.0f;
-    for (long long e = (long long)blockIdx.x * 256 + tid; e < total; e += (long long)gridDim.x * 256) {
-        const long long tt = e / per, rem = e - tt * per;
-        const long long off = tt * D.S + (long long)l * per + rem;
-        acc += seg_lam[off] * seg_d[off];
-    }
+    for (long long e = (long long)blockIdx.x * 256 + tid; e < per; e += (long long)gridDim.x * 256)
+        acc += seg_lam[off + e] * seg_d[off + e];
     sm[tid] = acc;
     __syncthreads();
     for (int s = 128; s > 0; s >>= 1) {
         if (tid < s) sm[tid] += sm[tid + s];
         __syncthreads();
     }
-    if (tid == 0) part[((long long)seg * D.L + l) * gridDim.x + blockIdx.x] = sm[0];
+    if (tid == 0) part[((long long)(t0 + tt) * D.L + l) * kTauBlocks + blockIdx.x] = sm[0];
 }
 
+// dtau_l = -(dt / tau_l^2) * sum over timesteps (latest first) of the step sums.
 __global__ void k_rate_dtau_final(Dims D, const float* __restrict__ tau,
                                   const float* __restrict__ part, float* __restrict__ dtau) {
     const int l = threadIdx.x;
     if (blockIdx.x != 0 || l >= D.L) return;
     float s = 0.0f;
-    for (int seg = D.nseg - 1; seg >= 0; --seg)
-        for (int q = 0; q < kTauBlocks; ++q) s += part[((long long)seg * D.L + l) * kTauBlocks + q];
-    const float t = __ldg(tau + l);
-    dtau[l] = s * (-D.dt / (t * t));
+    for (int t = D.T - 1; t >= 0; --t) {
+        float st = 0.0f;
+        for (int q = 0; q < kTauBlocks; ++q) st += part[((long long)t * D.L + l) * kTauBlocks + q];
+        s += st;
+    }
+    const float tv = __ldg(tau + l);
+    dtau[l] = s * (-D.dt / (tv * tv));
 }
 
 Dims make_dims(const SgRateShape& s) {
@@ -333,7 +350,7 @@ Work carve(const Dims& D, void* base) {
     w.carry = take(D.S);
     w.y = take((long long)D.T * D.B * D.O);
     w.loss_tb = take((long long)D.T * D.B);
-    w.tau_part = take((long long)D.nseg * D.L * kTauBlocks);
+    w.tau_part = take((long long)D.T * D.L * kTauBlocks);
     return w;
 }
 
@@ -361,7 +378,7 @@ void forward(const Dims& D, const float* x, const float* w, const float* wo, con
             SG_CUDA(cudaMemcpyAsync(W.ckpt + (long long)(t / D.k) * D.S, v[q],
                                     D.S * sizeof(float), cudaMemcpyDeviceToDevice, st));
     }
-    k_rate_loss<<<1, 32, 0, st>>>(D, W.loss_tb, loss);
+    k_rate_loss<<<1, 256, 0, st>>>(D, W.loss_tb, loss);
     SG_LAUNCH_CHECK();
     if (y_out)
         SG_CUDA(cudaMemcpyAsync(y_out, W.y, (size_t)D.T * D.B * D.O * sizeof(float),
@@ -409,8 +426,8 @@ void backward(const Dims& D, const float* x, const float* w, const float* wo, co
         k_rate_dwo<<<grid_of((long long)D.O * D.N), 256, 0, st>>>(D, c, nt, W.y, target, gscale,
                                                                   W.seg_r, dwo);
         SG_LAUNCH_CHECK();
-        k_rate_dtau_partial<<<dim3(kTauBlocks, D.L), 256, 0, st>>>(D, seg, nt, W.seg_lam,
-                                                                   W.seg_d, W.tau_part);
+        k_rate_dtau_partial<<<dim3(kTauBlocks, D.L, nt), 256, 0, st>>>(D, c, W.seg_lam, W.seg_d,
+                                                                       W.tau_part);
         SG_LAUNCH_CHECK();
     }
     k_rate_dtau_final<<<1, 32, 0, st>>>(D, tau, W.tau_part, dtau);

@@ -169,7 +169,22 @@ def _load_library(path=None):
         lib.sg_batch_synchronize.argtypes = (c_void_p,)
         lib.sg_batch_synchronize.restype = c_int
         lib.sg_batch_destroy.argtypes = (c_void_p,)
+    if hasattr(lib, "sg_rate_forward"):
+        lib.sg_rate_workspace_bytes.argtypes = (POINTER(RateShape),)
+        lib.sg_rate_workspace_bytes.restype = c_longlong
+        lib.sg_rate_forward.argtypes = (POINTER(RateShape),) + (c_void_p,) * 9
+        lib.sg_rate_forward.restype = c_int
+        lib.sg_rate_backward.argtypes = ((POINTER(RateShape),) + (c_void_p,) * 5 + (c_float,)
+                                         + (c_void_p,) * 6)
+        lib.sg_rate_backward.restype = c_int
     return lib, path
+
+
+class RateShape(Structure):
+    """SgRateShape of include/syngen.h."""
+    _fields_ = [("layers", c_int), ("rows", c_int), ("cols", c_int), ("field", c_int),
+                ("outputs", c_int), ("batch", c_int), ("steps", c_int), ("checkpoint", c_int),
+                ("dt", c_float)]
 
 
 class BatchInstance(Structure):
@@ -587,6 +602,103 @@ class Batch:
 
     def __exit__(self, *exc):
         self.close()
+
+
+class RateNetwork:
+    """Differentiable leaky-integrator rate network (sg_rate_* in
+    include/syngen.h): ``layers`` layers of rows x cols neurons, convergent
+    field x field connections between consecutive layers, a readout of the
+    last layer, per-layer learnable time constants.  ``loss`` is a
+    torch.autograd-aware call whose backward pass is the library's hand-written
+    adjoint with a checkpoint every ``checkpoint`` steps."""
+
+    def __init__(self, layers=3, rows=64, cols=64, field=5, outputs=10, batch=64, steps=100,
+                 dt=1.0, checkpoint=10):
+        self.shape = RateShape(layers, rows, cols, field, outputs, batch, steps, checkpoint, dt)
+        n = _syn.sg_rate_workspace_bytes(ctypes.byref(self.shape))
+        if n < 0:
+            raise ValueError("invalid rate network: " + last_error())
+        self.workspace_bytes = int(n)
+        self.neurons = rows * cols
+
+    def parameter_shapes(self):
+        s = self.shape
+        return {"x": (s.steps, s.batch, self.neurons),
+                "weights": (max(s.layers - 1, 0), self.neurons, s.field * s.field),
+                "readout": (s.outputs, self.neurons), "tau": (s.layers,),
+                "target": (s.batch, s.outputs)}
+
+    def loss(self, x, weights, readout, tau, target):
+        return _rate_loss_function().apply(self, x, weights, readout, tau, target)
+
+    def _check(self, **tensors):
+        import torch
+        for name, shp in self.parameter_shapes().items():
+            t = tensors[name]
+            if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float32
+                    and t.is_contiguous() and tuple(t.shape) == shp):
+                raise ValueError("%s must be a contiguous float32 CUDA tensor of shape %s"
+                                 % (name, shp))
+
+    def _forward(self, x, weights, readout, tau, target, y=None):
+        import torch
+        self._check(x=x, weights=weights, readout=readout, tau=tau, target=target)
+        ws = torch.empty(self.workspace_bytes // 4, dtype=torch.float32, device=x.device)
+        loss = torch.empty((), dtype=torch.float32, device=x.device)
+        rc = _syn.sg_rate_forward(ctypes.byref(self.shape), x.data_ptr(),
+                                  weights.data_ptr() if weights.numel() else None,
+                                  readout.data_ptr(), tau.data_ptr(), target.data_ptr(),
+                                  y.data_ptr() if y is not None else None, loss.data_ptr(),
+                                  ws.data_ptr(), torch.cuda.current_stream(x.device).cuda_stream)
+        if rc != 0:
+            raise RuntimeError("rate forward failed: " + last_error())
+        return loss, ws
+
+    def _backward(self, ws, grad_loss, x, weights, readout, tau, target, want_dx=True):
+        import torch
+        dw = torch.empty_like(weights)
+        dR = torch.empty_like(readout)
+        dtau = torch.empty_like(tau)
+        dx = torch.empty_like(x) if want_dx else None
+        rc = _syn.sg_rate_backward(ctypes.byref(self.shape), x.data_ptr(),
+                                   weights.data_ptr() if weights.numel() else None,
+                                   readout.data_ptr(), tau.data_ptr(), target.data_ptr(),
+                                   float(grad_loss), ws.data_ptr(),
+                                   dw.data_ptr() if weights.numel() else None, dR.data_ptr(),
+                                   dtau.data_ptr(), dx.data_ptr() if dx is not None else None,
+                                   torch.cuda.current_stream(x.device).cuda_stream)
+        if rc != 0:
+            raise RuntimeError("rate backward failed: " + last_error())
+        return dx, dw, dR, dtau
+
+
+_RATE_FN = []
+
+
+def _rate_loss_function():
+    """torch.autograd.Function over sg_rate_forward / sg_rate_backward (built
+    on first use so that importing this module does not import torch)."""
+    if _RATE_FN:
+        return _RATE_FN[0]
+    import torch
+
+    class RateLoss(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, net, x, weights, readout, tau, target):
+            loss, ws = net._forward(x, weights, readout, tau, target)
+            ctx.net, ctx.ws = net, ws
+            ctx.save_for_backward(x, weights, readout, tau, target)
+            return loss
+
+        @staticmethod
+        def backward(ctx, grad_loss):
+            x, weights, readout, tau, target = ctx.saved_tensors
+            dx, dw, dR, dtau = ctx.net._backward(ctx.ws, float(grad_loss), x, weights, readout,
+                                                 tau, target, want_dx=ctx.needs_input_grad[1])
+            return None, dx, dw, dR, dtau, None
+
+    _RATE_FN.append(RateLoss)
+    return RateLoss
 
 
 def fill_in(defaults, props):
