@@ -46,7 +46,7 @@ def gpu_grads(torch, sg, net, p, steps_dx=True):
     loss = net.loss(t["x"], t["weights"], t["readout"], t["tau"], t["target"])
     loss.backward()
     torch.cuda.synchronize()
-    return (float(loss), t["weights"].grad.cpu().numpy(), t["readout"].grad.cpu().numpy(),
+    return (loss.item(), t["weights"].grad.cpu().numpy(), t["readout"].grad.cpu().numpy(),
             t["tau"].grad.cpu().numpy(), t["x"].grad.cpu().numpy())
 
 
@@ -94,8 +94,12 @@ def test_rate_grad_loss_scaling_and_no_input_grad(torch_sg):
         t[k].requires_grad_(True)
     (3.0 * net.loss(t["x"], t["weights"], t["readout"], t["tau"], t["target"])).backward()
     assert t["x"].grad is None
-    np.testing.assert_allclose(t["weights"].grad.cpu().numpy(), 3.0 * dw1, rtol=1e-6, atol=1e-12)
-    np.testing.assert_allclose(t["tau"].grad.cpu().numpy(), 3.0 * dtau1, rtol=1e-6, atol=1e-12)
+    # grad_loss scales dloss/dy before the adjoint runs, so elements with
+    # cancellation round differently from 3 x the unscaled gradient
+    for got, want in ((t["weights"].grad, dw1), (t["readout"].grad, dR1), (t["tau"].grad, dtau1)):
+        want = 3.0 * want
+        np.testing.assert_allclose(got.cpu().numpy(), want, rtol=1e-5,
+                                   atol=1e-5 * np.abs(want).max())
 
 
 def test_rate_finite_differences_on_gpu(torch_sg):
