@@ -3,16 +3,32 @@
 // both execute the same float/double expression sequence.
 #pragma once
 
+#include "exact_div.cuh"
+
 namespace sg {
 
 #ifdef __CUDACC__
 // Up to 10 hybrid-Euler substeps that stop once v >= 30 (NaN -> 30), with the
 // conductance-implicit voltage update and the recovery step whose time
 // constant is adjusted on the substep that crosses threshold.
+//
+// Every operation is the reference's, in its types (the double literals make
+// the voltage arithmetic double), with three rewrites that leave each result
+// bit-identical and save FP64 instructions:
+//  * comparisons with 30.0 are float comparisons (30 is a float and
+//    float -> double conversion is exact);
+//  * the conductance sum and the implicit-update denominator do not change
+//    within the step and are computed once;
+//  * the division by that denominator uses its correctly rounded reciprocal
+//    (div_rn_recip, exact).
 __device__ __forceinline__ void iz_integrate(float& voltage, float& recovery, float ampa_c,
                                              float nmda_c, float gabaa_c, float gabab_c, float mf,
                                              float base_current, float a, float b) {
-    for (int i = 0; (i < 10) && (voltage < 30.0); ++i) {
+    if (!(voltage < 30.0f)) return;
+    const float sum_c = ampa_c + nmda_c + gabaa_c + gabab_c;
+    const double den = 1 + (0.1 * sum_c);
+    const double rden = 1.0 / den;
+    for (int i = 0; (i < 10) && (voltage < 30.0f); ++i) {
         float current = -ampa_c * voltage;
         float q = (voltage + 80) / 60;
         float temp = q * q;
@@ -22,11 +38,12 @@ __device__ __forceinline__ void iz_integrate(float& voltage, float& recovery, fl
         current *= 1 + mf;
         current += base_current;
         float delta_v = (0.04 * voltage * voltage) + (5 * voltage) + 140 - recovery + current;
-        float sum_c = ampa_c + nmda_c + gabaa_c + gabab_c;
-        voltage = (voltage + 0.1 * (delta_v + (gabaa_c * -70) + (gabab_c * -90))) /
-                  (1 + (0.1 * sum_c));
-        voltage = (voltage != voltage) ? 30.0 : voltage;
-        float adjusted_tau = (voltage > 30.0) ? delta_v / (30.0 - voltage + delta_v) * 0.1 : 0.1;
+        voltage = div_rn_recip(voltage + 0.1 * (delta_v + (gabaa_c * -70) + (gabab_c * -90)),
+                               den, rden);
+        voltage = (voltage != voltage) ? 30.0f : voltage;
+        float adjusted_tau = (voltage > 30.0f)
+                                 ? (float)(delta_v / (30.0 - voltage + delta_v) * 0.1)
+                                 : (float)0.1;
         recovery += a * adjusted_tau * ((b * voltage) - recovery);
     }
 }

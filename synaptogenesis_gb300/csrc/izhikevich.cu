@@ -46,6 +46,54 @@ float istdp_dst(volatile int t) { return (float)(powf(t, 10) * 0.0000001 * 2.6 *
 // iSTDP tables, indexed by the time since a spike (1..31).
 struct IzLut { float src[33]; float dst[33]; };
 
+// One synapse of the STDP + STP updaters (izhikevich_attributes.cpp:404-520).
+// The reference's expressions are evaluated in its types (double literals
+// make the weight-derivative and short-term-w updates double), with rewrites
+// that leave every stored value bit-identical and save FP64 instructions:
+//  * a spike product that is zero (no destination / source spike) adds or
+//    subtracts +0.0 to a partial sum that is never zero, so it is skipped;
+//  * (U - sw) / F divides by the constant F through its correctly rounded
+//    reciprocal (div_rn_recip, exact).
+template <bool SUB>
+__device__ __forceinline__ void iz_learn_synapse(size_t wi, int src_tss, float dest_spike,
+                                                 float dest_exc_trace, int dest_tss, float lr,
+                                                 int stp_flag, float max_weight, float* w,
+                                                 float* presyn, float* wd, float* stp_r,
+                                                 float* stp_w, const IzLut& lut) {
+    constexpr double U = SUB ? 0.2 : 0.5;
+    constexpr int F = SUB ? 20 : 1000;
+    constexpr int D = SUB ? 700 : 800;
+    float weight = w[wi];
+    if (!(weight >= 0.0001f)) return;
+    const bool src_spike = src_tss == 0;
+    float src_trace, dest_trace;
+    if (!SUB) {
+        src_trace = (presyn[wi] = src_spike ? 0.004 : presyn[wi] * 0.933);
+        dest_trace = dest_exc_trace;
+    } else {
+        src_trace = (dest_spike > 0.0f && src_tss > 0 && src_tss < 32) ? lut.src[src_tss] : 0.0f;
+        dest_trace = (src_spike && dest_tss > 0 && dest_tss < 32) ? lut.dst[dest_tss] : 0.0f;
+    }
+    // wd -= (wd - 1e-6) * 1e-4 + dest_spike * src_trace - src_spike * dest_trace
+    float weight_delta = wd[wi];
+    double change = (weight_delta - 0.000001) * 0.0001;
+    if (dest_spike != 0.0f) change = change + (dest_spike * src_trace);
+    if (src_spike) change = change - (src_spike * dest_trace);
+    weight_delta = wd[wi] = weight_delta - change;
+    weight += lr * weight_delta;
+    w[wi] = fmaxf(0.0001f, fminf(max_weight, weight));
+    if (stp_flag) {
+        float r = stp_r[wi];
+        float sw = stp_w[wi];
+        stp_r[wi] += ((1 - r) / D) - (r * sw * src_spike);
+        // stp_w += (U - sw) / F + U * (1 - sw) * src_spike
+        double inc = div_rn_recip(U - sw, (double)F, 1.0 / F);
+        if (src_spike) inc = inc + (U * (1 - sw) * src_spike);
+        stp_w[wi] = stp_w[wi] + inc;
+    }
+}
+
+
 // ---------------------------------------------------------------------------
 // Kernels
 // ---------------------------------------------------------------------------
@@ -279,9 +327,6 @@ __global__ void __launch_bounds__(256) k_iz_learn_conv_tile(
     float* __restrict__ stp_r, float* __restrict__ stp_w, IzLut lut) {
     const int d = blockIdx.x * 32 + (threadIdx.x & 31);
     if (d >= g.to_size) return;
-    const double U = SUB ? 0.2 : 0.5;
-    const int F = SUB ? 20 : 1000;
-    const int D = SUB ? 700 : 800;
     const float dest_exc_trace = __ldg(to_exc + d);
     const int dest_tss = __ldg(to_tss + d);
     const float dest_spike = extract<SR>(__ldg(dest_out + d), 0);
@@ -289,30 +334,8 @@ __global__ void __launch_bounds__(256) k_iz_learn_conv_tile(
         int from = conv_source(g, d, k);
         if (from < 0) continue;
         size_t wi = (size_t)k * g.to_size + d;
-        float weight = w[wi];
-        if (weight >= 0.0001f) {
-            int src_tss = __ldg(from_tss + from);
-            bool src_spike = src_tss == 0;
-            float src_trace, dest_trace;
-            if (!SUB) {
-                src_trace = (presyn[wi] = src_spike ? 0.004 : presyn[wi] * 0.933);
-                dest_trace = dest_exc_trace;
-            } else {
-                src_trace = (dest_spike > 0.0f && src_tss > 0 && src_tss < 32) ? lut.src[src_tss] : 0.0f;
-                dest_trace = (src_spike && dest_tss > 0 && dest_tss < 32) ? lut.dst[dest_tss] : 0.0f;
-            }
-            float weight_delta = wd[wi];
-            weight_delta = wd[wi] -= (weight_delta - 0.000001) * 0.0001 + (dest_spike * src_trace) -
-                                     (src_spike * dest_trace);
-            weight += lr * weight_delta;
-            w[wi] = fmaxf(0.0001f, fminf(max_weight, weight));
-            if (stp_flag) {
-                float r = stp_r[wi];
-                float sw = stp_w[wi];
-                stp_r[wi] += ((1 - r) / D) - (r * sw * src_spike);
-                stp_w[wi] += ((U - sw) / F) + (U * (1 - sw) * src_spike);
-            }
-        }
+        iz_learn_synapse<SUB>(wi, __ldg(from_tss + from), dest_spike, dest_exc_trace, dest_tss, lr,
+                              stp_flag, max_weight, w, presyn, wd, stp_r, stp_w, lut);
     }
 }
 
@@ -453,38 +476,13 @@ __global__ void __launch_bounds__(128) k_iz_learn(
     float max_weight, float* w, float* presyn, float* wd, float* stp_r, float* stp_w, IzLut lut) {
     int d = blockIdx.x * blockDim.x + threadIdx.x;
     if (d >= g.n_dest) return;
-    const double U = SUB ? 0.2 : 0.5;
-    const int F = SUB ? 20 : 1000;
-    const int D = SUB ? 700 : 800;
     int to = dest_of<TY>(g, d);
     float dest_exc_trace = to_exc[to];
     int dest_tss = to_tss[to];
     float dest_spike = extract<SR>(dest_out[to], 0);
     for_each_source<TY>(g, d, [&](int from, int wi) {
-        float weight = w[wi];
-        if (weight >= 0.0001f) {
-            int src_tss = from_tss[from];
-            bool src_spike = src_tss == 0;
-            float src_trace, dest_trace;
-            if (!SUB) {
-                src_trace = (presyn[wi] = src_spike ? 0.004 : presyn[wi] * 0.933);
-                dest_trace = dest_exc_trace;
-            } else {
-                src_trace = (dest_spike > 0.0f && src_tss > 0 && src_tss < 32) ? lut.src[src_tss] : 0.0f;
-                dest_trace = (src_spike && dest_tss > 0 && dest_tss < 32) ? lut.dst[dest_tss] : 0.0f;
-            }
-            float weight_delta = wd[wi];
-            weight_delta = wd[wi] -= (weight_delta - 0.000001) * 0.0001 + (dest_spike * src_trace) -
-                                     (src_spike * dest_trace);
-            weight += lr * weight_delta;
-            w[wi] = fmaxf(0.0001f, fminf(max_weight, weight));
-            if (stp_flag) {
-                float r = stp_r[wi];
-                float sw = stp_w[wi];
-                stp_r[wi] += ((1 - r) / D) - (r * sw * src_spike);
-                stp_w[wi] += ((U - sw) / F) + (U * (1 - sw) * src_spike);
-            }
-        }
+        iz_learn_synapse<SUB>((size_t)wi, from_tss[from], dest_spike, dest_exc_trace, dest_tss, lr,
+                              stp_flag, max_weight, w, presyn, wd, stp_r, stp_w, lut);
     });
 }
 
@@ -501,9 +499,6 @@ __global__ void __launch_bounds__(256) k_iz_learn_2d(
     float* __restrict__ stp_r, float* __restrict__ stp_w, IzLut lut) {
     int col = blockIdx.x * blockDim.x + threadIdx.x;
     if (col >= ncols) return;
-    const double U = SUB ? 0.2 : 0.5;
-    const int F = SUB ? 20 : 1000;
-    const int D = SUB ? 700 : 800;
     int to = dest_of<SUBSET ? T_SUBSET : T_FC>(g, col);
     float dest_exc_trace = to_exc[to];
     int dest_tss = to_tss[to];
@@ -511,30 +506,9 @@ __global__ void __launch_bounds__(256) k_iz_learn_2d(
     int r0 = blockIdx.y * rows_per_block, r1 = min(nrows, r0 + rows_per_block);
     for (int row = r0; row < r1; ++row) {
         size_t wi = (size_t)row * ncols + col;
-        float weight = w[wi];
-        if (weight >= 0.0001f) {
-            int src_tss = __ldg(from_tss + row_source<SUBSET>(g, row));
-            bool src_spike = src_tss == 0;
-            float src_trace, dest_trace;
-            if (!SUB) {
-                src_trace = (presyn[wi] = src_spike ? 0.004 : presyn[wi] * 0.933);
-                dest_trace = dest_exc_trace;
-            } else {
-                src_trace = (dest_spike > 0.0f && src_tss > 0 && src_tss < 32) ? lut.src[src_tss] : 0.0f;
-                dest_trace = (src_spike && dest_tss > 0 && dest_tss < 32) ? lut.dst[dest_tss] : 0.0f;
-            }
-            float weight_delta = wd[wi];
-            weight_delta = wd[wi] -= (weight_delta - 0.000001) * 0.0001 + (dest_spike * src_trace) -
-                                     (src_spike * dest_trace);
-            weight += lr * weight_delta;
-            w[wi] = fmaxf(0.0001f, fminf(max_weight, weight));
-            if (stp_flag) {
-                float r = stp_r[wi];
-                float sw = stp_w[wi];
-                stp_r[wi] += ((1 - r) / D) - (r * sw * src_spike);
-                stp_w[wi] += ((U - sw) / F) + (U * (1 - sw) * src_spike);
-            }
-        }
+        iz_learn_synapse<SUB>(wi, __ldg(from_tss + row_source<SUBSET>(g, row)), dest_spike,
+                              dest_exc_trace, dest_tss, lr, stp_flag, max_weight, w, presyn, wd,
+                              stp_r, stp_w, lut);
     }
 }
 
