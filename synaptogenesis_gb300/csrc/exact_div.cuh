@@ -24,7 +24,11 @@ __device__ __forceinline__ double div_rn_recip(double a, double b, double y) {
     // a, b and q at least 2^-959 and below 2^961 in magnitude: r = a - b q
     // (about 2^-53 a) stays a normal number and nothing overflows
     const int ea = biased_exponent(a), eb = biased_exponent(b), eq = biased_exponent(q);
-    if (ea < 64 || ea > 1983 || eb < 64 || eb > 1983 || eq < 64 || eq > 1983) return a / b;
+    if (ea < 64 || ea > 1983 || eb < 64 || eb > 1983 || eq < 64 || eq > 1983) {
+        // a = +-0: a * y has the sign of a / b (and is NaN where a / b is)
+        if ((__double2hiint(a) & 0x7FFFFFFF) == 0 && __double2loint(a) == 0) return q;
+        return a / b;
+    }
     const double r = __fma_rn(-q, b, a);
     return __fma_rn(r, y, q);
 }

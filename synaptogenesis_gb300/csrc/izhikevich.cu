@@ -83,13 +83,18 @@ __device__ __forceinline__ void iz_learn_synapse(size_t wi, int src_tss, float d
     weight += lr * weight_delta;
     w[wi] = fmaxf(0.0001f, fminf(max_weight, weight));
     if (stp_flag) {
-        float r = stp_r[wi];
-        float sw = stp_w[wi];
-        stp_r[wi] += ((1 - r) / D) - (r * sw * src_spike);
-        // stp_w += (U - sw) / F + U * (1 - sw) * src_spike
-        double inc = div_rn_recip(U - sw, (double)F, 1.0 / F);
-        if (src_spike) inc = inc + (U * (1 - sw) * src_spike);
-        stp_w[wi] = stp_w[wi] + inc;
+        const float r = stp_r[wi];
+        const float sw = stp_w[wi];
+        // Without a source spike, R = 1 and w = U are fixed points: the
+        // increments are +0.0 and the stored values would not change.
+        if (src_spike || r != 1.0f || !isfinite(sw))
+            stp_r[wi] = r + (((1 - r) / D) - (r * sw * src_spike));
+        if (src_spike || !(U == (double)(float)U && sw == (float)U)) {
+            // stp_w += (U - sw) / F + U * (1 - sw) * src_spike
+            double inc = div_rn_recip(U - sw, (double)F, 1.0 / F);
+            if (src_spike) inc = inc + (U * (1 - sw) * src_spike);
+            stp_w[wi] = sw + inc;
+        }
     }
 }
 

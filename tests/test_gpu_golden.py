@@ -43,3 +43,32 @@ def test_library_matches_oracle_longer(syngen, name):
     want = run_oracle(case, steps=steps)
     problems = compare(got, want, nan_keys=float_like_keys(case))
     assert not problems, problems
+
+
+def test_plastic_short_term_fixed_points_match_oracle(syngen):
+    """The plastic case with half the synapses at the short-term fixed points
+    (w = U = 0.5 for "add" connections, R = 1), where the updater skips the
+    unchanged short-term values: bit-exact against the oracle."""
+    import copy
+
+    import numpy as np
+
+    from tests.golden.cases import Case
+    base = CASES["iz_plastic"]
+
+    def inject(rng, sizes):
+        d = base.inject(rng, sizes)
+        pick = np.random.default_rng(5)
+        for key in list(d):
+            if key[0] == "matrix" and key[2] == "short term w":
+                arr = d[key].copy()
+                arr[pick.random(arr.size) < 0.5] = np.float32(0.5)
+                d[key] = arr
+        return d
+
+    case = Case("iz_plastic_fixed_points", copy.deepcopy(base.net), 200, base.seed, inject=inject,
+                inputs=base.inputs, record=base.record, final=base.final, tol=base.tol)
+    got = run_library(case, syngen)
+    want = run_oracle(case)
+    problems = compare(got, want, nan_keys=float_like_keys(case))
+    assert not problems, problems
