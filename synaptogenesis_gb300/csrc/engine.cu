@@ -1,4 +1,5 @@
 #include "engine.h"
+#include "iz_cols_tma.cuh"
 
 #include <algorithm>
 #include <cstring>
@@ -392,7 +393,10 @@ long Engine::step(long n) {
     return i;
 }
 
-void Engine::synchronize() { SG_CUDA(cudaStreamSynchronize(stream_)); }
+void Engine::synchronize() {
+    SG_CUDA(cudaStreamSynchronize(stream_));
+    check_iz_cols_errors();
+}
 
 Props* Engine::report() {
     synchronize();

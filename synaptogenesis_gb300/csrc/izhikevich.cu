@@ -11,6 +11,7 @@
 #include <random>
 
 #include "cuda_check.h"
+#include "iz_cols_tma.cuh"
 #include "iz_neuron.cuh"
 #include "models.h"
 #include "state.h"
@@ -718,6 +719,21 @@ class IzhikevichModel : public Model {
         }
         int nrows = 0, ncols = 0;
         if (matrix_shape(c, nrows, ncols) && ncols % 4 == 0) {
+            if (!cs.device_plan_tried) {
+                cs.device_plan_tried = true;
+                const bool bit = c.from->output_type == OUT_BIT;
+                cs.device_plan = make_iz_cols_plan(
+                    nrows, ncols, cs.weights->df(), cs.var("short term R")->df(),
+                    cs.var("short term w")->df(), bit ? cs.delays->di() : nullptr,
+                    cs.var("short trace")->df(), lname ? cs.var("long trace")->df() : nullptr);
+            }
+            if (cs.device_plan) {
+                launch_iz_cols_tma(*static_cast<IzColsPlan*>(cs.device_plan.get()), cs.geom,
+                                   (int)c.from->output_type, c.type == SUBSET, src, g, stau, ltau,
+                                   sc, lc, ctx.stream);
+                ctx.count();
+                return;
+            }
             IzColsArgs a{cs.geom, nrows, ncols, src, cs.weights->df(), cs.var("short term R")->df(),
                          cs.var("short term w")->df(), cs.delays->di(), cs.var("short trace")->df(),
                          cs.var("long trace")->df(), g, stau, ltau, sc, lc};

@@ -1,4 +1,5 @@
 #include "state.h"
+#include "iz_cols_tma.cuh"
 
 #include <algorithm>
 #include <cstring>
@@ -180,6 +181,7 @@ void State::to_device(cudaStream_t stream) {
 void State::to_host(cudaStream_t stream) {
     if (on_host_) return;
     SG_CUDA(cudaStreamSynchronize(stream));
+    check_iz_cols_errors();
     for (auto& a : arrays_) {
         if (a->dev_count == 0 || a->scratch) continue;
         size_t n = std::min(a->dev_count, a->count);

@@ -70,6 +70,10 @@ struct ConnState {
     // Distances computed for a distance callback, reused by distance-based
     // delays like the reference's cached distances (weight_matrix.cpp:1372-1374).
     std::vector<float> cached_distances;
+    // Launch plan a model keeps for this connection's device arrays (built at
+    // the first step, once the arena exists).
+    std::shared_ptr<void> device_plan;
+    bool device_plan_tried = false;
     Array* var(const std::string& k) const;
 };
 
