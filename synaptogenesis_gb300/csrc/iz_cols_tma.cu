@@ -37,6 +37,9 @@ constexpr int kMaxWidth = 32;    // columns per CTA at most
 constexpr int kThreads = 256;
 constexpr int kArrays = 6;       // w, R, w_stp, [delay], short, [long]
 constexpr int kWaitLimit = 1 << 20;
+// The thread that issues the TMA loads and stores (and waits on its store
+// groups): in a warp that adds no column sums, so neither delays the other.
+constexpr int kProducer = 96;
 
 struct ColsMaps {
     CUtensorMap m[2][kArrays];   // [wide band, narrow band][array]
@@ -122,7 +125,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int nchunks = (p.nrows + kR - 1) / kR;
     const uint32_t stage_tx = (uint32_t)(NA * tile_floats * 4);
 
-    auto issue = [&](int ch) {               // thread 0 only
+    auto issue = [&](int ch) {               // producer thread only
         if (ch >= nchunks) return;
         const int s = ch % kStages;
         const uint32_t bar = smem_u32(&bars[s]);
@@ -147,7 +150,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     load_words(0);
     __syncthreads();
-    if (tid == 0)
+    if (tid == kProducer)
         for (int c = 0; c < kStages - 1; ++c) issue(c);
 
     // this thread's elements of a chunk tile: (row j, column c), fixed
@@ -162,13 +165,25 @@ __global__ void __launch_bounds__(kThreads, 1)
     float short_sum = 0.0f, long_sum = 0.0f;
     const bool short_owner = tid < width;
     const bool long_owner = LONG && tid >= 128 && tid < 128 + width;
+    // The column's pre-decay traces of a chunk are loaded first and then
+    // added in row order: the loads overlap, only the adds are serial.
     auto consume = [&](int ch) {
+        if (!short_owner && !long_owner) return;
         const int nr = min(kR, p.nrows - ch * kR);
-        const float* sb = sums + (ch & 1) * 2 * kR * kMaxWidth;
-        if (short_owner)
-            for (int j = 0; j < nr; ++j) short_sum += sb[j * width + tid];
-        else if (long_owner)
-            for (int j = 0; j < nr; ++j) long_sum += sb[kR * kMaxWidth + j * width + (tid - 128)];
+        const float* col = sums + (ch & 1) * 2 * kR * kMaxWidth +
+                           (short_owner ? tid : kR * kMaxWidth + (tid - 128));
+        float acc = short_owner ? short_sum : long_sum;
+        if (nr == kR) {
+            float v[kR];
+#pragma unroll
+            for (int j = 0; j < kR; ++j) v[j] = col[j * width];
+#pragma unroll
+            for (int j = 0; j < kR; ++j) acc += v[j];
+        } else {
+            for (int j = 0; j < nr; ++j) acc += col[j * width];
+        }
+        if (short_owner) short_sum = acc;
+        else long_sum = acc;
     };
 
     int ch = 0;
@@ -203,7 +218,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (s_abort) break;
-        if (tid == 0) {
+        if (tid == kProducer) {
             tma_store(&mp[A_ST], col0, ch * kR, smem_u32(tile(s, A_ST)));
             if (LONG) tma_store(&mp[A_LT], col0, ch * kR, smem_u32(tile(s, A_LT)));
             asm volatile("cp.async.bulk.commit_group;" ::: "memory");
@@ -216,7 +231,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (s_abort) {
         // loads issued for chunks ch .. ch+S-2 may still be landing: wait
         // for them (bounded) before the shared memory goes away
-        if (tid == 0) {
+        if (tid == kProducer) {
             atomicExch(&g_cols_error, 1);
             for (int c = ch; c < min(nchunks, ch + kStages - 1); ++c)
                 mbar_wait(smem_u32(&bars[c % kStages]), (uint32_t)((c / kStages) & 1));
@@ -232,7 +247,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (short_owner) p.short_cond[to] += short_sum;
         else p.long_cond[to] += long_sum;
     }
-    if (tid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    if (tid == kProducer) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
 size_t cols_smem_bytes(int na, int wmax) {
