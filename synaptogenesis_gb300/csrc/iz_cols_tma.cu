@@ -1,28 +1,24 @@
 // Izhikevich trace activator for fully connected and subset matrices
 // (src/core/state/impl/izhikevich_attributes.cpp:228-352 over the loops of
 // src/core/engine/kernel/synapse_kernel.h:111-251), fed by the Tensor Memory
-// Accelerator.
+// Accelerator's bulk copies.
 //
-// The matrices are [source row][destination column] (the reference's GPU
-// layout).  Each CTA owns a band of 4*k destination columns -- the columns
-// are split into as many bands as there are SMs (24 or 28 columns for 4096),
-// so every SM streams -- and walks every source row in 32-row chunks:
-//   * one thread issues, per chunk, one 2-D TMA tile load per array (weights,
-//     short-term R and w, delays, short and long traces) into an 8-stage
-//     shared-memory ring, completing on the stage's mbarrier;
-//   * all threads compute the synapses of the chunk, write the pre-decay
-//     traces to a sums tile and the decayed traces back into the stage;
-//   * one thread writes the decayed trace tiles back with TMA stores;
-//   * one thread per column adds the chunk's pre-decay traces in row order,
-//     keeping the reference's sequential fp32 sum.
+// The matrices are banded: [destination / 8][source][destination % 8], so the
+// 32 source rows of a band form one contiguous 1 KB block per array.  Each
+// CTA owns a run of bands (3 or 4 for 4096 destinations: the bands are spread
+// over every SM) and walks the source rows in 32-row chunks:
+//   * one producer thread issues, per chunk, one bulk copy per band and array
+//     (weights, short-term R and w, delays, short and long traces) into an
+//     8-stage shared-memory ring, completing on the stage's mbarrier;
+//   * all threads compute the chunk's synapses, write the pre-decay traces to
+//     a sums tile and the decayed traces back into the stage;
+//   * the producer writes the decayed traces back with bulk stores;
+//   * one thread per destination adds the chunk's pre-decay traces in source
+//     order, keeping the reference's sequential fp32 sum.
 // Every mbarrier wait is bounded: if one runs out, the kernel records the
 // fact in a device flag, waits (bounded) for its loads in flight, drains its
 // stores and returns; check_iz_cols_errors reports it on the host.
-#include <cuda.h>
-#include <cudaTypedefs.h>
-
 #include <algorithm>
-#include <mutex>
 
 #include "cuda_check.h"
 #include "iz_cols_tma.cuh"
@@ -31,23 +27,24 @@ namespace sg {
 
 namespace {
 
-constexpr int kR = 32;           // rows per chunk
-constexpr int kStages = 8;
-constexpr int kMaxWidth = 32;    // columns per CTA at most
+constexpr int kR = 32;                   // source rows per chunk
+#ifndef SG_COLS_STAGES
+#define SG_COLS_STAGES 8
+#endif
+constexpr int kStages = SG_COLS_STAGES;
+constexpr int kMaxBands = 4;             // bands per CTA at most (32 destinations)
 constexpr int kThreads = 256;
-constexpr int kArrays = 6;       // w, R, w_stp, [delay], short, [long]
+constexpr int kSumPitch = 40;            // sums row pitch: conflict-free writes and reads
 constexpr int kWaitLimit = 1 << 20;
-// The thread that issues the TMA loads and stores (and waits on its store
-// groups): in a warp that adds no column sums, so neither delays the other.
+constexpr int kBlockFloats = kR * kBand; // one band's chunk: 32 rows x 8 destinations
+// The thread that issues the copies (and waits on its store groups): in a
+// warp that adds no sums, so neither delays the other.
 constexpr int kProducer = 96;
-
-struct ColsMaps {
-    CUtensorMap m[2][kArrays];   // [wide band, narrow band][array]
-};
 
 struct ColsParams {
     DGeom g;
-    int nrows, ncols, base_units, extra;
+    int nrows, ncols, base_bands, extra;
+    const float* arrays[6];              // w, R, w_stp, [delay], short, [long]
     const uint32_t* src;
     float gcond, short_tau, long_tau;
     float* short_cond;
@@ -74,20 +71,19 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
-__device__ __forceinline__ void tma_load(uint32_t dst, const CUtensorMap* map, int x, int y,
-                                         uint32_t bar) {
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes,
+                                          uint32_t bar) {
     asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3}], [%4];"
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
         :
-        : "r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "r"(dst), "l"(src), "r"(bytes), "r"(bar)
         : "memory");
 }
 
-__device__ __forceinline__ void tma_store(const CUtensorMap* map, int x, int y, uint32_t src) {
-    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];"
+__device__ __forceinline__ void bulk_store(void* dst, uint32_t src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
                  :
-                 : "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(src)
+                 : "l"(dst), "r"(src), "r"(bytes)
                  : "memory");
 }
 
@@ -99,42 +95,42 @@ __device__ __forceinline__ int source_of_row(const DGeom& g, int row) {
 }
 
 template <int SR, bool LONG, bool SUBSET>
-__global__ void __launch_bounds__(kThreads, 1)
-    k_iz_cols_tma(const __grid_constant__ ColsMaps maps, const ColsParams p) {
+__global__ void __launch_bounds__(kThreads, 1) k_iz_cols_bulk(const ColsParams p) {
     constexpr int HAS_D = SR == S_BIT ? 1 : 0;
     constexpr int NA = 4 + HAS_D + (LONG ? 1 : 0);
     constexpr int A_ST = 3 + HAS_D, A_LT = 4 + HAS_D;
-    extern __shared__ unsigned char smem_raw[];
+    constexpr int kTile = kMaxBands * kBlockFloats;        // floats per array per stage
+    extern __shared__ __align__(128) float smem[];
     __shared__ uint32_t s_words[2][kR];
     __shared__ int s_abort;
+    float* stages = smem;                                  // [S][NA][bands][32][8]
+    float* sums = stages + (size_t)kStages * NA * kTile;   // [2][2][32][kSumPitch]
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sums + 4 * kR * kSumPitch);
 
     const int tid = threadIdx.x, b = blockIdx.x;
-    const bool wide = b < p.extra;
-    const int width = 4 * (p.base_units + (wide ? 1 : 0));
-    const int col0 = 4 * (b * p.base_units + min(b, p.extra));
-    const CUtensorMap* mp = maps.m[wide ? 0 : 1];
-    const int tile_floats = kR * width;
-    const int tile_bytes = (tile_floats * 4 + 127) / 128 * 128;
-    unsigned char* base =
-        reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-    float* sums = reinterpret_cast<float*>(base + (size_t)kStages * NA * tile_bytes);  // [2][2][R*w]
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sums + 4 * kR * kMaxWidth);
-    auto tile = [&](int s, int a) {
-        return reinterpret_cast<float*>(base + ((size_t)s * NA + a) * tile_bytes);
-    };
+    const int nb = p.base_bands + (b < p.extra ? 1 : 0);
+    const int band0 = b * p.base_bands + min(b, p.extra);
+    const int ncol = nb * kBand;
     const int nchunks = (p.nrows + kR - 1) / kR;
-    const uint32_t stage_tx = (uint32_t)(NA * tile_floats * 4);
+    auto tile = [&](int s, int a) { return stages + ((size_t)s * NA + a) * kTile; };
+    auto block_src = [&](int a, int band, int ch) {        // first float of a band's chunk
+        return p.arrays[a] + ((size_t)(band0 + band) * p.nrows + (size_t)ch * kR) * kBand;
+    };
+    auto chunk_rows = [&](int ch) { return min(kR, p.nrows - ch * kR); };
 
-    auto issue = [&](int ch) {               // producer thread only
+    auto issue = [&](int ch) {                             // producer only
         if (ch >= nchunks) return;
         const int s = ch % kStages;
         const uint32_t bar = smem_u32(&bars[s]);
+        const uint32_t bytes = (uint32_t)chunk_rows(ch) * kBand * 4;
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
-                     "r"(stage_tx)
+                     "r"(bytes * NA * nb)
                      : "memory");
-        for (int a = 0; a < NA; ++a) tma_load(smem_u32(tile(s, a)), &mp[a], col0, ch * kR, bar);
+        for (int a = 0; a < NA; ++a)
+            for (int k = 0; k < nb; ++k)
+                bulk_load(smem_u32(tile(s, a) + k * kBlockFloats), block_src(a, k, ch), bytes, bar);
     };
-    auto load_words = [&](int ch) {          // threads 0..R-1
+    auto load_words = [&](int ch) {                        // threads 0..31
         if (tid < kR) {
             const int row = ch * kR + tid;
             s_words[ch & 1][tid] =
@@ -153,34 +149,35 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (tid == kProducer)
         for (int c = 0; c < kStages - 1; ++c) issue(c);
 
-    // this thread's elements of a chunk tile: (row j, column c), fixed
-    constexpr int kPer = kR * kMaxWidth / kThreads;
-    int ej[kPer], eo[kPer];
+    // this thread's elements: offset e = band * 256 + row * 8 + lane8
+    constexpr int kPer = kTile / kThreads;
+    int eo[kPer], ej[kPer], ecol[kPer];
 #pragma unroll
     for (int k = 0; k < kPer; ++k) {
         const int e = tid + k * kThreads;
-        ej[k] = e / width;
-        eo[k] = e < tile_floats ? e : -1;      // element offset j * width + c
+        eo[k] = e < nb * kBlockFloats ? e : -1;
+        ej[k] = (e % kBlockFloats) / kBand;
+        ecol[k] = (e / kBlockFloats) * kBand + e % kBand;
     }
     float short_sum = 0.0f, long_sum = 0.0f;
-    const bool short_owner = tid < width;
-    const bool long_owner = LONG && tid >= 128 && tid < 128 + width;
-    // The column's pre-decay traces of a chunk are loaded first and then
-    // added in row order: the loads overlap, only the adds are serial.
+    const bool short_owner = tid < ncol;
+    const bool long_owner = LONG && tid >= 128 && tid < 128 + ncol;
+    // A destination's pre-decay traces of a chunk are loaded first and then
+    // added in source order: the loads overlap, only the adds are serial.
     auto consume = [&](int ch) {
         if (!short_owner && !long_owner) return;
-        const int nr = min(kR, p.nrows - ch * kR);
-        const float* col = sums + (ch & 1) * 2 * kR * kMaxWidth +
-                           (short_owner ? tid : kR * kMaxWidth + (tid - 128));
+        const int nr = chunk_rows(ch);
+        const float* col = sums + (ch & 1) * 2 * kR * kSumPitch +
+                           (short_owner ? tid : kR * kSumPitch + (tid - 128));
         float acc = short_owner ? short_sum : long_sum;
         if (nr == kR) {
             float v[kR];
 #pragma unroll
-            for (int j = 0; j < kR; ++j) v[j] = col[j * width];
+            for (int j = 0; j < kR; ++j) v[j] = col[j * kSumPitch];
 #pragma unroll
             for (int j = 0; j < kR; ++j) acc += v[j];
         } else {
-            for (int j = 0; j < nr; ++j) acc += col[j * width];
+            for (int j = 0; j < nr; ++j) acc += col[j * kSumPitch];
         }
         if (short_owner) short_sum = acc;
         else long_sum = acc;
@@ -191,7 +188,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int s = ch % kStages;
         if (!mbar_wait(smem_u32(&bars[s]), (uint32_t)((ch / kStages) & 1))) s_abort = 1;
         if (ch > 0) consume(ch - 1);
-        float* sb = sums + (ch & 1) * 2 * kR * kMaxWidth;
+        float* sb = sums + (ch & 1) * 2 * kR * kSumPitch;
         const float* tw = tile(s, 0);
         const float* tr = tile(s, 1);
         const float* tsw = tile(s, 2);
@@ -205,12 +202,13 @@ __global__ void __launch_bounds__(kThreads, 1)
             const float spike = extract<SR>(word, delay);
             const float weight = tw[o] * (tr[o] * tsw[o]);
             const float st = tst[o] + (spike * weight * p.gcond);
-            sb[o] = st;
+            const int so = ej[k] * kSumPitch + ecol[k];
+            sb[so] = st;
             tst[o] = st * p.short_tau;
             if (LONG) {
                 float* tlt = tile(s, A_LT);
                 const float lt = tlt[o] + (spike * weight * p.gcond);
-                sb[kR * kMaxWidth + o] = lt;
+                sb[kR * kSumPitch + so] = lt;
                 tlt[o] = lt * p.long_tau;
             }
         }
@@ -219,18 +217,24 @@ __global__ void __launch_bounds__(kThreads, 1)
         __syncthreads();
         if (s_abort) break;
         if (tid == kProducer) {
-            tma_store(&mp[A_ST], col0, ch * kR, smem_u32(tile(s, A_ST)));
-            if (LONG) tma_store(&mp[A_LT], col0, ch * kR, smem_u32(tile(s, A_LT)));
+            const uint32_t bytes = (uint32_t)chunk_rows(ch) * kBand * 4;
+            for (int k = 0; k < nb; ++k) {
+                bulk_store(const_cast<float*>(block_src(A_ST, k, ch)),
+                           smem_u32(tile(s, A_ST) + k * kBlockFloats), bytes);
+                if (LONG)
+                    bulk_store(const_cast<float*>(block_src(A_LT, k, ch)),
+                               smem_u32(tile(s, A_LT) + k * kBlockFloats), bytes);
+            }
             asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-            // the buffer about to be refilled was stored from one chunk ago
+            // the stage about to be refilled was stored from one chunk ago
             asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
             issue(ch + kStages - 1);
         }
     }
 
     if (s_abort) {
-        // loads issued for chunks ch .. ch+S-2 may still be landing: wait
-        // for them (bounded) before the shared memory goes away
+        // loads issued for chunks ch .. ch+S-2 may still be landing: wait for
+        // them (bounded) before the shared memory goes away
         if (tid == kProducer) {
             atomicExch(&g_cols_error, 1);
             for (int c = ch; c < min(nchunks, ch + kStages - 1); ++c)
@@ -243,38 +247,26 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (nchunks > 0) consume(nchunks - 1);
     if (short_owner || long_owner) {
         const int c = short_owner ? tid : tid - 128;
-        const int to = dest_of<SUBSET ? T_SUBSET : T_FC>(p.g, col0 + c);
-        if (short_owner) p.short_cond[to] += short_sum;
-        else p.long_cond[to] += long_sum;
+        const int col = band0 * kBand + c;
+        if (col < p.ncols) {
+            const int to = dest_of<SUBSET ? T_SUBSET : T_FC>(p.g, col);
+            if (short_owner) p.short_cond[to] += short_sum;
+            else p.long_cond[to] += long_sum;
+        }
     }
     if (tid == kProducer) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
-size_t cols_smem_bytes(int na, int wmax) {
-    const size_t tile_bytes = ((size_t)kR * wmax * 4 + 127) / 128 * 128;
-    return 128 + (size_t)kStages * na * tile_bytes + (size_t)4 * kR * kMaxWidth * 4 +
+size_t cols_smem_bytes(int na) {
+    return (size_t)kStages * na * kMaxBands * kBlockFloats * 4 + (size_t)4 * kR * kSumPitch * 4 +
            kStages * sizeof(uint64_t);
-}
-
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-    static std::once_flag once;
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    std::call_once(once, [] {
-        void* f = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
-                                             &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
-    });
-    return fn;
 }
 
 }  // namespace
 
 struct IzColsPlan {
-    ColsMaps maps;
-    int nrows = 0, ncols = 0, n_cta = 0, base_units = 0, extra = 0, na = 0;
+    ColsParams base;
+    int n_cta = 0, na = 0;
     bool has_delay = false, long_trace = false;
     size_t smem = 0;
 };
@@ -282,51 +274,34 @@ struct IzColsPlan {
 std::shared_ptr<IzColsPlan> make_iz_cols_plan(int nrows, int ncols, const float* w,
                                               const float* stp_r, const float* stp_w,
                                               const int* delays, float* short_tr,
-                                              float* long_tr) {
-    if (nrows < 1 || ncols < 4 || ncols % 4 != 0) return nullptr;
-    auto encode = encode_fn();
-    if (!encode) return nullptr;
+                                              float* long_tr, int ctas) {
+    if (nrows < 1 || ncols < 1) return nullptr;
     int dev = 0, sms = 0, optin = 0;
     SG_CUDA(cudaGetDevice(&dev));
     SG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     SG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     auto plan = std::make_shared<IzColsPlan>();
-    const int q = ncols / 4;                                   // 4-column units
-    plan->n_cta = std::max(std::min(sms, q), (q + kMaxWidth / 4 - 1) / (kMaxWidth / 4));
-    plan->base_units = q / plan->n_cta;
-    plan->extra = q % plan->n_cta;
-    plan->nrows = nrows;
-    plan->ncols = ncols;
+    const int bands = (ncols + kBand - 1) / kBand;
+    plan->n_cta = std::max(std::min(ctas > 0 ? ctas : sms, bands),
+                           (bands + kMaxBands - 1) / kMaxBands);
     plan->has_delay = delays != nullptr;
     plan->long_trace = long_tr != nullptr;
     plan->na = 4 + (plan->has_delay ? 1 : 0) + (plan->long_trace ? 1 : 0);
-    const int wmax = 4 * (plan->base_units + (plan->extra ? 1 : 0));
-    plan->smem = cols_smem_bytes(plan->na, wmax);
-    if (wmax > kMaxWidth || (long long)plan->smem > optin) return nullptr;
-    const void* arrays[kArrays];
+    plan->smem = cols_smem_bytes(plan->na);
+    if ((long long)plan->smem > optin) return nullptr;
+    ColsParams& p = plan->base;
+    p = ColsParams{};
+    p.nrows = nrows;
+    p.ncols = ncols;
+    p.base_bands = bands / plan->n_cta;
+    p.extra = bands % plan->n_cta;
     int a = 0;
-    arrays[a++] = w;
-    arrays[a++] = stp_r;
-    arrays[a++] = stp_w;
-    if (plan->has_delay) arrays[a++] = delays;
-    arrays[a++] = short_tr;
-    if (plan->long_trace) arrays[a++] = long_tr;
-    for (int band = 0; band < 2; ++band) {
-        const int width = 4 * (plan->base_units + (band == 0 ? 1 : 0));
-        if (width < 4 || (band == 0 && plan->extra == 0)) continue;
-        for (int i = 0; i < plan->na; ++i) {
-            cuuint64_t dims[2] = {(cuuint64_t)ncols, (cuuint64_t)nrows};
-            cuuint64_t strides[1] = {(cuuint64_t)ncols * 4};
-            cuuint32_t box[2] = {(cuuint32_t)width, (cuuint32_t)kR};
-            cuuint32_t estr[2] = {1, 1};
-            CUresult r = encode(&plan->maps.m[band][i], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
-                                const_cast<void*>(arrays[i]), dims, strides, box, estr,
-                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                                CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-            if (r != CUDA_SUCCESS) return nullptr;
-        }
-    }
+    p.arrays[a++] = w;
+    p.arrays[a++] = stp_r;
+    p.arrays[a++] = stp_w;
+    if (plan->has_delay) p.arrays[a++] = reinterpret_cast<const float*>(delays);
+    p.arrays[a++] = short_tr;
+    if (plan->long_trace) p.arrays[a++] = long_tr;
     return plan;
 }
 
@@ -334,11 +309,11 @@ template <int SR, bool LONG, bool SUBSET>
 static void launch_t(const IzColsPlan& plan, const ColsParams& p, cudaStream_t s) {
     static int configured = 0;
     if (configured < (int)plan.smem) {
-        SG_CUDA(cudaFuncSetAttribute(k_iz_cols_tma<SR, LONG, SUBSET>,
+        SG_CUDA(cudaFuncSetAttribute(k_iz_cols_bulk<SR, LONG, SUBSET>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem));
         configured = (int)plan.smem;
     }
-    k_iz_cols_tma<SR, LONG, SUBSET><<<plan.n_cta, kThreads, plan.smem, s>>>(plan.maps, p);
+    k_iz_cols_bulk<SR, LONG, SUBSET><<<plan.n_cta, kThreads, plan.smem, s>>>(p);
     SG_LAUNCH_CHECK();
 }
 
@@ -346,8 +321,14 @@ void launch_iz_cols_tma(const IzColsPlan& plan, const DGeom& g, int src_type, bo
                         const uint32_t* src, float gcond, float short_tau, float long_tau,
                         float* short_cond, float* long_cond, cudaStream_t stream) {
     if ((src_type == S_BIT) != plan.has_delay) throw SgError("cols plan: delay array mismatch");
-    ColsParams p{g, plan.nrows, plan.ncols, plan.base_units, plan.extra, src,
-                 gcond, short_tau, long_tau, short_cond, long_cond};
+    ColsParams p = plan.base;
+    p.g = g;
+    p.src = src;
+    p.gcond = gcond;
+    p.short_tau = short_tau;
+    p.long_tau = long_tau;
+    p.short_cond = short_cond;
+    p.long_cond = long_cond;
     const bool lng = plan.long_trace;
 #define SG_COLS(SRV)                                                         \
     if (lng) {                                                               \
@@ -369,7 +350,7 @@ void check_iz_cols_errors() {
     if (flag) {
         int zero = 0;
         SG_CUDA(cudaMemcpyToSymbol(g_cols_error, &zero, sizeof(int)));
-        throw SgError("Izhikevich column activator: a TMA pipeline wait timed out");
+        throw SgError("Izhikevich column activator: a bulk-copy pipeline wait timed out");
     }
 }
 

@@ -1,5 +1,5 @@
 // Izhikevich trace activator for fully connected and subset matrices, fed by
-// the Tensor Memory Accelerator (see iz_cols_tma.cu).
+// the Tensor Memory Accelerator's bulk copies (see iz_cols_tma.cu).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -10,18 +10,19 @@
 
 namespace sg {
 
-// Tensor maps and the column split of one connection's matrices, built once
-// for the arrays' device addresses.
+// Column split of one connection's banded matrices.
 struct IzColsPlan;
 
-// nrows x ncols device matrices ([source row][destination column], ncols a
-// multiple of 4); delays may be null (FLOAT / INT sources), long_tr null for
-// single-trace opcodes.  Returns null when the split or the tensor maps are
-// not possible (the caller then uses the cp.async kernel).
+// nrows sources x ncols destinations, every array banded
+// (banded_index(destination, source, nrows)); delays may be null (FLOAT / INT
+// sources), long_tr null for single-trace opcodes.  bands_per_cta_max limits
+// each CTA to that many bands of kBand destinations; ctas = 0 spreads the
+// bands over every SM.  Returns null if the kernel cannot run this shape
+// (the caller then uses the per-destination activator).
 std::shared_ptr<IzColsPlan> make_iz_cols_plan(int nrows, int ncols, const float* w,
                                               const float* stp_r, const float* stp_w,
                                               const int* delays, float* short_tr,
-                                              float* long_tr);
+                                              float* long_tr, int ctas = 0);
 
 void launch_iz_cols_tma(const IzColsPlan& plan, const DGeom& g, int src_type, bool subset,
                         const uint32_t* src, float gcond, float short_tau, float long_tau,

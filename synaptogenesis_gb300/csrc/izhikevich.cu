@@ -4,8 +4,6 @@
 // term (IZ_* and STDP constants are double literals); the library is built
 // with --fmad=false so nothing is contracted.  powf(x, 2) is x * x, which is
 // what the reference's optimised build computes.
-#include <cuda_pipeline.h>
-
 #include <cmath>
 #include <cstdlib>
 #include <random>
@@ -146,115 +144,6 @@ __device__ __forceinline__ int row_source(const DGeom& g, int row) {
     return (row / fkc + g.fr0) * g.from_cols + (row % fkc + g.fc0);
 }
 
-// Trace activator for fully connected and subset matrices, which have many
-// sources per destination and (in the device layout [source][destination])
-// rows of contiguous destinations.  One CTA owns 32 destination columns and
-// streams every source row through a 6-stage cp.async pipeline of 32-row
-// tiles (weights, short-term R and w, delays, short and long traces), so the
-// loads of later tiles are in flight while a tile is processed.  All 256
-// threads do the per-synapse work (one warp per row, one lane per column) and
-// write the decayed traces straight back; the pre-decay traces go to a
-// double-buffered shared tile from which one lane per column adds them in row
-// order, keeping the reference's sequential fp32 sum.  Needs ncols % 4 == 0.
-constexpr int kColsR = 32;       // rows per stage
-constexpr int kColsS = 6;        // stages
-
-template <int SR, bool LONG, bool SUBSET>
-__global__ void __launch_bounds__(256, 1) k_iz_activate_cols(
-    DGeom g, int nrows, int ncols, const uint32_t* __restrict__ src, const float* __restrict__ w,
-    const float* __restrict__ stp_r, const float* __restrict__ stp_w, const int* __restrict__ delays,
-    float* __restrict__ short_tr, float* __restrict__ long_tr, float gcond, float short_tau,
-    float long_tau, float* __restrict__ short_cond, float* __restrict__ long_cond) {
-    constexpr int R = kColsR, S = kColsS;
-    constexpr int HAS_D = SR == S_BIT ? 1 : 0;
-    constexpr int NA = 4 + HAS_D + (LONG ? 1 : 0);     // w, r, sw, [delay], st, [lt]
-    extern __shared__ float4 smem4[];
-    float* stage_mem = reinterpret_cast<float*>(smem4);
-    float* sums = stage_mem + S * NA * R * 32;         // [2 buffers][2 kinds][R][32]
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int col0 = blockIdx.x * 32;
-    const int col = col0 + lane;
-    const bool colok = col < ncols;
-    const int nchunks = (nrows + R - 1) / R;
-
-    auto src_array = [&](int a) -> const float* {
-        if (a == 0) return w;
-        if (a == 1) return stp_r;
-        if (a == 2) return stp_w;
-        if (HAS_D && a == 3) return reinterpret_cast<const float*>(delays);
-        if (a == 3 + HAS_D) return short_tr;
-        return long_tr;
-    };
-    auto issue = [&](int ch) {
-        if (ch < nchunks) {
-            float* st = stage_mem + (size_t)(ch % S) * NA * R * 32;
-            for (int e = tid; e < NA * R * 8; e += 256) {
-                int a = e / (R * 8), rem = e - a * (R * 8), j = rem >> 3, p = rem & 7;
-                int row = ch * R + j, c = col0 + p * 4;
-                if (row < nrows && c < ncols)
-                    __pipeline_memcpy_async(st + (a * R + j) * 32 + p * 4,
-                                            src_array(a) + (size_t)row * ncols + c, 16);
-            }
-        }
-        __pipeline_commit();
-    };
-
-    float short_sum = 0.0f, long_sum = 0.0f;
-    auto consume = [&](int ch) {
-        int nr = min(R, nrows - ch * R);
-        const float* sb = sums + (ch & 1) * 2 * R * 32;
-        if (warp == 0)
-            for (int j = 0; j < nr; ++j) short_sum += sb[j * 32 + lane];
-        else if (LONG && warp == 1)
-            for (int j = 0; j < nr; ++j) long_sum += sb[R * 32 + j * 32 + lane];
-    };
-
-    for (int s = 0; s < S - 1; ++s) issue(s);
-    for (int ch = 0; ch < nchunks; ++ch) {
-        __pipeline_wait_prior(S - 2);
-        __syncthreads();
-        issue(ch + S - 1);
-        if (ch > 0) consume(ch - 1);
-        const float* st = stage_mem + (size_t)(ch % S) * NA * R * 32;
-        float* sb = sums + (ch & 1) * 2 * R * 32;
-#pragma unroll
-        for (int i = 0; i < R / 8; ++i) {
-            int j = warp + 8 * i;
-            int row = ch * R + j;
-            float st_pre = 0.0f, lt_pre = 0.0f;
-            if (row < nrows && colok) {
-                int o = j * 32 + lane;
-                uint32_t word = __ldg(src + row_source<SUBSET>(g, row));
-                int delay = HAS_D ? __float_as_int(st[3 * R * 32 + o]) : 0;
-                float spike = extract<SR>(word, delay);
-                float weight = st[o] * (st[R * 32 + o] * st[2 * R * 32 + o]);
-                st_pre = st[(3 + HAS_D) * R * 32 + o] + (spike * weight * gcond);
-                size_t gi = (size_t)row * ncols + col;
-                short_tr[gi] = st_pre * short_tau;
-                if (LONG) {
-                    lt_pre = st[(4 + HAS_D) * R * 32 + o] + (spike * weight * gcond);
-                    long_tr[gi] = lt_pre * long_tau;
-                }
-            }
-            sb[j * 32 + lane] = st_pre;
-            if (LONG) sb[R * 32 + j * 32 + lane] = lt_pre;
-        }
-    }
-    __syncthreads();
-    if (nchunks > 0) consume(nchunks - 1);
-    if (colok) {
-        int to = dest_of<SUBSET ? T_SUBSET : T_FC>(g, col);
-        if (warp == 0) short_cond[to] += short_sum;
-        if (LONG && warp == 1) long_cond[to] += long_sum;
-    }
-}
-
-template <int SR, bool LONG, bool SUBSET>
-size_t iz_cols_smem() {
-    constexpr int NA = 4 + (SR == S_BIT ? 1 : 0) + (LONG ? 1 : 0);
-    return (size_t)(kColsS * NA * kColsR * 32 + 2 * 2 * kColsR * 32) * sizeof(float);
-}
-
 // Source of kernel position k of destination d for a non-convolutional
 // convergent connection (synapse_kernel.h:384-421); -1 if it is skipped.
 __device__ __forceinline__ int conv_source(const DGeom& g, int d, int k) {
@@ -359,41 +248,6 @@ static bool matrix_shape(const Connection& c, int& nrows, int& ncols) {
         return true;
     }
     return false;
-}
-
-struct IzColsArgs {
-    DGeom g;
-    int nrows, ncols;
-    const uint32_t* src;
-    const float *w, *stp_r, *stp_w;
-    const int* delays;
-    float *short_tr, *long_tr;
-    float gcond, short_tau, long_tau;
-    float *short_cond, *long_cond;
-};
-
-template <int SR, bool LONG, bool SUBSET>
-static void launch_cols_t(const IzColsArgs& a, cudaStream_t s) {
-    static bool configured = false;
-    size_t smem = iz_cols_smem<SR, LONG, SUBSET>();
-    if (!configured) {
-        SG_CUDA(cudaFuncSetAttribute(k_iz_activate_cols<SR, LONG, SUBSET>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = true;
-    }
-    k_iz_activate_cols<SR, LONG, SUBSET><<<blocks_for(a.ncols, 32), 256, smem, s>>>(
-        a.g, a.nrows, a.ncols, a.src, a.w, a.stp_r, a.stp_w, a.delays, a.short_tr, a.long_tr,
-        a.gcond, a.short_tau, a.long_tau, a.short_cond, a.long_cond);
-    SG_LAUNCH_CHECK();
-}
-
-template <int SR>
-static void launch_cols(const IzColsArgs& a, bool long_trace, bool subset, cudaStream_t s) {
-    if (long_trace) {
-        if (subset) launch_cols_t<SR, true, true>(a, s); else launch_cols_t<SR, true, false>(a, s);
-    } else {
-        if (subset) launch_cols_t<SR, false, true>(a, s); else launch_cols_t<SR, false, false>(a, s);
-    }
 }
 
 // Gap junctions (izhikevich_attributes.cpp:354-366)
@@ -511,7 +365,7 @@ __global__ void __launch_bounds__(256) k_iz_learn_2d(
     float dest_spike = extract<SR>(dest_out[to], 0);
     int r0 = blockIdx.y * rows_per_block, r1 = min(nrows, r0 + rows_per_block);
     for (int row = r0; row < r1; ++row) {
-        size_t wi = (size_t)row * ncols + col;
+        size_t wi = (size_t)banded_index(col, row, nrows);
         iz_learn_synapse<SUB>(wi, __ldg(from_tss + row_source<SUBSET>(g, row)), dest_spike,
                               dest_exc_trace, dest_tss, lr, stp_flag, max_weight, w, presyn, wd,
                               stp_r, stp_w, lut);
@@ -585,7 +439,7 @@ class IzhikevichModel : public Model {
         cs.params["stp"] = c.parameter("short term plasticity", "true") == "true" ? 1.0f : 0.0f;
         for (const char* k : {"short trace", "long trace", "presyn trace", "short term R",
                               "short term w", "weight derivatives"})
-            cs.vars[k] = st.add_array(k, 'f', n, LAYOUT_MATRIX, R, C);
+            cs.vars[k] = st.add_array(k, 'f', n, matrix_layout(c), R, C);
         size_t tss_n = std::max<size_t>(n, c.from->size);
         cs.vars["time since spike"] = st.add_array("time since spike", 'i', tss_n, LAYOUT_SOURCE,
                                                    1, 1, c.from->size);
@@ -600,7 +454,7 @@ class IzhikevichModel : public Model {
         for (size_t i = 0; i < tss_n; ++i) tss[i] = 32;
 
         if (!cs.delays) {
-            cs.delays = st.add_array("delays", 'i', n, LAYOUT_MATRIX, R, C);
+            cs.delays = st.add_array("delays", 'i', n, matrix_layout(c), R, C);
             int32_t* dl = cs.delays->hi();
             if (c.parameter("myelinated", "false") == "true") {
                 for (size_t i = 0; i < n; ++i) dl[i] = c.delay;
@@ -631,9 +485,8 @@ class IzhikevichModel : public Model {
         cs.last_visits = st.add_array("last visits", 'i', (size_t)nsrc * 32);
         int32_t* cnt = cs.visit_counts->hi();
         int32_t* last = cs.last_visits->hi();
-        const bool transposed = R > 1 && C > 1;
         enumerate_visits(c, [&](int, int, int from, long wi, int, int) {
-            long dev = transposed ? (wi % C) * (long)R + wi / C : wi;
+            long dev = (long)device_index(*cs.weights, (size_t)wi);
             last[(size_t)from * 32 + (cnt[from] % 32)] = (int)dev;
             cnt[from]++;
         });
@@ -718,7 +571,7 @@ class IzhikevichModel : public Model {
             return;
         }
         int nrows = 0, ncols = 0;
-        if (matrix_shape(c, nrows, ncols) && ncols % 4 == 0) {
+        if (matrix_shape(c, nrows, ncols)) {
             if (!cs.device_plan_tried) {
                 cs.device_plan_tried = true;
                 const bool bit = c.from->output_type == OUT_BIT;
@@ -734,16 +587,6 @@ class IzhikevichModel : public Model {
                 ctx.count();
                 return;
             }
-            IzColsArgs a{cs.geom, nrows, ncols, src, cs.weights->df(), cs.var("short term R")->df(),
-                         cs.var("short term w")->df(), cs.delays->di(), cs.var("short trace")->df(),
-                         cs.var("long trace")->df(), g, stau, ltau, sc, lc};
-            int sr = (int)c.from->output_type;
-            bool subset = c.type == SUBSET;
-            if (sr == S_FLOAT) launch_cols<S_FLOAT>(a, lname != nullptr, subset, ctx.stream);
-            else if (sr == S_BIT) launch_cols<S_BIT>(a, lname != nullptr, subset, ctx.stream);
-            else launch_cols<S_INT>(a, lname != nullptr, subset, ctx.stream);
-            ctx.count();
-            return;
         }
 #define SG_IZ_ACT(LONG)                                                                        \
     SG_DISPATCH_TYPE_SRC((int)c.type, (int)c.from->output_type,                                \

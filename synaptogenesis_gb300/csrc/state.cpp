@@ -86,6 +86,8 @@ Array* State::add_array(const std::string& name, char dtype, size_t count, Array
     a->name = name;
     a->dtype = dtype;
     a->count = count;
+    if (!dev_count && layout == LAYOUT_BANDED)     // whole bands of destinations
+        dev_count = (size_t)((rows + kBand - 1) / kBand) * kBand * (size_t)cols;
     a->dev_count = dev_count ? dev_count : count;
     a->layout = layout;
     a->rows = rows;
@@ -110,7 +112,7 @@ void State::build() {
         auto cs = std::make_unique<ConnState>();
         cs->conn = c;
         cs->geom = make_geom(*c);
-        cs->weights = add_array("weights", 'f', c->num_weights, LAYOUT_MATRIX, c->matrix_rows,
+        cs->weights = add_array("weights", 'f', c->num_weights, matrix_layout(*c), c->matrix_rows,
                                 c->matrix_cols);
         conns.push_back(std::move(cs));
     }
@@ -158,18 +160,50 @@ static bool needs_transpose(const Array& a) {
     return a.layout == LAYOUT_MATRIX && a.rows > 1 && a.cols > 1;
 }
 
+ArrayLayout matrix_layout(const Connection& c) {
+    return (c.type == FULLY_CONNECTED || c.type == SUBSET) ? LAYOUT_BANDED : LAYOUT_MATRIX;
+}
+
+size_t device_index(const Array& a, size_t i) {
+    if (a.layout == LAYOUT_BANDED) return (size_t)banded_index(i / a.cols, i % a.cols, a.cols);
+    if (needs_transpose(a)) return (i % a.cols) * a.rows + i / a.cols;
+    return i;
+}
+
+// host [rows][cols] -> device bands (padding stays zero) and back.
+static void to_bands(const uint32_t* in, uint32_t* out, int rows, int cols) {
+    for (int r = 0; r < rows; ++r) {
+        uint32_t* o = out + banded_index(r, 0, cols);
+        const uint32_t* ir = in + (size_t)r * cols;
+        for (int c = 0; c < cols; ++c) o[(size_t)c * kBand] = ir[c];
+    }
+}
+
+static void from_bands(const uint32_t* in, uint32_t* out, int rows, int cols) {
+    for (int r = 0; r < rows; ++r) {
+        const uint32_t* i = in + banded_index(r, 0, cols);
+        uint32_t* orow = out + (size_t)r * cols;
+        for (int c = 0; c < cols; ++c) orow[c] = i[(size_t)c * kBand];
+    }
+}
+
 void State::to_device(cudaStream_t stream) {
     if (!arena_) allocate_device();
     if (!on_host_) return;
     for (auto& a : arrays_) {
         if (a->dev_count == 0 || a->scratch) continue;
         const uint32_t* src = a->host.data();
-        if (needs_transpose(*a)) {
+        size_t n = std::min(a->dev_count, a->count);
+        if (a->layout == LAYOUT_BANDED) {
+            scratch_.assign(a->dev_count, 0u);
+            to_bands(a->host.data(), scratch_.data(), a->rows, a->cols);
+            src = scratch_.data();
+            n = a->dev_count;
+        } else if (needs_transpose(*a)) {
             scratch_.resize(a->count);
             transpose(a->host.data(), scratch_.data(), a->rows, a->cols);
             src = scratch_.data();
         }
-        size_t n = std::min(a->dev_count, a->count);
         SG_CUDA(cudaMemcpy(a->dev, src, n * 4, cudaMemcpyHostToDevice));
     }
     for (auto& cp : network->connections)
@@ -185,7 +219,11 @@ void State::to_host(cudaStream_t stream) {
     for (auto& a : arrays_) {
         if (a->dev_count == 0 || a->scratch) continue;
         size_t n = std::min(a->dev_count, a->count);
-        if (needs_transpose(*a)) {
+        if (a->layout == LAYOUT_BANDED) {
+            scratch_.resize(a->dev_count);
+            SG_CUDA(cudaMemcpy(scratch_.data(), a->dev, a->dev_count * 4, cudaMemcpyDeviceToHost));
+            from_bands(scratch_.data(), a->host.data(), a->rows, a->cols);
+        } else if (needs_transpose(*a)) {
             scratch_.resize(a->count);
             SG_CUDA(cudaMemcpy(scratch_.data(), a->dev, n * 4, cudaMemcpyDeviceToHost));
             // device [cols][rows] -> host [rows][cols]

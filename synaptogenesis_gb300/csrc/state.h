@@ -24,6 +24,7 @@ enum ArrayLayout {
     LAYOUT_PLAIN = 0,        // same layout on host and device
     LAYOUT_MATRIX = 1,       // host [rows][cols] <-> device [cols][rows]
     LAYOUT_SOURCE = 2,       // host array of num_weights, device keeps the first from_size
+    LAYOUT_BANDED = 3,       // host [rows][cols] <-> device banded_index(row, col, cols)
 };
 
 struct Array {
@@ -45,6 +46,13 @@ struct Array {
     int32_t* di() const { return static_cast<int32_t*>(dev); }
     uint32_t* du() const { return static_cast<uint32_t*>(dev); }
 };
+
+// Device layout of a connection's per-synapse matrices: banded for fully
+// connected and subset connections, transposed otherwise.
+ArrayLayout matrix_layout(const Connection& c);
+
+// Device element of host element `i` of a per-synapse array.
+size_t device_index(const Array& a, size_t i);
 
 struct LayerState {
     Layer* layer = nullptr;

@@ -7,10 +7,14 @@
 //   one to one       the destination itself                 :257-286
 //   convergent       kernel rows/cols, wrap or skip          :384-461
 //   divergent        inverse window, C truncating division   :506-581
-// Weight indices are in the device layout, where consecutive destinations
-// are contiguous so one thread per destination reads coalesced:
-//   fully connected  w[from * to_size + to]
-//   subset           w[from_k * to_k_size + to_k]
+// Weight indices are in the device layout.  Fully connected and subset
+// matrices are stored in bands of kBand consecutive destinations,
+// [destination / kBand][source][destination % kBand] (banded_index), so the
+// stream of a band of destinations is contiguous in HBM and a chunk of its
+// rows is one block; arborized matrices keep consecutive destinations
+// contiguous:
+//   fully connected  banded_index(to, from, from_size)
+//   subset           banded_index(to_k, from_k, from_k_size)
 //   one to one       w[i]
 //   convergent       w[k * to_size + to]   (convolutional: w[k])
 //   divergent        w[k * to_size + to]   (convolutional: w[k])
@@ -34,6 +38,19 @@ struct DGeom {
 };
 
 enum { T_FC = 0, T_SUBSET = 1, T_ONE = 2, T_CONV = 3, T_DIV = 4 };
+
+constexpr int kBand = 8;
+
+#ifdef __CUDACC__
+#define SG_HOST_DEVICE __host__ __device__ __forceinline__
+#else
+#define SG_HOST_DEVICE inline
+#endif
+
+// Device index of (destination, source) in a banded matrix with nsrc sources.
+SG_HOST_DEVICE long banded_index(long dest, long src, long nsrc) {
+    return (dest / kBand) * (nsrc * kBand) + src * kBand + dest % kBand;
+}
 enum { S_FLOAT = 0, S_BIT = 1, S_INT = 2 };
 
 #ifdef __CUDACC__
@@ -86,12 +103,12 @@ __device__ __forceinline__ int dest_of(const DGeom& g, int d) {
 template <int TYPE, class F>
 __device__ __forceinline__ void for_each_source(const DGeom& g, int d, F&& f) {
     if (TYPE == T_FC) {
-        int wi = d;
-        for (int from = 0; from < g.from_size; ++from, wi += g.to_size) f(from, wi);
+        int wi = (int)banded_index(d, 0, g.from_size);
+        for (int from = 0; from < g.from_size; ++from, wi += kBand) f(from, wi);
     } else if (TYPE == T_SUBSET) {
-        int fk = 0;
+        int wi = (int)banded_index(d, 0, (g.fr1 - g.fr0) * (g.fc1 - g.fc0));
         for (int fr = g.fr0; fr < g.fr1; ++fr)
-            for (int fc = g.fc0; fc < g.fc1; ++fc, ++fk) f(fr * g.from_cols + fc, fk * g.tk_size + d);
+            for (int fc = g.fc0; fc < g.fc1; ++fc, wi += kBand) f(fr * g.from_cols + fc, wi);
     } else if (TYPE == T_ONE) {
         f(d, d);
     } else if (TYPE == T_CONV) {

@@ -216,7 +216,7 @@ void init_weights(State& st, ConnState& cs) {
     }
     if (cfg.has("delay callback")) {
         if (!cs.delays) {
-            cs.delays = st.add_array("delays", 'i', n, LAYOUT_MATRIX, c.matrix_rows, c.matrix_cols);
+            cs.delays = st.add_array("delays", 'i', n, matrix_layout(c), c.matrix_rows, c.matrix_cols);
             for (size_t i = 0; i < n; ++i) cs.delays->hi()[i] = c.delay;
         }
         Callbacks::find(cb.delay, cfg.get("delay callback"), "delay")(id, (int)n, w, cs.delays->hi());
