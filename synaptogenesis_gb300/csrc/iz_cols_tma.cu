@@ -1,24 +1,29 @@
 // Izhikevich trace activator for fully connected and subset matrices
 // (src/core/state/impl/izhikevich_attributes.cpp:228-352 over the loops of
 // src/core/engine/kernel/synapse_kernel.h:111-251), fed by the Tensor Memory
-// Accelerator's bulk copies.
+// Accelerator.
 //
 // The matrices are banded: [destination / 8][source][destination % 8], so the
-// 32 source rows of a band form one contiguous 1 KB block per array.  Each
-// CTA owns a run of bands (3 or 4 for 4096 destinations: the bands are spread
-// over every SM) and walks the source rows in 32-row chunks:
-//   * one producer thread issues, per chunk, one bulk copy per band and array
-//     (weights, short-term R and w, delays, short and long traces) into an
-//     8-stage shared-memory ring, completing on the stage's mbarrier;
+// kR source rows of a band form one contiguous block per array (1 KB for 32
+// rows).  Each CTA owns a run of bands (3 or 4 for 4096 destinations: the
+// bands are spread over every SM) and walks the source rows in kR-row chunks:
+//   * one producer thread issues, per chunk, one 3-D tensor TMA load per array
+//     (weights, short-term R and w, delays, short and long traces) of box
+//     {8 destinations, kR rows, the CTA's bands} into a shared-memory ring,
+//     completing on the stage's mbarrier;
 //   * all threads compute the chunk's synapses, write the pre-decay traces to
 //     a sums tile and the decayed traces back into the stage;
-//   * the producer writes the decayed traces back with bulk stores;
+//   * the producer writes the decayed traces back with TMA tensor stores;
 //   * one thread per destination adds the chunk's pre-decay traces in source
 //     order, keeping the reference's sequential fp32 sum.
 // Every mbarrier wait is bounded: if one runs out, the kernel records the
 // fact in a device flag, waits (bounded) for its loads in flight, drains its
 // stores and returns; check_iz_cols_errors reports it on the host.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
+#include <mutex>
 
 #include "cuda_check.h"
 #include "iz_cols_tma.cuh"
@@ -27,10 +32,13 @@ namespace sg {
 
 namespace {
 
-constexpr int kR = 32;                   // source rows per chunk
+#ifndef SG_COLS_ROWS
+#define SG_COLS_ROWS 32
+#endif
 #ifndef SG_COLS_STAGES
 #define SG_COLS_STAGES 8
 #endif
+constexpr int kR = SG_COLS_ROWS;         // source rows per chunk
 constexpr int kStages = SG_COLS_STAGES;
 constexpr int kMaxBands = 4;             // bands per CTA at most (32 destinations)
 constexpr int kThreads = 256;
@@ -41,10 +49,15 @@ constexpr int kBlockFloats = kR * kBand; // one band's chunk: 32 rows x 8 destin
 // warp that adds no sums, so neither delays the other.
 constexpr int kProducer = 96;
 
+constexpr int kArrays = 6;               // w, R, w_stp, [delay], short, [long]
+
+struct ColsMaps {
+    CUtensorMap m[2][kArrays];           // [bands of the wider CTAs, narrower][array]
+};
+
 struct ColsParams {
     DGeom g;
     int nrows, ncols, base_bands, extra;
-    const float* arrays[6];              // w, R, w_stp, [delay], short, [long]
     const uint32_t* src;
     float gcond, short_tau, long_tau;
     float* short_cond;
@@ -71,19 +84,20 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
-__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes,
+__device__ __forceinline__ void tma_load3(uint32_t dst, const CUtensorMap* map, int y, int z,
                                           uint32_t bar) {
     asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];"
         :
-        : "r"(dst), "l"(src), "r"(bytes), "r"(bar)
+        : "r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(y), "r"(z), "r"(bar)
         : "memory");
 }
 
-__device__ __forceinline__ void bulk_store(void* dst, uint32_t src, uint32_t bytes) {
-    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+__device__ __forceinline__ void tma_store3(const CUtensorMap* map, int y, int z, uint32_t src) {
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];"
                  :
-                 : "l"(dst), "r"(src), "r"(bytes)
+                 : "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(y), "r"(z), "r"(src)
                  : "memory");
 }
 
@@ -95,15 +109,18 @@ __device__ __forceinline__ int source_of_row(const DGeom& g, int row) {
 }
 
 template <int SR, bool LONG, bool SUBSET>
-__global__ void __launch_bounds__(kThreads, 1) k_iz_cols_bulk(const ColsParams p) {
+__global__ void __launch_bounds__(kThreads, 1)
+    k_iz_cols_bulk(const __grid_constant__ ColsMaps maps, const ColsParams p) {
     constexpr int HAS_D = SR == S_BIT ? 1 : 0;
     constexpr int NA = 4 + HAS_D + (LONG ? 1 : 0);
     constexpr int A_ST = 3 + HAS_D, A_LT = 4 + HAS_D;
     constexpr int kTile = kMaxBands * kBlockFloats;        // floats per array per stage
-    extern __shared__ __align__(128) float smem[];
+    extern __shared__ unsigned char smem_raw[];
     __shared__ uint32_t s_words[2][kR];
     __shared__ int s_abort;
-    float* stages = smem;                                  // [S][NA][bands][32][8]
+    // TMA destinations: 128-byte aligned (the allocation has 128 bytes to spare)
+    float* stages = reinterpret_cast<float*>(                // [S][NA][bands][kR][8]
+        (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     float* sums = stages + (size_t)kStages * NA * kTile;   // [2][2][32][kSumPitch]
     uint64_t* bars = reinterpret_cast<uint64_t*>(sums + 4 * kR * kSumPitch);
 
@@ -112,23 +129,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_iz_cols_bulk(const ColsParams p
     const int band0 = b * p.base_bands + min(b, p.extra);
     const int ncol = nb * kBand;
     const int nchunks = (p.nrows + kR - 1) / kR;
+    const CUtensorMap* mp = maps.m[b < p.extra ? 0 : 1];
     auto tile = [&](int s, int a) { return stages + ((size_t)s * NA + a) * kTile; };
-    auto block_src = [&](int a, int band, int ch) {        // first float of a band's chunk
-        return p.arrays[a] + ((size_t)(band0 + band) * p.nrows + (size_t)ch * kR) * kBand;
-    };
     auto chunk_rows = [&](int ch) { return min(kR, p.nrows - ch * kR); };
 
     auto issue = [&](int ch) {                             // producer only
         if (ch >= nchunks) return;
         const int s = ch % kStages;
         const uint32_t bar = smem_u32(&bars[s]);
-        const uint32_t bytes = (uint32_t)chunk_rows(ch) * kBand * 4;
+        // the full box is counted, rows past the end included (zero-filled)
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
-                     "r"(bytes * NA * nb)
+                     "r"((uint32_t)(NA * nb * kBlockFloats * 4))
                      : "memory");
-        for (int a = 0; a < NA; ++a)
-            for (int k = 0; k < nb; ++k)
-                bulk_load(smem_u32(tile(s, a) + k * kBlockFloats), block_src(a, k, ch), bytes, bar);
+        for (int a = 0; a < NA; ++a) tma_load3(smem_u32(tile(s, a)), &mp[a], ch * kR, band0, bar);
     };
     auto load_words = [&](int ch) {                        // threads 0..31
         if (tid < kR) {
@@ -217,14 +230,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_iz_cols_bulk(const ColsParams p
         __syncthreads();
         if (s_abort) break;
         if (tid == kProducer) {
-            const uint32_t bytes = (uint32_t)chunk_rows(ch) * kBand * 4;
-            for (int k = 0; k < nb; ++k) {
-                bulk_store(const_cast<float*>(block_src(A_ST, k, ch)),
-                           smem_u32(tile(s, A_ST) + k * kBlockFloats), bytes);
-                if (LONG)
-                    bulk_store(const_cast<float*>(block_src(A_LT, k, ch)),
-                               smem_u32(tile(s, A_LT) + k * kBlockFloats), bytes);
-            }
+            tma_store3(&mp[A_ST], ch * kR, band0, smem_u32(tile(s, A_ST)));
+            if (LONG) tma_store3(&mp[A_LT], ch * kR, band0, smem_u32(tile(s, A_LT)));
             asm volatile("cp.async.bulk.commit_group;" ::: "memory");
             // the stage about to be refilled was stored from one chunk ago
             asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
@@ -258,13 +265,28 @@ __global__ void __launch_bounds__(kThreads, 1) k_iz_cols_bulk(const ColsParams p
 }
 
 size_t cols_smem_bytes(int na) {
-    return (size_t)kStages * na * kMaxBands * kBlockFloats * 4 + (size_t)4 * kR * kSumPitch * 4 +
-           kStages * sizeof(uint64_t);
+    return 128 + (size_t)kStages * na * kMaxBands * kBlockFloats * 4 +
+           (size_t)4 * kR * kSumPitch * 4 + kStages * sizeof(uint64_t);
 }
 
 }  // namespace
 
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    });
+    return fn;
+}
+
 struct IzColsPlan {
+    ColsMaps maps;
     ColsParams base;
     int n_cta = 0, na = 0;
     bool has_delay = false, long_trace = false;
@@ -276,6 +298,8 @@ std::shared_ptr<IzColsPlan> make_iz_cols_plan(int nrows, int ncols, const float*
                                               const int* delays, float* short_tr,
                                               float* long_tr, int ctas) {
     if (nrows < 1 || ncols < 1) return nullptr;
+    auto encode = encode_fn();
+    if (!encode) return nullptr;
     int dev = 0, sms = 0, optin = 0;
     SG_CUDA(cudaGetDevice(&dev));
     SG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -295,13 +319,31 @@ std::shared_ptr<IzColsPlan> make_iz_cols_plan(int nrows, int ncols, const float*
     p.ncols = ncols;
     p.base_bands = bands / plan->n_cta;
     p.extra = bands % plan->n_cta;
+    const void* arrays[kArrays];
     int a = 0;
-    p.arrays[a++] = w;
-    p.arrays[a++] = stp_r;
-    p.arrays[a++] = stp_w;
-    if (plan->has_delay) p.arrays[a++] = reinterpret_cast<const float*>(delays);
-    p.arrays[a++] = short_tr;
-    if (plan->long_trace) p.arrays[a++] = long_tr;
+    arrays[a++] = w;
+    arrays[a++] = stp_r;
+    arrays[a++] = stp_w;
+    if (plan->has_delay) arrays[a++] = delays;
+    arrays[a++] = short_tr;
+    if (plan->long_trace) arrays[a++] = long_tr;
+    // [band][source row][8 destinations] as a 3-D tensor; box {8, kR, bands}
+    for (int wide = 0; wide < 2; ++wide) {
+        const int nb = p.base_bands + (wide == 0 ? 1 : 0);
+        if (nb < 1 || nb > kMaxBands || (wide == 0 && p.extra == 0)) continue;
+        for (int i = 0; i < plan->na; ++i) {
+            cuuint64_t dims[3] = {(cuuint64_t)kBand, (cuuint64_t)nrows, (cuuint64_t)bands};
+            cuuint64_t strides[2] = {(cuuint64_t)kBand * 4, (cuuint64_t)nrows * kBand * 4};
+            cuuint32_t box[3] = {(cuuint32_t)kBand, (cuuint32_t)kR, (cuuint32_t)nb};
+            cuuint32_t estr[3] = {1, 1, 1};
+            CUresult r = encode(&plan->maps.m[wide][i], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                                const_cast<void*>(arrays[i]), dims, strides, box, estr,
+                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) return nullptr;
+        }
+    }
     return plan;
 }
 
@@ -313,7 +355,7 @@ static void launch_t(const IzColsPlan& plan, const ColsParams& p, cudaStream_t s
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem));
         configured = (int)plan.smem;
     }
-    k_iz_cols_bulk<SR, LONG, SUBSET><<<plan.n_cta, kThreads, plan.smem, s>>>(p);
+    k_iz_cols_bulk<SR, LONG, SUBSET><<<plan.n_cta, kThreads, plan.smem, s>>>(plan.maps, p);
     SG_LAUNCH_CHECK();
 }
 
@@ -350,7 +392,7 @@ void check_iz_cols_errors() {
     if (flag) {
         int zero = 0;
         SG_CUDA(cudaMemcpyToSymbol(g_cols_error, &zero, sizeof(int)));
-        throw SgError("Izhikevich column activator: a bulk-copy pipeline wait timed out");
+        throw SgError("Izhikevich column activator: a TMA pipeline wait timed out");
     }
 }
 
