@@ -7,13 +7,15 @@
 // kR source rows of a band form one contiguous block per array (1 KB for 32
 // rows).  Each CTA owns a run of bands (3 or 4 for 4096 destinations: the
 // bands are spread over every SM) and walks the source rows in kR-row chunks:
-//   * one producer thread issues, per chunk, one 3-D tensor TMA load per array
+//   * a producer warp issues, per chunk, one 3-D tensor TMA load per array
 //     (weights, short-term R and w, delays, short and long traces) of box
 //     {8 destinations, kR rows, the CTA's bands} into a shared-memory ring,
 //     completing on the stage's mbarrier;
-//   * all threads compute the chunk's synapses, write the pre-decay traces to
-//     a sums tile and the decayed traces back into the stage;
-//   * the producer writes the decayed traces back with TMA tensor stores;
+//   * 8 compute warps compute the chunk's synapses, write the pre-decay traces
+//     to a sums tile and the decayed traces back into the stage, and arrive on
+//     the stage's "consumed" mbarrier (they synchronise only among themselves);
+//   * the producer writes the decayed traces back with TMA tensor stores and
+//     refills the stage once the stores have read it;
 //   * one thread per destination adds the chunk's pre-decay traces in source
 //     order, keeping the reference's sequential fp32 sum.
 // Every mbarrier wait is bounded: if one runs out, the kernel records the
@@ -41,13 +43,14 @@ namespace {
 constexpr int kR = SG_COLS_ROWS;         // source rows per chunk
 constexpr int kStages = SG_COLS_STAGES;
 constexpr int kMaxBands = 4;             // bands per CTA at most (32 destinations)
-constexpr int kThreads = 256;
+constexpr int kCompute = 256;            // compute threads (8 warps)
+constexpr int kThreads = kCompute + 32;  // plus one producer warp
 constexpr int kSumPitch = 40;            // sums row pitch: conflict-free writes and reads
 constexpr int kWaitLimit = 1 << 20;
 constexpr int kBlockFloats = kR * kBand; // one band's chunk: 32 rows x 8 destinations
-// The thread that issues the copies (and waits on its store groups): in a
-// warp that adds no sums, so neither delays the other.
-constexpr int kProducer = 96;
+// The thread that issues the TMA copies and waits on its store groups: lane 0
+// of the producer warp, which takes no part in the compute warps' barriers.
+constexpr int kProducer = kCompute;
 
 constexpr int kArrays = 6;               // w, R, w_stp, [delay], short, [long]
 
@@ -121,8 +124,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     // TMA destinations: 128-byte aligned (the allocation has 128 bytes to spare)
     float* stages = reinterpret_cast<float*>(                // [S][NA][bands][kR][8]
         (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-    float* sums = stages + (size_t)kStages * NA * kTile;   // [2][2][32][kSumPitch]
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sums + 4 * kR * kSumPitch);
+    float* sums = stages + (size_t)kStages * NA * kTile;   // [2][2][kR][kSumPitch]
+    uint64_t* full = reinterpret_cast<uint64_t*>(sums + 4 * kR * kSumPitch);
+    uint64_t* consumed = full + kStages;
 
     const int tid = threadIdx.x, b = blockIdx.x;
     const int nb = p.base_bands + (b < p.extra ? 1 : 0);
@@ -132,141 +136,161 @@ __global__ void __launch_bounds__(kThreads, 1)
     const CUtensorMap* mp = maps.m[b < p.extra ? 0 : 1];
     auto tile = [&](int s, int a) { return stages + ((size_t)s * NA + a) * kTile; };
     auto chunk_rows = [&](int ch) { return min(kR, p.nrows - ch * kR); };
+    auto parity = [](int ch) { return (uint32_t)((ch / kStages) & 1); };
 
-    auto issue = [&](int ch) {                             // producer only
-        if (ch >= nchunks) return;
-        const int s = ch % kStages;
-        const uint32_t bar = smem_u32(&bars[s]);
-        // the full box is counted, rows past the end included (zero-filled)
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
-                     "r"((uint32_t)(NA * nb * kBlockFloats * 4))
-                     : "memory");
-        for (int a = 0; a < NA; ++a) tma_load3(smem_u32(tile(s, a)), &mp[a], ch * kR, band0, bar);
-    };
-    auto load_words = [&](int ch) {                        // threads 0..31
+    if (tid == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[s])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&consumed[s])),
+                         "r"(kCompute));
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_abort = 0;
+    }
+    auto load_words = [&](int ch) {                        // compute threads 0..kR-1
         if (tid < kR) {
             const int row = ch * kR + tid;
             s_words[ch & 1][tid] =
                 (ch < nchunks && row < p.nrows) ? __ldg(p.src + source_of_row<SUBSET>(p.g, row)) : 0u;
         }
     };
-
-    if (tid == 0) {
-        for (int s = 0; s < kStages; ++s)
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[s])));
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        s_abort = 0;
-    }
     load_words(0);
     __syncthreads();
-    if (tid == kProducer)
-        for (int c = 0; c < kStages - 1; ++c) issue(c);
 
-    // this thread's elements: offset e = band * 256 + row * 8 + lane8
-    constexpr int kPer = kTile / kThreads;
-    int eo[kPer], ej[kPer], ecol[kPer];
-#pragma unroll
-    for (int k = 0; k < kPer; ++k) {
-        const int e = tid + k * kThreads;
-        eo[k] = e < nb * kBlockFloats ? e : -1;
-        ej[k] = (e % kBlockFloats) / kBand;
-        ecol[k] = (e / kBlockFloats) * kBand + e % kBand;
-    }
-    float short_sum = 0.0f, long_sum = 0.0f;
-    const bool short_owner = tid < ncol;
-    const bool long_owner = LONG && tid >= 128 && tid < 128 + ncol;
-    // A destination's pre-decay traces of a chunk are loaded first and then
-    // added in source order: the loads overlap, only the adds are serial.
-    auto consume = [&](int ch) {
-        if (!short_owner && !long_owner) return;
-        const int nr = chunk_rows(ch);
-        const float* col = sums + (ch & 1) * 2 * kR * kSumPitch +
-                           (short_owner ? tid : kR * kSumPitch + (tid - 128));
-        float acc = short_owner ? short_sum : long_sum;
-        if (nr == kR) {
-            float v[kR];
-#pragma unroll
-            for (int j = 0; j < kR; ++j) v[j] = col[j * kSumPitch];
-#pragma unroll
-            for (int j = 0; j < kR; ++j) acc += v[j];
-        } else {
-            for (int j = 0; j < nr; ++j) acc += col[j * kSumPitch];
-        }
-        if (short_owner) short_sum = acc;
-        else long_sum = acc;
-    };
-
-    int ch = 0;
-    for (; ch < nchunks; ++ch) {
-        const int s = ch % kStages;
-        if (!mbar_wait(smem_u32(&bars[s]), (uint32_t)((ch / kStages) & 1))) s_abort = 1;
-        if (ch > 0) consume(ch - 1);
-        float* sb = sums + (ch & 1) * 2 * kR * kSumPitch;
-        const float* tw = tile(s, 0);
-        const float* tr = tile(s, 1);
-        const float* tsw = tile(s, 2);
-        float* tst = tile(s, A_ST);
-#pragma unroll
-        for (int k = 0; k < kPer; ++k) {
-            const int o = eo[k];
-            if (o < 0) continue;
-            const uint32_t word = s_words[ch & 1][ej[k]];
-            const int delay = HAS_D ? __float_as_int(tile(s, 3)[o]) : 0;
-            const float spike = extract<SR>(word, delay);
-            const float weight = tw[o] * (tr[o] * tsw[o]);
-            const float st = tst[o] + (spike * weight * p.gcond);
-            const int so = ej[k] * kSumPitch + ecol[k];
-            sb[so] = st;
-            tst[o] = st * p.short_tau;
-            if (LONG) {
-                float* tlt = tile(s, A_LT);
-                const float lt = tlt[o] + (spike * weight * p.gcond);
-                sb[kR * kSumPitch + so] = lt;
-                tlt[o] = lt * p.long_tau;
+    if (tid >= kCompute) {
+        // ---- producer warp: loads into free stages, stores of finished ones
+        if (tid == kProducer) {
+            auto issue = [&](int ch) {
+                const int s = ch % kStages;
+                const uint32_t bar = smem_u32(&full[s]);
+                // the full box is counted, rows past the end included (zero-filled)
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                             "r"((uint32_t)(NA * nb * kBlockFloats * 4))
+                             : "memory");
+                for (int a = 0; a < NA; ++a)
+                    tma_load3(smem_u32(tile(s, a)), &mp[a], ch * kR, band0, bar);
+            };
+            int issued = min(kStages, nchunks);
+            for (int c = 0; c < issued; ++c) issue(c);
+            int ch = 0;
+            for (; ch < nchunks; ++ch) {
+                const int s = ch % kStages;
+                if (!mbar_wait(smem_u32(&consumed[s]), parity(ch))) break;
+                tma_store3(&mp[A_ST], ch * kR, band0, smem_u32(tile(s, A_ST)));
+                if (LONG) tma_store3(&mp[A_LT], ch * kR, band0, smem_u32(tile(s, A_LT)));
+                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                if (ch + kStages < nchunks) {
+                    // the stage is refilled once its traces have been read out
+                    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                    issue(ch + kStages);
+                    ++issued;
+                }
             }
-        }
-        load_words(ch + 1);
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (s_abort) break;
-        if (tid == kProducer) {
-            tma_store3(&mp[A_ST], ch * kR, band0, smem_u32(tile(s, A_ST)));
-            if (LONG) tma_store3(&mp[A_LT], ch * kR, band0, smem_u32(tile(s, A_LT)));
-            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-            // the stage about to be refilled was stored from one chunk ago
-            asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
-            issue(ch + kStages - 1);
-        }
-    }
-
-    if (s_abort) {
-        // loads issued for chunks ch .. ch+S-2 may still be landing: wait for
-        // them (bounded) before the shared memory goes away
-        if (tid == kProducer) {
-            atomicExch(&g_cols_error, 1);
-            for (int c = ch; c < min(nchunks, ch + kStages - 1); ++c)
-                mbar_wait(smem_u32(&bars[c % kStages]), (uint32_t)((c / kStages) & 1));
+            if (ch < nchunks) {
+                // the compute warps stopped: let the loads in flight land
+                // (bounded) before the shared memory goes away
+                atomicExch(&g_cols_error, 1);
+                for (int c = ch; c < issued; ++c) mbar_wait(smem_u32(&full[c % kStages]), parity(c));
+            }
             asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
         }
-        __syncthreads();
-        return;
-    }
-    if (nchunks > 0) consume(nchunks - 1);
-    if (short_owner || long_owner) {
-        const int c = short_owner ? tid : tid - 128;
-        const int col = band0 * kBand + c;
-        if (col < p.ncols) {
-            const int to = dest_of<SUBSET ? T_SUBSET : T_FC>(p.g, col);
-            if (short_owner) p.short_cond[to] += short_sum;
-            else p.long_cond[to] += long_sum;
+    } else {
+        // ---- compute warps
+        constexpr int kPer = kTile / kCompute;
+        int eo[kPer], ej[kPer], ecol[kPer];             // offset band*kR*8 + row*8 + lane8
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            const int e = tid + k * kCompute;
+            eo[k] = e < nb * kBlockFloats ? e : -1;
+            ej[k] = (e % kBlockFloats) / kBand;
+            ecol[k] = (e / kBlockFloats) * kBand + e % kBand;
+        }
+        float short_sum = 0.0f, long_sum = 0.0f;
+        const bool short_owner = tid < ncol;
+        const bool long_owner = LONG && tid >= 128 && tid < 128 + ncol;
+        // A destination's pre-decay traces of a chunk are loaded first and
+        // then added in source order: the loads overlap, only the adds are serial.
+        auto consume = [&](int ch) {
+            if (!short_owner && !long_owner) return;
+            const int nr = chunk_rows(ch);
+            const float* col = sums + (ch & 1) * 2 * kR * kSumPitch +
+                               (short_owner ? tid : kR * kSumPitch + (tid - 128));
+            float acc = short_owner ? short_sum : long_sum;
+            if (nr == kR) {
+                float v[kR];
+#pragma unroll
+                for (int j = 0; j < kR; ++j) v[j] = col[j * kSumPitch];
+#pragma unroll
+                for (int j = 0; j < kR; ++j) acc += v[j];
+            } else {
+                for (int j = 0; j < nr; ++j) acc += col[j * kSumPitch];
+            }
+            if (short_owner) short_sum = acc;
+            else long_sum = acc;
+        };
+
+        bool aborted = false;
+        for (int ch = 0; ch < nchunks; ++ch) {
+            const int s = ch % kStages;
+            if (!mbar_wait(smem_u32(&full[s]), parity(ch))) s_abort = 1;
+            if (ch > 0) consume(ch - 1);
+            float* sb = sums + (ch & 1) * 2 * kR * kSumPitch;
+            const float* tw = tile(s, 0);
+            const float* tr = tile(s, 1);
+            const float* tsw = tile(s, 2);
+            float* tst = tile(s, A_ST);
+#pragma unroll
+            for (int k = 0; k < kPer; ++k) {
+                const int o = eo[k];
+                if (o < 0) continue;
+                const uint32_t word = s_words[ch & 1][ej[k]];
+                const int delay = HAS_D ? __float_as_int(tile(s, 3)[o]) : 0;
+                const float spike = extract<SR>(word, delay);
+                const float weight = tw[o] * (tr[o] * tsw[o]);
+                const float st = tst[o] + (spike * weight * p.gcond);
+                const int so = ej[k] * kSumPitch + ecol[k];
+                sb[so] = st;
+                tst[o] = st * p.short_tau;
+                if (LONG) {
+                    float* tlt = tile(s, A_LT);
+                    const float lt = tlt[o] + (spike * weight * p.gcond);
+                    sb[kR * kSumPitch + so] = lt;
+                    tlt[o] = lt * p.long_tau;
+                }
+            }
+            load_words(ch + 1);
+            // the decayed traces are read by the TMA store: generic-proxy
+            // writes become visible to the async proxy before the arrival
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&consumed[s]))
+                         : "memory");
+            asm volatile("bar.sync 1, %0;" ::"n"(kCompute) : "memory");
+            if (s_abort) {
+                aborted = true;
+                break;
+            }
+        }
+        if (aborted) {
+            if (tid == 0) atomicExch(&g_cols_error, 1);
+        } else {
+            if (nchunks > 0) consume(nchunks - 1);
+            if (short_owner || long_owner) {
+                const int c = short_owner ? tid : tid - 128;
+                const int col = band0 * kBand + c;
+                if (col < p.ncols) {
+                    const int to = dest_of<SUBSET ? T_SUBSET : T_FC>(p.g, col);
+                    if (short_owner) p.short_cond[to] += short_sum;
+                    else p.long_cond[to] += long_sum;
+                }
+            }
         }
     }
-    if (tid == kProducer) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    __syncthreads();
 }
 
 size_t cols_smem_bytes(int na) {
     return 128 + (size_t)kStages * na * kMaxBands * kBlockFloats * 4 +
-           (size_t)4 * kR * kSumPitch * 4 + kStages * sizeof(uint64_t);
+           (size_t)4 * kR * kSumPitch * 4 + 2 * kStages * sizeof(uint64_t);
 }
 
 }  // namespace
