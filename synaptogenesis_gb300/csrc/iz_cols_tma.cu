@@ -7,9 +7,9 @@
 // kR source rows of a band form one contiguous block per array (1 KB for 32
 // rows).  Each CTA owns a run of bands (3 or 4 for 4096 destinations: the
 // bands are spread over every SM) and walks the source rows in kR-row chunks:
-//   * a producer warp issues, per chunk, one 3-D tensor TMA load per array
-//     (weights, short-term R and w, delays, short and long traces) of box
-//     {8 destinations, kR rows, the CTA's bands} into a shared-memory ring,
+//   * a producer warp issues, per chunk, one 2-D tensor TMA load per array
+//     (weights, short-term R and w, delays, short and long traces) whose box
+//     rows are the CTA's bands' contiguous chunks, into a shared-memory ring,
 //     completing on the stage's mbarrier;
 //   * 8 compute warps compute the chunk's synapses, write the pre-decay traces
 //     to a sums tile and the decayed traces back into the stage, and arrive on
@@ -35,7 +35,7 @@ namespace sg {
 namespace {
 
 #ifndef SG_COLS_ROWS
-#define SG_COLS_ROWS 32
+#define SG_COLS_ROWS 32                  // kR * 8 floats per TMA box row: at most 256
 #endif
 #ifndef SG_COLS_STAGES
 #define SG_COLS_STAGES 8
@@ -87,20 +87,22 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
-__device__ __forceinline__ void tma_load3(uint32_t dst, const CUtensorMap* map, int y, int z,
+// A banded array seen as a 2-D tensor [band][source row * 8 + lane]: one box
+// row is a band's whole chunk (kR * 8 contiguous floats).
+__device__ __forceinline__ void tma_load2(uint32_t dst, const CUtensorMap* map, int x, int y,
                                           uint32_t bar) {
     asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3, %4}], [%5];"
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];"
         :
-        : "r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(y), "r"(z), "r"(bar)
+        : "r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
         : "memory");
 }
 
-__device__ __forceinline__ void tma_store3(const CUtensorMap* map, int y, int z, uint32_t src) {
-    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];"
+__device__ __forceinline__ void tma_store2(const CUtensorMap* map, int x, int y, uint32_t src) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];"
                  :
-                 : "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(y), "r"(z), "r"(src)
+                 : "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(src)
                  : "memory");
 }
 
@@ -168,7 +170,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                              "r"((uint32_t)(NA * nb * kBlockFloats * 4))
                              : "memory");
                 for (int a = 0; a < NA; ++a)
-                    tma_load3(smem_u32(tile(s, a)), &mp[a], ch * kR, band0, bar);
+                    tma_load2(smem_u32(tile(s, a)), &mp[a], ch * kBlockFloats, band0, bar);
             };
             int issued = min(kStages, nchunks);
             for (int c = 0; c < issued; ++c) issue(c);
@@ -176,8 +178,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (; ch < nchunks; ++ch) {
                 const int s = ch % kStages;
                 if (!mbar_wait(smem_u32(&consumed[s]), parity(ch))) break;
-                tma_store3(&mp[A_ST], ch * kR, band0, smem_u32(tile(s, A_ST)));
-                if (LONG) tma_store3(&mp[A_LT], ch * kR, band0, smem_u32(tile(s, A_LT)));
+                tma_store2(&mp[A_ST], ch * kBlockFloats, band0, smem_u32(tile(s, A_ST)));
+                if (LONG) tma_store2(&mp[A_LT], ch * kBlockFloats, band0, smem_u32(tile(s, A_LT)));
                 asm volatile("cp.async.bulk.commit_group;" ::: "memory");
                 if (ch + kStages < nchunks) {
                     // the stage is refilled once its traces have been read out
@@ -351,16 +353,16 @@ std::shared_ptr<IzColsPlan> make_iz_cols_plan(int nrows, int ncols, const float*
     if (plan->has_delay) arrays[a++] = delays;
     arrays[a++] = short_tr;
     if (plan->long_trace) arrays[a++] = long_tr;
-    // [band][source row][8 destinations] as a 3-D tensor; box {8, kR, bands}
+    // [band][source row * 8 + lane] as a 2-D tensor; box {kR * 8, bands}
     for (int wide = 0; wide < 2; ++wide) {
         const int nb = p.base_bands + (wide == 0 ? 1 : 0);
         if (nb < 1 || nb > kMaxBands || (wide == 0 && p.extra == 0)) continue;
         for (int i = 0; i < plan->na; ++i) {
-            cuuint64_t dims[3] = {(cuuint64_t)kBand, (cuuint64_t)nrows, (cuuint64_t)bands};
-            cuuint64_t strides[2] = {(cuuint64_t)kBand * 4, (cuuint64_t)nrows * kBand * 4};
-            cuuint32_t box[3] = {(cuuint32_t)kBand, (cuuint32_t)kR, (cuuint32_t)nb};
-            cuuint32_t estr[3] = {1, 1, 1};
-            CUresult r = encode(&plan->maps.m[wide][i], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+            cuuint64_t dims[2] = {(cuuint64_t)nrows * kBand, (cuuint64_t)bands};
+            cuuint64_t strides[1] = {(cuuint64_t)nrows * kBand * 4};
+            cuuint32_t box[2] = {(cuuint32_t)kBlockFloats, (cuuint32_t)nb};
+            cuuint32_t estr[2] = {1, 1};
+            CUresult r = encode(&plan->maps.m[wide][i], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
                                 const_cast<void*>(arrays[i]), dims, strides, box, estr,
                                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
