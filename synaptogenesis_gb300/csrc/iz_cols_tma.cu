@@ -23,6 +23,7 @@
 // stores and returns; check_iz_cols_errors reports it on the host.
 #include <cuda.h>
 #include <cudaTypedefs.h>
+#include <cuda_pipeline.h>
 
 #include <algorithm>
 #include <mutex>
@@ -121,7 +122,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     constexpr int A_ST = 3 + HAS_D, A_LT = 4 + HAS_D;
     constexpr int kTile = kMaxBands * kBlockFloats;        // floats per array per stage
     extern __shared__ unsigned char smem_raw[];
-    __shared__ uint32_t s_words[2][kR];
+    __shared__ uint32_t s_words[kStages][kR];   // source words, one slot per stage
     __shared__ int s_abort;
     // TMA destinations: 128-byte aligned (the allocation has 128 bytes to spare)
     float* stages = reinterpret_cast<float*>(                // [S][NA][bands][kR][8]
@@ -149,14 +150,21 @@ __global__ void __launch_bounds__(kThreads, 1)
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_abort = 0;
     }
-    auto load_words = [&](int ch) {                        // compute threads 0..kR-1
-        if (tid < kR) {
+    // Source words of a chunk, fetched by warp 0 with cp.async kStages-1
+    // chunks ahead of their use (one commit group per chunk).
+    auto fetch_words = [&](int ch) {
+        if (ch < nchunks && tid < kR) {
             const int row = ch * kR + tid;
-            s_words[ch & 1][tid] =
-                (ch < nchunks && row < p.nrows) ? __ldg(p.src + source_of_row<SUBSET>(p.g, row)) : 0u;
+            if (row < p.nrows)
+                __pipeline_memcpy_async(&s_words[ch % kStages][tid],
+                                        p.src + source_of_row<SUBSET>(p.g, row), 4);
         }
+        __pipeline_commit();
     };
-    load_words(0);
+    if (tid < kR) {
+        for (int c = 0; c < kStages - 1; ++c) fetch_words(c);
+        __pipeline_wait_prior(kStages - 2);                // chunk 0 landed
+    }
     __syncthreads();
 
     if (tid >= kCompute) {
@@ -245,7 +253,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int k = 0; k < kPer; ++k) {
                 const int o = eo[k];
                 if (o < 0) continue;
-                const uint32_t word = s_words[ch & 1][ej[k]];
+                const uint32_t word = s_words[s][ej[k]];
                 const int delay = HAS_D ? __float_as_int(tile(s, 3)[o]) : 0;
                 const float spike = extract<SR>(word, delay);
                 const float weight = tw[o] * (tr[o] * tsw[o]);
@@ -260,7 +268,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                     tlt[o] = lt * p.long_tau;
                 }
             }
-            load_words(ch + 1);
+            if (tid < kR) {
+                fetch_words(ch + kStages - 1);
+                __pipeline_wait_prior(kStages - 2);        // chunk ch+1 landed
+            }
             // the decayed traces are read by the TMA store: generic-proxy
             // writes become visible to the async proxy before the arrival
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
