@@ -12,12 +12,14 @@
 //     rows are the CTA's bands' contiguous chunks, into a shared-memory ring,
 //     completing on the stage's mbarrier;
 //   * 8 compute warps compute the chunk's synapses, write the pre-decay traces
-//     to a sums tile and the decayed traces back into the stage, and arrive on
-//     the stage's "consumed" mbarrier (they synchronise only among themselves);
+//     to a ring of sums tiles and the decayed traces back into the stage, and
+//     arrive on the stage's "consumed" mbarrier (they synchronise only among
+//     themselves; warp 0 also prefetches the chunks' source words);
 //   * the producer writes the decayed traces back with TMA tensor stores and
 //     refills the stage once the stores have read it;
-//   * one thread per destination adds the chunk's pre-decay traces in source
-//     order, keeping the reference's sequential fp32 sum.
+//   * two sum warps, one lane per destination, add each chunk's pre-decay
+//     traces in source order (the reference's sequential fp32 sum) while the
+//     compute warps go on with the next chunks.
 // Every mbarrier wait is bounded: if one runs out, the kernel records the
 // fact in a device flag, waits (bounded) for its loads in flight, drains its
 // stores and returns; check_iz_cols_errors reports it on the host.
@@ -45,13 +47,15 @@ constexpr int kR = SG_COLS_ROWS;         // source rows per chunk
 constexpr int kStages = SG_COLS_STAGES;
 constexpr int kMaxBands = 4;             // bands per CTA at most (32 destinations)
 constexpr int kCompute = 256;            // compute threads (8 warps)
-constexpr int kThreads = kCompute + 32;  // plus one producer warp
+constexpr int kSumWarps = 2;             // short-trace and long-trace sums
+constexpr int kSumBufs = 3;              // chunks of sums in flight to the sum warps
+constexpr int kThreads = kCompute + 32 * kSumWarps + 32;   // plus one producer warp
 constexpr int kSumPitch = 40;            // sums row pitch: conflict-free writes and reads
 constexpr int kWaitLimit = 1 << 20;
 constexpr int kBlockFloats = kR * kBand; // one band's chunk: 32 rows x 8 destinations
 // The thread that issues the TMA copies and waits on its store groups: lane 0
 // of the producer warp, which takes no part in the compute warps' barriers.
-constexpr int kProducer = kCompute;
+constexpr int kProducer = kCompute + 32 * kSumWarps;
 
 constexpr int kArrays = 6;               // w, R, w_stp, [delay], short, [long]
 
@@ -121,15 +125,18 @@ __global__ void __launch_bounds__(kThreads, 1)
     constexpr int NA = 4 + HAS_D + (LONG ? 1 : 0);
     constexpr int A_ST = 3 + HAS_D, A_LT = 4 + HAS_D;
     constexpr int kTile = kMaxBands * kBlockFloats;        // floats per array per stage
+    constexpr int kSumBuf = 2 * kR * kSumPitch;            // one chunk's short + long sums
     extern __shared__ unsigned char smem_raw[];
-    __shared__ uint32_t s_words[kStages][kR];   // source words, one slot per stage
+    __shared__ uint32_t s_words[kStages][kR];              // source words, one slot per stage
     __shared__ int s_abort;
     // TMA destinations: 128-byte aligned (the allocation has 128 bytes to spare)
     float* stages = reinterpret_cast<float*>(                // [S][NA][bands][kR][8]
         (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-    float* sums = stages + (size_t)kStages * NA * kTile;   // [2][2][kR][kSumPitch]
-    uint64_t* full = reinterpret_cast<uint64_t*>(sums + 4 * kR * kSumPitch);
+    float* sums = stages + (size_t)kStages * NA * kTile;   // [kSumBufs][2][kR][kSumPitch]
+    uint64_t* full = reinterpret_cast<uint64_t*>(sums + kSumBufs * kSumBuf);
     uint64_t* consumed = full + kStages;
+    uint64_t* sums_full = consumed + kStages;
+    uint64_t* sums_empty = sums_full + kSumBufs;
 
     const int tid = threadIdx.x, b = blockIdx.x;
     const int nb = p.base_bands + (b < p.extra ? 1 : 0);
@@ -140,12 +147,19 @@ __global__ void __launch_bounds__(kThreads, 1)
     auto tile = [&](int s, int a) { return stages + ((size_t)s * NA + a) * kTile; };
     auto chunk_rows = [&](int ch) { return min(kR, p.nrows - ch * kR); };
     auto parity = [](int ch) { return (uint32_t)((ch / kStages) & 1); };
+    auto sum_parity = [](int ch) { return (uint32_t)((ch / kSumBufs) & 1); };
 
     if (tid == 0) {
         for (int s = 0; s < kStages; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[s])));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&consumed[s])),
                          "r"(kCompute));
+        }
+        for (int q = 0; q < kSumBufs; ++q) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&sums_full[q])),
+                         "r"(kCompute));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&sums_empty[q])),
+                         "r"(32 * kSumWarps));
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_abort = 0;
@@ -167,7 +181,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     __syncthreads();
 
-    if (tid >= kCompute) {
+    if (tid >= kProducer) {
         // ---- producer warp: loads into free stages, stores of finished ones
         if (tid == kProducer) {
             auto issue = [&](int ch) {
@@ -204,6 +218,42 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
         }
+    } else if (tid >= kCompute) {
+        // ---- sum warps: warp kCompute/32 adds the short traces, the next the
+        // long ones; one lane per destination, each chunk's rows in order
+        const int kind = (tid - kCompute) / 32, c = (tid - kCompute) % 32;
+        const bool owner = c < ncol && (kind == 0 || LONG);
+        float acc = 0.0f;
+        int ch = 0;
+        for (; ch < nchunks; ++ch) {
+            const int q = ch % kSumBufs;
+            if (!mbar_wait(smem_u32(&sums_full[q]), sum_parity(ch))) break;
+            if (owner) {
+                const float* col = sums + q * kSumBuf + kind * kR * kSumPitch + c;
+                const int nr = chunk_rows(ch);
+                if (nr == kR) {
+                    float v[kR];
+#pragma unroll
+                    for (int j = 0; j < kR; ++j) v[j] = col[j * kSumPitch];
+#pragma unroll
+                    for (int j = 0; j < kR; ++j) acc += v[j];
+                } else {
+                    for (int j = 0; j < nr; ++j) acc += col[j * kSumPitch];
+                }
+            }
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&sums_empty[q]))
+                         : "memory");
+        }
+        if (ch == nchunks && owner) {
+            const int col = band0 * kBand + c;
+            if (col < p.ncols) {
+                const int to = dest_of<SUBSET ? T_SUBSET : T_FC>(p.g, col);
+                if (kind == 0) p.short_cond[to] += acc;
+                else p.long_cond[to] += acc;
+            }
+        } else if (ch < nchunks && c == 0) {
+            atomicExch(&g_cols_error, 1);
+        }
     } else {
         // ---- compute warps
         constexpr int kPer = kTile / kCompute;
@@ -215,36 +265,15 @@ __global__ void __launch_bounds__(kThreads, 1)
             ej[k] = (e % kBlockFloats) / kBand;
             ecol[k] = (e / kBlockFloats) * kBand + e % kBand;
         }
-        float short_sum = 0.0f, long_sum = 0.0f;
-        const bool short_owner = tid < ncol;
-        const bool long_owner = LONG && tid >= 128 && tid < 128 + ncol;
-        // A destination's pre-decay traces of a chunk are loaded first and
-        // then added in source order: the loads overlap, only the adds are serial.
-        auto consume = [&](int ch) {
-            if (!short_owner && !long_owner) return;
-            const int nr = chunk_rows(ch);
-            const float* col = sums + (ch & 1) * 2 * kR * kSumPitch +
-                               (short_owner ? tid : kR * kSumPitch + (tid - 128));
-            float acc = short_owner ? short_sum : long_sum;
-            if (nr == kR) {
-                float v[kR];
-#pragma unroll
-                for (int j = 0; j < kR; ++j) v[j] = col[j * kSumPitch];
-#pragma unroll
-                for (int j = 0; j < kR; ++j) acc += v[j];
-            } else {
-                for (int j = 0; j < nr; ++j) acc += col[j * kSumPitch];
-            }
-            if (short_owner) short_sum = acc;
-            else long_sum = acc;
-        };
-
         bool aborted = false;
         for (int ch = 0; ch < nchunks; ++ch) {
-            const int s = ch % kStages;
+            const int s = ch % kStages, q = ch % kSumBufs;
             if (!mbar_wait(smem_u32(&full[s]), parity(ch))) s_abort = 1;
-            if (ch > 0) consume(ch - 1);
-            float* sb = sums + (ch & 1) * 2 * kR * kSumPitch;
+            // the sums buffer is free once the sum warps have read chunk ch - kSumBufs
+            if (ch >= kSumBufs &&
+                !mbar_wait(smem_u32(&sums_empty[q]), sum_parity(ch - kSumBufs)))
+                s_abort = 1;
+            float* sb = sums + q * kSumBuf;
             const float* tw = tile(s, 0);
             const float* tr = tile(s, 1);
             const float* tsw = tile(s, 2);
@@ -268,6 +297,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                     tlt[o] = lt * p.long_tau;
                 }
             }
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&sums_full[q]))
+                         : "memory");
             if (tid < kR) {
                 fetch_words(ch + kStages - 1);
                 __pipeline_wait_prior(kStages - 2);        // chunk ch+1 landed
@@ -283,27 +314,14 @@ __global__ void __launch_bounds__(kThreads, 1)
                 break;
             }
         }
-        if (aborted) {
-            if (tid == 0) atomicExch(&g_cols_error, 1);
-        } else {
-            if (nchunks > 0) consume(nchunks - 1);
-            if (short_owner || long_owner) {
-                const int c = short_owner ? tid : tid - 128;
-                const int col = band0 * kBand + c;
-                if (col < p.ncols) {
-                    const int to = dest_of<SUBSET ? T_SUBSET : T_FC>(p.g, col);
-                    if (short_owner) p.short_cond[to] += short_sum;
-                    else p.long_cond[to] += long_sum;
-                }
-            }
-        }
+        if (aborted && tid == 0) atomicExch(&g_cols_error, 1);
     }
     __syncthreads();
 }
 
 size_t cols_smem_bytes(int na) {
     return 128 + (size_t)kStages * na * kMaxBands * kBlockFloats * 4 +
-           (size_t)4 * kR * kSumPitch * 4 + 2 * kStages * sizeof(uint64_t);
+           (size_t)kSumBufs * 2 * kR * kSumPitch * 4 + (2 * kStages + 2 * kSumBufs) * sizeof(uint64_t);
 }
 
 }  // namespace
