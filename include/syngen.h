@@ -235,8 +235,8 @@ void sg_batch_destroy(SG_BATCH batch);
  *
  * `layers` layers of rows x cols neurons; layer 0 is driven by the input
  * sequence x, layer l >= 1 by a convergent connection from layer l-1
- * (field x field, stride 1, offset -field/2, no wrap: out-of-range sources are
- * skipped); every layer integrates v += (dt / tau_l) (-v + I), rate
+ * (field x field with field odd and at most 9, stride 1, offset -field/2, no
+ * wrap: out-of-range sources are skipped); outputs at most 16; every layer integrates v += (dt / tau_l) (-v + I), rate
  * sigmoid(v), v = 0 at the start; every layer reads the previous step's rates.
  * A readout R (outputs x N) of the last layer's rates gives y[t]; the loss is
  * the mean over (t, b, o) of (y[t][b][o] - target[b][o])^2.

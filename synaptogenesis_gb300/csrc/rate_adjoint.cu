@@ -32,7 +32,14 @@
 // The forward pass stores v every `checkpoint` steps; the backward pass
 // recomputes each segment's states from its checkpoint (bit-identical: the
 // same kernel on the same inputs), then runs the adjoint back through it.
-// Every sum has a fixed order, so results are deterministic.
+// Every sum has a fixed order, and every gradient accumulator takes one
+// timestep's sum at a time, so results are deterministic and do not depend on
+// the checkpoint stride.
+//
+// Layout on the device: the convergent weights are transposed once per call
+// into the workspace as [layer][k][neuron], so that consecutive threads
+// (consecutive neurons) read consecutive weights; the readout is reduced per
+// 256-neuron block inside the step kernel and finished at the end.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -49,56 +56,86 @@ namespace {
 using namespace sg;
 
 constexpr int kMaxOutputs = 16;
+constexpr int kMaxField = 9;
 constexpr int kTauBlocks = 64;
+constexpr int kBlock = 256;
 
 struct Dims {
-    int L, rows, cols, N, field, h, K, O, B, T, k, nseg;
+    int L, rows, cols, N, field, h, K, O, B, T, k, nseg, nchunk;
     float dt;
     long long S;   // L * B * N
 };
 
 __device__ __forceinline__ float sigmoid(float v) { return 1.0f / (1.0f + expf(-v)); }
 
-// One forward timestep of every layer and batch element.
-__global__ void __launch_bounds__(256) k_rate_step(Dims D, const float* __restrict__ x_t,
-                                                   const float* __restrict__ w,
-                                                   const float* __restrict__ tau,
-                                                   const float* __restrict__ v_prev,
-                                                   const float* __restrict__ r_prev,
-                                                   float* __restrict__ v_new,
-                                                   float* __restrict__ r_new,
-                                                   float* __restrict__ d_out) {
+// wt[l][k][i] = w[l][i][k]
+__global__ void k_rate_transpose(Dims D, const float* __restrict__ w, float* __restrict__ wt) {
     long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= D.S) return;
-    const int l = (int)(idx / ((long long)D.B * D.N));
-    const int rem = (int)(idx - (long long)l * D.B * D.N);
-    const int b = rem / D.N, i = rem - b * D.N;
-    const float a = D.dt / __ldg(tau + l);
-    float I;
-    if (l == 0) {
-        I = __ldg(x_t + (long long)b * D.N + i);
-    } else {
-        const float* wr = w + ((long long)(l - 1) * D.N + i) * D.K;
-        const float* src = r_prev + ((long long)(l - 1) * D.B + b) * D.N;
-        const int ir = i / D.cols, ic = i - ir * D.cols;
-        I = 0.0f;
-        int k = 0;
-        for (int kr = 0; kr < D.field; ++kr) {
-            const int sr = ir - D.h + kr;
-            if (sr < 0 || sr >= D.rows) { k += D.field; continue; }
-            for (int kc = 0; kc < D.field; ++kc, ++k) {
-                const int sc = ic - D.h + kc;
-                if (sc < 0 || sc >= D.cols) continue;
-                I += __ldg(wr + k) * src[sr * D.cols + sc];
+    if (idx >= (long long)(D.L - 1) * D.N * D.K) return;
+    const long long per = (long long)D.N * D.K;
+    const int l = (int)(idx / per);
+    const int rem = (int)(idx - l * per);
+    const int k = rem / D.N, i = rem - k * D.N;
+    wt[idx] = w[l * per + (long long)i * D.K + k];
+}
+
+// One forward timestep: grid (N / 256, L * B).  Blocks of the last layer also
+// reduce their neurons' readout contributions (fixed tree) into
+// ypart[b][block][o] when ypart is given.
+__global__ void __launch_bounds__(kBlock) k_rate_step(
+    Dims D, const float* __restrict__ x_t, const float* __restrict__ wt,
+    const float* __restrict__ wo, const float* __restrict__ tau, const float* __restrict__ v_prev,
+    const float* __restrict__ r_prev, float* __restrict__ v_new, float* __restrict__ r_new,
+    float* __restrict__ d_out, float* __restrict__ ypart) {
+    __shared__ float red[kBlock / 32][kMaxOutputs];
+    const int l = blockIdx.y / D.B, b = blockIdx.y - l * D.B;
+    const int i = blockIdx.x * kBlock + threadIdx.x;
+    const bool ok = i < D.N;
+    const long long idx = ((long long)l * D.B + b) * D.N + i;
+    float rn = 0.0f;
+    if (ok) {
+        const float a = D.dt / __ldg(tau + l);
+        float I;
+        if (l == 0) {
+            I = __ldg(x_t + (long long)b * D.N + i);
+        } else {
+            const float* wl = wt + (long long)(l - 1) * D.K * D.N + i;
+            const float* src = r_prev + ((long long)(l - 1) * D.B + b) * D.N;
+            const int ir = i / D.cols, ic = i - ir * D.cols;
+            I = 0.0f;
+            int k = 0;
+            for (int kr = 0; kr < D.field; ++kr) {
+                const int sr = ir - D.h + kr;
+                if (sr < 0 || sr >= D.rows) { k += D.field; continue; }
+                for (int kc = 0; kc < D.field; ++kc, ++k) {
+                    const int sc = ic - D.h + kc;
+                    if (sc < 0 || sc >= D.cols) continue;
+                    I += __ldg(wl + (long long)k * D.N) * src[sr * D.cols + sc];
+                }
             }
         }
+        const float vp = v_prev[idx];
+        const float d = -vp + I;
+        const float vn = vp + a * d;
+        v_new[idx] = vn;
+        rn = sigmoid(vn);
+        r_new[idx] = rn;
+        if (d_out) d_out[idx] = d;
     }
-    const float vp = v_prev[idx];
-    const float d = -vp + I;
-    const float vn = vp + a * d;
-    v_new[idx] = vn;
-    r_new[idx] = sigmoid(vn);
-    if (d_out) d_out[idx] = d;
+    if (ypart && l == D.L - 1) {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        for (int o = 0; o < D.O; ++o) {
+            float c = ok ? __ldg(wo + (long long)o * D.N + i) * rn : 0.0f;
+            for (int off = 16; off > 0; off >>= 1) c += __shfl_down_sync(0xFFFFFFFFu, c, off);
+            if (lane == 0) red[warp][o] = c;
+        }
+        __syncthreads();
+        if (threadIdx.x < D.O) {
+            float y = 0.0f;
+            for (int w = 0; w < kBlock / 32; ++w) y += red[w][threadIdx.x];
+            ypart[((long long)b * D.nchunk + blockIdx.x) * D.O + threadIdx.x] = y;
+        }
+    }
 }
 
 // r = sigmoid(v) for a whole state (checkpoint reload / initial state).
@@ -107,44 +144,24 @@ __global__ void k_rate_rates(long long S, const float* __restrict__ v, float* __
     if (idx < S) r[idx] = sigmoid(v[idx]);
 }
 
-// Readout of one timestep: one CTA per batch element; y[b][o] and the
-// element's squared error, each reduced in a fixed tree.
-__global__ void __launch_bounds__(256) k_rate_readout(Dims D, const float* __restrict__ r_last,
-                                                      const float* __restrict__ wo,
-                                                      const float* __restrict__ target,
-                                                      float* __restrict__ y_t,
-                                                      float* __restrict__ loss_t) {
-    __shared__ float part[kMaxOutputs][256];
-    const int b = blockIdx.x, tid = threadIdx.x;
-    const float* r = r_last + (long long)b * D.N;
-    float acc[kMaxOutputs];
-#pragma unroll
-    for (int o = 0; o < kMaxOutputs; ++o) acc[o] = 0.0f;
-    for (int i = tid; i < D.N; i += 256) {
-        const float ri = r[i];
-#pragma unroll
-        for (int o = 0; o < kMaxOutputs; ++o)
-            if (o < D.O) acc[o] += __ldg(wo + (long long)o * D.N + i) * ri;
+// y[t][b][o] = sum of the blocks' partial readouts (block order) and the
+// squared error of each (t, b).
+__global__ void k_rate_finish(Dims D, const float* __restrict__ ypart,
+                              const float* __restrict__ target, float* __restrict__ y,
+                              float* __restrict__ loss_tb) {
+    long long tb = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tb >= (long long)D.T * D.B) return;
+    const int b = (int)(tb % D.B);
+    const float* yp = ypart + tb * D.nchunk * D.O;
+    float e = 0.0f;
+    for (int o = 0; o < D.O; ++o) {
+        float s = 0.0f;
+        for (int c = 0; c < D.nchunk; ++c) s += yp[(long long)c * D.O + o];
+        y[tb * D.O + o] = s;
+        const float diff = s - target[(long long)b * D.O + o];
+        e += diff * diff;
     }
-#pragma unroll
-    for (int o = 0; o < kMaxOutputs; ++o)
-        if (o < D.O) part[o][tid] = acc[o];
-    __syncthreads();
-    for (int s = 128; s > 0; s >>= 1) {
-        if (tid < s)
-            for (int o = 0; o < D.O; ++o) part[o][tid] += part[o][tid + s];
-        __syncthreads();
-    }
-    if (tid == 0) {
-        float e = 0.0f;
-        for (int o = 0; o < D.O; ++o) {
-            const float yo = part[o][0];
-            y_t[(long long)b * D.O + o] = yo;
-            const float diff = yo - target[(long long)b * D.O + o];
-            e += diff * diff;
-        }
-        loss_t[b] = e;
-    }
+    loss_tb[tb] = e;
 }
 
 // loss = sum over (t, b) of the squared errors / (T B O): 256 strided
@@ -164,29 +181,34 @@ __global__ void __launch_bounds__(256) k_rate_loss(Dims D, const float* __restri
     if (tid == 0) *loss = sm[0] / (float)((long long)D.T * D.B * D.O);
 }
 
-// Adjoint of one timestep for every layer and batch element: lambda[t] from
-// lambda[t+1] (the next layer's inputs at t+1 read the rates of t).
-__global__ void __launch_bounds__(256) k_rate_lambda(
-    Dims D, const float* __restrict__ w, const float* __restrict__ wo,
-    const float* __restrict__ tau, const float* __restrict__ y_t,
-    const float* __restrict__ target, float gscale, const float* __restrict__ r_t,
+// gy[t][b][o] = gscale * (y - target), for every step.
+__global__ void k_rate_gy(Dims D, float gscale, const float* __restrict__ y,
+                          const float* __restrict__ target, float* __restrict__ gy) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)D.T * D.B * D.O) return;
+    const long long bo = e % ((long long)D.B * D.O);
+    gy[e] = gscale * (y[e] - target[bo]);
+}
+
+// Adjoint of one timestep for every layer and batch element (grid like the
+// step kernel): lambda[t] from lambda[t+1] (the next layer's inputs at t+1
+// read the rates of t).
+__global__ void __launch_bounds__(kBlock) k_rate_lambda(
+    Dims D, const float* __restrict__ wt, const float* __restrict__ wo,
+    const float* __restrict__ tau, const float* __restrict__ gy_t, const float* __restrict__ r_t,
     const float* __restrict__ lam_next, float* __restrict__ lam, float* __restrict__ dx_t) {
-    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= D.S) return;
-    const int l = (int)(idx / ((long long)D.B * D.N));
-    const int rem = (int)(idx - (long long)l * D.B * D.N);
-    const int b = rem / D.N, i = rem - b * D.N;
+    const int l = blockIdx.y / D.B, b = blockIdx.y - l * D.B;
+    const int i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= D.N) return;
+    const long long idx = ((long long)l * D.B + b) * D.N + i;
     float g = 0.0f;
     if (l == D.L - 1) {
-        for (int o = 0; o < D.O; ++o) {
-            const float gy = gscale * (__ldg(y_t + (long long)b * D.O + o) -
-                                       __ldg(target + (long long)b * D.O + o));
-            g += __ldg(wo + (long long)o * D.N + i) * gy;
-        }
+        for (int o = 0; o < D.O; ++o)
+            g += __ldg(wo + (long long)o * D.N + i) * __ldg(gy_t + (long long)b * D.O + o);
     } else {
         // destinations j of layer l+1 whose window holds i: j = i + h - (kr, kc)
         const float a1 = D.dt / __ldg(tau + l + 1);
-        const float* wl = w + (long long)l * D.N * D.K;        // weights into layer l+1
+        const float* wl = wt + (long long)l * D.K * D.N;          // weights into layer l+1
         const float* ln = lam_next + ((long long)(l + 1) * D.B + b) * D.N;
         const int ir = i / D.cols, ic = i - ir * D.cols;
         for (int kr = 0; kr < D.field; ++kr) {
@@ -196,7 +218,7 @@ __global__ void __launch_bounds__(256) k_rate_lambda(
                 const int jc = ic + D.h - kc;
                 if (jc < 0 || jc >= D.cols) continue;
                 const int j = jr * D.cols + jc;
-                g += __ldg(wl + (long long)j * D.K + kr * D.field + kc) * (a1 * ln[j]);
+                g += __ldg(wl + (long long)(kr * D.field + kc) * D.N + j) * (a1 * ln[j]);
             }
         }
     }
@@ -207,57 +229,83 @@ __global__ void __launch_bounds__(256) k_rate_lambda(
     if (l == 0 && dx_t) dx_t[(long long)b * D.N + i] = a * lv;
 }
 
-// dW over one segment: one thread per (layer >= 1, destination j, k).  The
-// accumulator takes one timestep's batch sum at a time, latest step first, so
-// the result does not depend on where the segments start.
-__global__ void __launch_bounds__(256) k_rate_dw(Dims D, int nt, const float* __restrict__ tau,
-                                                 const float* __restrict__ seg_lam,
-                                                 const float* __restrict__ seg_r,
-                                                 float* __restrict__ dw) {
+// dW over one segment: one thread per (layer >= 1, kernel row kr,
+// destination j) holding the row's field accumulators.  Each accumulator
+// takes one timestep's batch sum at a time, latest step first, so the result
+// does not depend on where the segments start.
+__global__ void __launch_bounds__(kBlock) k_rate_dw(Dims D, int nt, const float* __restrict__ tau,
+                                                   const float* __restrict__ seg_lam,
+                                                   const float* __restrict__ seg_r,
+                                                   float* __restrict__ dw) {
     long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long per = (long long)D.N * D.K;
-    if (idx >= (long long)(D.L - 1) * per) return;
-    const int l = 1 + (int)(idx / per);
-    const int rem = (int)(idx - (long long)(l - 1) * per);
-    const int j = rem / D.K, k = rem - j * D.K;
+    if (idx >= (long long)(D.L - 1) * D.field * D.N) return;
+    const int j = (int)(idx % D.N);
+    const int lk = (int)(idx / D.N);
+    const int kr = lk % D.field, l = 1 + lk / D.field;
     const int jr = j / D.cols, jc = j - jr * D.cols;
-    const int sr = jr - D.h + k / D.field, sc = jc - D.h + k % D.field;
-    if (sr < 0 || sr >= D.rows || sc < 0 || sc >= D.cols) return;
-    const int s = sr * D.cols + sc;
+    const int sr = jr - D.h + kr;
+    if (sr < 0 || sr >= D.rows) return;
     const float a = D.dt / __ldg(tau + l);
-    float acc = dw[idx];
+    float* out = dw + ((long long)(l - 1) * D.N + j) * D.K + kr * D.field;
+    float acc[kMaxField], st[kMaxField];
+    int sc0 = jc - D.h;
+#pragma unroll
+    for (int kc = 0; kc < kMaxField; ++kc)
+        if (kc < D.field) acc[kc] = out[kc];
     for (int tt = nt - 1; tt >= 0; --tt) {
         // lambda of step t = c + tt + 1 and the source rates of step t - 1
-        const float* lam = seg_lam + (long long)tt * D.S + (long long)l * D.B * D.N;
-        const float* r = seg_r + (long long)tt * D.S + (long long)(l - 1) * D.B * D.N;
-        float st = 0.0f;
-        for (int b = 0; b < D.B; ++b) st += lam[(long long)b * D.N + j] * r[(long long)b * D.N + s];
-        acc += a * st;
+        const float* lam = seg_lam + (long long)tt * D.S + (long long)l * D.B * D.N + j;
+        const float* rr = seg_r + (long long)tt * D.S + (long long)(l - 1) * D.B * D.N +
+                          sr * D.cols + sc0;
+#pragma unroll
+        for (int kc = 0; kc < kMaxField; ++kc) st[kc] = 0.0f;
+        for (int b = 0; b < D.B; ++b) {
+            const float lv = lam[(long long)b * D.N];
+            const float* rb = rr + (long long)b * D.N;
+#pragma unroll
+            for (int kc = 0; kc < kMaxField; ++kc)
+                if (kc < D.field && sc0 + kc >= 0 && sc0 + kc < D.cols) st[kc] += lv * rb[kc];
+        }
+#pragma unroll
+        for (int kc = 0; kc < kMaxField; ++kc)
+            if (kc < D.field) acc[kc] += a * st[kc];
     }
-    dw[idx] = acc;
+#pragma unroll
+    for (int kc = 0; kc < kMaxField; ++kc)
+        if (kc < D.field && sc0 + kc >= 0 && sc0 + kc < D.cols) out[kc] = acc[kc];
 }
 
-// dR over one segment: one thread per (output o, neuron i).
-__global__ void __launch_bounds__(256) k_rate_dwo(Dims D, int t0, int nt, const float* __restrict__ y,
-                                                  const float* __restrict__ target, float gscale,
-                                                  const float* __restrict__ seg_r,
-                                                  float* __restrict__ dwo) {
-    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long long)D.O * D.N) return;
-    const int o = (int)(idx / D.N), i = (int)(idx - (long long)o * D.N);
-    float acc = dwo[idx];
+// dR over one segment: one thread per neuron i holding every output's
+// accumulator; per timestep the batch sum, then the accumulator.
+__global__ void __launch_bounds__(kBlock) k_rate_dwo(Dims D, int t0, int nt,
+                                                    const float* __restrict__ gy,
+                                                    const float* __restrict__ seg_r,
+                                                    float* __restrict__ dwo) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= D.N) return;
+    float acc[kMaxOutputs], st[kMaxOutputs];
+#pragma unroll
+    for (int o = 0; o < kMaxOutputs; ++o)
+        if (o < D.O) acc[o] = dwo[(long long)o * D.N + i];
     for (int tt = nt - 1; tt >= 0; --tt) {
         const int t = t0 + tt + 1;                      // 1-based step
-        const float* yt = y + (long long)(t - 1) * D.B * D.O;
-        const float* r = seg_r + (long long)(tt + 1) * D.S + (long long)(D.L - 1) * D.B * D.N;
-        float st = 0.0f;
+        const float* g = gy + (long long)(t - 1) * D.B * D.O;
+        const float* r = seg_r + (long long)(tt + 1) * D.S + (long long)(D.L - 1) * D.B * D.N + i;
+#pragma unroll
+        for (int o = 0; o < kMaxOutputs; ++o) st[o] = 0.0f;
         for (int b = 0; b < D.B; ++b) {
-            const float gy = gscale * (yt[(long long)b * D.O + o] - target[(long long)b * D.O + o]);
-            st += gy * r[(long long)b * D.N + i];
+            const float rv = r[(long long)b * D.N];
+#pragma unroll
+            for (int o = 0; o < kMaxOutputs; ++o)
+                if (o < D.O) st[o] += __ldg(g + (long long)b * D.O + o) * rv;
         }
-        acc += st;
+#pragma unroll
+        for (int o = 0; o < kMaxOutputs; ++o)
+            if (o < D.O) acc[o] += st[o];
     }
-    dwo[idx] = acc;
+#pragma unroll
+    for (int o = 0; o < kMaxOutputs; ++o)
+        if (o < D.O) dwo[(long long)o * D.N + i] = acc[o];
 }
 
 // Partial sums of lambda * d per (timestep, layer): grid (kTauBlocks, L, nt),
@@ -283,17 +331,22 @@ __global__ void __launch_bounds__(256) k_rate_dtau_partial(Dims D, int t0,
     if (tid == 0) part[((long long)(t0 + tt) * D.L + l) * kTauBlocks + blockIdx.x] = sm[0];
 }
 
-// dtau_l = -(dt / tau_l^2) * sum over timesteps (latest first) of the step sums.
-__global__ void k_rate_dtau_final(Dims D, const float* __restrict__ tau,
-                                  const float* __restrict__ part, float* __restrict__ dtau) {
-    const int l = threadIdx.x;
-    if (blockIdx.x != 0 || l >= D.L) return;
-    float s = 0.0f;
-    for (int t = D.T - 1; t >= 0; --t) {
+// dtau_l = -(dt / tau_l^2) * sum over timesteps (latest first) of the step
+// sums; each step sum adds its blocks' partials in block order.
+__global__ void __launch_bounds__(256) k_rate_dtau_final(Dims D, const float* __restrict__ tau,
+                                                         const float* __restrict__ part,
+                                                         float* __restrict__ step_sums,
+                                                         float* __restrict__ dtau) {
+    for (int e = threadIdx.x; e < D.T * D.L; e += blockDim.x) {
         float st = 0.0f;
-        for (int q = 0; q < kTauBlocks; ++q) st += part[((long long)t * D.L + l) * kTauBlocks + q];
-        s += st;
+        for (int q = 0; q < kTauBlocks; ++q) st += part[(long long)e * kTauBlocks + q];
+        step_sums[e] = st;
     }
+    __syncthreads();
+    const int l = threadIdx.x;
+    if (l >= D.L) return;
+    float s = 0.0f;
+    for (int t = D.T - 1; t >= 0; --t) s += step_sums[(long long)t * D.L + l];
     const float tv = __ldg(tau + l);
     dtau[l] = s * (-D.dt / (tv * tv));
 }
@@ -304,8 +357,10 @@ Dims make_dims(const SgRateShape& s) {
         throw SgError("rate network: sizes must be positive");
     if (s.outputs < 1 || s.outputs > kMaxOutputs)
         throw SgError("rate network: outputs must lie in 1..16");
-    if (s.field < 1 || s.field % 2 == 0) throw SgError("rate network: field must be odd");
+    if (s.field < 1 || s.field % 2 == 0 || s.field > kMaxField)
+        throw SgError("rate network: field must be odd and at most 9");
     if (!(s.dt > 0.0f)) throw SgError("rate network: dt must be positive");
+    if ((long long)s.layers * s.batch > 65535) throw SgError("rate network: layers x batch too large");
     Dims D;
     D.L = s.layers;
     D.rows = s.rows;
@@ -319,6 +374,7 @@ Dims make_dims(const SgRateShape& s) {
     D.T = s.steps;
     D.k = s.checkpoint;
     D.nseg = (s.steps + s.checkpoint - 1) / s.checkpoint;
+    D.nchunk = (D.N + kBlock - 1) / kBlock;
     D.dt = s.dt;
     D.S = (long long)D.L * D.B * D.N;
     return D;
@@ -326,9 +382,11 @@ Dims make_dims(const SgRateShape& s) {
 
 // Workspace layout (floats): checkpoints [nseg][S], segment states v, r
 // [k+1][S], drives d and adjoints lambda [k][S], the lambda carried across
-// segments [S], outputs y [T][B][O], squared errors [T][B], tau partials.
+// segments [S], outputs y [T][B][O] and their partial sums, squared errors
+// [T][B], dloss/dy [T][B][O], tau partials, transposed weights.
 struct Work {
-    float *ckpt, *seg_v, *seg_r, *seg_d, *seg_lam, *carry, *y, *loss_tb, *tau_part;
+    float *ckpt, *seg_v, *seg_r, *seg_d, *seg_lam, *carry, *y, *ypart, *loss_tb, *gy, *tau_part,
+        *tau_steps, *wt;
     long long floats;
 };
 
@@ -349,16 +407,36 @@ Work carve(const Dims& D, void* base) {
     w.seg_lam = take((long long)D.k * D.S);
     w.carry = take(D.S);
     w.y = take((long long)D.T * D.B * D.O);
+    w.ypart = take((long long)D.T * D.B * D.nchunk * D.O);
     w.loss_tb = take((long long)D.T * D.B);
+    w.gy = take((long long)D.T * D.B * D.O);
     w.tau_part = take((long long)D.T * D.L * kTauBlocks);
+    w.tau_steps = take((long long)D.T * D.L);
+    w.wt = take((long long)std::max(D.L - 1, 0) * D.K * D.N);
     return w;
 }
 
 unsigned grid_of(long long n) { return (unsigned)((n + 255) / 256); }
 
+void transpose_weights(const Dims& D, const float* w, const Work& W, cudaStream_t st) {
+    if (D.L < 2) return;
+    k_rate_transpose<<<grid_of((long long)(D.L - 1) * D.N * D.K), 256, 0, st>>>(D, w, W.wt);
+    SG_LAUNCH_CHECK();
+}
+
+void step(const Dims& D, const float* x_t, const float* wo, const float* tau, const Work& W,
+          const float* v_prev, const float* r_prev, float* v_new, float* r_new, float* d_out,
+          float* ypart, cudaStream_t st) {
+    dim3 grid(D.nchunk, D.L * D.B);
+    k_rate_step<<<grid, kBlock, 0, st>>>(D, x_t, W.wt, wo, tau, v_prev, r_prev, v_new, r_new, d_out,
+                                         ypart);
+    SG_LAUNCH_CHECK();
+}
+
 void forward(const Dims& D, const float* x, const float* w, const float* wo, const float* tau,
              const float* target, float* y_out, float* loss, void* ws, cudaStream_t st) {
     Work W = carve(D, ws);
+    transpose_weights(D, w, W, st);
     float* v[2] = {W.seg_v, W.seg_v + D.S};
     float* r[2] = {W.seg_r, W.seg_r + D.S};
     SG_CUDA(cudaMemsetAsync(v[0], 0, D.S * sizeof(float), st));
@@ -367,17 +445,15 @@ void forward(const Dims& D, const float* x, const float* w, const float* wo, con
     SG_CUDA(cudaMemsetAsync(W.ckpt, 0, D.S * sizeof(float), st));
     for (int t = 1; t <= D.T; ++t) {
         const int p = (t - 1) & 1, q = t & 1;
-        k_rate_step<<<grid_of(D.S), 256, 0, st>>>(D, x + (long long)(t - 1) * D.B * D.N, w, tau,
-                                                  v[p], r[p], v[q], r[q], nullptr);
-        SG_LAUNCH_CHECK();
-        k_rate_readout<<<D.B, 256, 0, st>>>(D, r[q] + (long long)(D.L - 1) * D.B * D.N, wo,
-                                            target, W.y + (long long)(t - 1) * D.B * D.O,
-                                            W.loss_tb + (long long)(t - 1) * D.B);
-        SG_LAUNCH_CHECK();
+        step(D, x + (long long)(t - 1) * D.B * D.N, wo, tau, W, v[p], r[p], v[q], r[q], nullptr,
+             W.ypart + (long long)(t - 1) * D.B * D.nchunk * D.O, st);
         if (t % D.k == 0 && t < D.T)
             SG_CUDA(cudaMemcpyAsync(W.ckpt + (long long)(t / D.k) * D.S, v[q],
                                     D.S * sizeof(float), cudaMemcpyDeviceToDevice, st));
     }
+    k_rate_finish<<<grid_of((long long)D.T * D.B), 256, 0, st>>>(D, W.ypart, target, W.y,
+                                                                 W.loss_tb);
+    SG_LAUNCH_CHECK();
     k_rate_loss<<<1, 256, 0, st>>>(D, W.loss_tb, loss);
     SG_LAUNCH_CHECK();
     if (y_out)
@@ -389,29 +465,30 @@ void backward(const Dims& D, const float* x, const float* w, const float* wo, co
               const float* target, float grad_loss, void* ws, float* dw, float* dwo,
               float* dtau, float* dx, cudaStream_t st) {
     Work W = carve(D, ws);
+    transpose_weights(D, w, W, st);
     const float gscale = grad_loss * 2.0f / (float)((long long)D.T * D.B * D.O);
+    k_rate_gy<<<grid_of((long long)D.T * D.B * D.O), 256, 0, st>>>(D, gscale, W.y, target, W.gy);
+    SG_LAUNCH_CHECK();
     if (D.L > 1)
         SG_CUDA(cudaMemsetAsync(dw, 0, (size_t)(D.L - 1) * D.N * D.K * sizeof(float), st));
     SG_CUDA(cudaMemsetAsync(dwo, 0, (size_t)D.O * D.N * sizeof(float), st));
     SG_CUDA(cudaMemsetAsync(W.carry, 0, D.S * sizeof(float), st));
+    const dim3 grid(D.nchunk, D.L * D.B);
     for (int seg = D.nseg - 1; seg >= 0; --seg) {
         const int c = seg * D.k, nt = std::min(D.k, D.T - c);
         SG_CUDA(cudaMemcpyAsync(W.seg_v, W.ckpt + (long long)seg * D.S, D.S * sizeof(float),
                                 cudaMemcpyDeviceToDevice, st));
         k_rate_rates<<<grid_of(D.S), 256, 0, st>>>(D.S, W.seg_v, W.seg_r);
         SG_LAUNCH_CHECK();
-        for (int tt = 1; tt <= nt; ++tt) {
-            k_rate_step<<<grid_of(D.S), 256, 0, st>>>(
-                D, x + (long long)(c + tt - 1) * D.B * D.N, w, tau, W.seg_v + (tt - 1) * D.S,
-                W.seg_r + (tt - 1) * D.S, W.seg_v + tt * D.S, W.seg_r + tt * D.S,
-                W.seg_d + (tt - 1) * D.S);
-            SG_LAUNCH_CHECK();
-        }
+        for (int tt = 1; tt <= nt; ++tt)
+            step(D, x + (long long)(c + tt - 1) * D.B * D.N, wo, tau, W, W.seg_v + (tt - 1) * D.S,
+                 W.seg_r + (tt - 1) * D.S, W.seg_v + tt * D.S, W.seg_r + tt * D.S,
+                 W.seg_d + (tt - 1) * D.S, nullptr, st);
         for (int tt = nt; tt >= 1; --tt) {
             const int t = c + tt;
             const float* lam_next = tt == nt ? W.carry : W.seg_lam + (long long)tt * D.S;
-            k_rate_lambda<<<grid_of(D.S), 256, 0, st>>>(
-                D, w, wo, tau, W.y + (long long)(t - 1) * D.B * D.O, target, gscale,
+            k_rate_lambda<<<grid, kBlock, 0, st>>>(
+                D, W.wt, wo, tau, W.gy + (long long)(t - 1) * D.B * D.O,
                 W.seg_r + (long long)tt * D.S, lam_next, W.seg_lam + (long long)(tt - 1) * D.S,
                 dx ? dx + (long long)(t - 1) * D.B * D.N : nullptr);
             SG_LAUNCH_CHECK();
@@ -419,18 +496,17 @@ void backward(const Dims& D, const float* x, const float* w, const float* wo, co
         SG_CUDA(cudaMemcpyAsync(W.carry, W.seg_lam, D.S * sizeof(float),
                                 cudaMemcpyDeviceToDevice, st));
         if (D.L > 1) {
-            k_rate_dw<<<grid_of((long long)(D.L - 1) * D.N * D.K), 256, 0, st>>>(
+            k_rate_dw<<<grid_of((long long)(D.L - 1) * D.field * D.N), kBlock, 0, st>>>(
                 D, nt, tau, W.seg_lam, W.seg_r, dw);
             SG_LAUNCH_CHECK();
         }
-        k_rate_dwo<<<grid_of((long long)D.O * D.N), 256, 0, st>>>(D, c, nt, W.y, target, gscale,
-                                                                  W.seg_r, dwo);
+        k_rate_dwo<<<grid_of(D.N), kBlock, 0, st>>>(D, c, nt, W.gy, W.seg_r, dwo);
         SG_LAUNCH_CHECK();
         k_rate_dtau_partial<<<dim3(kTauBlocks, D.L, nt), 256, 0, st>>>(D, c, W.seg_lam, W.seg_d,
                                                                        W.tau_part);
         SG_LAUNCH_CHECK();
     }
-    k_rate_dtau_final<<<1, 32, 0, st>>>(D, tau, W.tau_part, dtau);
+    k_rate_dtau_final<<<1, 256, 0, st>>>(D, tau, W.tau_part, W.tau_steps, dtau);
     SG_LAUNCH_CHECK();
 }
 

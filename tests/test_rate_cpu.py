@@ -54,10 +54,11 @@ def test_rate_shape_validation_and_workspace():
     net = syngen.RateNetwork(layers=3, rows=64, cols=64, field=5, outputs=10, batch=64,
                              steps=100, checkpoint=10)
     S = 3 * 64 * 4096
-    # checkpoints (10) + segment v, r (11 each) + d, lambda (10 each) + carry
+    # checkpoints (10) + segment v, r (11 each) + d, lambda (10 each) + carry,
+    # plus outputs, readout partials, transposed weights (under 2 S together)
     assert net.workspace_bytes >= (10 + 11 + 11 + 10 + 10 + 1) * S * 4
-    assert net.workspace_bytes < (10 + 11 + 11 + 10 + 10 + 2) * S * 4
-    for bad in (dict(outputs=17), dict(field=4), dict(steps=0), dict(checkpoint=0),
-                dict(dt=0.0)):
+    assert net.workspace_bytes < (10 + 11 + 11 + 10 + 10 + 3) * S * 4
+    for bad in (dict(outputs=17), dict(field=4), dict(field=11), dict(steps=0),
+                dict(checkpoint=0), dict(dt=0.0)):
         with pytest.raises(ValueError):
             syngen.RateNetwork(**dict(dict(rows=8, cols=8, batch=2, steps=4), **bad))
