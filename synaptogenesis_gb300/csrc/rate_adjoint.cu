@@ -229,83 +229,130 @@ __global__ void __launch_bounds__(kBlock) k_rate_lambda(
     if (l == 0 && dx_t) dx_t[(long long)b * D.N + i] = a * lv;
 }
 
-// dW over one segment: one thread per (layer >= 1, kernel row kr,
-// destination j) holding the row's field accumulators.  Each accumulator
-// takes one timestep's batch sum at a time, latest step first, so the result
-// does not depend on where the segments start.
+// dW over one segment.  A CTA covers 32 destinations j of one (layer >= 1,
+// kernel row kr) for all of the row's kernel columns; its 8 thread groups
+// take 8 batch elements each.  Per timestep (latest first) a group sums its
+// elements in order, the groups' sums are added in group order, and the
+// accumulator takes the step's total: a fixed order that does not depend on
+// where the segments start.
+constexpr int kGroups = 8;
+
 __global__ void __launch_bounds__(kBlock) k_rate_dw(Dims D, int nt, const float* __restrict__ tau,
                                                    const float* __restrict__ seg_lam,
                                                    const float* __restrict__ seg_r,
                                                    float* __restrict__ dw) {
-    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long long)(D.L - 1) * D.field * D.N) return;
-    const int j = (int)(idx % D.N);
-    const int lk = (int)(idx / D.N);
+    __shared__ float part[kGroups][32][kMaxField + 1];
+    const int jl = threadIdx.x & 31, g = threadIdx.x >> 5;
+    const int tiles = (D.N + 31) / 32;
+    const int tile = blockIdx.x % tiles, lk = blockIdx.x / tiles;
     const int kr = lk % D.field, l = 1 + lk / D.field;
-    const int jr = j / D.cols, jc = j - jr * D.cols;
-    const int sr = jr - D.h + kr;
-    if (sr < 0 || sr >= D.rows) return;
+    const int j = tile * 32 + jl;
+    const bool ok = j < D.N;
+    const int jr = ok ? j / D.cols : 0, jc = ok ? j - jr * D.cols : 0;
+    const int sr = jr - D.h + kr, sc0 = jc - D.h;
+    const bool row_ok = ok && sr >= 0 && sr < D.rows;
     const float a = D.dt / __ldg(tau + l);
+    const int bpg = (D.B + kGroups - 1) / kGroups;
+    const int b0 = g * bpg, b1 = min(D.B, b0 + bpg);
     float* out = dw + ((long long)(l - 1) * D.N + j) * D.K + kr * D.field;
-    float acc[kMaxField], st[kMaxField];
-    int sc0 = jc - D.h;
+    float acc[kMaxField];
 #pragma unroll
-    for (int kc = 0; kc < kMaxField; ++kc)
-        if (kc < D.field) acc[kc] = out[kc];
-    for (int tt = nt - 1; tt >= 0; --tt) {
-        // lambda of step t = c + tt + 1 and the source rates of step t - 1
-        const float* lam = seg_lam + (long long)tt * D.S + (long long)l * D.B * D.N + j;
-        const float* rr = seg_r + (long long)tt * D.S + (long long)(l - 1) * D.B * D.N +
-                          sr * D.cols + sc0;
-#pragma unroll
-        for (int kc = 0; kc < kMaxField; ++kc) st[kc] = 0.0f;
-        for (int b = 0; b < D.B; ++b) {
-            const float lv = lam[(long long)b * D.N];
-            const float* rb = rr + (long long)b * D.N;
-#pragma unroll
-            for (int kc = 0; kc < kMaxField; ++kc)
-                if (kc < D.field && sc0 + kc >= 0 && sc0 + kc < D.cols) st[kc] += lv * rb[kc];
-        }
+    for (int kc = 0; kc < kMaxField; ++kc) acc[kc] = 0.0f;
+    if (g == 0 && row_ok) {
 #pragma unroll
         for (int kc = 0; kc < kMaxField; ++kc)
-            if (kc < D.field) acc[kc] += a * st[kc];
+            if (kc < D.field) acc[kc] = out[kc];
     }
+    for (int tt = nt - 1; tt >= 0; --tt) {
+        // lambda of step t = c + tt + 1 and the source rates of step t - 1
+        float st[kMaxField];
 #pragma unroll
-    for (int kc = 0; kc < kMaxField; ++kc)
-        if (kc < D.field && sc0 + kc >= 0 && sc0 + kc < D.cols) out[kc] = acc[kc];
+        for (int kc = 0; kc < kMaxField; ++kc) st[kc] = 0.0f;
+        if (row_ok) {
+            const float* lam = seg_lam + (long long)tt * D.S + (long long)l * D.B * D.N + j;
+            const float* rr = seg_r + (long long)tt * D.S + (long long)(l - 1) * D.B * D.N +
+                              sr * D.cols + sc0;
+            for (int b = b0; b < b1; ++b) {
+                const float lv = lam[(long long)b * D.N];
+                const float* rb = rr + (long long)b * D.N;
+#pragma unroll
+                for (int kc = 0; kc < kMaxField; ++kc)
+                    if (kc < D.field && sc0 + kc >= 0 && sc0 + kc < D.cols) st[kc] += lv * rb[kc];
+            }
+        }
+#pragma unroll
+        for (int kc = 0; kc < kMaxField; ++kc) part[g][jl][kc] = st[kc];
+        __syncthreads();
+        if (g == 0) {
+#pragma unroll
+            for (int kc = 0; kc < kMaxField; ++kc) {
+                float tot = 0.0f;
+                for (int q = 0; q < kGroups; ++q) tot += part[q][jl][kc];
+                acc[kc] += a * tot;
+            }
+        }
+        __syncthreads();
+    }
+    if (g == 0 && row_ok) {
+#pragma unroll
+        for (int kc = 0; kc < kMaxField; ++kc)
+            if (kc < D.field && sc0 + kc >= 0 && sc0 + kc < D.cols) out[kc] = acc[kc];
+    }
 }
 
-// dR over one segment: one thread per neuron i holding every output's
-// accumulator; per timestep the batch sum, then the accumulator.
+// dR over one segment, the same scheme: a CTA covers 32 neurons i for every
+// output, its 8 groups take 8 batch elements each.
 __global__ void __launch_bounds__(kBlock) k_rate_dwo(Dims D, int t0, int nt,
                                                     const float* __restrict__ gy,
                                                     const float* __restrict__ seg_r,
                                                     float* __restrict__ dwo) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= D.N) return;
-    float acc[kMaxOutputs], st[kMaxOutputs];
+    __shared__ float part[kGroups][32][kMaxOutputs + 1];
+    const int il = threadIdx.x & 31, g = threadIdx.x >> 5;
+    const int i = blockIdx.x * 32 + il;
+    const bool ok = i < D.N;
+    const int bpg = (D.B + kGroups - 1) / kGroups;
+    const int b0 = g * bpg, b1 = min(D.B, b0 + bpg);
+    float acc[kMaxOutputs];
 #pragma unroll
-    for (int o = 0; o < kMaxOutputs; ++o)
-        if (o < D.O) acc[o] = dwo[(long long)o * D.N + i];
-    for (int tt = nt - 1; tt >= 0; --tt) {
-        const int t = t0 + tt + 1;                      // 1-based step
-        const float* g = gy + (long long)(t - 1) * D.B * D.O;
-        const float* r = seg_r + (long long)(tt + 1) * D.S + (long long)(D.L - 1) * D.B * D.N + i;
-#pragma unroll
-        for (int o = 0; o < kMaxOutputs; ++o) st[o] = 0.0f;
-        for (int b = 0; b < D.B; ++b) {
-            const float rv = r[(long long)b * D.N];
-#pragma unroll
-            for (int o = 0; o < kMaxOutputs; ++o)
-                if (o < D.O) st[o] += __ldg(g + (long long)b * D.O + o) * rv;
-        }
+    for (int o = 0; o < kMaxOutputs; ++o) acc[o] = 0.0f;
+    if (g == 0 && ok) {
 #pragma unroll
         for (int o = 0; o < kMaxOutputs; ++o)
-            if (o < D.O) acc[o] += st[o];
+            if (o < D.O) acc[o] = dwo[(long long)o * D.N + i];
     }
+    for (int tt = nt - 1; tt >= 0; --tt) {
+        const int t = t0 + tt + 1;                      // 1-based step
+        const float* gt = gy + (long long)(t - 1) * D.B * D.O;
+        float st[kMaxOutputs];
 #pragma unroll
-    for (int o = 0; o < kMaxOutputs; ++o)
-        if (o < D.O) dwo[(long long)o * D.N + i] = acc[o];
+        for (int o = 0; o < kMaxOutputs; ++o) st[o] = 0.0f;
+        if (ok) {
+            const float* r = seg_r + (long long)(tt + 1) * D.S + (long long)(D.L - 1) * D.B * D.N + i;
+            for (int b = b0; b < b1; ++b) {
+                const float rv = r[(long long)b * D.N];
+#pragma unroll
+                for (int o = 0; o < kMaxOutputs; ++o)
+                    if (o < D.O) st[o] += __ldg(gt + (long long)b * D.O + o) * rv;
+            }
+        }
+#pragma unroll
+        for (int o = 0; o < kMaxOutputs; ++o) part[g][il][o] = st[o];
+        __syncthreads();
+        if (g == 0) {
+#pragma unroll
+            for (int o = 0; o < kMaxOutputs; ++o) {
+                float tot = 0.0f;
+                for (int q = 0; q < kGroups; ++q) tot += part[q][il][o];
+                acc[o] += tot;
+            }
+        }
+        __syncthreads();
+    }
+    if (g == 0 && ok) {
+#pragma unroll
+        for (int o = 0; o < kMaxOutputs; ++o)
+            if (o < D.O) dwo[(long long)o * D.N + i] = acc[o];
+    }
 }
 
 // Partial sums of lambda * d per (timestep, layer): grid (kTauBlocks, L, nt),
@@ -496,11 +543,11 @@ void backward(const Dims& D, const float* x, const float* w, const float* wo, co
         SG_CUDA(cudaMemcpyAsync(W.carry, W.seg_lam, D.S * sizeof(float),
                                 cudaMemcpyDeviceToDevice, st));
         if (D.L > 1) {
-            k_rate_dw<<<grid_of((long long)(D.L - 1) * D.field * D.N), kBlock, 0, st>>>(
+            k_rate_dw<<<(unsigned)((D.L - 1) * D.field * ((D.N + 31) / 32)), kBlock, 0, st>>>(
                 D, nt, tau, W.seg_lam, W.seg_r, dw);
             SG_LAUNCH_CHECK();
         }
-        k_rate_dwo<<<grid_of(D.N), kBlock, 0, st>>>(D, c, nt, W.gy, W.seg_r, dwo);
+        k_rate_dwo<<<(unsigned)((D.N + 31) / 32), kBlock, 0, st>>>(D, c, nt, W.gy, W.seg_r, dwo);
         SG_LAUNCH_CHECK();
         k_rate_dtau_partial<<<dim3(kTauBlocks, D.L, nt), 256, 0, st>>>(D, c, W.seg_lam, W.seg_d,
                                                                        W.tau_part);
