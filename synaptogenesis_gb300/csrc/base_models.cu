@@ -1,5 +1,6 @@
 // Base activator (all connection types, every opcode) and the stateless
 // neural models: relay, rate_encoding, game_of_life.
+#include <algorithm>
 #include <cmath>
 
 #include "cuda_check.h"
@@ -503,6 +504,155 @@ __global__ void __launch_bounds__(256) k_gol_bits_tile(int rows, int cols, int w
     }
 }
 
+// ---------------------------------------------------------------------------
+// game_of_life on bit planes (whole-run path).
+//
+// A cell's state is its 32-bit output-history word (bit 31 newest).  A step
+// reads the newest bit of the neighbours and the cell's own bit 0, and shifts
+// the word right by one with the new state in bit 31.  Stored as bit planes --
+// plane p holds bit p of 32 consecutive cells of a row in one word -- a step
+// only has to produce one new plane: a ring of kPlaneRing planes where, after
+// T steps, bit p of every word is plane (T + p) % kPlaneRing.  The words are
+// turned into planes at the start of a run and back (with the input register
+// of the last step) at its end, so nothing outside the run sees the planes.
+//
+// k_gol_planes_steps advances K <= kPlaneK steps per launch with no trip to
+// global memory in between: a CTA keeps the newest plane of its tile of
+// kPlaneTY rows x kPlaneTX words plus a halo of kPlaneK rows and one word on
+// each side, and the K oldest planes it needs; wrong values enter the halo
+// from its outer edge at one cell per step and never reach the tile within K
+// steps (a halo word is 32 cells wide).
+constexpr int kPlaneRing = 64;
+constexpr int kPlaneK = 16;
+constexpr int kPlaneTY = 64;
+constexpr int kPlaneTX = 8;
+constexpr int kPlaneHY = kPlaneTY + 2 * kPlaneK;
+constexpr int kPlaneHX = kPlaneTX + 2;
+constexpr size_t kPlaneSmem = (size_t)(2 + kPlaneK) * kPlaneHY * kPlaneHX * sizeof(uint32_t);
+
+// Words of one row segment (32 cells) -> the 32 plane words of the segment.
+__global__ void k_gol_words_to_planes(int rows, int W, const uint32_t* __restrict__ words,
+                                      uint32_t* __restrict__ planes) {
+    const long long seg = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (seg >= (long long)rows * W) return;
+    const uint32_t w = words[seg * 32 + lane];
+    const size_t plane_words = (size_t)rows * W;
+    uint32_t mine = 0;
+#pragma unroll
+    for (int p = 0; p < 32; ++p) {
+        const uint32_t b = __ballot_sync(0xFFFFFFFFu, (w >> p) & 1u);
+        if (lane == p) mine = b;
+    }
+    planes[(size_t)lane * plane_words + seg] = mine;      // after 0 steps bit p is plane p
+}
+
+// Planes after T steps -> words; and, if T > 0, the input register of the
+// last step: the weighted count of the neighbours' newest bits one step
+// earlier (plane T + 30).
+__global__ void k_gol_planes_to_words(int rows, int W, long long T,
+                                      const uint32_t* __restrict__ planes,
+                                      uint32_t* __restrict__ words, float* __restrict__ input_out,
+                                      unsigned mask9) {
+    const long long seg = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (seg >= (long long)rows * W) return;
+    const size_t plane_words = (size_t)rows * W;
+    const uint32_t pw = planes[(size_t)((T + lane) % kPlaneRing) * plane_words + seg];
+    uint32_t word = 0;
+#pragma unroll
+    for (int p = 0; p < 32; ++p) word |= ((__shfl_sync(0xFFFFFFFFu, pw, p) >> lane) & 1u) << p;
+    words[seg * 32 + lane] = word;
+    if (T == 0 || !input_out) return;
+    const int r = (int)(seg / W), x = (int)(seg - (long long)r * W);
+    const uint32_t* prev = planes + (size_t)((T + 30) % kPlaneRing) * plane_words;
+    uint32_t c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        int rr = r + k - 1;
+        rr = rr < 0 ? rr + rows : (rr >= rows ? rr - rows : rr);
+        const int xl = x == 0 ? W - 1 : x - 1, xr = x == W - 1 ? 0 : x + 1;
+        const uint32_t n = prev[(size_t)rr * W + x];
+        const uint32_t wv = (n << 1) | (prev[(size_t)rr * W + xl] >> 31);
+        const uint32_t ev = (n >> 1) | (prev[(size_t)rr * W + xr] << 31);
+        if (mask9 & (1u << (k * 3 + 0))) csa_add(c0, c1, c2, c3, wv);
+        if (mask9 & (1u << (k * 3 + 1))) csa_add(c0, c1, c2, c3, n);
+        if (mask9 & (1u << (k * 3 + 2))) csa_add(c0, c1, c2, c3, ev);
+    }
+    const unsigned cnt = ((c0 >> lane) & 1u) | (((c1 >> lane) & 1u) << 1) |
+                         (((c2 >> lane) & 1u) << 2) | (((c3 >> lane) & 1u) << 3);
+    input_out[seg * 32 + lane] = (float)cnt;
+}
+
+// K steps (1 <= K <= kPlaneK) of a toroidal board, starting after T0 steps.
+__global__ void __launch_bounds__(256) k_gol_planes_steps(int rows, int W, long long T0, int K,
+                                                          uint32_t* __restrict__ planes,
+                                                          unsigned mask9, unsigned smask,
+                                                          unsigned bmask) {
+    extern __shared__ uint32_t plane_smem[];
+    // cur[2][HY][HX]: newest plane, double buffered; old[K][HY][HX]: the
+    // planes that are bit 0 at steps T0 .. T0+K-1
+    auto cur = reinterpret_cast<uint32_t(*)[kPlaneHY][kPlaneHX]>(plane_smem);
+    auto old = reinterpret_cast<uint32_t(*)[kPlaneHY][kPlaneHX]>(plane_smem + 2 * kPlaneHY * kPlaneHX);
+    const size_t plane_words = (size_t)rows * W;
+    const int r0 = blockIdx.y * kPlaneTY, w0 = blockIdx.x * kPlaneTX;
+    const int hy0 = kPlaneK - K;             // halo rows K steps do not need
+    const uint32_t* newest = planes + (size_t)((T0 + 31) % kPlaneRing) * plane_words;
+    for (int e = threadIdx.x; e < kPlaneHY * kPlaneHX; e += blockDim.x) {
+        const int hy = e / kPlaneHX, hx = e - hy * kPlaneHX;
+        int gr = (r0 - kPlaneK + hy) % rows, gw = (w0 - 1 + hx) % W;
+        if (gr < 0) gr += rows;
+        if (gw < 0) gw += W;
+        const size_t off = (size_t)gr * W + gw;
+        cur[0][hy][hx] = newest[off];
+        for (int s = 0; s < K; ++s)
+            old[s][hy][hx] = planes[(size_t)((T0 + s) % kPlaneRing) * plane_words + off];
+    }
+    __syncthreads();
+    int c = 0;
+    for (int s = 0; s < K; ++s) {
+        uint32_t* out = planes + (size_t)((T0 + s + 32) % kPlaneRing) * plane_words;
+        for (int e = threadIdx.x; e < kPlaneHY * kPlaneHX; e += blockDim.x) {
+            const int hy = e / kPlaneHX, hx = e - hy * kPlaneHX;
+            if (hy <= hy0 || hy >= kPlaneHY - 1 - hy0) {
+                cur[c ^ 1][hy][hx] = 0u;         // edge of what K steps need
+                continue;
+            }
+            uint32_t c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t* row = cur[c][hy - 1 + k];
+                const uint32_t n = row[hx];
+                const uint32_t lw = hx > 0 ? row[hx - 1] : 0u;
+                const uint32_t rw = hx < kPlaneHX - 1 ? row[hx + 1] : 0u;
+                const uint32_t wv = (n << 1) | (lw >> 31);
+                const uint32_t ev = (n >> 1) | (rw << 31);
+                if (mask9 & (1u << (k * 3 + 0))) csa_add(c0, c1, c2, c3, wv);
+                if (mask9 & (1u << (k * 3 + 1))) csa_add(c0, c1, c2, c3, n);
+                if (mask9 & (1u << (k * 3 + 2))) csa_add(c0, c1, c2, c3, ev);
+            }
+            uint32_t S = 0, B = 0;
+#pragma unroll
+            for (int v = 0; v < 10; ++v) {
+                if (!(((smask | bmask) >> v) & 1u)) continue;
+                const uint32_t eq = ~((c0 ^ ((v & 1) ? ~0u : 0u)) | (c1 ^ ((v & 2) ? ~0u : 0u)) |
+                                      (c2 ^ ((v & 4) ? ~0u : 0u)) | (c3 ^ ((v & 8) ? ~0u : 0u)));
+                if ((smask >> v) & 1u) S |= eq;
+                if ((bmask >> v) & 1u) B |= eq;
+            }
+            const uint32_t O = old[s][hy][hx];
+            const uint32_t L = (O & S) | (~O & B);
+            cur[c ^ 1][hy][hx] = L;
+            const int ty = hy - kPlaneK, tx = hx - 1;
+            if (ty >= 0 && ty < kPlaneTY && tx >= 0 && tx < kPlaneTX && r0 + ty < rows &&
+                w0 + tx < W)
+                out[(size_t)(r0 + ty) * W + w0 + tx] = L;
+        }
+        __syncthreads();
+        c ^= 1;
+    }
+}
+
 // Mask of counts in [lo, hi] (counts of a 3x3 kernel are 0..9).
 static unsigned count_mask(int lo, int hi) {
     unsigned m = 0;
@@ -565,7 +715,58 @@ class GameOfLifeModel : public Model {
             Array* swap = st.add_array("output swap", 'u', l.size);
             swap->scratch = true;
             ls.internal["output swap"] = swap;
+            const Connection& c = *l.inputs[0];
+            if (c.delay == 0 && c.arbor.wrap && l.cols % 32 == 0) {
+                Array* planes = st.add_array("planes", 'u', (size_t)kPlaneRing * (l.size / 32));
+                planes->scratch = true;
+                ls.internal["planes"] = planes;
+            }
         }
+    }
+    // Whole-run path on bit planes: a toroidal board whose only input is its
+    // own 0/1-weight 3x3 connection with delay 0.
+    bool can_advance_alone(State& st, const LayerState& ls) const override {
+        const Layer& l = *ls.layer;
+        if (!fusable_shape(l) || !ls.internal.count("planes")) return false;
+        const ConnState& cs = *st.conn_state(l.inputs[0]);
+        auto bm = cs.params.find("bits mask");
+        return bm != cs.params.end() && bm->second >= 0.0f;
+    }
+    long advance_alone(State& st, LayerState& ls, long n, cudaStream_t s) const override {
+        const Layer& l = *ls.layer;
+        const ConnState& cs = *st.conn_state(l.inputs[0]);
+        const unsigned mask9 = (unsigned)cs.params.at("bits mask");
+        const unsigned smask = count_mask((int)ls.params.at("smin"), (int)ls.params.at("smax"));
+        const unsigned bmask = count_mask((int)ls.params.at("bmin"), (int)ls.params.at("bmax"));
+        const int W = l.cols / 32;
+        uint32_t* planes = ls.internal.at("planes")->du();
+        uint32_t* words = ls.output->du();
+        const long long segs = (long long)l.rows * W;
+        long launches = 0;
+        k_gol_words_to_planes<<<blocks_for(segs * 32, 256), 256, 0, s>>>(l.rows, W, words, planes);
+        SG_LAUNCH_CHECK();
+        ++launches;
+        static bool configured = false;
+        if (!configured) {
+            SG_CUDA(cudaFuncSetAttribute(k_gol_planes_steps,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPlaneSmem));
+            configured = true;
+        }
+        const dim3 grid((unsigned)((W + kPlaneTX - 1) / kPlaneTX),
+                        (unsigned)((l.rows + kPlaneTY - 1) / kPlaneTY));
+        long long T = 0;
+        while (T < n) {
+            const int K = (int)std::min<long long>(kPlaneK, n - T);
+            k_gol_planes_steps<<<grid, 256, kPlaneSmem, s>>>(l.rows, W, T, K, planes, mask9, smask,
+                                                             bmask);
+            SG_LAUNCH_CHECK();
+            ++launches;
+            T += K;
+        }
+        k_gol_planes_to_words<<<blocks_for(segs * 32, 256), 256, 0, s>>>(
+            l.rows, W, T, planes, words, ls.input->df(), mask9);
+        SG_LAUNCH_CHECK();
+        return launches + 1;
     }
     bool fuses_input(State&, const Connection& c, const StepCtx& ctx) const override {
         return fusable_shape(*c.to) && !ctx.is_input(*c.to);

@@ -93,6 +93,11 @@ Engine::Engine(Network* net, Environment* env, State* state, const Props& args)
             if (init && init->get("type", "normal") != "flat") step_counter_ = true;
         }
         state_->to_device(stream_);
+        // No environment and every layer self-contained: whole runs per layer.
+        alone_ = modules_.empty() && !net_->layers.empty() && args.get_bool("whole runs", true);
+        for (auto& lp : net_->layers)
+            alone_ = alone_ &&
+                     find_model(lp->model)->can_advance_alone(*state_, *state_->layer_state(lp.get()));
         for (auto& lp : net_->layers) {
             if (layer_io_[lp->index] & 1) input_layers_.push_back(lp.get());
             if (layer_io_[lp->index] & 2) output_layers_.push_back(lp.get());
@@ -337,6 +342,17 @@ long Engine::step(long n) {
     auto t0 = std::chrono::steady_clock::now();
     SG_CUDA(cudaEventRecord(ev0, stream_));
     long i = 0;
+    if (alone_ && n > 0) {
+        for (auto& lp : net_->layers) {
+            const Model* m = find_model(lp->model);
+            long k = 0;
+            const std::string group = std::string(lp->model) + ".advance";
+            timed(group, 0, [&] { k = m->advance_alone(*state_, *state_->layer_state(lp.get()), n, stream_); });
+            launches_ += k;
+            if (profile_) prof_[group].launches += k;
+        }
+        i = n;
+    }
     while (n == 0 || i < n) {
         if (interrupt_flag) break;
         if (use_graphs_ && n != 0 && n - i > graph_steps_) {

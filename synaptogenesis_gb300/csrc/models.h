@@ -56,6 +56,15 @@ class Model {
     virtual void update(State& st, LayerState& ls, const StepCtx& ctx) const = 0;
     // Whether a plastic connection into this model has an updater.
     virtual bool learns(const Connection& c) const { return false; }
+    // Whole-run path: can this layer advance n steps on its own -- nothing
+    // else reads or writes it between steps (the engine has checked that no
+    // environment module touches it)?  If so, advance_alone runs the n steps
+    // and leaves the state exactly as n calls of the per-step path would;
+    // it returns the number of kernels launched.
+    virtual bool can_advance_alone(State& st, const LayerState& ls) const { return false; }
+    virtual long advance_alone(State& st, LayerState& ls, long n, cudaStream_t s) const {
+        return 0;
+    }
     virtual void learn(State& st, ConnState& cs, const StepCtx& ctx) const {}
 };
 

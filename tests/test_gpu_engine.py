@@ -106,3 +106,38 @@ def test_izhikevich_graph_replay_equals_stepwise(sg):
                         for k in ("voltage", "recovery", "output", "nmda", "time since spike")})
     for k in results[0]:
         assert np.array_equal(results[0][k].view(np.uint32), results[1][k].view(np.uint32)), k
+
+
+@pytest.mark.parametrize("rows,cols,rule", [
+    (96, 160, dict(survival_min=2, survival_max=3, birth_min=3, birth_max=3)),
+    (20, 32, dict(survival_min=2, survival_max=4, birth_min=3, birth_max=3)),
+    (130, 288, dict(diagonal=True, survival_min=3, survival_max=4, birth_min=3, birth_max=5)),
+    (257, 64, dict(survival_min=1, survival_max=5, birth_min=2, birth_max=3))])
+def test_gol_whole_runs_equal_per_step_path(sg, rows, cols, rule):
+    """Without an environment a toroidal game_of_life board advances whole runs
+    on bit planes (many steps per launch); words and the input register equal
+    the per-step path's and the oracle's for step counts around the launch
+    size (16 steps)."""
+    words = np.random.default_rng(rows * cols).integers(0, 2**32, rows * cols,
+                                                       dtype=np.uint64).astype(np.uint32)
+    chunks = [1, 16, 17, 33, 100, 5]
+    net_dict = gol_net(rows, cols, **rule)
+    results = []
+    for whole in (True, False):
+        net = sg.Network(net_dict)
+        net.build_state()
+        net.get_neuron_data("g", "board", "output").to_np_array().view(np.uint32)[:] = words
+        with sg.Engine(net, None, {"whole runs": whole}) as eng:
+            for n in chunks:
+                assert eng.step(n) == n
+                results.append((whole, n,
+                                net.get_neuron_data("g", "board", "output").to_np_array()
+                                .view(np.uint32).copy(),
+                                net.get_neuron_data("g", "board", "input").to_np_array().copy()))
+    half = len(results) // 2
+    for (_, n, wa, ia), (_, _, wb, ib) in zip(results[:half], results[half:]):
+        assert np.array_equal(wa, wb), n
+        assert np.array_equal(ia, ib), n
+    go, gi, oo, oi = run_both(sg, net_dict, words, chunks)
+    assert np.array_equal(go, oo)
+    assert np.array_equal(gi, oi)
