@@ -584,7 +584,51 @@ __global__ void k_gol_planes_to_words(int rows, int W, long long T,
     input_out[seg * 32 + lane] = (float)cnt;
 }
 
+// Neighbour count of 32 cells (bit-sliced, bits c0..c3) from the three rows'
+// west / centre / east words.  MODE 1: the 8 outer neighbours; MODE 2: all 9;
+// MODE 0: any subset given by mask9 (bit kr*3+kc).
+__device__ __forceinline__ uint32_t maj3(uint32_t a, uint32_t b, uint32_t c) {
+    return (a & b) | (c & (a ^ b));
+}
+
+template <int MODE>
+__device__ __forceinline__ void plane_count(const uint32_t (&w)[3], const uint32_t (&n)[3],
+                                            const uint32_t (&e)[3], unsigned mask9, uint32_t& c0,
+                                            uint32_t& c1, uint32_t& c2, uint32_t& c3) {
+    if (MODE == 0) {
+        c0 = c1 = c2 = c3 = 0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (mask9 & (1u << (k * 3 + 0))) csa_add(c0, c1, c2, c3, w[k]);
+            if (mask9 & (1u << (k * 3 + 1))) csa_add(c0, c1, c2, c3, n[k]);
+            if (mask9 & (1u << (k * 3 + 2))) csa_add(c0, c1, c2, c3, e[k]);
+        }
+        return;
+    }
+    // each row as a 2-bit number (ones, twos), then the three rows added
+    const uint32_t ts = w[0] ^ n[0] ^ e[0], tc = maj3(w[0], n[0], e[0]);
+    const uint32_t bs = w[2] ^ n[2] ^ e[2], bc = maj3(w[2], n[2], e[2]);
+    uint32_t ms, mc;
+    if (MODE == 2) { ms = w[1] ^ n[1] ^ e[1]; mc = maj3(w[1], n[1], e[1]); }
+    else { ms = w[1] ^ e[1]; mc = w[1] & e[1]; }
+    c0 = ts ^ ms ^ bs;
+    const uint32_t k1 = maj3(ts, ms, bs);                 // carry into the twos
+    const uint32_t x = tc ^ mc ^ bc, y = maj3(tc, mc, bc);
+    c1 = x ^ k1;
+    const uint32_t k2 = x & k1;                            // carry into the fours
+    c2 = y ^ k2;
+    c3 = y & k2;
+}
+
 // K steps (1 <= K <= kPlaneK) of a toroidal board, starting after T0 steps.
+// A thread owns one word column hx of the haloed tile and kPlaneRPT rows; per
+// step it loads its rows' 3 x (kPlaneRPT + 2) neighbourhood once and computes
+// only rows still needed by the remaining steps.
+constexpr int kPlaneCols = kPlaneHX;
+constexpr int kPlaneGroups = 256 / kPlaneCols;
+constexpr int kPlaneRPT = (kPlaneHY + kPlaneGroups - 1) / kPlaneGroups;
+
+template <int MODE>
 __global__ void __launch_bounds__(256) k_gol_planes_steps(int rows, int W, long long T0, int K,
                                                           uint32_t* __restrict__ planes,
                                                           unsigned mask9, unsigned smask,
@@ -609,44 +653,53 @@ __global__ void __launch_bounds__(256) k_gol_planes_steps(int rows, int W, long 
             old[s][hy][hx] = planes[(size_t)((T0 + s) % kPlaneRing) * plane_words + off];
     }
     __syncthreads();
+    const int hx = threadIdx.x % kPlaneCols, rg = threadIdx.x / kPlaneCols;
+    const bool active = rg < kPlaneGroups;
+    const int ry0 = rg * kPlaneRPT;
     int c = 0;
     for (int s = 0; s < K; ++s) {
-        uint32_t* out = planes + (size_t)((T0 + s + 32) % kPlaneRing) * plane_words;
-        for (int e = threadIdx.x; e < kPlaneHY * kPlaneHX; e += blockDim.x) {
-            const int hy = e / kPlaneHX, hx = e - hy * kPlaneHX;
-            if (hy <= hy0 || hy >= kPlaneHY - 1 - hy0) {
-                cur[c ^ 1][hy][hx] = 0u;         // edge of what K steps need
-                continue;
-            }
-            uint32_t c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+        // rows valid after s steps: [hy0 + s, HY - 1 - hy0 - s]; needed next:
+        const int lo = hy0 + s + 1, hi = kPlaneHY - 2 - hy0 - s;
+        if (active && ry0 + kPlaneRPT - 1 >= lo && ry0 <= hi) {
+            uint32_t wl[kPlaneRPT + 2], wn[kPlaneRPT + 2], we[kPlaneRPT + 2];
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const uint32_t* row = cur[c][hy - 1 + k];
-                const uint32_t n = row[hx];
-                const uint32_t lw = hx > 0 ? row[hx - 1] : 0u;
-                const uint32_t rw = hx < kPlaneHX - 1 ? row[hx + 1] : 0u;
-                const uint32_t wv = (n << 1) | (lw >> 31);
-                const uint32_t ev = (n >> 1) | (rw << 31);
-                if (mask9 & (1u << (k * 3 + 0))) csa_add(c0, c1, c2, c3, wv);
-                if (mask9 & (1u << (k * 3 + 1))) csa_add(c0, c1, c2, c3, n);
-                if (mask9 & (1u << (k * 3 + 2))) csa_add(c0, c1, c2, c3, ev);
+            for (int q = 0; q < kPlaneRPT + 2; ++q) {
+                const int hy = ry0 - 1 + q;
+                const bool ok = hy >= 0 && hy < kPlaneHY;
+                const uint32_t n = ok ? cur[c][hy][hx] : 0u;
+                const uint32_t l = ok && hx > 0 ? cur[c][hy][hx - 1] : 0u;
+                const uint32_t r = ok && hx < kPlaneHX - 1 ? cur[c][hy][hx + 1] : 0u;
+                wn[q] = n;
+                wl[q] = (n << 1) | (l >> 31);
+                we[q] = (n >> 1) | (r << 31);
             }
-            uint32_t S = 0, B = 0;
+            uint32_t* out = planes + (size_t)((T0 + s + 32) % kPlaneRing) * plane_words;
 #pragma unroll
-            for (int v = 0; v < 10; ++v) {
-                if (!(((smask | bmask) >> v) & 1u)) continue;
-                const uint32_t eq = ~((c0 ^ ((v & 1) ? ~0u : 0u)) | (c1 ^ ((v & 2) ? ~0u : 0u)) |
-                                      (c2 ^ ((v & 4) ? ~0u : 0u)) | (c3 ^ ((v & 8) ? ~0u : 0u)));
-                if ((smask >> v) & 1u) S |= eq;
-                if ((bmask >> v) & 1u) B |= eq;
+            for (int q = 0; q < kPlaneRPT; ++q) {
+                const int hy = ry0 + q;
+                if (hy < lo || hy > hi) continue;
+                const uint32_t w3[3] = {wl[q], wl[q + 1], wl[q + 2]};
+                const uint32_t n3[3] = {wn[q], wn[q + 1], wn[q + 2]};
+                const uint32_t e3[3] = {we[q], we[q + 1], we[q + 2]};
+                uint32_t c0, c1, c2, c3;
+                plane_count<MODE>(w3, n3, e3, mask9, c0, c1, c2, c3);
+                uint32_t S = 0, B = 0;
+#pragma unroll
+                for (int v = 0; v < 10; ++v) {
+                    if (!(((smask | bmask) >> v) & 1u)) continue;
+                    const uint32_t eq = ~((c0 ^ ((v & 1) ? ~0u : 0u)) | (c1 ^ ((v & 2) ? ~0u : 0u)) |
+                                          (c2 ^ ((v & 4) ? ~0u : 0u)) | (c3 ^ ((v & 8) ? ~0u : 0u)));
+                    if ((smask >> v) & 1u) S |= eq;
+                    if ((bmask >> v) & 1u) B |= eq;
+                }
+                const uint32_t O = old[s][hy][hx];
+                const uint32_t L = (O & S) | (~O & B);
+                cur[c ^ 1][hy][hx] = L;
+                const int ty = hy - kPlaneK, tx = hx - 1;
+                if (ty >= 0 && ty < kPlaneTY && tx >= 0 && tx < kPlaneTX && r0 + ty < rows &&
+                    w0 + tx < W)
+                    out[(size_t)(r0 + ty) * W + w0 + tx] = L;
             }
-            const uint32_t O = old[s][hy][hx];
-            const uint32_t L = (O & S) | (~O & B);
-            cur[c ^ 1][hy][hx] = L;
-            const int ty = hy - kPlaneK, tx = hx - 1;
-            if (ty >= 0 && ty < kPlaneTY && tx >= 0 && tx < kPlaneTX && r0 + ty < rows &&
-                w0 + tx < W)
-                out[(size_t)(r0 + ty) * W + w0 + tx] = L;
         }
         __syncthreads();
         c ^= 1;
@@ -746,19 +799,22 @@ class GameOfLifeModel : public Model {
         k_gol_words_to_planes<<<blocks_for(segs * 32, 256), 256, 0, s>>>(l.rows, W, words, planes);
         SG_LAUNCH_CHECK();
         ++launches;
-        static bool configured = false;
-        if (!configured) {
-            SG_CUDA(cudaFuncSetAttribute(k_gol_planes_steps,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPlaneSmem));
-            configured = true;
+        // counting kernel: the 8 outer neighbours, all 9, or any other 0/1 mask
+        const int mode = (mask9 & 0x1EFu) == 0x1EFu ? ((mask9 & 0x10u) ? 2 : 1) : 0;
+        auto kernel = mode == 1 ? k_gol_planes_steps<1>
+                                : (mode == 2 ? k_gol_planes_steps<2> : k_gol_planes_steps<0>);
+        static bool configured[3] = {false, false, false};
+        if (!configured[mode]) {
+            SG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kPlaneSmem));
+            configured[mode] = true;
         }
         const dim3 grid((unsigned)((W + kPlaneTX - 1) / kPlaneTX),
                         (unsigned)((l.rows + kPlaneTY - 1) / kPlaneTY));
         long long T = 0;
         while (T < n) {
             const int K = (int)std::min<long long>(kPlaneK, n - T);
-            k_gol_planes_steps<<<grid, 256, kPlaneSmem, s>>>(l.rows, W, T, K, planes, mask9, smask,
-                                                             bmask);
+            kernel<<<grid, 256, kPlaneSmem, s>>>(l.rows, W, T, K, planes, mask9, smask, bmask);
             SG_LAUNCH_CHECK();
             ++launches;
             T += K;
