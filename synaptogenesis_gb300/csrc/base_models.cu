@@ -522,7 +522,7 @@ __global__ void __launch_bounds__(256) k_gol_bits_tile(int rows, int cols, int w
 // each side, and the K oldest planes it needs; wrong values enter the halo
 // from its outer edge at one cell per step and never reach the tile within K
 // steps (a halo word is 32 cells wide).
-constexpr int kPlaneRing = 64;
+constexpr int kPlaneRing = 64;          // a power of two
 constexpr int kPlaneK = 16;
 constexpr int kPlaneTY = 64;
 constexpr int kPlaneTX = 8;
@@ -624,12 +624,13 @@ __device__ __forceinline__ void plane_count(const uint32_t (&w)[3], const uint32
 // A thread owns one word column hx of the haloed tile and kPlaneRPT rows; per
 // step it loads its rows' 3 x (kPlaneRPT + 2) neighbourhood once and computes
 // only rows still needed by the remaining steps.
+constexpr int kPlaneThreads = 512;
 constexpr int kPlaneCols = kPlaneHX;
-constexpr int kPlaneGroups = 256 / kPlaneCols;
+constexpr int kPlaneGroups = kPlaneThreads / kPlaneCols;
 constexpr int kPlaneRPT = (kPlaneHY + kPlaneGroups - 1) / kPlaneGroups;
 
 template <int MODE>
-__global__ void __launch_bounds__(256) k_gol_planes_steps(int rows, int W, long long T0, int K,
+__global__ void __launch_bounds__(kPlaneThreads) k_gol_planes_steps(int rows, int W, long long T0, int K,
                                                           uint32_t* __restrict__ planes,
                                                           unsigned mask9, unsigned smask,
                                                           unsigned bmask) {
@@ -641,7 +642,8 @@ __global__ void __launch_bounds__(256) k_gol_planes_steps(int rows, int W, long 
     const size_t plane_words = (size_t)rows * W;
     const int r0 = blockIdx.y * kPlaneTY, w0 = blockIdx.x * kPlaneTX;
     const int hy0 = kPlaneK - K;             // halo rows K steps do not need
-    const uint32_t* newest = planes + (size_t)((T0 + 31) % kPlaneRing) * plane_words;
+    const int t0 = (int)(T0 & (kPlaneRing - 1));           // ring index of step T0
+    const uint32_t* newest = planes + (size_t)((t0 + 31) & (kPlaneRing - 1)) * plane_words;
     for (int e = threadIdx.x; e < kPlaneHY * kPlaneHX; e += blockDim.x) {
         const int hy = e / kPlaneHX, hx = e - hy * kPlaneHX;
         int gr = (r0 - kPlaneK + hy) % rows, gw = (w0 - 1 + hx) % W;
@@ -650,7 +652,7 @@ __global__ void __launch_bounds__(256) k_gol_planes_steps(int rows, int W, long 
         const size_t off = (size_t)gr * W + gw;
         cur[0][hy][hx] = newest[off];
         for (int s = 0; s < K; ++s)
-            old[s][hy][hx] = planes[(size_t)((T0 + s) % kPlaneRing) * plane_words + off];
+            old[s][hy][hx] = planes[(size_t)((t0 + s) & (kPlaneRing - 1)) * plane_words + off];
     }
     __syncthreads();
     const int hx = threadIdx.x % kPlaneCols, rg = threadIdx.x / kPlaneCols;
@@ -673,7 +675,7 @@ __global__ void __launch_bounds__(256) k_gol_planes_steps(int rows, int W, long 
                 wl[q] = (n << 1) | (l >> 31);
                 we[q] = (n >> 1) | (r << 31);
             }
-            uint32_t* out = planes + (size_t)((T0 + s + 32) % kPlaneRing) * plane_words;
+            uint32_t* out = planes + (size_t)((t0 + s + 32) & (kPlaneRing - 1)) * plane_words;
 #pragma unroll
             for (int q = 0; q < kPlaneRPT; ++q) {
                 const int hy = ry0 + q;
@@ -814,7 +816,8 @@ class GameOfLifeModel : public Model {
         long long T = 0;
         while (T < n) {
             const int K = (int)std::min<long long>(kPlaneK, n - T);
-            kernel<<<grid, 256, kPlaneSmem, s>>>(l.rows, W, T, K, planes, mask9, smask, bmask);
+            kernel<<<grid, kPlaneThreads, kPlaneSmem, s>>>(l.rows, W, T, K, planes, mask9, smask,
+                                                           bmask);
             SG_LAUNCH_CHECK();
             ++launches;
             T += K;
