@@ -61,7 +61,7 @@ constexpr int kTauBlocks = 64;
 constexpr int kBlock = 256;
 
 struct Dims {
-    int L, rows, cols, N, field, h, K, O, B, T, k, nseg, nchunk;
+    int L, rows, cols, N, field, h, K, O, B, T, k, nseg, nchunk, bg;
     float dt;
     long long S;   // L * B * N
 };
@@ -79,61 +79,114 @@ __global__ void k_rate_transpose(Dims D, const float* __restrict__ w, float* __r
     wt[idx] = w[l * per + (long long)i * D.K + k];
 }
 
-// One forward timestep: grid (N / 256, L * B).  Blocks of the last layer also
-// reduce their neurons' readout contributions (fixed tree) into
-// ypart[b][block][o] when ypart is given.
+// One forward timestep: grid (tiles of 16 x 16 neurons, layers, groups of
+// D.bg batch elements).  A thread keeps its neuron's field x field weights
+// (and, in the last layer, its readout weights) in registers; per batch
+// element the CTA stages the source rates of its tile plus the kernel's halo
+// (zero outside the layer: a skipped source adds w * 0) in shared memory,
+// double-buffered, with the next element's halo fetched into registers while
+// the current one is summed.  Tiles of the last layer reduce their readout
+// contributions (fixed tree) into ypart[b][tile][o].
+constexpr int kTileSide = 16;
+constexpr int kMaxBatchGroup = 8;
+
+// Source window of a tile: element e of the (16 + 2h)^2 halo, zero outside.
+template <int F>
+struct Halo {
+    static constexpr int H = F / 2, SIDE = kTileSide + 2 * H, COUNT = SIDE * SIDE;
+    static constexpr int PER = (COUNT + kBlock - 1) / kBlock;
+    __device__ static void fetch(const Dims& D, const float* plane, float scale, int ty0, int tx0,
+                                 float (&reg)[PER]) {
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int e = threadIdx.x + q * kBlock;
+            const int sy = e / SIDE, sx = e - sy * SIDE;
+            const int r = ty0 - H + sy, c = tx0 - H + sx;
+            reg[q] = (e < COUNT && r >= 0 && r < D.rows && c >= 0 && c < D.cols)
+                         ? scale * plane[r * D.cols + c] : 0.0f;
+        }
+    }
+    __device__ static void stage(const float (&reg)[PER], float (*dst)[SIDE + 1]) {
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int e = threadIdx.x + q * kBlock;
+            const int sy = e / SIDE, sx = e - sy * SIDE;
+            if (e < COUNT) dst[sy][sx] = reg[q];
+        }
+    }
+};
+
+template <int F>
 __global__ void __launch_bounds__(kBlock) k_rate_step(
-    Dims D, const float* __restrict__ x_t, const float* __restrict__ wt,
-    const float* __restrict__ wo, const float* __restrict__ tau, const float* __restrict__ v_prev,
+    Dims D, const float* __restrict__ x_t, const float* wt, const float* wo,
+    const float* __restrict__ tau, const float* __restrict__ v_prev,
     const float* __restrict__ r_prev, float* __restrict__ v_new, float* __restrict__ r_new,
     float* __restrict__ d_out, float* __restrict__ ypart) {
+    using W = Halo<F>;
+    __shared__ float src[2][W::SIDE][W::SIDE + 1];
     __shared__ float red[kBlock / 32][kMaxOutputs];
-    const int l = blockIdx.y / D.B, b = blockIdx.y - l * D.B;
-    const int i = blockIdx.x * kBlock + threadIdx.x;
-    const bool ok = i < D.N;
-    const long long idx = ((long long)l * D.B + b) * D.N + i;
-    float rn = 0.0f;
-    if (ok) {
-        const float a = D.dt / __ldg(tau + l);
-        float I;
-        if (l == 0) {
-            I = __ldg(x_t + (long long)b * D.N + i);
-        } else {
-            const float* wl = wt + (long long)(l - 1) * D.K * D.N + i;
-            const float* src = r_prev + ((long long)(l - 1) * D.B + b) * D.N;
-            const int ir = i / D.cols, ic = i - ir * D.cols;
-            I = 0.0f;
-            int k = 0;
-            for (int kr = 0; kr < D.field; ++kr) {
-                const int sr = ir - D.h + kr;
-                if (sr < 0 || sr >= D.rows) { k += D.field; continue; }
-                for (int kc = 0; kc < D.field; ++kc, ++k) {
-                    const int sc = ic - D.h + kc;
-                    if (sc < 0 || sc >= D.cols) continue;
-                    I += __ldg(wl + (long long)k * D.N) * src[sr * D.cols + sc];
-                }
-            }
-        }
-        const float vp = v_prev[idx];
-        const float d = -vp + I;
-        const float vn = vp + a * d;
-        v_new[idx] = vn;
-        rn = sigmoid(vn);
-        r_new[idx] = rn;
-        if (d_out) d_out[idx] = d;
-    }
-    if (ypart && l == D.L - 1) {
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        for (int o = 0; o < D.O; ++o) {
-            float c = ok ? __ldg(wo + (long long)o * D.N + i) * rn : 0.0f;
-            for (int off = 16; off > 0; off >>= 1) c += __shfl_down_sync(0xFFFFFFFFu, c, off);
-            if (lane == 0) red[warp][o] = c;
-        }
+    const int tiles_x = (D.cols + kTileSide - 1) / kTileSide;
+    const int tile = blockIdx.x, l = blockIdx.y;
+    const int ty0 = (tile / tiles_x) * kTileSide, tx0 = (tile % tiles_x) * kTileSide;
+    const int tr = threadIdx.x / kTileSide, tc = threadIdx.x % kTileSide;
+    const int ir = ty0 + tr, ic = tx0 + tc;
+    const bool ok = ir < D.rows && ic < D.cols;
+    const int i = ir * D.cols + ic;
+    const bool readout = ypart && l == D.L - 1;
+    const float a = D.dt / __ldg(tau + l);
+    // plain loads: kept in registers across the batch loop's barriers
+    float wk[F * F];
+#pragma unroll
+    for (int k = 0; k < F * F; ++k)
+        wk[k] = (l >= 1 && ok) ? wt[((long long)(l - 1) * F * F + k) * D.N + i] : 0.0f;
+    float wov[kMaxOutputs];
+#pragma unroll
+    for (int o = 0; o < kMaxOutputs; ++o)
+        wov[o] = (readout && ok && o < D.O) ? wo[(long long)o * D.N + i] : 0.0f;
+    const int b0 = blockIdx.z * D.bg, b1 = min(D.B, b0 + D.bg);
+    const float* rp = l >= 1 ? r_prev + (long long)(l - 1) * D.B * D.N : nullptr;
+    float pre[W::PER];
+    if (l >= 1) W::fetch(D, rp + (long long)b0 * D.N, 1.0f, ty0, tx0, pre);
+    for (int b = b0, buf = 0; b < b1; ++b, buf ^= 1) {
+        if (l >= 1) W::stage(pre, src[buf]);
+        const long long idx = ((long long)l * D.B + b) * D.N + i;
+        const float vp = ok ? v_prev[idx] : 0.0f;
+        float I = (ok && l == 0) ? __ldg(x_t + (long long)b * D.N + i) : 0.0f;
         __syncthreads();
-        if (threadIdx.x < D.O) {
-            float y = 0.0f;
-            for (int w = 0; w < kBlock / 32; ++w) y += red[w][threadIdx.x];
-            ypart[((long long)b * D.nchunk + blockIdx.x) * D.O + threadIdx.x] = y;
+        if (l >= 1 && b + 1 < b1) W::fetch(D, rp + (long long)(b + 1) * D.N, 1.0f, ty0, tx0, pre);
+        float rn = 0.0f;
+        if (ok) {
+            if (l >= 1) {
+#pragma unroll
+                for (int kr = 0; kr < F; ++kr)
+#pragma unroll
+                    for (int kc = 0; kc < F; ++kc) I += wk[kr * F + kc] * src[buf][tr + kr][tc + kc];
+            }
+            const float d = -vp + I;
+            const float vn = vp + a * d;
+            v_new[idx] = vn;
+            rn = sigmoid(vn);
+            r_new[idx] = rn;
+            if (d_out) d_out[idx] = d;
+        }
+        if (readout) {
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+            float c[kMaxOutputs];
+#pragma unroll
+            for (int o = 0; o < kMaxOutputs; ++o) c[o] = wov[o] * rn;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+                for (int o = 0; o < kMaxOutputs; ++o) c[o] += __shfl_down_sync(0xFFFFFFFFu, c[o], off);
+            if (lane == 0)
+#pragma unroll
+                for (int o = 0; o < kMaxOutputs; ++o) red[warp][o] = c[o];
+            __syncthreads();
+            if (threadIdx.x < D.O) {
+                float y = 0.0f;
+                for (int w = 0; w < kBlock / 32; ++w) y += red[w][threadIdx.x];
+                ypart[((long long)b * D.nchunk + tile) * D.O + threadIdx.x] = y;
+            }
         }
     }
 }
@@ -190,43 +243,73 @@ __global__ void k_rate_gy(Dims D, float gscale, const float* __restrict__ y,
     gy[e] = gscale * (y[e] - target[bo]);
 }
 
-// Adjoint of one timestep for every layer and batch element (grid like the
-// step kernel): lambda[t] from lambda[t+1] (the next layer's inputs at t+1
-// read the rates of t).
+// Adjoint of one timestep, grid like the step kernel: lambda[t] from
+// lambda[t+1] (the next layer's inputs at t+1 read the rates of t).  Neuron i
+// of layer l feeds destinations j = i + h - (kr, kc) of layer l+1; the thread
+// keeps those field x field weights (zero where j is outside the layer) in
+// registers, and per batch element the CTA stages a_{l+1} * lambda_{l+1}[t+1]
+// of its tile plus halo in shared memory, double-buffered like the step.
+template <int F>
 __global__ void __launch_bounds__(kBlock) k_rate_lambda(
-    Dims D, const float* __restrict__ wt, const float* __restrict__ wo,
-    const float* __restrict__ tau, const float* __restrict__ gy_t, const float* __restrict__ r_t,
+    Dims D, const float* wt, const float* wo, const float* __restrict__ tau,
+    const float* __restrict__ gy_t, const float* __restrict__ r_t,
     const float* __restrict__ lam_next, float* __restrict__ lam, float* __restrict__ dx_t) {
-    const int l = blockIdx.y / D.B, b = blockIdx.y - l * D.B;
-    const int i = blockIdx.x * kBlock + threadIdx.x;
-    if (i >= D.N) return;
-    const long long idx = ((long long)l * D.B + b) * D.N + i;
-    float g = 0.0f;
-    if (l == D.L - 1) {
-        for (int o = 0; o < D.O; ++o)
-            g += __ldg(wo + (long long)o * D.N + i) * __ldg(gy_t + (long long)b * D.O + o);
-    } else {
-        // destinations j of layer l+1 whose window holds i: j = i + h - (kr, kc)
-        const float a1 = D.dt / __ldg(tau + l + 1);
-        const float* wl = wt + (long long)l * D.K * D.N;          // weights into layer l+1
-        const float* ln = lam_next + ((long long)(l + 1) * D.B + b) * D.N;
-        const int ir = i / D.cols, ic = i - ir * D.cols;
-        for (int kr = 0; kr < D.field; ++kr) {
-            const int jr = ir + D.h - kr;
-            if (jr < 0 || jr >= D.rows) continue;
-            for (int kc = 0; kc < D.field; ++kc) {
-                const int jc = ic + D.h - kc;
-                if (jc < 0 || jc >= D.cols) continue;
-                const int j = jr * D.cols + jc;
-                g += __ldg(wl + (long long)(kr * D.field + kc) * D.N + j) * (a1 * ln[j]);
+    using W = Halo<F>;
+    constexpr int H = W::H;
+    __shared__ float P[2][W::SIDE][W::SIDE + 1];
+    const int tiles_x = (D.cols + kTileSide - 1) / kTileSide;
+    const int tile = blockIdx.x, l = blockIdx.y;
+    const int ty0 = (tile / tiles_x) * kTileSide, tx0 = (tile % tiles_x) * kTileSide;
+    const int tr = threadIdx.x / kTileSide, tc = threadIdx.x % kTileSide;
+    const int ir = ty0 + tr, ic = tx0 + tc;
+    const bool ok = ir < D.rows && ic < D.cols;
+    const int i = ir * D.cols + ic;
+    const bool last = l == D.L - 1;
+    const float a = D.dt / __ldg(tau + l);
+    const float a1 = last ? 0.0f : D.dt / __ldg(tau + l + 1);
+    float wk[F * F];
+#pragma unroll
+    for (int kr = 0; kr < F; ++kr)
+#pragma unroll
+        for (int kc = 0; kc < F; ++kc) {
+            const int jr = ir + H - kr, jc = ic + H - kc;
+            wk[kr * F + kc] = (!last && ok && jr >= 0 && jr < D.rows && jc >= 0 && jc < D.cols)
+                                  ? wt[((long long)l * F * F + kr * F + kc) * D.N + jr * D.cols + jc]
+                                  : 0.0f;
+        }
+    float wov[kMaxOutputs];
+#pragma unroll
+    for (int o = 0; o < kMaxOutputs; ++o)
+        wov[o] = (last && ok && o < D.O) ? wo[(long long)o * D.N + i] : 0.0f;
+    const int b0 = blockIdx.z * D.bg, b1 = min(D.B, b0 + D.bg);
+    const float* ln = last ? nullptr : lam_next + (long long)(l + 1) * D.B * D.N;
+    float pre[W::PER];
+    if (!last) W::fetch(D, ln + (long long)b0 * D.N, a1, ty0, tx0, pre);
+    for (int b = b0, buf = 0; b < b1; ++b, buf ^= 1) {
+        if (!last) W::stage(pre, P[buf]);
+        const long long idx = ((long long)l * D.B + b) * D.N + i;
+        const float r = ok ? r_t[idx] : 0.0f;
+        const float own = ok ? lam_next[idx] : 0.0f;
+        __syncthreads();
+        if (!last && b + 1 < b1) W::fetch(D, ln + (long long)(b + 1) * D.N, a1, ty0, tx0, pre);
+        if (ok) {
+            float g = 0.0f;
+            if (last) {
+#pragma unroll
+                for (int o = 0; o < kMaxOutputs; ++o)
+                    if (o < D.O) g += wov[o] * __ldg(gy_t + (long long)b * D.O + o);
+            } else {
+#pragma unroll
+                for (int kr = 0; kr < F; ++kr)
+#pragma unroll
+                    for (int kc = 0; kc < F; ++kc)
+                        g += wk[kr * F + kc] * P[buf][tr + 2 * H - kr][tc + 2 * H - kc];
             }
+            const float lv = r * (1.0f - r) * g + (1.0f - a) * own;
+            lam[idx] = lv;
+            if (l == 0 && dx_t) dx_t[(long long)b * D.N + i] = a * lv;
         }
     }
-    const float a = D.dt / __ldg(tau + l);
-    const float r = r_t[idx];
-    const float lv = r * (1.0f - r) * g + (1.0f - a) * lam_next[idx];
-    lam[idx] = lv;
-    if (l == 0 && dx_t) dx_t[(long long)b * D.N + i] = a * lv;
 }
 
 // dW over one segment.  A CTA covers 32 destinations j of one (layer >= 1,
@@ -421,7 +504,12 @@ Dims make_dims(const SgRateShape& s) {
     D.T = s.steps;
     D.k = s.checkpoint;
     D.nseg = (s.steps + s.checkpoint - 1) / s.checkpoint;
-    D.nchunk = (D.N + kBlock - 1) / kBlock;
+    D.nchunk = ((D.rows + kTileSide - 1) / kTileSide) * ((D.cols + kTileSide - 1) / kTileSide);
+    // batch elements per CTA: the largest group that still gives four CTAs
+    // per SM (152 SMs), fewer halo and weight reloads per element
+    D.bg = 1;
+    for (int g = kMaxBatchGroup; g > 1; g >>= 1)
+        if ((long long)D.nchunk * D.L * ((D.B + g - 1) / g) >= 4 * 152) { D.bg = g; break; }
     D.dt = s.dt;
     D.S = (long long)D.L * D.B * D.N;
     return D;
@@ -471,12 +559,32 @@ void transpose_weights(const Dims& D, const float* w, const Work& W, cudaStream_
     SG_LAUNCH_CHECK();
 }
 
+dim3 tile_grid(const Dims& D) {
+    return dim3((unsigned)D.nchunk, (unsigned)D.L, (unsigned)((D.B + D.bg - 1) / D.bg));
+}
+
+#define SG_RATE_FIELD(F_RT, CALL)                                                 \
+    switch (F_RT) {                                                               \
+        case 1: { constexpr int F = 1; CALL; } break;                             \
+        case 3: { constexpr int F = 3; CALL; } break;                             \
+        case 5: { constexpr int F = 5; CALL; } break;                             \
+        case 7: { constexpr int F = 7; CALL; } break;                             \
+        default: { constexpr int F = 9; CALL; } break;                            \
+    }
+
 void step(const Dims& D, const float* x_t, const float* wo, const float* tau, const Work& W,
           const float* v_prev, const float* r_prev, float* v_new, float* r_new, float* d_out,
           float* ypart, cudaStream_t st) {
-    dim3 grid(D.nchunk, D.L * D.B);
-    k_rate_step<<<grid, kBlock, 0, st>>>(D, x_t, W.wt, wo, tau, v_prev, r_prev, v_new, r_new, d_out,
-                                         ypart);
+    SG_RATE_FIELD(D.field, (k_rate_step<F><<<tile_grid(D), kBlock, 0, st>>>(
+                               D, x_t, W.wt, wo, tau, v_prev, r_prev, v_new, r_new, d_out, ypart)));
+    SG_LAUNCH_CHECK();
+}
+
+void lambda_step(const Dims& D, const float* wo, const float* tau, const Work& W,
+                 const float* gy_t, const float* r_t, const float* lam_next, float* lam, float* dx_t,
+                 cudaStream_t st) {
+    SG_RATE_FIELD(D.field, (k_rate_lambda<F><<<tile_grid(D), kBlock, 0, st>>>(
+                               D, W.wt, wo, tau, gy_t, r_t, lam_next, lam, dx_t)));
     SG_LAUNCH_CHECK();
 }
 
@@ -520,7 +628,6 @@ void backward(const Dims& D, const float* x, const float* w, const float* wo, co
         SG_CUDA(cudaMemsetAsync(dw, 0, (size_t)(D.L - 1) * D.N * D.K * sizeof(float), st));
     SG_CUDA(cudaMemsetAsync(dwo, 0, (size_t)D.O * D.N * sizeof(float), st));
     SG_CUDA(cudaMemsetAsync(W.carry, 0, D.S * sizeof(float), st));
-    const dim3 grid(D.nchunk, D.L * D.B);
     for (int seg = D.nseg - 1; seg >= 0; --seg) {
         const int c = seg * D.k, nt = std::min(D.k, D.T - c);
         SG_CUDA(cudaMemcpyAsync(W.seg_v, W.ckpt + (long long)seg * D.S, D.S * sizeof(float),
@@ -534,11 +641,10 @@ void backward(const Dims& D, const float* x, const float* w, const float* wo, co
         for (int tt = nt; tt >= 1; --tt) {
             const int t = c + tt;
             const float* lam_next = tt == nt ? W.carry : W.seg_lam + (long long)tt * D.S;
-            k_rate_lambda<<<grid, kBlock, 0, st>>>(
-                D, W.wt, wo, tau, W.gy + (long long)(t - 1) * D.B * D.O,
-                W.seg_r + (long long)tt * D.S, lam_next, W.seg_lam + (long long)(tt - 1) * D.S,
-                dx ? dx + (long long)(t - 1) * D.B * D.N : nullptr);
-            SG_LAUNCH_CHECK();
+            lambda_step(D, wo, tau, W, W.gy + (long long)(t - 1) * D.B * D.O,
+                        W.seg_r + (long long)tt * D.S, lam_next,
+                        W.seg_lam + (long long)(tt - 1) * D.S,
+                        dx ? dx + (long long)(t - 1) * D.B * D.N : nullptr, st);
         }
         SG_CUDA(cudaMemcpyAsync(W.carry, W.seg_lam, D.S * sizeof(float),
                                 cudaMemcpyDeviceToDevice, st));
