@@ -177,7 +177,8 @@ __global__ void __launch_bounds__(kBlock) k_rate_step(
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1)
 #pragma unroll
-                for (int o = 0; o < kMaxOutputs; ++o) c[o] += __shfl_down_sync(0xFFFFFFFFu, c[o], off);
+                for (int o = 0; o < kMaxOutputs; ++o)
+                    if (o < D.O) c[o] += __shfl_down_sync(0xFFFFFFFFu, c[o], off);
             if (lane == 0)
 #pragma unroll
                 for (int o = 0; o < kMaxOutputs; ++o) red[warp][o] = c[o];
@@ -312,130 +313,142 @@ __global__ void __launch_bounds__(kBlock) k_rate_lambda(
     }
 }
 
-// dW over one segment.  A CTA covers 32 destinations j of one (layer >= 1,
-// kernel row kr) for all of the row's kernel columns; its 8 thread groups
-// take 8 batch elements each.  Per timestep (latest first) a group sums its
-// elements in order, the groups' sums are added in group order, and the
-// accumulator takes the step's total: a fixed order that does not depend on
-// where the segments start.
+// dW, one timestep of a segment per CTA row: grid ((L-1) * field * tiles of
+// 32 destinations j, timesteps).  A CTA covers 32 destinations j of one
+// (layer >= 1, kernel row kr) for all of the row's kernel columns; its 8
+// thread groups take 8 batch elements each, loading a group's lambdas and
+// source rates before summing them.  The groups' sums are added in group
+// order and written as the step's total to part[tt][l-1][j][k];
+// k_rate_dw_acc then adds the steps, latest first, into dW: a fixed order
+// that does not depend on where the segments start.
 constexpr int kGroups = 8;
+constexpr int kUnroll = 8;
 
-__global__ void __launch_bounds__(kBlock) k_rate_dw(Dims D, int nt, const float* __restrict__ tau,
-                                                   const float* __restrict__ seg_lam,
+template <int F>
+__global__ void __launch_bounds__(kBlock) k_rate_dw(Dims D, const float* __restrict__ seg_lam,
                                                    const float* __restrict__ seg_r,
-                                                   float* __restrict__ dw) {
-    __shared__ float part[kGroups][32][kMaxField + 1];
+                                                   float* __restrict__ part) {
+    constexpr int H = F / 2, K = F * F;
+    __shared__ float gsum[kGroups][32][F + 1];
     const int jl = threadIdx.x & 31, g = threadIdx.x >> 5;
     const int tiles = (D.N + 31) / 32;
     const int tile = blockIdx.x % tiles, lk = blockIdx.x / tiles;
-    const int kr = lk % D.field, l = 1 + lk / D.field;
+    const int kr = lk % F, l = 1 + lk / F, tt = blockIdx.y;
     const int j = tile * 32 + jl;
     const bool ok = j < D.N;
     const int jr = ok ? j / D.cols : 0, jc = ok ? j - jr * D.cols : 0;
-    const int sr = jr - D.h + kr, sc0 = jc - D.h;
+    const int sr = jr - H + kr, sc0 = jc - H;
     const bool row_ok = ok && sr >= 0 && sr < D.rows;
-    const float a = D.dt / __ldg(tau + l);
     const int bpg = (D.B + kGroups - 1) / kGroups;
     const int b0 = g * bpg, b1 = min(D.B, b0 + bpg);
-    float* out = dw + ((long long)(l - 1) * D.N + j) * D.K + kr * D.field;
-    float acc[kMaxField];
+    // lambda of step t = c + tt + 1 and the source rates of step t - 1
+    float st[F];
 #pragma unroll
-    for (int kc = 0; kc < kMaxField; ++kc) acc[kc] = 0.0f;
-    if (g == 0 && row_ok) {
+    for (int kc = 0; kc < F; ++kc) st[kc] = 0.0f;
+    if (row_ok) {
+        const float* lam = seg_lam + (long long)tt * D.S + (long long)l * D.B * D.N + j;
+        const float* rr = seg_r + (long long)tt * D.S + (long long)(l - 1) * D.B * D.N +
+                          sr * D.cols + sc0;
+        for (int bb = b0; bb < b1; bb += kUnroll) {
+            float lv[kUnroll], rv[kUnroll][F];
 #pragma unroll
-        for (int kc = 0; kc < kMaxField; ++kc)
-            if (kc < D.field) acc[kc] = out[kc];
-    }
-    for (int tt = nt - 1; tt >= 0; --tt) {
-        // lambda of step t = c + tt + 1 and the source rates of step t - 1
-        float st[kMaxField];
+            for (int u = 0; u < kUnroll; ++u) {
+                const bool in = bb + u < b1;
+                lv[u] = in ? lam[(long long)(bb + u) * D.N] : 0.0f;
 #pragma unroll
-        for (int kc = 0; kc < kMaxField; ++kc) st[kc] = 0.0f;
-        if (row_ok) {
-            const float* lam = seg_lam + (long long)tt * D.S + (long long)l * D.B * D.N + j;
-            const float* rr = seg_r + (long long)tt * D.S + (long long)(l - 1) * D.B * D.N +
-                              sr * D.cols + sc0;
-            for (int b = b0; b < b1; ++b) {
-                const float lv = lam[(long long)b * D.N];
-                const float* rb = rr + (long long)b * D.N;
+                for (int kc = 0; kc < F; ++kc)
+                    rv[u][kc] = (in && sc0 + kc >= 0 && sc0 + kc < D.cols)
+                                    ? rr[(long long)(bb + u) * D.N + kc] : 0.0f;
+            }
 #pragma unroll
-                for (int kc = 0; kc < kMaxField; ++kc)
-                    if (kc < D.field && sc0 + kc >= 0 && sc0 + kc < D.cols) st[kc] += lv * rb[kc];
+            for (int u = 0; u < kUnroll; ++u) {
+                if (bb + u >= b1) break;
+#pragma unroll
+                for (int kc = 0; kc < F; ++kc)
+                    if (sc0 + kc >= 0 && sc0 + kc < D.cols) st[kc] += lv[u] * rv[u][kc];
             }
         }
-#pragma unroll
-        for (int kc = 0; kc < kMaxField; ++kc) part[g][jl][kc] = st[kc];
-        __syncthreads();
-        if (g == 0) {
-#pragma unroll
-            for (int kc = 0; kc < kMaxField; ++kc) {
-                float tot = 0.0f;
-                for (int q = 0; q < kGroups; ++q) tot += part[q][jl][kc];
-                acc[kc] += a * tot;
-            }
-        }
-        __syncthreads();
     }
-    if (g == 0 && row_ok) {
 #pragma unroll
-        for (int kc = 0; kc < kMaxField; ++kc)
-            if (kc < D.field && sc0 + kc >= 0 && sc0 + kc < D.cols) out[kc] = acc[kc];
+    for (int kc = 0; kc < F; ++kc) gsum[g][jl][kc] = st[kc];
+    __syncthreads();
+    if (g == 0 && ok) {
+        float* out = part + (((long long)tt * (D.L - 1) + (l - 1)) * D.N + j) * K + kr * F;
+#pragma unroll
+        for (int kc = 0; kc < F; ++kc) {
+            float tot = 0.0f;
+            for (int q = 0; q < kGroups; ++q) tot += gsum[q][jl][kc];
+            out[kc] = tot;
+        }
     }
 }
 
-// dR over one segment, the same scheme: a CTA covers 32 neurons i for every
-// output, its 8 groups take 8 batch elements each.
-__global__ void __launch_bounds__(kBlock) k_rate_dwo(Dims D, int t0, int nt,
-                                                    const float* __restrict__ gy,
+// dW[l-1][j][k] += a_l * part[tt] for the segment's steps, latest first.
+__global__ void k_rate_dw_acc(Dims D, int nt, const float* __restrict__ tau,
+                              const float* __restrict__ part, float* __restrict__ dw) {
+    const long long per = (long long)D.N * D.K, n = (long long)(D.L - 1) * per;
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const float a = D.dt / __ldg(tau + 1 + (int)(e / per));
+    float acc = dw[e];
+    for (int tt = nt - 1; tt >= 0; --tt) acc += a * part[(long long)tt * n + e];
+    dw[e] = acc;
+}
+
+// dR, the same scheme: grid (tiles of 32 neurons i, timesteps), a CTA covers
+// its 32 neurons for every output with 8 groups of batch elements, the step's
+// total goes to part[tt][o][i] and k_rate_dwo_acc adds the steps latest first.
+__global__ void __launch_bounds__(kBlock) k_rate_dwo(Dims D, int t0, const float* __restrict__ gy,
                                                     const float* __restrict__ seg_r,
-                                                    float* __restrict__ dwo) {
-    __shared__ float part[kGroups][32][kMaxOutputs + 1];
+                                                    float* __restrict__ part) {
+    __shared__ float gsum[kGroups][32][kMaxOutputs + 1];
     const int il = threadIdx.x & 31, g = threadIdx.x >> 5;
-    const int i = blockIdx.x * 32 + il;
+    const int i = blockIdx.x * 32 + il, tt = blockIdx.y;
     const bool ok = i < D.N;
     const int bpg = (D.B + kGroups - 1) / kGroups;
     const int b0 = g * bpg, b1 = min(D.B, b0 + bpg);
-    float acc[kMaxOutputs];
+    const int t = t0 + tt + 1;                          // 1-based step
+    const float* gt = gy + (long long)(t - 1) * D.B * D.O;
+    float st[kMaxOutputs];
 #pragma unroll
-    for (int o = 0; o < kMaxOutputs; ++o) acc[o] = 0.0f;
-    if (g == 0 && ok) {
+    for (int o = 0; o < kMaxOutputs; ++o) st[o] = 0.0f;
+    if (ok) {
+        const float* r = seg_r + (long long)(tt + 1) * D.S + (long long)(D.L - 1) * D.B * D.N + i;
+        for (int bb = b0; bb < b1; bb += kUnroll) {
+            float rv[kUnroll];
 #pragma unroll
-        for (int o = 0; o < kMaxOutputs; ++o)
-            if (o < D.O) acc[o] = dwo[(long long)o * D.N + i];
-    }
-    for (int tt = nt - 1; tt >= 0; --tt) {
-        const int t = t0 + tt + 1;                      // 1-based step
-        const float* gt = gy + (long long)(t - 1) * D.B * D.O;
-        float st[kMaxOutputs];
+            for (int u = 0; u < kUnroll; ++u) rv[u] = bb + u < b1 ? r[(long long)(bb + u) * D.N] : 0.0f;
 #pragma unroll
-        for (int o = 0; o < kMaxOutputs; ++o) st[o] = 0.0f;
-        if (ok) {
-            const float* r = seg_r + (long long)(tt + 1) * D.S + (long long)(D.L - 1) * D.B * D.N + i;
-            for (int b = b0; b < b1; ++b) {
-                const float rv = r[(long long)b * D.N];
+            for (int u = 0; u < kUnroll; ++u) {
+                if (bb + u >= b1) break;
 #pragma unroll
                 for (int o = 0; o < kMaxOutputs; ++o)
-                    if (o < D.O) st[o] += __ldg(gt + (long long)b * D.O + o) * rv;
+                    if (o < D.O) st[o] += __ldg(gt + (long long)(bb + u) * D.O + o) * rv[u];
             }
         }
-#pragma unroll
-        for (int o = 0; o < kMaxOutputs; ++o) part[g][il][o] = st[o];
-        __syncthreads();
-        if (g == 0) {
-#pragma unroll
-            for (int o = 0; o < kMaxOutputs; ++o) {
-                float tot = 0.0f;
-                for (int q = 0; q < kGroups; ++q) tot += part[q][il][o];
-                acc[o] += tot;
-            }
-        }
-        __syncthreads();
     }
+#pragma unroll
+    for (int o = 0; o < kMaxOutputs; ++o) gsum[g][il][o] = st[o];
+    __syncthreads();
     if (g == 0 && ok) {
 #pragma unroll
-        for (int o = 0; o < kMaxOutputs; ++o)
-            if (o < D.O) dwo[(long long)o * D.N + i] = acc[o];
+        for (int o = 0; o < kMaxOutputs; ++o) {
+            if (o >= D.O) break;
+            float tot = 0.0f;
+            for (int q = 0; q < kGroups; ++q) tot += gsum[q][il][o];
+            part[((long long)tt * D.O + o) * D.N + i] = tot;
+        }
     }
+}
+
+__global__ void k_rate_dwo_acc(Dims D, int nt, const float* __restrict__ part,
+                               float* __restrict__ dwo) {
+    const long long n = (long long)D.O * D.N;
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    float acc = dwo[e];
+    for (int tt = nt - 1; tt >= 0; --tt) acc += part[(long long)tt * n + e];
+    dwo[e] = acc;
 }
 
 // Partial sums of lambda * d per (timestep, layer): grid (kTauBlocks, L, nt),
@@ -491,6 +504,8 @@ Dims make_dims(const SgRateShape& s) {
         throw SgError("rate network: field must be odd and at most 9");
     if (!(s.dt > 0.0f)) throw SgError("rate network: dt must be positive");
     if ((long long)s.layers * s.batch > 65535) throw SgError("rate network: layers x batch too large");
+    if (std::min(s.checkpoint, s.steps) > 65535)
+        throw SgError("rate network: at most 65535 steps between checkpoints");
     Dims D;
     D.L = s.layers;
     D.rows = s.rows;
@@ -518,10 +533,11 @@ Dims make_dims(const SgRateShape& s) {
 // Workspace layout (floats): checkpoints [nseg][S], segment states v, r
 // [k+1][S], drives d and adjoints lambda [k][S], the lambda carried across
 // segments [S], outputs y [T][B][O] and their partial sums, squared errors
-// [T][B], dloss/dy [T][B][O], tau partials, transposed weights.
+// [T][B], dloss/dy [T][B][O], tau partials, transposed weights, and the
+// per-step weight and readout gradient totals of one segment.
 struct Work {
     float *ckpt, *seg_v, *seg_r, *seg_d, *seg_lam, *carry, *y, *ypart, *loss_tb, *gy, *tau_part,
-        *tau_steps, *wt;
+        *tau_steps, *wt, *dw_part, *dwo_part;
     long long floats;
 };
 
@@ -548,6 +564,9 @@ Work carve(const Dims& D, void* base) {
     w.tau_part = take((long long)D.T * D.L * kTauBlocks);
     w.tau_steps = take((long long)D.T * D.L);
     w.wt = take((long long)std::max(D.L - 1, 0) * D.K * D.N);
+    const long long seg = std::min(D.k, D.T);
+    w.dw_part = take(seg * std::max(D.L - 1, 0) * D.N * D.K);
+    w.dwo_part = take(seg * D.O * D.N);
     return w;
 }
 
@@ -649,11 +668,18 @@ void backward(const Dims& D, const float* x, const float* w, const float* wo, co
         SG_CUDA(cudaMemcpyAsync(W.carry, W.seg_lam, D.S * sizeof(float),
                                 cudaMemcpyDeviceToDevice, st));
         if (D.L > 1) {
-            k_rate_dw<<<(unsigned)((D.L - 1) * D.field * ((D.N + 31) / 32)), kBlock, 0, st>>>(
-                D, nt, tau, W.seg_lam, W.seg_r, dw);
+            const dim3 grid((unsigned)((D.L - 1) * D.field * ((D.N + 31) / 32)), (unsigned)nt);
+            SG_RATE_FIELD(D.field, (k_rate_dw<F><<<grid, kBlock, 0, st>>>(D, W.seg_lam, W.seg_r,
+                                                                         W.dw_part)));
+            SG_LAUNCH_CHECK();
+            k_rate_dw_acc<<<grid_of((long long)(D.L - 1) * D.N * D.K), 256, 0, st>>>(
+                D, nt, tau, W.dw_part, dw);
             SG_LAUNCH_CHECK();
         }
-        k_rate_dwo<<<(unsigned)((D.N + 31) / 32), kBlock, 0, st>>>(D, c, nt, W.gy, W.seg_r, dwo);
+        k_rate_dwo<<<dim3((unsigned)((D.N + 31) / 32), (unsigned)nt), kBlock, 0, st>>>(
+            D, c, W.gy, W.seg_r, W.dwo_part);
+        SG_LAUNCH_CHECK();
+        k_rate_dwo_acc<<<grid_of((long long)D.O * D.N), 256, 0, st>>>(D, nt, W.dwo_part, dwo);
         SG_LAUNCH_CHECK();
         k_rate_dtau_partial<<<dim3(kTauBlocks, D.L, nt), 256, 0, st>>>(D, c, W.seg_lam, W.seg_d,
                                                                        W.tau_part);

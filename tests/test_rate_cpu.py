@@ -55,9 +55,12 @@ def test_rate_shape_validation_and_workspace():
                              steps=100, checkpoint=10)
     S = 3 * 64 * 4096
     # checkpoints (10) + segment v, r (11 each) + d, lambda (10 each) + carry,
-    # plus outputs, readout partials, transposed weights (under 2 S together)
-    assert net.workspace_bytes >= (10 + 11 + 11 + 10 + 10 + 1) * S * 4
-    assert net.workspace_bytes < (10 + 11 + 11 + 10 + 10 + 3) * S * 4
+    # plus outputs, readout partials, transposed weights (under 2 S together),
+    # plus a segment's per-step weight (10 x 2 x 4096 x 25) and readout
+    # (10 x 10 x 4096) gradient totals
+    steps = 10 * 2 * 4096 * 25 + 10 * 10 * 4096
+    assert net.workspace_bytes >= ((10 + 11 + 11 + 10 + 10 + 1) * S + steps) * 4
+    assert net.workspace_bytes < ((10 + 11 + 11 + 10 + 10 + 3) * S + steps) * 4
     for bad in (dict(outputs=17), dict(field=4), dict(field=11), dict(steps=0),
                 dict(checkpoint=0), dict(dt=0.0)):
         with pytest.raises(ValueError):
