@@ -177,7 +177,7 @@ def rate_workload():
                 "steps of N(0,1) input, MSE to U(0,1) targets (seed 4), checkpoint every 10",
         "unit": "sequence-timesteps/s",
         "dtype": "f32",
-        "kernel": "forward pass (k_rate_step + k_rate_readout per timestep)",
+        "kernel": "k_rate_step (forward pass time per timestep: one launch per timestep, readout fused)",
         "cpu_seconds": 12.0,
         "rate": True,
     }
@@ -733,7 +733,7 @@ def run_rate(args, rank, world, local):
             "fwd_s": fwd_s, "one_s": one_s, "e2e_value": per_step * e2e_steps * world / e2e_max,
             "e2e_steps": e2e_steps, "h2d": h2d, "d2h": d2h,
             "fwd_us_per_timestep": fwd_s * 1e6 / (args.steps * c["steps"]),
-            "fwd_bytes_per_timestep": fwd_bytes, "loss": float(loss)}
+            "fwd_bytes_per_timestep": fwd_bytes, "loss": float(loss.detach())}
 
 
 def rate_line(args, world, r, wl, cb):
@@ -741,11 +741,13 @@ def rate_line(args, world, r, wl, cb):
     c = RATE_CFG
     per_step = c["batch"] * c["steps"]
     achieved = r["fwd_bytes_per_timestep"] / (r["fwd_us_per_timestep"] * 1e-6) / 1e9
-    # kernel launches per forward + adjoint: forward 2 per timestep (step,
-    # readout) + initial rates + loss; backward 2 per timestep (recompute,
-    # adjoint) + per segment rates, dW, dR, dtau partials + the dtau total
+    # kernel launches per forward + adjoint: forward = weight transpose,
+    # initial rates, one step per timestep (readout fused), outputs, loss;
+    # backward = weight transpose, dloss/dy, per timestep a recomputed step and
+    # an adjoint step, per segment the rates, dW and its accumulation, dR and
+    # its accumulation, dtau partials, and the dtau total
     nseg = -(-c["steps"] // c["checkpoint"])
-    launches = (2 * c["steps"] + 2) + (2 * c["steps"] + 4 * nseg + 1)
+    launches = (c["steps"] + 4) + (2 * c["steps"] + 6 * nseg + 3)
     return {
         "metric": "sequence-timesteps/s (rate forward + adjoint)",
         "value": r["units"] / r["dev_s"], "unit": wl["unit"], "n_gpus": world,
