@@ -521,12 +521,15 @@ class Batch {
         words_ = dalloc<uint32_t>(2 * n_neurons_, owned_);
         conv_ew_ = dalloc<float>(n_groups_ * K_ * 32, owned_);
         conv_tr_ = dalloc<float2>(n_groups_ * K_ * 32, owned_);
-        SG_CUDA(cudaMemcpy(d_inst_, inst_.data(), inst_.size() * sizeof(InstDev),
-                           cudaMemcpyHostToDevice));
-        SG_CUDA(cudaMemcpy(d_group_inst_, group_inst_h_.data(), n_groups_ * sizeof(int),
-                           cudaMemcpyHostToDevice));
+        // Every upload goes through stream_ (non-blocking): a plain cudaMemcpy
+        // from pageable memory may return before its DMA lands and is not
+        // ordered with this stream's kernels.
+        SG_CUDA(cudaMemcpyAsync(d_inst_, inst_.data(), inst_.size() * sizeof(InstDev),
+                                cudaMemcpyHostToDevice, stream_));
+        SG_CUDA(cudaMemcpyAsync(d_group_inst_, group_inst_h_.data(), n_groups_ * sizeof(int),
+                                cudaMemcpyHostToDevice, stream_));
         unsigned long long* total = reinterpret_cast<unsigned long long*>(d_counters_ + 3);
-        SG_CUDA(cudaMemset(total, 0, sizeof(unsigned long long)));
+        SG_CUDA(cudaMemsetAsync(total, 0, sizeof(unsigned long long), stream_));
         unsigned blocks = blocks_for(n_groups_ * 32, 256);
         k_batch_count<<<blocks, 256, 0, stream_>>>(d_inst_, d_group_inst_, n_groups_,
                                                    d_group_slots_, total);
@@ -545,8 +548,8 @@ class Batch {
             acc += group_slots_h_[g];
         }
         slot_rows_ = acc;
-        SG_CUDA(cudaMemcpy(d_group_base_, base.data(), n_groups_ * sizeof(long long),
-                           cudaMemcpyHostToDevice));
+        SG_CUDA(cudaMemcpyAsync(d_group_base_, base.data(), n_groups_ * sizeof(long long),
+                                cudaMemcpyHostToDevice, stream_));
         fc_in_ = dalloc<uint2>(slot_rows_ * 32, owned_);
         fc_tr_ = dalloc<float2>(slot_rows_ * 32, owned_);
         k_batch_fill<<<blocks, 256, 0, stream_>>>(d_inst_, d_group_inst_, n_groups_, d_group_base_,
@@ -615,8 +618,8 @@ class Batch {
             units_cap_ = std::max(units_h_.size(), (size_t)(n_groups_ + 1));
             d_units_ = dalloc<Unit>(units_cap_, owned_);
         }
-        SG_CUDA(cudaMemcpy(d_units_, units_h_.data(), units_h_.size() * sizeof(Unit),
-                           cudaMemcpyHostToDevice));
+        SG_CUDA(cudaMemcpyAsync(d_units_, units_h_.data(), units_h_.size() * sizeof(Unit),
+                                cudaMemcpyHostToDevice, stream_));
         int per_sm = 0;
         SG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_step, threads_,
                                                               smem_));

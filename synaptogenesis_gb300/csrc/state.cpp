@@ -142,6 +142,9 @@ void State::allocate_device() {
     arena_bytes_ = std::max<size_t>(off, 256);
     SG_CUDA(cudaMalloc(&arena_, arena_bytes_));
     SG_CUDA(cudaMemset(arena_, 0, arena_bytes_));
+    // the engine's streams are non-blocking: nothing orders them after this
+    // legacy-stream memset, so it completes before any upload or kernel
+    SG_CUDA(cudaDeviceSynchronize());
     for (auto& a : arrays_) a->dev = static_cast<char*>(arena_) + a->dev_offset;
 }
 
@@ -204,7 +207,9 @@ void State::to_device(cudaStream_t stream) {
             transpose(a->host.data(), scratch_.data(), a->rows, a->cols);
             src = scratch_.data();
         }
-        SG_CUDA(cudaMemcpy(a->dev, src, n * 4, cudaMemcpyHostToDevice));
+        // on the engine's stream: a pageable cudaMemcpy may return before its
+        // DMA lands and would not be ordered with that stream's kernels
+        SG_CUDA(cudaMemcpyAsync(a->dev, src, n * 4, cudaMemcpyHostToDevice, stream));
     }
     for (auto& cp : network->connections)
         find_model(cp->to->model)->prepare_device(*this, *conns[cp->index], stream);
