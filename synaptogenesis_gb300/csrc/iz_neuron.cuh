@@ -3,6 +3,7 @@
 // both execute the same float/double expression sequence.
 #pragma once
 
+#include "exact_convert.cuh"
 #include "exact_div.cuh"
 
 namespace sg {
@@ -12,21 +13,24 @@ namespace sg {
 // conductance-implicit voltage update and the recovery step whose time
 // constant is adjusted on the substep that crosses threshold.
 //
-// Every operation is the reference's, in its types (the double literals make
-// the voltage arithmetic double), with three rewrites that leave each result
-// bit-identical and save FP64 instructions:
+// Every operation is the reference's, in its types and order (the double
+// literals make the voltage arithmetic double; each double operation is
+// written out as the IEEE intrinsic C++ promotion implies), with four
+// rewrites that leave each result bit-identical and save FP64 instructions:
 //  * comparisons with 30.0 are float comparisons (30 is a float and
 //    float -> double conversion is exact);
 //  * the conductance sum and the implicit-update denominator do not change
 //    within the step and are computed once;
 //  * the division by that denominator uses its correctly rounded reciprocal
-//    (div_rn_recip, exact).
+//    (div_rn_recip, exact);
+//  * float <-> double conversions run in integer arithmetic (f2d_exact,
+//    d2f_rn), off the FP64 pipe.
 __device__ __forceinline__ void iz_integrate(float& voltage, float& recovery, float ampa_c,
                                              float nmda_c, float gabaa_c, float gabab_c, float mf,
                                              float base_current, float a, float b) {
     if (!(voltage < 30.0f)) return;
     const float sum_c = ampa_c + nmda_c + gabaa_c + gabab_c;
-    const double den = 1 + (0.1 * sum_c);
+    const double den = __dadd_rn(1.0, __dmul_rn(0.1, f2d_exact(sum_c)));   // 1 + (0.1 * sum_c)
     const double rden = 1.0 / den;
     for (int i = 0; (i < 10) && (voltage < 30.0f); ++i) {
         float current = -ampa_c * voltage;
@@ -37,9 +41,17 @@ __device__ __forceinline__ void iz_integrate(float& voltage, float& recovery, fl
         current -= gabab_c * (voltage + 90);
         current *= 1 + mf;
         current += base_current;
-        float delta_v = (0.04 * voltage * voltage) + (5 * voltage) + 140 - recovery + current;
-        voltage = div_rn_recip(voltage + 0.1 * (delta_v + (gabaa_c * -70) + (gabab_c * -90)),
-                               den, rden);
+        // delta_v = (0.04 * voltage * voltage) + (5 * voltage) + 140 - recovery + current
+        const double vd = f2d_exact(voltage);
+        double dv = __dmul_rn(__dmul_rn(0.04, vd), vd);
+        dv = __dadd_rn(dv, f2d_exact(5 * voltage));
+        dv = __dadd_rn(dv, 140.0);
+        dv = __dsub_rn(dv, f2d_exact(recovery));
+        dv = __dadd_rn(dv, f2d_exact(current));
+        const float delta_v = d2f_rn(dv);
+        // voltage = (voltage + 0.1 * (delta_v + (gabaa_c * -70) + (gabab_c * -90))) / den
+        const float drive = delta_v + (gabaa_c * -70) + (gabab_c * -90);
+        voltage = d2f_rn(div_rn_recip(__dadd_rn(vd, __dmul_rn(0.1, f2d_exact(drive))), den, rden));
         voltage = (voltage != voltage) ? 30.0f : voltage;
         float adjusted_tau = (voltage > 30.0f)
                                  ? (float)(delta_v / (30.0 - voltage + delta_v) * 0.1)

@@ -67,7 +67,9 @@ __device__ __forceinline__ void iz_learn_synapse(size_t wi, int src_tss, float d
     const bool src_spike = src_tss == 0;
     float src_trace, dest_trace;
     if (!SUB) {
-        src_trace = (presyn[wi] = src_spike ? 0.004 : presyn[wi] * 0.933);
+        // presyn = src_spike ? 0.004 : presyn * 0.933, stored as float
+        src_trace = src_spike ? (float)0.004 : mul_fd_rn(presyn[wi], 0.933);
+        presyn[wi] = src_trace;
         dest_trace = dest_exc_trace;
     } else {
         src_trace = (dest_spike > 0.0f && src_tss > 0 && src_tss < 32) ? lut.src[src_tss] : 0.0f;
@@ -75,10 +77,11 @@ __device__ __forceinline__ void iz_learn_synapse(size_t wi, int src_tss, float d
     }
     // wd -= (wd - 1e-6) * 1e-4 + dest_spike * src_trace - src_spike * dest_trace
     float weight_delta = wd[wi];
-    double change = (weight_delta - 0.000001) * 0.0001;
-    if (dest_spike != 0.0f) change = change + (dest_spike * src_trace);
-    if (src_spike) change = change - (src_spike * dest_trace);
-    weight_delta = wd[wi] = weight_delta - change;
+    const double wdd = f2d_exact(weight_delta);
+    double change = __dmul_rn(__dsub_rn(wdd, 0.000001), 0.0001);
+    if (dest_spike != 0.0f) change = __dadd_rn(change, f2d_exact(dest_spike * src_trace));
+    if (src_spike) change = __dsub_rn(change, f2d_exact(src_spike * dest_trace));
+    weight_delta = wd[wi] = d2f_rn(__dsub_rn(wdd, change));
     weight += lr * weight_delta;
     w[wi] = fmaxf(0.0001f, fminf(max_weight, weight));
     if (stp_flag) {
@@ -90,9 +93,10 @@ __device__ __forceinline__ void iz_learn_synapse(size_t wi, int src_tss, float d
             stp_r[wi] = r + (((1 - r) / D) - (r * sw * src_spike));
         if (src_spike || !(U == (double)(float)U && sw == (float)U)) {
             // stp_w += (U - sw) / F + U * (1 - sw) * src_spike
-            double inc = div_rn_recip(U - sw, (double)F, 1.0 / F);
+            const double swd = f2d_exact(sw);
+            double inc = div_rn_recip(__dsub_rn(U, swd), (double)F, 1.0 / F);
             if (src_spike) inc = inc + (U * (1 - sw) * src_spike);
-            stp_w[wi] = sw + inc;
+            stp_w[wi] = d2f_rn(__dadd_rn(swd, inc));
         }
     }
 }
