@@ -95,6 +95,8 @@ template <int F>
 struct Halo {
     static constexpr int H = F / 2, SIDE = kTileSide + 2 * H, COUNT = SIDE * SIDE;
     static constexpr int PER = (COUNT + kBlock - 1) / kBlock;
+    // row pitch = 16 (mod 32): the two tile rows a warp reads hit disjoint banks
+    static constexpr int PITCH = SIDE <= 16 ? 16 : 48;
     __device__ static void fetch(const Dims& D, const float* plane, float scale, int ty0, int tx0,
                                  float (&reg)[PER]) {
 #pragma unroll
@@ -106,7 +108,7 @@ struct Halo {
                          ? scale * plane[r * D.cols + c] : 0.0f;
         }
     }
-    __device__ static void stage(const float (&reg)[PER], float (*dst)[SIDE + 1]) {
+    __device__ static void stage(const float (&reg)[PER], float (*dst)[PITCH]) {
 #pragma unroll
         for (int q = 0; q < PER; ++q) {
             const int e = threadIdx.x + q * kBlock;
@@ -123,7 +125,7 @@ __global__ void __launch_bounds__(kBlock) k_rate_step(
     const float* __restrict__ r_prev, float* __restrict__ v_new, float* __restrict__ r_new,
     float* __restrict__ d_out, float* __restrict__ ypart) {
     using W = Halo<F>;
-    __shared__ float src[2][W::SIDE][W::SIDE + 1];
+    __shared__ float src[2][W::SIDE][W::PITCH];
     __shared__ float red[kBlock / 32][kMaxOutputs];
     const int tiles_x = (D.cols + kTileSide - 1) / kTileSide;
     const int tile = blockIdx.x, l = blockIdx.y;
@@ -257,7 +259,7 @@ __global__ void __launch_bounds__(kBlock) k_rate_lambda(
     const float* __restrict__ lam_next, float* __restrict__ lam, float* __restrict__ dx_t) {
     using W = Halo<F>;
     constexpr int H = W::H;
-    __shared__ float P[2][W::SIDE][W::SIDE + 1];
+    __shared__ float P[2][W::SIDE][W::PITCH];
     const int tiles_x = (D.cols + kTileSide - 1) / kTileSide;
     const int tile = blockIdx.x, l = blockIdx.y;
     const int ty0 = (tile / tiles_x) * kTileSide, tx0 = (tile % tiles_x) * kTileSide;
