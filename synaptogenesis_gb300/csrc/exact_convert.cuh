@@ -45,6 +45,34 @@ __device__ __forceinline__ float d2f_rn(double d) {
     return __double2float_rn(d);                // float subnormal, overflow, inf, NaN
 }
 
+// (double)f * c for a positive normal double c (a constant at the call
+// sites): the 77-bit product of the significands rounded to nearest even.
+__device__ __forceinline__ double mul_df_rn(float f, double c) {
+    const uint64_t cb = (uint64_t)__double_as_longlong(c);
+    const uint64_t mc = (cb & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int ec = (int)((cb >> 52) & 0x7FF) - 1023;
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xFFu;
+    if (e - 1u < 254u) {
+        const uint64_t mf = (u & 0x7FFFFFu) | 0x800000u;
+        const uint64_t lo = mc * mf, hi = __umul64hi(mc, mf);
+        const int top = (int)(hi >> 12) & 1;
+        const int sh = 23 + top;
+        uint64_t m = (lo >> sh) | (hi << (64 - sh));
+        const uint64_t rem = lo & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+        int ex = (int)e - 127 + ec + top;
+        m += (rem > half || (rem == half && (m & 1))) ? 1 : 0;
+        if (m >> 53) { m >>= 1; ++ex; }
+        if (ex >= -1022 && ex <= 1023)
+            return __longlong_as_double((long long)(((uint64_t)(u & 0x80000000u) << 32) |
+                                                    ((uint64_t)(ex + 1023) << 52) |
+                                                    (m & 0xFFFFFFFFFFFFFull)));
+    } else if ((u << 1) == 0u) {
+        return __hiloint2double((int)(u & 0x80000000u), 0);      // +-0 * c = +-0
+    }
+    return __dmul_rn((double)f, c);
+}
+
 // (float)(f * c) for a positive normal double c (a constant at the call
 // sites, so its significand and exponent fold at compile time): the double
 // product rounded to nearest even (53 bits), then to float (24 bits) -- the

@@ -23,14 +23,15 @@ namespace sg {
 //    within the step and are computed once;
 //  * the division by that denominator uses its correctly rounded reciprocal
 //    (div_rn_recip, exact);
-//  * float <-> double conversions run in integer arithmetic (f2d_exact,
-//    d2f_rn), off the FP64 pipe.
+//  * float <-> double conversions and the products of a float with a double
+//    constant run in integer arithmetic (f2d_exact, d2f_rn, mul_df_rn), off
+//    the FP64 pipe.
 __device__ __forceinline__ void iz_integrate(float& voltage, float& recovery, float ampa_c,
                                              float nmda_c, float gabaa_c, float gabab_c, float mf,
                                              float base_current, float a, float b) {
     if (!(voltage < 30.0f)) return;
     const float sum_c = ampa_c + nmda_c + gabaa_c + gabab_c;
-    const double den = __dadd_rn(1.0, __dmul_rn(0.1, f2d_exact(sum_c)));   // 1 + (0.1 * sum_c)
+    const double den = __dadd_rn(1.0, mul_df_rn(sum_c, 0.1));   // 1 + (0.1 * sum_c)
     const double rden = 1.0 / den;
     for (int i = 0; (i < 10) && (voltage < 30.0f); ++i) {
         float current = -ampa_c * voltage;
@@ -43,7 +44,7 @@ __device__ __forceinline__ void iz_integrate(float& voltage, float& recovery, fl
         current += base_current;
         // delta_v = (0.04 * voltage * voltage) + (5 * voltage) + 140 - recovery + current
         const double vd = f2d_exact(voltage);
-        double dv = __dmul_rn(__dmul_rn(0.04, vd), vd);
+        double dv = __dmul_rn(mul_df_rn(voltage, 0.04), vd);
         dv = __dadd_rn(dv, f2d_exact(5 * voltage));
         dv = __dadd_rn(dv, 140.0);
         dv = __dsub_rn(dv, f2d_exact(recovery));
@@ -51,7 +52,7 @@ __device__ __forceinline__ void iz_integrate(float& voltage, float& recovery, fl
         const float delta_v = d2f_rn(dv);
         // voltage = (voltage + 0.1 * (delta_v + (gabaa_c * -70) + (gabab_c * -90))) / den
         const float drive = delta_v + (gabaa_c * -70) + (gabab_c * -90);
-        voltage = d2f_rn(div_rn_recip(__dadd_rn(vd, __dmul_rn(0.1, f2d_exact(drive))), den, rden));
+        voltage = d2f_rn(div_rn_recip(__dadd_rn(vd, mul_df_rn(drive, 0.1)), den, rden));
         voltage = (voltage != voltage) ? 30.0f : voltage;
         float adjusted_tau = (voltage > 30.0f)
                                  ? (float)(delta_v / (30.0 - voltage + delta_v) * 0.1)

@@ -94,7 +94,7 @@ __device__ __forceinline__ void iz_learn_synapse(size_t wi, int src_tss, float d
         if (src_spike || !(U == (double)(float)U && sw == (float)U)) {
             // stp_w += (U - sw) / F + U * (1 - sw) * src_spike
             const double swd = f2d_exact(sw);
-            double inc = div_rn_recip(__dsub_rn(U, swd), (double)F, 1.0 / F);
+            double inc = div_const_rn<F>(__dsub_rn(U, swd));
             if (src_spike) inc = inc + (U * (1 - sw) * src_spike);
             stp_w[wi] = d2f_rn(__dadd_rn(swd, inc));
         }

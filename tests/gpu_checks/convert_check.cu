@@ -50,6 +50,19 @@ __global__ void k_mul_all(double c, Result* r) {
     atomicAdd(&r->checked, checked);
 }
 
+// every float bit pattern times the constant c, kept in double:
+// mul_df_rn(f, c) == (double)f * c
+__global__ void k_muld_all(double c, Result* r) {
+    unsigned long long checked = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+         i < (1ull << 32); i += (unsigned long long)gridDim.x * blockDim.x) {
+        const float f = __uint_as_float((uint32_t)i);
+        record(r, !same(sg::mul_df_rn(f, c), __dmul_rn((double)f, c)), i);
+        ++checked;
+    }
+    atomicAdd(&r->checked, checked);
+}
+
 // d2f_rn on n doubles: raw random bit patterns (every exponent), values of
 // the float range whose 29 dropped bits are an exact tie, one either side of
 // it, zero, all ones or random, and the exponents at the edges of the float
@@ -120,4 +133,9 @@ extern "C" int check_d2f(unsigned long long n, unsigned long long seed, unsigned
     g_n = n;
     g_seed = seed;
     return run([](Result* d) { k_d2f<<<152 * 8, 256>>>(g_n, g_seed, d); }, out);
+}
+
+extern "C" int check_muld_all(double c, unsigned long long* out) {
+    g_c = c;
+    return run([](Result* d) { k_muld_all<<<152 * 8, 256>>>(g_c, d); }, out);
 }

@@ -66,6 +66,29 @@ __global__ void k_random(unsigned long long n, unsigned long long seed, Result* 
     atomicAdd(&r->checked, checked);
 }
 
+// div_const_rn<F>: (U - sw) / F for every finite float sw, and raw doubles
+// over the whole exponent range, against the IEEE division.
+template <int F>
+__global__ void k_const_int(double U, unsigned long long n_random, unsigned long long seed,
+                            Result* r) {
+    unsigned long long checked = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+         i < (1ull << 32) + n_random; i += (unsigned long long)gridDim.x * blockDim.x) {
+        double x;
+        if (i < (1ull << 32)) {
+            const float sw = __uint_as_float((uint32_t)i);
+            if (!isfinite(sw)) continue;
+            x = U - sw;
+        } else {
+            x = __longlong_as_double((long long)sg::rng_bits(seed, 3, i));
+            if (isnan(x)) continue;
+        }
+        record(r, __double_as_longlong(x / F) != __double_as_longlong(sg::div_const_rn<F>(x)), i);
+        ++checked;
+    }
+    atomicAdd(&r->checked, checked);
+}
+
 int run(void (*launch)(Result*), unsigned long long* out) {
     Result* d = nullptr;
     if (cudaMalloc(&d, sizeof(Result)) != cudaSuccess) return -1;
@@ -99,4 +122,16 @@ extern "C" int check_random_pairs(unsigned long long n, unsigned long long seed,
     g_n = n;
     g_seed = seed;
     return run([](Result* d) { k_random<<<152 * 8, 256>>>(g_n, g_seed, d); }, out);
+}
+
+extern "C" int check_integer_divisor(double U, int F, unsigned long long n_random,
+                                     unsigned long long seed, unsigned long long* out) {
+    g_U = U;
+    g_F = F;
+    g_n = n_random;
+    g_seed = seed;
+    if (F == 1000) return run([](Result* d) { k_const_int<1000><<<152 * 8, 256>>>(g_U, g_n, g_seed, d); }, out);
+    if (F == 20) return run([](Result* d) { k_const_int<20><<<152 * 8, 256>>>(g_U, g_n, g_seed, d); }, out);
+    if (F == 3) return run([](Result* d) { k_const_int<3><<<152 * 8, 256>>>(g_U, g_n, g_seed, d); }, out);
+    return -3;
 }
