@@ -620,17 +620,27 @@ __device__ __forceinline__ void plane_count(const uint32_t (&w)[3], const uint32
     c3 = y & k2;
 }
 
+__device__ __forceinline__ void cp_async_u32(uint32_t* dst, const uint32_t* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(
+                     (unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+
 // K steps (1 <= K <= kPlaneK) of a toroidal board, starting after T0 steps.
 // A thread owns one word column hx of the haloed tile and kPlaneRPT rows; per
 // step it loads its rows' 3 x (kPlaneRPT + 2) neighbourhood once and computes
-// only rows still needed by the remaining steps.
+// only rows still needed by the remaining steps.  CONWAY: survival on 2 or 3
+// neighbours, birth on 3 (the rule the schema defaults to), as four logic
+// operations; otherwise any survival and birth count masks.
 constexpr int kPlaneThreads = 512;
 constexpr int kPlaneCols = kPlaneHX;
 constexpr int kPlaneGroups = kPlaneThreads / kPlaneCols;
 constexpr int kPlaneRPT = (kPlaneHY + kPlaneGroups - 1) / kPlaneGroups;
 
-template <int MODE>
-__global__ void __launch_bounds__(kPlaneThreads) k_gol_planes_steps(int rows, int W, long long T0, int K,
+template <int MODE, bool CONWAY>
+__global__ void __launch_bounds__(kPlaneThreads) k_gol_planes_steps(int rows, int W, int ty,
+                                                          long long T0, int K,
                                                           uint32_t* __restrict__ planes,
                                                           unsigned mask9, unsigned smask,
                                                           unsigned bmask) {
@@ -640,40 +650,47 @@ __global__ void __launch_bounds__(kPlaneThreads) k_gol_planes_steps(int rows, in
     auto cur = reinterpret_cast<uint32_t(*)[kPlaneHY][kPlaneHX]>(plane_smem);
     auto old = reinterpret_cast<uint32_t(*)[kPlaneHY][kPlaneHX]>(plane_smem + 2 * kPlaneHY * kPlaneHX);
     const size_t plane_words = (size_t)rows * W;
-    const int r0 = blockIdx.y * kPlaneTY, w0 = blockIdx.x * kPlaneTX;
+    // tile of ty <= kPlaneTY rows; its haloed rows 0 .. hy_n - 1
+    const int r0 = blockIdx.y * ty, w0 = blockIdx.x * kPlaneTX, hy_n = ty + 2 * kPlaneK;
     const int hy0 = kPlaneK - K;             // halo rows K steps do not need
     const int t0 = (int)(T0 & (kPlaneRing - 1));           // ring index of step T0
     const uint32_t* newest = planes + (size_t)((t0 + 31) & (kPlaneRing - 1)) * plane_words;
-    for (int e = threadIdx.x; e < kPlaneHY * kPlaneHX; e += blockDim.x) {
+    // every word of the K + 1 planes in flight at once (cp.async), then one wait
+    for (int e = threadIdx.x; e < hy_n * kPlaneHX; e += blockDim.x) {
         const int hy = e / kPlaneHX, hx = e - hy * kPlaneHX;
         int gr = (r0 - kPlaneK + hy) % rows, gw = (w0 - 1 + hx) % W;
         if (gr < 0) gr += rows;
         if (gw < 0) gw += W;
         const size_t off = (size_t)gr * W + gw;
-        cur[0][hy][hx] = newest[off];
+        cp_async_u32(&cur[0][hy][hx], newest + off);
         for (int s = 0; s < K; ++s)
-            old[s][hy][hx] = planes[(size_t)((t0 + s) & (kPlaneRing - 1)) * plane_words + off];
+            cp_async_u32(&old[s][hy][hx],
+                         planes + (size_t)((t0 + s) & (kPlaneRing - 1)) * plane_words + off);
     }
+    asm volatile("cp.async.commit_group;\ncp.async.wait_all;\n" ::: "memory");
     __syncthreads();
     const int hx = threadIdx.x % kPlaneCols, rg = threadIdx.x / kPlaneCols;
     const bool active = rg < kPlaneGroups;
     const int ry0 = rg * kPlaneRPT;
+    // this thread's column lies in the tile (its words go to global memory)
+    const bool col_out = hx >= 1 && hx <= kPlaneTX && w0 + hx - 1 < W;
+    const int ty_end = min(ty, rows - r0);
     int c = 0;
     for (int s = 0; s < K; ++s) {
         // rows valid after s steps: [hy0 + s, HY - 1 - hy0 - s]; needed next:
-        const int lo = hy0 + s + 1, hi = kPlaneHY - 2 - hy0 - s;
+        const int lo = hy0 + s + 1, hi = hy_n - 2 - hy0 - s;
         if (active && ry0 + kPlaneRPT - 1 >= lo && ry0 <= hi) {
             uint32_t wl[kPlaneRPT + 2], wn[kPlaneRPT + 2], we[kPlaneRPT + 2];
 #pragma unroll
             for (int q = 0; q < kPlaneRPT + 2; ++q) {
                 const int hy = ry0 - 1 + q;
-                const bool ok = hy >= 0 && hy < kPlaneHY;
+                const bool ok = hy >= 0 && hy < hy_n;
                 const uint32_t n = ok ? cur[c][hy][hx] : 0u;
                 const uint32_t l = ok && hx > 0 ? cur[c][hy][hx - 1] : 0u;
                 const uint32_t r = ok && hx < kPlaneHX - 1 ? cur[c][hy][hx + 1] : 0u;
                 wn[q] = n;
-                wl[q] = (n << 1) | (l >> 31);
-                we[q] = (n >> 1) | (r << 31);
+                wl[q] = __funnelshift_l(l, n, 1);          // (n << 1) | (l >> 31)
+                we[q] = __funnelshift_r(n, r, 1);          // (n >> 1) | (r << 31)
             }
             uint32_t* out = planes + (size_t)((t0 + s + 32) & (kPlaneRing - 1)) * plane_words;
 #pragma unroll
@@ -685,27 +702,39 @@ __global__ void __launch_bounds__(kPlaneThreads) k_gol_planes_steps(int rows, in
                 const uint32_t e3[3] = {we[q], we[q + 1], we[q + 2]};
                 uint32_t c0, c1, c2, c3;
                 plane_count<MODE>(w3, n3, e3, mask9, c0, c1, c2, c3);
-                uint32_t S = 0, B = 0;
-#pragma unroll
-                for (int v = 0; v < 10; ++v) {
-                    if (!(((smask | bmask) >> v) & 1u)) continue;
-                    const uint32_t eq = ~((c0 ^ ((v & 1) ? ~0u : 0u)) | (c1 ^ ((v & 2) ? ~0u : 0u)) |
-                                          (c2 ^ ((v & 4) ? ~0u : 0u)) | (c3 ^ ((v & 8) ? ~0u : 0u)));
-                    if ((smask >> v) & 1u) S |= eq;
-                    if ((bmask >> v) & 1u) B |= eq;
-                }
                 const uint32_t O = old[s][hy][hx];
-                const uint32_t L = (O & S) | (~O & B);
+                uint32_t L;
+                if (CONWAY) {
+                    // count 3 (0011): alive; count 2 (0010): alive if it was
+                    L = c1 & ~c2 & ~c3 & (c0 | O);
+                } else {
+                    uint32_t S = 0, B = 0;
+#pragma unroll
+                    for (int v = 0; v < 10; ++v) {
+                        if (!(((smask | bmask) >> v) & 1u)) continue;
+                        const uint32_t eq = ~((c0 ^ ((v & 1) ? ~0u : 0u)) | (c1 ^ ((v & 2) ? ~0u : 0u)) |
+                                              (c2 ^ ((v & 4) ? ~0u : 0u)) | (c3 ^ ((v & 8) ? ~0u : 0u)));
+                        if ((smask >> v) & 1u) S |= eq;
+                        if ((bmask >> v) & 1u) B |= eq;
+                    }
+                    L = (O & S) | (~O & B);
+                }
                 cur[c ^ 1][hy][hx] = L;
-                const int ty = hy - kPlaneK, tx = hx - 1;
-                if (ty >= 0 && ty < kPlaneTY && tx >= 0 && tx < kPlaneTX && r0 + ty < rows &&
-                    w0 + tx < W)
-                    out[(size_t)(r0 + ty) * W + w0 + tx] = L;
+                const int ty = hy - kPlaneK;
+                if (col_out && (unsigned)ty < (unsigned)ty_end)
+                    out[(size_t)(r0 + ty) * W + w0 + hx - 1] = L;
             }
         }
         __syncthreads();
         c ^= 1;
     }
+}
+
+static int num_sms() {
+    int dev = 0, n = 0;
+    SG_CUDA(cudaGetDevice(&dev));
+    SG_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+    return n;
 }
 
 // Mask of counts in [lo, hi] (counts of a 3x3 kernel are 0..9).
@@ -801,23 +830,40 @@ class GameOfLifeModel : public Model {
         k_gol_words_to_planes<<<blocks_for(segs * 32, 256), 256, 0, s>>>(l.rows, W, words, planes);
         SG_LAUNCH_CHECK();
         ++launches;
-        // counting kernel: the 8 outer neighbours, all 9, or any other 0/1 mask
+        // counting kernel: the 8 outer neighbours, all 9, or any other 0/1
+        // mask; the B3/S23 rule as its own instance
         const int mode = (mask9 & 0x1EFu) == 0x1EFu ? ((mask9 & 0x10u) ? 2 : 1) : 0;
-        auto kernel = mode == 1 ? k_gol_planes_steps<1>
-                                : (mode == 2 ? k_gol_planes_steps<2> : k_gol_planes_steps<0>);
-        static bool configured[3] = {false, false, false};
-        if (!configured[mode]) {
+        const bool conway = smask == count_mask(2, 3) && bmask == count_mask(3, 3);
+        using Kernel = void (*)(int, int, int, long long, int, uint32_t*, unsigned, unsigned,
+                                unsigned);
+        static const Kernel kernels[6] = {k_gol_planes_steps<0, false>, k_gol_planes_steps<1, false>,
+                                          k_gol_planes_steps<2, false>, k_gol_planes_steps<0, true>,
+                                          k_gol_planes_steps<1, true>,  k_gol_planes_steps<2, true>};
+        const int which = mode + (conway ? 3 : 0);
+        const Kernel kernel = kernels[which];
+        static bool configured[6] = {false, false, false, false, false, false};
+        if (!configured[which]) {
             SG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kPlaneSmem));
-            configured[mode] = true;
+            configured[which] = true;
         }
-        const dim3 grid((unsigned)((W + kPlaneTX - 1) / kPlaneTX),
-                        (unsigned)((l.rows + kPlaneTY - 1) / kPlaneTY));
+        // tile height: fewest haloed rows on the busiest SM (CTAs spread
+        // evenly over the SMs, all resident)
+        const int gx = (W + kPlaneTX - 1) / kPlaneTX;
+        const int sms = num_sms();
+        int ty = kPlaneTY;
+        long long best = -1;
+        for (int t = kPlaneTY; t >= 16; --t) {
+            const long long ctas = (long long)gx * ((l.rows + t - 1) / t);
+            const long long cost = (ctas + sms - 1) / sms * (t + 2 * kPlaneK);
+            if (best < 0 || cost < best) { best = cost; ty = t; }
+        }
+        const dim3 grid((unsigned)gx, (unsigned)((l.rows + ty - 1) / ty));
         long long T = 0;
         while (T < n) {
             const int K = (int)std::min<long long>(kPlaneK, n - T);
-            kernel<<<grid, kPlaneThreads, kPlaneSmem, s>>>(l.rows, W, T, K, planes, mask9, smask,
-                                                           bmask);
+            kernel<<<grid, kPlaneThreads, kPlaneSmem, s>>>(l.rows, W, ty, T, K, planes, mask9,
+                                                           smask, bmask);
             SG_LAUNCH_CHECK();
             ++launches;
             T += K;
