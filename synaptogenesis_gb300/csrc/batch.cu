@@ -370,6 +370,9 @@ class Batch {
                                        device_));
         layout(spec, count);
         generate();
+        // counters, words and neurons start defined before the autotuner's
+        // real steps (device allocations are not cleared)
+        reset();
         if (tile_rows > 0 && tile_cblocks > 0) {
             set_tile(tile_rows, tile_cblocks);
         } else {
