@@ -51,24 +51,45 @@ struct IzLut { float src[33]; float dst[33]; };
 // that leave every stored value bit-identical and save FP64 instructions:
 //  * a spike product that is zero (no destination / source spike) adds or
 //    subtracts +0.0 to a partial sum that is never zero, so it is skipped;
-//  * (U - sw) / F divides by the constant F through its correctly rounded
-//    reciprocal (div_rn_recip, exact).
+//  * (U - sw) / F divides by the integer constant F in integer arithmetic
+//    (div_const_rn, exact), and the float <-> double conversions and the
+//    trace decay product run in integer arithmetic (exact_convert.cuh).
+// iz_learn_load reads a synapse's variables and iz_learn_apply updates them,
+// so that a thread can have several synapses' loads in flight at once.
+struct LearnVals {
+    float w, presyn, wd, r, sw;
+};
+
 template <bool SUB>
-__device__ __forceinline__ void iz_learn_synapse(size_t wi, int src_tss, float dest_spike,
-                                                 float dest_exc_trace, int dest_tss, float lr,
-                                                 int stp_flag, float max_weight, float* w,
-                                                 float* presyn, float* wd, float* stp_r,
-                                                 float* stp_w, const IzLut& lut) {
+__device__ __forceinline__ LearnVals iz_learn_load(size_t wi, int stp_flag, const float* w,
+                                                   const float* presyn, const float* wd,
+                                                   const float* stp_r, const float* stp_w) {
+    LearnVals v;
+    v.w = w[wi];
+    v.presyn = SUB ? 0.0f : presyn[wi];
+    v.wd = wd[wi];
+    v.r = stp_flag ? stp_r[wi] : 0.0f;
+    v.sw = stp_flag ? stp_w[wi] : 0.0f;
+    return v;
+}
+
+template <bool SUB>
+__device__ __forceinline__ void iz_learn_apply(size_t wi, const LearnVals& v, int src_tss,
+                                               float dest_spike, float dest_exc_trace,
+                                               int dest_tss, float lr, int stp_flag,
+                                               float max_weight, float* w, float* presyn,
+                                               float* wd, float* stp_r, float* stp_w,
+                                               const IzLut& lut) {
     constexpr double U = SUB ? 0.2 : 0.5;
     constexpr int F = SUB ? 20 : 1000;
     constexpr int D = SUB ? 700 : 800;
-    float weight = w[wi];
+    float weight = v.w;
     if (!(weight >= 0.0001f)) return;
     const bool src_spike = src_tss == 0;
     float src_trace, dest_trace;
     if (!SUB) {
         // presyn = src_spike ? 0.004 : presyn * 0.933, stored as float
-        src_trace = src_spike ? (float)0.004 : mul_fd_rn(presyn[wi], 0.933);
+        src_trace = src_spike ? (float)0.004 : mul_fd_rn(v.presyn, 0.933);
         presyn[wi] = src_trace;
         dest_trace = dest_exc_trace;
     } else {
@@ -76,7 +97,7 @@ __device__ __forceinline__ void iz_learn_synapse(size_t wi, int src_tss, float d
         dest_trace = (src_spike && dest_tss > 0 && dest_tss < 32) ? lut.dst[dest_tss] : 0.0f;
     }
     // wd -= (wd - 1e-6) * 1e-4 + dest_spike * src_trace - src_spike * dest_trace
-    float weight_delta = wd[wi];
+    float weight_delta = v.wd;
     const double wdd = f2d_exact(weight_delta);
     double change = __dmul_rn(__dsub_rn(wdd, 0.000001), 0.0001);
     if (dest_spike != 0.0f) change = __dadd_rn(change, f2d_exact(dest_spike * src_trace));
@@ -85,8 +106,8 @@ __device__ __forceinline__ void iz_learn_synapse(size_t wi, int src_tss, float d
     weight += lr * weight_delta;
     w[wi] = fmaxf(0.0001f, fminf(max_weight, weight));
     if (stp_flag) {
-        const float r = stp_r[wi];
-        const float sw = stp_w[wi];
+        const float r = v.r;
+        const float sw = v.sw;
         // Without a source spike, R = 1 and w = U are fixed points: the
         // increments are +0.0 and the stored values would not change.
         if (src_spike || r != 1.0f || !isfinite(sw))
@@ -99,6 +120,17 @@ __device__ __forceinline__ void iz_learn_synapse(size_t wi, int src_tss, float d
             stp_w[wi] = d2f_rn(__dadd_rn(swd, inc));
         }
     }
+}
+
+template <bool SUB>
+__device__ __forceinline__ void iz_learn_synapse(size_t wi, int src_tss, float dest_spike,
+                                                 float dest_exc_trace, int dest_tss, float lr,
+                                                 int stp_flag, float max_weight, float* w,
+                                                 float* presyn, float* wd, float* stp_r,
+                                                 float* stp_w, const IzLut& lut) {
+    iz_learn_apply<SUB>(wi, iz_learn_load<SUB>(wi, stp_flag, w, presyn, wd, stp_r, stp_w), src_tss,
+                        dest_spike, dest_exc_trace, dest_tss, lr, stp_flag, max_weight, w, presyn,
+                        wd, stp_r, stp_w, lut);
 }
 
 
@@ -217,7 +249,11 @@ __global__ void __launch_bounds__(256) k_iz_activate_conv_tile(
 }
 
 // Updater for non-convolutional convergent connections: one thread per
-// synapse (kernel position, destination), coalesced along destinations.
+// synapse (kernel position, destination), coalesced along destinations.  A
+// thread takes its kernel positions kLearnBatch at a time and loads all of
+// their variables before updating any (distinct synapses: no overlap).
+constexpr int kLearnBatch = 4;
+
 template <int SR, bool SUB>
 __global__ void __launch_bounds__(256) k_iz_learn_conv_tile(
     DGeom g, int K, const uint32_t* __restrict__ dest_out, const float* __restrict__ to_exc,
@@ -229,12 +265,28 @@ __global__ void __launch_bounds__(256) k_iz_learn_conv_tile(
     const float dest_exc_trace = __ldg(to_exc + d);
     const int dest_tss = __ldg(to_tss + d);
     const float dest_spike = extract<SR>(__ldg(dest_out + d), 0);
-    for (int k = (threadIdx.x >> 5) + blockIdx.y * 8; k < K; k += 8 * gridDim.y) {
-        int from = conv_source(g, d, k);
-        if (from < 0) continue;
-        size_t wi = (size_t)k * g.to_size + d;
-        iz_learn_synapse<SUB>(wi, __ldg(from_tss + from), dest_spike, dest_exc_trace, dest_tss, lr,
-                              stp_flag, max_weight, w, presyn, wd, stp_r, stp_w, lut);
+    const int kstep = 8 * gridDim.y;
+    for (int k0 = (threadIdx.x >> 5) + blockIdx.y * 8; k0 < K; k0 += kstep * kLearnBatch) {
+        LearnVals v[kLearnBatch];
+        int src_tss[kLearnBatch];
+        bool ok[kLearnBatch];
+#pragma unroll
+        for (int b = 0; b < kLearnBatch; ++b) {
+            const int k = k0 + b * kstep;
+            const int from = k < K ? conv_source(g, d, k) : -1;
+            ok[b] = from >= 0;
+            if (ok[b]) {
+                v[b] = iz_learn_load<SUB>((size_t)k * g.to_size + d, stp_flag, w, presyn, wd,
+                                          stp_r, stp_w);
+                src_tss[b] = __ldg(from_tss + from);
+            }
+        }
+#pragma unroll
+        for (int b = 0; b < kLearnBatch; ++b)
+            if (ok[b])
+                iz_learn_apply<SUB>((size_t)(k0 + b * kstep) * g.to_size + d, v[b], src_tss[b],
+                                    dest_spike, dest_exc_trace, dest_tss, lr, stp_flag, max_weight,
+                                    w, presyn, wd, stp_r, stp_w, lut);
     }
 }
 
