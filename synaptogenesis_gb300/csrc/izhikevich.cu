@@ -324,8 +324,11 @@ __global__ void k_iz_gap(DGeom g, const float* __restrict__ voltage, const float
 // visit in serial order: t = spike ? 0 : min(32, t + 1).  The result depends
 // only on the last visit that saw a spike and on how many visits follow it,
 // so each source scans its last (at most 32) visits backwards.
+// A source whose last visits all read the same delay (uniform[f] >= 0, the
+// usual case) either sees a spike at every one of them (0) or at none.
 __global__ void k_iz_time_since_spike(int n_src, const int* __restrict__ counts,
                                       const int* __restrict__ last, const int* __restrict__ delays,
+                                      const int* __restrict__ uniform,
                                       const uint32_t* __restrict__ src, int src_type,
                                       int* __restrict__ tss) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
@@ -333,6 +336,16 @@ __global__ void k_iz_time_since_spike(int n_src, const int* __restrict__ counts,
     int n = counts[f];
     if (n == 0) return;
     uint32_t word = src[f];
+    const int du = uniform[f];
+    if (du >= 0) {
+        if (extract_rt(word, du, src_type) > 0.0f) {
+            tss[f] = 0;
+        } else {
+            const int t = tss[f] + n;
+            tss[f] = t < 32 ? t : 32;
+        }
+        return;
+    }
     int m = n < 32 ? n : 32;
     const int* L = last + (size_t)f * 32;
     for (int j = m - 1; j >= 0; --j) {
@@ -341,6 +354,20 @@ __global__ void k_iz_time_since_spike(int n_src, const int* __restrict__ counts,
     }
     int t = tss[f] + n;
     tss[f] = t < 32 ? t : 32;
+}
+
+// The delay shared by all of a source's last (at most 32) visits, or -1.
+__global__ void k_iz_uniform_delay(int n_src, const int* __restrict__ counts,
+                                   const int* __restrict__ last, const int* __restrict__ delays,
+                                   int* __restrict__ uniform) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_src) return;
+    const int m = min(counts[f], 32);
+    const int* L = last + (size_t)f * 32;
+    int d = m > 0 ? delays[L[0]] : -1;
+    for (int j = 1; j < m && d >= 0; ++j)
+        if (delays[L[j]] != d) d = -1;
+    uniform[f] = d;
 }
 
 // Neuron update (izhikevich_attributes.cpp:102-213)
@@ -435,6 +462,17 @@ class IzhikevichModel : public Model {
   public:
     const char* name() const override { return "izhikevich"; }
     OutputType output_type() const override { return OUT_BIT; }
+
+    // After every upload (delays may have changed): which sources' last
+    // visits share one delay.
+    void prepare_device(State&, ConnState& cs, cudaStream_t s) const override {
+        if (!cs.uniform_delay) return;
+        const int n = cs.conn->from->size;
+        k_iz_uniform_delay<<<blocks_for(n, 256), 256, 0, s>>>(n, cs.visit_counts->di(),
+                                                              cs.last_visits->di(),
+                                                              cs.delays->di(), cs.uniform_delay->di());
+        SG_LAUNCH_CHECK();
+    }
 
     // Constructor of IzhikevichAttributes (izhikevich_attributes.cpp:587-662)
     void build_layer(State& st, LayerState& ls) const override {
@@ -539,6 +577,8 @@ class IzhikevichModel : public Model {
         int nsrc = c.from->size;
         cs.visit_counts = st.add_array("visit counts", 'i', nsrc);
         cs.last_visits = st.add_array("last visits", 'i', (size_t)nsrc * 32);
+        cs.uniform_delay = st.add_array("uniform delay", 'i', nsrc);
+        cs.uniform_delay->scratch = true;
         int32_t* cnt = cs.visit_counts->hi();
         int32_t* last = cs.last_visits->hi();
         enumerate_visits(c, [&](int, int, int from, long wi, int, int) {
@@ -594,8 +634,9 @@ class IzhikevichModel : public Model {
         const uint32_t* src = st.dev_output(c.from, word_index(c.delay, c.from->output_type));
         // time since spike, from the same (pre-update) source words
         k_iz_time_since_spike<<<blocks_for(c.from->size, 256), 256, 0, ctx.stream>>>(
-            c.from->size, cs.visit_counts->di(), cs.last_visits->di(), cs.delays->di(), src,
-            (int)c.from->output_type, cs.var("time since spike")->di());
+            c.from->size, cs.visit_counts->di(), cs.last_visits->di(), cs.delays->di(),
+            cs.uniform_delay->di(), src, (int)c.from->output_type,
+            cs.var("time since spike")->di());
         SG_LAUNCH_CHECK();
         ctx.count();
         int serial = c.convolutional ? 1 : 0;
