@@ -216,22 +216,47 @@ __global__ void __launch_bounds__(256) k_iz_activate_conv_tile(
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int d = blockIdx.x * 32 + lane;
     const bool ok = d < g.to_size;
-    for (int k = warp; k < K; k += 8) {
-        int from = ok ? conv_source(g, d, k) : -1;
-        float st_pre = 0.0f, lt_pre = 0.0f;
-        if (from >= 0) {
-            size_t wi = (size_t)k * g.to_size + d;
-            float spike = extract<SR>(__ldg(src + from), SR == S_BIT ? __ldg(delays + wi) : 0);
-            float weight = __ldg(w + wi) * (__ldg(stp_r + wi) * __ldg(stp_w + wi));
-            st_pre = short_tr[wi] + (spike * weight * gcond);
-            short_tr[wi] = st_pre * short_tau;
-            if (LONG) {
-                lt_pre = long_tr[wi] + (spike * weight * gcond);
-                long_tr[wi] = lt_pre * long_tau;
+    constexpr int B = 4;                 // kernel positions whose loads are in flight together
+    for (int k0 = warp; k0 < K; k0 += 8 * B) {
+        uint32_t word[B];
+        int dl[B];
+        float wv[B], rv[B], sv[B], st0[B], lt0[B];
+        bool on[B];
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            const int k = k0 + 8 * b;
+            const int from = (ok && k < K) ? conv_source(g, d, k) : -1;
+            on[b] = from >= 0;
+            if (on[b]) {
+                const size_t wi = (size_t)k * g.to_size + d;
+                word[b] = __ldg(src + from);
+                dl[b] = SR == S_BIT ? __ldg(delays + wi) : 0;
+                wv[b] = __ldg(w + wi);
+                rv[b] = __ldg(stp_r + wi);
+                sv[b] = __ldg(stp_w + wi);
+                st0[b] = short_tr[wi];
+                lt0[b] = LONG ? long_tr[wi] : 0.0f;
             }
         }
-        s_st[k][lane] = st_pre;
-        if (LONG) s_lt[k][lane] = lt_pre;
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            const int k = k0 + 8 * b;
+            if (k >= K) break;
+            float st_pre = 0.0f, lt_pre = 0.0f;
+            if (on[b]) {
+                const size_t wi = (size_t)k * g.to_size + d;
+                const float spike = extract<SR>(word[b], dl[b]);
+                const float weight = wv[b] * (rv[b] * sv[b]);
+                st_pre = st0[b] + (spike * weight * gcond);
+                short_tr[wi] = st_pre * short_tau;
+                if (LONG) {
+                    lt_pre = lt0[b] + (spike * weight * gcond);
+                    long_tr[wi] = lt_pre * long_tau;
+                }
+            }
+            s_st[k][lane] = st_pre;
+            if (LONG) s_lt[k][lane] = lt_pre;
+        }
     }
     __syncthreads();
     if (!ok) return;
