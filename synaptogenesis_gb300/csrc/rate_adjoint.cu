@@ -66,7 +66,12 @@ struct Dims {
     long long S;   // L * B * N
 };
 
-__device__ __forceinline__ float sigmoid(float v) { return 1.0f / (1.0f + expf(-v)); }
+// The rate network is checked against an FP64 restatement (not a bit-exact
+// reference), so it uses the fast exponential and a correctly rounded
+// reciprocal (relative error a few units in the last place), and explicit
+// fused multiply-adds in its sums; every kernel is deterministic, so the
+// backward pass recomputes the forward states bit for bit.
+__device__ __forceinline__ float sigmoid(float v) { return __frcp_rn(1.0f + __expf(-v)); }
 
 // wt[l][k][i] = w[l][i][k]
 __global__ void k_rate_transpose(Dims D, const float* __restrict__ w, float* __restrict__ wt) {
@@ -91,30 +96,35 @@ constexpr int kTileSide = 16;
 constexpr int kMaxBatchGroup = 8;
 
 // Source window of a tile: element e of the (16 + 2h)^2 halo, zero outside.
+// A thread copies elements threadIdx.x + q * kBlock; their plane offsets
+// (-1 outside the layer) and shared-memory slots (-1 past the window) are the
+// same for every batch element and are worked out once.
 template <int F>
 struct Halo {
     static constexpr int H = F / 2, SIDE = kTileSide + 2 * H, COUNT = SIDE * SIDE;
     static constexpr int PER = (COUNT + kBlock - 1) / kBlock;
     // row pitch = 16 (mod 32): the two tile rows a warp reads hit disjoint banks
     static constexpr int PITCH = SIDE <= 16 ? 16 : 48;
-    __device__ static void fetch(const Dims& D, const float* plane, float scale, int ty0, int tx0,
-                                 float (&reg)[PER]) {
+    int off[PER], slot[PER];
+    __device__ Halo(const Dims& D, int ty0, int tx0) {
 #pragma unroll
         for (int q = 0; q < PER; ++q) {
             const int e = threadIdx.x + q * kBlock;
             const int sy = e / SIDE, sx = e - sy * SIDE;
             const int r = ty0 - H + sy, c = tx0 - H + sx;
-            reg[q] = (e < COUNT && r >= 0 && r < D.rows && c >= 0 && c < D.cols)
-                         ? scale * plane[r * D.cols + c] : 0.0f;
+            slot[q] = e < COUNT ? sy * PITCH + sx : -1;
+            off[q] = (r >= 0 && r < D.rows && c >= 0 && c < D.cols) ? r * D.cols + c : -1;
         }
     }
-    __device__ static void stage(const float (&reg)[PER], float (*dst)[PITCH]) {
+    __device__ void fetch(const float* plane, float scale, float (&reg)[PER]) const {
 #pragma unroll
-        for (int q = 0; q < PER; ++q) {
-            const int e = threadIdx.x + q * kBlock;
-            const int sy = e / SIDE, sx = e - sy * SIDE;
-            if (e < COUNT) dst[sy][sx] = reg[q];
-        }
+        for (int q = 0; q < PER; ++q)
+            reg[q] = (slot[q] >= 0 && off[q] >= 0) ? scale * plane[off[q]] : 0.0f;
+    }
+    __device__ void stage(const float (&reg)[PER], float* dst) const {
+#pragma unroll
+        for (int q = 0; q < PER; ++q)
+            if (slot[q] >= 0) dst[slot[q]] = reg[q];
     }
 };
 
@@ -147,22 +157,31 @@ __global__ void __launch_bounds__(kBlock) k_rate_step(
         wov[o] = (readout && ok && o < D.O) ? wo[(long long)o * D.N + i] : 0.0f;
     const int b0 = blockIdx.z * D.bg, b1 = min(D.B, b0 + D.bg);
     const float* rp = l >= 1 ? r_prev + (long long)(l - 1) * D.B * D.N : nullptr;
+    const W halo(D, ty0, tx0);
     float pre[W::PER];
-    if (l >= 1) W::fetch(D, rp + (long long)b0 * D.N, 1.0f, ty0, tx0, pre);
+    if (l >= 1) halo.fetch(rp + (long long)b0 * D.N, 1.0f, pre);
     for (int b = b0, buf = 0; b < b1; ++b, buf ^= 1) {
-        if (l >= 1) W::stage(pre, src[buf]);
+        if (l >= 1) halo.stage(pre, &src[buf][0][0]);
         const long long idx = ((long long)l * D.B + b) * D.N + i;
         const float vp = ok ? v_prev[idx] : 0.0f;
         float I = (ok && l == 0) ? __ldg(x_t + (long long)b * D.N + i) : 0.0f;
         __syncthreads();
-        if (l >= 1 && b + 1 < b1) W::fetch(D, rp + (long long)(b + 1) * D.N, 1.0f, ty0, tx0, pre);
+        if (l >= 1 && b + 1 < b1) halo.fetch(rp + (long long)(b + 1) * D.N, 1.0f, pre);
         float rn = 0.0f;
         if (ok) {
             if (l >= 1) {
+                // one partial sum per kernel row (independent chains), rows
+                // added in order
+                float part[F];
 #pragma unroll
-                for (int kr = 0; kr < F; ++kr)
+                for (int kr = 0; kr < F; ++kr) {
+                    part[kr] = 0.0f;
 #pragma unroll
-                    for (int kc = 0; kc < F; ++kc) I += wk[kr * F + kc] * src[buf][tr + kr][tc + kc];
+                    for (int kc = 0; kc < F; ++kc)
+                        part[kr] = __fmaf_rn(wk[kr * F + kc], src[buf][tr + kr][tc + kc], part[kr]);
+                }
+#pragma unroll
+                for (int kr = 0; kr < F; ++kr) I += part[kr];
             }
             const float d = -vp + I;
             const float vn = vp + a * d;
@@ -172,18 +191,26 @@ __global__ void __launch_bounds__(kBlock) k_rate_step(
             if (d_out) d_out[idx] = d;
         }
         if (readout) {
+            // butterfly transpose reduction: after the exchanges with lanes
+            // 16, 8, 4, 2 apart a lane holds one output's partial sum of 32
+            // lanes' contributions -- output lane >> 1 -- and the exchange
+            // with the neighbour completes it (16 shuffles for 16 outputs)
             const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
             float c[kMaxOutputs];
 #pragma unroll
             for (int o = 0; o < kMaxOutputs; ++o) c[o] = wov[o] * rn;
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1)
+            for (int half = kMaxOutputs / 2; half >= 1; half /= 2) {
+                const bool up = lane & (2 * half);
 #pragma unroll
-                for (int o = 0; o < kMaxOutputs; ++o)
-                    if (o < D.O) c[o] += __shfl_down_sync(0xFFFFFFFFu, c[o], off);
-            if (lane == 0)
-#pragma unroll
-                for (int o = 0; o < kMaxOutputs; ++o) red[warp][o] = c[o];
+                for (int j = 0; j < half; ++j) {
+                    const float send = up ? c[j] : c[j + half];
+                    const float keep = up ? c[j + half] : c[j];
+                    c[j] = keep + __shfl_xor_sync(0xFFFFFFFFu, send, 2 * half);
+                }
+            }
+            const float y_lane = c[0] + __shfl_xor_sync(0xFFFFFFFFu, c[0], 1);
+            if ((lane & 1) == 0 && (lane >> 1) < D.O) red[warp][lane >> 1] = y_lane;
             __syncthreads();
             if (threadIdx.x < D.O) {
                 float y = 0.0f;
@@ -286,15 +313,16 @@ __global__ void __launch_bounds__(kBlock) k_rate_lambda(
         wov[o] = (last && ok && o < D.O) ? wo[(long long)o * D.N + i] : 0.0f;
     const int b0 = blockIdx.z * D.bg, b1 = min(D.B, b0 + D.bg);
     const float* ln = last ? nullptr : lam_next + (long long)(l + 1) * D.B * D.N;
+    const W halo(D, ty0, tx0);
     float pre[W::PER];
-    if (!last) W::fetch(D, ln + (long long)b0 * D.N, a1, ty0, tx0, pre);
+    if (!last) halo.fetch(ln + (long long)b0 * D.N, a1, pre);
     for (int b = b0, buf = 0; b < b1; ++b, buf ^= 1) {
-        if (!last) W::stage(pre, P[buf]);
+        if (!last) halo.stage(pre, &P[buf][0][0]);
         const long long idx = ((long long)l * D.B + b) * D.N + i;
         const float r = ok ? r_t[idx] : 0.0f;
         const float own = ok ? lam_next[idx] : 0.0f;
         __syncthreads();
-        if (!last && b + 1 < b1) W::fetch(D, ln + (long long)(b + 1) * D.N, a1, ty0, tx0, pre);
+        if (!last && b + 1 < b1) halo.fetch(ln + (long long)(b + 1) * D.N, a1, pre);
         if (ok) {
             float g = 0.0f;
             if (last) {
@@ -302,11 +330,17 @@ __global__ void __launch_bounds__(kBlock) k_rate_lambda(
                 for (int o = 0; o < kMaxOutputs; ++o)
                     if (o < D.O) g += wov[o] * __ldg(gy_t + (long long)b * D.O + o);
             } else {
+                float part[F];
 #pragma unroll
-                for (int kr = 0; kr < F; ++kr)
+                for (int kr = 0; kr < F; ++kr) {
+                    part[kr] = 0.0f;
 #pragma unroll
                     for (int kc = 0; kc < F; ++kc)
-                        g += wk[kr * F + kc] * P[buf][tr + 2 * H - kr][tc + 2 * H - kc];
+                        part[kr] = __fmaf_rn(wk[kr * F + kc], P[buf][tr + 2 * H - kr][tc + 2 * H - kc],
+                                             part[kr]);
+                }
+#pragma unroll
+                for (int kr = 0; kr < F; ++kr) g += part[kr];
             }
             const float lv = r * (1.0f - r) * g + (1.0f - a) * own;
             lam[idx] = lv;
@@ -367,7 +401,7 @@ __global__ void __launch_bounds__(kBlock) k_rate_dw(Dims D, const float* __restr
                 if (bb + u >= b1) break;
 #pragma unroll
                 for (int kc = 0; kc < F; ++kc)
-                    if (sc0 + kc >= 0 && sc0 + kc < D.cols) st[kc] += lv[u] * rv[u][kc];
+                    if (sc0 + kc >= 0 && sc0 + kc < D.cols) st[kc] = __fmaf_rn(lv[u], rv[u][kc], st[kc]);
             }
         }
     }
@@ -425,7 +459,7 @@ __global__ void __launch_bounds__(kBlock) k_rate_dwo(Dims D, int t0, const float
                 if (bb + u >= b1) break;
 #pragma unroll
                 for (int o = 0; o < kMaxOutputs; ++o)
-                    if (o < D.O) st[o] += __ldg(gt + (long long)(bb + u) * D.O + o) * rv[u];
+                    if (o < D.O) st[o] = __fmaf_rn(__ldg(gt + (long long)(bb + u) * D.O + o), rv[u], st[o]);
             }
         }
     }
