@@ -221,6 +221,225 @@ __global__ void __launch_bounds__(kBlock) k_rate_step(
     }
 }
 
+// Many timesteps of one batch element on one 16 x 16 tile in one launch.
+// A layer's own state is pointwise in time and layer l at step t reads layer
+// l-1 at step t-1 within +-h, so the tile of the last layer for any number
+// of steps needs layer l over the tile plus (L-1-l) h on each side and
+// nothing else: the CTA keeps v and r of those regions (and the stencil
+// weights of layers >= 1 over them) in shared memory and advances them step
+// by step with no global exchange.  Halo neurons are computed exactly as
+// their owners compute them (same inputs, same operations), so each CTA's
+// tile neurons equal those of any other split -- and the backward pass's
+// recompute from a checkpoint reproduces the forward states bit for bit.
+//   mode 0 (forward): steps 1..T from v = 0; writes the checkpoints
+//     (t % k == 0, t < T) and the per-tile readout partials ypart.
+//   mode 1 (recompute): nt steps from the checkpointed v at step c; writes
+//     the segment's r (steps c..c+nt), drives d and v at step c.
+// The input of the next step is fetched with cp.async during the current one.
+struct FusedRegions {
+    int L, H;
+    __device__ __host__ int side(int l) const { return kTileSide + 2 * (L - 1 - l) * H; }
+    __device__ __host__ int off(int l) const {      // float offset of region l
+        int o = 0;
+        for (int m = 0; m < l; ++m) o += side(m) * side(m);
+        return o;
+    }
+    __device__ __host__ int total() const { return off(L); }
+    __device__ __host__ int woff(int l, int K) const {   // weights of layers 1..l-1
+        int o = 0;
+        for (int m = 1; m < l; ++m) o += K * side(m) * side(m);
+        return o;
+    }
+};
+
+__host__ __device__ inline size_t fused_smem_floats(int L, int F) {
+    const FusedRegions R{L, F / 2};
+    const int s0 = R.side(0);
+    // v, r (two buffers), input (two buffers), weights, readout weights of
+    // the tile, readout partials, and two per-position tables (32-bit ints)
+    return (size_t)3 * R.total() + 2 * s0 * s0 + R.woff(L, F * F) + kMaxOutputs * kBlock +
+           2 * (kBlock / 32) * kMaxOutputs + 2 * R.total();
+}
+
+__device__ __forceinline__ void cp_async_f32_zfill(float* dst, const float* src, bool valid) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(
+                     (unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src), "r"(valid ? 4 : 0)
+                 : "memory");
+}
+
+constexpr int kOwnBit = 1 << 30;
+
+template <int F>
+__global__ void __launch_bounds__(kBlock) k_rate_fused(
+    Dims D, int mode, int c, int nt, const float* __restrict__ x, const float* __restrict__ wt,
+    const float* __restrict__ wo, const float* __restrict__ tau, const float* __restrict__ v0,
+    float* __restrict__ ckpt, float* __restrict__ ypart, float* __restrict__ seg_v,
+    float* __restrict__ seg_r, float* __restrict__ seg_d) {
+    constexpr int H = F / 2, K = F * F;
+    extern __shared__ float fs[];
+    const FusedRegions R{D.L, H};
+    const int tot = R.total(), s0 = R.side(0);
+    float* vs = fs;                                          // v, then r[2], then x[2]
+    float* rs = fs + tot;
+    float* xs = fs + 3 * tot;
+    float* ws = xs + 2 * s0 * s0;                            // stencil weights, layers >= 1
+    float* ows = ws + R.woff(D.L, K);                        // [O][256] readout weights
+    float* red = ows + kMaxOutputs * kBlock;                 // [2][8][16]
+    // per region position: its global index, with kOwnBit for tile neurons,
+    // or -1 outside the layer; and the offset of its stencil window in the
+    // previous layer's region
+    int* info = reinterpret_cast<int*>(red + 2 * (kBlock / 32) * kMaxOutputs);
+    int* sbase = info + tot;
+    const int tiles_x = (D.cols + kTileSide - 1) / kTileSide;
+    const int tile = blockIdx.x, b = blockIdx.y;
+    const int ty0 = (tile / tiles_x) * kTileSide, tx0 = (tile % tiles_x) * kTileSide;
+    const int tid = threadIdx.x;
+    const long long S = D.S;
+
+    // tables, initial state, weights
+    for (int l = 0, o = 0, op = 0, sp = 0, wofs = 0; l < D.L; ++l) {
+        const int sd = R.side(l), q = (D.L - 1 - l) * H;
+        for (int p = tid; p < sd * sd; p += kBlock) {
+            const int py = p / sd, px = p - py * sd;
+            const int gy = ty0 - q + py, gx = tx0 - q + px;
+            const bool in = gy >= 0 && gy < D.rows && gx >= 0 && gx < D.cols;
+            const int gi = in ? gy * D.cols + gx : -1;
+            const bool own = py >= q && py < q + kTileSide && px >= q && px < q + kTileSide;
+            info[o + p] = in ? (gi | (own ? kOwnBit : 0)) : -1;
+            sbase[o + p] = l >= 1 ? op + py * sp + px : 0;
+            const long long gl = ((long long)l * D.B + b) * D.N + gi;
+            const float v = (in && v0) ? v0[gl] : 0.0f;
+            const float r = in ? sigmoid(v) : 0.0f;
+            vs[o + p] = v;
+            rs[o + p] = r;
+            rs[tot + o + p] = 0.0f;
+            if (mode == 1 && in && own) {
+                seg_v[gl] = v;
+                seg_r[gl] = r;
+            }
+            if (l >= 1) {
+#pragma unroll
+                for (int k = 0; k < K; ++k)
+                    ws[wofs + k * sd * sd + p] =
+                        in ? __ldg(wt + ((long long)(l - 1) * K + k) * D.N + gi) : 0.0f;
+            }
+            if (l == D.L - 1) {                               // the tile itself: p = tid
+                for (int k = 0; k < kMaxOutputs; ++k)
+                    ows[k * kBlock + p] = (in && k < D.O) ? __ldg(wo + (long long)k * D.N + gi) : 0.0f;
+            }
+        }
+        op = o;
+        sp = sd;
+        o += sd * sd;
+        if (l >= 1) wofs += K * sd * sd;
+    }
+    __syncthreads();
+    {
+        const float* xt = x + ((long long)c * D.B + b) * D.N;
+        for (int p = tid; p < s0 * s0; p += kBlock) {
+            const int code = info[p];
+            cp_async_f32_zfill(&xs[p], code >= 0 ? xt + (code & (kOwnBit - 1)) : xt, code >= 0);
+        }
+        asm volatile("cp.async.commit_group;\ncp.async.wait_all;\n" ::: "memory");
+    }
+    __syncthreads();
+
+    const int lane = tid & 31, warp = tid >> 5;
+    for (int tt = 1; tt <= nt; ++tt) {
+        const int t = c + tt, cur = (tt - 1) & 1;
+        const float* r_old = rs + cur * tot;
+        float* r_new = rs + (cur ^ 1) * tot;
+        const float* x_cur = xs + cur * s0 * s0;
+        if (tt < nt) {                                       // next step's input
+            const float* xt = x + ((long long)t * D.B + b) * D.N;
+            float* xn = xs + (cur ^ 1) * s0 * s0;
+            for (int p = tid; p < s0 * s0; p += kBlock) {
+                const int code = info[p];
+                cp_async_f32_zfill(&xn[p], code >= 0 ? xt + (code & (kOwnBit - 1)) : xt, code >= 0);
+            }
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+        }
+        const bool store_ckpt = mode == 0 && t % D.k == 0 && t < D.T;
+        float r_last = 0.0f;                                  // tile neuron of the last layer
+        for (int l = 0, o = 0, wofs = 0; l < D.L; ++l) {
+            const int sd = R.side(l), sd2 = sd * sd, sp = sd + 2 * H;
+            const float a = D.dt / __ldg(tau + l);
+            for (int p = tid; p < sd2; p += kBlock) {
+                const int code = info[o + p];
+                if (code < 0) continue;
+                float I;
+                if (l == 0) {
+                    I = x_cur[p];
+                } else {
+                    // one partial sum per kernel row, rows added in order
+                    const float* src = r_old + sbase[o + p];
+                    const float* wl = ws + wofs + p;
+                    float part[F];
+#pragma unroll
+                    for (int kr = 0; kr < F; ++kr) {
+                        part[kr] = 0.0f;
+#pragma unroll
+                        for (int kc = 0; kc < F; ++kc)
+                            part[kr] = __fmaf_rn(wl[(kr * F + kc) * sd2], src[kr * sp + kc], part[kr]);
+                    }
+                    I = 0.0f;
+#pragma unroll
+                    for (int kr = 0; kr < F; ++kr) I += part[kr];
+                }
+                const float vp = vs[o + p];
+                const float d = -vp + I;
+                const float vn = vp + a * d;
+                const float rn = sigmoid(vn);
+                vs[o + p] = vn;
+                r_new[o + p] = rn;
+                if (code & kOwnBit) {
+                    const long long gl = ((long long)l * D.B + b) * D.N + (code & (kOwnBit - 1));
+                    if (mode == 1) {
+                        seg_v[tt * S + gl] = vn;
+                        seg_r[tt * S + gl] = rn;
+                        seg_d[(tt - 1) * S + gl] = d;
+                    } else if (store_ckpt) {
+                        ckpt[(long long)(t / D.k) * S + gl] = vn;
+                    }
+                    if (l == D.L - 1) r_last = rn;
+                }
+            }
+            o += sd2;
+            if (l >= 1) wofs += K * sd2;
+        }
+        if (mode == 0) {
+            // readout of the tile's last-layer neurons (thread tid owns
+            // position tid of the 16 x 16 region): butterfly transpose
+            // reduction per warp, warps added in order
+            float cv[kMaxOutputs];
+#pragma unroll
+            for (int q = 0; q < kMaxOutputs; ++q) cv[q] = ows[q * kBlock + tid] * r_last;
+#pragma unroll
+            for (int half = kMaxOutputs / 2; half >= 1; half /= 2) {
+                const bool up = lane & (2 * half);
+#pragma unroll
+                for (int j = 0; j < half; ++j) {
+                    const float send = up ? cv[j] : cv[j + half];
+                    const float keep = up ? cv[j + half] : cv[j];
+                    cv[j] = keep + __shfl_xor_sync(0xFFFFFFFFu, send, 2 * half);
+                }
+            }
+            const float y_lane = cv[0] + __shfl_xor_sync(0xFFFFFFFFu, cv[0], 1);
+            float* rd = red + cur * (kBlock / 32) * kMaxOutputs;
+            if ((lane & 1) == 0 && (lane >> 1) < D.O) rd[warp * kMaxOutputs + (lane >> 1)] = y_lane;
+        }
+        asm volatile("cp.async.wait_all;\n" ::: "memory");
+        __syncthreads();
+        if (mode == 0 && tid < D.O) {
+            const float* rd = red + cur * (kBlock / 32) * kMaxOutputs;
+            float y = 0.0f;
+            for (int w = 0; w < kBlock / 32; ++w) y += rd[w * kMaxOutputs + tid];
+            ypart[(((long long)(t - 1) * D.B + b) * D.nchunk + tile) * D.O + tid] = y;
+        }
+    }
+}
+
 // r = sigmoid(v) for a whole state (checkpoint reload / initial state).
 __global__ void k_rate_rates(long long S, const float* __restrict__ v, float* __restrict__ r) {
     long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -643,23 +862,54 @@ void lambda_step(const Dims& D, const float* wo, const float* tau, const Work& W
     SG_LAUNCH_CHECK();
 }
 
+// Shared memory of the multi-step kernel, or 0 where it does not fit (the
+// per-step kernels run instead, for the forward pass and the recompute alike).
+size_t fused_bytes(const Dims& D) {
+    static int optin = -1;
+    if (optin < 0) {
+        int dev = 0;
+        SG_CUDA(cudaGetDevice(&dev));
+        SG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    }
+    const size_t bytes = fused_smem_floats(D.L, D.field) * sizeof(float);
+    return bytes <= (size_t)optin ? bytes : 0;
+}
+
+void fused(const Dims& D, int mode, int c, int nt, const float* x, const float* wo,
+           const float* tau, const Work& W, const float* v0, float* ckpt, float* ypart,
+           float* seg_v, float* seg_r, float* seg_d, cudaStream_t st) {
+    const size_t bytes = fused_bytes(D);
+    const dim3 grid((unsigned)D.nchunk, (unsigned)D.B);
+    SG_RATE_FIELD(D.field, ({
+        SG_CUDA(cudaFuncSetAttribute(k_rate_fused<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)bytes));
+        k_rate_fused<F><<<grid, kBlock, bytes, st>>>(D, mode, c, nt, x, W.wt, wo, tau, v0, ckpt,
+                                                     ypart, seg_v, seg_r, seg_d);
+    }));
+    SG_LAUNCH_CHECK();
+}
+
 void forward(const Dims& D, const float* x, const float* w, const float* wo, const float* tau,
              const float* target, float* y_out, float* loss, void* ws, cudaStream_t st) {
     Work W = carve(D, ws);
     transpose_weights(D, w, W, st);
-    float* v[2] = {W.seg_v, W.seg_v + D.S};
-    float* r[2] = {W.seg_r, W.seg_r + D.S};
-    SG_CUDA(cudaMemsetAsync(v[0], 0, D.S * sizeof(float), st));
-    k_rate_rates<<<grid_of(D.S), 256, 0, st>>>(D.S, v[0], r[0]);
-    SG_LAUNCH_CHECK();
     SG_CUDA(cudaMemsetAsync(W.ckpt, 0, D.S * sizeof(float), st));
-    for (int t = 1; t <= D.T; ++t) {
-        const int p = (t - 1) & 1, q = t & 1;
-        step(D, x + (long long)(t - 1) * D.B * D.N, wo, tau, W, v[p], r[p], v[q], r[q], nullptr,
-             W.ypart + (long long)(t - 1) * D.B * D.nchunk * D.O, st);
-        if (t % D.k == 0 && t < D.T)
-            SG_CUDA(cudaMemcpyAsync(W.ckpt + (long long)(t / D.k) * D.S, v[q],
-                                    D.S * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    if (fused_bytes(D)) {
+        fused(D, 0, 0, D.T, x, wo, tau, W, nullptr, W.ckpt, W.ypart, nullptr, nullptr, nullptr, st);
+    } else {
+        float* v[2] = {W.seg_v, W.seg_v + D.S};
+        float* r[2] = {W.seg_r, W.seg_r + D.S};
+        SG_CUDA(cudaMemsetAsync(v[0], 0, D.S * sizeof(float), st));
+        k_rate_rates<<<grid_of(D.S), 256, 0, st>>>(D.S, v[0], r[0]);
+        SG_LAUNCH_CHECK();
+        for (int t = 1; t <= D.T; ++t) {
+            const int p = (t - 1) & 1, q = t & 1;
+            step(D, x + (long long)(t - 1) * D.B * D.N, wo, tau, W, v[p], r[p], v[q], r[q], nullptr,
+                 W.ypart + (long long)(t - 1) * D.B * D.nchunk * D.O, st);
+            if (t % D.k == 0 && t < D.T)
+                SG_CUDA(cudaMemcpyAsync(W.ckpt + (long long)(t / D.k) * D.S, v[q],
+                                        D.S * sizeof(float), cudaMemcpyDeviceToDevice, st));
+        }
     }
     k_rate_finish<<<grid_of((long long)D.T * D.B), 256, 0, st>>>(D, W.ypart, target, W.y,
                                                                  W.loss_tb);
@@ -685,14 +935,19 @@ void backward(const Dims& D, const float* x, const float* w, const float* wo, co
     SG_CUDA(cudaMemsetAsync(W.carry, 0, D.S * sizeof(float), st));
     for (int seg = D.nseg - 1; seg >= 0; --seg) {
         const int c = seg * D.k, nt = std::min(D.k, D.T - c);
-        SG_CUDA(cudaMemcpyAsync(W.seg_v, W.ckpt + (long long)seg * D.S, D.S * sizeof(float),
-                                cudaMemcpyDeviceToDevice, st));
-        k_rate_rates<<<grid_of(D.S), 256, 0, st>>>(D.S, W.seg_v, W.seg_r);
-        SG_LAUNCH_CHECK();
-        for (int tt = 1; tt <= nt; ++tt)
-            step(D, x + (long long)(c + tt - 1) * D.B * D.N, wo, tau, W, W.seg_v + (tt - 1) * D.S,
-                 W.seg_r + (tt - 1) * D.S, W.seg_v + tt * D.S, W.seg_r + tt * D.S,
-                 W.seg_d + (tt - 1) * D.S, nullptr, st);
+        if (fused_bytes(D)) {
+            fused(D, 1, c, nt, x, wo, tau, W, W.ckpt + (long long)seg * D.S, nullptr, nullptr,
+                  W.seg_v, W.seg_r, W.seg_d, st);
+        } else {
+            SG_CUDA(cudaMemcpyAsync(W.seg_v, W.ckpt + (long long)seg * D.S, D.S * sizeof(float),
+                                    cudaMemcpyDeviceToDevice, st));
+            k_rate_rates<<<grid_of(D.S), 256, 0, st>>>(D.S, W.seg_v, W.seg_r);
+            SG_LAUNCH_CHECK();
+            for (int tt = 1; tt <= nt; ++tt)
+                step(D, x + (long long)(c + tt - 1) * D.B * D.N, wo, tau, W,
+                     W.seg_v + (tt - 1) * D.S, W.seg_r + (tt - 1) * D.S, W.seg_v + tt * D.S,
+                     W.seg_r + tt * D.S, W.seg_d + (tt - 1) * D.S, nullptr, st);
+        }
         for (int tt = nt; tt >= 1; --tt) {
             const int t = c + tt;
             const float* lam_next = tt == nt ? W.carry : W.seg_lam + (long long)tt * D.S;
