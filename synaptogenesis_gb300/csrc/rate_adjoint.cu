@@ -252,13 +252,14 @@ struct FusedRegions {
     }
 };
 
-__host__ __device__ inline size_t fused_smem_floats(int L, int F) {
+template <int F>
+__host__ __device__ inline size_t fused_smem_floats(int L) {
     const FusedRegions R{L, F / 2};
     const int s0 = R.side(0);
     // v, r (two buffers), input (two buffers), weights, readout weights of
-    // the tile, readout partials, and two per-position tables (32-bit ints)
-    return (size_t)3 * R.total() + 2 * s0 * s0 + R.woff(L, F * F) + kMaxOutputs * kBlock +
-           2 * (kBlock / 32) * kMaxOutputs + 2 * R.total();
+    // the tile, readout partials, a_l, and two per-position tables (32-bit ints)
+    return (size_t)3 * R.total() + 2 * s0 * s0 + R.woff(L, F * F) +
+           kMaxOutputs * kBlock + 2 * (kBlock / 32) * kMaxOutputs + L + 2 * R.total();
 }
 
 __device__ __forceinline__ void cp_async_f32_zfill(float* dst, const float* src, bool valid) {
@@ -280,16 +281,19 @@ __global__ void __launch_bounds__(kBlock) k_rate_fused(
     extern __shared__ float fs[];
     const FusedRegions R{D.L, H};
     const int tot = R.total(), s0 = R.side(0);
-    float* vs = fs;                                          // v, then r[2], then x[2]
-    float* rs = fs + tot;
-    float* xs = fs + 3 * tot;
-    float* ws = xs + 2 * s0 * s0;                            // stencil weights, layers >= 1
-    float* ows = ws + R.woff(D.L, K);                        // [O][256] readout weights
+    // weights first, then v, r[2], x[2], readout weights,
+    // readout partials, a_l, tables
+    float* ws = fs;                                          // [k][position], layers >= 1
+    float* vs = ws + R.woff(D.L, K);
+    float* rs = vs + tot;
+    float* xs = vs + 3 * tot;
+    float* ows = xs + 2 * s0 * s0;                           // [O][256] readout weights
     float* red = ows + kMaxOutputs * kBlock;                 // [2][8][16]
+    float* as = red + 2 * (kBlock / 32) * kMaxOutputs;       // dt / tau_l
     // per region position: its global index, with kOwnBit for tile neurons,
     // or -1 outside the layer; and the offset of its stencil window in the
     // previous layer's region
-    int* info = reinterpret_cast<int*>(red + 2 * (kBlock / 32) * kMaxOutputs);
+    int* info = reinterpret_cast<int*>(as + D.L);
     int* sbase = info + tot;
     const int tiles_x = (D.cols + kTileSide - 1) / kTileSide;
     const int tile = blockIdx.x, b = blockIdx.y;
@@ -334,6 +338,7 @@ __global__ void __launch_bounds__(kBlock) k_rate_fused(
         o += sd * sd;
         if (l >= 1) wofs += K * sd * sd;
     }
+    for (int l = tid; l < D.L; l += kBlock) as[l] = D.dt / __ldg(tau + l);
     __syncthreads();
     {
         const float* xt = x + ((long long)c * D.B + b) * D.N;
@@ -364,7 +369,7 @@ __global__ void __launch_bounds__(kBlock) k_rate_fused(
         float r_last = 0.0f;                                  // tile neuron of the last layer
         for (int l = 0, o = 0, wofs = 0; l < D.L; ++l) {
             const int sd = R.side(l), sd2 = sd * sd, sp = sd + 2 * H;
-            const float a = D.dt / __ldg(tau + l);
+            const float a = as[l];
             for (int p = tid; p < sd2; p += kBlock) {
                 const int code = info[o + p];
                 if (code < 0) continue;
@@ -871,7 +876,9 @@ size_t fused_bytes(const Dims& D) {
         SG_CUDA(cudaGetDevice(&dev));
         SG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     }
-    const size_t bytes = fused_smem_floats(D.L, D.field) * sizeof(float);
+    size_t floats = 0;
+    SG_RATE_FIELD(D.field, (floats = fused_smem_floats<F>(D.L)));
+    const size_t bytes = floats * sizeof(float);
     return bytes <= (size_t)optin ? bytes : 0;
 }
 
