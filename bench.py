@@ -177,7 +177,7 @@ def rate_workload():
                 "steps of N(0,1) input, MSE to U(0,1) targets (seed 4), checkpoint every 10",
         "unit": "sequence-timesteps/s",
         "dtype": "f32",
-        "kernel": "k_rate_step (forward pass time per timestep: one launch per timestep, readout fused)",
+        "kernel": "k_rate_fused (forward pass: one launch for all timesteps; time per timestep)",
         "cpu_seconds": 12.0,
         "rate": True,
     }
@@ -741,13 +741,13 @@ def rate_line(args, world, r, wl, cb):
     c = RATE_CFG
     per_step = c["batch"] * c["steps"]
     achieved = r["fwd_bytes_per_timestep"] / (r["fwd_us_per_timestep"] * 1e-6) / 1e9
-    # kernel launches per forward + adjoint: forward = weight transpose,
-    # initial rates, one step per timestep (readout fused), outputs, loss;
-    # backward = weight transpose, dloss/dy, per timestep a recomputed step and
-    # an adjoint step, per segment the rates, dW and its accumulation, dR and
-    # its accumulation, dtau partials, and the dtau total
+    # kernel launches per forward + adjoint: forward = weight transpose, the
+    # multi-step forward kernel, outputs, loss; backward = weight transpose,
+    # dloss/dy, per segment the multi-step recompute, dW and its accumulation,
+    # dR and its accumulation, dtau partials, per timestep an adjoint step,
+    # and the dtau total
     nseg = -(-c["steps"] // c["checkpoint"])
-    launches = (c["steps"] + 4) + (2 * c["steps"] + 6 * nseg + 3)
+    launches = 4 + (2 + 6 * nseg + c["steps"] + 1)
     return {
         "metric": "sequence-timesteps/s (rate forward + adjoint)",
         "value": r["units"] / r["dev_s"], "unit": wl["unit"], "n_gpus": world,
