@@ -573,74 +573,60 @@ __global__ void __launch_bounds__(kBlock) k_rate_lambda(
     }
 }
 
-// dW, one timestep of a segment per CTA row: grid ((L-1) * field * tiles of
-// 32 destinations j, timesteps).  A CTA covers 32 destinations j of one
-// (layer >= 1, kernel row kr) for all of the row's kernel columns; its 8
-// thread groups take 8 batch elements each, loading a group's lambdas and
-// source rates before summing them.  The groups' sums are added in group
-// order and written as the step's total to part[tt][l-1][j][k];
-// k_rate_dw_acc then adds the steps, latest first, into dW: a fixed order
-// that does not depend on where the segments start.
+// The dR kernel below takes the batch in kGroups groups of thread warps,
+// kUnroll elements' loads in flight at a time.
 constexpr int kGroups = 8;
 constexpr int kUnroll = 8;
 
+// dW, staged: grid (tiles, layers >= 1, timesteps of the segment).  Thread
+// j of a 16 x 16 tile of layer l holds its F x F sums over the batch, in
+// batch order, of lambda_l[t][j] times the source rates of t-1 in its window;
+// per batch element the CTA stages the window (tile plus halo, zero outside
+// the layer) in shared memory, double-buffered with the next element fetched
+// into registers.  The step's totals go to part[tt][l-1][j][k], and
+// k_rate_dw_acc adds the steps latest first into dW: a fixed order that does
+// not depend on where the segments start.
 template <int F>
-__global__ void __launch_bounds__(kBlock) k_rate_dw(Dims D, const float* __restrict__ seg_lam,
-                                                   const float* __restrict__ seg_r,
-                                                   float* __restrict__ part) {
-    constexpr int H = F / 2, K = F * F;
-    __shared__ float gsum[kGroups][32][F + 1];
-    const int jl = threadIdx.x & 31, g = threadIdx.x >> 5;
-    const int tiles = (D.N + 31) / 32;
-    const int tile = blockIdx.x % tiles, lk = blockIdx.x / tiles;
-    const int kr = lk % F, l = 1 + lk / F, tt = blockIdx.y;
-    const int j = tile * 32 + jl;
-    const bool ok = j < D.N;
-    const int jr = ok ? j / D.cols : 0, jc = ok ? j - jr * D.cols : 0;
-    const int sr = jr - H + kr, sc0 = jc - H;
-    const bool row_ok = ok && sr >= 0 && sr < D.rows;
-    const int bpg = (D.B + kGroups - 1) / kGroups;
-    const int b0 = g * bpg, b1 = min(D.B, b0 + bpg);
-    // lambda of step t = c + tt + 1 and the source rates of step t - 1
-    float st[F];
+__global__ void __launch_bounds__(kBlock) k_rate_dw_staged(Dims D, const float* __restrict__ seg_lam,
+                                                          const float* __restrict__ seg_r,
+                                                          float* __restrict__ part) {
+    using W = Halo<F>;
+    constexpr int K = F * F;
+    __shared__ float win[2][W::SIDE][W::PITCH];
+    const int tiles_x = (D.cols + kTileSide - 1) / kTileSide;
+    const int tile = blockIdx.x, l = 1 + blockIdx.y, tt = blockIdx.z;
+    const int ty0 = (tile / tiles_x) * kTileSide, tx0 = (tile % tiles_x) * kTileSide;
+    const int tr = threadIdx.x / kTileSide, tc = threadIdx.x % kTileSide;
+    const int jr = ty0 + tr, jc = tx0 + tc;
+    const bool ok = jr < D.rows && jc < D.cols;
+    const int j = jr * D.cols + jc;
+    const float* lam = seg_lam + (long long)tt * D.S + (long long)l * D.B * D.N;
+    const float* rp = seg_r + (long long)tt * D.S + (long long)(l - 1) * D.B * D.N;
+    const W halo(D, ty0, tx0);
+    float acc[K];
 #pragma unroll
-    for (int kc = 0; kc < F; ++kc) st[kc] = 0.0f;
-    if (row_ok) {
-        const float* lam = seg_lam + (long long)tt * D.S + (long long)l * D.B * D.N + j;
-        const float* rr = seg_r + (long long)tt * D.S + (long long)(l - 1) * D.B * D.N +
-                          sr * D.cols + sc0;
-        for (int bb = b0; bb < b1; bb += kUnroll) {
-            float lv[kUnroll], rv[kUnroll][F];
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u) {
-                const bool in = bb + u < b1;
-                lv[u] = in ? lam[(long long)(bb + u) * D.N] : 0.0f;
-#pragma unroll
-                for (int kc = 0; kc < F; ++kc)
-                    rv[u][kc] = (in && sc0 + kc >= 0 && sc0 + kc < D.cols)
-                                    ? rr[(long long)(bb + u) * D.N + kc] : 0.0f;
-            }
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u) {
-                if (bb + u >= b1) break;
-#pragma unroll
-                for (int kc = 0; kc < F; ++kc)
-                    if (sc0 + kc >= 0 && sc0 + kc < D.cols) st[kc] = __fmaf_rn(lv[u], rv[u][kc], st[kc]);
-            }
+    for (int k = 0; k < K; ++k) acc[k] = 0.0f;
+    float pre[W::PER];
+    halo.fetch(rp, 1.0f, pre);
+    float lv = ok ? lam[j] : 0.0f;
+    for (int b = 0, buf = 0; b < D.B; ++b, buf ^= 1) {
+        halo.stage(pre, &win[buf][0][0]);
+        const float lcur = lv;
+        __syncthreads();
+        if (b + 1 < D.B) {
+            halo.fetch(rp + (long long)(b + 1) * D.N, 1.0f, pre);
+            lv = ok ? lam[(long long)(b + 1) * D.N + j] : 0.0f;
         }
-    }
 #pragma unroll
-    for (int kc = 0; kc < F; ++kc) gsum[g][jl][kc] = st[kc];
-    __syncthreads();
-    if (g == 0 && ok) {
-        float* out = part + (((long long)tt * (D.L - 1) + (l - 1)) * D.N + j) * K + kr * F;
+        for (int kr = 0; kr < F; ++kr)
 #pragma unroll
-        for (int kc = 0; kc < F; ++kc) {
-            float tot = 0.0f;
-            for (int q = 0; q < kGroups; ++q) tot += gsum[q][jl][kc];
-            out[kc] = tot;
-        }
+            for (int kc = 0; kc < F; ++kc)
+                acc[kr * F + kc] = __fmaf_rn(lcur, win[buf][tr + kr][tc + kc], acc[kr * F + kc]);
     }
+    if (!ok) return;
+    float* out = part + (((long long)tt * (D.L - 1) + (l - 1)) * D.N + j) * K;
+#pragma unroll
+    for (int k = 0; k < K; ++k) out[k] = acc[k];
 }
 
 // dW[l-1][j][k] += a_l * part[tt] for the segment's steps, latest first.
@@ -966,9 +952,9 @@ void backward(const Dims& D, const float* x, const float* w, const float* wo, co
         SG_CUDA(cudaMemcpyAsync(W.carry, W.seg_lam, D.S * sizeof(float),
                                 cudaMemcpyDeviceToDevice, st));
         if (D.L > 1) {
-            const dim3 grid((unsigned)((D.L - 1) * D.field * ((D.N + 31) / 32)), (unsigned)nt);
-            SG_RATE_FIELD(D.field, (k_rate_dw<F><<<grid, kBlock, 0, st>>>(D, W.seg_lam, W.seg_r,
-                                                                         W.dw_part)));
+            const dim3 grid((unsigned)D.nchunk, (unsigned)(D.L - 1), (unsigned)nt);
+            SG_RATE_FIELD(D.field, (k_rate_dw_staged<F><<<grid, kBlock, 0, st>>>(
+                                       D, W.seg_lam, W.seg_r, W.dw_part)));
             SG_LAUNCH_CHECK();
             k_rate_dw_acc<<<grid_of((long long)(D.L - 1) * D.N * D.K), 256, 0, st>>>(
                 D, nt, tau, W.dw_part, dw);
