@@ -76,6 +76,8 @@ DGeom make_geom(const Connection& c) {
 State::State(Network* net) : network(net) { build(); }
 
 State::~State() {
+    for (void* p : registered_) cudaHostUnregister(p);
+    if (stage_) cudaFree(stage_);
     if (arena_) cudaFree(arena_);
 }
 
@@ -142,21 +144,29 @@ void State::allocate_device() {
     arena_bytes_ = std::max<size_t>(off, 256);
     SG_CUDA(cudaMalloc(&arena_, arena_bytes_));
     SG_CUDA(cudaMemset(arena_, 0, arena_bytes_));
+    // staging for the arrays whose device layout differs from the host's
+    size_t stage = 0;
+    for (auto& a : arrays_) {
+        if (a->scratch || a->dev_count == 0) continue;
+        if (a->layout == LAYOUT_BANDED) stage = std::max(stage, a->count);
+        else if (a->layout == LAYOUT_MATRIX && a->rows > 1 && a->cols > 1)
+            stage = std::max(stage, a->count);
+    }
+    if (stage) SG_CUDA(cudaMalloc(&stage_, stage * sizeof(uint32_t)));
+    // page-lock the host mirrors in place, so that the copies are direct DMA;
+    // where the system refuses, copies go through the driver's staging
+    for (auto& a : arrays_) {
+        if (a->scratch || a->host.empty()) continue;
+        if (cudaHostRegister(a->host.data(), a->host.size() * sizeof(uint32_t),
+                             cudaHostRegisterDefault) == cudaSuccess)
+            registered_.push_back(a->host.data());
+        else
+            cudaGetLastError();
+    }
     // the engine's streams are non-blocking: nothing orders them after this
     // legacy-stream memset, so it completes before any upload or kernel
     SG_CUDA(cudaDeviceSynchronize());
     for (auto& a : arrays_) a->dev = static_cast<char*>(arena_) + a->dev_offset;
-}
-
-// Blocked transpose of a [rows][cols] matrix of 32-bit words.
-static void transpose(const uint32_t* in, uint32_t* out, int rows, int cols) {
-    const int B = 64;
-    for (int r0 = 0; r0 < rows; r0 += B)
-        for (int c0 = 0; c0 < cols; c0 += B) {
-            int r1 = std::min(rows, r0 + B), c1 = std::min(cols, c0 + B);
-            for (int r = r0; r < r1; ++r)
-                for (int c = c0; c < c1; ++c) out[(size_t)c * rows + r] = in[(size_t)r * cols + c];
-        }
 }
 
 static bool needs_transpose(const Array& a) {
@@ -173,43 +183,27 @@ size_t device_index(const Array& a, size_t i) {
     return i;
 }
 
-// host [rows][cols] -> device bands (padding stays zero) and back.
-static void to_bands(const uint32_t* in, uint32_t* out, int rows, int cols) {
-    for (int r = 0; r < rows; ++r) {
-        uint32_t* o = out + banded_index(r, 0, cols);
-        const uint32_t* ir = in + (size_t)r * cols;
-        for (int c = 0; c < cols; ++c) o[(size_t)c * kBand] = ir[c];
-    }
-}
-
-static void from_bands(const uint32_t* in, uint32_t* out, int rows, int cols) {
-    for (int r = 0; r < rows; ++r) {
-        const uint32_t* i = in + banded_index(r, 0, cols);
-        uint32_t* orow = out + (size_t)r * cols;
-        for (int c = 0; c < cols; ++c) orow[c] = i[(size_t)c * kBand];
-    }
-}
-
 void State::to_device(cudaStream_t stream) {
     if (!arena_) allocate_device();
     if (!on_host_) return;
+    // Everything on the engine's stream (a pageable cudaMemcpy may return
+    // before its DMA lands and would not be ordered with that stream's
+    // kernels).  Arrays with another device layout go through the staging
+    // buffer and a conversion kernel; the stream orders each conversion
+    // before the next copy into the buffer.
     for (auto& a : arrays_) {
         if (a->dev_count == 0 || a->scratch) continue;
         const uint32_t* src = a->host.data();
-        size_t n = std::min(a->dev_count, a->count);
         if (a->layout == LAYOUT_BANDED) {
-            scratch_.assign(a->dev_count, 0u);
-            to_bands(a->host.data(), scratch_.data(), a->rows, a->cols);
-            src = scratch_.data();
-            n = a->dev_count;
+            SG_CUDA(cudaMemcpyAsync(stage_, src, a->count * 4, cudaMemcpyHostToDevice, stream));
+            launch_to_bands(stage_, a->du(), a->rows, a->cols, a->dev_count, stream);
         } else if (needs_transpose(*a)) {
-            scratch_.resize(a->count);
-            transpose(a->host.data(), scratch_.data(), a->rows, a->cols);
-            src = scratch_.data();
+            SG_CUDA(cudaMemcpyAsync(stage_, src, a->count * 4, cudaMemcpyHostToDevice, stream));
+            launch_transpose(stage_, a->du(), a->rows, a->cols, stream);
+        } else {
+            const size_t n = std::min(a->dev_count, a->count);
+            SG_CUDA(cudaMemcpyAsync(a->dev, src, n * 4, cudaMemcpyHostToDevice, stream));
         }
-        // on the engine's stream: a pageable cudaMemcpy may return before its
-        // DMA lands and would not be ordered with that stream's kernels
-        SG_CUDA(cudaMemcpyAsync(a->dev, src, n * 4, cudaMemcpyHostToDevice, stream));
     }
     for (auto& cp : network->connections)
         find_model(cp->to->model)->prepare_device(*this, *conns[cp->index], stream);
@@ -223,20 +217,21 @@ void State::to_host(cudaStream_t stream) {
     check_iz_cols_errors();
     for (auto& a : arrays_) {
         if (a->dev_count == 0 || a->scratch) continue;
-        size_t n = std::min(a->dev_count, a->count);
+        const size_t n = std::min(a->dev_count, a->count);
         if (a->layout == LAYOUT_BANDED) {
-            scratch_.resize(a->dev_count);
-            SG_CUDA(cudaMemcpy(scratch_.data(), a->dev, a->dev_count * 4, cudaMemcpyDeviceToHost));
-            from_bands(scratch_.data(), a->host.data(), a->rows, a->cols);
+            launch_from_bands(a->du(), stage_, a->rows, a->cols, a->dev_count, stream);
+            SG_CUDA(cudaMemcpyAsync(a->host.data(), stage_, a->count * 4, cudaMemcpyDeviceToHost,
+                                    stream));
         } else if (needs_transpose(*a)) {
-            scratch_.resize(a->count);
-            SG_CUDA(cudaMemcpy(scratch_.data(), a->dev, n * 4, cudaMemcpyDeviceToHost));
             // device [cols][rows] -> host [rows][cols]
-            transpose(scratch_.data(), a->host.data(), a->cols, a->rows);
+            launch_transpose(a->du(), stage_, a->cols, a->rows, stream);
+            SG_CUDA(cudaMemcpyAsync(a->host.data(), stage_, a->count * 4, cudaMemcpyDeviceToHost,
+                                    stream));
         } else {
-            SG_CUDA(cudaMemcpy(a->host.data(), a->dev, n * 4, cudaMemcpyDeviceToHost));
+            SG_CUDA(cudaMemcpyAsync(a->host.data(), a->dev, n * 4, cudaMemcpyDeviceToHost, stream));
         }
     }
+    SG_CUDA(cudaStreamSynchronize(stream));
     on_host_ = true;
 }
 

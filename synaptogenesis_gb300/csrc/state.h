@@ -129,9 +129,20 @@ class State {
     std::vector<std::unique_ptr<Array>> arrays_;
     void* arena_ = nullptr;
     size_t arena_bytes_ = 0;
+    // device buffer for the layout conversions of uploads and downloads
+    uint32_t* stage_ = nullptr;
+    // host arrays registered with CUDA (page-locked in place) for the copies
+    std::vector<void*> registered_;
     bool on_host_ = true;
-    std::vector<uint32_t> scratch_;
 };
+
+// Layout conversions on the device (csrc/layout.cu): host [rows][cols] to and
+// from the banded device layout, and a [rows][cols] -> [cols][rows] transpose.
+void launch_to_bands(const uint32_t* in, uint32_t* out, int rows, int cols, size_t dev_count,
+                     cudaStream_t s);
+void launch_from_bands(const uint32_t* in, uint32_t* out, int rows, int cols, size_t dev_count,
+                       cudaStream_t s);
+void launch_transpose(const uint32_t* in, uint32_t* out, int rows, int cols, cudaStream_t s);
 
 DGeom make_geom(const Connection& c);
 
