@@ -264,12 +264,30 @@ void Engine::enqueue_step(bool last) {
             });
         }
     }
-    // 3. neuron updates
-    for (auto& lp : net_->layers) {
-        const Model* m = find_model(lp->model);
-        timed(std::string(lp->model) + ".update", 1, [&] {
-            m->update(*state_, *state_->layer_state(lp.get()), ctx);
-        });
+    // 3. neuron updates: the layers of each model together where the model
+    // can (a layer's update touches only its own arrays, so the order of
+    // updates does not matter)
+    {
+        std::vector<std::pair<const Model*, std::vector<LayerState*>>> groups;
+        for (auto& lp : net_->layers) {
+            const Model* m = find_model(lp->model);
+            auto it = std::find_if(groups.begin(), groups.end(),
+                                   [&](const auto& g) { return g.first == m; });
+            if (it == groups.end()) {
+                groups.push_back({m, {}});
+                it = groups.end() - 1;
+            }
+            it->second.push_back(state_->layer_state(lp.get()));
+        }
+        for (auto& g : groups) {
+            const std::string name = std::string(g.first->name()) + ".update";
+            bool done = false;
+            if (g.second.size() > 1)
+                timed(name, 1, [&] { done = g.first->update_group(*state_, g.second, ctx); });
+            if (!done)
+                for (LayerState* ls : g.second)
+                    timed(name, 1, [&] { g.first->update(*state_, *ls, ctx); });
+        }
     }
     // 4. plasticity
     if (learning_)

@@ -395,29 +395,49 @@ __global__ void k_iz_uniform_delay(int n_src, const int* __restrict__ counts,
     uniform[f] = d;
 }
 
-// Neuron update (izhikevich_attributes.cpp:102-213)
-__global__ void __launch_bounds__(256) k_iz_update(
-    int size, int history, const float* __restrict__ inputs, uint32_t* spikes, float* ampa,
-    float* nmda, float* gabaa, float* gabab, float* mult, float* dopamine, float* voltages,
-    float* recoveries, float* post_traces, int* tss, const float* __restrict__ as,
-    const float* __restrict__ bs, const float* __restrict__ cs, const float* __restrict__ ds) {
-    int nid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (nid >= size) return;
-    float ampa_c = ampa[nid], nmda_c = nmda[nid], gabaa_c = gabaa[nid], gabab_c = gabab[nid];
-    float mf = mult[nid];
-    float voltage = voltages[nid];
-    float recovery = recoveries[nid];
-    float base_current = inputs[nid];
-    iz_integrate(voltage, recovery, ampa_c, nmda_c, gabaa_c, gabab_c, mf, base_current, as[nid],
-                 bs[nid]);
-    ampa[nid] = 0.0f;
-    nmda[nid] = 0.0f;
-    gabaa[nid] = 0.0f;
-    gabab[nid] = 0.0f;
-    mult[nid] = 0.0f;
-    dopamine[nid] *= 0.95;
-    unsigned int spike = voltage >= 30.0;
+// Neuron update (izhikevich_attributes.cpp:102-213).  One launch updates the
+// Izhikevich layers of a step together (their neurons concatenated), so that
+// enough warps are in flight for the FP64 pipe; each layer's arrays are its
+// own.  The products with double constants (decays 0.95) and their float
+// results go through mul_fd_rn, bit-identical to the double arithmetic.
+struct IzLayerArgs {
+    int size, history;
+    const float* inputs;
+    uint32_t* spikes;
+    float *ampa, *nmda, *gabaa, *gabab, *mult, *dopamine, *voltages, *recoveries, *post_traces;
+    int* tss;
+    const float *as, *bs, *cs, *ds;
+};
+constexpr int kIzGroup = 8;
+struct IzUpdateGroup {
+    int n;
+    int start[kIzGroup + 1];           // first flattened neuron of each layer
+    IzLayerArgs L[kIzGroup];
+};
+
+__global__ void __launch_bounds__(256) k_iz_update(IzUpdateGroup G) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= G.start[G.n]) return;
+    int l = 0;
+    while (l + 1 < G.n && g >= G.start[l + 1]) ++l;
+    const IzLayerArgs& A = G.L[l];
+    const int nid = g - G.start[l], size = A.size, history = A.history;
+    float ampa_c = A.ampa[nid], nmda_c = A.nmda[nid], gabaa_c = A.gabaa[nid], gabab_c = A.gabab[nid];
+    float mf = A.mult[nid];
+    float voltage = A.voltages[nid];
+    float recovery = A.recoveries[nid];
+    float base_current = A.inputs[nid];
+    iz_integrate(voltage, recovery, ampa_c, nmda_c, gabaa_c, gabab_c, mf, base_current,
+                 __ldg(A.as + nid), __ldg(A.bs + nid));
+    A.ampa[nid] = 0.0f;
+    A.nmda[nid] = 0.0f;
+    A.gabaa[nid] = 0.0f;
+    A.gabab[nid] = 0.0f;
+    A.mult[nid] = 0.0f;
+    A.dopamine[nid] = mul_fd_rn(A.dopamine[nid], 0.95);            // dopamine *= 0.95
+    const unsigned int spike = voltage >= 30.0f;                     // 30.0 is a float value
     // SHIFT_BIT_OUTPUTS (state/attributes.h:321-333)
+    uint32_t* spikes = A.spikes;
     uint32_t curr = spikes[(size_t)size * (history - 1) + nid];
     for (int idx = history - 1; idx > 0; --idx) {
         uint32_t prev = spikes[(size_t)size * (idx - 1) + nid];
@@ -425,12 +445,13 @@ __global__ void __launch_bounds__(256) k_iz_update(
         curr = prev;
     }
     spikes[nid] = (curr >> 1) | (spike << 31);
-    bool prev_bit = curr >> 31;
-    post_traces[nid] = prev_bit ? 0.004 : (post_traces[nid] * 0.95);
-    int t = tss[nid] + 1;
-    tss[nid] = prev_bit ? 0 : (t < 32 ? t : 32);
-    voltages[nid] = spike ? cs[nid] : voltage;
-    recoveries[nid] = recovery + (spike * ds[nid]);
+    const bool prev_bit = curr >> 31;
+    // post_trace = prev_bit ? 0.004 : post_trace * 0.95, stored as float
+    A.post_traces[nid] = prev_bit ? (float)0.004 : mul_fd_rn(A.post_traces[nid], 0.95);
+    int t = A.tss[nid] + 1;
+    A.tss[nid] = prev_bit ? 0 : (t < 32 ? t : 32);
+    A.voltages[nid] = spike ? __ldg(A.cs + nid) : voltage;
+    A.recoveries[nid] = recovery + (spike * __ldg(A.ds + nid));
 }
 
 
@@ -723,15 +744,38 @@ class IzhikevichModel : public Model {
     }
 
     void update(State& st, LayerState& ls, const StepCtx& ctx) const override {
-        const Layer& l = *ls.layer;
-        k_iz_update<<<blocks_for(l.size, 256), 256, 0, ctx.stream>>>(
-            l.size, l.history(), ls.input->df(), ls.output->du(), ls.var("ampa")->df(),
-            ls.var("nmda")->df(), ls.var("gabaa")->df(), ls.var("gabab")->df(), ls.var("mult")->df(),
-            ls.var("dopamine")->df(), ls.var("voltage")->df(), ls.var("recovery")->df(),
-            ls.var("post trace")->df(), ls.var("time since spike")->di(), ls.var("a")->df(),
-            ls.var("b")->df(), ls.var("c")->df(), ls.var("d")->df());
-        SG_LAUNCH_CHECK();
-        ctx.count();
+        std::vector<LayerState*> one{&ls};
+        update_group(st, one, ctx);
+    }
+
+    // All of a step's Izhikevich layers in one launch (kIzGroup at a time).
+    bool update_group(State&, const std::vector<LayerState*>& group,
+                      const StepCtx& ctx) const override {
+        for (size_t first = 0; first < group.size(); first += kIzGroup) {
+            IzUpdateGroup G{};
+            G.n = (int)std::min<size_t>(kIzGroup, group.size() - first);
+            int total = 0;
+            for (int i = 0; i < G.n; ++i) {
+                LayerState& ls = *group[first + i];
+                const Layer& l = *ls.layer;
+                G.start[i] = total;
+                G.L[i] = IzLayerArgs{l.size, l.history(), ls.input->df(), ls.output->du(),
+                                     ls.var("ampa")->df(), ls.var("nmda")->df(),
+                                     ls.var("gabaa")->df(), ls.var("gabab")->df(),
+                                     ls.var("mult")->df(), ls.var("dopamine")->df(),
+                                     ls.var("voltage")->df(), ls.var("recovery")->df(),
+                                     ls.var("post trace")->df(), ls.var("time since spike")->di(),
+                                     ls.var("a")->df(), ls.var("b")->df(), ls.var("c")->df(),
+                                     ls.var("d")->df()};
+                total += l.size;
+            }
+            G.start[G.n] = total;
+            if (total == 0) continue;
+            k_iz_update<<<blocks_for(total, 256), 256, 0, ctx.stream>>>(G);
+            SG_LAUNCH_CHECK();
+            ctx.count();
+        }
+        return true;
     }
 
     bool learns(const Connection& c) const override { return true; }

@@ -54,6 +54,12 @@ class Model {
     }
     // Neuron update of one layer.
     virtual void update(State& st, LayerState& ls, const StepCtx& ctx) const = 0;
+    // Update several layers of this model at once (their updates touch only
+    // their own arrays); false: the engine updates them one by one.
+    virtual bool update_group(State& st, const std::vector<LayerState*>& group,
+                              const StepCtx& ctx) const {
+        return false;
+    }
     // Whether a plastic connection into this model has an updater.
     virtual bool learns(const Connection& c) const { return false; }
     // Whole-run path: can this layer advance n steps on its own -- nothing
