@@ -85,6 +85,18 @@ class Engine {
     State* state_;
     Props args_;
     cudaStream_t stream_;
+    // Learning runs on a second stream, overlapping the next step's input and
+    // activations: learn(c) at step t reads the destination's state of t and
+    // writes c's arrays, and the only later work touching either before the
+    // next learning is activate(c) at t+1 (the destination's update comes
+    // after it), so learn_ev_[c] orders the two.  Joined back before a graph
+    // capture ends, a run returns and the state is read.
+    cudaStream_t side_ = nullptr;
+    bool overlap_ = false, side_pending_ = false;
+    cudaEvent_t fork_ev_ = nullptr, join_ev_ = nullptr;
+    std::vector<cudaEvent_t> learn_ev_;
+    std::vector<char> learn_pending_;
+    void join_side();
     bool learning_ = true, suppress_ = false, verbose_ = false, use_graphs_ = true;
     bool profile_ = false;
     int env_rate_ = 1;

@@ -54,8 +54,9 @@ def run_oracle(case, steps=None):
     return out
 
 
-def run_library(case, syngen, steps=None):
-    """Runs ``case`` through the drop-in front-end ``syngen`` (either library)."""
+def run_library(case, syngen, steps=None, extra_args=None):
+    """Runs ``case`` through the drop-in front-end ``syngen`` (either library);
+    ``extra_args`` are added to the run arguments."""
     steps = case.steps if steps is None else steps
     sizes = case_sizes(case)
     injections = case.injections(sizes)
@@ -108,9 +109,10 @@ def run_library(case, syngen, steps=None):
         modules.append({"type": "callback", "layers": [
             {"structure": s, "layer": l, "output": True, "function": "golden_out", "id": i}
             for i, (s, l) in enumerate(case.record)]})
-    report = net.run(syngen.Environment({"modules": modules}),
-                     {"iterations": steps, "multithreaded": False, "worker threads": 0,
-                      "learning flag": case.learning})
+    args = {"iterations": steps, "multithreaded": False, "worker threads": 0,
+            "learning flag": case.learning}
+    args.update(extra_args or {})
+    report = net.run(syngen.Environment({"modules": modules}), args)
     assert report is not None and report.obj is not None, "run failed"
     out = {"rec/%s/%s" % k: np.stack(v) for k, v in rec.items()}
     for key in case.final:

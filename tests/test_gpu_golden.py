@@ -72,3 +72,16 @@ def test_plastic_short_term_fixed_points_match_oracle(syngen):
     want = run_oracle(case)
     problems = compare(got, want, nan_keys=float_like_keys(case))
     assert not problems, problems
+
+
+@pytest.mark.parametrize("overlap", [True, False])
+def test_overlapped_learning_matches_oracle(syngen, overlap):
+    """Learning on the engine's second stream, overlapping the next step's
+    activations (the default for large plastic networks), forced on and off
+    for the plastic case: bit-exact against the oracle either way."""
+    case = CASES["iz_plastic"]
+    steps = 2 * case.steps
+    got = run_library(case, syngen, steps=steps, extra_args={"overlap learning": overlap})
+    want = run_oracle(case, steps=steps)
+    problems = compare(got, want, nan_keys=float_like_keys(case))
+    assert not problems, problems
