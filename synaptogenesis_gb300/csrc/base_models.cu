@@ -151,11 +151,11 @@ __global__ void __launch_bounds__(256) k_gol_fused(DGeom g, int delay, const uin
 // Bit-sliced game_of_life step (same semantics as k_gol_fused) for a 3x3
 // kernel whose weights are all 0 or 1, stride 1, spacing 1, offset -1, and
 // rows of whole 32-cell segments.  With 0/1 weights the reference's fp32
-// sequential sum is an exact integer count, so counting bits is exact.
-// One thread owns one 32-cell segment of one row:
-//   * gathers bit (31 - delay) of its 32 history words (128-bit loads) into a
-//     plane word, for the rows above, itself and below, plus the boundary bits
-//     of the neighbouring segments (west / east shifts, wrap or zero);
+// sequential sum is an exact integer count, so counting bits is exact.  For
+// one 32-cell segment of one row, the step
+//   * gathers bit (31 - delay) of the 32 history words into a plane word, for
+//     the rows above, itself and below, plus the boundary bits of the
+//     neighbouring segments (west / east shifts, wrap or zero);
 //   * adds the planes selected by the weight mask with a bit-sliced counter
 //     (c3 c2 c1 c0 per cell);
 //   * evaluates survival / birth as plane logic against bit 0 (the state 32
@@ -171,210 +171,7 @@ __device__ __forceinline__ void csa_add(uint32_t& c0, uint32_t& c1, uint32_t& c2
     c3 ^= x;
 }
 
-__global__ void __launch_bounds__(256) k_gol_bits(int rows, int cols, int wrap, int delay,
-                                                  unsigned mask9, const uint32_t* __restrict__ cur,
-                                                  uint32_t* __restrict__ next,
-                                                  float* __restrict__ input_out, unsigned smask,
-                                                  unsigned bmask) {
-    const int segs = cols >> 5;
-    int gid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= rows * segs) return;
-    const int r = gid / segs, s = gid - r * segs;
-    uint32_t N[3], W[3], E[3];
-    uint4 own[8];
-    uint32_t O = 0;
-#pragma unroll
-    for (int dr = 0; dr < 3; ++dr) {
-        int rr = r + dr - 1;
-        bool valid = true;
-        if (wrap) rr = rr < 0 ? rr + rows : (rr >= rows ? rr - rows : rr);
-        else valid = rr >= 0 && rr < rows;
-        uint32_t P = 0, wb = 0, eb = 0;
-        if (valid) {
-            const uint32_t* row = cur + (size_t)rr * cols;
-            const uint4* p = reinterpret_cast<const uint4*>(row + (s << 5));
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                uint4 v = __ldg(p + q);
-                P |= (newest_bit(v.x, delay) << (4 * q)) | (newest_bit(v.y, delay) << (4 * q + 1)) |
-                     (newest_bit(v.z, delay) << (4 * q + 2)) | (newest_bit(v.w, delay) << (4 * q + 3));
-                if (dr == 1) {
-                    own[q] = v;
-                    O |= ((v.x & 1u) << (4 * q)) | ((v.y & 1u) << (4 * q + 1)) |
-                         ((v.z & 1u) << (4 * q + 2)) | ((v.w & 1u) << (4 * q + 3));
-                }
-            }
-            int cl = (s << 5) - 1, ce = (s << 5) + 32;
-            if (wrap) {
-                cl = cl < 0 ? cols - 1 : cl;
-                ce = ce >= cols ? 0 : ce;
-                wb = newest_bit(__ldg(row + cl), delay);
-                eb = newest_bit(__ldg(row + ce), delay);
-            } else {
-                wb = cl >= 0 ? newest_bit(__ldg(row + cl), delay) : 0u;
-                eb = ce < cols ? newest_bit(__ldg(row + ce), delay) : 0u;
-            }
-        }
-        N[dr] = P;
-        W[dr] = (P << 1) | wb;         // bit i: cell i-1 (kernel column 0)
-        E[dr] = (P >> 1) | (eb << 31); // bit i: cell i+1 (kernel column 2)
-    }
-    uint32_t c0 = 0, c1 = 0, c2 = 0, c3 = 0;
-#pragma unroll
-    for (int kr = 0; kr < 3; ++kr) {
-        if (mask9 & (1u << (kr * 3 + 0))) csa_add(c0, c1, c2, c3, W[kr]);
-        if (mask9 & (1u << (kr * 3 + 1))) csa_add(c0, c1, c2, c3, N[kr]);
-        if (mask9 & (1u << (kr * 3 + 2))) csa_add(c0, c1, c2, c3, E[kr]);
-    }
-    uint32_t S = 0, B = 0;
-    for (int v = 0; v < 10; ++v) {
-        if (!(((smask | bmask) >> v) & 1u)) continue;
-        uint32_t e = ~((c0 ^ ((v & 1) ? ~0u : 0u)) | (c1 ^ ((v & 2) ? ~0u : 0u)) |
-                       (c2 ^ ((v & 4) ? ~0u : 0u)) | (c3 ^ ((v & 8) ? ~0u : 0u)));
-        if ((smask >> v) & 1u) S |= e;
-        if ((bmask >> v) & 1u) B |= e;
-    }
-    const uint32_t L = (O & S) | (~O & B);
-    uint4* out = reinterpret_cast<uint4*>(next + (size_t)r * cols + (s << 5));
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        uint4 v = own[q];
-        v.x = (v.x >> 1) | (((L >> (4 * q)) & 1u) << 31);
-        v.y = (v.y >> 1) | (((L >> (4 * q + 1)) & 1u) << 31);
-        v.z = (v.z >> 1) | (((L >> (4 * q + 2)) & 1u) << 31);
-        v.w = (v.w >> 1) | (((L >> (4 * q + 3)) & 1u) << 31);
-        out[q] = v;
-    }
-    if (input_out) {
-        float4* in = reinterpret_cast<float4*>(input_out + (size_t)r * cols + (s << 5));
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            float f[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                int i = 4 * q + k;
-                f[k] = (float)(((c0 >> i) & 1u) | (((c1 >> i) & 1u) << 1) | (((c2 >> i) & 1u) << 2) |
-                               (((c3 >> i) & 1u) << 3));
-            }
-            in[q] = make_float4(f[0], f[1], f[2], f[3]);
-        }
-    }
-}
-
-// Coalesced variant of k_gol_bits.  A warp owns a strip of 32 segments
-// (1024 cells) and walks kGolRows rows down it, keeping a 3-row window of
-// planes.  Planes are gathered with one coalesced 128-byte load per segment
-// and __ballot_sync (lane t keeps the ballot of segment t); new words are
-// written back with coalesced stores, lane i writing cell i of each segment.
-constexpr int kGolRows = 4;
-
-struct GolPlanes { uint32_t n, w, e, o; };   // newest bit, west, east, bit 0
-
-__device__ __forceinline__ GolPlanes gol_gather(const uint32_t* __restrict__ cur, int rows, int cols,
-                                                int segs, int sx, int rr, int wrap, int delay,
-                                                bool bit0) {
-    const int lane = threadIdx.x & 31;
-    GolPlanes p{0u, 0u, 0u, 0u};
-    bool valid = true;
-    if (wrap) rr = rr < 0 ? rr + rows : (rr >= rows ? rr - rows : rr);
-    else valid = rr >= 0 && rr < rows;
-    if (!valid) return p;
-    const uint32_t* row = cur + (size_t)rr * cols;
-    const int seg = sx * 32 + lane;
-    uint32_t mine = 0, mine0 = 0;
-#pragma unroll 8
-    for (int t = 0; t < 32; ++t) {
-        int sg = sx * 32 + t;
-        uint32_t word = sg < segs ? __ldg(row + sg * 32 + lane) : 0u;
-        uint32_t b = __ballot_sync(0xffffffffu, newest_bit(word, delay));
-        if (lane == t) mine = b;
-        if (bit0) {
-            uint32_t b0 = __ballot_sync(0xffffffffu, word & 1u);
-            if (lane == t) mine0 = b0;
-        }
-    }
-    p.o = mine0;
-    uint32_t west = __shfl_up_sync(0xffffffffu, mine, 1) >> 31;
-    uint32_t east = __shfl_down_sync(0xffffffffu, mine, 1) & 1u;
-    if (seg < segs) {
-        if (lane == 0) {
-            int cl = seg * 32 - 1;
-            if (cl < 0) west = wrap ? newest_bit(__ldg(row + cols - 1), delay) : 0u;
-            else west = newest_bit(__ldg(row + cl), delay);
-        }
-        if (lane == 31 || seg + 1 >= segs) {
-            int ce = seg * 32 + 32;
-            if (ce >= cols) east = wrap ? newest_bit(__ldg(row), delay) : 0u;
-            else east = newest_bit(__ldg(row + ce), delay);
-        }
-    }
-    p.n = mine;
-    p.w = (mine << 1) | west;
-    p.e = (mine >> 1) | (east << 31);
-    return p;
-}
-
-__global__ void __launch_bounds__(256, 2) k_gol_bits_strip(int rows, int cols, int wrap, int delay,
-                                                        unsigned mask9, const uint32_t* __restrict__ cur,
-                                                        uint32_t* __restrict__ next,
-                                                        float* __restrict__ input_out, unsigned smask,
-                                                        unsigned bmask) {
-    const int segs = cols >> 5;
-    const int strips = (segs + 31) >> 5;
-    const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    const int sx = warp_id % strips;
-    const int r0 = (warp_id / strips) * kGolRows;
-    if (r0 >= rows) return;
-    const int r1 = min(rows, r0 + kGolRows);
-    GolPlanes up = gol_gather(cur, rows, cols, segs, sx, r0 - 1, wrap, delay, false);
-    GolPlanes mid = gol_gather(cur, rows, cols, segs, sx, r0, wrap, delay, true);
-    for (int r = r0; r < r1; ++r) {
-        GolPlanes down = gol_gather(cur, rows, cols, segs, sx, r + 1, wrap, delay, r + 1 < r1);
-        const uint32_t O = mid.o;
-        uint32_t c0 = 0, c1 = 0, c2 = 0, c3 = 0;
-        auto add_row = [&](const GolPlanes& p, int kr) {
-            if (mask9 & (1u << (kr * 3 + 0))) csa_add(c0, c1, c2, c3, p.w);
-            if (mask9 & (1u << (kr * 3 + 1))) csa_add(c0, c1, c2, c3, p.n);
-            if (mask9 & (1u << (kr * 3 + 2))) csa_add(c0, c1, c2, c3, p.e);
-        };
-        add_row(up, 0);
-        add_row(mid, 1);
-        add_row(down, 2);
-        uint32_t S = 0, B = 0;
-        for (int v = 0; v < 10; ++v) {
-            if (!(((smask | bmask) >> v) & 1u)) continue;
-            uint32_t e = ~((c0 ^ ((v & 1) ? ~0u : 0u)) | (c1 ^ ((v & 2) ? ~0u : 0u)) |
-                           (c2 ^ ((v & 4) ? ~0u : 0u)) | (c3 ^ ((v & 8) ? ~0u : 0u)));
-            if ((smask >> v) & 1u) S |= e;
-            if ((bmask >> v) & 1u) B |= e;
-        }
-        const uint32_t L = (O & S) | (~O & B);
-        const uint32_t* src_row = cur + (size_t)r * cols;
-        uint32_t* dst_row = next + (size_t)r * cols;
-#pragma unroll 4
-        for (int t = 0; t < 32; ++t) {
-            int sg = sx * 32 + t;
-            uint32_t Lt = __shfl_sync(0xffffffffu, L, t);
-            if (sg < segs) {
-                uint32_t word = __ldg(src_row + sg * 32 + lane);
-                dst_row[sg * 32 + lane] = (word >> 1) | (((Lt >> lane) & 1u) << 31);
-            }
-            if (input_out) {
-                uint32_t a0 = __shfl_sync(0xffffffffu, c0, t), a1 = __shfl_sync(0xffffffffu, c1, t);
-                uint32_t a2 = __shfl_sync(0xffffffffu, c2, t), a3 = __shfl_sync(0xffffffffu, c3, t);
-                if (sg < segs)
-                    input_out[(size_t)r * cols + sg * 32 + lane] =
-                        (float)(((a0 >> lane) & 1u) | (((a1 >> lane) & 1u) << 1) |
-                                (((a2 >> lane) & 1u) << 2) | (((a3 >> lane) & 1u) << 3));
-            }
-        }
-        up = mid;
-        mid = down;
-    }
-}
-
-// Shared-memory tiled variant of k_gol_bits.  A CTA (8 warps) owns 8 rows of
+// The bit-sliced step in shared-memory tiles.  A CTA (8 warps) owns 8 rows of
 // a 1024-cell strip (32 segments).  It stages the 8 rows plus one halo row
 // above and below with coalesced 128-bit loads into shared memory, padded to
 // 33 words per segment so that lane j reading word i of its own segment hits
