@@ -350,6 +350,15 @@ __global__ void __launch_bounds__(kBlock) k_rate_fused(
     }
     __syncthreads();
 
+    // The last layer's region is the tile itself: thread tid owns position
+    // tid, whose weights (small fields) it keeps in registers.
+    constexpr bool kRegLast = F <= 5;
+    float wlast[kRegLast ? K : 1];
+    if (kRegLast && D.L >= 2) {
+        const float* wl = ws + R.woff(D.L - 1, K) + tid;
+#pragma unroll
+        for (int k = 0; k < (kRegLast ? K : 1); ++k) wlast[k] = wl[k * kTileSide * kTileSide];
+    }
     const int lane = tid & 31, warp = tid >> 5;
     for (int tt = 1; tt <= nt; ++tt) {
         const int t = c + tt, cur = (tt - 1) & 1;
@@ -381,12 +390,24 @@ __global__ void __launch_bounds__(kBlock) k_rate_fused(
                     const float* src = r_old + sbase[o + p];
                     const float* wl = ws + wofs + p;
                     float part[F];
+                    if (kRegLast && l == D.L - 1) {
 #pragma unroll
-                    for (int kr = 0; kr < F; ++kr) {
-                        part[kr] = 0.0f;
+                        for (int kr = 0; kr < F; ++kr) {
+                            part[kr] = 0.0f;
 #pragma unroll
-                        for (int kc = 0; kc < F; ++kc)
-                            part[kr] = __fmaf_rn(wl[(kr * F + kc) * sd2], src[kr * sp + kc], part[kr]);
+                            for (int kc = 0; kc < F; ++kc)
+                                part[kr] = __fmaf_rn(wlast[kRegLast ? kr * F + kc : 0],
+                                                     src[kr * sp + kc], part[kr]);
+                        }
+                    } else {
+#pragma unroll
+                        for (int kr = 0; kr < F; ++kr) {
+                            part[kr] = 0.0f;
+#pragma unroll
+                            for (int kc = 0; kc < F; ++kc)
+                                part[kr] = __fmaf_rn(wl[(kr * F + kc) * sd2], src[kr * sp + kc],
+                                                     part[kr]);
+                        }
                     }
                     I = 0.0f;
 #pragma unroll
