@@ -234,7 +234,8 @@ __global__ void __launch_bounds__(kBlock) k_rate_step(
 //   mode 0 (forward): steps 1..T from v = 0; writes the checkpoints
 //     (t % k == 0, t < T) and the per-tile readout partials ypart.
 //   mode 1 (recompute): nt steps from the checkpointed v at step c; writes
-//     the segment's r (steps c..c+nt), drives d and v at step c.
+//     the segment's r (steps c..c+nt) and drives d, which is all the adjoint
+//     kernels read.
 // The input of the next step is fetched with cp.async during the current one.
 struct FusedRegions {
     int L, H;
@@ -275,8 +276,8 @@ template <int F>
 __global__ void __launch_bounds__(kBlock) k_rate_fused(
     Dims D, int mode, int c, int nt, const float* __restrict__ x, const float* __restrict__ wt,
     const float* __restrict__ wo, const float* __restrict__ tau, const float* __restrict__ v0,
-    float* __restrict__ ckpt, float* __restrict__ ypart, float* __restrict__ seg_v,
-    float* __restrict__ seg_r, float* __restrict__ seg_d) {
+    float* __restrict__ ckpt, float* __restrict__ ypart, float* __restrict__ seg_r,
+    float* __restrict__ seg_d) {
     constexpr int H = F / 2, K = F * F;
     extern __shared__ float fs[];
     const FusedRegions R{D.L, H};
@@ -318,10 +319,7 @@ __global__ void __launch_bounds__(kBlock) k_rate_fused(
             vs[o + p] = v;
             rs[o + p] = r;
             rs[tot + o + p] = 0.0f;
-            if (mode == 1 && in && own) {
-                seg_v[gl] = v;
-                seg_r[gl] = r;
-            }
+            if (mode == 1 && in && own) seg_r[gl] = r;
             if (l >= 1) {
 #pragma unroll
                 for (int k = 0; k < K; ++k)
@@ -422,7 +420,6 @@ __global__ void __launch_bounds__(kBlock) k_rate_fused(
                 if (code & kOwnBit) {
                     const long long gl = ((long long)l * D.B + b) * D.N + (code & (kOwnBit - 1));
                     if (mode == 1) {
-                        seg_v[tt * S + gl] = vn;
                         seg_r[tt * S + gl] = rn;
                         seg_d[(tt - 1) * S + gl] = d;
                     } else if (store_ckpt) {
@@ -891,14 +888,14 @@ size_t fused_bytes(const Dims& D) {
 
 void fused(const Dims& D, int mode, int c, int nt, const float* x, const float* wo,
            const float* tau, const Work& W, const float* v0, float* ckpt, float* ypart,
-           float* seg_v, float* seg_r, float* seg_d, cudaStream_t st) {
+           float* seg_r, float* seg_d, cudaStream_t st) {
     const size_t bytes = fused_bytes(D);
     const dim3 grid((unsigned)D.nchunk, (unsigned)D.B);
     SG_RATE_FIELD(D.field, ({
         SG_CUDA(cudaFuncSetAttribute(k_rate_fused<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)bytes));
         k_rate_fused<F><<<grid, kBlock, bytes, st>>>(D, mode, c, nt, x, W.wt, wo, tau, v0, ckpt,
-                                                     ypart, seg_v, seg_r, seg_d);
+                                                     ypart, seg_r, seg_d);
     }));
     SG_LAUNCH_CHECK();
 }
@@ -909,7 +906,7 @@ void forward(const Dims& D, const float* x, const float* w, const float* wo, con
     transpose_weights(D, w, W, st);
     SG_CUDA(cudaMemsetAsync(W.ckpt, 0, D.S * sizeof(float), st));
     if (fused_bytes(D)) {
-        fused(D, 0, 0, D.T, x, wo, tau, W, nullptr, W.ckpt, W.ypart, nullptr, nullptr, nullptr, st);
+        fused(D, 0, 0, D.T, x, wo, tau, W, nullptr, W.ckpt, W.ypart, nullptr, nullptr, st);
     } else {
         float* v[2] = {W.seg_v, W.seg_v + D.S};
         float* r[2] = {W.seg_r, W.seg_r + D.S};
@@ -951,7 +948,7 @@ void backward(const Dims& D, const float* x, const float* w, const float* wo, co
         const int c = seg * D.k, nt = std::min(D.k, D.T - c);
         if (fused_bytes(D)) {
             fused(D, 1, c, nt, x, wo, tau, W, W.ckpt + (long long)seg * D.S, nullptr, nullptr,
-                  W.seg_v, W.seg_r, W.seg_d, st);
+                  W.seg_r, W.seg_d, st);
         } else {
             SG_CUDA(cudaMemcpyAsync(W.seg_v, W.ckpt + (long long)seg * D.S, D.S * sizeof(float),
                                     cudaMemcpyDeviceToDevice, st));
