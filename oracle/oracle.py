@@ -141,8 +141,53 @@ class Layer:
         self.size = self.rows * self.cols
         self.output_type = MODELS[self.model]
         self.inputs, self.outputs = [], []
-        if p.child_arrays.get("dendrites"):
-            raise ValueError("oracle: dendritic trees are not restated")
+        self.root = Dendrite("root", self, None, 0, OPCODES["add"], False, 0.0)
+        self._add_dendrites(self.root, p.child_arrays.get("dendrites", []))
+        self.registers = self.root.max_register() + 1
+
+    def dendrites(self):  # breadth first, root first (layer.cpp:62-77)
+        out = [self.root]
+        for d in out:
+            out.extend(ch for ch in d.children if isinstance(ch, Dendrite))
+        return out
+
+    def dendrite(self, name):
+        for d in self.dendrites():
+            if d.name == name:
+                return d
+        return None
+
+    def _add_dendrites(self, parent, configs):  # layer.cpp:135-153, dendritic_node.cpp:80-104
+        for dp in configs:
+            if not dp.has("name"):
+                raise ValueError("Attempted to dendrite without name to layer!")
+            name = dp.get("name")
+            if parent.second_order:
+                raise ValueError("Second order dendritic nodes cannot have internal children!")
+            if self.dendrite(name) is not None:
+                raise ValueError("Duplicate dendritic node name: " + name + "!")
+            node = Dendrite(name, self, parent, self.root.max_register() + 1,
+                            OPCODES[dp.get("opcode", "add")], dp.get_bool("second order", False),
+                            dp.get_float("init", 0.0))
+            parent.children.append(node)
+            self._add_dendrites(node, dp.child_arrays.get("children", []))
+
+
+class Dendrite:
+    """A node of a layer's dendritic tree (network/dendritic_node.cpp:5-52).
+    children: internal Dendrite nodes and leaf Conn objects in creation
+    order; a second-order node's first connection is its host (not a child)."""
+
+    def __init__(self, name, layer, parent, reg, opcode, second_order, init):
+        self.name, self.layer, self.parent, self.reg = name, layer, parent, reg
+        self.opcode, self.second_order = opcode, second_order
+        self.init = np.float32(init)
+        self.children = []
+        self.host = None
+
+    def max_register(self):  # dendritic_node.cpp:142-153
+        regs = [self.reg] + [ch.max_register() for ch in self.children if isinstance(ch, Dendrite)]
+        return max(regs)
 
 
 class Conn:
@@ -156,6 +201,13 @@ class Conn:
         self.type = CONN_TYPES[p.get("type", "fully connected")]
         self.opcode = OPCODES[p.get("opcode", "add")]
         self.convolutional = p.get_bool("convolutional", False)
+        # dendritic node and second-order role (connection.cpp:132-144)
+        self.node = to.dendrite(p.get("dendrite", "root"))
+        if self.node is None:
+            raise ValueError("Cannot find Dendritic Node " + p.get("dendrite", "root") + "!")
+        self.second_order = self.node.second_order
+        self.so_host = self.second_order and self.node.host is None
+        self.so_slave = self.second_order and not self.so_host
         if p.get_bool("sparse", False) or p.get_bool("randomized projection", False):
             raise ValueError("oracle: sparse / randomized projections are not restated")
         c = _Conn()
@@ -206,6 +258,17 @@ class Conn:
             self.num_weights = frm.size * to.size
         c.num_weights = self.num_weights
         self.c = c
+        if self.second_order and self.plastic:  # connection.cpp:149-153
+            raise ValueError("Plastic second order connections are not supported!")
+        if self.so_slave:  # connection.cpp:163-191
+            host = self.node.host
+            if (self.type != host.type or self.convolutional != host.convolutional
+                    or self.num_weights != host.num_weights):
+                raise ValueError("Second order connection does not match host connection!")
+            if self.convolutional and (c.row_field * c.col_field != frm.size or c.row_spacing != 1
+                                       or c.col_spacing != 1 or c.row_stride != 0 or c.col_stride != 0):
+                raise ValueError("Second order convolutional connections must have fields that are "
+                                 "the size of the input layer, and must have 0 stride and 1 spacing!")
         self._visits()
 
     def _visits(self):
@@ -262,6 +325,10 @@ class OracleNetwork:
             conn = Conn(cp, frm, to)
             frm.outputs.append(conn)
             to.inputs.append(conn)
+            if conn.so_host:  # dendritic_node.cpp:106-140
+                conn.node.host = conn
+            else:
+                conn.node.children.append(conn)
             self.conns.append(conn)
         self._build_state()
 
@@ -275,11 +342,12 @@ class OracleNetwork:
     def _build_state(self):
         self.neuron = {}
         self.matrix = {}
+        self.so_weights = {}
         L = lib()
         for l in self.layers:
             max_delay = max([c.delay for c in l.outputs] + [0])
             l.history = 1 + (max_delay // 32 if l.output_type == BIT else max_delay)
-            st = {"input": np.zeros(l.size, np.float32),
+            st = {"input": np.zeros(l.registers * l.size, np.float32),   # attributes.cpp:21-26
                   "output": np.zeros(l.history * l.size, np.uint32)}
             if l.model == "izhikevich":
                 for k in ("ampa", "nmda", "gabaa", "gabab", "mult", "dopamine",
@@ -294,6 +362,8 @@ class OracleNetwork:
             self.neuron[l] = st
         for c in self.conns:
             self.matrix[c] = m = {"weights": self._init_weights(c)}
+            if c.so_host:  # weight_matrix.cpp:79-80 (not readable through the getters)
+                self.so_weights[c] = np.zeros(c.num_weights, np.float32)
             if c.to.model == "izhikevich":
                 n = c.num_weights
                 m["short trace"] = np.zeros(n, np.float32)
@@ -400,32 +470,75 @@ class OracleNetwork:
     def get_weight_matrix(self, conn, key="weights"):
         return self.matrix[self.connection(conn)][key]
 
+    # -- engine build ------------------------------------------------------
+    def start_engine(self):
+        """What building an engine does to the state: internal dendritic
+        registers other than second-order ones are set to their init values
+        (cluster_node.cpp:116-129).  run() calls it; step() calls it once."""
+        for l in self.layers:
+            for d in l.dendrites():
+                if d is not l.root and not d.second_order:
+                    self.neuron[l]["input"][d.reg * l.size:(d.reg + 1) * l.size] = d.init
+        self._engine_started = True
+
+    def _dendrite_plan(self, node, ops):  # cluster_node.cpp:115-207 (post-order)
+        if node.second_order:
+            ops.append(("copy", node))
+        for ch in node.children:
+            if isinstance(ch, Dendrite):
+                self._dendrite_plan(ch, ops)
+                if node.reg != ch.reg:
+                    ops.append(("fold", node, ch))
+            else:
+                ops.append(("conn", ch, node))
+        if node.second_order:
+            if node.host is None:
+                raise ValueError("Missing host connection for second order node!")
+            ops.append(("conn", node.host, node))
+        return ops
+
     # -- one timestep ------------------------------------------------------
     def step(self, inputs=None, learning=True):
         """inputs: {layer name: float32 array} for layers fed by an input module."""
+        if not getattr(self, "_engine_started", False):
+            self.start_engine()
         inputs = inputs or {}
         L = lib()
-        # init / input transfer (instruction.cpp:3-30, instruction.h:474-489)
+        # init / input transfer into register 0 (instruction.cpp:3-30,
+        # instruction.h:474-489)
         for l in self.layers:
-            st = self.neuron[l]
+            reg0 = self.neuron[l]["input"][:l.size]
             init = l.p.child("init config")
             is_input = l.name in inputs
             if is_input:
-                st["input"][:] = np.asarray(inputs[l.name], np.float32)
+                reg0[:] = np.asarray(inputs[l.name], np.float32)
             if init is not None:
                 if init.get("type", "normal") != "flat":
                     raise ValueError("oracle: only flat init configs are restated")
                 v = np.float32(init.get_float("value", 1.0))
                 if is_input:
-                    st["input"] += v
+                    reg0 += v
                 else:
-                    st["input"][:] = v
+                    reg0[:] = v
             elif not is_input:
-                st["input"][:] = 0.0
+                reg0[:] = 0.0
         # synaptic activation: every connection reads outputs of step t-1
         for l in self.layers:
-            for c in l.inputs:
-                self._activate(L, c)
+            if l.registers == 1:
+                for c in l.inputs:
+                    self._activate(L, c)
+                continue
+            inp = self.neuron[l]["input"]
+            for op in self._dendrite_plan(l.root, []):
+                if op[0] == "copy":  # instruction.h:461-472
+                    host = op[1].host
+                    self.so_weights[host][:] = self.matrix[host]["weights"]
+                elif op[0] == "fold":
+                    node, ch = op[1], op[2]
+                    L.sg_calc_internal(l.size, _p(inp[ch.reg * l.size:]), _p(inp[node.reg * l.size:]),
+                                       ch.opcode, ctypes.c_float(ch.init))
+                else:
+                    self._activate(L, op[1])
         # neuron updates
         for l in self.layers:
             self._update(L, l)
@@ -439,6 +552,7 @@ class OracleNetwork:
     def run(self, steps, input_fn=None, learning=True, record=None):
         """record: list of (layer, key) recorded after every step."""
         trace = {k: [] for k in (record or [])}
+        self.start_engine()
         for t in range(steps):
             self.step(input_fn(t) if input_fn else None, learning)
             for k in trace:
@@ -454,9 +568,22 @@ class OracleNetwork:
         st, m = self.neuron[c.to], self.matrix[c]
         src = self._src_words(c)
         geo = (c.rows, _p(c.dst), _p(c.ptr), _p(c.from_idx), _p(c.w_idx))
-        if c.to.model == "izhikevich" and c.p.get("direct", "false") != "true":
+        reg = st["input"][c.node.reg * c.to.size:(c.node.reg + 1) * c.to.size]
+        direct = c.p.get("direct", "false") == "true"
+        if c.to.model == "izhikevich" and not direct and c.second_order:
+            raise ValueError("Unimplemented connection type!")   # izhikevich_attributes.cpp:371-379
+        if c.so_slave:
+            so = self.so_weights[c.node.host]
+            if c.convolutional:
+                L.sg_act_second_order_conv(c.frm.size, _p(src), c.frm.output_type, c.delay, c.opcode,
+                                           _p(m["weights"]), _p(so))
+            else:
+                L.sg_act_second_order(*geo, _p(src), c.frm.output_type, c.delay, c.opcode,
+                                      _p(m["weights"]), _p(so))
+            return
+        if c.to.model == "izhikevich" and not direct:
             if c.opcode == OPCODES["gap"]:
-                L.sg_act_gap(*geo, _p(st["voltage"]), _p(m["weights"]), _p(st["input"]))
+                L.sg_act_gap(*geo, _p(st["voltage"]), _p(m["weights"]), _p(reg))
                 return
             targets = {0: ("ampa", 0.8, "nmda", 0.993), 1: ("gabaa", 0.833, "gabab", 0.993),
                        2: ("mult", 0.95, None, -1.0), 5: ("dopamine", 0.95, None, -1.0)}
@@ -469,8 +596,8 @@ class OracleNetwork:
                         ctypes.c_float(c.baseline_conductance), ctypes.c_float(stau),
                         ctypes.c_float(ltau), _p(st[sname]), _p(st[lname] if lname else st[sname]))
         else:
-            L.sg_act_base(*geo, _p(src), c.frm.output_type, c.delay, c.opcode,
-                          _p(m["weights"]), _p(st["input"]))
+            w = self.so_weights[c] if c.so_host else m["weights"]
+            L.sg_act_base(*geo, _p(src), c.frm.output_type, c.delay, c.opcode, _p(w), _p(reg))
 
     def _update(self, L, l):
         st = self.neuron[l]

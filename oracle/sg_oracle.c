@@ -181,6 +181,37 @@ void sg_act_base(int rows, const int *dst, const long *ptr, const int *from_idx,
     }
 }
 
+/* Second-order slave (ACTIVATE_ALL_SECOND_ORDER, synapse_kernel.h:918-975):
+ * each visited synapse modulates the host's weight copy with the slave's own
+ * opcode; the host later activates with that copy. */
+void sg_act_second_order(int rows, const int *dst, const long *ptr, const int *from_idx,
+                         const int *w_idx, const uint32_t *src_words, int src_type, int delay,
+                         int opcode, const float *weights, float *so) {
+    (void)dst;
+    for (int r = 0; r < rows; ++r)
+        for (long v = ptr[r]; v < ptr[r + 1]; ++v) {
+            float val = extract(src_words[from_idx[v]], delay, src_type) * weights[w_idx[v]];
+            so[w_idx[v]] = aggregate(so[w_idx[v]], val, opcode);
+        }
+}
+
+/* Convolutional slave: the one-to-one loop (synapse_kernel.h:255-275) over
+ * the shared kernel, whose size is the source layer's. */
+void sg_act_second_order_conv(int n, const uint32_t *src_words, int src_type, int delay,
+                              int opcode, const float *weights, float *so) {
+    for (int k = 0; k < n; ++k)
+        so[k] = aggregate(so[k], extract(src_words[k], delay, src_type) * weights[k], opcode);
+}
+
+/* calc_internal_SERIAL (kernel.cpp:161-170): fold an internal dendritic
+ * node's register into its parent's, then reset it to its init value. */
+void sg_calc_internal(int size, float *src, float *dst, int opcode, float trail) {
+    for (int i = 0; i < size; ++i) {
+        dst[i] = aggregate(dst[i], src[i], opcode);
+        src[i] = trail;
+    }
+}
+
 /* Izhikevich trace activators: izhikevich_attributes.cpp:228-352.
  * long_tau < 0 selects the single-trace variants (mult, reward).
  * from_tss is updated per visit in serial order (F7). */

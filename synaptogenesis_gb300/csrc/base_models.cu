@@ -60,15 +60,93 @@ void launch_base_activator(State& st, ConnState& cs, float* inputs, cudaStream_t
     const uint32_t* src = st.dev_output(c.from, word_index(c.delay, c.from->output_type));
     const int threads = 128;
     unsigned blocks = blocks_for(cs.geom.n_dest, threads);
+    // a second-order host reads the copy of its weights the slaves modulated
+    // (synapse_data.cpp:20-23)
+    const float* w = cs.so_weights ? cs.so_weights->df() : cs.weights->df();
     SG_DISPATCH_TYPE_SRC((int)c.type, (int)c.from->output_type,
         (k_activate_base<TY, SR><<<blocks, threads, 0, s>>>(cs.geom, src, c.delay, (int)c.opcode,
-                                                           cs.weights->df(), inputs)));
+                                                           w, inputs)));
     SG_LAUNCH_CHECK();
 }
 
+float* input_register(State& st, const ConnState& cs) {
+    const Layer* l = cs.conn->to;
+    return st.layer_state(cs.conn->to)->input->df() + (size_t)cs.reg * l->size;
+}
+
 void Model::activate(State& st, ConnState& cs, const StepCtx& ctx) const {
-    launch_base_activator(st, cs, st.layer_state(cs.conn->to)->input->df(), ctx.stream);
+    launch_base_activator(st, cs, input_register(st, cs), ctx.stream);
     ctx.count();
+}
+
+// ---------------------------------------------------------------------------
+// Dendritic trees and second-order connections
+// ---------------------------------------------------------------------------
+// Second-order slave (ACTIVATE_ALL_SECOND_ORDER, synapse_kernel.h:918-975):
+// every visited synapse modulates the host's weight copy with the slave's own
+// opcode, so[wi] = aggregate(so[wi], extract(out[from]) * w[wi]).  Each
+// weight index belongs to one destination, so threads never share an entry.
+template <int TY, int SR>
+__global__ void __launch_bounds__(256) k_activate_second_order(DGeom g, const uint32_t* __restrict__ src,
+                                                               int delay, int opcode,
+                                                               const float* __restrict__ w,
+                                                               const int* __restrict__ remap,
+                                                               float* __restrict__ so) {
+    int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= g.n_dest) return;
+    for_each_source<TY>(g, d, [&](int from, int wi) {
+        const float val = extract<SR>(src[from], delay) * w[wi];
+        const int si = remap ? remap[wi] : wi;
+        so[si] = aggregate(so[si], val, opcode);
+    });
+}
+
+// Convolutional slave: a one-to-one pass over the shared kernel, whose size
+// is the source layer's (CALC_ONE_TO_ONE of the same macros).
+template <int SR>
+__global__ void k_activate_second_order_conv(int n, const uint32_t* __restrict__ src, int delay,
+                                             int opcode, const float* __restrict__ w,
+                                             float* __restrict__ so) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    so[k] = aggregate(so[k], extract<SR>(src[k], delay) * w[k], opcode);
+}
+
+void launch_second_order_slave(State& st, ConnState& cs, float* so, cudaStream_t s) {
+    const Connection& c = *cs.conn;
+    const uint32_t* src = st.dev_output(c.from, word_index(c.delay, c.from->output_type));
+    const int sr = (int)c.from->output_type;
+    if (c.convolutional) {
+        const int n = c.from->size;
+        unsigned blocks = blocks_for(n, 256);
+        switch (sr) {
+            case 0: k_activate_second_order_conv<0><<<blocks, 256, 0, s>>>(n, src, c.delay, (int)c.opcode, cs.weights->df(), so); break;
+            case 1: k_activate_second_order_conv<1><<<blocks, 256, 0, s>>>(n, src, c.delay, (int)c.opcode, cs.weights->df(), so); break;
+            default: k_activate_second_order_conv<2><<<blocks, 256, 0, s>>>(n, src, c.delay, (int)c.opcode, cs.weights->df(), so); break;
+        }
+    } else {
+        const int* remap = cs.so_remap ? cs.so_remap->di() : nullptr;
+        unsigned blocks = blocks_for(cs.geom.n_dest, 128);
+        SG_DISPATCH_TYPE_SRC((int)c.type, sr,
+            (k_activate_second_order<TY, SR><<<blocks, 128, 0, s>>>(cs.geom, src, c.delay, (int)c.opcode,
+                                                                    cs.weights->df(), remap, so)));
+    }
+    SG_LAUNCH_CHECK();
+}
+
+// calc_internal (kernel.cpp:160-182): fold a node's register into its
+// parent's with the node's opcode, then reset it to the node's init value.
+__global__ void k_dendrite_fold(int n, float* __restrict__ src, float* __restrict__ dst, int opcode,
+                                float trail) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    dst[i] = aggregate(dst[i], src[i], opcode);
+    src[i] = trail;
+}
+
+void launch_dendrite_fold(int n, float* src, float* dst, int opcode, float trail, cudaStream_t s) {
+    k_dendrite_fold<<<blocks_for(n, 256), 256, 0, s>>>(n, src, dst, opcode, trail);
+    SG_LAUNCH_CHECK();
 }
 
 // ---------------------------------------------------------------------------
@@ -577,11 +655,11 @@ class GameOfLifeModel : public Model {
   public:
     const char* name() const override { return "game_of_life"; }
     OutputType output_type() const override { return OUT_BIT; }
-    // The fused step applies to a layer whose only input is its own
-    // convergent "add" connection reading word 0, with no init config, no
-    // environment input and a one-word history.
+    // The fused step applies to a layer without dendritic nodes whose only
+    // input is its own convergent "add" connection reading word 0, with no
+    // init config, no environment input and a one-word history.
     static bool fusable_shape(const Layer& l) {
-        if (l.inputs.size() != 1) return false;
+        if (l.inputs.size() != 1 || l.has_dendrites()) return false;
         const Connection* c = l.inputs[0];
         return c->from == &l && c->type == CONVERGENT && c->opcode == OP_ADD && c->delay < 32 &&
                l.history() == 1 && !l.config.child("init config");

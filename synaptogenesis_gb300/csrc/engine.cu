@@ -129,11 +129,28 @@ Engine::Engine(Network* net, Environment* env, State* state, const Props& args)
             Props* init = lp->config.child("init config");
             if (init && init->get("type", "normal") != "flat") step_counter_ = true;
         }
+        // dendritic trees: activation order, and the internal registers set
+        // to their init values (cluster_node.cpp:116-129; second-order nodes
+        // and the root are not set)
+        dend_ops_.assign(net_->layers.size(), {});
+        for (auto& lp : net_->layers)
+            if (lp->has_dendrites()) plan_dendrites(lp->root.get(), dend_ops_[lp->index]);
         state_->to_device(stream_);
+        for (auto& lp : net_->layers) {
+            if (!lp->has_dendrites()) continue;
+            float* in = state_->layer_state(lp.get())->input->df();
+            for (Dendrite* d : lp->dendrites()) {
+                if (d == lp->root.get() || d->second_order) continue;
+                k_set_value<<<blocks_for(lp->size, 256), 256, 0, stream_>>>(
+                    in + (size_t)d->reg * lp->size, lp->size, d->init, 1);
+                SG_LAUNCH_CHECK();
+            }
+            state_->mark_device_newer();
+        }
         // No environment and every layer self-contained: whole runs per layer.
         alone_ = modules_.empty() && !net_->layers.empty() && args.get_bool("whole runs", true);
         for (auto& lp : net_->layers)
-            alone_ = alone_ &&
+            alone_ = alone_ && !lp->has_dendrites() &&
                      find_model(lp->model)->can_advance_alone(*state_, *state_->layer_state(lp.get()));
         for (auto& lp : net_->layers) {
             if (layer_io_[lp->index] & 1) input_layers_.push_back(lp.get());
@@ -187,6 +204,26 @@ Engine::~Engine() {
         for (auto& e : kv.second.events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
     running = false;
     interrupt_flag = false;
+}
+
+void Engine::plan_dendrites(Dendrite* node, std::vector<DendOp>& ops) {
+    // a second-order node starts from a fresh copy of its host's weights
+    if (node->second_order) ops.push_back({DendOp::SO_COPY, nullptr, node, nullptr});
+    for (auto& ch : node->children) {
+        if (ch.conn) {
+            ops.push_back({DendOp::CONN, ch.conn, node, nullptr});
+        } else {
+            plan_dendrites(ch.node, ops);
+            if (node->reg != ch.node->reg) ops.push_back({DendOp::FOLD, nullptr, node, ch.node});
+        }
+    }
+    // the host goes last: it reads the weights its slaves modulated
+    if (node->second_order) {
+        if (!node->host)
+            throw SgError("Error building cluster node for " + node->layer->str() +
+                          ":\n  Missing host connection for second order node!");
+        ops.push_back({DendOp::CONN, node->host, node, nullptr});
+    }
 }
 
 void Engine::build_modules() {
@@ -253,7 +290,7 @@ void Engine::enqueue_step(bool last) {
         LayerState* ls = state_->layer_state(l);
         float* in = ls->input->df();
         bool is_input = (layer_io_[l->index] & 1) != 0;
-        bool all_fused = !l->inputs.empty();
+        bool all_fused = !l->inputs.empty() && !l->has_dendrites();
         for (Connection* c : l->inputs) all_fused = all_fused && m->fuses_input(*state_, *c, ctx);
         if (all_fused && !is_input) continue;   // the fused update writes the register itself
         if (is_input) {
@@ -303,17 +340,48 @@ void Engine::enqueue_step(bool last) {
     // learning from the last step (side stream) go last, so that the other
     // layers' activations overlap that learning; activations into different
     // layers touch different arrays, and each layer keeps its own order.
+    auto activate_conn = [&](Layer* l, const Model* m, Connection* c) {
+        if (overlap_ && learn_pending_[c->index]) {    // after its learning of the last step
+            SG_CUDA(cudaStreamWaitEvent(stream_, learn_ev_[c->index], 0));
+            learn_pending_[c->index] = 0;
+        }
+        ConnState& cs = *state_->conn_state(c);
+        if (c->second_order_slave) {
+            float* so = state_->conn_state(c->node->host)->so_weights->df();
+            timed("second_order.slave." + std::string(conn_type_name(c->type)), 1, [&] {
+                launch_second_order_slave(*state_, cs, so, stream_);
+            });
+            ++launches_;
+            return;
+        }
+        timed(std::string(l->model) + ".activate." + conn_type_name(c->type), 1, [&] {
+            m->activate(*state_, cs, ctx);
+        });
+    };
     auto activate_layer = [&](Layer* l) {
         const Model* m = find_model(l->model);
-        for (Connection* c : l->inputs) {
-            if (m->fuses_input(*state_, *c, ctx)) continue;
-            if (overlap_ && learn_pending_[c->index]) {    // after its learning of the last step
-                SG_CUDA(cudaStreamWaitEvent(stream_, learn_ev_[c->index], 0));
-                learn_pending_[c->index] = 0;
+        if (!l->has_dendrites()) {
+            for (Connection* c : l->inputs)
+                if (!m->fuses_input(*state_, *c, ctx)) activate_conn(l, m, c);
+            return;
+        }
+        float* in = state_->layer_state(l)->input->df();
+        for (const DendOp& op : dend_ops_[l->index]) {
+            if (op.kind == DendOp::CONN) {
+                activate_conn(l, m, op.conn);
+            } else if (op.kind == DendOp::SO_COPY) {
+                // SecondOrderWeightTransferInstruction (instruction.h:461-472)
+                ConnState& hs = *state_->conn_state(op.node->host);
+                SG_CUDA(cudaMemcpyAsync(hs.so_weights->df(), hs.weights->df(), hs.weights->dev_count * 4,
+                                        cudaMemcpyDeviceToDevice, stream_));
+            } else {
+                timed("dendrite.fold", 1, [&] {
+                    launch_dendrite_fold(l->size, in + (size_t)op.child->reg * l->size,
+                                         in + (size_t)op.node->reg * l->size, (int)op.child->opcode,
+                                         op.child->init, stream_);
+                });
+                ++launches_;
             }
-            timed(std::string(l->model) + ".activate." + conn_type_name(c->type), 1, [&] {
-                m->activate(*state_, *state_->conn_state(c), ctx);
-            });
         }
     };
     std::vector<Layer*> deferred;

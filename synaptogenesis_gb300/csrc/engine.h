@@ -72,6 +72,16 @@ class Engine {
         long launches = 0;
     };
 
+    // One step of a layer's synaptic input, in the order of the dendritic
+    // tree's post-order walk (cluster_node.cpp:115-207).
+    struct DendOp {
+        enum Kind { CONN, SO_COPY, FOLD } kind;
+        Connection* conn = nullptr;      // CONN
+        Dendrite* node = nullptr;        // CONN: node fed; SO_COPY: second-order node; FOLD: parent
+        Dendrite* child = nullptr;       // FOLD: internal child folded into node
+    };
+    void plan_dendrites(Dendrite* node, std::vector<DendOp>& ops);
+
     void build_modules();
     void feed_input();
     void report_output(long i);
@@ -101,6 +111,7 @@ class Engine {
     bool profile_ = false;
     int env_rate_ = 1;
     std::vector<Module> modules_;
+    std::vector<std::vector<DendOp>> dend_ops_;   // per layer, for layers with dendritic trees
     std::vector<int> layer_io_;          // per layer: bit0 input, bit1 output
     std::vector<Layer*> input_layers_, output_layers_;
     std::vector<float*> in_pinned_, in_staging_;

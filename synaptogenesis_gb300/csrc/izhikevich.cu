@@ -644,25 +644,31 @@ class IzhikevichModel : public Model {
         if (c.parameter("direct", "false") != "true" && c.opcode != OP_ADD && c.opcode != OP_SUB &&
             c.opcode != OP_MULT && c.opcode != OP_REWARD && c.opcode != OP_GAP)
             throw SgError(c.str() + ": Unimplemented connection type!");
+        // trace activators write conductances, not a register, and keep no
+        // weight copy: second order only through the base activator
+        // (izhikevich_attributes.cpp:371-379)
+        if (c.parameter("direct", "false") != "true" && c.second_order)
+            throw SgError(c.str() + ": Unimplemented connection type!");
     }
 
     void activate(State& st, ConnState& cs, const StepCtx& ctx) const override {
         Connection& c = *cs.conn;
         LayerState& to = *st.layer_state(c.to);
         if (c.parameter("direct", "false") == "true") {
-            launch_base_activator(st, cs, to.input->df(), ctx.stream);
+            launch_base_activator(st, cs, input_register(st, cs), ctx.stream);
             ctx.count();
             return;
         }
         const int threads = 128;
         unsigned blocks = blocks_for(cs.geom.n_dest, threads);
         if (c.opcode == OP_GAP) {
+            float* reg = input_register(st, cs);
             switch (c.type) {
-                case 0: k_iz_gap<0><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), to.input->df()); break;
-                case 1: k_iz_gap<1><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), to.input->df()); break;
-                case 2: k_iz_gap<2><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), to.input->df()); break;
-                case 3: k_iz_gap<3><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), to.input->df()); break;
-                case 4: k_iz_gap<4><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), to.input->df()); break;
+                case 0: k_iz_gap<0><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), reg); break;
+                case 1: k_iz_gap<1><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), reg); break;
+                case 2: k_iz_gap<2><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), reg); break;
+                case 3: k_iz_gap<3><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), reg); break;
+                case 4: k_iz_gap<4><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), reg); break;
             }
             SG_LAUNCH_CHECK();
             ctx.count();

@@ -85,5 +85,11 @@ std::vector<std::string> model_names();
 // Base activator launch (ACTIVATE_ALL(activate_base), kernel.cpp:217):
 // inputs[to] = aggregate(inputs[to], sum_k extract(out[from], delay) * w).
 void launch_base_activator(State& st, ConnState& cs, float* inputs, cudaStream_t s);
+// Input register of the dendritic node a connection feeds.
+float* input_register(State& st, const ConnState& cs);
+// Second-order slave: modulates the host's per-step weight copy `so`.
+void launch_second_order_slave(State& st, ConnState& cs, float* so, cudaStream_t s);
+// Internal dendritic node: dst = aggregate(dst, src); src = trail.
+void launch_dendrite_fold(int n, float* src, float* dst, int opcode, float trail, cudaStream_t s);
 
 }  // namespace sg

@@ -43,11 +43,63 @@ std::string Layer::str() const {
     return "[Layer: " + name + " (" + structure->name + ")]";
 }
 
+int Dendrite::max_register() const {
+    int m = reg;
+    for (auto& ch : children)
+        if (ch.node) m = std::max(m, ch.node->max_register());
+    return m;
+}
+
+std::string Dendrite::str() const { return "[Dendrite: " + name + " (" + layer->name + ")]"; }
+
+std::vector<Dendrite*> Layer::dendrites() const {
+    std::vector<Dendrite*> out{root.get()};
+    for (size_t i = 0; i < out.size(); ++i)
+        for (auto& ch : out[i]->children)
+            if (ch.node) out.push_back(ch.node);
+    return out;
+}
+
+Dendrite* Layer::dendrite(const std::string& n) const {
+    for (Dendrite* d : dendrites())
+        if (d->name == n) return d;
+    return nullptr;
+}
+
+// Layer::add_dendrites and DendriticNode::add_child (layer.cpp:135-153,
+// dendritic_node.cpp:80-104): depth first, so registers follow the pre-order
+// of the config.
+static void add_dendrites(Layer* l, Dendrite* parent, const std::vector<Props*>& configs) {
+    for (Props* d : configs) {
+        if (!d->has("name")) throw SgError("Attempted to dendrite without name to layer!");
+        const std::string name = d->get("name");
+        if (parent->second_order)
+            throw SgError("Error in dendritic node " + name + " of " + l->str() +
+                          "\n  Second order dendritic nodes cannot have internal children!");
+        if (l->dendrite(name))
+            throw SgError("Error in dendritic node of " + l->str() +
+                          "\n  Duplicate dendritic node name: " + name + "!");
+        auto node = std::make_unique<Dendrite>();
+        node->name = name;
+        node->layer = l;
+        node->parent = parent;
+        node->reg = l->root->max_register() + 1;
+        node->opcode = parse_opcode(d->get("opcode", "add"));
+        node->second_order = d->get_bool("second order", false);
+        node->init = d->get_float("init", 0.0f);
+        Dendrite* raw = node.get();
+        parent->children.push_back({raw, nullptr});
+        parent->owned.push_back(std::move(node));
+        add_dendrites(l, raw, d->child_array("children"));
+    }
+}
+
 // Same text as the reference's Connection::str() (connection.cpp:251-259); it
 // also keys saved state records.
 std::string Connection::str() const {
     return "[Connection: " + from->name + " (" + from->structure->name + ") -> " + to->name +
-           " (" + to->structure->name + ") {Node: root} name=" + name + "]";
+           " (" + to->structure->name + ") {Node: " + (node ? node->name : std::string("root")) +
+           "} name=" + name + "]";
 }
 
 // ArborizedConfig (connection_config.cpp:8-45), including the "column offset"
@@ -122,12 +174,15 @@ Network::Network(const Props& config) : config_(config) {
             l->size = l->rows * l->cols;
             l->plastic = lp->get_bool("plastic", false);
             if (lp->get_bool("ghost", false)) throw SgError("ghost layers are not supported");
-            if (!lp->child_array("dendrites").empty())
-                throw SgError("Layer " + l->name + ": dendritic trees are not supported");
             const Model* m = find_model(l->model);
             if (!m) throw SgError("Unrecognized neural model \"" + l->model + "\"");
             l->output_type = m->output_type();
             l->structure = st.get();
+            l->root = std::make_unique<Dendrite>();
+            l->root->name = "root";
+            l->root->layer = l.get();
+            add_dendrites(l.get(), l->root.get(), lp->child_array("dendrites"));
+            l->registers = l->root->max_register() + 1;
             for (auto* other : st->layers)
                 if (other->name == l->name) throw SgError("Repeated layer name : \"" + l->name + "\"");
             l->index = (int)layers.size();
@@ -196,8 +251,12 @@ void Network::add_connection(const Props& p) {
         c->from = p.has("from structure") ? layer(p.get("from structure"), fl) : find_layer(fl);
         c->to = p.has("to structure") ? layer(p.get("to structure"), tl) : find_layer(tl);
     }
-    if (p.get("dendrite", "root") != "root")
-        throw SgError(c->str() + ": dendritic nodes are not supported");
+    const std::string dn = p.get("dendrite", "root");
+    c->node = c->to->dendrite(dn);
+    if (!c->node) throw SgError("Error in " + c->to->str() + ":\n  Cannot find Dendritic Node " + dn + "!");
+    c->second_order = c->node->second_order;
+    c->second_order_host = c->second_order && !c->node->host;
+    c->second_order_slave = c->second_order && !c->second_order_host;
     c->plastic = p.get_bool("plastic", true);
     c->delay = p.get_int("delay", 0);
     c->max_weight = p.get_float("max weight", 1.0f);
@@ -205,8 +264,11 @@ void Network::add_connection(const Props& p) {
     c->opcode = parse_opcode(p.get("opcode", "add"));
     c->convolutional = p.get_bool("convolutional", false);
     if (c->delay < 0) throw SgError("Attempted to construct ConnectionConfig with negative delay!");
-    if (p.get_bool("sparse", false) || p.get_bool("randomized projection", false))
+    if (p.get_bool("sparse", false) || p.get_bool("randomized projection", false)) {
+        if (c->second_order)
+            throw SgError("Error in " + c->str() + ":\n  Sparse second order connections are not supported!");
         throw SgError(c->str() + ": sparse connections are not supported");
+    }
     if (c->convolutional && c->type != CONVERGENT && c->type != DIVERGENT)
         throw SgError("Only convergent/divergent connections can be convolutional!");
     Layer *from = c->from, *to = c->to;
@@ -249,9 +311,29 @@ void Network::add_connection(const Props& p) {
         }
     }
     if (c->num_weights >= (1L << 31)) throw SgError(c->str() + ": more than 2^31 weights");
+    // second-order rules (connection.cpp:149-191)
+    if (c->second_order && c->plastic)
+        throw SgError("Error in " + c->str() + ":\n  Plastic second order connections are not supported!");
+    if (c->second_order_slave) {
+        const Connection* host = c->node->host;
+        if (c->type != host->type || c->convolutional != host->convolutional ||
+            c->num_weights != host->num_weights)
+            throw SgError("Error in " + c->str() + ":\n  Second order connection does not match host connection!");
+        // a convolutional slave runs like a one-to-one connection over the
+        // host's kernel, so its field is the whole source layer
+        const Arbor& a = c->arbor;
+        if (c->convolutional && (a.kernel() != from->size || a.row_spacing != 1 ||
+                                 a.col_spacing != 1 || a.row_stride != 0 || a.col_stride != 0))
+            throw SgError("Error in " + c->str() +
+                          ":\n  Second order convolutional connections must have fields that are the "
+                          "size of the input layer, and must have 0 stride and 1 spacing!");
+    }
     c->index = (int)connections.size();
     from->outputs.push_back(c.get());
     to->inputs.push_back(c.get());
+    // DendriticNode::add_child(Connection*) (dendritic_node.cpp:106-140)
+    if (c->second_order_host) c->node->host = c.get();
+    else c->node->children.push_back({nullptr, c.get()});
     connections.push_back(std::move(c));
 }
 

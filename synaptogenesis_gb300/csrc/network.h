@@ -43,6 +43,36 @@ struct SubsetCfg {
 
 struct Structure;
 struct Connection;
+struct Layer;
+
+// A node of a layer's dendritic tree (network/dendritic_node.cpp:5-146).
+// The root owns input register 0; every internal node gets its own register,
+// one past the highest register of the tree when it is created (so registers
+// follow the pre-order of the layer's "dendrites" config); connections
+// aggregate into the register of the node they name.  Children keep creation
+// order: the internal nodes of the layer config first, then the connections
+// in the order they are created.  A second-order node holds no internal
+// children; its first connection is the host, whose weights the other
+// connections (slaves) modulate every step, and the host is not a child.
+struct Dendrite {
+    std::string name;
+    Layer* layer = nullptr;
+    Dendrite* parent = nullptr;
+    int reg = 0;
+    Opcode opcode = OP_ADD;        // aggregation into the parent's register
+    bool second_order = false;
+    float init = 0.0f;             // register value after each aggregation
+    struct Child {
+        Dendrite* node;            // internal child, or
+        Connection* conn;          // leaf connection
+    };
+    std::vector<Child> children;
+    Connection* host = nullptr;    // second-order host connection
+    std::vector<std::unique_ptr<Dendrite>> owned;
+
+    int max_register() const;
+    std::string str() const;
+};
 
 struct Layer {
     Props config;
@@ -52,9 +82,16 @@ struct Layer {
     int rows = 0, cols = 0, size = 0;
     bool plastic = false;
     OutputType output_type = OUT_FLOAT;
-    std::vector<Connection*> inputs;    // in JSON order (dendritic DFS order)
+    std::vector<Connection*> inputs;    // in JSON order
     std::vector<Connection*> outputs;
     int index = 0;                      // position in network order
+    std::unique_ptr<Dendrite> root;     // dendritic tree (register 0)
+    int registers = 1;                  // input registers: max register + 1
+
+    // Nodes in breadth-first order, root first (layer.cpp:62-77).
+    std::vector<Dendrite*> dendrites() const;
+    Dendrite* dendrite(const std::string& name) const;      // nullptr if absent
+    bool has_dendrites() const { return registers > 1; }   // internal nodes
 
     int max_delay() const;
     int history() const { return 1 + word_index(max_delay(), output_type); }
@@ -77,6 +114,10 @@ struct Connection {
     bool convolutional = false;
     Arbor arbor;
     SubsetCfg subset;
+    Dendrite* node = nullptr;           // dendritic node it feeds
+    bool second_order = false;          // on a second-order node
+    bool second_order_host = false;     // that node's first connection
+    bool second_order_slave = false;
     long num_weights = 0;
     int matrix_rows = 0, matrix_cols = 0;
     int index = 0;

@@ -104,7 +104,9 @@ void State::build() {
         Layer* l = lp.get();
         auto ls = std::make_unique<LayerState>();
         ls->layer = l;
-        ls->input = add_array("input", 'f', l->size);
+        // one register per dendritic node with its own register
+        // (attributes.cpp:21-26); get_neuron_data("input") returns them all
+        ls->input = add_array("input", 'f', (size_t)l->registers * l->size);
         ls->output = add_array("output", 'u', (size_t)l->history() * l->size);
         find_model(l->model)->build_layer(*this, *ls);
         layers.push_back(std::move(ls));
@@ -116,7 +118,26 @@ void State::build() {
         cs->geom = make_geom(*c);
         cs->weights = add_array("weights", 'f', c->num_weights, matrix_layout(*c), c->matrix_rows,
                                 c->matrix_cols);
+        cs->reg = c->node ? c->node->reg : 0;
+        if (c->second_order_host) {
+            cs->so_weights = add_array("second order weights", 'f', c->num_weights, matrix_layout(*c),
+                                       c->matrix_rows, c->matrix_cols);
+            cs->so_weights->scratch = true;
+        }
         conns.push_back(std::move(cs));
+    }
+    // Slaves share the host's flat weight index; where their device layouts
+    // differ, a table maps the slave's device positions to the host's.
+    for (auto& cp : network->connections) {
+        Connection* c = cp.get();
+        if (!c->second_order_slave || c->convolutional) continue;
+        const Array& hw = *conns[c->node->host->index]->weights;
+        const Array& sw = *conns[c->index]->weights;
+        if (hw.layout == sw.layout && hw.rows == sw.rows && hw.cols == sw.cols) continue;
+        Array* remap = add_array("second order remap", 'i', sw.dev_count);
+        for (size_t i = 0; i < (size_t)c->num_weights; ++i)
+            remap->hi()[device_index(sw, i)] = (int32_t)device_index(hw, i);
+        conns[c->index]->so_remap = remap;
     }
     // Weight initialisation and model processing follow the reference's order:
     // all matrices of a layer are created with the layer's attributes

@@ -85,6 +85,15 @@ struct ConnState {
     // the first step, once the arena exists).
     std::shared_ptr<void> device_plan;
     bool device_plan_tried = false;
+    // Input register of the dendritic node the connection feeds.
+    int reg = 0;
+    // Second-order host: the per-step copy of its weights that the slaves
+    // modulate and the host's activation reads (device only, same layout as
+    // the weights; weight_matrix.cpp:79-80).
+    Array* so_weights = nullptr;
+    // Second-order slave whose device layout differs from the host's (subset
+    // windows of another shape): host device index of each slave device index.
+    Array* so_remap = nullptr;
     Array* var(const std::string& k) const;
 };
 

@@ -311,6 +311,151 @@ def cases():
                     final=[("neuron", "s", "iz", k) for k in
                            ("voltage", "recovery", "mult", "dopamine", "input", "output")]
                     + [("neuron", "s", "ro", "output")]))
+
+    # --- dendritic trees ---------------------------------------------------
+    # Registers: tree a=1, a1=2, a2=3, b=4, c=5; rtree h=1, g=2; board n=1;
+    # iz m=1.  Root-level connections listed first still run after the
+    # internal subtrees (post-order walk).
+    conv3 = {"field size": 3, "wrap": False}
+    net = {"structures": [{"name": "d", "type": "parallel", "layers": [
+        _layer("src", "relay", 6, 8),
+        _layer("aux", "relay", 6, 8),
+        _layer("tree", "relay", 6, 8, dendrites=[
+            {"name": "a", "opcode": "mult", "init": 1.0, "children": [
+                {"name": "a1", "opcode": "add"},
+                {"name": "a2", "opcode": "sub", "init": 0.5}]},
+            {"name": "b", "opcode": "sub"},
+            {"name": "c", "opcode": "pool", "init": -2.0}]),
+        _layer("rtree", "rate_encoding", 4, 5, dendrites=[
+            {"name": "h", "opcode": "mult_heaviside", "init": 0.25},
+            {"name": "g", "opcode": "div", "init": 2.0}]),
+        _layer("board", "game_of_life", 12, 12, dendrites=[{"name": "n", "opcode": "add"}]),
+        _layer("iz", "izhikevich", 6, 8, dendrites=[{"name": "m", "opcode": "mult", "init": 1.0}]),
+    ]}], "connections": [
+        {"name": "t_root", "from layer": "src", "to layer": "tree", "type": "one to one",
+         "opcode": "add", "plastic": False},
+        {"name": "t_a", "from layer": "src", "to layer": "tree", "type": "convergent",
+         "opcode": "add", "plastic": False, "dendrite": "a", "arborized config": conv3},
+        {"name": "t_a1", "from layer": "aux", "to layer": "tree", "type": "fully connected",
+         "opcode": "add", "plastic": False, "dendrite": "a1"},
+        {"name": "t_a2", "from layer": "src", "to layer": "tree", "type": "one to one",
+         "opcode": "mult", "plastic": False, "dendrite": "a2"},
+        {"name": "t_a1b", "from layer": "aux", "to layer": "tree", "type": "convergent",
+         "opcode": "sub", "plastic": False, "dendrite": "a1",
+         "arborized config": {"field size": 3, "wrap": True}},
+        {"name": "t_b", "from layer": "src", "to layer": "tree", "type": "convergent",
+         "convolutional": True, "opcode": "add", "plastic": False, "dendrite": "b",
+         "arborized config": {"field size": 3, "wrap": True}},
+        {"name": "t_c", "from layer": "aux", "to layer": "tree", "type": "one to one",
+         "opcode": "add", "plastic": False, "dendrite": "c"},
+        {"name": "t_root2", "from layer": "aux", "to layer": "tree", "type": "one to one",
+         "opcode": "sub", "plastic": False},
+        {"name": "r_h", "from layer": "src", "to layer": "rtree", "type": "fully connected",
+         "opcode": "add", "plastic": False, "dendrite": "h"},
+        {"name": "r_g", "from layer": "aux", "to layer": "rtree", "type": "subset",
+         "opcode": "add", "plastic": False, "dendrite": "g",
+         "subset config": {"from row start": 0, "from row end": 3, "from column start": 1,
+                           "from column end": 5, "to row start": 1, "to row end": 3,
+                           "to column start": 0, "to column end": 4}},
+        {"name": "r_root", "from layer": "src", "to layer": "rtree", "type": "fully connected",
+         "opcode": "add", "plastic": False},
+        {"name": "nbr", "from layer": "board", "to layer": "board", "type": "convergent",
+         "convolutional": True, "plastic": False, "opcode": "add", "dendrite": "n",
+         "weight config": {"type": "flat", "weight": 1.0, "diagonal": False},
+         "arborized config": {"field size": 3, "wrap": True}},
+        {"name": "i_drive", "from layer": "src", "to layer": "iz", "type": "one to one",
+         "opcode": "add", "plastic": False, "direct": True},
+        {"name": "i_gate", "from layer": "aux", "to layer": "iz", "type": "one to one",
+         "opcode": "mult", "plastic": False, "direct": True, "dendrite": "m"},
+        {"name": "i_trace", "from layer": "board", "to layer": "iz", "type": "fully connected",
+         "opcode": "add", "plastic": False, "dendrite": "m"},
+    ]}
+    dend_conns = [c["name"] for c in net["connections"] if c["name"] not in ("nbr",)]
+
+    def inj_dend(rng, sizes):
+        d = {}
+        for name in dend_conns:
+            n = sizes["conn:" + name]
+            d[("matrix", name, "weights")] = rng.uniform(-1.0, 1.0, n).astype(np.float32)
+        d[("matrix", "i_drive", "weights")] = rng.uniform(5.0, 25.0, sizes["conn:i_drive"]).astype(np.float32)
+        d[("matrix", "i_gate", "weights")] = rng.uniform(0.0, 2.0, sizes["conn:i_gate"]).astype(np.float32)
+        d[("matrix", "i_trace", "weights")] = rng.uniform(0.0, 0.01, sizes["conn:i_trace"]).astype(np.float32)
+        # whole history words: bit 0 (the rule's "previously alive") random too
+        d[("neuron", "d", "board", "output")] = rng.integers(0, 2**32, sizes["board"],
+                                                             dtype=np.uint64).astype(np.uint32)
+        return d
+    out.append(Case("dendrites", net, 16, 71, inject=inj_dend,
+                    inputs={"src": lambda rng, t, n: rng.normal(0.0, 1.0, n),
+                            "aux": lambda rng, t, n: rng.normal(0.0, 1.0, n)},
+                    record=[("d", l) for l in ("tree", "rtree", "board", "iz")],
+                    final=[("neuron", "d", l, "input") for l in ("tree", "rtree", "board", "iz")]
+                    + [("neuron", "d", "iz", k) for k in ("voltage", "recovery", "post trace")]
+                    + [("matrix", "i_trace", "short term R")]))
+
+    # --- second-order nodes --------------------------------------------------
+    # so_fc: host + two slaves on g (register 1, not initialised at build);
+    # so_mix: second-order q inside p, and a convolutional host/slave pair on
+    # k; so_sub: subset host and slave of different window shapes.
+    net = {"structures": [{"name": "o", "type": "parallel", "layers": [
+        _layer("src", "relay", 6, 8),
+        _layer("mod", "relay", 6, 8),
+        _layer("m9", "relay", 3, 3),
+        _layer("so_fc", "relay", 4, 5, dendrites=[
+            {"name": "g", "second order": True, "opcode": "add", "init": 0.25}]),
+        _layer("so_mix", "relay", 6, 8, dendrites=[
+            {"name": "p", "opcode": "add", "init": 1.0, "children": [
+                {"name": "q", "second order": True, "opcode": "mult", "init": 1.0}]},
+            {"name": "k", "second order": True, "opcode": "sub"}]),
+        _layer("so_sub", "relay", 4, 6, dendrites=[{"name": "s", "second order": True}]),
+    ]}], "connections": [
+        {"name": "fc_host", "from layer": "src", "to layer": "so_fc", "type": "fully connected",
+         "opcode": "add", "plastic": False, "dendrite": "g"},
+        {"name": "fc_slave1", "from layer": "mod", "to layer": "so_fc", "type": "fully connected",
+         "opcode": "mult", "plastic": False, "dendrite": "g"},
+        {"name": "fc_slave2", "from layer": "src", "to layer": "so_fc", "type": "fully connected",
+         "opcode": "add", "plastic": False, "dendrite": "g"},
+        {"name": "fc_root", "from layer": "mod", "to layer": "so_fc", "type": "fully connected",
+         "opcode": "add", "plastic": False},
+        {"name": "q_host", "from layer": "src", "to layer": "so_mix", "type": "convergent",
+         "opcode": "add", "plastic": False, "dendrite": "q",
+         "arborized config": {"field size": 3, "wrap": True}},
+        {"name": "q_slave", "from layer": "mod", "to layer": "so_mix", "type": "convergent",
+         "opcode": "mult", "plastic": False, "dendrite": "q", "arborized config": conv3},
+        {"name": "p_leaf", "from layer": "mod", "to layer": "so_mix", "type": "one to one",
+         "opcode": "add", "plastic": False, "dendrite": "p"},
+        {"name": "k_host", "from layer": "src", "to layer": "so_mix", "type": "convergent",
+         "convolutional": True, "opcode": "add", "plastic": False, "dendrite": "k",
+         "arborized config": {"field size": 3, "wrap": True}},
+        {"name": "k_slave", "from layer": "m9", "to layer": "so_mix", "type": "convergent",
+         "convolutional": True, "opcode": "mult", "plastic": False, "dendrite": "k",
+         "arborized config": {"field size": 3, "stride": 0, "spacing": 1}},
+        {"name": "s_host", "from layer": "src", "to layer": "so_sub", "type": "subset",
+         "opcode": "add", "plastic": False, "dendrite": "s",
+         "subset config": {"from row start": 0, "from row end": 2, "from column start": 0,
+                           "from column end": 4, "to row start": 0, "to row end": 2,
+                           "to column start": 0, "to column end": 3}},
+        {"name": "s_slave", "from layer": "mod", "to layer": "so_sub", "type": "subset",
+         "opcode": "add", "plastic": False, "dendrite": "s",
+         "subset config": {"from row start": 1, "from row end": 5, "from column start": 2,
+                           "from column end": 5, "to row start": 1, "to row end": 3,
+                           "to column start": 2, "to column end": 4}},
+    ]}
+    so_conns = [c["name"] for c in net["connections"]]
+
+    def inj_so(rng, sizes):
+        d = {}
+        for name in so_conns:
+            n = sizes["conn:" + name]
+            lo, hi = (0.5, 1.5) if name in ("fc_slave1", "q_slave", "k_slave") else (-1.0, 1.0)
+            d[("matrix", name, "weights")] = rng.uniform(lo, hi, n).astype(np.float32)
+        return d
+    out.append(Case("second_order", net, 12, 81, inject=inj_so,
+                    inputs={"src": lambda rng, t, n: rng.normal(0.0, 1.0, n),
+                            "mod": lambda rng, t, n: rng.normal(0.0, 1.0, n),
+                            "m9": lambda rng, t, n: rng.normal(1.0, 0.5, n)},
+                    record=[("o", l) for l in ("so_fc", "so_mix", "so_sub")],
+                    final=[("neuron", "o", l, "input") for l in ("so_fc", "so_mix", "so_sub")]
+                    + [("matrix", c, "weights") for c in ("fc_host", "q_host", "k_host", "s_host")]))
     return out
 
 

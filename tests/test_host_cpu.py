@@ -42,7 +42,7 @@ def test_library_exports_every_header_function(sg):
 
 
 @pytest.mark.parametrize("name", ["iz_opcodes", "iz_plastic", "base_all_types", "iz_c0_8",
-                                  "gol_two_word_history"])
+                                  "gol_two_word_history", "dendrites", "second_order"])
 def test_initial_state_matches_oracle(sg, name):
     from oracle.oracle import OracleNetwork
     from tests.golden.cases import CASES
@@ -102,6 +102,74 @@ def test_invalid_networks_fail_like_the_reference(sg, bad):
     n = sg.Network(bad)
     assert n.obj is None          # create_network returns nullptr
     assert sg.last_error()
+
+
+def _dendrite_net(dendrites, conns, model="relay"):
+    return {"structures": [{"name": "s", "layers": [
+        {"name": "a", "neural model": "relay", "rows": 3, "columns": 3},
+        {"name": "b", "neural model": "relay", "rows": 3, "columns": 3},
+        {"name": "t", "neural model": model, "rows": 3, "columns": 3, "dendrites": dendrites}]}],
+        "connections": conns}
+
+
+_SO = [{"name": "g", "second order": True}]
+_FC = {"from layer": "a", "to layer": "t", "type": "fully connected", "plastic": False}
+
+# Each network breaks one rule of the reference's dendritic trees
+# (layer.cpp:135-153, dendritic_node.cpp:80-140, connection.cpp:149-191).
+DENDRITE_ERRORS = [
+    ("Attempted to dendrite without name", _dendrite_net([{"opcode": "add"}], [])),
+    ("Duplicate dendritic node name", _dendrite_net([{"name": "x"}, {"name": "x"}], [])),
+    ("Duplicate dendritic node name", _dendrite_net([{"name": "root"}], [])),
+    ("cannot have internal children",
+     _dendrite_net([{"name": "g", "second order": True, "children": [{"name": "h"}]}], [])),
+    ("Cannot find Dendritic Node", _dendrite_net([{"name": "x"}], [dict(_FC, dendrite="y")])),
+    ("Plastic second order", _dendrite_net(_SO, [dict(_FC, dendrite="g", plastic=True)])),
+    ("does not match host", _dendrite_net(_SO, [
+        dict(_FC, dendrite="g"),
+        {"from layer": "b", "to layer": "t", "type": "one to one", "plastic": False, "dendrite": "g"}])),
+    ("must have fields that are the size of the input layer", _dendrite_net(_SO, [
+        {"from layer": "a", "to layer": "t", "type": "convergent", "convolutional": True,
+         "plastic": False, "dendrite": "g", "arborized config": {"field size": 3}},
+        {"from layer": "b", "to layer": "t", "type": "convergent", "convolutional": True,
+         "plastic": False, "dendrite": "g", "arborized config": {"field size": 3, "stride": 1}}])),
+]
+
+
+@pytest.mark.parametrize("message,net", DENDRITE_ERRORS)
+def test_invalid_dendritic_trees_fail_like_the_reference(sg, message, net):
+    from oracle.oracle import OracleNetwork
+    n = sg.Network(net)
+    assert n.obj is None and message in sg.last_error(), sg.last_error()
+    with pytest.raises(ValueError, match=message):
+        OracleNetwork(net)
+
+
+def test_izhikevich_second_order_needs_direct_connections(sg):
+    net = _dendrite_net(_SO, [dict(_FC, dendrite="g"), dict(_FC, dendrite="g")], model="izhikevich")
+    n = sg.Network(net)
+    n.build_state()
+    assert n.state is None and "Unimplemented connection type" in sg.last_error()
+    net = _dendrite_net(_SO, [dict(_FC, dendrite="g", direct=True), dict(_FC, dendrite="g", direct=True)],
+                        model="izhikevich")
+    n = sg.Network(net)
+    n.build_state()
+    assert n.state, sg.last_error()
+
+
+def test_dendritic_registers_and_node_names(sg):
+    """Registers follow the config's pre-order; each connection's name
+    (its saved-state key) carries its node."""
+    from oracle.oracle import OracleNetwork
+    net = _dendrite_net([{"name": "p", "children": [{"name": "p1"}, {"name": "p2"}]}, {"name": "q"}],
+                        [dict(_FC, dendrite="p2", name="c1"), dict(_FC, name="c0")])
+    o = OracleNetwork(net)
+    t = o.layer("t")
+    assert [(d.name, d.reg) for d in t.dendrites()] == [("root", 0), ("p", 1), ("q", 4), ("p1", 2), ("p2", 3)]
+    n = sg.Network(net)
+    n.build_state()
+    assert n.get_neuron_data("s", "t", "input").size == 5 * 9
+    assert n.get_neuron_data("s", "a", "input").size == 9
 
 
 def test_izhikevich_gap_must_be_self_connection(sg):
