@@ -208,8 +208,11 @@ class Conn:
         self.second_order = self.node.second_order
         self.so_host = self.second_order and self.node.host is None
         self.so_slave = self.second_order and not self.so_host
-        if p.get_bool("sparse", False) or p.get_bool("randomized projection", False):
-            raise ValueError("oracle: sparse / randomized projections are not restated")
+        self.sparse = p.get_bool("sparse", False) or p.get_bool("randomized projection", False)
+        if self.sparse and self.second_order:
+            raise ValueError("Sparse second order connections are not supported!")
+        if p.get_bool("randomized projection", False):
+            raise ValueError("oracle: randomized projections are not restated")
         c = _Conn()
         c.type, c.opcode, c.convolutional = self.type, self.opcode, int(self.convolutional)
         c.from_rows, c.from_cols, c.to_rows, c.to_cols = frm.rows, frm.cols, to.rows, to.cols
@@ -257,6 +260,7 @@ class Conn:
         else:
             self.num_weights = frm.size * to.size
         c.num_weights = self.num_weights
+        self.dense_num_weights = self.num_weights
         self.c = c
         if self.second_order and self.plastic:  # connection.cpp:149-153
             raise ValueError("Plastic second order connections are not supported!")
@@ -287,6 +291,73 @@ class Conn:
         self.rows = rows.value
         self.nvisits = n
 
+    def sparsify(self, w):
+        """WeightMatrix::sparsify + adjust_sparse_indices (weight_matrix.cpp:
+        510-651, 253-338): keeps each matrix row's nonzero synapses, in order,
+        in a [to_size][kmax] matrix padded with zero weights and -1 indices.
+        The connection becomes SPARSE (connection.cpp:219-222); returns the
+        compacted weights."""
+        if self.convolutional:
+            raise ValueError("Cannot sparsify convolutional weight matrix!")
+        rows, cols = self.matrix_rows_cols()
+        n_dense = self.num_weights
+        nv = self.nvisits
+        wi = self.w_idx[:nv]
+        dst_of_visit = np.repeat(self.dst[:self.rows], np.diff(self.ptr[:self.rows + 1]))
+        fr = np.full(n_dense, -1, np.int64)
+        fc = np.full(n_dense, -1, np.int64)
+        tr = np.full(n_dense, -1, np.int64)
+        tc = np.full(n_dense, -1, np.int64)
+        used = np.zeros(n_dense, bool)
+        fr[wi], fc[wi] = self.pre_row[:nv], self.pre_col[:nv]
+        tr[wi], tc[wi] = dst_of_visit // self.to.cols, dst_of_visit % self.to.cols
+        used[wi] = True
+        visited = used.copy()
+        used &= (w != 0.0)
+        counts = used.reshape(rows, cols).sum(1)
+        kmax = int(counts.max()) if rows else 0
+        if kmax == 0:   # all-zero matrix: one synapse per row, where it exists
+            kmax = 1
+            first = np.arange(rows) * cols
+            used[first] = visited[first]
+        to_size = self.to.size
+        n = kmax * to_size
+        nw = np.zeros(n, np.float32)
+        self.sp_from_row = np.full(n, -1, np.int64)
+        self.sp_from_col = np.full(n, -1, np.int64)
+        self.sp_to_row = np.full(n, -1, np.int64)
+        self.sp_to_col = np.full(n, -1, np.int64)
+        nonzero = np.zeros(to_size, np.int64)
+        for r in range(rows):
+            keep = np.nonzero(used[r * cols:(r + 1) * cols])[0] + r * cols
+            j = r * kmax + np.arange(keep.size)
+            nw[j] = w[keep]
+            self.sp_from_row[j], self.sp_from_col[j] = fr[keep], fc[keep]
+            self.sp_to_row[j], self.sp_to_col[j] = tr[keep], tc[keep]
+            nonzero[r] = keep.size
+        wrap = self.type in (3, 4) and bool(self.c.wrap)
+        frm_rows, frm_cols = self.frm.rows, self.frm.cols
+        a, b = self.sp_from_row.copy(), self.sp_from_col.copy()
+        if wrap:
+            a, b = a % frm_rows, b % frm_cols   # Python's % is already non-negative
+        # the kernel's view (synapse_kernel.h:303-366): row to of the compacted
+        # matrix serves destination to (a subset's window rows land on the
+        # layer's first destinations, as in the reference)
+        self.type = 5
+        self.num_weights = n
+        self.kmax = kmax
+        self.rows = to_size
+        self.dst = np.arange(to_size + 1, dtype=np.int32)
+        self.ptr = np.zeros(to_size + 2, np.int64)
+        self.ptr[1:to_size + 1] = np.cumsum(nonzero)
+        idx = np.concatenate([t * kmax + np.arange(nonzero[t]) for t in range(to_size)] or [np.zeros(0, int)])
+        self.nvisits = idx.size
+        self.w_idx = np.ascontiguousarray(np.append(idx, 0).astype(np.int32))
+        self.from_idx = np.ascontiguousarray(np.append(a[idx] * frm_cols + b[idx], 0).astype(np.int32))
+        self.pre_row = np.ascontiguousarray(np.append(self.sp_from_row[idx], 0).astype(np.int32))
+        self.pre_col = np.ascontiguousarray(np.append(self.sp_from_col[idx], 0).astype(np.int32))
+        return nw
+
     def matrix_rows_cols(self):  # connection.cpp:229-248
         if self.convolutional:
             rows = 1
@@ -308,8 +379,12 @@ class Conn:
 class OracleNetwork:
     """Builds the network and its state from a reference-schema dict."""
 
-    def __init__(self, net, seed=0):
+    def __init__(self, net, seed=0, weight_callbacks=None):
+        """weight_callbacks: {name: fn(id, weights)} for weight configs with a
+        "callback" (weight_matrix.cpp:853-869); fn fills the dense weights in
+        place before any sparsification."""
         self.rng = np.random.default_rng(seed)
+        self.weight_callbacks = weight_callbacks or {}
         top = Props(net)
         self.layers, self.conns, self.structures = [], [], []
         for sp in top.child_arrays.get("structures", []):
@@ -361,7 +436,10 @@ class OracleNetwork:
                              _p(st["voltage"]), _p(st["recovery"]))
             self.neuron[l] = st
         for c in self.conns:
-            self.matrix[c] = m = {"weights": self._init_weights(c)}
+            w = self._init_weights(c)
+            if c.sparse:
+                w = c.sparsify(w)
+            self.matrix[c] = m = {"weights": w}
             if c.so_host:  # weight_matrix.cpp:79-80 (not readable through the getters)
                 self.so_weights[c] = np.zeros(c.num_weights, np.float32)
             if c.to.model == "izhikevich":
@@ -399,6 +477,8 @@ class OracleNetwork:
             w = np.array(vals[:n], np.float32)
         else:
             raise ValueError("oracle: weight config " + t)
+        if wc.has("callback"):
+            self.weight_callbacks[wc.get("callback")](wc.get_int("id", 0), w)
         if not wc.get_bool("diagonal", True):   # weight_matrix.cpp:951-977
             if c.type == 0:
                 w[np.arange(c.frm.size) * c.frm.size + np.arange(c.frm.size)] = 0
@@ -442,6 +522,9 @@ class OracleNetwork:
         fcol[wi] = c.pre_col[:c.nvisits]
         tr[wi] = dst_of_visit // c.to.cols
         tcol[wi] = dst_of_visit % c.to.cols
+        if c.type == 5:   # compacted indices, before wrapping, -1 pads
+            fr, fcol = c.sp_from_row.astype(np.int32), c.sp_from_col.astype(np.int32)
+            tr, tcol = c.sp_to_row.astype(np.int32), c.sp_to_col.astype(np.int32)
         dist = np.zeros(n, np.float32)
         delays = np.zeros(n, np.int32)
         rc = lib().sg_distance_delays(

@@ -669,6 +669,7 @@ class IzhikevichModel : public Model {
                 case 2: k_iz_gap<2><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), reg); break;
                 case 3: k_iz_gap<3><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), reg); break;
                 case 4: k_iz_gap<4><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), reg); break;
+                case 5: k_iz_gap<5><<<blocks, threads, 0, ctx.stream>>>(cs.geom, to.var("voltage")->df(), cs.weights->df(), reg); break;
             }
             SG_LAUNCH_CHECK();
             ctx.count();

@@ -26,7 +26,7 @@ Opcode parse_opcode(const std::string& s) {
 }
 const char* conn_type_name(ConnType t) {
     for (auto& p : kConnTypes) if (p.second == t) return p.first.c_str();
-    return "?";
+    return t == SPARSE ? "sparse" : "?";
 }
 const char* opcode_name(Opcode o) {
     for (auto& p : kOpcodes) if (p.second == o) return p.first.c_str();
@@ -264,11 +264,11 @@ void Network::add_connection(const Props& p) {
     c->opcode = parse_opcode(p.get("opcode", "add"));
     c->convolutional = p.get_bool("convolutional", false);
     if (c->delay < 0) throw SgError("Attempted to construct ConnectionConfig with negative delay!");
-    if (p.get_bool("sparse", false) || p.get_bool("randomized projection", false)) {
-        if (c->second_order)
-            throw SgError("Error in " + c->str() + ":\n  Sparse second order connections are not supported!");
-        throw SgError(c->str() + ": sparse connections are not supported");
-    }
+    c->sparse = p.get_bool("sparse", false) || p.get_bool("randomized projection", false);
+    if (c->sparse && c->second_order)
+        throw SgError("Error in " + c->str() + ":\n  Sparse second order connections are not supported!");
+    if (p.get_bool("randomized projection", false))
+        throw SgError(c->str() + ": randomized projections are not supported");
     if (c->convolutional && c->type != CONVERGENT && c->type != DIVERGENT)
         throw SgError("Only convergent/divergent connections can be convolutional!");
     Layer *from = c->from, *to = c->to;
@@ -311,6 +311,10 @@ void Network::add_connection(const Props& p) {
         }
     }
     if (c->num_weights >= (1L << 31)) throw SgError(c->str() + ": more than 2^31 weights");
+    c->dense_type = c->type;
+    c->dense_num_weights = c->num_weights;
+    c->dense_rows = c->matrix_rows;
+    c->dense_cols = c->matrix_cols;
     // second-order rules (connection.cpp:149-191)
     if (c->second_order && c->plastic)
         throw SgError("Error in " + c->str() + ":\n  Plastic second order connections are not supported!");

@@ -14,7 +14,10 @@
 namespace sg {
 
 enum OutputType { OUT_FLOAT = 0, OUT_BIT = 1, OUT_INT = 2 };
-enum ConnType { FULLY_CONNECTED = 0, SUBSET = 1, ONE_TO_ONE = 2, CONVERGENT = 3, DIVERGENT = 4 };
+// SPARSE is internal (util/constants.h:71-78): a "sparse" connection takes it
+// when its state is built and its zero weights are compacted away.
+enum ConnType { FULLY_CONNECTED = 0, SUBSET = 1, ONE_TO_ONE = 2, CONVERGENT = 3, DIVERGENT = 4,
+                SPARSE = 5 };
 enum Opcode {
     OP_ADD = 0, OP_SUB, OP_MULT, OP_DIV, OP_POOL, OP_REWARD, OP_MODULATE, OP_GAP,
     OP_ADD_HEAVISIDE, OP_SUB_HEAVISIDE, OP_MULT_HEAVISIDE
@@ -44,6 +47,17 @@ struct SubsetCfg {
 struct Structure;
 struct Connection;
 struct Layer;
+
+// Compacted synapse table of a sparse connection (weight_matrix.cpp:510-651,
+// 253-338): destination to keeps its nonzero[to] synapses first in row
+// to of a [to_size][kmax] matrix, in the dense matrix's order; -1 pads.
+struct SparseTable {
+    int kmax = 0;
+    std::vector<int> nonzero;             // [to_size]
+    std::vector<int> from;                // [to_size * kmax] source index, wrapped
+    // Indices before wrapping (what distances are measured from), -1 pads.
+    std::vector<int> from_row, from_col, to_row, to_col;
+};
 
 // A node of a layer's dendritic tree (network/dendritic_node.cpp:5-146).
 // The root owns input register 0; every internal node gets its own register,
@@ -114,6 +128,15 @@ struct Connection {
     bool convolutional = false;
     Arbor arbor;
     SubsetCfg subset;
+    bool sparse = false;                // "sparse": compacted at state build
+    // Set while a state is built from this network, like the reference's
+    // Connection::sparsify (connection.cpp:219-222): type SPARSE, num_weights
+    // and matrix_cols of the compacted matrix, and its table.  The dense
+    // description is kept so that another state can be built.
+    std::shared_ptr<SparseTable> sparse_table;
+    ConnType dense_type = FULLY_CONNECTED;
+    long dense_num_weights = 0;
+    int dense_rows = 0, dense_cols = 0;
     Dendrite* node = nullptr;           // dendritic node it feeds
     bool second_order = false;          // on a second-order node
     bool second_order_host = false;     // that node's first connection

@@ -46,6 +46,7 @@ DGeom make_geom(const Connection& c) {
     g.tk_cols = s.tc1 - s.tc0;
     g.tk_size = s.to_size();
     g.n_dest = c.dest_count();
+    g.kmax = c.sparse_table ? c.sparse_table->kmax : 0;
     // Range of source coordinates before wrapping, per axis.
     g.wrap_fast = 0;
     if (c.type == CONVERGENT || c.type == DIVERGENT) {
@@ -81,6 +82,13 @@ State::~State() {
     if (arena_) cudaFree(arena_);
 }
 
+void State::remove_array(Array* a) {
+    if (arena_) throw SgError("state arrays cannot be removed after device allocation");
+    arrays_.erase(std::remove_if(arrays_.begin(), arrays_.end(),
+                                 [a](const std::unique_ptr<Array>& p) { return p.get() == a; }),
+                  arrays_.end());
+}
+
 Array* State::add_array(const std::string& name, char dtype, size_t count, ArrayLayout layout,
                         int rows, int cols, size_t dev_count) {
     if (arena_) throw SgError("state arrays cannot be added after device allocation");
@@ -100,6 +108,16 @@ Array* State::add_array(const std::string& name, char dtype, size_t count, Array
 }
 
 void State::build() {
+    // a sparse connection is compacted anew from this state's weights
+    for (auto& cp : network->connections) {
+        Connection* c = cp.get();
+        if (!c->sparse) continue;
+        c->type = c->dense_type;
+        c->num_weights = c->dense_num_weights;
+        c->matrix_rows = c->dense_rows;
+        c->matrix_cols = c->dense_cols;
+        c->sparse_table.reset();
+    }
     for (auto& lp : network->layers) {
         Layer* l = lp.get();
         auto ls = std::make_unique<LayerState>();
@@ -143,7 +161,10 @@ void State::build() {
     // all matrices of a layer are created with the layer's attributes
     // (attributes.cpp:31-36), then processed (state.cpp:98-106).
     for (auto& lp : network->layers) {
-        for (Connection* c : lp->inputs) init_weights(*this, *conns[c->index]);
+        for (Connection* c : lp->inputs) {
+            init_weights(*this, *conns[c->index]);
+            if (c->sparse) sparsify(*this, *conns[c->index]);
+        }
         for (Connection* c : lp->inputs)
             find_model(lp->model)->build_matrix(*this, *conns[c->index]);
     }
@@ -188,6 +209,11 @@ void State::allocate_device() {
     // legacy-stream memset, so it completes before any upload or kernel
     SG_CUDA(cudaDeviceSynchronize());
     for (auto& a : arrays_) a->dev = static_cast<char*>(arena_) + a->dev_offset;
+    for (auto& cs : conns)
+        if (cs->sparse_nonzero) {
+            cs->geom.nz = cs->sparse_nonzero->di();
+            cs->geom.sfrom = cs->sparse_from->di();
+        }
 }
 
 static bool needs_transpose(const Array& a) {

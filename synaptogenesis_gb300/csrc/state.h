@@ -94,6 +94,10 @@ struct ConnState {
     // Second-order slave whose device layout differs from the host's (subset
     // windows of another shape): host device index of each slave device index.
     Array* so_remap = nullptr;
+    // Sparse connection: synapses per destination ([to_size]) and each
+    // synapse's source (same layout as the weights).
+    Array* sparse_nonzero = nullptr;
+    Array* sparse_from = nullptr;
     Array* var(const std::string& k) const;
 };
 
@@ -113,6 +117,7 @@ class State {
     Array* add_array(const std::string& name, char dtype, size_t count,
                      ArrayLayout layout = LAYOUT_PLAIN, int rows = 1, int cols = 1,
                      size_t dev_count = 0);
+    void remove_array(Array* a);
 
     // Host <-> device movement.
     void to_device(cudaStream_t stream);     // uploads if the host copy is newer

@@ -7,6 +7,7 @@
 //   one to one       the destination itself                 :257-286
 //   convergent       kernel rows/cols, wrap or skip          :384-461
 //   divergent        inverse window, C truncating division   :506-581
+//   sparse           the destination's compacted synapses    :303-366
 // Weight indices are in the device layout.  Fully connected and subset
 // matrices are stored in bands of kBand consecutive destinations,
 // [destination / kBand][source][destination % kBand] (banded_index), so the
@@ -18,6 +19,7 @@
 //   one to one       w[i]
 //   convergent       w[k * to_size + to]   (convolutional: w[k])
 //   divergent        w[k * to_size + to]   (convolutional: w[k])
+//   sparse           w[k * to_size + to]
 // Floating-point order is the reference's serial order; the library is built
 // with --fmad=false so no multiply-add is contracted.
 #pragma once
@@ -35,9 +37,14 @@ struct DGeom {
     // Every wrapped source coordinate lies in [-n, 2n): one conditional add or
     // subtract gives the same result as ((x % n) + n) % n.
     int wrap_fast;
+    // Sparse: synapses per destination and their sources, [k][to] like the
+    // weights (device pointers, set once the state is on the device).
+    int kmax;
+    const int* nz;
+    const int* sfrom;
 };
 
-enum { T_FC = 0, T_SUBSET = 1, T_ONE = 2, T_CONV = 3, T_DIV = 4 };
+enum { T_FC = 0, T_SUBSET = 1, T_ONE = 2, T_CONV = 3, T_DIV = 4, T_SPARSE = 5 };
 
 constexpr int kBand = 8;
 
@@ -128,6 +135,10 @@ __device__ __forceinline__ void for_each_source(const DGeom& g, int d, F&& f) {
                 f(fr * g.from_cols + fc, g.conv ? k : k * g.to_size + d);
             }
         }
+    } else if (TYPE == T_SPARSE) {
+        const int n = g.nz[d];
+        int wi = d;
+        for (int i = 0; i < n; ++i, wi += g.to_size) f(g.sfrom[wi], wi);
     } else {  // T_DIV
         const int tr = d / g.to_cols, tc = d % g.to_cols;
         const int sr0 = (tr + g.rsp * (-g.ro - g.rf + g.rs)) / g.rs;
@@ -171,6 +182,9 @@ __device__ __forceinline__ void for_each_source(const DGeom& g, int d, F&& f) {
         case 12: { constexpr int TY = 4, SR = 0; BODY; } break;                       \
         case 13: { constexpr int TY = 4, SR = 1; BODY; } break;                       \
         case 14: { constexpr int TY = 4, SR = 2; BODY; } break;                       \
+        case 15: { constexpr int TY = 5, SR = 0; BODY; } break;                       \
+        case 16: { constexpr int TY = 5, SR = 1; BODY; } break;                       \
+        case 17: { constexpr int TY = 5, SR = 2; BODY; } break;                       \
     }
 
 }  // namespace sg

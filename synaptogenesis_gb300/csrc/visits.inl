@@ -1,7 +1,8 @@
 // Host-side serial enumeration of a connection's synapse visits (host layout
 // weight indices), in the reference's loop order:
 //   src/core/engine/kernel/synapse_kernel.h:115-149 (FC), :182-228 (subset),
-//   :257-286 (one to one), :384-461 (convergent), :506-581 (divergent).
+//   :257-286 (one to one), :384-461 (convergent), :506-581 (divergent),
+//   :303-366 (sparse: each destination's compacted synapses).
 #pragma once
 
 namespace sg {
@@ -79,6 +80,15 @@ void enumerate_visits(const Connection& c, F&& f) {
                             f(to, to, fr * fl.cols + fc, woff + k, sr, sc);
                         }
                 }
+            break;
+        }
+        case SPARSE: {
+            const SparseTable& t = *c.sparse_table;
+            for (int to = 0; to < tl.size; ++to) {
+                long wi = (long)to * t.kmax;
+                for (int i = 0; i < t.nonzero[to]; ++i, ++wi)
+                    f(to, to, t.from[wi], wi, t.from_row[wi], t.from_col[wi]);
+            }
             break;
         }
     }

@@ -1,6 +1,8 @@
 #include "weight_init.h"
 
+#include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <sstream>
 
 #include "callbacks.h"
@@ -20,6 +22,20 @@ std::mt19937_64 make_rng(const Props& cfg, uint64_t salt) {
 Indices compute_indices(const Connection& c) {
     Indices ix;
     size_t n = c.num_weights;
+    if (c.type == SPARSE) {      // the compacted indices, as before wrapping
+        const SparseTable& t = *c.sparse_table;
+        const int fcols = c.from->cols, tcols = c.to->cols;
+        ix.from_row = t.from_row; ix.from_col = t.from_col;
+        ix.to_row = t.to_row; ix.to_col = t.to_col;
+        ix.from_index.assign(n, -1); ix.to_index.assign(n, -1); ix.used.assign(n, 0);
+        for (size_t i = 0; i < n; ++i) {
+            if (t.to_row[i] < 0) continue;
+            ix.from_index[i] = t.from_row[i] * fcols + t.from_col[i];
+            ix.to_index[i] = t.to_row[i] * tcols + t.to_col[i];
+            ix.used[i] = 1;
+        }
+        return ix;
+    }
     ix.from_row.assign(n, -1); ix.from_col.assign(n, -1); ix.from_index.assign(n, -1);
     ix.to_row.assign(n, -1); ix.to_col.assign(n, -1); ix.to_index.assign(n, -1);
     ix.used.assign(n, 0);
@@ -224,6 +240,105 @@ void init_weights(State& st, ConnState& cs) {
     if (Props* m = cfg.child("circular mask")) circular_mask(c, *m, w);
     for (Props* m : cfg.child_array("circular mask")) circular_mask(c, *m, w);
     if (!cfg.get_bool("diagonal", true)) clear_diagonal(c, w);
+}
+
+// ---------------------------------------------------------------------------
+// WeightMatrix::sparsify and adjust_sparse_indices (weight_matrix.cpp:510-651,
+// 253-338), run when the dense weights (and any callback delays or
+// distances) are in place, before the model processes the matrix.
+// ---------------------------------------------------------------------------
+void sparsify(State& st, ConnState& cs) {
+    Connection& c = *cs.conn;
+    if (c.convolutional)
+        throw SgError("Error intializing weight matrix for " + c.str() +
+                      "\n   Cannot sparsify convolutional weight matrix!");
+    const int rows = c.matrix_rows, cols = c.matrix_cols, to_size = c.to->size;
+    const float* w = cs.weights->hf();
+    Indices ix = compute_indices(c);
+    std::vector<int> used(ix.used);
+    int kmax = 0;
+    for (int r = 0; r < rows; ++r) {
+        int nz = 0;
+        for (int k = 0; k < cols; ++k) {
+            size_t i = (size_t)r * cols + k;
+            if (w[i] == 0.0f) used[i] = 0;
+            nz += used[i];
+        }
+        kmax = std::max(kmax, nz);
+    }
+    if (kmax == 0) {
+        // an all-zero matrix keeps one synapse per row (its first weight
+        // position); rows whose first position is no synapse stay empty
+        // instead of reading outside the source layer
+        kmax = 1;
+        for (int r = 0; r < rows; ++r) used[(size_t)r * cols] = ix.used[(size_t)r * cols];
+    }
+    const size_t n = (size_t)kmax * to_size;
+    auto t = std::make_shared<SparseTable>();
+    t->kmax = kmax;
+    t->nonzero.assign(to_size, 0);
+    t->from.assign(n, -1);
+    t->from_row.assign(n, -1); t->from_col.assign(n, -1);
+    t->to_row.assign(n, -1); t->to_col.assign(n, -1);
+    std::vector<float> nw(n, 0.0f);
+    std::vector<size_t> old_of(n, (size_t)-1);
+    for (int r = 0; r < rows; ++r) {
+        int k = 0;
+        for (int col = 0; col < cols; ++col) {
+            size_t i = (size_t)r * cols + col;
+            if (!used[i]) continue;
+            size_t j = (size_t)r * kmax + k++;
+            nw[j] = w[i];
+            old_of[j] = i;
+            t->from_row[j] = ix.from_row[i]; t->from_col[j] = ix.from_col[i];
+            t->to_row[j] = ix.to_row[i]; t->to_col[j] = ix.to_col[i];
+        }
+        t->nonzero[r] = k;
+    }
+    // wrapped source indices for the kernels (adjust_sparse_indices); a
+    // non-wrapping arbor never keeps a synapse outside the source layer
+    const bool wrap = (c.dense_type == CONVERGENT || c.dense_type == DIVERGENT) && c.arbor.wrap;
+    const int fr = c.from->rows, fc = c.from->cols;
+    for (size_t j = 0; j < n; ++j) {
+        if (t->to_row[j] < 0) continue;                 // padding
+        int a = t->from_row[j], b = t->from_col[j];
+        if (wrap) { a = (a % fr + fr) % fr; b = (b % fc + fc) % fc; }
+        else if (a < 0 || a >= fr || b < 0 || b >= fc)
+            throw SgError(c.str() + ": sparse synapse outside the source layer");
+        t->from[j] = a * fc + b;
+    }
+    // compact the callback-set per-synapse arrays the same way
+    auto compact = [&](const uint32_t* src, uint32_t fill) {
+        std::vector<uint32_t> out(n, fill);
+        for (size_t j = 0; j < n; ++j) if (old_of[j] != (size_t)-1) out[j] = src[old_of[j]];
+        return out;
+    };
+    if (!cs.cached_distances.empty()) {
+        std::vector<float> d(n, 0.0f);
+        for (size_t j = 0; j < n; ++j) if (old_of[j] != (size_t)-1) d[j] = cs.cached_distances[old_of[j]];
+        cs.cached_distances = std::move(d);
+    }
+    std::vector<uint32_t> delays;
+    if (cs.delays) delays = compact(cs.delays->hu(), 0u);
+    // Connection::sparsify: the compacted shape (connection.cpp:219-222)
+    c.type = SPARSE;
+    c.num_weights = (long)n;
+    c.matrix_rows = to_size;
+    c.matrix_cols = kmax;
+    c.sparse_table = t;
+    st.remove_array(cs.weights);
+    cs.weights = st.add_array("weights", 'f', n, matrix_layout(c), c.matrix_rows, c.matrix_cols);
+    std::memcpy(cs.weights->hf(), nw.data(), n * 4);
+    if (cs.delays) {
+        st.remove_array(cs.delays);
+        cs.delays = st.add_array("delays", 'i', n, matrix_layout(c), c.matrix_rows, c.matrix_cols);
+        std::memcpy(cs.delays->hu(), delays.data(), n * 4);
+    }
+    cs.sparse_nonzero = st.add_array("nonzero counts", 'i', to_size);
+    std::memcpy(cs.sparse_nonzero->hi(), t->nonzero.data(), (size_t)to_size * 4);
+    cs.sparse_from = st.add_array("from indices", 'i', n, matrix_layout(c), c.matrix_rows, c.matrix_cols);
+    std::memcpy(cs.sparse_from->hi(), t->from.data(), n * 4);
+    cs.geom = make_geom(c);
 }
 
 }  // namespace sg

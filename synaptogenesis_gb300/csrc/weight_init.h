@@ -19,6 +19,9 @@ uint64_t global_seed();
 std::mt19937_64 make_rng(const Props& cfg, uint64_t salt);
 
 void init_weights(State& st, ConnState& cs);
+// Compacts a "sparse" connection's initialised weights (and any callback
+// delays / distances): the connection becomes SPARSE.
+void sparsify(State& st, ConnState& cs);
 
 // Pre-wrap source / destination coordinates per weight (host layout), as the
 // reference's index kernels leave them (weight_matrix.cpp:1039-1195).

@@ -40,6 +40,29 @@ class Case:
         return self.inject(_rng(self.seed), sizes)
 
 
+def callback_injections(net, injections):
+    """Moves the injections that must happen while a state is built into
+    weight-config callbacks, as the reference's front-end offers them
+    (weight_matrix.cpp:853-869, 930-949): ("matrix", c, "init weights") sets
+    the dense weights before a sparse connection is compacted, and
+    ("matrix", c, "delays") the per-synapse delays.  Returns the rewritten
+    network, the remaining injections and {id: array} per callback kind; a
+    connection's id is its position in the network."""
+    import copy
+    net = copy.deepcopy(net)
+    rest = dict(injections)
+    weights, delays = {}, {}
+    for i, c in enumerate(net["connections"]):
+        for key, kind, store in ((("matrix", c["name"], "init weights"), "callback", weights),
+                                 (("matrix", c["name"], "delays"), "delay callback", delays)):
+            if key in rest:
+                wc = c.setdefault("weight config", {"type": "flat", "weight": 1.0})
+                wc[kind] = "golden_weight" if kind == "callback" else "golden_delay"
+                wc["id"] = i
+                store[i] = rest.pop(key)
+    return net, rest, weights, delays
+
+
 def _layer(name, model, rows, cols, **kw):
     d = {"name": name, "neural model": model, "rows": rows, "columns": cols}
     d.update(kw)
@@ -456,6 +479,75 @@ def cases():
                     record=[("o", l) for l in ("so_fc", "so_mix", "so_sub")],
                     final=[("neuron", "o", l, "input") for l in ("so_fc", "so_mix", "so_sub")]
                     + [("matrix", c, "weights") for c in ("fc_host", "q_host", "k_host", "s_host")]))
+
+    # --- sparse connections --------------------------------------------------
+    # Dense weights with zeros go in through a weight callback before the
+    # state compacts them: fully connected, wrapping and clipped convergent,
+    # divergent, subset (its window rows serve the layer's first
+    # destinations, as in the reference), one to one, an all-zero matrix,
+    # and plastic / non-plastic Izhikevich connections with distance delays.
+    net = {"structures": [{"name": "p", "type": "parallel", "layers": [
+        _layer("src", "relay", 6, 8),
+        _layer("sfc", "relay", 5, 6),
+        _layer("sconv", "relay", 6, 8),
+        _layer("sdiv", "rate_encoding", 12, 16),
+        _layer("ssub", "relay", 4, 6),
+        _layer("sone", "relay", 6, 8),
+        _layer("iz_in", "relay", 8, 8),
+        _layer("iz", "izhikevich", 8, 8),
+    ]}], "connections": [
+        {"name": "p_fc", "from layer": "src", "to layer": "sfc", "type": "fully connected",
+         "opcode": "add", "plastic": False, "sparse": True},
+        {"name": "p_conv_wrap", "from layer": "src", "to layer": "sconv", "type": "convergent",
+         "opcode": "add", "plastic": False, "sparse": True,
+         "arborized config": {"field size": 3, "wrap": True}},
+        {"name": "p_conv_clip", "from layer": "src", "to layer": "sconv", "type": "convergent",
+         "opcode": "sub", "plastic": False, "sparse": True,
+         "arborized config": {"field size": 5, "spacing": 2, "wrap": False}},
+        {"name": "p_div", "from layer": "src", "to layer": "sdiv", "type": "divergent",
+         "opcode": "add", "plastic": False, "sparse": True,
+         "arborized config": {"field size": 3, "stride": 2, "wrap": True}},
+        {"name": "p_sub", "from layer": "src", "to layer": "ssub", "type": "subset",
+         "opcode": "add", "plastic": False, "sparse": True,
+         "subset config": {"from row start": 1, "from row end": 5, "from column start": 2,
+                           "from column end": 7, "to row start": 1, "to row end": 4,
+                           "to column start": 2, "to column end": 6}},
+        {"name": "p_one", "from layer": "src", "to layer": "sone", "type": "one to one",
+         "opcode": "add", "plastic": False, "sparse": True},
+        {"name": "p_zero", "from layer": "src", "to layer": "sone", "type": "fully connected",
+         "opcode": "sub", "plastic": False, "sparse": True},
+        {"name": "i_drive", "from layer": "iz_in", "to layer": "iz", "type": "one to one",
+         "opcode": "add", "plastic": False, "direct": True},
+        {"name": "i_ff", "from layer": "iz_in", "to layer": "iz", "type": "fully connected",
+         "opcode": "add", "plastic": False, "sparse": True},
+        {"name": "i_rec", "from layer": "iz", "to layer": "iz", "type": "convergent",
+         "opcode": "add", "plastic": True, "sparse": True, "max weight": 0.5,
+         "arborized config": {"field size": 5, "wrap": True}},
+    ]}
+    sparse_conns = [c["name"] for c in net["connections"] if c.get("sparse")]
+
+    def inj_sparse(rng, sizes):
+        d = {}
+        for name in sparse_conns:
+            n = sizes["dense:" + name]
+            w = rng.uniform(-1.0, 1.0, n).astype(np.float32)
+            if name in ("i_ff", "i_rec"):
+                w = np.abs(w) * np.float32(0.02 if name == "i_ff" else 0.3)
+            w[rng.random(n) < 0.5] = 0.0
+            if name == "p_zero":
+                w[:] = 0.0
+            d[("matrix", name, "init weights")] = w
+        d[("matrix", "i_drive", "weights")] = np.full(64, 1.0, np.float32)
+        return d
+    out.append(Case("sparse", net, 60, 91, inject=inj_sparse,
+                    inputs={"src": lambda rng, t, n: rng.normal(0.0, 1.0, n),
+                            "iz_in": lambda rng, t, n: (rng.random(n) < 0.15) * 12.0},
+                    record=[("p", l) for l in ("sfc", "sconv", "sdiv", "ssub", "sone", "iz")],
+                    final=[("neuron", "p", l, "input") for l in ("sfc", "sconv", "sdiv", "ssub", "sone")]
+                    + [("neuron", "p", "iz", k) for k in ("voltage", "recovery", "post trace")]
+                    + [("matrix", c, k) for c in ("i_rec", "i_ff")
+                       for k in ("weights", "short term w", "short term R", "presyn trace")]
+                    + [("matrix", c, "weights") for c in ("p_fc", "p_div", "p_sub", "p_zero")]))
     return out
 
 

@@ -24,7 +24,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, HERE)
 
-from cases import CASES  # noqa: E402
+from cases import CASES, callback_injections  # noqa: E402
 
 
 def load_reference_syngen():
@@ -46,23 +46,22 @@ def case_sizes(case):
     onet = OracleNetwork(case.net)
     sizes = {l.name: l.size for l in onet.layers}
     sizes.update({"conn:" + c.name: c.num_weights for c in onet.conns})
+    sizes.update({"dense:" + c.name: c.dense_num_weights for c in onet.conns})
     return sizes
 
 
 def run_case(sg, case):
     sizes = case_sizes(case)
-    injections = case.injections(sizes)
     # Delays are not a readable/writable weight-matrix variable in the
-    # reference; they go in through a delay callback at build time.
-    net_dict = copy.deepcopy(case.net)
-    delay_arrays = []
-    for c in net_dict["connections"]:
-        key = ("matrix", c["name"], "delays")
-        if key in injections:
-            wc = c.setdefault("weight config", {"type": "flat", "weight": 1.0})
-            wc["delay callback"] = "golden_delay"
-            wc["id"] = len(delay_arrays)
-            delay_arrays.append(injections.pop(key))
+    # reference, and a sparse connection's dense weights exist only while its
+    # state is built: both go in through weight-config callbacks.
+    net_dict, injections, weight_arrays, delay_arrays = callback_injections(
+        case.net, case.injections(sizes))
+
+    def weight_cb(ID, size, weights):
+        arr = weight_arrays[ID]
+        assert size == arr.size
+        sg.FloatArray(size, weights).to_np_array()[:] = arr
 
     def delay_cb(ID, size, weights, delays):
         arr = delay_arrays[ID]
@@ -70,10 +69,15 @@ def run_case(sg, case):
         sg.IntArray(size, delays).to_np_array()[:] = arr
 
     sg._delay_weight_callbacks = {}     # the reference front-end never defines it
+    if not hasattr(sg, "_weight_callbacks"):
+        sg._weight_callbacks = {}
+    sg.create_weight_callback("golden_weight", weight_cb)
     sg.create_delay_weight_callback("golden_delay", delay_cb)
     net = sg.Network(net_dict)
     net.build_state()
     for c in case.net["connections"]:
+        if c.get("sparse"):
+            continue
         got = net.get_weight_matrix(c["name"], "weights").size
         assert got == sizes["conn:" + c["name"]], (c["name"], got)
     for key, arr in injections.items():

@@ -18,6 +18,7 @@ def case_sizes(case):
     onet = OracleNetwork(case.net)
     sizes = {l.name: l.size for l in onet.layers}
     sizes.update({"conn:" + c.name: c.num_weights for c in onet.conns})
+    sizes.update({"dense:" + c.name: c.dense_num_weights for c in onet.conns})
     return sizes
 
 
@@ -29,10 +30,20 @@ def _as_u32(a):
 def run_oracle(case, steps=None):
     """Runs ``case`` on the CPU oracle; returns the fixture-shaped dict."""
     from oracle.oracle import OracleNetwork
+    from tests.golden.cases import callback_injections
     steps = case.steps if steps is None else steps
-    net = OracleNetwork(case.net)
     sizes = case_sizes(case)
-    for key, arr in case.injections(sizes).items():
+    injections = case.injections(sizes)
+    # dense weights of sparse connections through the weight callback; the
+    # other injections go into the built state
+    _, _, weight_arrays, _ = callback_injections(case.net, injections)
+    net_dict, _, _, _ = callback_injections(
+        case.net, {k: v for k, v in injections.items() if k[2] == "init weights"})
+    net = OracleNetwork(net_dict, weight_callbacks={
+        "golden_weight": lambda ID, w: w.__setitem__(slice(None), weight_arrays[ID])})
+    for key, arr in injections.items():
+        if key[2] == "init weights":
+            continue
         if key[0] == "neuron":
             dst = net.get_neuron_data(key[2], key[3])
         else:
@@ -57,23 +68,19 @@ def run_oracle(case, steps=None):
 def run_library(case, syngen, steps=None, extra_args=None):
     """Runs ``case`` through the drop-in front-end ``syngen`` (either library);
     ``extra_args`` are added to the run arguments."""
+    from tests.golden.cases import callback_injections
     steps = case.steps if steps is None else steps
     sizes = case_sizes(case)
-    injections = case.injections(sizes)
-    import copy
-    net_dict = copy.deepcopy(case.net)
-    delay_arrays = []
-    for c in net_dict["connections"]:
-        key = ("matrix", c["name"], "delays")
-        if key in injections:
-            wc = c.setdefault("weight config", {"type": "flat", "weight": 1.0})
-            wc["delay callback"] = "golden_delay"
-            wc["id"] = len(delay_arrays)
-            delay_arrays.append(injections.pop(key))
+    net_dict, injections, weight_arrays, delay_arrays = callback_injections(
+        case.net, case.injections(sizes))
+
+    def weight_cb(ID, size, weights):
+        syngen.FloatArray(size, weights).to_np_array()[:] = weight_arrays[ID]
 
     def delay_cb(ID, size, weights, delays):
         syngen.IntArray(size, delays).to_np_array()[:] = delay_arrays[ID]
 
+    syngen.create_weight_callback("golden_weight", weight_cb)
     syngen.create_delay_weight_callback("golden_delay", delay_cb)
     net = syngen.Network(net_dict)
     net.build_state()

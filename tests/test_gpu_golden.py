@@ -15,7 +15,7 @@ from tests.harness import compare, float_like_keys, load_fixture, run_library, r
 
 pytestmark = pytest.mark.gpu
 
-RATE_KEYS = ("rec/s/one", "rec/s/div", "rec/d/rtree")
+RATE_KEYS = ("rec/s/one", "rec/s/div", "rec/d/rtree", "rec/p/sdiv")
 RATE_TOL = 1e-5
 
 
@@ -88,12 +88,12 @@ def test_overlapped_learning_matches_oracle(syngen, overlap):
 
 
 @pytest.mark.parametrize("graphs", [True, False])
-@pytest.mark.parametrize("name", ["dendrites", "second_order"])
-def test_dendritic_trees_without_environment(syngen, name, graphs):
-    """The dendritic-tree and second-order cases with no I/O modules (so the
-    engine captures its steps in CUDA graphs, or not), their source layers
-    driven by flat init configs: bit-exact against the oracle over twice the
-    fixture's steps, rate_encoding outputs within RATE_TOL (tanhf)."""
+@pytest.mark.parametrize("name", ["dendrites", "second_order", "sparse"])
+def test_cases_without_environment(syngen, name, graphs):
+    """The dendritic-tree, second-order and sparse cases with no I/O modules
+    (so the engine captures its steps in CUDA graphs, or not), their source
+    layers driven by flat init configs: bit-exact against the oracle over
+    twice the fixture's steps, rate_encoding outputs within RATE_TOL (tanhf)."""
     import copy
 
     from tests.golden.cases import Case
@@ -109,6 +109,7 @@ def test_dendritic_trees_without_environment(syngen, name, graphs):
     case = Case(name + "_no_env", net, 2 * base.steps, base.seed, inject=base.inject, final=final)
     got = run_library(case, syngen, extra_args={"graphs": graphs})
     want = run_oracle(case)
-    problems = compare(got, want, tol=RATE_TOL, float_keys=("neuron/d/rtree/output",),
+    problems = compare(got, want, tol=RATE_TOL,
+                       float_keys=("neuron/d/rtree/output", "neuron/p/sdiv/output"),
                        nan_keys=float_like_keys(case))
     assert not problems, problems

@@ -42,7 +42,7 @@ def test_library_exports_every_header_function(sg):
 
 
 @pytest.mark.parametrize("name", ["iz_opcodes", "iz_plastic", "base_all_types", "iz_c0_8",
-                                  "gol_two_word_history", "dendrites", "second_order"])
+                                  "gol_two_word_history", "dendrites", "second_order", "sparse"])
 def test_initial_state_matches_oracle(sg, name):
     from oracle.oracle import OracleNetwork
     from tests.golden.cases import CASES
@@ -61,6 +61,37 @@ def test_initial_state_matches_oracle(sg, name):
             assert got.size == v.size or k == "time since spike", (c.name, k)
             if k != "weights":
                 assert np.array_equal(got.view(np.uint32)[:v.size], v.view(np.uint32)), (c.name, k)
+
+
+def test_sparse_compaction_matches_oracle(sg):
+    """Sparse connections compacted from dense weights set by a weight
+    callback: every per-synapse array (compacted weights, distance delays
+    with their -1 padding, Izhikevich variables) equals the oracle's."""
+    from oracle.oracle import OracleNetwork
+    from tests.golden.cases import CASES, callback_injections
+    from tests.harness import case_sizes
+    case = CASES["sparse"]
+    net_dict, _, weights, _ = callback_injections(
+        case.net, {k: v for k, v in case.injections(case_sizes(case)).items()
+                   if k[2] == "init weights"})
+
+    def weight_cb(ID, size, ptr):
+        sg.FloatArray(size, ptr).to_np_array()[:] = weights[ID]
+
+    sg.create_weight_callback("golden_weight", weight_cb)
+    net = sg.Network(net_dict)
+    net.build_state()
+    assert net.state, sg.last_error()
+    onet = OracleNetwork(net_dict, weight_callbacks={
+        "golden_weight": lambda ID, w: w.__setitem__(slice(None), weights[ID])})
+    for c in onet.conns:
+        for k, v in onet.matrix[c].items():
+            got = net.get_weight_matrix(c.name, k).to_np_array()
+            n = v.size if k == "time since spike" else got.size
+            assert got.size == v.size or k == "time since spike", (c.name, k, got.size, v.size)
+            assert np.array_equal(got.view(np.uint32)[:n], v.view(np.uint32)[:n]), (c.name, k)
+    assert onet.connection("p_zero").num_weights == 48          # one synapse per destination
+    assert onet.connection("i_rec").kmax < 25
 
 
 def test_column_offset_quirk_and_weight_counts(sg):
