@@ -31,7 +31,27 @@ FLOAT, BIT, INT = 0, 1, 2
 CONN_TYPES = {"fully connected": 0, "subset": 1, "one to one": 2, "convergent": 3, "divergent": 4}
 OPCODES = {"add": 0, "sub": 1, "mult": 2, "div": 3, "pool": 4, "reward": 5, "modulate": 6,
            "gap": 7, "add_heaviside": 8, "sub_heaviside": 9, "mult_heaviside": 10}
-MODELS = {"izhikevich": BIT, "relay": FLOAT, "game_of_life": BIT, "rate_encoding": FLOAT}
+MODELS = {"izhikevich": BIT, "relay": FLOAT, "game_of_life": BIT, "rate_encoding": FLOAT,
+          "binary threshold": FLOAT, "backprop_rate_encoding": FLOAT,
+          "hebbian_rate_encoding": FLOAT, "perceptron": FLOAT, "sine generator": FLOAT,
+          "poisson generator": BIT}
+GLOBAL_SEED = 0x5EED5EED     # the library's default sg_set_seed value
+# Which sine the reference's sine generator evaluates: its unqualified
+# sin(float) resolves to the C library's double sin (pinned by the fixture).
+SINE_USES_SINF = False
+
+
+def rng_uniform(seed, stream, index):
+    """Counter-based uniform draw in [0, 1) (SplitMix64 finaliser of a
+    linear mix of seed, stream and index), as the library's generators use."""
+    m = (1 << 64) - 1
+    z = (seed * 0x9E3779B97F4A7C15 + stream * 0xD1B54A32D192ED03) & m
+    z = (np.uint64(z) + np.asarray(index, np.uint64))
+    with np.errstate(over="ignore"):
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(40)).astype(np.float32) * np.float32(1.0 / 16777216.0)
 IZ_PARAMS = {  # izhikevich_attributes.cpp:28-35
     "default": (0.02, 0.2, -70.0, 2), "regular": (0.02, 0.2, -65.0, 8),
     "bursting": (0.02, 0.2, -55.0, 4), "chattering": (0.02, 0.2, -50.0, 2),
@@ -424,6 +444,11 @@ class OracleNetwork:
             l.history = 1 + (max_delay // 32 if l.output_type == BIT else max_delay)
             st = {"input": np.zeros(l.registers * l.size, np.float32),   # attributes.cpp:21-26
                   "output": np.zeros(l.history * l.size, np.uint32)}
+            if l.model == "backprop_rate_encoding":   # feedforward structures only
+                raise ValueError("Cluster compatibility conflict detected!")
+            elif l.model == "perceptron":
+                st["expected"] = np.zeros(l.size, np.float32)
+            l.iteration = 0     # sine / Poisson generator step count
             if l.model == "izhikevich":
                 for k in ("ampa", "nmda", "gabaa", "gabab", "mult", "dopamine",
                           "voltage", "recovery", "post trace"):
@@ -627,6 +652,10 @@ class OracleNetwork:
             self._update(L, l)
         # plasticity
         if learning:
+            for c in self.conns:
+                if c.plastic and c.to.model == "perceptron":
+                    raise ValueError("perceptron learning reads source outputs that the reference "
+                                     "binds only in feedforward structures")
             for l in self.layers:
                 for c in l.inputs:
                     if c.plastic and c.to.model == "izhikevich":
@@ -664,6 +693,12 @@ class OracleNetwork:
                 L.sg_act_second_order(*geo, _p(src), c.frm.output_type, c.delay, c.opcode,
                                       _p(m["weights"]), _p(so))
             return
+        if c.to.model == "perceptron":   # perceptron_attributes.cpp:35-47
+            if c.second_order or c.convolutional:
+                raise ValueError("Unimplemented connection type!")
+            L.sg_act_perceptron(*geo, _p(src), c.frm.output_type, c.delay, c.opcode,
+                                _p(m["weights"]), _p(reg))
+            return
         if c.to.model == "izhikevich" and not direct:
             if c.opcode == OPCODES["gap"]:
                 L.sg_act_gap(*geo, _p(st["voltage"]), _p(m["weights"]), _p(reg))
@@ -692,8 +727,24 @@ class OracleNetwork:
         elif l.model == "relay":
             L.sg_relay(l.size, l.history, _p(st["input"]), _p(st["output"]),
                        int(l.p.get("ramp", "false") == "true"))
-        elif l.model == "rate_encoding":
+        elif l.model in ("rate_encoding", "backprop_rate_encoding", "hebbian_rate_encoding"):
             L.sg_rate(l.size, l.history, _p(st["input"]), _p(st["output"]))
+        elif l.model == "binary threshold":
+            L.sg_bin_thresh(l.size, l.history, _p(st["input"]), _p(st["output"]))
+        elif l.model == "perceptron":
+            per_neuron = sum(c.num_weights for c in l.inputs) // l.size   # layer.cpp:110-115
+            L.sg_perceptron(l.size, l.history, per_neuron, _p(st["input"]), _p(st["output"]))
+        elif l.model == "sine generator":
+            freq = np.float32(2 * np.pi / 1000 * np.float64(np.float32(l.p.get("frequency", "10"))))
+            L.sg_sine(l.size, l.history, ctypes.c_float(freq), l.iteration, int(SINE_USES_SINF),
+                      _p(st["input"]), _p(st["output"]))
+            l.iteration += 1
+        elif l.model == "poisson generator":
+            seed = int(l.p.get("seed")) if l.p.has("seed") else \
+                GLOBAL_SEED ^ ((0xC0FFEE1234567 * (self.layers.index(l) + 1)) & ((1 << 64) - 1))
+            draws = rng_uniform(seed, l.iteration, np.arange(l.size))
+            L.sg_poisson_gen(l.size, l.history, _p(draws), _p(st["input"]), _p(st["output"]))
+            l.iteration += 1
         elif l.model == "game_of_life":
             L.sg_gol(l.size, l.history, _p(st["input"]), _p(st["output"]),
                      l.p.get_int("survival_min", 2), l.p.get_int("survival_max", 3),

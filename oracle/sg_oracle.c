@@ -418,6 +418,50 @@ void sg_relay(int size, int history, const float *inputs, float *outputs, int ra
 
 /* Rate encoding: rate_encoding_attributes.cpp:122-131.  In C++ tanh(float)
  * resolves to the float overload, i.e. tanhf. */
+/* binary threshold (bin_thresh_attributes.cpp:9-17) */
+void sg_bin_thresh(int size, int history, const float *inputs, float *outputs) {
+    for (int nid = 0; nid < size; ++nid)
+        shift_float(outputs, size, history, nid, inputs[nid] > 0);
+}
+
+/* perceptron update (perceptron_attributes.cpp:13-21): the input over the
+ * layer's weights per neuron (an int) */
+void sg_perceptron(int size, int history, int per_neuron, const float *inputs, float *outputs) {
+    for (int nid = 0; nid < size; ++nid)
+        shift_float(outputs, size, history, nid, inputs[nid] / per_neuron);
+}
+
+/* perceptron activator (perceptron_attributes.cpp:27-33) */
+void sg_act_perceptron(int rows, const int *dst, const long *ptr, const int *from_idx,
+                       const int *w_idx, const uint32_t *src_words, int src_type, int delay,
+                       int opcode, const float *weights, float *inputs) {
+    for (int r = 0; r < rows; ++r) {
+        float sum = 0.0;
+        for (long v = ptr[r]; v < ptr[r + 1]; ++v)
+            sum += (extract(src_words[from_idx[v]], delay, src_type) > 0) * weights[w_idx[v]];
+        inputs[dst[r]] = aggregate(inputs[dst[r]], sum, opcode);
+    }
+}
+
+/* sine generator (sine_generator_attributes.cpp:11-23): wave from the float
+ * product frequency * iteration; use_sinf selects the float sine overload,
+ * otherwise the sine is taken in double and the wave rounded to float. */
+void sg_sine(int size, int history, float frequency, int iteration, int use_sinf,
+             const float *inputs, float *outputs) {
+    float x = frequency * iteration;
+    float wave = use_sinf ? (1 + sinf(x)) / 2 : (float)((1 + sin(x)) / 2);
+    for (int nid = 0; nid < size; ++nid)
+        shift_float(outputs, size, history, nid, inputs[nid] * wave);
+}
+
+/* poisson generator (poisson_generator_attributes.cpp:9-24) with the draws
+ * given */
+void sg_poisson_gen(int size, int history, const float *draws, const float *inputs,
+                    uint32_t *spikes) {
+    for (int nid = 0; nid < size; ++nid)
+        shift_bit(spikes, size, history, nid, draws[nid] < inputs[nid]);
+}
+
 void sg_rate(int size, int history, const float *inputs, float *outputs) {
     for (int nid = 0; nid < size; ++nid) {
         float input = inputs[nid];

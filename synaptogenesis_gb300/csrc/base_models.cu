@@ -4,6 +4,7 @@
 #include <cmath>
 
 #include "cuda_check.h"
+#include "history.cuh"
 #include "models.h"
 #include "state.h"
 
@@ -147,27 +148,6 @@ __global__ void k_dendrite_fold(int n, float* __restrict__ src, float* __restric
 void launch_dendrite_fold(int n, float* src, float* dst, int opcode, float trail, cudaStream_t s) {
     k_dendrite_fold<<<blocks_for(n, 256), 256, 0, s>>>(n, src, dst, opcode, trail);
     SG_LAUNCH_CHECK();
-}
-
-// ---------------------------------------------------------------------------
-// Output history shifts (state/attributes.h:316-333)
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t shift_bits(uint32_t* out, int size, int history, int nid,
-                                               uint32_t new_bit) {
-    uint32_t curr = out[(size_t)size * (history - 1) + nid];
-    for (int idx = history - 1; idx > 0; --idx) {
-        uint32_t prev = out[(size_t)size * (idx - 1) + nid];
-        out[(size_t)size * idx + nid] = (curr >> 1) | (prev << 31);
-        curr = prev;
-    }
-    out[nid] = (curr >> 1) | (new_bit << 31);
-    return curr >> 31;
-}
-
-__device__ __forceinline__ void shift_floats(float* out, int size, int history, int nid, float v) {
-    for (int idx = history - 1; idx > 0; --idx)
-        out[(size_t)size * idx + nid] = out[(size_t)size * (idx - 1) + nid];
-    out[nid] = v;
 }
 
 // relay_attributes.cpp:10-18 (the ramp is std::fmax on doubles, i.e. fmax)

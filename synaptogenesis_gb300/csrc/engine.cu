@@ -107,6 +107,13 @@ Engine::Engine(Network* net, Environment* env, State* state, const Props& args)
         // per step against 342 us for graphs without overlap (graph replay
         // did not run the two branches concurrently, 332 us).  One stream
         // when profiling, so that the per-group timings stay separate.
+        if (learning_)
+            for (auto& lp : net_->layers)
+                for (Connection* c : lp->inputs)
+                    if (c->plastic) {
+                        std::string e = find_model(lp->model)->learning_error(*c);
+                        if (!e.empty()) throw SgError(c->str() + ": " + e);
+                    }
         long long learned = 0;
         if (learning_)
             for (auto& lp : net_->layers)

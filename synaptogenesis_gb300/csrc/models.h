@@ -62,6 +62,9 @@ class Model {
     }
     // Whether a plastic connection into this model has an updater.
     virtual bool learns(const Connection& c) const { return false; }
+    // Non-empty when a run with learning cannot update this plastic
+    // connection; the engine refuses to start with that message.
+    virtual std::string learning_error(const Connection& c) const { return ""; }
     // Whole-run path: can this layer advance n steps on its own -- nothing
     // else reads or writes it between steps (the engine has checked that no
     // environment module touches it)?  If so, advance_alone runs the n steps

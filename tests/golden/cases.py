@@ -548,6 +548,41 @@ def cases():
                     + [("matrix", c, k) for c in ("i_rec", "i_ff")
                        for k in ("weights", "short term w", "short term R", "presyn trace")]
                     + [("matrix", c, "weights") for c in ("p_fc", "p_div", "p_sub", "p_zero")]))
+
+    # --- the smaller neural models -----------------------------------------
+    # binary threshold, hebbian rate encoding (its rule is never applied by
+    # the reference), perceptron, sine generator.
+    net = {"structures": [{"name": "m", "type": "parallel", "layers": [
+        _layer("src", "relay", 6, 8),
+        _layer("bt", "binary threshold", 6, 8),
+        _layer("hb", "hebbian_rate_encoding", 6, 8),
+        _layer("pc", "perceptron", 4, 5),
+        _layer("sg", "sine generator", 6, 8, frequency=37),
+    ]}], "connections": [
+        {"name": "m_bt", "from layer": "src", "to layer": "bt", "type": "one to one",
+         "opcode": "add", "plastic": False},
+        {"name": "m_hb", "from layer": "src", "to layer": "hb", "type": "fully connected",
+         "opcode": "add", "plastic": True},
+        {"name": "m_pc", "from layer": "src", "to layer": "pc", "type": "fully connected",
+         "opcode": "add", "plastic": False},
+        {"name": "m_pc_sub", "from layer": "bt", "to layer": "pc", "type": "subset",
+         "opcode": "sub", "plastic": False,
+         "subset config": {"from row start": 0, "from row end": 3, "from column start": 1,
+                           "from column end": 5, "to row start": 1, "to row end": 3,
+                           "to column start": 0, "to column end": 4}},
+        {"name": "m_sg", "from layer": "src", "to layer": "sg", "type": "one to one",
+         "opcode": "add", "plastic": False},
+    ]}
+    model_conns = [c["name"] for c in net["connections"]]
+
+    def inj_models(rng, sizes):
+        return {("matrix", name, "weights"): rng.uniform(-1.0, 1.0, sizes["conn:" + name]).astype(np.float32)
+                for name in model_conns}
+    out.append(Case("models", net, 40, 101, inject=inj_models,
+                    inputs={"src": lambda rng, t, n: rng.normal(0.0, 1.0, n)},
+                    record=[("m", l) for l in ("bt", "hb", "pc", "sg")],
+                    final=[("neuron", "m", l, "input") for l in ("bt", "hb", "pc", "sg")]
+                    + [("matrix", "m_hb", "weights")]))
     return out
 
 

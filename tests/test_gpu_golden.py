@@ -15,7 +15,7 @@ from tests.harness import compare, float_like_keys, load_fixture, run_library, r
 
 pytestmark = pytest.mark.gpu
 
-RATE_KEYS = ("rec/s/one", "rec/s/div", "rec/d/rtree", "rec/p/sdiv")
+RATE_KEYS = ("rec/s/one", "rec/s/div", "rec/d/rtree", "rec/p/sdiv", "rec/m/hb")
 RATE_TOL = 1e-5
 
 

@@ -42,7 +42,8 @@ def test_library_exports_every_header_function(sg):
 
 
 @pytest.mark.parametrize("name", ["iz_opcodes", "iz_plastic", "base_all_types", "iz_c0_8",
-                                  "gol_two_word_history", "dendrites", "second_order", "sparse"])
+                                  "gol_two_word_history", "dendrites", "second_order", "sparse",
+                                  "models"])
 def test_initial_state_matches_oracle(sg, name):
     from oracle.oracle import OracleNetwork
     from tests.golden.cases import CASES
@@ -201,6 +202,27 @@ def test_dendritic_registers_and_node_names(sg):
     n.build_state()
     assert n.get_neuron_data("s", "t", "input").size == 5 * 9
     assert n.get_neuron_data("s", "a", "input").size == 9
+
+
+def test_model_build_errors_match_the_reference(sg):
+    """backprop_rate_encoding builds only in feedforward structures; the
+    perceptron has no convolutional activator."""
+    from oracle.oracle import OracleNetwork
+    net = {"structures": [{"name": "s", "layers": [
+        {"name": "a", "neural model": "backprop_rate_encoding", "rows": 2, "columns": 2}]}]}
+    n = sg.Network(net)
+    n.build_state()
+    assert n.state is None and "Cluster compatibility conflict" in sg.last_error()
+    with pytest.raises(ValueError, match="Cluster compatibility"):
+        OracleNetwork(net)
+    net = {"structures": [{"name": "s", "layers": [
+        {"name": "a", "neural model": "relay", "rows": 4, "columns": 4},
+        {"name": "p", "neural model": "perceptron", "rows": 4, "columns": 4}]}],
+        "connections": [{"from layer": "a", "to layer": "p", "type": "convergent",
+                         "convolutional": True, "arborized config": {"field size": 3}}]}
+    n = sg.Network(net)
+    n.build_state()
+    assert n.state is None and "Unimplemented connection type" in sg.last_error()
 
 
 def test_izhikevich_gap_must_be_self_connection(sg):
