@@ -34,7 +34,7 @@ OPCODES = {"add": 0, "sub": 1, "mult": 2, "div": 3, "pool": 4, "reward": 5, "mod
 MODELS = {"izhikevich": BIT, "relay": FLOAT, "game_of_life": BIT, "rate_encoding": FLOAT,
           "binary threshold": FLOAT, "backprop_rate_encoding": FLOAT,
           "hebbian_rate_encoding": FLOAT, "perceptron": FLOAT, "sine generator": FLOAT,
-          "poisson generator": BIT}
+          "poisson generator": BIT, "spnet": BIT}
 GLOBAL_SEED = 0x5EED5EED     # the library's default sg_set_seed value
 # Which sine the reference's sine generator evaluates: its unqualified
 # sin(float) resolves to the C library's double sin (pinned by the fixture).
@@ -449,6 +449,15 @@ class OracleNetwork:
             elif l.model == "perceptron":
                 st["expected"] = np.zeros(l.size, np.float32)
             l.iteration = 0     # sine / Poisson generator step count
+            if l.model == "spnet":   # spnet_attributes.cpp:369-425
+                for k in ("voltage", "recovery", "post trace"):
+                    st[k] = np.zeros(l.size, np.float32)
+                st["time since spike"] = np.full(l.size, 32, np.int32)
+                a, b, c, d = IZ_PARAMS[l.p.get("params", "regular")]
+                for k, v in zip("abcd", (a, b, c, d)):
+                    st[k] = np.full(l.size, v, np.float32)
+                L.sg_iz_init(l.size, _p(st["a"]), _p(st["b"]), _p(st["c"]),
+                             _p(st["voltage"]), _p(st["recovery"]))
             if l.model == "izhikevich":
                 for k in ("ampa", "nmda", "gabaa", "gabab", "mult", "dopamine",
                           "voltage", "recovery", "post trace"):
@@ -467,6 +476,14 @@ class OracleNetwork:
             self.matrix[c] = m = {"weights": w}
             if c.so_host:  # weight_matrix.cpp:79-80 (not readable through the getters)
                 self.so_weights[c] = np.zeros(c.num_weights, np.float32)
+            if c.to.model == "spnet":   # spnet_attributes.cpp:440-494
+                n = c.num_weights
+                m["presyn trace"] = np.zeros(n, np.float32)
+                m["time since spike"] = np.full(n, 32, np.int32)
+                m["weight derivative"] = np.zeros(n, np.float32)
+                m["delays"] = self._default_delays(c)
+                c.baseline_conductance = c.p.get_float("conductance", 1.0)
+                c.learning_rate = c.p.get_float("learning rate", 0.1)
             if c.to.model == "izhikevich":
                 n = c.num_weights
                 m["short trace"] = np.zeros(n, np.float32)
@@ -660,6 +677,8 @@ class OracleNetwork:
                 for c in l.inputs:
                     if c.plastic and c.to.model == "izhikevich":
                         self._learn(L, c)
+                    elif c.plastic and c.to.model == "spnet":
+                        self._learn_spnet(L, c)
 
     def run(self, steps, input_fn=None, learning=True, record=None):
         """record: list of (layer, key) recorded after every step."""
@@ -692,6 +711,13 @@ class OracleNetwork:
             else:
                 L.sg_act_second_order(*geo, _p(src), c.frm.output_type, c.delay, c.opcode,
                                       _p(m["weights"]), _p(so))
+            return
+        if c.to.model == "spnet":   # spnet_attributes.cpp:202-214
+            if c.second_order:
+                raise ValueError("Unimplemented connection type!")
+            L.sg_act_spnet(*geo, _p(src), c.frm.output_type, _p(m["weights"]), _p(m["delays"]),
+                           _p(m["time since spike"]), ctypes.c_float(c.baseline_conductance),
+                           c.opcode, _p(reg))
             return
         if c.to.model == "perceptron":   # perceptron_attributes.cpp:35-47
             if c.second_order or c.convolutional:
@@ -729,6 +755,10 @@ class OracleNetwork:
                        int(l.p.get("ramp", "false") == "true"))
         elif l.model in ("rate_encoding", "backprop_rate_encoding", "hebbian_rate_encoding"):
             L.sg_rate(l.size, l.history, _p(st["input"]), _p(st["output"]))
+        elif l.model == "spnet":
+            L.sg_spnet_neurons(l.size, l.history, _p(st["input"]), _p(st["output"]),
+                               *[_p(st[k]) for k in ("voltage", "recovery", "post trace",
+                                                     "time since spike", "a", "b", "c", "d")])
         elif l.model == "binary threshold":
             L.sg_bin_thresh(l.size, l.history, _p(st["input"]), _p(st["output"]))
         elif l.model == "perceptron":
@@ -761,3 +791,13 @@ class OracleNetwork:
                     ctypes.c_float(c.max_weight), _p(st["post trace"]), _p(st["time since spike"]),
                     _p(st["output"][:c.to.size]), _p(ft), _p(m["weights"]), _p(m["presyn trace"]),
                     _p(m["weight derivatives"]), _p(m["short term R"]), _p(m["short term w"]))
+
+    def _learn_spnet(self, L, c):  # spnet_attributes.cpp:288-306
+        if c.convolutional or c.second_order or c.opcode not in (0, 1):
+            raise ValueError("Unimplemented connection type!")
+        st, m = self.neuron[c.to], self.matrix[c]
+        L.sg_upd_spnet(c.rows, _p(c.dst), _p(c.ptr), _p(c.from_idx), _p(c.w_idx),
+                       c.frm.output_type, int(c.opcode == 1), ctypes.c_float(c.learning_rate),
+                       ctypes.c_float(c.max_weight), _p(st["post trace"]), _p(st["time since spike"]),
+                       _p(st["output"][:c.to.size]), _p(m["time since spike"]), _p(m["weights"]),
+                       _p(m["presyn trace"]), _p(m["weight derivative"]))

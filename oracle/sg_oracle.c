@@ -390,6 +390,88 @@ void sg_iz_neurons(int size, int history, const float *inputs, uint32_t *spikes,
 
 /* Resting-state settle loop of the Izhikevich constructor:
  * izhikevich_attributes.cpp:628-649 */
+/* spnet neuron update (spnet_attributes.cpp:96-166): the Izhikevich Euler
+ * loop without conductances; the post trace steps by 0.1 or decays by 0.95. */
+void sg_spnet_neurons(int size, int history, const float *inputs, uint32_t *spikes,
+                      float *voltages, float *recoveries, float *post_traces, int *tss,
+                      const float *as, const float *bs, const float *cs, const float *ds) {
+    for (int nid = 0; nid < size; ++nid) {
+        float voltage = voltages[nid];
+        float recovery = recoveries[nid];
+        float current = inputs[nid];
+        float a = as[nid];
+        float b = bs[nid];
+        for (int i = 0; (i < 10) && (voltage < 30.0); ++i) {
+            float delta_v = (0.04 * voltage * voltage) + (5 * voltage) + 140 - recovery + current;
+            voltage += delta_v * 0.1;
+            voltage = (voltage != voltage) ? 30.0 : voltage;
+            float adjusted_tau = (voltage > 30.0) ? delta_v / (30.0 - voltage + delta_v) * 0.1 : 0.1;
+            recovery += a * adjusted_tau * ((b * voltage) - recovery);
+        }
+        unsigned int spike = voltage >= 30.0;
+        int prev_bit = shift_bit(spikes, size, history, nid, spike);
+        post_traces[nid] = (prev_bit) ? (post_traces[nid] + 0.1) : (post_traces[nid] * 0.95);
+        tss[nid] = (prev_bit) ? 0 : (tss[nid] + 1 < 32 ? tss[nid] + 1 : 32);
+        voltages[nid] = (spike) ? cs[nid] : voltage;
+        recoveries[nid] = recovery + (spike * ds[nid]);
+    }
+}
+
+/* spnet activator (spnet_attributes.cpp:172-214): per-synapse delays, the
+ * source's time since spike updated per visit, any aggregation opcode. */
+void sg_act_spnet(int rows, const int *dst, const long *ptr, const int *from_idx,
+                  const int *w_idx, const uint32_t *src_words, int src_type,
+                  const float *weights, const int *delays, int *from_tss,
+                  float baseline_conductance, int opcode, float *inputs) {
+    for (int r = 0; r < rows; ++r) {
+        float sum = 0.0;
+        for (long v = ptr[r]; v < ptr[r + 1]; ++v) {
+            int f = from_idx[v], w = w_idx[v];
+            float spike = extract(src_words[f], delays[w], src_type);
+            from_tss[f] = (spike > 0.0) ? 0 : (from_tss[f] + 1 < 32 ? from_tss[f] + 1 : 32);
+            float weight = weights[w];
+            sum += spike * weight * baseline_conductance;
+        }
+        inputs[dst[r]] = aggregate(inputs[dst[r]], sum, opcode);
+    }
+}
+
+/* spnet updater (spnet_attributes.cpp:220-306) */
+void sg_upd_spnet(int rows, const int *dst, const long *ptr, const int *from_idx,
+                  const int *w_idx, int src_type, int is_sub, float learning_rate,
+                  float max_weight, const float *to_exc_traces, const int *to_tss,
+                  const uint32_t *dest_words, const int *from_tss, float *weights,
+                  float *presyn_traces, float *dws) {
+    for (int r = 0; r < rows; ++r) {
+        int to = dst[r];
+        float dest_exc_trace = to_exc_traces[to];
+        int dest_time_since_spike = to_tss[to];
+        float dest_spike = extract(dest_words[to], 0, src_type);
+        for (long e = ptr[r]; e < ptr[r + 1]; ++e) {
+            int f = from_idx[e], w = w_idx[e];
+            float weight = weights[w];
+            if (weight >= 0.0001f) {
+                int src_time_since_spike = from_tss[f];
+                int src_spike = src_time_since_spike == 0;
+                float src_trace = (!is_sub)
+                    ? (presyn_traces[w] = (src_spike) ? (presyn_traces[w] + 0.1)
+                                                      : presyn_traces[w] * 0.95)
+                    : ((dest_spike > 0.0 && src_time_since_spike > 0 && src_time_since_spike < 32)
+                           ? sg_istdp_src(src_time_since_spike) : 0.0f);
+                float dest_trace = (!is_sub)
+                    ? dest_exc_trace
+                    : ((src_spike && dest_time_since_spike > 0 && dest_time_since_spike < 32)
+                           ? sg_istdp_dst(dest_time_since_spike) : 0.0f);
+                float dw = dws[w] = 0.9 * dws[w] + (dest_spike * src_trace) - (src_spike * dest_trace);
+                float weight_delta = dw + 0.01;
+                weight += learning_rate * weight_delta;
+                float capped = (max_weight < weight) ? max_weight : weight;
+                weights[w] = (0.0001f > capped) ? 0.0001f : capped;
+            }
+        }
+    }
+}
+
 void sg_iz_init(int size, const float *as, const float *bs, const float *cs,
                 float *v_out, float *r_out) {
     for (int j = 0; j < size; ++j) {

@@ -9,6 +9,7 @@
 #include <random>
 
 #include "cuda_check.h"
+#include "history.cuh"
 #include "iz_cols_tma.cuh"
 #include "iz_neuron.cuh"
 #include "models.h"
@@ -504,6 +505,107 @@ __global__ void __launch_bounds__(256) k_iz_learn_2d(
 // ---------------------------------------------------------------------------
 // Model
 // ---------------------------------------------------------------------------
+// Neuron parameters ("params") and the settled resting voltage and recovery
+// of an Izhikevich-type layer (izhikevich_attributes.cpp:587-662,
+// spnet_attributes.cpp:369-425); time since spike starts at 32.
+static void iz_params_and_rest(LayerState& ls) {
+    const Layer& l = *ls.layer;
+    float *as = ls.vars["a"]->hf(), *bs = ls.vars["b"]->hf(), *cs = ls.vars["c"]->hf(),
+          *ds = ls.vars["d"]->hf();
+    std::string p = l.parameter("params", "regular");
+    if (p == "random positive" || p == "random negative") {
+        auto rng = make_rng(l.config, 7 + l.index);
+        std::uniform_real_distribution<float> u(0.0f, 1.0f);
+        for (int i = 0; i < l.size; ++i) {
+            if (p == "random positive") {
+                as[i] = 0.02f; bs[i] = 0.2f;
+                cs[i] = -65.0 + (15.0 * std::pow(u(rng), 2));
+                ds[i] = 8.0 - (6.0 * std::pow(u(rng), 2));
+            } else {
+                as[i] = 0.02 + (0.08 * u(rng)); bs[i] = 0.25 - (0.05 * u(rng));
+                cs[i] = -65.0f; ds[i] = 2.0f;
+            }
+        }
+    } else {
+        IzParams q = preset(p);
+        for (int i = 0; i < l.size; ++i) { as[i] = q.a; bs[i] = q.b; cs[i] = q.c; ds[i] = q.d; }
+    }
+    float* v = ls.vars["voltage"]->hf();
+    float* r = ls.vars["recovery"]->hf();
+    int32_t* tss = ls.vars["time since spike"]->hi();
+    for (int j = 0; j < l.size; ++j) {
+        tss[j] = 32;
+        // settle to the resting state
+        float vv = cs[j], rr = bs[j] * cs[j], dv, dr, a = as[j], b = bs[j];
+        do {
+            dv = (0.04 * vv * vv) + (5 * vv) + 140 - rr;
+            vv += dv;
+            dr = a * ((b * vv) - rr);
+            rr += dr;
+        } while (std::fabs(dv) > 0.001 && std::fabs(dr) > 0.001);
+        v[j] = vv;
+        r[j] = rr;
+    }
+}
+
+// Per-synapse delays (myelinated, random or from distances at 0.15 per
+// step) and, per source, its last (up to 32) visits in serial order as
+// device weight indices plus its visit count -- what the time-since-spike
+// kernel scans (izhikevich_attributes.cpp:730-751).
+static void iz_delays_and_visits(State& st, ConnState& cs) {
+    Connection& c = *cs.conn;
+    size_t n = c.num_weights;
+    int R = c.matrix_rows, C = c.matrix_cols;
+    if (!cs.delays) {
+        cs.delays = st.add_array("delays", 'i', n, matrix_layout(c), R, C);
+        int32_t* dl = cs.delays->hi();
+        if (c.parameter("myelinated", "false") == "true") {
+            for (size_t i = 0; i < n; ++i) dl[i] = c.delay;
+        } else if (c.config.has("random delay")) {
+            int mx = std::stoi(c.parameter("random delay", "0"));
+            if (mx > 31) throw SgError("Randomized axons cannot have delays greater than 31!");
+            auto rng = make_rng(c.config, 3000 + c.index);
+            std::uniform_int_distribution<int> u(0, mx);
+            for (size_t i = 0; i < n; ++i) dl[i] = u(rng);
+        } else {
+            std::vector<float> dist = cs.cached_distances;
+            if (dist.empty()) {
+                Indices ix = compute_indices(c);
+                dist = compute_distances(c, ix,
+                                         std::stof(c.from->parameter("neuron spacing", "0.1")),
+                                         std::stof(c.to->parameter("neuron spacing", "0.1")),
+                                         std::stof(c.parameter("x offset", "0.0")),
+                                         std::stof(c.parameter("y offset", "0.0")));
+            }
+            compute_delays(c, dist, 0.15f, c.parameter("cap delay", "false") == "true", dl);
+        }
+    }
+    cs.vars["delays"] = cs.delays;
+
+    // Last (up to 32) visits of each source in serial order, device indices.
+    int nsrc = c.from->size;
+    cs.visit_counts = st.add_array("visit counts", 'i', nsrc);
+    cs.last_visits = st.add_array("last visits", 'i', (size_t)nsrc * 32);
+    cs.uniform_delay = st.add_array("uniform delay", 'i', nsrc);
+    cs.uniform_delay->scratch = true;
+    int32_t* cnt = cs.visit_counts->hi();
+    int32_t* last = cs.last_visits->hi();
+    enumerate_visits(c, [&](int, int, int from, long wi, int, int) {
+        long dev = (long)device_index(*cs.weights, (size_t)wi);
+        last[(size_t)from * 32 + (cnt[from] % 32)] = (int)dev;
+        cnt[from]++;
+    });
+    // unroll each ring so that entries 0..m-1 are in serial order
+    std::vector<int32_t> tmp(32);
+    for (int f = 0; f < nsrc; ++f) {
+        int m = std::min(cnt[f], 32);
+        if (cnt[f] <= 32) continue;
+        int start = cnt[f] % 32;
+        for (int j = 0; j < m; ++j) tmp[j] = last[(size_t)f * 32 + (start + j) % 32];
+        for (int j = 0; j < m; ++j) last[(size_t)f * 32 + j] = tmp[j];
+    }
+}
+
 class IzhikevichModel : public Model {
   public:
     const char* name() const override { return "izhikevich"; }
@@ -527,42 +629,7 @@ class IzhikevichModel : public Model {
                               "recovery", "post trace", "a", "b", "c", "d"})
             ls.vars[k] = st.add_array(k, 'f', l.size);
         ls.vars["time since spike"] = st.add_array("time since spike", 'i', l.size);
-        float *as = ls.vars["a"]->hf(), *bs = ls.vars["b"]->hf(), *cs = ls.vars["c"]->hf(),
-              *ds = ls.vars["d"]->hf();
-        std::string p = l.parameter("params", "regular");
-        if (p == "random positive" || p == "random negative") {
-            auto rng = make_rng(l.config, 7 + l.index);
-            std::uniform_real_distribution<float> u(0.0f, 1.0f);
-            for (int i = 0; i < l.size; ++i) {
-                if (p == "random positive") {
-                    as[i] = 0.02f; bs[i] = 0.2f;
-                    cs[i] = -65.0 + (15.0 * std::pow(u(rng), 2));
-                    ds[i] = 8.0 - (6.0 * std::pow(u(rng), 2));
-                } else {
-                    as[i] = 0.02 + (0.08 * u(rng)); bs[i] = 0.25 - (0.05 * u(rng));
-                    cs[i] = -65.0f; ds[i] = 2.0f;
-                }
-            }
-        } else {
-            IzParams q = preset(p);
-            for (int i = 0; i < l.size; ++i) { as[i] = q.a; bs[i] = q.b; cs[i] = q.c; ds[i] = q.d; }
-        }
-        float* v = ls.vars["voltage"]->hf();
-        float* r = ls.vars["recovery"]->hf();
-        int32_t* tss = ls.vars["time since spike"]->hi();
-        for (int j = 0; j < l.size; ++j) {
-            tss[j] = 32;
-            // settle to the resting state
-            float vv = cs[j], rr = bs[j] * cs[j], dv, dr, a = as[j], b = bs[j];
-            do {
-                dv = (0.04 * vv * vv) + (5 * vv) + 140 - rr;
-                vv += dv;
-                dr = a * ((b * vv) - rr);
-                rr += dr;
-            } while (std::fabs(dv) > 0.001 && std::fabs(dr) > 0.001);
-            v[j] = vv;
-            r[j] = rr;
-        }
+        iz_params_and_rest(ls);
         for (Connection* c : l.inputs)
             if (c->opcode == OP_GAP && c->from != c->to)
                 throw SgError("Error " + c->str() +
@@ -593,54 +660,7 @@ class IzhikevichModel : public Model {
         int32_t* tss = cs.vars["time since spike"]->hi();
         for (size_t i = 0; i < tss_n; ++i) tss[i] = 32;
 
-        if (!cs.delays) {
-            cs.delays = st.add_array("delays", 'i', n, matrix_layout(c), R, C);
-            int32_t* dl = cs.delays->hi();
-            if (c.parameter("myelinated", "false") == "true") {
-                for (size_t i = 0; i < n; ++i) dl[i] = c.delay;
-            } else if (c.config.has("random delay")) {
-                int mx = std::stoi(c.parameter("random delay", "0"));
-                if (mx > 31) throw SgError("Randomized axons cannot have delays greater than 31!");
-                auto rng = make_rng(c.config, 3000 + c.index);
-                std::uniform_int_distribution<int> u(0, mx);
-                for (size_t i = 0; i < n; ++i) dl[i] = u(rng);
-            } else {
-                std::vector<float> dist = cs.cached_distances;
-                if (dist.empty()) {
-                    Indices ix = compute_indices(c);
-                    dist = compute_distances(c, ix,
-                                             std::stof(c.from->parameter("neuron spacing", "0.1")),
-                                             std::stof(c.to->parameter("neuron spacing", "0.1")),
-                                             std::stof(c.parameter("x offset", "0.0")),
-                                             std::stof(c.parameter("y offset", "0.0")));
-                }
-                compute_delays(c, dist, 0.15f, c.parameter("cap delay", "false") == "true", dl);
-            }
-        }
-        cs.vars["delays"] = cs.delays;
-
-        // Last (up to 32) visits of each source in serial order, device indices.
-        int nsrc = c.from->size;
-        cs.visit_counts = st.add_array("visit counts", 'i', nsrc);
-        cs.last_visits = st.add_array("last visits", 'i', (size_t)nsrc * 32);
-        cs.uniform_delay = st.add_array("uniform delay", 'i', nsrc);
-        cs.uniform_delay->scratch = true;
-        int32_t* cnt = cs.visit_counts->hi();
-        int32_t* last = cs.last_visits->hi();
-        enumerate_visits(c, [&](int, int, int from, long wi, int, int) {
-            long dev = (long)device_index(*cs.weights, (size_t)wi);
-            last[(size_t)from * 32 + (cnt[from] % 32)] = (int)dev;
-            cnt[from]++;
-        });
-        // unroll each ring so that entries 0..m-1 are in serial order
-        std::vector<int32_t> tmp(32);
-        for (int f = 0; f < nsrc; ++f) {
-            int m = std::min(cnt[f], 32);
-            if (cnt[f] <= 32) continue;
-            int start = cnt[f] % 32;
-            for (int j = 0; j < m; ++j) tmp[j] = last[(size_t)f * 32 + (start + j) % 32];
-            for (int j = 0; j < m; ++j) last[(size_t)f * 32 + j] = tmp[j];
-        }
+        iz_delays_and_visits(st, cs);
         if (c.parameter("direct", "false") != "true" && c.opcode != OP_ADD && c.opcode != OP_SUB &&
             c.opcode != OP_MULT && c.opcode != OP_REWARD && c.opcode != OP_GAP)
             throw SgError(c.str() + ": Unimplemented connection type!");
@@ -866,5 +886,192 @@ class IzhikevichModel : public Model {
     }
 };
 SG_REGISTER_MODEL(IzhikevichModel);
+
+// ---------------------------------------------------------------------------
+// spnet (spnet_attributes.cpp): Izhikevich neurons driven by the plain
+// current of their synapses, sum(spike * w * conductance), with STDP on a
+// presynaptic trace (+0.1, decay 0.95) and the weight derivative
+// dw = 0.9 dw + post * pre - ..., weights kept in [0.0001, max weight].
+// Sources' time since spike and the per-synapse delays are the Izhikevich
+// model's (same visit tables and kernels).
+// ---------------------------------------------------------------------------
+template <int TY, int SR>
+__global__ void __launch_bounds__(128) k_spnet_activate(DGeom g, const uint32_t* __restrict__ src,
+                                                        const float* __restrict__ w,
+                                                        const int* __restrict__ delays, float gc,
+                                                        int opcode, float* __restrict__ inputs) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= g.n_dest) return;
+    float sum = 0.0f;
+    for_each_source<TY>(g, d, [&](int from, int wi) {
+        const float spike = extract<SR>(src[from], delays[wi]);
+        sum += spike * w[wi] * gc;
+    });
+    const int to = dest_of<TY>(g, d);
+    inputs[to] = aggregate(inputs[to], sum, opcode);
+}
+
+// spnet_attributes.cpp:96-166, the reference's expressions as written: the
+// double constants promote, and the float stores round.
+__global__ void __launch_bounds__(256) k_spnet_update(int size, int history, const float* __restrict__ in,
+                                                      uint32_t* spikes, float* vs, float* rs, float* post,
+                                                      int* tss, const float* __restrict__ as,
+                                                      const float* __restrict__ bs,
+                                                      const float* __restrict__ cs,
+                                                      const float* __restrict__ ds) {
+    const int nid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nid >= size) return;
+    float voltage = vs[nid];
+    float recovery = rs[nid];
+    const float current = in[nid];
+    const float a = as[nid], b = bs[nid];
+    for (int i = 0; (i < 10) && (voltage < 30.0); ++i) {
+        const float delta_v = (0.04 * voltage * voltage) + (5 * voltage) + 140 - recovery + current;
+        voltage += delta_v * 0.1;
+        voltage = (voltage != voltage) ? 30.0f : voltage;
+        const float adjusted_tau = (voltage > 30.0) ? delta_v / (30.0 - voltage + delta_v) * 0.1 : 0.1;
+        recovery += a * adjusted_tau * ((b * voltage) - recovery);
+    }
+    const uint32_t spike = voltage >= 30.0;
+    const uint32_t prev_bit = shift_bits(spikes, size, history, nid, spike);
+    post[nid] = prev_bit ? (float)(post[nid] + 0.1) : (float)(post[nid] * 0.95);
+    tss[nid] = prev_bit ? 0 : min(32, tss[nid] + 1);
+    vs[nid] = spike ? cs[nid] : voltage;
+    rs[nid] = recovery + (spike * ds[nid]);
+}
+
+// spnet_attributes.cpp:220-286 ("add": presynaptic trace against the
+// postsynaptic trace; "sub": the inverse-STDP terms of the time since spike,
+// tabulated on the host with the host's powf / expf).
+template <int TY, int SR, bool SUB>
+__global__ void __launch_bounds__(128) k_spnet_learn(DGeom g, const uint32_t* __restrict__ dest_out,
+                                                     const float* __restrict__ post,
+                                                     const int* __restrict__ to_tss,
+                                                     const int* __restrict__ from_tss, float lr,
+                                                     float max_weight, float* w, float* presyn,
+                                                     float* dws, IzLut lut) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= g.n_dest) return;
+    const int to = dest_of<TY>(g, d);
+    const float dest_exc = post[to];
+    const int dtss = to_tss[to];
+    const float dest_spike = extract<SR>(dest_out[to], 0);    // the source's extractor
+    for_each_source<TY>(g, d, [&](int from, int wi) {
+        float weight = w[wi];
+        if (!(weight >= 0.0001f)) return;
+        const int stss = from_tss[from];
+        const bool src_spike = stss == 0;
+        float src_trace, dest_trace;
+        if (!SUB) {
+            const float p = presyn[wi];
+            src_trace = presyn[wi] = src_spike ? (float)(p + 0.1) : (float)(p * 0.95);
+            dest_trace = dest_exc;
+        } else {
+            src_trace = (dest_spike > 0.0f && stss > 0 && stss < 32) ? lut.src[stss] : 0.0f;
+            dest_trace = (src_spike && dtss > 0 && dtss < 32) ? lut.dst[dtss] : 0.0f;
+        }
+        const float dw = 0.9 * dws[wi] + (dest_spike * src_trace) - (src_spike * dest_trace);
+        dws[wi] = dw;
+        const float weight_delta = dw + 0.01;
+        weight += lr * weight_delta;
+        const float capped = (max_weight < weight) ? max_weight : weight;
+        w[wi] = (0.0001f > capped) ? 0.0001f : capped;
+    });
+}
+
+class SpnetModel : public Model {
+  public:
+    const char* name() const override { return "spnet"; }
+    OutputType output_type() const override { return OUT_BIT; }
+
+    void prepare_device(State&, ConnState& cs, cudaStream_t s) const override {
+        if (!cs.uniform_delay) return;
+        const int n = cs.conn->from->size;
+        k_iz_uniform_delay<<<blocks_for(n, 256), 256, 0, s>>>(n, cs.visit_counts->di(),
+                                                              cs.last_visits->di(),
+                                                              cs.delays->di(), cs.uniform_delay->di());
+        SG_LAUNCH_CHECK();
+    }
+
+    void build_layer(State& st, LayerState& ls) const override {
+        const Layer& l = *ls.layer;
+        for (const char* k : {"voltage", "recovery", "post trace", "a", "b", "c", "d"})
+            ls.vars[k] = st.add_array(k, 'f', l.size);
+        ls.vars["time since spike"] = st.add_array("time since spike", 'i', l.size);
+        iz_params_and_rest(ls);
+    }
+
+    // process_weight_matrix and the activator / updater checks
+    // (spnet_attributes.cpp:202-214, 288-306, 440-494)
+    void build_matrix(State& st, ConnState& cs) const override {
+        Connection& c = *cs.conn;
+        if (c.second_order) throw SgError(c.str() + ": Unimplemented connection type!");
+        if (c.plastic && (c.convolutional || (c.opcode != OP_ADD && c.opcode != OP_SUB)))
+            throw SgError(c.str() + ": Unimplemented connection type!");
+        const size_t n = c.num_weights;
+        cs.params["conductance"] = std::stof(c.parameter("conductance", "1.0"));
+        cs.params["learning rate"] = std::stof(c.parameter("learning rate", "0.1"));
+        for (const char* k : {"presyn trace", "weight derivative"})
+            cs.vars[k] = st.add_array(k, 'f', n, matrix_layout(c), c.matrix_rows, c.matrix_cols);
+        const size_t tss_n = std::max<size_t>(n, c.from->size);
+        cs.vars["time since spike"] = st.add_array("time since spike", 'i', tss_n, LAYOUT_SOURCE,
+                                                   1, 1, c.from->size);
+        int32_t* tss = cs.vars["time since spike"]->hi();
+        for (size_t i = 0; i < tss_n; ++i) tss[i] = 32;
+        iz_delays_and_visits(st, cs);
+    }
+
+    void activate(State& st, ConnState& cs, const StepCtx& ctx) const override {
+        const Connection& c = *cs.conn;
+        const uint32_t* src = st.dev_output(c.from, word_index(c.delay, c.from->output_type));
+        k_iz_time_since_spike<<<blocks_for(c.from->size, 256), 256, 0, ctx.stream>>>(
+            c.from->size, cs.visit_counts->di(), cs.last_visits->di(), cs.delays->di(),
+            cs.uniform_delay->di(), src, (int)c.from->output_type, cs.var("time since spike")->di());
+        SG_LAUNCH_CHECK();
+        const unsigned blocks = blocks_for(cs.geom.n_dest, 128);
+        float* inputs = input_register(st, cs);
+        SG_DISPATCH_TYPE_SRC((int)c.type, (int)c.from->output_type,
+            (k_spnet_activate<TY, SR><<<blocks, 128, 0, ctx.stream>>>(
+                cs.geom, src, cs.weights->df(), cs.delays->di(), cs.params.at("conductance"),
+                (int)c.opcode, inputs)));
+        SG_LAUNCH_CHECK();
+        ctx.count(2);
+    }
+
+    void update(State&, LayerState& ls, const StepCtx& ctx) const override {
+        const Layer& l = *ls.layer;
+        k_spnet_update<<<blocks_for(l.size, 256), 256, 0, ctx.stream>>>(
+            l.size, l.history(), ls.input->df(), ls.output->du(), ls.var("voltage")->df(),
+            ls.var("recovery")->df(), ls.var("post trace")->df(), ls.var("time since spike")->di(),
+            ls.var("a")->df(), ls.var("b")->df(), ls.var("c")->df(), ls.var("d")->df());
+        SG_LAUNCH_CHECK();
+        ctx.count();
+    }
+
+    bool learns(const Connection& c) const override { return true; }
+
+    void learn(State& st, ConnState& cs, const StepCtx& ctx) const override {
+        const Connection& c = *cs.conn;
+        LayerState& to = *st.layer_state(c.to);
+        static IzLut lut = [] {
+            IzLut t{};
+            for (int i = 1; i < 32; ++i) { t.src[i] = istdp_src(i); t.dst[i] = istdp_dst(i); }
+            return t;
+        }();
+        const unsigned blocks = blocks_for(cs.geom.n_dest, 128);
+#define SG_SPNET_LEARN(SUBV)                                                                    \
+    SG_DISPATCH_TYPE_SRC((int)c.type, (int)c.from->output_type,                                \
+        (k_spnet_learn<TY, SR, SUBV><<<blocks, 128, 0, ctx.stream>>>(                          \
+            cs.geom, st.dev_output(c.to, 0), to.var("post trace")->df(),                       \
+            to.var("time since spike")->di(), cs.var("time since spike")->di(),                \
+            cs.params.at("learning rate"), c.max_weight, cs.weights->df(),                     \
+            cs.var("presyn trace")->df(), cs.var("weight derivative")->df(), lut)))
+        if (c.opcode == OP_SUB) { SG_SPNET_LEARN(true); } else { SG_SPNET_LEARN(false); }
+#undef SG_SPNET_LEARN
+        SG_LAUNCH_CHECK();
+        ctx.count();
+    }
+};
+SG_REGISTER_MODEL(SpnetModel);
 
 }  // namespace sg

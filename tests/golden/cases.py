@@ -583,6 +583,42 @@ def cases():
                     record=[("m", l) for l in ("bt", "hb", "pc", "sg")],
                     final=[("neuron", "m", l, "input") for l in ("bt", "hb", "pc", "sg")]
                     + [("matrix", "m_hb", "weights")]))
+
+    # --- spnet (Izhikevich's polychronization network) ---------------------
+    # Excitatory layer with recurrent STDP ("add") and inhibitory feedback
+    # with inverse STDP ("sub"), distance delays, a Poisson-like drive.
+    net = {"structures": [{"name": "n", "type": "parallel", "layers": [
+        _layer("in", "relay", 10, 10),
+        _layer("exc", "spnet", 10, 10, params="regular"),
+        _layer("inh", "spnet", 5, 5, params="fast"),
+    ]}], "connections": [
+        {"name": "n_drive", "from layer": "in", "to layer": "exc", "type": "one to one",
+         "opcode": "add", "plastic": False},
+        {"name": "n_rec", "from layer": "exc", "to layer": "exc", "type": "convergent",
+         "opcode": "add", "plastic": True, "max weight": 10.0,
+         "arborized config": {"field size": 5, "wrap": True}},
+        {"name": "n_ei", "from layer": "exc", "to layer": "inh", "type": "convergent",
+         "opcode": "add", "plastic": False,
+         "arborized config": {"field size": 3, "stride": 2, "wrap": True}},
+        {"name": "n_ie", "from layer": "inh", "to layer": "exc", "type": "fully connected",
+         "opcode": "sub", "plastic": True, "max weight": 5.0},
+    ]}
+
+    def inj_spnet(rng, sizes):
+        return {
+            ("matrix", "n_drive", "weights"): np.full(sizes["conn:n_drive"], 20.0, np.float32),
+            ("matrix", "n_rec", "weights"): rng.uniform(0.0, 6.0, sizes["conn:n_rec"]).astype(np.float32),
+            ("matrix", "n_ei", "weights"): rng.uniform(0.0, 20.0, sizes["conn:n_ei"]).astype(np.float32),
+            ("matrix", "n_ie", "weights"): rng.uniform(0.0, 4.0, sizes["conn:n_ie"]).astype(np.float32),
+        }
+    out.append(Case("spnet", net, 200, 111, inject=inj_spnet,
+                    inputs={"in": lambda rng, t, n: (rng.random(n) < 0.25) * 1.0},
+                    record=[("n", "exc"), ("n", "inh")],
+                    final=[("neuron", "n", "exc", k) for k in
+                           ("voltage", "recovery", "post trace", "time since spike", "input")]
+                    + [("neuron", "n", "inh", k) for k in ("voltage", "recovery")]
+                    + [("matrix", c, k) for c in ("n_rec", "n_ie")
+                       for k in ("weights", "presyn trace", "weight derivative", "time since spike")]))
     return out
 
 
