@@ -34,7 +34,7 @@ OPCODES = {"add": 0, "sub": 1, "mult": 2, "div": 3, "pool": 4, "reward": 5, "mod
 MODELS = {"izhikevich": BIT, "relay": FLOAT, "game_of_life": BIT, "rate_encoding": FLOAT,
           "binary threshold": FLOAT, "backprop_rate_encoding": FLOAT,
           "hebbian_rate_encoding": FLOAT, "perceptron": FLOAT, "sine generator": FLOAT,
-          "poisson generator": BIT, "spnet": BIT}
+          "poisson generator": BIT, "spnet": BIT, "oscillator": FLOAT, "som": FLOAT}
 GLOBAL_SEED = 0x5EED5EED     # the library's default sg_set_seed value
 # Which sine the reference's sine generator evaluates: its unqualified
 # sin(float) resolves to the C library's double sin (pinned by the fixture).
@@ -448,6 +448,12 @@ class OracleNetwork:
                 raise ValueError("Cluster compatibility conflict detected!")
             elif l.model == "perceptron":
                 st["expected"] = np.zeros(l.size, np.float32)
+            elif l.model == "oscillator":   # oscillator_attributes.cpp:12-22
+                st["state"] = np.zeros(l.size, np.float32)
+                st["bold"] = np.zeros(l.size, np.float32)
+            elif l.model == "som":   # som_attributes.cpp:100-106
+                st["plasticity"] = np.zeros(l.size, np.float32)
+                l.winner = 0
             l.iteration = 0     # sine / Poisson generator step count
             if l.model == "spnet":   # spnet_attributes.cpp:369-425
                 for k in ("voltage", "recovery", "post trace"):
@@ -476,6 +482,14 @@ class OracleNetwork:
             self.matrix[c] = m = {"weights": w}
             if c.so_host:  # weight_matrix.cpp:79-80 (not readable through the getters)
                 self.so_weights[c] = np.zeros(c.num_weights, np.float32)
+            if c.to.model == "som":   # som_attributes.cpp:108-121
+                m["output cache"] = np.zeros(c.num_weights, np.float32)
+                c.learning_rate = c.p.get_float("learning rate", 0.01)
+                c.neighbor_learning_rate = c.p.get_float("neighbor learning rate", 0.001)
+                c.neighborhood_size = c.p.get_int("neighborhood size", 2)
+            if c.to.model in ("som", "oscillator") and (c.second_order or
+                                                        (c.to.model == "som" and c.convolutional)):
+                raise ValueError("Unimplemented connection type!")
             if c.to.model == "spnet":   # spnet_attributes.cpp:440-494
                 n = c.num_weights
                 m["presyn trace"] = np.zeros(n, np.float32)
@@ -630,8 +644,11 @@ class OracleNetwork:
         inputs = inputs or {}
         L = lib()
         # init / input transfer into register 0 (instruction.cpp:3-30,
-        # instruction.h:474-489)
+        # instruction.h:474-489), and the models' init keys
+        # (cluster_node.cpp:46-50)
         for l in self.layers:
+            if l.model == "oscillator":
+                self.neuron[l]["bold"][:] = 0.0
             reg0 = self.neuron[l]["input"][:l.size]
             init = l.p.child("init config")
             is_input = l.name in inputs
@@ -670,15 +687,22 @@ class OracleNetwork:
         # plasticity
         if learning:
             for c in self.conns:
-                if c.plastic and c.to.model == "perceptron":
-                    raise ValueError("perceptron learning reads source outputs that the reference "
-                                     "binds only in feedforward structures")
+                if c.plastic and c.to.model in ("perceptron", "oscillator"):
+                    raise ValueError(c.to.model + " learning reads source outputs that the "
+                                     "reference binds only in feedforward structures")
             for l in self.layers:
                 for c in l.inputs:
                     if c.plastic and c.to.model == "izhikevich":
                         self._learn(L, c)
                     elif c.plastic and c.to.model == "spnet":
                         self._learn_spnet(L, c)
+                    elif c.plastic and c.to.model == "som":   # som_attributes.cpp:58-79
+                        m = self.matrix[c]
+                        L.sg_upd_som(c.rows, _p(c.dst), _p(c.ptr), _p(c.w_idx), c.to.cols, c.to.winner,
+                                     _p(self.neuron[c.to]["plasticity"]), _p(m["output cache"]),
+                                     ctypes.c_float(c.learning_rate),
+                                     ctypes.c_float(c.neighbor_learning_rate), c.neighborhood_size,
+                                     _p(m["weights"]))
 
     def run(self, steps, input_fn=None, learning=True, record=None):
         """record: list of (layer, key) recorded after every step."""
@@ -718,6 +742,14 @@ class OracleNetwork:
             L.sg_act_spnet(*geo, _p(src), c.frm.output_type, _p(m["weights"]), _p(m["delays"]),
                            _p(m["time since spike"]), ctypes.c_float(c.baseline_conductance),
                            c.opcode, _p(reg))
+            return
+        if c.to.model == "oscillator":
+            L.sg_act_oscillator(*geo, _p(src), c.frm.output_type, c.delay, c.opcode,
+                                _p(m["weights"]), _p(reg), _p(st["bold"]))
+            return
+        if c.to.model == "som":
+            L.sg_act_som(*geo, _p(src), c.frm.output_type, c.delay, int(c.opcode == OPCODES["modulate"]),
+                         _p(m["weights"]), _p(m["output cache"]), _p(reg), _p(st["plasticity"]))
             return
         if c.to.model == "perceptron":   # perceptron_attributes.cpp:35-47
             if c.second_order or c.convolutional:
@@ -759,6 +791,16 @@ class OracleNetwork:
             L.sg_spnet_neurons(l.size, l.history, _p(st["input"]), _p(st["output"]),
                                *[_p(st[k]) for k in ("voltage", "recovery", "post trace",
                                                      "time since spike", "a", "b", "c", "d")])
+        elif l.model == "oscillator":
+            L.sg_oscillator(l.size, l.history, ctypes.c_float(l.p.get_float("tonic", 0.0)),
+                            ctypes.c_float(l.p.get_float("tau", 0.1)),
+                            ctypes.c_float(l.p.get_float("decay", 0.1)), _p(st["input"]),
+                            _p(st["state"]), _p(st["bold"]), _p(st["output"]))
+        elif l.model == "som":
+            w = ctypes.c_int()
+            L.sg_som(l.size, l.history, ctypes.c_float(l.p.get_float("rbf scale", 1.0)),
+                     _p(st["input"]), _p(st["output"]), ctypes.byref(w))
+            l.winner = w.value
         elif l.model == "binary threshold":
             L.sg_bin_thresh(l.size, l.history, _p(st["input"]), _p(st["output"]))
         elif l.model == "perceptron":

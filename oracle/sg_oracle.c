@@ -19,6 +19,7 @@
  *   divergent        w[to * (n_w / to_size) + k] / w[k]  synapse_kernel.h:567-570
  */
 #include <math.h>
+#include <stdlib.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -542,6 +543,91 @@ void sg_poisson_gen(int size, int history, const float *draws, const float *inpu
                     uint32_t *spikes) {
     for (int nid = 0; nid < size; ++nid)
         shift_bit(spikes, size, history, nid, draws[nid] < inputs[nid]);
+}
+
+/* oscillator activator (oscillator_attributes.cpp:60-92) */
+void sg_act_oscillator(int rows, const int *dst, const long *ptr, const int *from_idx,
+                       const int *w_idx, const uint32_t *src_words, int src_type, int delay,
+                       int opcode, const float *weights, float *inputs, float *bold) {
+    for (int r = 0; r < rows; ++r) {
+        float sum = 0.0, abs_sum = 0.0;
+        for (long v = ptr[r]; v < ptr[r + 1]; ++v) {
+            float val = extract(src_words[from_idx[v]], delay, src_type) * weights[w_idx[v]];
+            sum += val;
+            abs_sum += fabsf(val);
+        }
+        inputs[dst[r]] = aggregate(inputs[dst[r]], sum, opcode);
+        bold[dst[r]] += abs_sum;
+    }
+}
+
+/* oscillator update (oscillator_attributes.cpp:38-55) */
+void sg_oscillator(int size, int history, float tonic, float tau, float decay,
+                   const float *inputs, float *state, float *bold, float *outputs) {
+    for (int nid = 0; nid < size; ++nid) {
+        float st = state[nid];
+        float recur = st + (decay * (tonic - st));
+        state[nid] = st = (tau * inputs[nid]) + recur;
+        bold[nid] += recur;
+        float t = tanhf(st);
+        shift_float(outputs, size, history, nid, (0.0f > t) ? 0.0f : t);
+    }
+}
+
+/* som activators (som_attributes.cpp:35-56): squared distance added to the
+ * input (outputs cached per synapse), or for "modulate" the plasticity */
+void sg_act_som(int rows, const int *dst, const long *ptr, const int *from_idx,
+                const int *w_idx, const uint32_t *src_words, int src_type, int delay,
+                int modulate, const float *weights, float *cache, float *inputs,
+                float *plasticity) {
+    for (int r = 0; r < rows; ++r) {
+        float acc = 0.0;
+        for (long v = ptr[r]; v < ptr[r + 1]; ++v) {
+            int w = w_idx[v];
+            float out = extract(src_words[from_idx[v]], delay, src_type);
+            if (modulate) {
+                acc += weights[w] * out;
+            } else {
+                float val = out - weights[w];
+                cache[w] = out;
+                acc += val * val;
+            }
+        }
+        if (modulate) plasticity[dst[r]] = acc;
+        else inputs[dst[r]] += acc;
+    }
+}
+
+/* som update (som_attributes.cpp:13-31): winner, then exp(-rbf * x^2) */
+void sg_som(int size, int history, float rbf_scale, const float *inputs, float *outputs,
+            int *winner) {
+    float min = inputs[0];
+    int min_node = 0;
+    for (int i = 0; i < size; ++i)
+        if (inputs[i] < min) { min = inputs[i]; min_node = i; }
+    *winner = min_node;
+    for (int nid = 0; nid < size; ++nid) {
+        float input = inputs[nid];
+        shift_float(outputs, size, history, nid, expf(-rbf_scale * (input * input)));
+    }
+}
+
+/* som updater (som_attributes.cpp:58-79) */
+void sg_upd_som(int rows, const int *dst, const long *ptr, const int *w_idx, int to_cols,
+                int winner, const float *plasticity, const float *cache, float lr, float nlr,
+                int nbhd, float *weights) {
+    int wr = winner / to_cols, wc = winner % to_cols;
+    for (int r = 0; r < rows; ++r) {
+        int to = dst[r];
+        int rd = abs(wr - (to / to_cols)), cd = abs(wc - (to % to_cols));
+        for (long v = ptr[r]; v < ptr[r + 1]; ++v) {
+            int w = w_idx[v];
+            if (to == winner)
+                weights[w] += plasticity[to] * lr * (cache[w] - weights[w]);
+            else if (rd + cd <= nbhd)
+                weights[w] += plasticity[to] * nlr * (cache[w] - weights[w]);
+        }
+    }
 }
 
 void sg_rate(int size, int history, const float *inputs, float *outputs) {

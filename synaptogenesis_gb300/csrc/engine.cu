@@ -295,6 +295,7 @@ void Engine::enqueue_step(bool last) {
         Layer* l = lp.get();
         const Model* m = find_model(l->model);
         LayerState* ls = state_->layer_state(l);
+        m->begin_step(*state_, *ls, ctx);
         float* in = ls->input->df();
         bool is_input = (layer_io_[l->index] & 1) != 0;
         bool all_fused = !l->inputs.empty() && !l->has_dendrites();

@@ -1,6 +1,6 @@
 // The reference's smaller neural models: binary threshold, the two
-// rate-encoding variants, perceptron, sine generator and Poisson generator
-// (src/core/state/impl/*_attributes.cpp).  Each update is one thread per
+// rate-encoding variants, perceptron, sine generator, Poisson generator,
+// oscillator and self-organising map (src/core/state/impl/*_attributes.cpp).  Each update is one thread per
 // neuron over the layer's input register and output history.
 #include <cmath>
 
@@ -236,5 +236,246 @@ class PoissonGeneratorModel : public Model {
     }
 };
 SG_REGISTER_MODEL(PoissonGeneratorModel);
+
+// ---------------------------------------------------------------------------
+// oscillator (oscillator_attributes.cpp): a leaky state relaxing towards
+// "tonic", output max(0, tanh(state)), and a "bold" signal -- cleared every
+// step (its init key), then the absolute synaptic inputs and the leak added.
+// Its updaters read source outputs the reference binds only in feedforward
+// structures, and its second-order kernels write the weight copy of the
+// slave's own matrix (which only hosts have): both are refused here.
+// ---------------------------------------------------------------------------
+template <int TY, int SR>
+__global__ void __launch_bounds__(128) k_activate_oscillator(DGeom g, const uint32_t* __restrict__ src,
+                                                             int delay, int opcode,
+                                                             const float* __restrict__ w,
+                                                             float* __restrict__ inputs,
+                                                             float* __restrict__ bold) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= g.n_dest) return;
+    float sum = 0.0f, abs_sum = 0.0f;
+    for_each_source<TY>(g, d, [&](int from, int wi) {
+        const float val = extract<SR>(src[from], delay) * w[wi];
+        sum += val;
+        abs_sum += fabsf(val);
+    });
+    const int to = dest_of<TY>(g, d);
+    inputs[to] = aggregate(inputs[to], sum, opcode);
+    bold[to] += abs_sum;
+}
+
+__global__ void k_oscillator(int size, int history, float tonic, float tau, float decay,
+                             const float* __restrict__ in, float* state, float* bold, float* out) {
+    const int nid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nid >= size) return;
+    float st = state[nid];
+    const float recur = st + (decay * (tonic - st));
+    state[nid] = st = (tau * in[nid]) + recur;
+    bold[nid] += recur;
+    const float t = tanhf(st);
+    shift_floats(out, size, history, nid, (0.0f > t) ? 0.0f : t);
+}
+
+class OscillatorModel : public Model {
+  public:
+    const char* name() const override { return "oscillator"; }
+    OutputType output_type() const override { return OUT_FLOAT; }
+    void build_layer(State& st, LayerState& ls) const override {
+        const Layer& l = *ls.layer;
+        ls.params["tonic"] = std::stof(l.parameter("tonic", "0.0"));
+        ls.params["tau"] = std::stof(l.parameter("tau", "0.1"));
+        ls.params["decay"] = std::stof(l.parameter("decay", "0.1"));
+        ls.vars["state"] = st.add_array("state", 'f', l.size);
+        ls.vars["bold"] = st.add_array("bold", 'f', l.size);
+    }
+    void build_matrix(State&, ConnState& cs) const override {
+        if (cs.conn->second_order) throw SgError(cs.conn->str() + ": Unimplemented connection type!");
+    }
+    std::string learning_error(const Connection&) const override {
+        return "oscillator learning reads source outputs that the reference binds only in "
+               "feedforward structures (set \"plastic\": false or run without learning)";
+    }
+    void begin_step(State&, LayerState& ls, const StepCtx& ctx) const override {
+        SG_CUDA(cudaMemsetAsync(ls.var("bold")->df(), 0, (size_t)ls.layer->size * 4, ctx.stream));
+    }
+    void activate(State& st, ConnState& cs, const StepCtx& ctx) const override {
+        const Connection& c = *cs.conn;
+        const uint32_t* src = st.dev_output(c.from, word_index(c.delay, c.from->output_type));
+        float* bold = st.layer_state(c.to)->var("bold")->df();
+        SG_DISPATCH_TYPE_SRC((int)c.type, (int)c.from->output_type,
+            (k_activate_oscillator<TY, SR><<<blocks_for(cs.geom.n_dest, 128), 128, 0, ctx.stream>>>(
+                cs.geom, src, c.delay, (int)c.opcode, cs.weights->df(), input_register(st, cs), bold)));
+        SG_LAUNCH_CHECK();
+        ctx.count();
+    }
+    void update(State&, LayerState& ls, const StepCtx& ctx) const override {
+        const Layer& l = *ls.layer;
+        k_oscillator<<<blocks_for(l.size, 256), 256, 0, ctx.stream>>>(
+            l.size, l.history(), ls.params.at("tonic"), ls.params.at("tau"), ls.params.at("decay"),
+            ls.input->df(), ls.var("state")->df(), ls.var("bold")->df(), ls.output->df());
+        SG_LAUNCH_CHECK();
+        ctx.count();
+    }
+};
+SG_REGISTER_MODEL(OscillatorModel);
+
+// ---------------------------------------------------------------------------
+// som (som_attributes.cpp): synaptic input is the squared distance between
+// the sources' outputs and the weights (added, whatever the opcode), with
+// the outputs cached per synapse; "modulate" connections set the neuron's
+// plasticity instead.  The update finds the winner (first neuron of least
+// input) and outputs exp(-rbf scale * input^2); learning pulls the winner's
+// weights (and, slower, those within the Manhattan neighbourhood) towards
+// the cached outputs.  A convolutional connection's cache entry would be
+// written by every destination in turn: refused here.
+// ---------------------------------------------------------------------------
+template <int TY, int SR, bool MOD>
+__global__ void __launch_bounds__(128) k_activate_som(DGeom g, const uint32_t* __restrict__ src,
+                                                      int delay, const float* __restrict__ w,
+                                                      float* __restrict__ cache,
+                                                      float* __restrict__ inputs,
+                                                      float* __restrict__ plasticity) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= g.n_dest) return;
+    float acc = 0.0f;
+    for_each_source<TY>(g, d, [&](int from, int wi) {
+        const float out = extract<SR>(src[from], delay);
+        if (MOD) {
+            acc += w[wi] * out;
+        } else {
+            const float val = out - w[wi];
+            cache[wi] = out;
+            acc += val * val;
+        }
+    });
+    const int to = dest_of<TY>(g, d);
+    if (MOD) plasticity[to] = acc;
+    else inputs[to] += acc;
+}
+
+// The serial scan's winner (som_attributes.cpp:18-27): starting from neuron
+// 0, each strictly smaller input takes over, so the winner is the first
+// neuron of least (non-NaN) input, or 0 when input 0 is NaN.  One block: a
+// strided scan per thread, then a tree that keeps the lower index on ties.
+__global__ void __launch_bounds__(1024) k_som_winner(int size, const float* __restrict__ in, int* winner) {
+    __shared__ float sv[1024];
+    __shared__ int si[1024];
+    float best = 0.0f;
+    int bi = -1;
+    for (int i = threadIdx.x; i < size; i += blockDim.x) {
+        const float v = in[i];
+        if (v == v && (bi < 0 || v < best)) { best = v; bi = i; }
+    }
+    sv[threadIdx.x] = best;
+    si[threadIdx.x] = bi;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) {
+            const float ov = sv[threadIdx.x + h], mv = sv[threadIdx.x];
+            const int oi = si[threadIdx.x + h], mi = si[threadIdx.x];
+            if (oi >= 0 && (mi < 0 || ov < mv || (ov == mv && oi < mi))) {
+                sv[threadIdx.x] = ov;
+                si[threadIdx.x] = oi;
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *winner = (si[0] < 0 || in[0] != in[0]) ? 0 : si[0];
+}
+
+__global__ void k_som(int size, int history, float rbf_scale, const float* __restrict__ in, float* out) {
+    const int nid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nid >= size) return;
+    const float input = in[nid];
+    shift_floats(out, size, history, nid, expf(-rbf_scale * (input * input)));
+}
+
+template <int TY>
+__global__ void __launch_bounds__(128) k_learn_som(DGeom g, const int* __restrict__ winner,
+                                                   const float* __restrict__ plasticity,
+                                                   const float* __restrict__ cache, float lr, float nlr,
+                                                   int nbhd, float* w) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= g.n_dest) return;
+    const int to = dest_of<TY>(g, d);
+    const int win = *winner;
+    const int row_dist = abs(win / g.to_cols - to / g.to_cols);
+    const int col_dist = abs(win % g.to_cols - to % g.to_cols);
+    const bool is_win = to == win;
+    if (!is_win && row_dist + col_dist > nbhd) return;
+    const float rate = is_win ? lr : nlr;
+    const float p = plasticity[to];
+    for_each_source<TY>(g, d, [&](int, int wi) { w[wi] += p * rate * (cache[wi] - w[wi]); });
+}
+
+class SomModel : public Model {
+  public:
+    const char* name() const override { return "som"; }
+    OutputType output_type() const override { return OUT_FLOAT; }
+    void build_layer(State& st, LayerState& ls) const override {
+        ls.params["rbf scale"] = std::stof(ls.layer->parameter("rbf scale", "1"));
+        ls.vars["plasticity"] = st.add_array("plasticity", 'f', ls.layer->size);
+        ls.internal["winner"] = st.add_array("winner", 'i', 1);
+    }
+    void build_matrix(State& st, ConnState& cs) const override {
+        const Connection& c = *cs.conn;
+        if (c.second_order || c.convolutional) throw SgError(c.str() + ": Unimplemented connection type!");
+        cs.params["learning rate"] = std::stof(c.parameter("learning rate", "0.01"));
+        cs.params["neighbor learning rate"] = std::stof(c.parameter("neighbor learning rate", "0.001"));
+        cs.params["neighborhood size"] = (float)std::stoi(c.parameter("neighborhood size", "2"));
+        cs.vars["output cache"] = st.add_array("output cache", 'f', c.num_weights, matrix_layout(c),
+                                               c.matrix_rows, c.matrix_cols);
+    }
+    void activate(State& st, ConnState& cs, const StepCtx& ctx) const override {
+        const Connection& c = *cs.conn;
+        const uint32_t* src = st.dev_output(c.from, word_index(c.delay, c.from->output_type));
+        float* plast = st.layer_state(c.to)->var("plasticity")->df();
+        const unsigned blocks = blocks_for(cs.geom.n_dest, 128);
+        if (c.opcode == OP_MODULATE) {
+            SG_DISPATCH_TYPE_SRC((int)c.type, (int)c.from->output_type,
+                (k_activate_som<TY, SR, true><<<blocks, 128, 0, ctx.stream>>>(
+                    cs.geom, src, c.delay, cs.weights->df(), cs.var("output cache")->df(),
+                    input_register(st, cs), plast)));
+        } else {
+            SG_DISPATCH_TYPE_SRC((int)c.type, (int)c.from->output_type,
+                (k_activate_som<TY, SR, false><<<blocks, 128, 0, ctx.stream>>>(
+                    cs.geom, src, c.delay, cs.weights->df(), cs.var("output cache")->df(),
+                    input_register(st, cs), plast)));
+        }
+        SG_LAUNCH_CHECK();
+        ctx.count();
+    }
+    void update(State&, LayerState& ls, const StepCtx& ctx) const override {
+        const Layer& l = *ls.layer;
+        k_som_winner<<<1, 1024, 0, ctx.stream>>>(l.size, ls.input->df(), ls.internal.at("winner")->di());
+        SG_LAUNCH_CHECK();
+        k_som<<<blocks_for(l.size, 256), 256, 0, ctx.stream>>>(l.size, l.history(), ls.params.at("rbf scale"),
+                                                              ls.input->df(), ls.output->df());
+        SG_LAUNCH_CHECK();
+        ctx.count(2);
+    }
+    bool learns(const Connection&) const override { return true; }
+    void learn(State& st, ConnState& cs, const StepCtx& ctx) const override {
+        const Connection& c = *cs.conn;
+        LayerState& to = *st.layer_state(c.to);
+        const unsigned blocks = blocks_for(cs.geom.n_dest, 128);
+        const int* win = to.internal.at("winner")->di();
+        const float* plast = to.var("plasticity")->df();
+        const float* cache = cs.var("output cache")->df();
+        const float lr = cs.params.at("learning rate"), nlr = cs.params.at("neighbor learning rate");
+        const int nb = (int)cs.params.at("neighborhood size");
+        switch ((int)c.type) {
+            case 0: k_learn_som<0><<<blocks, 128, 0, ctx.stream>>>(cs.geom, win, plast, cache, lr, nlr, nb, cs.weights->df()); break;
+            case 1: k_learn_som<1><<<blocks, 128, 0, ctx.stream>>>(cs.geom, win, plast, cache, lr, nlr, nb, cs.weights->df()); break;
+            case 2: k_learn_som<2><<<blocks, 128, 0, ctx.stream>>>(cs.geom, win, plast, cache, lr, nlr, nb, cs.weights->df()); break;
+            case 3: k_learn_som<3><<<blocks, 128, 0, ctx.stream>>>(cs.geom, win, plast, cache, lr, nlr, nb, cs.weights->df()); break;
+            case 4: k_learn_som<4><<<blocks, 128, 0, ctx.stream>>>(cs.geom, win, plast, cache, lr, nlr, nb, cs.weights->df()); break;
+            case 5: k_learn_som<5><<<blocks, 128, 0, ctx.stream>>>(cs.geom, win, plast, cache, lr, nlr, nb, cs.weights->df()); break;
+        }
+        SG_LAUNCH_CHECK();
+        ctx.count();
+    }
+};
+SG_REGISTER_MODEL(SomModel);
 
 }  // namespace sg

@@ -52,6 +52,9 @@ class Model {
     virtual bool fuses_input(State& st, const Connection& c, const StepCtx& ctx) const {
         return false;
     }
+    // Start of a step, before any synaptic input: per-layer buffers the
+    // reference re-initialises every step (get_init_keys, cluster_node.cpp:46-50).
+    virtual void begin_step(State& st, LayerState& ls, const StepCtx& ctx) const {}
     // Neuron update of one layer.
     virtual void update(State& st, LayerState& ls, const StepCtx& ctx) const = 0;
     // Update several layers of this model at once (their updates touch only

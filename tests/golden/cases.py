@@ -619,6 +619,38 @@ def cases():
                     + [("neuron", "n", "inh", k) for k in ("voltage", "recovery")]
                     + [("matrix", c, k) for c in ("n_rec", "n_ie")
                        for k in ("weights", "presyn trace", "weight derivative", "time since spike")]))
+
+    # --- oscillator and self-organising map --------------------------------
+    net = {"structures": [{"name": "o", "type": "parallel", "layers": [
+        _layer("src", "relay", 6, 8),
+        _layer("mod", "relay", 4, 4),
+        _layer("osc", "oscillator", 6, 8, tonic=0.2, tau=0.3, decay=0.2),
+        _layer("som", "som", 5, 5, **{"rbf scale": 0.002}),
+    ]}], "connections": [
+        {"name": "o_conv", "from layer": "src", "to layer": "osc", "type": "convergent",
+         "opcode": "add", "plastic": False, "arborized config": {"field size": 3, "wrap": True}},
+        {"name": "o_one", "from layer": "src", "to layer": "osc", "type": "one to one",
+         "opcode": "sub", "plastic": False},
+        {"name": "s_fc", "from layer": "src", "to layer": "som", "type": "fully connected",
+         "opcode": "add", "plastic": True, "learning rate": 0.05, "neighborhood size": 1},
+        {"name": "s_mod", "from layer": "mod", "to layer": "som", "type": "fully connected",
+         "opcode": "modulate", "plastic": False},
+    ]}
+
+    def inj_osc_som(rng, sizes):
+        return {
+            ("matrix", "o_conv", "weights"): rng.uniform(-1.0, 1.0, sizes["conn:o_conv"]).astype(np.float32),
+            ("matrix", "o_one", "weights"): rng.uniform(-1.0, 1.0, sizes["conn:o_one"]).astype(np.float32),
+            ("matrix", "s_fc", "weights"): rng.uniform(-1.0, 1.0, sizes["conn:s_fc"]).astype(np.float32),
+            ("matrix", "s_mod", "weights"): rng.uniform(0.0, 0.2, sizes["conn:s_mod"]).astype(np.float32),
+        }
+    out.append(Case("oscillator_som", net, 40, 121, inject=inj_osc_som,
+                    inputs={"src": lambda rng, t, n: rng.normal(0.0, 1.0, n),
+                            "mod": lambda rng, t, n: rng.uniform(0.0, 1.0, n)},
+                    record=[("o", "osc"), ("o", "som")],
+                    final=[("neuron", "o", "osc", k) for k in ("state", "bold", "input")]
+                    + [("neuron", "o", "som", k) for k in ("plasticity", "input")]
+                    + [("matrix", "s_fc", k) for k in ("weights", "output cache")]))
     return out
 
 

@@ -3,9 +3,9 @@ recorded results (bit-exact), and against the oracle.
 
 Bit-exact: spike rasters, output-history words, voltages, recoveries,
 conductances, traces, weights and all integer state.  Two allowances, both
-written here: rate_encoding outputs go through tanhf (the GPU's tanhf and the
-host C library's may differ in the last bit), so they compare with relative
-tolerance 1e-5; and in fp32 arrays any two NaNs match (x86, Arm and the GPU
+written here: outputs that go through tanhf or expf (rate encoding and its
+variants, oscillator, som; the GPU's and the host C library's may differ in
+the last bit) compare with relative tolerance 1e-5; and in fp32 arrays any two NaNs match (x86, Arm and the GPU
 each produce a different default NaN payload for 0/0).
 """
 import pytest
@@ -15,7 +15,8 @@ from tests.harness import compare, float_like_keys, load_fixture, run_library, r
 
 pytestmark = pytest.mark.gpu
 
-RATE_KEYS = ("rec/s/one", "rec/s/div", "rec/d/rtree", "rec/p/sdiv", "rec/m/hb")
+RATE_KEYS = ("rec/s/one", "rec/s/div", "rec/d/rtree", "rec/p/sdiv", "rec/m/hb", "rec/o/osc",
+             "rec/o/som")
 RATE_TOL = 1e-5
 
 

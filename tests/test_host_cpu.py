@@ -43,7 +43,7 @@ def test_library_exports_every_header_function(sg):
 
 @pytest.mark.parametrize("name", ["iz_opcodes", "iz_plastic", "base_all_types", "iz_c0_8",
                                   "gol_two_word_history", "dendrites", "second_order", "sparse",
-                                  "models", "spnet"])
+                                  "models", "spnet", "oscillator_som"])
 def test_initial_state_matches_oracle(sg, name):
     from oracle.oracle import OracleNetwork
     from tests.golden.cases import CASES
@@ -223,6 +223,12 @@ def test_model_build_errors_match_the_reference(sg):
     n = sg.Network(net)
     n.build_state()
     assert n.state is None and "Unimplemented connection type" in sg.last_error()
+    net["structures"][0]["layers"][1]["neural model"] = "som"
+    n = sg.Network(net)
+    n.build_state()
+    assert n.state is None and "Unimplemented connection type" in sg.last_error()
+    with pytest.raises(ValueError, match="Unimplemented connection type"):
+        OracleNetwork(net)
 
 
 def test_izhikevich_gap_must_be_self_connection(sg):
