@@ -34,7 +34,8 @@ OPCODES = {"add": 0, "sub": 1, "mult": 2, "div": 3, "pool": 4, "reward": 5, "mod
 MODELS = {"izhikevich": BIT, "relay": FLOAT, "game_of_life": BIT, "rate_encoding": FLOAT,
           "binary threshold": FLOAT, "backprop_rate_encoding": FLOAT,
           "hebbian_rate_encoding": FLOAT, "perceptron": FLOAT, "sine generator": FLOAT,
-          "poisson generator": BIT, "spnet": BIT, "oscillator": FLOAT, "som": FLOAT}
+          "poisson generator": BIT, "spnet": BIT, "oscillator": FLOAT, "som": FLOAT,
+          "nvm": FLOAT, "nvm_heaviside": FLOAT, "nvm_compare": FLOAT}
 GLOBAL_SEED = 0x5EED5EED     # the library's default sg_set_seed value
 # Which sine the reference's sine generator evaluates: its unqualified
 # sin(float) resolves to the C library's double sin (pinned by the fixture).
@@ -451,6 +452,17 @@ class OracleNetwork:
             elif l.model == "oscillator":   # oscillator_attributes.cpp:12-22
                 st["state"] = np.zeros(l.size, np.float32)
                 st["bold"] = np.zeros(l.size, np.float32)
+            elif l.model.startswith("nvm"):   # nvm_attributes.cpp:12-27
+                off = np.float32(1.0 - float(np.float32(l.p.get("noise offset", "0.5"))))
+                if off > 1.0 or off < 0.0:
+                    raise ValueError("Noise offset must be in [0,1]!")
+                st["state"] = np.zeros(l.size, np.float32)
+                st["context"] = np.ones(l.size, np.float32)
+                if l.model == "nvm_compare":
+                    st["true_state"] = np.zeros(l.size, np.float32)
+                    l.tolerance = np.float32(1.0 - float(np.float32(l.p.get("tolerance", "1.0"))))
+                l.gates = np.array([1.0, 0.0, 0.0], np.float32)   # activity, learning, noise
+                l.gain = np.float32(l.p.get("gain", "1."))
             elif l.model == "som":   # som_attributes.cpp:100-106
                 st["plasticity"] = np.zeros(l.size, np.float32)
                 l.winner = 0
@@ -743,6 +755,9 @@ class OracleNetwork:
                            _p(m["time since spike"]), ctypes.c_float(c.baseline_conductance),
                            c.opcode, _p(reg))
             return
+        if c.to.model.startswith("nvm"):
+            self._activate_nvm(L, c, st, m, src, geo, reg)
+            return
         if c.to.model == "oscillator":
             L.sg_act_oscillator(*geo, _p(src), c.frm.output_type, c.delay, c.opcode,
                                 _p(m["weights"]), _p(reg), _p(st["bold"]))
@@ -791,6 +806,11 @@ class OracleNetwork:
             L.sg_spnet_neurons(l.size, l.history, _p(st["input"]), _p(st["output"]),
                                *[_p(st[k]) for k in ("voltage", "recovery", "post trace",
                                                      "time since spike", "a", "b", "c", "d")])
+        elif l.model.startswith("nvm"):
+            if l.gates[2] != 0.0:
+                raise ValueError("oracle: NVM noise draws are not restated")
+            L.sg_nvm_update(int(l.model != "nvm"), l.size, l.history, _p(st["input"]), _p(st["state"]),
+                            _p(st["context"]), _p(st["output"]), ctypes.c_float(l.gain))
         elif l.model == "oscillator":
             L.sg_oscillator(l.size, l.history, ctypes.c_float(l.p.get_float("tonic", 0.0)),
                             ctypes.c_float(l.p.get_float("tau", 0.1)),
@@ -843,3 +863,46 @@ class OracleNetwork:
                        ctypes.c_float(c.max_weight), _p(st["post trace"]), _p(st["time since spike"]),
                        _p(st["output"][:c.to.size]), _p(m["time since spike"]), _p(m["weights"]),
                        _p(m["presyn trace"]), _p(m["weight derivative"]))
+
+    def _activate_nvm(self, L, c, st, m, src, geo, reg):
+        """NVM activator choice (nvm_attributes.cpp:163-187,
+        nvm_compare_attributes.cpp:60-69) and the layer's gates."""
+        if c.second_order:
+            raise ValueError("Unimplemented connection type!")
+        l = c.to
+        flag = lambda k: c.p.get(k, "false") == "true"
+        kinds = [("decay", 0), ("gate", 1), ("learning", 2), ("noise", 3)]
+        if not (l.model == "nvm_compare" and c.plastic):
+            for name, g in kinds:
+                if flag(name):
+                    if c.c.type == 1:   # a subset window (an empty one writes nothing)
+                        gv = np.float32(lib_gate(L, c, src))
+                        if g == 0:
+                            l.gates[0] = np.float32(1.0) - gv
+                        else:
+                            l.gates[{1: 0, 2: 1, 3: 2}[g]] = gv
+                    return
+            if flag("context"):
+                L.sg_act_nvm_context(c.frm.size, _p(src), c.frm.output_type, c.delay, c.opcode,
+                                     _p(m["weights"]), ctypes.c_float(l.gates[0]), _p(st["context"]))
+                return
+        if l.model == "nvm_compare" and c.plastic:
+            kind = 3
+        elif c.plastic:
+            kind = 2
+        elif flag("gated"):
+            kind = 1
+        else:
+            kind = 0
+        truth = st["true_state"] if l.model == "nvm_compare" else st["state"]
+        L.sg_act_nvm(kind, *geo, _p(src), c.frm.output_type, c.delay, c.opcode, _p(m["weights"]),
+                     _p(reg), ctypes.c_float(l.gates[0]), ctypes.c_float(l.gates[1]),
+                     _p(st["state"]), _p(st["context"]), _p(truth),
+                     ctypes.c_float(c.p.get_float("norm", 1.0)), c.num_weights // l.size,
+                     ctypes.c_float(getattr(l, "tolerance", 0.0)))
+
+
+def lib_gate(L, c, src):
+    L.sg_nvm_gate.restype = ctypes.c_float
+    return L.sg_nvm_gate(ctypes.byref(c.c), _p(src), c.frm.output_type, c.delay,
+                         int(c.p.get("decay", "false") == "true"))

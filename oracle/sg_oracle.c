@@ -630,6 +630,87 @@ void sg_upd_som(int rows, const int *dst, const long *ptr, const int *w_idx, int
     }
 }
 
+/* NVM gate connection (nvm_attributes.cpp:61-95): the subset window's
+ * sources reduced by min from 1 (decay) or max from 0; returns the value */
+float sg_nvm_gate(const sg_conn *c, const uint32_t *src_words, int src_type, int delay,
+                  int decay) {
+    float gv = decay ? 1.0f : 0.0f;
+    for (int fr = c->fr0; fr < c->fr1; ++fr)
+        for (int fc = c->fc0; fc < c->fc1; ++fc) {
+            float v = extract(src_words[fr * c->from_cols + fc], delay, src_type);
+            gv = decay ? ((gv < v) ? gv : v) : ((gv > v) ? gv : v);
+        }
+    return gv;
+}
+
+/* NVM activators (nvm_attributes.cpp:97-160, nvm_compare_attributes.cpp:
+ * 26-58): kind 0 plain, 1 gated, 2 plastic, 3 compare-plastic */
+void sg_act_nvm(int kind, int rows, const int *dst, const long *ptr, const int *from_idx,
+                const int *w_idx, const uint32_t *src_words, int src_type, int delay,
+                int opcode, float *weights, float *inputs, float ag, float lg,
+                const float *state, const float *context, const float *true_state,
+                float norm_param, int per_neuron, float tolerance) {
+    if (kind == 1 && ag < 0.5f) return;
+    if ((kind == 2 || kind == 3) && ag < 0.5f && lg < 0.5f) return;
+    float norm = (kind == 2) ? norm_param * per_neuron : norm_param;
+    for (int r = 0; r < rows; ++r) {
+        int to = dst[r];
+        if ((kind == 1 || kind == 2) && !(context[to] > 0.5f)) continue;
+        float sum = 0.0;
+        for (long v = ptr[r]; v < ptr[r + 1]; ++v)
+            sum += extract(src_words[from_idx[v]], delay, src_type) * weights[w_idx[v]];
+        if (kind <= 1) {
+            inputs[to] = aggregate(inputs[to], sum, opcode);
+        } else if (kind == 2) {
+            if (ag > 0.5f) inputs[to] = aggregate(inputs[to], sum, opcode);
+            if (lg > 0.5f) {
+                float temp = state[to] - sum;
+                for (long v = ptr[r]; v < ptr[r + 1]; ++v)
+                    weights[w_idx[v]] += extract(src_words[from_idx[v]], delay, src_type) * temp / norm;
+            }
+        } else {
+            if (ag > 0.5f) {
+                sum -= true_state[to] * ((tolerance * per_neuron) - 1);
+                inputs[to] = ag * aggregate(inputs[to], sum, opcode);
+            }
+            if (lg > 0.5f) {
+                float temp = inputs[to] = true_state[to];
+                for (long v = ptr[r]; v < ptr[r + 1]; ++v)
+                    weights[w_idx[v]] = extract(src_words[from_idx[v]], delay, src_type) * temp / norm;
+            }
+        }
+    }
+}
+
+/* NVM context connection (nvm_attributes.cpp:150-160): the one-to-one loop */
+void sg_act_nvm_context(int n, const uint32_t *src_words, int src_type, int delay, int opcode,
+                        const float *weights, float ag, float *context) {
+    if (ag < 0.5f) return;
+    for (int i = 0; i < n; ++i) {
+        float sum = 0.0;
+        sum += extract(src_words[i], delay, src_type) * weights[i];
+        context[i] = aggregate(context[i], sum, opcode);
+    }
+}
+
+/* nvm / nvm_heaviside updates with the noise gate closed
+ * (nvm_attributes.cpp:38-52, nvm_heaviside_attributes.cpp:11-25) */
+void sg_nvm_update(int heaviside, int size, int history, const float *inputs, float *state,
+                   float *context, float *outputs, float gain) {
+    for (int nid = 0; nid < size; ++nid) {
+        float input = inputs[nid] + 0.;
+        if (!heaviside) {
+            state[nid] = input;
+            context[nid] = 1.;
+            shift_float(outputs, size, history, nid, tanhf(input));
+        } else {
+            state[nid] = gain * ((input > 0) - (input <= 0));
+            context[nid] = 1.;
+            shift_float(outputs, size, history, nid, (float)(input > 0.));
+        }
+    }
+}
+
 void sg_rate(int size, int history, const float *inputs, float *outputs) {
     for (int nid = 0; nid < size; ++nid) {
         float input = inputs[nid];

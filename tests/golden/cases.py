@@ -651,6 +651,62 @@ def cases():
                     final=[("neuron", "o", "osc", k) for k in ("state", "bold", "input")]
                     + [("neuron", "o", "som", k) for k in ("plasticity", "input")]
                     + [("matrix", "s_fc", k) for k in ("weights", "output cache")]))
+
+    # --- neural virtual machine models ------------------------------------
+    # Gate connections (decay, then activity gate, learning gate) from a
+    # control layer; plain, gated, context and plastic connections into nvm;
+    # nvm_heaviside; nvm_compare learning its true state.
+    def window(r0, r1, c0, c1):
+        return {"from row start": 0, "from row end": 1, "from column start": c0,
+                "from column end": c1, "to row start": r0, "to row end": r1,
+                "to column start": 0, "to column end": 4}
+    net = {"structures": [{"name": "v", "type": "parallel", "layers": [
+        _layer("ctl", "relay", 1, 6),
+        _layer("x", "relay", 4, 4),
+        _layer("mem", "nvm", 4, 4),
+        _layer("hv", "nvm_heaviside", 4, 4, gain=2.0),
+        _layer("cmp", "nvm_compare", 4, 4, tolerance=0.75),
+    ]}], "connections": [
+        {"name": "v_decay", "from layer": "ctl", "to layer": "mem", "type": "subset", "decay": True,
+         "plastic": False, "subset config": window(0, 1, 0, 1)},
+        {"name": "v_gate", "from layer": "ctl", "to layer": "mem", "type": "subset", "gate": True,
+         "plastic": False, "subset config": window(0, 2, 1, 3)},
+        {"name": "v_learn", "from layer": "ctl", "to layer": "mem", "type": "subset", "learning": True,
+         "plastic": False, "subset config": window(1, 4, 3, 4)},
+        {"name": "v_plain", "from layer": "x", "to layer": "mem", "type": "one to one",
+         "opcode": "add", "plastic": False},
+        {"name": "v_ctx", "from layer": "x", "to layer": "mem", "type": "one to one",
+         "context": True, "plastic": False},
+        {"name": "v_gated", "from layer": "x", "to layer": "mem", "type": "fully connected",
+         "gated": True, "plastic": False},
+        {"name": "v_rec", "from layer": "mem", "to layer": "mem", "type": "fully connected",
+         "plastic": True, "norm": 2.0},
+        {"name": "h_in", "from layer": "x", "to layer": "hv", "type": "convergent", "plastic": False,
+         "arborized config": {"field size": 3, "wrap": True}},
+        {"name": "h_gated", "from layer": "mem", "to layer": "hv", "type": "one to one",
+         "gated": True, "plastic": False},
+        {"name": "c_gate", "from layer": "ctl", "to layer": "cmp", "type": "subset", "gate": True,
+         "plastic": False, "subset config": window(0, 1, 4, 5)},
+        {"name": "c_learn", "from layer": "ctl", "to layer": "cmp", "type": "subset", "learning": True,
+         "plastic": False, "subset config": window(0, 1, 5, 6)},
+        {"name": "c_plastic", "from layer": "x", "to layer": "cmp", "type": "fully connected",
+         "plastic": True, "norm": 4.0},
+    ]}
+    nvm_conns = [c["name"] for c in net["connections"]]
+
+    def inj_nvm(rng, sizes):
+        d = {("matrix", n, "weights"): rng.uniform(-1.0, 1.0, sizes["conn:" + n]).astype(np.float32)
+             for n in nvm_conns}
+        d[("neuron", "v", "cmp", "true_state")] = np.where(rng.random(16) < 0.5, -1.0, 1.0).astype(np.float32)
+        return d
+    out.append(Case("nvm", net, 40, 131, inject=inj_nvm,
+                    inputs={"ctl": lambda rng, t, n: (rng.random(n) < 0.6) * 1.0,
+                            "x": lambda rng, t, n: rng.normal(0.0, 1.0, n)},
+                    record=[("v", "mem"), ("v", "hv"), ("v", "cmp")],
+                    final=[("neuron", "v", "mem", k) for k in ("state", "context", "input")]
+                    + [("neuron", "v", "hv", k) for k in ("state", "input")]
+                    + [("neuron", "v", "cmp", "input")]
+                    + [("matrix", c, "weights") for c in ("v_rec", "c_plastic")]))
     return out
 
 

@@ -43,7 +43,7 @@ def test_library_exports_every_header_function(sg):
 
 @pytest.mark.parametrize("name", ["iz_opcodes", "iz_plastic", "base_all_types", "iz_c0_8",
                                   "gol_two_word_history", "dendrites", "second_order", "sparse",
-                                  "models", "spnet", "oscillator_som"])
+                                  "models", "spnet", "oscillator_som", "nvm"])
 def test_initial_state_matches_oracle(sg, name):
     from oracle.oracle import OracleNetwork
     from tests.golden.cases import CASES
