@@ -35,7 +35,8 @@ MODELS = {"izhikevich": BIT, "relay": FLOAT, "game_of_life": BIT, "rate_encoding
           "binary threshold": FLOAT, "backprop_rate_encoding": FLOAT,
           "hebbian_rate_encoding": FLOAT, "perceptron": FLOAT, "sine generator": FLOAT,
           "poisson generator": BIT, "spnet": BIT, "oscillator": FLOAT, "som": FLOAT,
-          "nvm": FLOAT, "nvm_heaviside": FLOAT, "nvm_compare": FLOAT}
+          "nvm": FLOAT, "nvm_heaviside": FLOAT, "nvm_compare": FLOAT, "vp_max": FLOAT,
+          "sample": FLOAT}
 GLOBAL_SEED = 0x5EED5EED     # the library's default sg_set_seed value
 # Which sine the reference's sine generator evaluates: its unqualified
 # sin(float) resolves to the C library's double sin (pinned by the fixture).
@@ -445,7 +446,7 @@ class OracleNetwork:
             l.history = 1 + (max_delay // 32 if l.output_type == BIT else max_delay)
             st = {"input": np.zeros(l.registers * l.size, np.float32),   # attributes.cpp:21-26
                   "output": np.zeros(l.history * l.size, np.uint32)}
-            if l.model == "backprop_rate_encoding":   # feedforward structures only
+            if l.model in ("backprop_rate_encoding", "sample"):   # feedforward structures only
                 raise ValueError("Cluster compatibility conflict detected!")
             elif l.model == "perceptron":
                 st["expected"] = np.zeros(l.size, np.float32)
@@ -699,7 +700,7 @@ class OracleNetwork:
         # plasticity
         if learning:
             for c in self.conns:
-                if c.plastic and c.to.model in ("perceptron", "oscillator"):
+                if c.plastic and c.to.model in ("perceptron", "oscillator", "vp_max"):
                     raise ValueError(c.to.model + " learning reads source outputs that the "
                                      "reference binds only in feedforward structures")
             for l in self.layers:
@@ -757,6 +758,12 @@ class OracleNetwork:
             return
         if c.to.model.startswith("nvm"):
             self._activate_nvm(L, c, st, m, src, geo, reg)
+            return
+        if c.to.model == "vp_max":   # vp_max_attributes.cpp:72-85
+            if c.second_order:
+                raise ValueError("Unimplemented connection type!")
+            L.sg_act_vp_max(*geo, _p(src), c.frm.output_type, c.delay, c.opcode, _p(m["weights"]),
+                            _p(reg))
             return
         if c.to.model == "oscillator":
             L.sg_act_oscillator(*geo, _p(src), c.frm.output_type, c.delay, c.opcode,
@@ -821,6 +828,8 @@ class OracleNetwork:
             L.sg_som(l.size, l.history, ctypes.c_float(l.p.get_float("rbf scale", 1.0)),
                      _p(st["input"]), _p(st["output"]), ctypes.byref(w))
             l.winner = w.value
+        elif l.model == "vp_max":
+            L.sg_relay(l.size, l.history, _p(st["input"]), _p(st["output"]), 0)
         elif l.model == "binary threshold":
             L.sg_bin_thresh(l.size, l.history, _p(st["input"]), _p(st["output"]))
         elif l.model == "perceptron":

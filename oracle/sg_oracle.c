@@ -711,6 +711,20 @@ void sg_nvm_update(int heaviside, int size, int history, const float *inputs, fl
     }
 }
 
+/* vp_max activator (vp_max_attributes.cpp:46-70) */
+void sg_act_vp_max(int rows, const int *dst, const long *ptr, const int *from_idx,
+                   const int *w_idx, const uint32_t *src_words, int src_type, int delay,
+                   int opcode, const float *weights, float *inputs) {
+    for (int r = 0; r < rows; ++r) {
+        float max_val = 0.0;
+        for (long v = ptr[r]; v < ptr[r + 1]; ++v) {
+            float val = extract(src_words[from_idx[v]], delay, src_type) * weights[w_idx[v]];
+            if (val > max_val) max_val = val;
+        }
+        inputs[dst[r]] = aggregate(inputs[dst[r]], max_val, opcode);
+    }
+}
+
 void sg_rate(int size, int history, const float *inputs, float *outputs) {
     for (int nid = 0; nid < size; ++nid) {
         float input = inputs[nid];

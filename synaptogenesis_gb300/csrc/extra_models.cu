@@ -478,4 +478,78 @@ class SomModel : public Model {
 };
 SG_REGISTER_MODEL(SomModel);
 
+// ---------------------------------------------------------------------------
+// vp_max (vp_max_attributes.cpp): synaptic input is the largest weighted
+// source value (at least 0), aggregated with the opcode; the output is the
+// input.  Its updaters read source outputs bound only in feedforward
+// structures and its second-order kernels write the weight copy of the
+// connection's own matrix (which only hosts have): both refused here.
+// ---------------------------------------------------------------------------
+template <int TY, int SR>
+__global__ void __launch_bounds__(128) k_activate_vp_max(DGeom g, const uint32_t* __restrict__ src,
+                                                         int delay, int opcode,
+                                                         const float* __restrict__ w,
+                                                         float* __restrict__ inputs) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= g.n_dest) return;
+    float max_val = 0.0f;
+    for_each_source<TY>(g, d, [&](int from, int wi) {
+        const float val = extract<SR>(src[from], delay) * w[wi];
+        if (val > max_val) max_val = val;
+    });
+    const int to = dest_of<TY>(g, d);
+    inputs[to] = aggregate(inputs[to], max_val, opcode);
+}
+
+__global__ void k_identity(int size, int history, const float* __restrict__ in, float* out) {
+    const int nid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nid >= size) return;
+    shift_floats(out, size, history, nid, in[nid]);
+}
+
+class VpMaxModel : public Model {
+  public:
+    const char* name() const override { return "vp_max"; }
+    OutputType output_type() const override { return OUT_FLOAT; }
+    void build_matrix(State&, ConnState& cs) const override {
+        if (cs.conn->second_order) throw SgError(cs.conn->str() + ": Unimplemented connection type!");
+    }
+    std::string learning_error(const Connection&) const override {
+        return "vp_max learning reads source outputs that the reference binds only in "
+               "feedforward structures (set \"plastic\": false or run without learning)";
+    }
+    void activate(State& st, ConnState& cs, const StepCtx& ctx) const override {
+        const Connection& c = *cs.conn;
+        const uint32_t* src = st.dev_output(c.from, word_index(c.delay, c.from->output_type));
+        SG_DISPATCH_TYPE_SRC((int)c.type, (int)c.from->output_type,
+            (k_activate_vp_max<TY, SR><<<blocks_for(cs.geom.n_dest, 128), 128, 0, ctx.stream>>>(
+                cs.geom, src, c.delay, (int)c.opcode, cs.weights->df(), input_register(st, cs))));
+        SG_LAUNCH_CHECK();
+        ctx.count();
+    }
+    void update(State&, LayerState& ls, const StepCtx& ctx) const override {
+        const Layer& l = *ls.layer;
+        k_identity<<<blocks_for(l.size, 256), 256, 0, ctx.stream>>>(l.size, l.history(), ls.input->df(),
+                                                                    ls.output->df());
+        SG_LAUNCH_CHECK();
+        ctx.count();
+    }
+};
+SG_REGISTER_MODEL(VpMaxModel);
+
+// sample (sample_attributes.cpp): the reference's template model builds only
+// in feedforward structures (check_compatibility), so with the parallel
+// structures supported here it reports the reference's compatibility error.
+class SampleModel : public Model {
+  public:
+    const char* name() const override { return "sample"; }
+    OutputType output_type() const override { return OUT_FLOAT; }
+    void build_layer(State&, LayerState& ls) const override {
+        throw SgError("Error building attributes for " + ls.layer->str() +
+                      ":\n  Cluster compatibility conflict detected!");
+    }
+    void update(State&, LayerState&, const StepCtx&) const override {}
+};
+SG_REGISTER_MODEL(SampleModel);
+
 }  // namespace sg

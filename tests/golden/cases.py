@@ -551,13 +551,14 @@ def cases():
 
     # --- the smaller neural models -----------------------------------------
     # binary threshold, hebbian rate encoding (its rule is never applied by
-    # the reference), perceptron, sine generator.
+    # the reference), perceptron, sine generator, vp_max.
     net = {"structures": [{"name": "m", "type": "parallel", "layers": [
         _layer("src", "relay", 6, 8),
         _layer("bt", "binary threshold", 6, 8),
         _layer("hb", "hebbian_rate_encoding", 6, 8),
         _layer("pc", "perceptron", 4, 5),
         _layer("sg", "sine generator", 6, 8, frequency=37),
+        _layer("vm", "vp_max", 6, 8),
     ]}], "connections": [
         {"name": "m_bt", "from layer": "src", "to layer": "bt", "type": "one to one",
          "opcode": "add", "plastic": False},
@@ -572,6 +573,10 @@ def cases():
                            "to column start": 0, "to column end": 4}},
         {"name": "m_sg", "from layer": "src", "to layer": "sg", "type": "one to one",
          "opcode": "add", "plastic": False},
+        {"name": "m_vm", "from layer": "src", "to layer": "vm", "type": "convergent",
+         "opcode": "add", "plastic": False, "arborized config": {"field size": 3, "wrap": True}},
+        {"name": "m_vm_sub", "from layer": "bt", "to layer": "vm", "type": "one to one",
+         "opcode": "sub", "plastic": False},
     ]}
     model_conns = [c["name"] for c in net["connections"]]
 
@@ -580,8 +585,8 @@ def cases():
                 for name in model_conns}
     out.append(Case("models", net, 40, 101, inject=inj_models,
                     inputs={"src": lambda rng, t, n: rng.normal(0.0, 1.0, n)},
-                    record=[("m", l) for l in ("bt", "hb", "pc", "sg")],
-                    final=[("neuron", "m", l, "input") for l in ("bt", "hb", "pc", "sg")]
+                    record=[("m", l) for l in ("bt", "hb", "pc", "sg", "vm")],
+                    final=[("neuron", "m", l, "input") for l in ("bt", "hb", "pc", "sg", "vm")]
                     + [("matrix", "m_hb", "weights")]))
 
     # --- spnet (Izhikevich's polychronization network) ---------------------

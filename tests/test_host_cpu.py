@@ -205,16 +205,17 @@ def test_dendritic_registers_and_node_names(sg):
 
 
 def test_model_build_errors_match_the_reference(sg):
-    """backprop_rate_encoding builds only in feedforward structures; the
-    perceptron has no convolutional activator."""
+    """backprop_rate_encoding and sample build only in feedforward
+    structures; the perceptron and som have no convolutional activator."""
     from oracle.oracle import OracleNetwork
-    net = {"structures": [{"name": "s", "layers": [
-        {"name": "a", "neural model": "backprop_rate_encoding", "rows": 2, "columns": 2}]}]}
-    n = sg.Network(net)
-    n.build_state()
-    assert n.state is None and "Cluster compatibility conflict" in sg.last_error()
-    with pytest.raises(ValueError, match="Cluster compatibility"):
-        OracleNetwork(net)
+    for model in ("backprop_rate_encoding", "sample"):
+        net = {"structures": [{"name": "s", "layers": [
+            {"name": "a", "neural model": model, "rows": 2, "columns": 2}]}]}
+        n = sg.Network(net)
+        n.build_state()
+        assert n.state is None and "Cluster compatibility conflict" in sg.last_error()
+        with pytest.raises(ValueError, match="Cluster compatibility"):
+            OracleNetwork(net)
     net = {"structures": [{"name": "s", "layers": [
         {"name": "a", "neural model": "relay", "rows": 4, "columns": 4},
         {"name": "p", "neural model": "perceptron", "rows": 4, "columns": 4}]}],
