@@ -218,6 +218,7 @@ class Conn:
         self.name = p.get("name", "")
         self.frm, self.to = frm, to
         self.plastic = p.get_bool("plastic", True)            # connection_config.cpp:213
+        self.recurrent = p.get_bool("recurrent", False)
         self.delay = p.get_int("delay", 0)
         self.max_weight = p.get_float("max weight", 1.0)
         self.type = CONN_TYPES[p.get("type", "fully connected")]
@@ -409,13 +410,15 @@ class OracleNetwork:
         self.weight_callbacks = weight_callbacks or {}
         top = Props(net)
         self.layers, self.conns, self.structures = [], [], []
+        self.cluster_type = {}
         for sp in top.child_arrays.get("structures", []):
             sname = sp.get("name")
-            if sp.get("type", "parallel") != "parallel":
-                raise ValueError("oracle: only parallel structures are restated")
+            self.cluster_type[sname] = sp.get("type", "parallel")
             self.structures.append(sname)
             for lp in sp.child_arrays.get("layers", []):
-                self.layers.append(Layer(sname, lp))
+                layer = Layer(sname, lp)
+                layer.cluster_type = self.cluster_type[sname]
+                self.layers.append(layer)
         for cp in top.child_arrays.get("connections", []):
             frm = self._find(cp.get("from layer"), cp.get("from structure", None))
             to = self._find(cp.get("to layer"), cp.get("to structure", None))
@@ -427,7 +430,50 @@ class OracleNetwork:
             else:
                 conn.node.children.append(conn)
             self.conns.append(conn)
+        self.order = {st: self._order_structure(st) for st in self.structures
+                      if self.cluster_type[st] != "parallel"}
         self._build_state()
+
+    def _order_structure(self, st):
+        """SequentialCluster / FeedforwardCluster (sequential_cluster.cpp:
+        10-67, feedforward_cluster.cpp:8-36): layers placed backwards from the
+        structure's outputs, each before the layers it feeds."""
+        layers = [l for l in self.layers if l.structure == st]
+        inner = lambda c: c.frm.structure == st and c.to.structure == st
+        queue = [l for l in layers
+                 if all(not (c.to.structure == st and not c.recurrent) for c in l.outputs) or not l.outputs]
+        placed, stalled = [], 0
+        while queue:
+            cur = queue.pop(0)
+            if cur in placed:
+                stalled = 0
+                continue
+            if any(c.to is not cur and inner(c) and not c.recurrent and c.to not in placed
+                   for c in cur.outputs):
+                queue.append(cur)
+                stalled += 1
+                if stalled > len(queue):
+                    break
+                continue
+            stalled = 0
+            placed.append(cur)
+            queue.extend(c.frm for c in cur.inputs
+                         if c.frm is not cur and inner(c) and not c.recurrent and c.frm not in placed)
+        if len(placed) < len(layers):
+            raise ValueError("Sequential cluster failed to process all layers!")
+        if self.cluster_type[st] == "feedforward":
+            def acyclic(l, path):
+                if l in path:
+                    return False
+                path.append(l)
+                ok = all(acyclic(c.to, path) for c in l.outputs if c.to.structure == st)
+                path.pop()
+                return ok
+            for l in layers:
+                if all(not (c.frm.structure == st and not c.recurrent) for c in l.inputs) \
+                        and not acyclic(l, []):
+                    raise ValueError("Feedforward engine requires a structure with no cycles!")
+        return placed[::-1]
 
     def _find(self, name, structure):
         hits = [l for l in self.layers if l.name == name and (structure is None or l.structure == structure)]
@@ -446,8 +492,12 @@ class OracleNetwork:
             l.history = 1 + (max_delay // 32 if l.output_type == BIT else max_delay)
             st = {"input": np.zeros(l.registers * l.size, np.float32),   # attributes.cpp:21-26
                   "output": np.zeros(l.history * l.size, np.uint32)}
-            if l.model in ("backprop_rate_encoding", "sample"):   # feedforward structures only
-                raise ValueError("Cluster compatibility conflict detected!")
+            if l.model in ("backprop_rate_encoding", "sample") and l.cluster_type != "feedforward":
+                raise ValueError("Cluster compatibility conflict detected!")   # feedforward only
+            if l.model == "backprop_rate_encoding":
+                st["error deltas"] = np.zeros(l.size, np.float32)
+            if l.model == "sample":
+                st["neuron_var"] = np.zeros(l.size, np.float32)
             elif l.model == "perceptron":
                 st["expected"] = np.zeros(l.size, np.float32)
             elif l.model == "oscillator":   # oscillator_attributes.cpp:12-22
@@ -503,6 +553,18 @@ class OracleNetwork:
             if c.to.model in ("som", "oscillator") and (c.second_order or
                                                         (c.to.model == "som" and c.convolutional)):
                 raise ValueError("Unimplemented connection type!")
+            if c.to.model == "sample":   # sample_attributes.cpp:22-45
+                if c.second_order:
+                    raise ValueError("Unimplemented connection type!")
+                m["var1"] = np.zeros(c.num_weights, np.float32)
+                m["var2"] = np.zeros(c.num_weights, np.float32)
+                if c.p.get("second weights", "false") == "true":
+                    val = c.frm.p.get_float("value", 1.0)
+                    if val < 0:
+                        raise ValueError("Val cannot be negative!")
+                    m["var1"][:] = m["weights"] * np.float32(val)
+                if c.opcode == OPCODES["sub"]:
+                    m["var2"][:] = 1.0
             if c.to.model == "spnet":   # spnet_attributes.cpp:440-494
                 n = c.num_weights
                 m["presyn trace"] = np.zeros(n, np.float32)
@@ -677,38 +739,66 @@ class OracleNetwork:
                     reg0[:] = v
             elif not is_input:
                 reg0[:] = 0.0
-        # synaptic activation: every connection reads outputs of step t-1
-        for l in self.layers:
-            if l.registers == 1:
-                for c in l.inputs:
-                    self._activate(L, c)
-                continue
-            inp = self.neuron[l]["input"]
-            for op in self._dendrite_plan(l.root, []):
-                if op[0] == "copy":  # instruction.h:461-472
-                    host = op[1].host
-                    self.so_weights[host][:] = self.matrix[host]["weights"]
-                elif op[0] == "fold":
-                    node, ch = op[1], op[2]
-                    L.sg_calc_internal(l.size, _p(inp[ch.reg * l.size:]), _p(inp[node.reg * l.size:]),
-                                       ch.opcode, ctypes.c_float(ch.init))
+        if not self.order:
+            # synaptic activation: every connection reads outputs of step t-1
+            for l in self.layers:
+                self._activate_layer(L, l)
+            # neuron updates
+            for l in self.layers:
+                self._update(L, l)
+        else:
+            # the clusters' order (engine.cpp:226-315): parallel structures'
+            # non-input layers activate before the input is read
+            # (parallel_cluster.cpp:27-79, 105-118); then each structure in
+            # turn, a sequential one updating each layer right after its
+            # activations; then the parallel layers' updates
+            for st in self.structures:
+                if st not in self.order:
+                    for l in self.layers:
+                        if l.structure == st and l.name not in inputs:
+                            self._activate_layer(L, l)
+            for st in self.structures:
+                if st not in self.order:
+                    for l in self.layers:
+                        if l.structure == st and l.name in inputs:
+                            self._activate_layer(L, l)
                 else:
-                    self._activate(L, op[1])
-        # neuron updates
-        for l in self.layers:
-            self._update(L, l)
+                    for l in self.order[st]:
+                        self._activate_layer(L, l)
+                        self._update(L, l)
+            for st in self.structures:
+                if st not in self.order:
+                    for l in self.layers:
+                        if l.structure == st:
+                            self._update(L, l)
         # plasticity
         if learning:
             for c in self.conns:
-                if c.plastic and c.to.model in ("perceptron", "oscillator", "vp_max"):
-                    raise ValueError(c.to.model + " learning reads source outputs that the "
-                                     "reference binds only in feedforward structures")
+                bound = c.frm.structure == c.to.structure and c.to.cluster_type == "feedforward"
+                if c.plastic and c.to.model in ("perceptron", "oscillator", "vp_max", "sample"):
+                    if not bound:
+                        raise ValueError(c.to.model + " learning reads source outputs that the "
+                                         "reference binds only in feedforward structures")
+                    if c.convolutional and c.to.model != "perceptron":
+                        raise ValueError("convolutional " + c.to.model + " learning is not supported")
             for l in self.layers:
                 for c in l.inputs:
                     if c.plastic and c.to.model == "izhikevich":
                         self._learn(L, c)
                     elif c.plastic and c.to.model == "spnet":
                         self._learn_spnet(L, c)
+                    elif c.plastic and c.to.model == "perceptron":   # perceptron_attributes.cpp:51-60
+                        L.sg_upd_perceptron(c.rows, _p(c.dst), _p(c.ptr), _p(c.from_idx), _p(c.w_idx),
+                                            _p(self._src_words(c)), _p(self.neuron[c.to]["output"]),
+                                            _p(self.neuron[c.to]["expected"]), _p(self.matrix[c]["weights"]))
+                    elif c.plastic and c.to.model in ("oscillator", "vp_max"):
+                        L.sg_upd_toward_post(c.rows, _p(c.dst), _p(c.ptr), _p(c.from_idx), _p(c.w_idx),
+                                             _p(self._src_words(c)), c.frm.output_type, c.delay,
+                                             _p(self.neuron[c.to]["output"]), ctypes.c_float(1.0),
+                                             _p(self.matrix[c]["weights"]))
+                    elif c.plastic and c.to.model == "sample":
+                        # its updater is its activator (sample_attributes.cpp:229-247)
+                        self._activate(L, c)
                     elif c.plastic and c.to.model == "som":   # som_attributes.cpp:58-79
                         m = self.matrix[c]
                         L.sg_upd_som(c.rows, _p(c.dst), _p(c.ptr), _p(c.w_idx), c.to.cols, c.to.winner,
@@ -797,6 +887,23 @@ class OracleNetwork:
             w = self.so_weights[c] if c.so_host else m["weights"]
             L.sg_act_base(*geo, _p(src), c.frm.output_type, c.delay, c.opcode, _p(w), _p(reg))
 
+    def _activate_layer(self, L, l):
+        if l.registers == 1:
+            for c in l.inputs:
+                self._activate(L, c)
+            return
+        inp = self.neuron[l]["input"]
+        for op in self._dendrite_plan(l.root, []):
+            if op[0] == "copy":  # instruction.h:461-472
+                host = op[1].host
+                self.so_weights[host][:] = self.matrix[host]["weights"]
+            elif op[0] == "fold":
+                node, ch = op[1], op[2]
+                L.sg_calc_internal(l.size, _p(inp[ch.reg * l.size:]), _p(inp[node.reg * l.size:]),
+                                   ch.opcode, ctypes.c_float(ch.init))
+            else:
+                self._activate(L, op[1])
+
     def _update(self, L, l):
         st = self.neuron[l]
         if l.model == "izhikevich":
@@ -830,6 +937,8 @@ class OracleNetwork:
             l.winner = w.value
         elif l.model == "vp_max":
             L.sg_relay(l.size, l.history, _p(st["input"]), _p(st["output"]), 0)
+        elif l.model == "sample":   # sample_attributes.cpp:52-58: layer variable 0
+            L.sg_scale(l.size, l.history, ctypes.c_float(0.0), _p(st["input"]), _p(st["output"]))
         elif l.model == "binary threshold":
             L.sg_bin_thresh(l.size, l.history, _p(st["input"]), _p(st["output"]))
         elif l.model == "perceptron":

@@ -725,6 +725,44 @@ void sg_act_vp_max(int rows, const int *dst, const long *ptr, const int *from_id
     }
 }
 
+/* output = scale * input (sample_attributes.cpp:52-58) */
+void sg_scale(int size, int history, float scale, const float *inputs, float *outputs) {
+    for (int nid = 0; nid < size; ++nid)
+        shift_float(outputs, size, history, nid, scale * inputs[nid]);
+}
+
+/* perceptron updater (perceptron_attributes.cpp:51-60): source outputs read
+ * as floats */
+void sg_upd_perceptron(int rows, const int *dst, const long *ptr, const int *from_idx,
+                       const int *w_idx, const uint32_t *src_words, const float *dest_out,
+                       const float *expected, float *weights) {
+    for (int r = 0; r < rows; ++r) {
+        int to = dst[r];
+        float delta = expected[to] - dest_out[to];
+        for (long v = ptr[r]; v < ptr[r + 1]; ++v) {
+            union { uint32_t i; float f; } u;
+            u.i = src_words[from_idx[v]];
+            weights[w_idx[v]] += 0.05 * delta * u.f;
+        }
+    }
+}
+
+/* oscillator / vp_max / sample updaters (oscillator_attributes.cpp:196-206,
+ * vp_max_attributes.cpp:150-160, sample_attributes.cpp:201-212) */
+void sg_upd_toward_post(int rows, const int *dst, const long *ptr, const int *from_idx,
+                        const int *w_idx, const uint32_t *src_words, int src_type, int delay,
+                        const uint32_t *dest_words, float rate, float *weights) {
+    for (int r = 0; r < rows; ++r) {
+        int to = dst[r];
+        float to_out = extract(dest_words[to], 0, src_type);
+        for (long v = ptr[r]; v < ptr[r + 1]; ++v) {
+            float from_out = extract(src_words[from_idx[v]], delay, src_type);
+            float old = weights[w_idx[v]];
+            weights[w_idx[v]] = old + (rate * from_out * (to_out - (from_out * old)));
+        }
+    }
+}
+
 void sg_rate(int size, int history, const float *inputs, float *outputs) {
     for (int nid = 0; nid < size; ++nid) {
         float input = inputs[nid];

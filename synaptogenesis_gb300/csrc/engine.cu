@@ -119,7 +119,9 @@ Engine::Engine(Network* net, Environment* env, State* state, const Props& args)
             for (auto& lp : net_->layers)
                 for (Connection* c : lp->inputs)
                     if (c->plastic && find_model(lp->model)->learns(*c)) learned += c->num_weights;
-        overlap_ = learning_ && !profile_ && args.get_bool("overlap learning", learned >= (1LL << 20));
+        for (auto& sp : net_->structures) ordered_ = ordered_ || !sp->parallel();
+        overlap_ = learning_ && !profile_ && !ordered_ &&
+                   args.get_bool("overlap learning", learned >= (1LL << 20));
         if (overlap_) use_graphs_ = false;
         if (overlap_) {
             side_ = engine_side_stream();
@@ -155,7 +157,7 @@ Engine::Engine(Network* net, Environment* env, State* state, const Props& args)
             state_->mark_device_newer();
         }
         // No environment and every layer self-contained: whole runs per layer.
-        alone_ = modules_.empty() && !net_->layers.empty() && args.get_bool("whole runs", true);
+        alone_ = modules_.empty() && !net_->layers.empty() && !ordered_ && args.get_bool("whole runs", true);
         for (auto& lp : net_->layers)
             alone_ = alone_ && !lp->has_dendrites() &&
                      find_model(lp->model)->can_advance_alone(*state_, *state_->layer_state(lp.get()));
@@ -392,6 +394,39 @@ void Engine::enqueue_step(bool last) {
             }
         }
     };
+    if (ordered_) {
+        // Structures that are not all parallel: the reference's cluster
+        // order (engine.cpp:226-315).  Parallel structures activate their
+        // non-input layers before the input is read (parallel_cluster.cpp:
+        // 27-79, 105-118), then each structure in turn: a parallel one its
+        // input layers, a sequential / feedforward one every layer in its
+        // order with its update right after its activations (so later layers
+        // read this step's outputs); last, the parallel layers' updates.
+        auto update_layer = [&](Layer* l) {
+            const Model* m = find_model(l->model);
+            timed(std::string(m->name()) + ".update", 1, [&] {
+                m->update(*state_, *state_->layer_state(l), ctx);
+            });
+        };
+        for (auto& sp : net_->structures)
+            if (sp->parallel())
+                for (Layer* l : sp->layers)
+                    if (!(layer_io_[l->index] & 1)) activate_layer(l);
+        for (auto& sp : net_->structures) {
+            if (sp->parallel()) {
+                for (Layer* l : sp->layers)
+                    if (layer_io_[l->index] & 1) activate_layer(l);
+            } else {
+                for (Layer* l : sp->order) {
+                    activate_layer(l);
+                    update_layer(l);
+                }
+            }
+        }
+        for (auto& sp : net_->structures)
+            if (sp->parallel())
+                for (Layer* l : sp->layers) update_layer(l);
+    } else {
     std::vector<Layer*> deferred;
     for (auto& lp : net_->layers) {
         bool waits = false;
@@ -433,6 +468,7 @@ void Engine::enqueue_step(bool last) {
                 for (LayerState* ls : g.second)
                     timed(name, 1, [&] { g.first->update(*state_, *ls, ctx); });
         }
+    }
     }
     // 4. plasticity (on the side stream when overlapped, after this step's
     // updates)

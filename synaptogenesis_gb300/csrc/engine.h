@@ -127,6 +127,7 @@ class Engine {
     int graph_steps_ = 16;               // steps per captured graph (even)
     bool step_counter_ = false;          // a noise generator reads the step counter
     bool alone_ = false;                 // every layer advances whole runs on its own
+    bool ordered_ = false;               // a sequential or feedforward structure sets the step order
     long launches_ = 0, steps_ = 0;
     double wall_s_ = 0.0;
     float device_ms_ = 0.0f;

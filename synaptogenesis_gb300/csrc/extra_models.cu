@@ -20,6 +20,48 @@ static unsigned long long layer_seed(const Layer& l) {
                                 : (global_seed() ^ (0xC0FFEE1234567ULL * (unsigned long long)(l.index + 1)));
 }
 
+// The reference binds an updater's source outputs only when both layers sit
+// in one feedforward structure (synapse_data.cpp:36-51); elsewhere the
+// updaters that read them would dereference a null pointer.
+static bool sources_bound(const Connection& c) {
+    return c.from->structure == c.to->structure && c.to->structure->cluster_type == "feedforward";
+}
+
+// Update of oscillator and vp_max connections (oscillator_attributes.cpp:
+// 196-206, vp_max_attributes.cpp:150-160): w += out * (post - out * w).
+template <int TY, int SR>
+__global__ void __launch_bounds__(128) k_learn_toward_post(DGeom g, const uint32_t* __restrict__ src,
+                                                           int delay, const uint32_t* __restrict__ dest_out,
+                                                           float* w) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= g.n_dest) return;
+    const int to = dest_of<TY>(g, d);
+    const float to_out = extract<SR>(dest_out[to], 0);
+    for_each_source<TY>(g, d, [&](int from, int wi) {
+        const float from_out = extract<SR>(src[from], delay);
+        const float old = w[wi];
+        w[wi] = old + (from_out * (to_out - (from_out * old)));
+    });
+}
+
+static void launch_learn_toward_post(State& st, ConnState& cs, const StepCtx& ctx) {
+    const Connection& c = *cs.conn;
+    const uint32_t* src = st.dev_output(c.from, word_index(c.delay, c.from->output_type));
+    SG_DISPATCH_TYPE_SRC((int)c.type, (int)c.from->output_type,
+        (k_learn_toward_post<TY, SR><<<blocks_for(cs.geom.n_dest, 128), 128, 0, ctx.stream>>>(
+            cs.geom, src, c.delay, st.dev_output(c.to, 0), cs.weights->df())));
+    SG_LAUNCH_CHECK();
+    ctx.count();
+}
+
+static std::string toward_post_error(const Connection& c, const char* model) {
+    if (!sources_bound(c))
+        return std::string(model) + " learning reads source outputs that the reference binds only "
+               "in feedforward structures (set \"plastic\": false or run without learning)";
+    if (c.convolutional) return std::string("convolutional ") + model + " learning is not supported";
+    return "";
+}
+
 // ---------------------------------------------------------------------------
 // binary threshold (bin_thresh_attributes.cpp:9-17): output 1 where the input
 // is positive.
@@ -112,6 +154,19 @@ __global__ void __launch_bounds__(256) k_activate_perceptron(DGeom g, const uint
     inputs[to] = aggregate(inputs[to], sum, opcode);
 }
 
+template <int TY>
+__global__ void __launch_bounds__(128) k_learn_perceptron(DGeom g, const uint32_t* __restrict__ src,
+                                                          const float* __restrict__ dest_out,
+                                                          const float* __restrict__ expected, float* w) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= g.n_dest) return;
+    const int to = dest_of<TY>(g, d);
+    const float delta = expected[to] - dest_out[to];
+    for_each_source<TY>(g, d, [&](int from, int wi) {
+        w[wi] = (float)((double)w[wi] + 0.05 * delta * __uint_as_float(src[from]));
+    });
+}
+
 __global__ void k_perceptron(int size, int history, int per_neuron, const float* __restrict__ in,
                              float* out) {
     int nid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -130,12 +185,32 @@ class PerceptronModel : public Model {
         const Connection& c = *cs.conn;
         if (c.second_order || c.convolutional) throw SgError(c.str() + ": Unimplemented connection type!");
     }
-    // The reference's updater reads the source outputs, which it binds only
-    // within feedforward structures (synapse_data.cpp:36-51); in the parallel
-    // structures supported here its source pointer is null.
-    std::string learning_error(const Connection&) const override {
+    // The updater reads the source outputs (bound only within a feedforward
+    // structure): w += 0.05 * (expected - output) * source output
+    // (perceptron_attributes.cpp:51-60).
+    std::string learning_error(const Connection& c) const override {
+        if (sources_bound(c)) return "";
         return "perceptron learning reads source outputs that the reference binds only in "
                "feedforward structures (set \"plastic\": false or run without learning)";
+    }
+    bool learns(const Connection&) const override { return true; }
+    void learn(State& st, ConnState& cs, const StepCtx& ctx) const override {
+        const Connection& c = *cs.conn;
+        const uint32_t* src = st.dev_output(c.from, word_index(c.delay, c.from->output_type));
+        const LayerState& to = *st.layer_state(c.to);
+        const unsigned blocks = blocks_for(cs.geom.n_dest, 128);
+        const float* out = to.output->df();
+        const float* expected = to.var("expected")->df();
+        switch ((int)c.type) {
+            case 0: k_learn_perceptron<0><<<blocks, 128, 0, ctx.stream>>>(cs.geom, src, out, expected, cs.weights->df()); break;
+            case 1: k_learn_perceptron<1><<<blocks, 128, 0, ctx.stream>>>(cs.geom, src, out, expected, cs.weights->df()); break;
+            case 2: k_learn_perceptron<2><<<blocks, 128, 0, ctx.stream>>>(cs.geom, src, out, expected, cs.weights->df()); break;
+            case 3: k_learn_perceptron<3><<<blocks, 128, 0, ctx.stream>>>(cs.geom, src, out, expected, cs.weights->df()); break;
+            case 4: k_learn_perceptron<4><<<blocks, 128, 0, ctx.stream>>>(cs.geom, src, out, expected, cs.weights->df()); break;
+            case 5: k_learn_perceptron<5><<<blocks, 128, 0, ctx.stream>>>(cs.geom, src, out, expected, cs.weights->df()); break;
+        }
+        SG_LAUNCH_CHECK();
+        ctx.count();
     }
     void activate(State& st, ConnState& cs, const StepCtx& ctx) const override {
         const Connection& c = *cs.conn;
@@ -242,8 +317,9 @@ SG_REGISTER_MODEL(PoissonGeneratorModel);
 // "tonic", output max(0, tanh(state)), and a "bold" signal -- cleared every
 // step (its init key), then the absolute synaptic inputs and the leak added.
 // Its updaters read source outputs the reference binds only in feedforward
-// structures, and its second-order kernels write the weight copy of the
-// slave's own matrix (which only hosts have): both are refused here.
+// structures (learning elsewhere is refused), and its second-order kernels
+// write the weight copy of the slave's own matrix, which only hosts have
+// (refused).
 // ---------------------------------------------------------------------------
 template <int TY, int SR>
 __global__ void __launch_bounds__(128) k_activate_oscillator(DGeom g, const uint32_t* __restrict__ src,
@@ -291,9 +367,12 @@ class OscillatorModel : public Model {
     void build_matrix(State&, ConnState& cs) const override {
         if (cs.conn->second_order) throw SgError(cs.conn->str() + ": Unimplemented connection type!");
     }
-    std::string learning_error(const Connection&) const override {
-        return "oscillator learning reads source outputs that the reference binds only in "
-               "feedforward structures (set \"plastic\": false or run without learning)";
+    std::string learning_error(const Connection& c) const override {
+        return toward_post_error(c, "oscillator");
+    }
+    bool learns(const Connection&) const override { return true; }
+    void learn(State& st, ConnState& cs, const StepCtx& ctx) const override {
+        launch_learn_toward_post(st, cs, ctx);
     }
     void begin_step(State&, LayerState& ls, const StepCtx& ctx) const override {
         SG_CUDA(cudaMemsetAsync(ls.var("bold")->df(), 0, (size_t)ls.layer->size * 4, ctx.stream));
@@ -481,9 +560,7 @@ SG_REGISTER_MODEL(SomModel);
 // ---------------------------------------------------------------------------
 // vp_max (vp_max_attributes.cpp): synaptic input is the largest weighted
 // source value (at least 0), aggregated with the opcode; the output is the
-// input.  Its updaters read source outputs bound only in feedforward
-// structures and its second-order kernels write the weight copy of the
-// connection's own matrix (which only hosts have): both refused here.
+// input.  Learning and second order as for the oscillator.
 // ---------------------------------------------------------------------------
 template <int TY, int SR>
 __global__ void __launch_bounds__(128) k_activate_vp_max(DGeom g, const uint32_t* __restrict__ src,
@@ -514,9 +591,12 @@ class VpMaxModel : public Model {
     void build_matrix(State&, ConnState& cs) const override {
         if (cs.conn->second_order) throw SgError(cs.conn->str() + ": Unimplemented connection type!");
     }
-    std::string learning_error(const Connection&) const override {
-        return "vp_max learning reads source outputs that the reference binds only in "
-               "feedforward structures (set \"plastic\": false or run without learning)";
+    std::string learning_error(const Connection& c) const override {
+        return toward_post_error(c, "vp_max");
+    }
+    bool learns(const Connection&) const override { return true; }
+    void learn(State& st, ConnState& cs, const StepCtx& ctx) const override {
+        launch_learn_toward_post(st, cs, ctx);
     }
     void activate(State& st, ConnState& cs, const StepCtx& ctx) const override {
         const Connection& c = *cs.conn;
@@ -537,18 +617,59 @@ class VpMaxModel : public Model {
 };
 SG_REGISTER_MODEL(VpMaxModel);
 
-// sample (sample_attributes.cpp): the reference's template model builds only
-// in feedforward structures (check_compatibility), so with the parallel
-// structures supported here it reports the reference's compatibility error.
+// sample (sample_attributes.cpp): the reference's template model, built only
+// in feedforward structures.  Base synaptic input, output = 0 * input (its
+// layer variable stays 0), and two per-synapse variables: var1 = weight * the
+// source layer's "value" where "second weights" is set, var2 = 0 for
+// "modulate" and 1 for "sub" connections.  Its updater for a
+// non-convolutional connection is its activator (get_updaters returns
+// activate_sample_map, sample_attributes.cpp:229-247): learning activates the
+// connection once more into the input register and leaves the weights.
+__global__ void k_scale(int size, int history, float scale, const float* __restrict__ in, float* out) {
+    const int nid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nid >= size) return;
+    shift_floats(out, size, history, nid, scale * in[nid]);
+}
+
 class SampleModel : public Model {
   public:
     const char* name() const override { return "sample"; }
     OutputType output_type() const override { return OUT_FLOAT; }
-    void build_layer(State&, LayerState& ls) const override {
-        throw SgError("Error building attributes for " + ls.layer->str() +
-                      ":\n  Cluster compatibility conflict detected!");
+    void build_layer(State& st, LayerState& ls) const override {
+        if (ls.layer->structure->cluster_type != "feedforward")
+            throw SgError("Error building attributes for " + ls.layer->str() +
+                          ":\n  Cluster compatibility conflict detected!");
+        ls.vars["neuron_var"] = st.add_array("neuron_var", 'f', ls.layer->size);
     }
-    void update(State&, LayerState&, const StepCtx&) const override {}
+    void build_matrix(State& st, ConnState& cs) const override {
+        const Connection& c = *cs.conn;
+        if (c.second_order) throw SgError(c.str() + ": Unimplemented connection type!");
+        cs.params["connection variable"] = std::stof(c.parameter("connection variable", "1.0"));
+        const size_t n = c.num_weights;
+        Array* v1 = cs.vars["var1"] = st.add_array("var1", 'f', n, matrix_layout(c), c.matrix_rows, c.matrix_cols);
+        Array* v2 = cs.vars["var2"] = st.add_array("var2", 'f', n, matrix_layout(c), c.matrix_rows, c.matrix_cols);
+        if (c.parameter("second weights", "false") == "true") {
+            const float val = std::stof(c.from->parameter("value", "1.0"));
+            if (val < 0)
+                throw SgError("Error initializing weight matrix for " + c.str() + " \n  Val cannot be negative!");
+            for (size_t i = 0; i < n; ++i) v1->hf()[i] = cs.weights->hf()[i] * val;
+        }
+        if (c.opcode == OP_SUB)
+            for (size_t i = 0; i < n; ++i) v2->hf()[i] = 1.0f;
+    }
+    std::string learning_error(const Connection& c) const override { return toward_post_error(c, "sample"); }
+    bool learns(const Connection&) const override { return true; }
+    void learn(State& st, ConnState& cs, const StepCtx& ctx) const override {
+        launch_base_activator(st, cs, input_register(st, cs), ctx.stream);
+        ctx.count();
+    }
+    void update(State&, LayerState& ls, const StepCtx& ctx) const override {
+        const Layer& l = *ls.layer;
+        k_scale<<<blocks_for(l.size, 256), 256, 0, ctx.stream>>>(l.size, l.history(), 0.0f, ls.input->df(),
+                                                                 ls.output->df());
+        SG_LAUNCH_CHECK();
+        ctx.count();
+    }
 };
 SG_REGISTER_MODEL(SampleModel);
 

@@ -1,6 +1,8 @@
 #include "network.h"
 
 #include <algorithm>
+#include <deque>
+#include <functional>
 #include <map>
 
 #include "models.h"
@@ -156,8 +158,6 @@ Network::Network(const Props& config) : config_(config) {
         if (st->cluster_type != "parallel" && st->cluster_type != "sequential" &&
             st->cluster_type != "feedforward")
             throw SgError("Unrecognized ClusterType: " + st->cluster_type);
-        if (st->cluster_type != "parallel")
-            throw SgError("Structure " + st->name + ": only \"parallel\" structures are supported");
         for (Props* lp : sp->child_array("layers")) {
             auto l = std::make_unique<Layer>();
             l->config = *lp;
@@ -192,6 +192,65 @@ Network::Network(const Props& config) : config_(config) {
         structures.push_back(std::move(st));
     }
     for (Props* cp : config.child_array("connections")) add_connection(*cp);
+    for (auto& st : structures)
+        if (!st->parallel()) order_structure(*st);
+}
+
+// SequentialCluster (sequential_cluster.cpp:10-67): a breadth-first walk
+// backwards from the structure's outputs; a layer is placed once every layer
+// it feeds (within the structure, not over recurrent connections) is placed,
+// and goes in front of them.  The reference loops forever on a cycle; here
+// a pass that places nothing ends the walk with its error.  Feedforward
+// structures must also have no cycle reachable from their inputs
+// (feedforward_cluster.cpp:8-36).
+void Network::order_structure(Structure& st) {
+    auto inner = [&](const Connection* c) { return c->from->structure == &st && c->to->structure == &st; };
+    std::deque<Layer*> queue;
+    for (Layer* l : st.layers) {
+        bool output = true;
+        for (Connection* c : l->outputs)
+            if (c->to->structure == &st && !c->recurrent) output = false;
+        if (output || l->outputs.empty()) queue.push_back(l);
+    }
+    std::vector<Layer*> placed;
+    auto is_placed = [&](const Layer* l) { return std::find(placed.begin(), placed.end(), l) != placed.end(); };
+    size_t stalled = 0;
+    while (!queue.empty()) {
+        Layer* cur = queue.front();
+        queue.pop_front();
+        if (is_placed(cur)) { stalled = 0; continue; }
+        bool wait = false;
+        for (Connection* c : cur->outputs)
+            if (c->to != cur && inner(c) && !c->recurrent && !is_placed(c->to)) wait = true;
+        if (wait) {
+            queue.push_back(cur);
+            if (++stalled > queue.size()) break;       // a full pass placed nothing: a cycle
+            continue;
+        }
+        stalled = 0;
+        placed.push_back(cur);
+        for (Connection* c : cur->inputs)
+            if (c->from != cur && inner(c) && !c->recurrent && !is_placed(c->from)) queue.push_back(c->from);
+    }
+    if (placed.size() < st.layers.size()) throw SgError("Sequential cluster failed to process all layers!");
+    st.order.assign(placed.rbegin(), placed.rend());
+    if (st.cluster_type == "feedforward") {
+        std::vector<Layer*> path;
+        std::function<bool(Layer*)> acyclic = [&](Layer* l) {
+            if (std::find(path.begin(), path.end(), l) != path.end()) return false;
+            path.push_back(l);
+            for (Connection* c : l->outputs)
+                if (c->to->structure == &st && !acyclic(c->to)) return false;
+            path.pop_back();
+            return true;
+        };
+        for (Layer* l : st.layers) {
+            bool input = true;
+            for (Connection* c : l->inputs)
+                if (c->from->structure == &st && !c->recurrent) input = false;
+            if (input && !acyclic(l)) throw SgError("Feedforward engine requires a structure with no cycles!");
+        }
+    }
 }
 
 Structure* Network::structure(const std::string& name) const {
@@ -258,6 +317,7 @@ void Network::add_connection(const Props& p) {
     c->second_order_host = c->second_order && !c->node->host;
     c->second_order_slave = c->second_order && !c->second_order_host;
     c->plastic = p.get_bool("plastic", true);
+    c->recurrent = p.get_bool("recurrent", false);
     c->delay = p.get_int("delay", 0);
     c->max_weight = p.get_float("max weight", 1.0f);
     c->type = parse_conn_type(p.get("type", "fully connected"));

@@ -121,6 +121,7 @@ struct Connection {
     Layer* from = nullptr;
     Layer* to = nullptr;
     bool plastic = true;
+    bool recurrent = false;             // ignored when ordering a structure's layers
     int delay = 0;
     float max_weight = 1.0f;
     ConnType type = FULLY_CONNECTED;
@@ -155,8 +156,12 @@ struct Connection {
 
 struct Structure {
     std::string name;
-    std::string cluster_type;
+    std::string cluster_type;          // "parallel", "sequential" or "feedforward"
     std::vector<Layer*> layers;
+    // Sequential / feedforward: the layers in the order they step, each after
+    // the layers that feed it (sequential_cluster.cpp:10-67).
+    std::vector<Layer*> order;
+    bool parallel() const { return cluster_type == "parallel"; }
 };
 
 class Network {
@@ -178,6 +183,7 @@ class Network {
 
   private:
     void add_connection(const Props& p);
+    void order_structure(Structure& st);
     Props config_;
 };
 

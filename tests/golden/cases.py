@@ -712,6 +712,58 @@ def cases():
                     + [("neuron", "v", "hv", k) for k in ("state", "input")]
                     + [("neuron", "v", "cmp", "input")]
                     + [("matrix", c, "weights") for c in ("v_rec", "c_plastic")]))
+
+    # --- sequential, feedforward and parallel structures ---------------------
+    # seq: layers step in dependency order (h2 -> h1 is recurrent, so it reads
+    # last step's h2); ff: feedforward, whose updaters read the sources'
+    # outputs (perceptron, oscillator, vp_max, sample learn); par: parallel,
+    # with an input layer that activates after the sequential structure.
+    net = {"structures": [
+        {"name": "seq", "type": "sequential", "layers": [
+            _layer("out", "relay", 4, 4), _layer("h2", "relay", 4, 4),
+            _layer("in", "relay", 4, 4), _layer("h1", "relay", 4, 4, ramp=True)]},
+        {"name": "ff", "type": "feedforward", "layers": [
+            _layer("x", "relay", 4, 4), _layer("p", "perceptron", 3, 3),
+            _layer("o", "oscillator", 4, 4), _layer("v", "vp_max", 4, 4),
+            _layer("sp", "sample", 4, 4), _layer("bp", "backprop_rate_encoding", 4, 4)]},
+        {"name": "par", "type": "parallel", "layers": [
+            _layer("q", "relay", 4, 4), _layer("r", "relay", 4, 4), _layer("z", "relay", 4, 4)]},
+    ], "connections": [
+        {"name": "s_in", "from layer": "in", "to layer": "h1", "type": "one to one", "plastic": False},
+        {"name": "s_12", "from layer": "h1", "to layer": "h2", "type": "fully connected", "plastic": False},
+        {"name": "s_back", "from layer": "h2", "to layer": "h1", "type": "one to one", "plastic": False,
+         "recurrent": True, "opcode": "sub"},
+        {"name": "s_out", "from layer": "h2", "to layer": "out", "type": "one to one", "plastic": False},
+        {"name": "f_p", "from layer": "x", "to layer": "p", "type": "fully connected", "plastic": True},
+        {"name": "f_o", "from layer": "x", "to layer": "o", "type": "one to one", "plastic": True},
+        {"name": "f_v", "from layer": "x", "to layer": "v", "type": "convergent", "plastic": True,
+         "arborized config": {"field size": 3, "wrap": True}},
+        {"name": "f_sp", "from layer": "x", "to layer": "sp", "type": "one to one", "plastic": True,
+         "connection variable": 0.5, "second weights": True, "opcode": "sub"},
+        {"name": "f_bp", "from layer": "x", "to layer": "bp", "type": "fully connected", "plastic": False},
+        {"name": "p_q", "from layer": "out", "to layer": "q", "type": "one to one", "plastic": False},
+        {"name": "p_r", "from layer": "v", "to layer": "r", "type": "one to one", "plastic": False},
+        {"name": "p_z", "from layer": "h2", "to layer": "z", "type": "one to one", "plastic": False},
+    ]}
+    struct_conns = [c["name"] for c in net["connections"]]
+
+    def inj_structs(rng, sizes):
+        d = {("matrix", n, "weights"): rng.uniform(-0.5, 0.5, sizes["conn:" + n]).astype(np.float32)
+             for n in struct_conns}
+        d[("neuron", "ff", "p", "expected")] = rng.uniform(-1.0, 1.0, 9).astype(np.float32)
+        return d
+    out.append(Case("structures", net, 20, 141, inject=inj_structs,
+                    inputs={"in": lambda rng, t, n: rng.normal(0.0, 1.0, n),
+                            "x": lambda rng, t, n: rng.normal(0.0, 1.0, n),
+                            "z": lambda rng, t, n: rng.normal(0.0, 1.0, n)},
+                    record=[(st, l) for st, l in (("seq", "h1"), ("seq", "h2"), ("seq", "out"),
+                                                  ("ff", "p"), ("ff", "o"), ("ff", "v"), ("ff", "sp"),
+                                                  ("ff", "bp"), ("par", "q"), ("par", "r"), ("par", "z"))],
+                    final=[("matrix", c, "weights") for c in ("f_p", "f_o", "f_v", "f_sp")]
+                    + [("matrix", "f_sp", k) for k in ("var1", "var2")]
+                    + [("neuron", "ff", "o", k) for k in ("state", "bold")]
+                    + [("neuron", "ff", "bp", "error deltas"), ("neuron", "par", "z", "input"),
+                       ("neuron", "ff", "sp", "input")]))
     return out
 
 

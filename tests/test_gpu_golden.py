@@ -3,13 +3,15 @@ recorded results (bit-exact), and against the oracle.
 
 Bit-exact: spike rasters, output-history words, voltages, recoveries,
 conductances, traces, weights and all integer state.  Two allowances, both
-written here: outputs that go through tanhf or expf (rate encoding and its
-variants, oscillator, som, nvm; the GPU's and the host C library's may differ in
-the last bit) compare with relative tolerance 1e-5, and so do the nvm case's
-state, inputs and recurrently learned weights, which those outputs feed back
-into (the host C library's tanhf is not correctly rounded, so no GPU
-evaluation reproduces it bit for bit); and in fp32 arrays any two NaNs match (x86, Arm and the GPU
-each produce a different default NaN payload for 0/0).
+written here:
+* outputs that go through tanhf or expf (rate encoding and its variants,
+  oscillator, som, nvm) compare with relative tolerance 1e-5, and so do the
+  values those outputs feed back into: the nvm case's state, inputs and
+  recurrently learned weights, and the structures case's oscillator weights,
+  state and bold.  The host C library's tanhf is not correctly rounded, so no
+  GPU evaluation reproduces it bit for bit;
+* in fp32 arrays any two NaNs match (x86, Arm and the GPU each produce a
+  different default NaN payload for 0/0).
 """
 import pytest
 
@@ -19,7 +21,8 @@ from tests.harness import compare, float_like_keys, load_fixture, run_library, r
 pytestmark = pytest.mark.gpu
 
 RATE_KEYS = ("rec/s/one", "rec/s/div", "rec/d/rtree", "rec/p/sdiv", "rec/m/hb", "rec/o/osc",
-             "rec/o/som", "rec/v/", "neuron/v/", "matrix/v_rec")
+             "rec/o/som", "rec/v/", "neuron/v/", "matrix/v_rec", "rec/ff/o", "rec/ff/bp",
+             "matrix/f_o", "neuron/ff/o/")
 RATE_TOL = 1e-5
 
 

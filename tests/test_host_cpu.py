@@ -43,7 +43,7 @@ def test_library_exports_every_header_function(sg):
 
 @pytest.mark.parametrize("name", ["iz_opcodes", "iz_plastic", "base_all_types", "iz_c0_8",
                                   "gol_two_word_history", "dendrites", "second_order", "sparse",
-                                  "models", "spnet", "oscillator_som", "nvm"])
+                                  "models", "spnet", "oscillator_som", "nvm", "structures"])
 def test_initial_state_matches_oracle(sg, name):
     from oracle.oracle import OracleNetwork
     from tests.golden.cases import CASES
@@ -230,6 +230,41 @@ def test_model_build_errors_match_the_reference(sg):
     assert n.state is None and "Unimplemented connection type" in sg.last_error()
     with pytest.raises(ValueError, match="Unimplemented connection type"):
         OracleNetwork(net)
+
+
+def _struct_net(kind, conns):
+    return {"structures": [{"name": "s", "type": kind, "layers": [
+        {"name": n, "neural model": "relay", "rows": 2, "columns": 2} for n in ("x", "a", "b")]}],
+        "connections": [{"from layer": f, "to layer": t, "type": "one to one", "plastic": False,
+                         "recurrent": r} for f, t, r in conns]}
+
+
+@pytest.mark.parametrize("kind,conns,message", [
+    ("sequential", [("x", "a", False), ("a", "b", False), ("b", "a", False)],
+     "Sequential cluster failed to process all layers"),
+    ("feedforward", [("x", "a", False), ("a", "b", False), ("b", "a", True)],
+     "Feedforward engine requires a structure with no cycles"),
+])
+def test_structure_order_errors_match_the_reference(sg, kind, conns, message):
+    """A sequential structure whose layers feed each other in a cycle (the
+    reference loops forever there; here the walk stops with its error), and
+    a feedforward structure with a cycle through a recurrent connection."""
+    from oracle.oracle import OracleNetwork
+    net = _struct_net(kind, conns)
+    n = sg.Network(net)
+    assert n.obj is None and message in sg.last_error(), sg.last_error()
+    with pytest.raises(ValueError, match=message):
+        OracleNetwork(net)
+
+
+def test_sequential_order_follows_the_reference(sg):
+    """Layers listed out of order step after the layers that feed them; a
+    recurrent connection does not constrain the order."""
+    from oracle.oracle import OracleNetwork
+    net = _struct_net("sequential", [("b", "a", False), ("a", "x", False), ("x", "b", True)])
+    o = OracleNetwork(net)
+    assert [l.name for l in o.order["s"]] == ["b", "a", "x"]
+    assert sg.Network(net).obj is not None
 
 
 def test_izhikevich_gap_must_be_self_connection(sg):
