@@ -6,7 +6,8 @@ the full 10,000-timestep run of that grid.  Metric: synapse updates per second
 (a synapse update is one (destination, weight) visit in one timestep: 9 per
 cell, as the reference computes the zero centre weight too).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload gol|iz_plastic]
+  python bench.py [--gpus N] [--steps K] [--warmup W]
+                  [--workload gol|iz_plastic|batched|rate_adjoint|spnet_sparse]
   python bench.py --impl reference ...   # the reference's own CPU path
 
 Timing: each step is bracketed by CUDA events recorded on the stream the
@@ -151,6 +152,70 @@ def iz_plastic_workload(side=256):
     }
 
 
+def spnet_sparse_workload(side=256):
+    """spnet (Izhikevich's polychronization model) with sparse connections: a
+    256x256 excitatory layer with recurrent STDP over a 15x15 field, a 128x128
+    inhibitory layer, half of every field's weights zero and compacted away,
+    distance delays within the excitatory layer (1 step between the layers),
+    a 5 Hz Poisson drive."""
+    import numpy as np
+    n = side * side
+
+    def layer(name, rows, params, drive=False):
+        d = {"name": name, "neural model": "spnet", "rows": rows, "columns": rows, "params": params}
+        if drive:
+            d["init config"] = {"type": "poisson", "rate": 5, "value": 20, "seed": 31}
+        return d
+
+    def weights(mx, seed):
+        return {"type": "random", "min weight": 0.01, "max weight": mx, "fraction": 0.5, "seed": seed}
+    net = {"structures": [{"name": "s", "type": "parallel", "layers": [
+        layer("exc", side, "regular", drive=True), layer("inh", side // 2, "fast")]}],
+        "connections": [
+            {"name": "ee", "from layer": "exc", "to layer": "exc", "type": "convergent", "sparse": True,
+             "opcode": "add", "plastic": True, "max weight": 10.0,
+             "arborized config": {"field size": 15, "wrap": True}, "weight config": weights(6.0, 41)},
+            {"name": "ei", "from layer": "exc", "to layer": "inh", "type": "convergent", "sparse": True,
+             "opcode": "add", "plastic": False, "myelinated": True, "delay": 1,
+             "arborized config": {"field size": 9, "stride": 2, "wrap": True},
+             "weight config": weights(8.0, 42)},
+            {"name": "ie", "from layer": "inh", "to layer": "exc", "type": "divergent", "sparse": True,
+             "opcode": "sub", "plastic": False, "myelinated": True, "delay": 1,
+             "arborized config": {"field size": 9, "stride": 2, "wrap": True},
+             "weight config": weights(4.0, 43)}]}
+    wl = {}
+
+    def inject(net_obj):
+        # synapses kept by the compaction: the nonzero compacted weights
+        counts = {c: int(np.count_nonzero(net_obj.get_weight_matrix(c, "weights").to_np_array()))
+                  for c in ("ee", "ei", "ie")}
+        wl["synapses"] = counts
+        wl["units_per_timestep"] = sum(counts.values()) + counts["ee"]   # activations + STDP
+        wl["bytes_per_launch"] = 28 * counts["ee"]
+
+    def result(net_obj):
+        return net_obj.get_neuron_data("s", "exc", "output").to_np_array()
+
+    wl.update({
+        "name": "spnet_sparse",
+        "desc": "spnet 256x256 excitatory (recurrent STDP, convergent 15x15 wrap) + 128x128 "
+                "inhibitory (convergent / divergent 9x9 stride 2), sparse connections with half "
+                "of each field zero, distance delays (1 step between layers), 5 Hz Poisson drive",
+        "net": net, "inject": inject, "result": result,
+        "timesteps": 1000,
+        "units_per_timestep": None,                     # set from the compacted state
+        "unit": "synapse-updates/s",
+        "dtype": "f32",
+        "kernel": "spnet.learn.sparse",
+        "bytes_per_launch": None,                       # w, presyn trace, dw r+w, source index
+        "bytes_per_timestep": None,
+        "state_bytes": None,
+        "cpu_seconds": 8.0,
+        "learning": True,
+    })
+    return wl
+
+
 def batched_workload():
     """Batched instances: 256 independent instances of the plain Izhikevich
     configuration, sides uniform in 16..128 (seed 3), advanced together."""
@@ -201,7 +266,7 @@ def rate_inputs(batch=64, seed=4):
 
 
 WORKLOADS = {"gol": gol_workload, "iz_plastic": iz_plastic_workload, "batched": batched_workload,
-             "rate_adjoint": rate_workload}
+             "rate_adjoint": rate_workload, "spnet_sparse": spnet_sparse_workload}
 
 # Sides of the instances timed one at a time (plain GPU path / reference CPU
 # path); the per-timestep time is fitted as alpha + beta * (recurrent synapses)
@@ -866,6 +931,7 @@ def main():
     r = run_gb300(args, rank, world, local)
     if rank != 0:
         return
+    wl = r["wl"]                 # as built: workloads may size themselves from their state
     peak, peak_kind = measured_peak()
     achieved = None
     if r["mean_us"]:

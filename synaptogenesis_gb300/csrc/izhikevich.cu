@@ -9,6 +9,7 @@
 #include <random>
 
 #include "cuda_check.h"
+#include "exact_convert.cuh"
 #include "history.cuh"
 #include "iz_cols_tma.cuh"
 #include "iz_neuron.cuh"
@@ -979,6 +980,53 @@ __global__ void __launch_bounds__(128) k_spnet_learn(DGeom g, const uint32_t* __
     });
 }
 
+// Sparse connections: one thread per compacted synapse (blockIdx.y is the
+// synapse's rank within its destination, x the destination), since each
+// synapse's update is independent.  The products with 0.9 / 0.95 go through
+// the integer helpers; the double sums stay double.  Bit-identical to
+// k_spnet_learn.
+template <int SR, bool SUB>
+__global__ void __launch_bounds__(256) k_spnet_learn_sparse(DGeom g, const uint32_t* __restrict__ dest_out,
+                                                            const float* __restrict__ post,
+                                                            const int* __restrict__ to_tss,
+                                                            const int* __restrict__ from_tss, float lr,
+                                                            float max_weight, float* __restrict__ w,
+                                                            float* __restrict__ presyn,
+                                                            float* __restrict__ dws, IzLut lut) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;
+    if (d >= g.to_size || i >= g.nz[d]) return;
+    const int wi = i * g.to_size + d;
+    float weight = w[wi];
+    if (!(weight >= 0.0001f)) return;
+    const int stss = from_tss[g.sfrom[wi]];
+    const bool src_spike = stss == 0;
+    const float dest_spike = extract<SR>(dest_out[d], 0);    // the source's extractor
+    float src_trace, dest_trace;
+    if (!SUB) {
+        const float p = presyn[wi];
+        src_trace = presyn[wi] = src_spike ? (float)(p + 0.1) : mul_fd_rn(p, 0.95);
+        dest_trace = post[d];
+    } else {
+        const int dtss = to_tss[d];
+        src_trace = (dest_spike > 0.0f && stss > 0 && stss < 32) ? lut.src[stss] : 0.0f;
+        dest_trace = (src_spike && dtss > 0 && dtss < 32) ? lut.dst[dtss] : 0.0f;
+    }
+    const float f1 = dest_spike * src_trace;
+    const float f2 = (src_spike ? 1.0f : 0.0f) * dest_trace;
+    const float dw0 = dws[wi];
+    // 0.9 dw + f1 - f2 in double: with f1, f2 zero and dw nonzero it is the
+    // rounded product alone
+    const float dw = (f1 == 0.0f && f2 == 0.0f && dw0 != 0.0f)
+                         ? mul_fd_rn(dw0, 0.9)
+                         : d2f_rn(__dadd_rn(__dadd_rn(mul_df_rn(dw0, 0.9), f2d_exact(f1)), -f2d_exact(f2)));
+    dws[wi] = dw;
+    const float weight_delta = d2f_rn(__dadd_rn(f2d_exact(dw), 0.01));
+    weight += lr * weight_delta;
+    const float capped = (max_weight < weight) ? max_weight : weight;
+    w[wi] = (0.0001f > capped) ? 0.0001f : capped;
+}
+
 class SpnetModel : public Model {
   public:
     const char* name() const override { return "spnet"; }
@@ -1058,6 +1106,25 @@ class SpnetModel : public Model {
             for (int i = 1; i < 32; ++i) { t.src[i] = istdp_src(i); t.dst[i] = istdp_dst(i); }
             return t;
         }();
+        if (c.type == SPARSE) {
+            const dim3 grid(blocks_for(c.to->size, 256), std::max(1, cs.geom.kmax));
+#define SG_SPNET_SPARSE(SRV, SUBV)                                                              \
+    k_spnet_learn_sparse<SRV, SUBV><<<grid, 256, 0, ctx.stream>>>(                              \
+        cs.geom, st.dev_output(c.to, 0), to.var("post trace")->df(),                           \
+        to.var("time since spike")->di(), cs.var("time since spike")->di(),                    \
+        cs.params.at("learning rate"), c.max_weight, cs.weights->df(),                         \
+        cs.var("presyn trace")->df(), cs.var("weight derivative")->df(), lut)
+            const bool sub = c.opcode == OP_SUB;
+            switch ((int)c.from->output_type) {
+                case 0: if (sub) SG_SPNET_SPARSE(0, true); else SG_SPNET_SPARSE(0, false); break;
+                case 1: if (sub) SG_SPNET_SPARSE(1, true); else SG_SPNET_SPARSE(1, false); break;
+                default: if (sub) SG_SPNET_SPARSE(2, true); else SG_SPNET_SPARSE(2, false); break;
+            }
+#undef SG_SPNET_SPARSE
+            SG_LAUNCH_CHECK();
+            ctx.count();
+            return;
+        }
         const unsigned blocks = blocks_for(cs.geom.n_dest, 128);
 #define SG_SPNET_LEARN(SUBV)                                                                    \
     SG_DISPATCH_TYPE_SRC((int)c.type, (int)c.from->output_type,                                \

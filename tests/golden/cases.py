@@ -607,22 +607,32 @@ def cases():
          "arborized config": {"field size": 3, "stride": 2, "wrap": True}},
         {"name": "n_ie", "from layer": "inh", "to layer": "exc", "type": "fully connected",
          "opcode": "sub", "plastic": True, "max weight": 5.0},
+        {"name": "n_sp", "from layer": "exc", "to layer": "exc", "type": "convergent",
+         "opcode": "add", "plastic": True, "max weight": 8.0, "sparse": True,
+         "arborized config": {"field size": 3, "wrap": True}},
+        {"name": "n_isp", "from layer": "inh", "to layer": "exc", "type": "fully connected",
+         "opcode": "sub", "plastic": True, "max weight": 4.0, "sparse": True},
     ]}
 
     def inj_spnet(rng, sizes):
-        return {
+        d = {
             ("matrix", "n_drive", "weights"): np.full(sizes["conn:n_drive"], 20.0, np.float32),
             ("matrix", "n_rec", "weights"): rng.uniform(0.0, 6.0, sizes["conn:n_rec"]).astype(np.float32),
             ("matrix", "n_ei", "weights"): rng.uniform(0.0, 20.0, sizes["conn:n_ei"]).astype(np.float32),
             ("matrix", "n_ie", "weights"): rng.uniform(0.0, 4.0, sizes["conn:n_ie"]).astype(np.float32),
         }
+        for name, hi in (("n_sp", 6.0), ("n_isp", 3.0)):   # sparse: half the weights zero
+            w = rng.uniform(0.0, hi, sizes["dense:" + name]).astype(np.float32)
+            w[rng.random(w.size) < 0.5] = 0.0
+            d[("matrix", name, "init weights")] = w
+        return d
     out.append(Case("spnet", net, 200, 111, inject=inj_spnet,
                     inputs={"in": lambda rng, t, n: (rng.random(n) < 0.25) * 1.0},
                     record=[("n", "exc"), ("n", "inh")],
                     final=[("neuron", "n", "exc", k) for k in
                            ("voltage", "recovery", "post trace", "time since spike", "input")]
                     + [("neuron", "n", "inh", k) for k in ("voltage", "recovery")]
-                    + [("matrix", c, k) for c in ("n_rec", "n_ie")
+                    + [("matrix", c, k) for c in ("n_rec", "n_ie", "n_sp", "n_isp")
                        for k in ("weights", "presyn trace", "weight derivative", "time since spike")]))
 
     # --- oscillator and self-organising map --------------------------------
