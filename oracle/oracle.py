@@ -779,8 +779,9 @@ class OracleNetwork:
                     if not bound:
                         raise ValueError(c.to.model + " learning reads source outputs that the "
                                          "reference binds only in feedforward structures")
-                    if c.convolutional and c.to.model != "perceptron":
-                        raise ValueError("convolutional " + c.to.model + " learning is not supported")
+                    if c.convolutional and c.to.model != "perceptron" and c.type != 3:
+                        raise ValueError("divergent convolutional " + c.to.model +
+                                         " learning is not supported")
             for l in self.layers:
                 for c in l.inputs:
                     if c.plastic and c.to.model == "izhikevich":
@@ -791,6 +792,13 @@ class OracleNetwork:
                         L.sg_upd_perceptron(c.rows, _p(c.dst), _p(c.ptr), _p(c.from_idx), _p(c.w_idx),
                                             _p(self._src_words(c)), _p(self.neuron[c.to]["output"]),
                                             _p(self.neuron[c.to]["expected"]), _p(self.matrix[c]["weights"]))
+                    elif c.plastic and c.convolutional and c.to.model in ("oscillator", "vp_max",
+                                                                          "sample"):
+                        rate = c.p.get_float("connection variable", 1.0) if c.to.model == "sample" else 1.0
+                        L.sg_upd_toward_post_conv(ctypes.byref(c.c), _p(self._src_words(c)),
+                                                  c.frm.output_type, c.delay,
+                                                  _p(self.neuron[c.to]["output"]), ctypes.c_float(rate),
+                                                  _p(self.matrix[c]["weights"]))
                     elif c.plastic and c.to.model in ("oscillator", "vp_max"):
                         L.sg_upd_toward_post(c.rows, _p(c.dst), _p(c.ptr), _p(c.from_idx), _p(c.w_idx),
                                              _p(self._src_words(c)), c.frm.output_type, c.delay,

@@ -763,6 +763,34 @@ void sg_upd_toward_post(int rows, const int *dst, const long *ptr, const int *fr
     }
 }
 
+/* Convergent convolutional learning per kernel weight
+ * (CALC_CONVERGENT_CONVOLUTIONAL_BY_WEIGHT, synapse_kernel.h:610-679) */
+void sg_upd_toward_post_conv(const sg_conn *c, const uint32_t *src_words, int src_type,
+                             int delay, const uint32_t *dest_words, float rate,
+                             float *weights) {
+    for (int kr = 0; kr < c->row_field; ++kr)
+        for (int kc = 0; kc < c->col_field; ++kc) {
+            int k = kr * c->col_field + kc;
+            float old = weights[k];
+            float delta = 0.0;
+            for (int tr = 0; tr < c->to_rows; ++tr)
+                for (int tc = 0; tc < c->to_cols; ++tc) {
+                    int fr = tr * c->row_stride + (c->row_spacing * c->row_offset) + kr * c->row_spacing;
+                    int fc = tc * c->col_stride + (c->col_spacing * c->col_offset) + kc * c->col_spacing;
+                    if (c->wrap) {
+                        fr = wrap_index(fr, c->from_rows);
+                        fc = wrap_index(fc, c->from_cols);
+                    } else if (fr < 0 || fr >= c->from_rows || fc < 0 || fc >= c->from_cols) {
+                        continue;
+                    }
+                    float from_out = extract(src_words[fr * c->from_cols + fc], delay, src_type);
+                    float to_out = extract(dest_words[tr * c->to_cols + tc], 0, src_type);
+                    delta += from_out * (to_out - (from_out * old));
+                }
+            weights[k] = old + (rate * delta / c->num_weights);
+        }
+}
+
 void sg_rate(int size, int history, const float *inputs, float *outputs) {
     for (int nid = 0; nid < size; ++nid) {
         float input = inputs[nid];

@@ -54,11 +54,57 @@ static void launch_learn_toward_post(State& st, ConnState& cs, const StepCtx& ct
     ctx.count();
 }
 
+// Convergent convolutional connections learn per kernel weight
+// (CALC_CONVERGENT_CONVOLUTIONAL_BY_WEIGHT, synapse_kernel.h:610-679): the
+// kernel weight's terms out * (post - out * w) summed over the destinations
+// in row-major order (sources outside a non-wrapping layer skipped), then
+// w += rate * sum / kernel size.  One thread per kernel weight.
+template <int SR>
+__global__ void k_learn_toward_post_conv(DGeom g, const uint32_t* __restrict__ src, int delay,
+                                         const uint32_t* __restrict__ dest_out, float rate, int n_weights,
+                                         float* w) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= g.rf * g.cf) return;
+    const int kr = k / g.cf, kc = k % g.cf;
+    const float old = w[k];
+    float delta = 0.0f;
+    for (int tr = 0; tr < g.to_rows; ++tr)
+        for (int tc = 0; tc < g.to_cols; ++tc) {
+            int fr = tr * g.rs + g.rsp * g.ro + kr * g.rsp;
+            int fc = tc * g.cs + g.csp * g.co + kc * g.csp;
+            if (g.wrap) {
+                fr = wrap_idx(fr, g.from_rows);
+                fc = wrap_idx(fc, g.from_cols);
+            } else if (fr < 0 || fr >= g.from_rows || fc < 0 || fc >= g.from_cols) {
+                continue;
+            }
+            const float from_out = extract<SR>(src[fr * g.from_cols + fc], delay);
+            const float to_out = extract<SR>(dest_out[tr * g.to_cols + tc], 0);
+            delta += from_out * (to_out - (from_out * old));
+        }
+    w[k] = old + (rate * delta / n_weights);
+}
+
+static void launch_learn_toward_post_conv(State& st, ConnState& cs, const StepCtx& ctx, float rate) {
+    const Connection& c = *cs.conn;
+    const uint32_t* src = st.dev_output(c.from, word_index(c.delay, c.from->output_type));
+    const uint32_t* dst = st.dev_output(c.to, 0);
+    const int k = c.arbor.kernel(), nw = (int)c.num_weights;
+    switch ((int)c.from->output_type) {
+        case 0: k_learn_toward_post_conv<0><<<blocks_for(k, 64), 64, 0, ctx.stream>>>(cs.geom, src, c.delay, dst, rate, nw, cs.weights->df()); break;
+        case 1: k_learn_toward_post_conv<1><<<blocks_for(k, 64), 64, 0, ctx.stream>>>(cs.geom, src, c.delay, dst, rate, nw, cs.weights->df()); break;
+        default: k_learn_toward_post_conv<2><<<blocks_for(k, 64), 64, 0, ctx.stream>>>(cs.geom, src, c.delay, dst, rate, nw, cs.weights->df()); break;
+    }
+    SG_LAUNCH_CHECK();
+    ctx.count();
+}
+
 static std::string toward_post_error(const Connection& c, const char* model) {
     if (!sources_bound(c))
         return std::string(model) + " learning reads source outputs that the reference binds only "
                "in feedforward structures (set \"plastic\": false or run without learning)";
-    if (c.convolutional) return std::string("convolutional ") + model + " learning is not supported";
+    if (c.convolutional && c.type != CONVERGENT)
+        return std::string("divergent convolutional ") + model + " learning is not supported";
     return "";
 }
 
@@ -372,7 +418,8 @@ class OscillatorModel : public Model {
     }
     bool learns(const Connection&) const override { return true; }
     void learn(State& st, ConnState& cs, const StepCtx& ctx) const override {
-        launch_learn_toward_post(st, cs, ctx);
+        if (cs.conn->convolutional) launch_learn_toward_post_conv(st, cs, ctx, 1.0f);
+        else launch_learn_toward_post(st, cs, ctx);
     }
     void begin_step(State&, LayerState& ls, const StepCtx& ctx) const override {
         SG_CUDA(cudaMemsetAsync(ls.var("bold")->df(), 0, (size_t)ls.layer->size * 4, ctx.stream));
@@ -596,7 +643,8 @@ class VpMaxModel : public Model {
     }
     bool learns(const Connection&) const override { return true; }
     void learn(State& st, ConnState& cs, const StepCtx& ctx) const override {
-        launch_learn_toward_post(st, cs, ctx);
+        if (cs.conn->convolutional) launch_learn_toward_post_conv(st, cs, ctx, 1.0f);
+        else launch_learn_toward_post(st, cs, ctx);
     }
     void activate(State& st, ConnState& cs, const StepCtx& ctx) const override {
         const Connection& c = *cs.conn;
@@ -624,7 +672,9 @@ SG_REGISTER_MODEL(VpMaxModel);
 // "modulate" and 1 for "sub" connections.  Its updater for a
 // non-convolutional connection is its activator (get_updaters returns
 // activate_sample_map, sample_attributes.cpp:229-247): learning activates the
-// connection once more into the input register and leaves the weights.
+// connection once more into the input register and leaves the weights.  A
+// convergent convolutional one learns per kernel weight at the rate of the
+// connection's "connection variable".
 __global__ void k_scale(int size, int history, float scale, const float* __restrict__ in, float* out) {
     const int nid = blockIdx.x * blockDim.x + threadIdx.x;
     if (nid >= size) return;
@@ -660,6 +710,10 @@ class SampleModel : public Model {
     std::string learning_error(const Connection& c) const override { return toward_post_error(c, "sample"); }
     bool learns(const Connection&) const override { return true; }
     void learn(State& st, ConnState& cs, const StepCtx& ctx) const override {
+        if (cs.conn->convolutional) {       // update_sample_convergent_convolutional
+            launch_learn_toward_post_conv(st, cs, ctx, cs.params.at("connection variable"));
+            return;
+        }
         launch_base_activator(st, cs, input_register(st, cs), ctx.stream);
         ctx.count();
     }

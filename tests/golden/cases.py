@@ -751,6 +751,11 @@ def cases():
         {"name": "f_sp", "from layer": "x", "to layer": "sp", "type": "one to one", "plastic": True,
          "connection variable": 0.5, "second weights": True, "opcode": "sub"},
         {"name": "f_bp", "from layer": "x", "to layer": "bp", "type": "fully connected", "plastic": False},
+        {"name": "f_vc", "from layer": "x", "to layer": "v", "type": "convergent", "plastic": True,
+         "convolutional": True, "arborized config": {"field size": 3, "wrap": True}},
+        {"name": "f_spc", "from layer": "x", "to layer": "sp", "type": "convergent", "plastic": True,
+         "convolutional": True, "connection variable": 2.0,
+         "arborized config": {"field size": 3, "wrap": False}},
         {"name": "p_q", "from layer": "out", "to layer": "q", "type": "one to one", "plastic": False},
         {"name": "p_r", "from layer": "v", "to layer": "r", "type": "one to one", "plastic": False},
         {"name": "p_z", "from layer": "h2", "to layer": "z", "type": "one to one", "plastic": False},
@@ -769,7 +774,7 @@ def cases():
                     record=[(st, l) for st, l in (("seq", "h1"), ("seq", "h2"), ("seq", "out"),
                                                   ("ff", "p"), ("ff", "o"), ("ff", "v"), ("ff", "sp"),
                                                   ("ff", "bp"), ("par", "q"), ("par", "r"), ("par", "z"))],
-                    final=[("matrix", c, "weights") for c in ("f_p", "f_o", "f_v", "f_sp")]
+                    final=[("matrix", c, "weights") for c in ("f_p", "f_o", "f_v", "f_sp", "f_vc", "f_spc")]
                     + [("matrix", "f_sp", k) for k in ("var1", "var2")]
                     + [("neuron", "ff", "o", k) for k in ("state", "bold")]
                     + [("neuron", "ff", "bp", "error deltas"), ("neuron", "par", "z", "input"),
