@@ -779,9 +779,7 @@ class OracleNetwork:
                     if not bound:
                         raise ValueError(c.to.model + " learning reads source outputs that the "
                                          "reference binds only in feedforward structures")
-                    if c.convolutional and c.to.model != "perceptron" and c.type != 3:
-                        raise ValueError("divergent convolutional " + c.to.model +
-                                         " learning is not supported")
+
             for l in self.layers:
                 for c in l.inputs:
                     if c.plastic and c.to.model == "izhikevich":

@@ -763,8 +763,8 @@ void sg_upd_toward_post(int rows, const int *dst, const long *ptr, const int *fr
     }
 }
 
-/* Convergent convolutional learning per kernel weight
- * (CALC_CONVERGENT_CONVOLUTIONAL_BY_WEIGHT, synapse_kernel.h:610-679) */
+/* Convolutional learning per kernel weight
+ * (CALC_{CONVERGENT,DIVERGENT}_CONVOLUTIONAL_BY_WEIGHT, synapse_kernel.h:610-796) */
 void sg_upd_toward_post_conv(const sg_conn *c, const uint32_t *src_words, int src_type,
                              int delay, const uint32_t *dest_words, float rate,
                              float *weights) {
@@ -775,8 +775,16 @@ void sg_upd_toward_post_conv(const sg_conn *c, const uint32_t *src_words, int sr
             float delta = 0.0;
             for (int tr = 0; tr < c->to_rows; ++tr)
                 for (int tc = 0; tc < c->to_cols; ++tc) {
-                    int fr = tr * c->row_stride + (c->row_spacing * c->row_offset) + kr * c->row_spacing;
-                    int fc = tc * c->col_stride + (c->col_spacing * c->col_offset) + kc * c->col_spacing;
+                    int fr, fc;
+                    if (c->type == DIVERGENT) {   /* synapse_kernel.h:710-746 */
+                        fr = (tr + c->row_spacing * (-c->row_offset - c->row_field + c->row_stride))
+                                 / c->row_stride + kr * c->row_spacing;
+                        fc = (tc + c->col_spacing * (-c->col_offset - c->col_field + c->col_stride))
+                                 / c->col_stride + kc * c->col_spacing;
+                    } else {
+                        fr = tr * c->row_stride + (c->row_spacing * c->row_offset) + kr * c->row_spacing;
+                        fc = tc * c->col_stride + (c->col_spacing * c->col_offset) + kc * c->col_spacing;
+                    }
                     if (c->wrap) {
                         fr = wrap_index(fr, c->from_rows);
                         fc = wrap_index(fc, c->from_cols);

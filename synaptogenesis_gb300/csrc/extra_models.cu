@@ -54,12 +54,14 @@ static void launch_learn_toward_post(State& st, ConnState& cs, const StepCtx& ct
     ctx.count();
 }
 
-// Convergent convolutional connections learn per kernel weight
-// (CALC_CONVERGENT_CONVOLUTIONAL_BY_WEIGHT, synapse_kernel.h:610-679): the
-// kernel weight's terms out * (post - out * w) summed over the destinations
-// in row-major order (sources outside a non-wrapping layer skipped), then
-// w += rate * sum / kernel size.  One thread per kernel weight.
-template <int SR>
+// Convolutional connections learn per kernel weight
+// (CALC_{CONVERGENT,DIVERGENT}_CONVOLUTIONAL_BY_WEIGHT, synapse_kernel.h:
+// 610-796): the kernel weight's terms out * (post - out * w) summed over the
+// destinations in row-major order (sources outside a non-wrapping layer
+// skipped), then w += rate * sum / kernel size.  One thread per kernel
+// weight.  A divergent destination's window starts at (t + spacing * (-offset
+// - field + stride)) / stride, truncating.
+template <int SR, bool DIV>
 __global__ void k_learn_toward_post_conv(DGeom g, const uint32_t* __restrict__ src, int delay,
                                          const uint32_t* __restrict__ dest_out, float rate, int n_weights,
                                          float* w) {
@@ -70,8 +72,10 @@ __global__ void k_learn_toward_post_conv(DGeom g, const uint32_t* __restrict__ s
     float delta = 0.0f;
     for (int tr = 0; tr < g.to_rows; ++tr)
         for (int tc = 0; tc < g.to_cols; ++tc) {
-            int fr = tr * g.rs + g.rsp * g.ro + kr * g.rsp;
-            int fc = tc * g.cs + g.csp * g.co + kc * g.csp;
+            int fr = DIV ? (tr + g.rsp * (-g.ro - g.rf + g.rs)) / g.rs + kr * g.rsp
+                         : tr * g.rs + g.rsp * g.ro + kr * g.rsp;
+            int fc = DIV ? (tc + g.csp * (-g.co - g.cf + g.cs)) / g.cs + kc * g.csp
+                         : tc * g.cs + g.csp * g.co + kc * g.csp;
             if (g.wrap) {
                 fr = wrap_idx(fr, g.from_rows);
                 fc = wrap_idx(fc, g.from_cols);
@@ -90,10 +94,15 @@ static void launch_learn_toward_post_conv(State& st, ConnState& cs, const StepCt
     const uint32_t* src = st.dev_output(c.from, word_index(c.delay, c.from->output_type));
     const uint32_t* dst = st.dev_output(c.to, 0);
     const int k = c.arbor.kernel(), nw = (int)c.num_weights;
-    switch ((int)c.from->output_type) {
-        case 0: k_learn_toward_post_conv<0><<<blocks_for(k, 64), 64, 0, ctx.stream>>>(cs.geom, src, c.delay, dst, rate, nw, cs.weights->df()); break;
-        case 1: k_learn_toward_post_conv<1><<<blocks_for(k, 64), 64, 0, ctx.stream>>>(cs.geom, src, c.delay, dst, rate, nw, cs.weights->df()); break;
-        default: k_learn_toward_post_conv<2><<<blocks_for(k, 64), 64, 0, ctx.stream>>>(cs.geom, src, c.delay, dst, rate, nw, cs.weights->df()); break;
+    const unsigned b = blocks_for(k, 64);
+    const int sel = (int)c.from->output_type * 2 + (c.type == DIVERGENT ? 1 : 0);
+    switch (sel) {
+        case 0: k_learn_toward_post_conv<0, false><<<b, 64, 0, ctx.stream>>>(cs.geom, src, c.delay, dst, rate, nw, cs.weights->df()); break;
+        case 1: k_learn_toward_post_conv<0, true><<<b, 64, 0, ctx.stream>>>(cs.geom, src, c.delay, dst, rate, nw, cs.weights->df()); break;
+        case 2: k_learn_toward_post_conv<1, false><<<b, 64, 0, ctx.stream>>>(cs.geom, src, c.delay, dst, rate, nw, cs.weights->df()); break;
+        case 3: k_learn_toward_post_conv<1, true><<<b, 64, 0, ctx.stream>>>(cs.geom, src, c.delay, dst, rate, nw, cs.weights->df()); break;
+        case 4: k_learn_toward_post_conv<2, false><<<b, 64, 0, ctx.stream>>>(cs.geom, src, c.delay, dst, rate, nw, cs.weights->df()); break;
+        default: k_learn_toward_post_conv<2, true><<<b, 64, 0, ctx.stream>>>(cs.geom, src, c.delay, dst, rate, nw, cs.weights->df()); break;
     }
     SG_LAUNCH_CHECK();
     ctx.count();
@@ -103,8 +112,6 @@ static std::string toward_post_error(const Connection& c, const char* model) {
     if (!sources_bound(c))
         return std::string(model) + " learning reads source outputs that the reference binds only "
                "in feedforward structures (set \"plastic\": false or run without learning)";
-    if (c.convolutional && c.type != CONVERGENT)
-        return std::string("divergent convolutional ") + model + " learning is not supported";
     return "";
 }
 
@@ -673,8 +680,8 @@ SG_REGISTER_MODEL(VpMaxModel);
 // non-convolutional connection is its activator (get_updaters returns
 // activate_sample_map, sample_attributes.cpp:229-247): learning activates the
 // connection once more into the input register and leaves the weights.  A
-// convergent convolutional one learns per kernel weight at the rate of the
-// connection's "connection variable".
+// convolutional one learns per kernel weight at the rate of the connection's
+// "connection variable".
 __global__ void k_scale(int size, int history, float scale, const float* __restrict__ in, float* out) {
     const int nid = blockIdx.x * blockDim.x + threadIdx.x;
     if (nid >= size) return;
@@ -710,7 +717,7 @@ class SampleModel : public Model {
     std::string learning_error(const Connection& c) const override { return toward_post_error(c, "sample"); }
     bool learns(const Connection&) const override { return true; }
     void learn(State& st, ConnState& cs, const StepCtx& ctx) const override {
-        if (cs.conn->convolutional) {       // update_sample_convergent_convolutional
+        if (cs.conn->convolutional) {       // update_sample_{convergent,divergent}_convolutional
             launch_learn_toward_post_conv(st, cs, ctx, cs.params.at("connection variable"));
             return;
         }

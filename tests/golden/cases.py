@@ -756,6 +756,8 @@ def cases():
         {"name": "f_spc", "from layer": "x", "to layer": "sp", "type": "convergent", "plastic": True,
          "convolutional": True, "connection variable": 2.0,
          "arborized config": {"field size": 3, "wrap": False}},
+        {"name": "f_od", "from layer": "x", "to layer": "o", "type": "divergent", "plastic": True,
+         "convolutional": True, "arborized config": {"field size": 2, "stride": 1, "wrap": False}},
         {"name": "p_q", "from layer": "out", "to layer": "q", "type": "one to one", "plastic": False},
         {"name": "p_r", "from layer": "v", "to layer": "r", "type": "one to one", "plastic": False},
         {"name": "p_z", "from layer": "h2", "to layer": "z", "type": "one to one", "plastic": False},
@@ -774,7 +776,8 @@ def cases():
                     record=[(st, l) for st, l in (("seq", "h1"), ("seq", "h2"), ("seq", "out"),
                                                   ("ff", "p"), ("ff", "o"), ("ff", "v"), ("ff", "sp"),
                                                   ("ff", "bp"), ("par", "q"), ("par", "r"), ("par", "z"))],
-                    final=[("matrix", c, "weights") for c in ("f_p", "f_o", "f_v", "f_sp", "f_vc", "f_spc")]
+                    final=[("matrix", c, "weights") for c in ("f_p", "f_o", "f_v", "f_sp", "f_vc", "f_spc",
+                                                              "f_od")]
                     + [("matrix", "f_sp", k) for k in ("var1", "var2")]
                     + [("neuron", "ff", "o", k) for k in ("state", "bold")]
                     + [("neuron", "ff", "bp", "error deltas"), ("neuron", "par", "z", "input"),

@@ -22,7 +22,7 @@ pytestmark = pytest.mark.gpu
 
 RATE_KEYS = ("rec/s/one", "rec/s/div", "rec/d/rtree", "rec/p/sdiv", "rec/m/hb", "rec/o/osc",
              "rec/o/som", "rec/v/", "neuron/v/", "matrix/v_rec", "rec/ff/o", "rec/ff/bp",
-             "matrix/f_o", "neuron/ff/o/")
+             "matrix/f_o", "neuron/ff/o/", "matrix/f_od")
 RATE_TOL = 1e-5
 
 
