@@ -43,6 +43,20 @@ GLOBAL_SEED = 0x5EED5EED     # the library's default sg_set_seed value
 SINE_USES_SINF = False
 
 
+def rng_bits(seed, stream, index):
+    """SplitMix64 finaliser of seed * A + stream * B + index (the library's
+    counter-based generator, counter_rng.h)."""
+    m = (1 << 64) - 1
+    z = (seed * 0x9E3779B97F4A7C15 + stream * 0xD1B54A32D192ED03 + index) & m
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & m
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & m
+    return z ^ (z >> 31)
+
+
+def rng_below(seed, stream, index, n):
+    return (rng_bits(seed, stream, index) >> 32) % n
+
+
 def rng_uniform(seed, stream, index):
     """Counter-based uniform draw in [0, 1) (SplitMix64 finaliser of a
     linear mix of seed, stream and index), as the library's generators use."""
@@ -232,10 +246,11 @@ class Conn:
         self.so_host = self.second_order and self.node.host is None
         self.so_slave = self.second_order and not self.so_host
         self.sparse = p.get_bool("sparse", False) or p.get_bool("randomized projection", False)
+        self.randomized = p.get_bool("randomized projection", False)
         if self.sparse and self.second_order:
             raise ValueError("Sparse second order connections are not supported!")
-        if p.get_bool("randomized projection", False):
-            raise ValueError("oracle: randomized projections are not restated")
+        if self.randomized and (self.convolutional or self.type in (0, 1, 4)):
+            raise ValueError("Cannot randomize projection on this weight matrix!")
         c = _Conn()
         c.type, c.opcode, c.convolutional = self.type, self.opcode, int(self.convolutional)
         c.from_rows, c.from_cols, c.to_rows, c.to_cols = frm.rows, frm.cols, to.rows, to.cols
@@ -335,6 +350,22 @@ class Conn:
         fr[wi], fc[wi] = self.pre_row[:nv], self.pre_col[:nv]
         tr[wi], tc[wi] = dst_of_visit // self.to.cols, dst_of_visit % self.to.cols
         used[wi] = True
+        fi = np.where(used, fr * self.frm.cols + fc, -1)
+        if self.randomized:   # weight_matrix.cpp:377-437, seeded draws
+            wc = self.p.child("weight config")
+            seed = int(wc.get("seed")) if (wc is not None and wc.has("seed")) else \
+                GLOBAL_SEED ^ ((0xA11CE5 * (self.index + 1)) & ((1 << 64) - 1))
+            for d in range(self.to.size):
+                nr = rng_below(seed, 2 * d, 0, self.frm.rows)
+                nc = rng_below(seed, 2 * d + 1, 0, self.frm.cols)
+                if self.type == 2:
+                    fr[d], fc[d], fi[d] = nr, nc, nr * self.frm.cols + nc
+                else:
+                    corner = d * cols
+                    dr, dc = nr - fr[corner], nc - fc[corner]
+                    fr[corner:corner + cols] += dr
+                    fc[corner:corner + cols] += dc
+                    fi[corner:corner + cols] = fr[corner:corner + cols] * self.frm.rows + fc[corner:corner + cols]
         visited = used.copy()
         used &= (w != 0.0)
         counts = used.reshape(rows, cols).sum(1)
@@ -351,18 +382,36 @@ class Conn:
         self.sp_to_row = np.full(n, -1, np.int64)
         self.sp_to_col = np.full(n, -1, np.int64)
         nonzero = np.zeros(to_size, np.int64)
+        sp_fi = np.full(n, -1, np.int64)
         for r in range(rows):
             keep = np.nonzero(used[r * cols:(r + 1) * cols])[0] + r * cols
             j = r * kmax + np.arange(keep.size)
             nw[j] = w[keep]
             self.sp_from_row[j], self.sp_from_col[j] = fr[keep], fc[keep]
             self.sp_to_row[j], self.sp_to_col[j] = tr[keep], tc[keep]
+            sp_fi[j] = fi[keep]
             nonzero[r] = keep.size
+        # adjust_sparse_indices (weight_matrix.cpp:253-338): wrap and recompute,
+        # or drop sources outside the layer and move the row's later sources
+        # up (only the sources: weights and delays stay in place)
         wrap = self.type in (3, 4) and bool(self.c.wrap)
         frm_rows, frm_cols = self.frm.rows, self.frm.cols
-        a, b = self.sp_from_row.copy(), self.sp_from_col.copy()
-        if wrap:
-            a, b = a % frm_rows, b % frm_cols   # Python's % is already non-negative
+        src = np.full(n, -1, np.int64)
+        for r in range(to_size):
+            kept = 0
+            for k in range(nonzero[r]):
+                j = r * kmax + k
+                a, b, idx = self.sp_from_row[j], self.sp_from_col[j], sp_fi[j]
+                if wrap:
+                    a, b = a % frm_rows, b % frm_cols
+                    idx = a * frm_cols + b
+                elif a < 0 or a >= frm_rows or b < 0 or b >= frm_cols:
+                    continue
+                if idx < 0 or idx >= self.frm.size:
+                    raise ValueError("randomized projection indexes outside the source layer")
+                src[r * kmax + kept] = idx
+                kept += 1
+            nonzero[r] = kept
         # the kernel's view (synapse_kernel.h:303-366): row to of the compacted
         # matrix serves destination to (a subset's window rows land on the
         # layer's first destinations, as in the reference)
@@ -376,7 +425,7 @@ class Conn:
         idx = np.concatenate([t * kmax + np.arange(nonzero[t]) for t in range(to_size)] or [np.zeros(0, int)])
         self.nvisits = idx.size
         self.w_idx = np.ascontiguousarray(np.append(idx, 0).astype(np.int32))
-        self.from_idx = np.ascontiguousarray(np.append(a[idx] * frm_cols + b[idx], 0).astype(np.int32))
+        self.from_idx = np.ascontiguousarray(np.append(src[idx], 0).astype(np.int32))
         self.pre_row = np.ascontiguousarray(np.append(self.sp_from_row[idx], 0).astype(np.int32))
         self.pre_col = np.ascontiguousarray(np.append(self.sp_from_col[idx], 0).astype(np.int32))
         return nw
@@ -423,6 +472,7 @@ class OracleNetwork:
             frm = self._find(cp.get("from layer"), cp.get("from structure", None))
             to = self._find(cp.get("to layer"), cp.get("to structure", None))
             conn = Conn(cp, frm, to)
+            conn.index = len(self.conns)
             frm.outputs.append(conn)
             to.inputs.append(conn)
             if conn.so_host:  # dendritic_node.cpp:106-140

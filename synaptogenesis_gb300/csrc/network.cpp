@@ -327,8 +327,7 @@ void Network::add_connection(const Props& p) {
     c->sparse = p.get_bool("sparse", false) || p.get_bool("randomized projection", false);
     if (c->sparse && c->second_order)
         throw SgError("Error in " + c->str() + ":\n  Sparse second order connections are not supported!");
-    if (p.get_bool("randomized projection", false))
-        throw SgError(c->str() + ": randomized projections are not supported");
+    c->randomized = p.get_bool("randomized projection", false);
     if (c->convolutional && c->type != CONVERGENT && c->type != DIVERGENT)
         throw SgError("Only convergent/divergent connections can be convolutional!");
     Layer *from = c->from, *to = c->to;
@@ -371,6 +370,20 @@ void Network::add_connection(const Props& p) {
         }
     }
     if (c->num_weights >= (1L << 31)) throw SgError(c->str() + ": more than 2^31 weights");
+    // WeightMatrix::randomize_projection (weight_matrix.cpp:355-507)
+    if (c->randomized) {
+        if (c->convolutional)
+            throw SgError("Error intializing weight matrix for " + c->str() +
+                          "\n   Cannot randomize projection on convolutional weight matrix!");
+        if (c->type == FULLY_CONNECTED)
+            throw SgError("Error intializing weight matrix for " + c->str() +
+                          "\n   Cannot randomize projection on fully connectedweight matrix!");
+        if (c->type == SUBSET)
+            throw SgError("Error intializing weight matrix for " + c->str() +
+                          "\n   Cannot randomize projection on subset weight matrix!");
+        if (c->type == DIVERGENT)
+            throw SgError(c->str() + ": randomized divergent projections are not supported");
+    }
     c->dense_type = c->type;
     c->dense_num_weights = c->num_weights;
     c->dense_rows = c->matrix_rows;

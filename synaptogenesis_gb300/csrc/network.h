@@ -130,6 +130,7 @@ struct Connection {
     Arbor arbor;
     SubsetCfg subset;
     bool sparse = false;                // "sparse": compacted at state build
+    bool randomized = false;            // "randomized projection" (also sparse)
     // Set while a state is built from this network, like the reference's
     // Connection::sparsify (connection.cpp:219-222): type SPARSE, num_weights
     // and matrix_cols of the compacted matrix, and its table.  The dense

@@ -6,6 +6,7 @@
 #include <sstream>
 
 #include "callbacks.h"
+#include "counter_rng.h"
 
 namespace sg {
 
@@ -255,6 +256,35 @@ void sparsify(State& st, ConnState& cs) {
     const int rows = c.matrix_rows, cols = c.matrix_cols, to_size = c.to->size;
     const float* w = cs.weights->hf();
     Indices ix = compute_indices(c);
+    const int frows = c.from->rows, fcols = c.from->cols;
+    if (c.randomized) {
+        // randomize_projection (weight_matrix.cpp:377-437), with seeded draws
+        // (the reference's generator is unseeded): one to one takes a random
+        // source per destination; convergent shifts each destination's field
+        // so that its first position lands on a random source, and -- as the
+        // reference -- indexes the shifted sources with the source layer's
+        // row count as the row pitch.
+        const Props* wc = c.config.child("weight config");
+        const uint64_t seed = (wc && wc->has("seed")) ? std::stoull(wc->get("seed"))
+                                                      : (g_seed ^ (0xA11CE5ULL * (uint64_t)(c.index + 1)));
+        for (int d = 0; d < to_size; ++d) {
+            const int nr = (int)rng_below(seed, 2 * (uint64_t)d, 0, (uint32_t)frows);
+            const int nc = (int)rng_below(seed, 2 * (uint64_t)d + 1, 0, (uint32_t)fcols);
+            if (c.type == ONE_TO_ONE) {
+                ix.from_row[d] = nr;
+                ix.from_col[d] = nc;
+                ix.from_index[d] = nr * fcols + nc;
+            } else {
+                const size_t corner = (size_t)d * cols;
+                const int dr = nr - ix.from_row[corner], dc = nc - ix.from_col[corner];
+                for (int k = 0; k < cols; ++k) {
+                    const int r = ix.from_row[corner + k] += dr;
+                    const int q = ix.from_col[corner + k] += dc;
+                    ix.from_index[corner + k] = r * frows + q;
+                }
+            }
+        }
+    }
     std::vector<int> used(ix.used);
     int kmax = 0;
     for (int r = 0; r < rows; ++r) {
@@ -295,17 +325,37 @@ void sparsify(State& st, ConnState& cs) {
         }
         t->nonzero[r] = k;
     }
-    // wrapped source indices for the kernels (adjust_sparse_indices); a
-    // non-wrapping arbor never keeps a synapse outside the source layer
+    // Source indices for the kernels (adjust_sparse_indices,
+    // weight_matrix.cpp:253-338): a wrapping arbor wraps its coordinates and
+    // recomputes the index; otherwise a synapse outside the source layer
+    // (only a randomized projection has them) is dropped and the row's later
+    // sources move up -- the sources only: the weights and delays stay where
+    // they are, as in the reference.
     const bool wrap = (c.dense_type == CONVERGENT || c.dense_type == DIVERGENT) && c.arbor.wrap;
-    const int fr = c.from->rows, fc = c.from->cols;
-    for (size_t j = 0; j < n; ++j) {
-        if (t->to_row[j] < 0) continue;                 // padding
-        int a = t->from_row[j], b = t->from_col[j];
-        if (wrap) { a = (a % fr + fr) % fr; b = (b % fc + fc) % fc; }
-        else if (a < 0 || a >= fr || b < 0 || b >= fc)
-            throw SgError(c.str() + ": sparse synapse outside the source layer");
-        t->from[j] = a * fc + b;
+    const int fr = frows, fc = fcols;
+    for (int r = 0; r < to_size; ++r) {
+        int kept = 0;
+        for (int k = 0; k < t->nonzero[r]; ++k) {
+            const size_t j = (size_t)r * kmax + k;
+            int a = t->from_row[j], b = t->from_col[j];
+            int idx = (int)ix.from_index[old_of[j]];
+            if (wrap) {
+                a = (a % fr + fr) % fr;
+                b = (b % fc + fc) % fc;
+                idx = a * fc + b;
+            } else if (a < 0 || a >= fr || b < 0 || b >= fc) {
+                continue;
+            }
+            // the row-pitch quirk of randomized convergent projections can
+            // index past a non-square source layer; the reference then reads
+            // outside its output array
+            if (idx < 0 || idx >= c.from->size)
+                throw SgError(c.str() + ": randomized projection indexes outside the source layer "
+                              "(the row pitch is its row count; use a square source layer)");
+            t->from[(size_t)r * kmax + kept++] = idx;
+        }
+        for (int k = kept; k < t->nonzero[r]; ++k) t->from[(size_t)r * kmax + k] = -1;
+        t->nonzero[r] = kept;
     }
     // compact the callback-set per-synapse arrays the same way
     auto compact = [&](const uint32_t* src, uint32_t fill) {

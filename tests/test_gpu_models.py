@@ -58,3 +58,17 @@ def test_perceptron_learning_is_refused(syngen):
     assert "perceptron learning" in syngen.last_error()
     report = n.run(syngen.Environment({"modules": []}), {"iterations": 2, "learning flag": False})
     assert report is not None and report.obj is not None, syngen.last_error()
+
+
+def test_randomized_projection_matches_oracle(syngen):
+    """Randomized one-to-one and convergent projections (seeded draws,
+    clipped and wrapping fields, relay and Izhikevich targets): bit-exact
+    against the oracle's restatement of the same draws and compaction."""
+    from tests.test_host_cpu import _randomized_net
+    case = Case("randomized", _randomized_net(), 40, 9,
+                inputs={"a": lambda rng, t, n: rng.normal(0.0, 5.0, n)},
+                record=[("s", "b"), ("s", "iz")],
+                final=[("neuron", "s", "b", "input"), ("neuron", "s", "iz", "voltage")])
+    got = run_library(case, syngen)
+    want = run_oracle(case)
+    assert not compare(got, want, nan_keys={"rec/s/b", "neuron/s/b/input", "neuron/s/iz/voltage"})

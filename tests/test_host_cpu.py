@@ -95,6 +95,74 @@ def test_sparse_compaction_matches_oracle(sg):
     assert onet.connection("i_rec").kmax < 25
 
 
+def _randomized_net():
+    """A one-to-one and two convergent randomized projections (relay and
+    Izhikevich targets, clipped and wrapping fields), seeded."""
+    return {"structures": [{"name": "s", "layers": [
+        {"name": "a", "neural model": "relay", "rows": 6, "columns": 6},
+        {"name": "b", "neural model": "relay", "rows": 6, "columns": 6},
+        {"name": "iz", "neural model": "izhikevich", "rows": 6, "columns": 6}]}],
+        "connections": [
+            {"name": "r1", "from layer": "a", "to layer": "b", "type": "one to one",
+             "randomized projection": True, "plastic": False,
+             "weight config": {"type": "flat", "weight": 0.5, "seed": 5}},
+            {"name": "r2", "from layer": "a", "to layer": "b", "type": "convergent",
+             "randomized projection": True, "plastic": False,
+             "arborized config": {"field size": 3, "wrap": False},
+             "weight config": {"type": "flat", "weight": 0.25, "seed": 6}},
+            {"name": "r3", "from layer": "a", "to layer": "iz", "type": "convergent",
+             "randomized projection": True, "plastic": False,
+             "arborized config": {"field size": 3, "wrap": True},
+             "weight config": {"type": "flat", "weight": 0.5, "seed": 7}}]}
+
+
+def test_randomized_projection_state_matches_oracle(sg):
+    """Randomized projections (seeded draws; the reference's are unseeded):
+    the compacted weights and the distance delays of the randomized sources
+    equal the oracle's, and the sources really moved."""
+    from oracle.oracle import OracleNetwork
+    net = _randomized_net()
+    n = sg.Network(net)
+    n.build_state()
+    assert n.state, sg.last_error()
+    o = OracleNetwork(net)
+    for c in o.conns:
+        for k, v in o.matrix[c].items():
+            got = n.get_weight_matrix(c.name, k).to_np_array()
+            m = min(got.size, v.size)
+            assert np.array_equal(got.view(np.uint32)[:m], v.view(np.uint32)[:m]), (c.name, k)
+    r1 = o.connection("r1")
+    assert not np.array_equal(r1.from_idx[:r1.nvisits], np.arange(36))
+
+
+def test_randomized_projection_outside_a_non_square_layer_is_refused(sg):
+    """The convergent form's row pitch (the source's row count) indexes past
+    a 6x5 source layer: refused at build instead of reading outside it."""
+    from oracle.oracle import OracleNetwork
+    net = _randomized_net()
+    for l in net["structures"][0]["layers"]:
+        l["columns"] = 5
+    net["connections"] = [net["connections"][1]]
+    n = sg.Network(net)
+    n.build_state()
+    assert n.state is None and "outside the source layer" in sg.last_error()
+    with pytest.raises(ValueError, match="outside the source layer"):
+        OracleNetwork(net)
+
+
+@pytest.mark.parametrize("conn", [
+    {"type": "fully connected"}, {"type": "subset"},
+    {"type": "convergent", "convolutional": True, "arborized config": {"field size": 3}}])
+def test_randomized_projection_errors(sg, conn):
+    net = _randomized_net()
+    bad = dict(net["connections"][0], **conn)
+    if conn["type"] == "subset":
+        bad["subset config"] = {"from row end": 2, "from column end": 2, "to row end": 2, "to column end": 2}
+    net["connections"] = [bad]
+    n = sg.Network(net)
+    assert n.obj is None and "randomize projection" in sg.last_error()
+
+
 def test_column_offset_quirk_and_weight_counts(sg):
     from oracle.oracle import OracleNetwork
     net = {"structures": [{"name": "s", "layers": [
