@@ -17,6 +17,14 @@
 namespace sg {
 
 #ifdef __CUDACC__
+// The rare operands' hardware paths, kept out of line so that the compiler
+// branches around them instead of predicating their FP64 instructions into
+// every lane.
+static __device__ __noinline__ double f2d_hw(float f) { return (double)f; }
+static __device__ __noinline__ float d2f_hw(double d) { return __double2float_rn(d); }
+static __device__ __noinline__ double mul_df_hw(float f, double c) { return __dmul_rn((double)f, c); }
+static __device__ __noinline__ float mul_fd_hw(float f, double c) { return __double2float_rn(__dmul_rn((double)f, c)); }
+
 // (double)f, exact.
 __device__ __forceinline__ double f2d_exact(float f) {
     const uint32_t u = __float_as_uint(f);
@@ -26,7 +34,7 @@ __device__ __forceinline__ double f2d_exact(float f) {
         return __hiloint2double((int)hi, (int)(u << 29));
     }
     if ((u << 1) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);   // +-0
-    return (double)f;                           // subnormal, infinite, NaN
+    return f2d_hw(f);                           // subnormal, infinite, NaN
 }
 
 // (float)d, round to nearest even.
@@ -42,7 +50,7 @@ __device__ __forceinline__ float d2f_rn(double d) {
         return __uint_as_float(r);
     }
     if (((hi << 1) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);    // +-0
-    return __double2float_rn(d);                // float subnormal, overflow, inf, NaN
+    return d2f_hw(d);                           // float subnormal, overflow, inf, NaN
 }
 
 // (double)f * c for a positive normal double c (a constant at the call
@@ -70,7 +78,7 @@ __device__ __forceinline__ double mul_df_rn(float f, double c) {
     } else if ((u << 1) == 0u) {
         return __hiloint2double((int)(u & 0x80000000u), 0);      // +-0 * c = +-0
     }
-    return __dmul_rn((double)f, c);
+    return mul_df_hw(f, c);
 }
 
 // (float)(f * c) for a positive normal double c (a constant at the call
@@ -104,7 +112,7 @@ __device__ __forceinline__ float mul_fd_rn(float f, double c) {
     } else if ((u << 1) == 0u) {
         return f;                                                 // +-0 * c = +-0
     }
-    return __double2float_rn(__dmul_rn((double)f, c));
+    return mul_fd_hw(f, c);
 }
 
 #endif

@@ -980,6 +980,12 @@ __global__ void __launch_bounds__(128) k_spnet_learn(DGeom g, const uint32_t* __
     });
 }
 
+// The STDP kernel's rare double expressions, out of line (see f2d_hw).
+static __device__ __noinline__ float spnet_trace_step(float p) { return (float)(p + 0.1); }
+static __device__ __noinline__ float spnet_dw_full(float dw0, float f1, float f2) {
+    return d2f_rn(__dadd_rn(__dadd_rn(mul_df_rn(dw0, 0.9), f2d_exact(f1)), -f2d_exact(f2)));
+}
+
 // Sparse connections: one thread per compacted synapse (blockIdx.y is the
 // synapse's rank within its destination, x the destination), since each
 // synapse's update is independent.  The products with 0.9 / 0.95 go through
@@ -1005,7 +1011,10 @@ __global__ void __launch_bounds__(256) k_spnet_learn_sparse(DGeom g, const uint3
     float src_trace, dest_trace;
     if (!SUB) {
         const float p = presyn[wi];
-        src_trace = presyn[wi] = src_spike ? (float)(p + 0.1) : mul_fd_rn(p, 0.95);
+        float np;
+        if (src_spike) np = spnet_trace_step(p);
+        else np = mul_fd_rn(p, 0.95);
+        src_trace = presyn[wi] = np;
         dest_trace = post[d];
     } else {
         const int dtss = to_tss[d];
@@ -1017,9 +1026,9 @@ __global__ void __launch_bounds__(256) k_spnet_learn_sparse(DGeom g, const uint3
     const float dw0 = dws[wi];
     // 0.9 dw + f1 - f2 in double: with f1, f2 zero and dw nonzero it is the
     // rounded product alone
-    const float dw = (f1 == 0.0f && f2 == 0.0f && dw0 != 0.0f)
-                         ? mul_fd_rn(dw0, 0.9)
-                         : d2f_rn(__dadd_rn(__dadd_rn(mul_df_rn(dw0, 0.9), f2d_exact(f1)), -f2d_exact(f2)));
+    float dw;
+    if (f1 == 0.0f && f2 == 0.0f && dw0 != 0.0f) dw = mul_fd_rn(dw0, 0.9);
+    else dw = spnet_dw_full(dw0, f1, f2);
     dws[wi] = dw;
     const float weight_delta = d2f_rn(__dadd_rn(f2d_exact(dw), 0.01));
     weight += lr * weight_delta;
