@@ -10,9 +10,14 @@ It restates, in Python plus the C file ``sg_oracle.c``:
   * the state each neural model allocates (state/attributes.cpp:16-37,
     state/impl/izhikevich_attributes.cpp:587-757), in the reference's host
     layout, under the reference's variable names,
-  * the engine's synchronous step order for "parallel" structures
-    (engine/engine.cpp:226-315, engine/cluster/parallel_cluster.cpp:27-131,
-    engine/cluster/cluster_node.cpp:7-212, engine/instruction.cpp:3-30).
+  * the engine's step order for parallel, sequential and feedforward
+    structures (engine/engine.cpp:226-315, engine/cluster/parallel_cluster.cpp:
+    27-131, engine/cluster/sequential_cluster.cpp:10-116,
+    engine/cluster/cluster_node.cpp:7-212, engine/instruction.cpp:3-30),
+    dendritic trees and second-order nodes (network/dendritic_node.cpp),
+  * sparse compaction and randomized projections
+    (state/weight_matrix.cpp:253-651),
+  * every neural model but debug (state/impl/*_attributes.cpp).
 Random initialisers of the reference are unseedable (util/tools.h:8); the
 oracle draws them from a seeded numpy generator instead, and parity runs
 inject every random quantity explicitly.
