@@ -10,6 +10,8 @@
 
 #include "cuda_check.h"
 #include "exact_convert.cuh"
+#include "exact_div.cuh"
+#include "ff_exact.cuh"
 #include "history.cuh"
 #include "iz_cols_tma.cuh"
 #include "iz_neuron.cuh"
@@ -50,12 +52,15 @@ struct IzLut { float src[33]; float dst[33]; };
 // One synapse of the STDP + STP updaters (izhikevich_attributes.cpp:404-520).
 // The reference's expressions are evaluated in its types (double literals
 // make the weight-derivative and short-term-w updates double), with rewrites
-// that leave every stored value bit-identical and save FP64 instructions:
+// that leave every stored value bit-identical:
+//  * the weight derivative and short-term w are float results of double
+//    expressions, evaluated in float-float arithmetic with a rounding test
+//    (ff_exact.cuh); the rare operands the test rejects take the double
+//    evaluation (wd_double, sw_double), kept out of line;
 //  * a spike product that is zero (no destination / source spike) adds or
 //    subtracts +0.0 to a partial sum that is never zero, so it is skipped;
-//  * (U - sw) / F divides by the integer constant F in integer arithmetic
-//    (div_const_rn, exact), and the float <-> double conversions and the
-//    trace decay product run in integer arithmetic (exact_convert.cuh).
+//  * the presynaptic trace decay product runs in integer arithmetic
+//    (exact_convert.cuh).
 // iz_learn_load reads a synapse's variables and iz_learn_apply updates them,
 // so that a thread can have several synapses' loads in flight at once.
 struct LearnVals {
@@ -75,6 +80,26 @@ __device__ __forceinline__ LearnVals iz_learn_load(size_t wi, int stp_flag, cons
     return v;
 }
 
+// wd - ((wd - 1e-6) * 1e-4 [+ p] [- q]) in double, rounded to float.
+static __device__ __noinline__ float wd_double(float x, float p, bool has_p, float q, bool has_q) {
+    const double xd = f2d_exact(x);
+    double change = __dmul_rn(__dsub_rn(xd, 0.000001), 0.0001);
+    if (has_p) change = __dadd_rn(change, f2d_exact(p));
+    if (has_q) change = __dsub_rn(change, f2d_exact(q));
+    return d2f_rn(__dsub_rn(xd, change));
+}
+
+// sw + ((U - sw) / F + U * (1 - sw) * spike) in double, rounded to float.
+template <bool SUB>
+static __device__ __noinline__ float sw_double(float sw, bool spike) {
+    constexpr double U = SUB ? 0.2 : 0.5;
+    constexpr int F = SUB ? 20 : 1000;
+    const double swd = f2d_exact(sw);
+    double inc = div_const_rn<F>(__dsub_rn(U, swd));
+    if (spike) inc = inc + (U * (1 - sw) * spike);
+    return d2f_rn(__dadd_rn(swd, inc));
+}
+
 template <bool SUB>
 __device__ __forceinline__ void iz_learn_apply(size_t wi, const LearnVals& v, int src_tss,
                                                float dest_spike, float dest_exc_trace,
@@ -83,7 +108,6 @@ __device__ __forceinline__ void iz_learn_apply(size_t wi, const LearnVals& v, in
                                                float* wd, float* stp_r, float* stp_w,
                                                const IzLut& lut) {
     constexpr double U = SUB ? 0.2 : 0.5;
-    constexpr int F = SUB ? 20 : 1000;
     constexpr int D = SUB ? 700 : 800;
     float weight = v.w;
     if (!(weight >= 0.0001f)) return;
@@ -99,12 +123,12 @@ __device__ __forceinline__ void iz_learn_apply(size_t wi, const LearnVals& v, in
         dest_trace = (src_spike && dest_tss > 0 && dest_tss < 32) ? lut.dst[dest_tss] : 0.0f;
     }
     // wd -= (wd - 1e-6) * 1e-4 + dest_spike * src_trace - src_spike * dest_trace
-    float weight_delta = v.wd;
-    const double wdd = f2d_exact(weight_delta);
-    double change = __dmul_rn(__dsub_rn(wdd, 0.000001), 0.0001);
-    if (dest_spike != 0.0f) change = __dadd_rn(change, f2d_exact(dest_spike * src_trace));
-    if (src_spike) change = __dsub_rn(change, f2d_exact(src_spike * dest_trace));
-    weight_delta = wd[wi] = d2f_rn(__dsub_rn(wdd, change));
+    const float p = dest_spike * src_trace;
+    const bool has_p = dest_spike != 0.0f;
+    float weight_delta;
+    if (!ff::weight_derivative(v.wd, p, has_p, dest_trace, src_spike, weight_delta))
+        weight_delta = wd_double(v.wd, p, has_p, dest_trace, src_spike);
+    wd[wi] = weight_delta;
     weight += lr * weight_delta;
     w[wi] = fmaxf(0.0001f, fminf(max_weight, weight));
     if (stp_flag) {
@@ -116,10 +140,9 @@ __device__ __forceinline__ void iz_learn_apply(size_t wi, const LearnVals& v, in
             stp_r[wi] = r + (((1 - r) / D) - (r * sw * src_spike));
         if (src_spike || !(U == (double)(float)U && sw == (float)U)) {
             // stp_w += (U - sw) / F + U * (1 - sw) * src_spike
-            const double swd = f2d_exact(sw);
-            double inc = div_const_rn<F>(__dsub_rn(U, swd));
-            if (src_spike) inc = inc + (U * (1 - sw) * src_spike);
-            stp_w[wi] = d2f_rn(__dadd_rn(swd, inc));
+            float nsw;
+            if (!ff::short_term_w<SUB>(sw, src_spike, nsw)) nsw = sw_double<SUB>(sw, src_spike);
+            stp_w[wi] = nsw;
         }
     }
 }

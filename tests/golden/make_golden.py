@@ -3,6 +3,11 @@
 Usage (in a checkout that has the reference sources):
     python oracle/build_ref.py
     OMP_NUM_THREADS=1 python tests/golden/make_golden.py [case ...]
+    OMP_NUM_THREADS=1 python tests/golden/make_golden.py c0_1000 c2_1000
+    python tests/golden/make_golden.py c1_10000      # game_of_life: any thread count
+
+The configurations at their stated sizes (c0_1000, c1_10000, c2_1000) are
+recorded as digests (see configs.py); the other cases as whole arrays.
 
 The reference library (oracle/_ref/libsyngen.so, built from the reference
 sources by oracle/build_ref.py) is driven through the reference's own Python
@@ -40,14 +45,7 @@ def load_reference_syngen():
     return mod
 
 
-def case_sizes(case):
-    """Layer sizes and weights per connection (checked against the reference below)."""
-    from oracle.oracle import OracleNetwork
-    onet = OracleNetwork(case.net)
-    sizes = {l.name: l.size for l in onet.layers}
-    sizes.update({"conn:" + c.name: c.num_weights for c in onet.conns})
-    sizes.update({"dense:" + c.name: c.dense_num_weights for c in onet.conns})
-    return sizes
+from tests.harness import case_sizes  # noqa: E402  (sizes checked against the reference below)
 
 
 def run_case(sg, case):
@@ -142,9 +140,30 @@ def _struct_of(case, layer):
     raise KeyError(layer)
 
 
+def scale_fixture(sg, name):
+    """Digest fixtures of the configurations at their stated sizes
+    (tests/golden/configs.py): per-step output digests and spike counts, and
+    state digests after 100 steps and at the end."""
+    from tests.golden import configs
+    from tests.harness import run_digest, run_gol_digest
+    if name == "c1_10000":
+        return run_gol_digest(sg, 2048, 10000, 1000)
+    case = {"c0_1000": configs.c0_case, "c2_1000": configs.c2_case}[name]()
+    return run_digest(case, sg, checkpoints=configs.CHECKPOINTS)
+
+
+SCALE = ("c0_1000", "c1_10000", "c2_1000")
+
+
 def main(names):
     sg = load_reference_syngen()
     for name in names or sorted(CASES):
+        if name in SCALE:
+            out = scale_fixture(sg, name)
+            path = os.path.join(HERE, name + ".npz")
+            np.savez_compressed(path, **out)
+            print("wrote", path, sum(v.nbytes for v in out.values()), "bytes")
+            continue
         out = run_case(sg, CASES[name])
         path = os.path.join(HERE, name + ".npz")
         np.savez_compressed(path, **out)

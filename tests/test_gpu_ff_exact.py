@@ -1,0 +1,61 @@
+"""The float-float evaluations of the STDP updater's double expressions
+(synaptogenesis_gb300/csrc/ff_exact.cuh) against the same expressions on the
+GPU's FP64 pipe: bit for bit wherever the rounding test accepts, over every
+float bit pattern for the weight derivative without spike terms and for
+short-term w (both opcodes, with and without a source spike), and on 2^32
+random operand triples with spike terms.  The test rejects non-finite
+operands, results below 2^-101 and values within the error bound of a
+rounding boundary; the rest must be a small fraction."""
+import ctypes
+import os
+import subprocess
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib(tmp_path_factory):
+    out = str(tmp_path_factory.mktemp("ffcheck") / "libffcheck_gpu.so")
+    nvcc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+    subprocess.run([nvcc, "-std=c++17", "-O3", "--fmad=false", "-shared", "-Xcompiler", "-fPIC",
+                    "-gencode", "arch=compute_103a,code=sm_103a",
+                    "-I", os.path.join(ROOT, "synaptogenesis_gb300", "csrc"),
+                    os.path.join(ROOT, "tests", "gpu_checks", "ff_check.cu"), "-o", out],
+                   check=True)
+    return ctypes.CDLL(out)
+
+
+def _out():
+    return (ctypes.c_ulonglong * 4)()
+
+
+def _ok(out, max_fallback):
+    assert out[0] == 0, "mismatch at %#x" % out[3]
+    assert out[2] <= max_fallback * out[1], (out[2], out[1])
+
+
+def test_weight_derivative_every_float(lib):
+    out = _out()
+    assert lib.check_wd_all(out) == 0
+    assert out[1] == 1 << 32
+    _ok(out, 0.12)        # non-finite and |x| >= 2^100 (11%), results below 2^-101
+
+
+@pytest.mark.parametrize("sub", [0, 1])
+@pytest.mark.parametrize("spike", [0, 1])
+def test_short_term_w_every_float(lib, sub, spike):
+    out = _out()
+    assert lib.check_sw_all(sub, spike, out) == 0
+    assert out[1] == 1 << 32
+    _ok(out, 0.21)
+
+
+def test_weight_derivative_random_spike_terms(lib):
+    out = _out()
+    assert lib.check_wd_random(ctypes.c_ulonglong(1 << 32), ctypes.c_ulonglong(3), out) == 0
+    assert out[1] == 1 << 32
+    _ok(out, 1e-3)
