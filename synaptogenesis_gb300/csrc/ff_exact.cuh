@@ -117,6 +117,8 @@ SG_FF bool rounds_to(float f, float g, float B) {
 }
 
 constexpr float kBound = 9.094947017729282379e-13f;   // 2^-40
+constexpr float kBound4 = 2.273736754432320595e-13f;  // 2^-42
+constexpr float kBound5 = 1.136868377216160297e-13f;  // 2^-43
 
 // Weight derivative of the STDP updater: (float)(x - c) with
 //   c = ((x - 1e-6) * 1e-4 [+ p] [- q])
@@ -201,6 +203,117 @@ SG_FF bool short_term_w(float sw, bool spike, float& out) {
     two_sum(r1, r2, f, g);
     const float M = add(add(a, mul(absf(d1), RF)), av);
     if (!rounds_to(f, g, mul(M, kBound))) return false;
+    out = f;
+    return true;
+}
+
+
+// Izhikevich voltage derivative of one Euler substep
+// (izhikevich_attributes.cpp:155-156):
+//   delta_v = (float)(0.04 * v * v + (5 * v) + 140 - recovery + current)
+// with the products and sums in double and 5 * v a float product.  With
+// u = 2^-24, the float-float value errs from the exact real expression by at
+// most u^2 (11 |P| + 10 S), P = 0.04 v v and S the largest partial sum, and
+// the reference's double roundings by less than 2^-53 (2 |P| + 5 S); the
+// bound used is 2^-43 (|P| + S), a factor of 2.9 above their sum.
+SG_FF bool iz_delta_v(float v, float recovery, float current, float& out) {
+    constexpr double C = 0.04;
+    constexpr float C1 = (float)C;
+    constexpr float C2 = (float)(C - (double)C1);
+    float h, l;
+    two_prod(v, C1, h, l);
+    l = add(l, mul(v, C2));                  // 0.04 v ~ h + l
+    float h2, l2;
+    two_prod(h, v, h2, l2);
+    l2 = add(l2, mul(l, v));                 // 0.04 v v ~ h2 + l2
+    const float v5 = mul(5.0f, v);
+    float s, e;
+    two_sum(h2, v5, s, e);
+    l2 = add(e, l2);
+    float smax = absf(s);
+    two_sum(s, 140.0f, s, e);
+    l2 = add(e, l2);
+    smax = fmaxf(smax, absf(s));
+    two_sum(s, -recovery, s, e);
+    l2 = add(e, l2);
+    smax = fmaxf(smax, absf(s));
+    two_sum(s, current, s, e);
+    l2 = add(e, l2);
+    smax = fmaxf(smax, absf(s));
+    float f, g;
+    two_sum(s, l2, f, g);
+    if (!rounds_to(f, g, mul(add(absf(h2), smax), kBound5))) return false;
+    out = f;
+    return true;
+}
+
+// The implicit voltage step of the substep (izhikevich_attributes.cpp:163-168):
+//   voltage = (float)((v + 0.1 * drive) / den),  den = 1 + 0.1 * sum_c
+// in double, where drive is the float sum the reference forms and den comes
+// from iz_denominator (den ~ d1 + d2, rd = 1 / d1 to float precision).
+SG_FF void iz_denominator(float sum_c, float& d1, float& d2) {
+    constexpr double T = 0.1;
+    constexpr float T1 = (float)T;
+    constexpr float T2 = (float)(T - (double)T1);
+    float b1, b2;
+    two_prod(sum_c, T1, b1, b2);
+    b2 = add(b2, mul(sum_c, T2));
+    float e;
+    two_sum(1.0f, b1, d1, e);
+    d2 = add(e, b2);
+}
+
+SG_FF bool iz_voltage(float v, float drive, float d1, float d2, float rd, float& out) {
+    constexpr double T = 0.1;
+    constexpr float T1 = (float)T;
+    constexpr float T2 = (float)(T - (double)T1);
+    float a1, a2;
+    two_prod(drive, T1, a1, a2);
+    a2 = add(a2, mul(drive, T2));            // 0.1 drive ~ a1 + a2
+    float n1, n2;
+    two_sum(v, a1, n1, n2);
+    n2 = add(n2, a2);                        // numerator ~ n1 + n2
+    const float q1 = mul(n1, rd);
+    float p1, p2;
+    two_prod(q1, d1, p1, p2);                // q1 d1 exactly
+    // numerator - q1 den, to float-float accuracy
+    const float r = sub(add(sub(sub(n1, p1), p2), n2), mul(q1, d2));
+    const float q2 = mul(r, rd);
+    float f, g;
+    two_sum(q1, q2, f, g);
+    const float M = add(mul(add(absf(v), absf(a1)), rd), absf(f));
+    if (!rounds_to(f, g, mul(M, kBound4))) return false;
+    out = f;
+    return true;
+}
+
+// Recovery time constant of the substep that crosses the threshold
+// (izhikevich_attributes.cpp:175-179):
+//   tau = (float)(delta_v / (30.0 - v + delta_v) * 0.1)
+// in double; 30 - v is exact.  The quotient's float-float error is below
+// 2^-44 of it plus 2^-48 of (|30 - v| + |delta_v|) / |denominator| of it.
+SG_FF bool iz_adjusted_tau(float v, float delta_v, float& out) {
+    constexpr double T = 0.1;
+    constexpr float T1 = (float)T;
+    constexpr float T2 = (float)(T - (double)T1);
+    float a1, a2;
+    two_sum(30.0f, -v, a1, a2);              // 30 - v exactly
+    float b1, b2;
+    two_sum(a1, delta_v, b1, b2);
+    b2 = add(b2, a2);                        // denominator ~ b1 + b2
+    const float r = 1.0f / b1;
+    const float q1 = mul(delta_v, r);
+    float p1, p2;
+    two_prod(q1, b1, p1, p2);
+    const float res = sub(sub(sub(delta_v, p1), p2), mul(q1, b2));
+    const float q2 = mul(res, r);            // quotient ~ q1 + q2
+    float t1, t2;
+    two_prod(q1, T1, t1, t2);
+    t2 = add(t2, add(mul(q1, T2), mul(q2, T1)));
+    float f, g;
+    two_sum(t1, t2, f, g);
+    const float M = mul(absf(f), add(2.0f, mul(add(absf(a1), absf(delta_v)), absf(r))));
+    if (!rounds_to(f, g, mul(M, kBound4))) return false;
     out = f;
     return true;
 }

@@ -421,10 +421,11 @@ __global__ void k_iz_uniform_delay(int n_src, const int* __restrict__ counts,
 }
 
 // Neuron update (izhikevich_attributes.cpp:102-213).  One launch updates the
-// Izhikevich layers of a step together (their neurons concatenated), so that
-// enough warps are in flight for the FP64 pipe; each layer's arrays are its
-// own.  The products with double constants (decays 0.95) and their float
-// results go through mul_fd_rn, bit-identical to the double arithmetic.
+// Izhikevich layers of a step together (their neurons concatenated); each
+// layer's arrays are its own.  The substeps run in float-float arithmetic
+// with rounding tests (iz_integrate_ff), bit-identical to the reference's
+// double evaluation; the products with double constants (decays 0.95) go
+// through mul_fd_rn.
 struct IzLayerArgs {
     int size, history;
     const float* inputs;
@@ -447,13 +448,10 @@ __global__ void __launch_bounds__(256) k_iz_update(IzUpdateGroup G) {
     while (l + 1 < G.n && g >= G.start[l + 1]) ++l;
     const IzLayerArgs& A = G.L[l];
     const int nid = g - G.start[l], size = A.size, history = A.history;
-    float ampa_c = A.ampa[nid], nmda_c = A.nmda[nid], gabaa_c = A.gabaa[nid], gabab_c = A.gabab[nid];
-    float mf = A.mult[nid];
     float voltage = A.voltages[nid];
     float recovery = A.recoveries[nid];
-    float base_current = A.inputs[nid];
-    iz_integrate(voltage, recovery, ampa_c, nmda_c, gabaa_c, gabab_c, mf, base_current,
-                 __ldg(A.as + nid), __ldg(A.bs + nid));
+    iz_integrate_ff(voltage, recovery, A.ampa[nid], A.nmda[nid], A.gabaa[nid], A.gabab[nid],
+                    A.mult[nid], A.inputs[nid], __ldg(A.as + nid), __ldg(A.bs + nid));
     A.ampa[nid] = 0.0f;
     A.nmda[nid] = 0.0f;
     A.gabaa[nid] = 0.0f;

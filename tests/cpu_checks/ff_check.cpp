@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <initializer_list>
 
 #include "ff_exact.cuh"
 
@@ -65,9 +66,85 @@ float draw(uint64_t z, float lim) {
     return (z & 1) ? -m : m;
 }
 
+// izhikevich_attributes.cpp:155-156 and 163-168, as the reference's C++
+// evaluates them
+float ref_dv(float v, float rec, float cur) {
+    return (float)((0.04 * v * v) + (5 * v) + 140 - rec + cur);
+}
+float ref_voltage(float v, float drive, float sum_c) {
+    return (float)((v + 0.1 * drive) / (1 + (0.1 * sum_c)));
+}
+float ref_tau(float v, float dv) { return (float)(dv / (30.0 - v + dv) * 0.1); }
+
+// Izhikevich substep operands: voltage mostly in [-100, 30] (a share exactly
+// at the reset values -65 and -50), recovery in [-30, 30], current and drive
+// log-uniform up to 100, conductance sums log-uniform up to 10.
+void iz_operands(uint64_t z0, float& v, float& rec, float& cur, float& sum_c) {
+    const uint64_t z1 = mix(z0), z2 = mix(z1), z3 = mix(z2);
+    const uint32_t sel = (uint32_t)(z0 >> 58);
+    v = sel < 4 ? -65.0f : sel < 6 ? -50.0f
+                         : (float)(-100.0 + 130.0 * (double)((z0 >> 11) & 0xFFFFFF) / 16777216.0);
+    rec = (float)(-30.0 + 60.0 * (double)((z1 >> 11) & 0xFFFFFF) / 16777216.0);
+    cur = draw(z2, 100.0f);
+    sum_c = std::fabs(draw(z3, 10.0f));
+}
+
 }  // namespace
 
 extern "C" {
+
+// n random Izhikevich substeps: delta_v and the implicit voltage update.
+int check_iz_random(unsigned long long n, unsigned long long seed, Result* dv, Result* vr,
+                    Result* tr) {
+    for (Result* r : {dv, vr, tr}) {
+        r->mismatches = r->checked = r->fallbacks = 0;
+        r->first = ~0ull;
+    }
+#pragma omp parallel
+    {
+        Result a{0, 0, 0, ~0ull}, b{0, 0, 0, ~0ull}, c{0, 0, 0, ~0ull};
+#pragma omp for schedule(static)
+        for (long long i = 0; i < (long long)n; ++i) {
+            float v, rec, cur, sum_c;
+            iz_operands(mix(seed * 0x100000001B3ull + (uint64_t)i), v, rec, cur, sum_c);
+            // the threshold-crossing substep: a derivative dv in [1, 1024) and
+            // a voltage past 30 by up to a tenth of it (v += 0.1 dv / den)
+            const float dvs = std::ldexp(1.0f + (v + 100.0f) / 130.0f, (int)((sum_c * 1e6f)) % 10);
+            const float vs = 30.0f + 0.1f * dvs * ((rec + 30.0f) / 60.0f) + 1e-3f;
+            float tau;
+            ++c.checked;
+            if (!sg::ff::iz_adjusted_tau(vs, dvs, tau)) {
+                ++c.fallbacks;
+            } else if (!same(tau, ref_tau(vs, dvs))) {
+                ++c.mismatches;
+                if ((unsigned long long)i < c.first) c.first = (unsigned long long)i;
+            }
+            float out;
+            ++a.checked;
+            if (!sg::ff::iz_delta_v(v, rec, cur, out)) {
+                ++a.fallbacks;
+            } else if (!same(out, ref_dv(v, rec, cur))) {
+                ++a.mismatches;
+                if ((unsigned long long)i < a.first) a.first = (unsigned long long)i;
+            }
+            float d1, d2;
+            sg::ff::iz_denominator(sum_c, d1, d2);
+            const float rd = 1.0f / d1;
+            ++b.checked;
+            if (!sg::ff::iz_voltage(v, cur, d1, d2, rd, out)) {
+                ++b.fallbacks;
+            } else if (!same(out, ref_voltage(v, cur, sum_c))) {
+                ++b.mismatches;
+                if ((unsigned long long)i < b.first) b.first = (unsigned long long)i;
+            }
+        }
+        merge(dv, a);
+        merge(vr, b);
+        merge(tr, c);
+    }
+    return 0;
+}
+
 
 // Every float x with (bits - offset) % stride == 0, no spike terms.
 int check_wd_strided(unsigned long long stride, unsigned long long offset, Result* r) {

@@ -111,19 +111,75 @@ __global__ void k_wd_random(unsigned long long n, unsigned long long seed, Resul
     atomicAdd(&r->fallbacks, fallbacks);
 }
 
+// izhikevich_attributes.cpp:155-156 and 163-168 in double
+__device__ float ref_dv(float v, float rec, float cur) {
+    double d = __dmul_rn(__dmul_rn(0.04, (double)v), (double)v);
+    d = __dadd_rn(d, (double)__fmul_rn(5.0f, v));
+    d = __dadd_rn(d, 140.0);
+    d = __dsub_rn(d, (double)rec);
+    d = __dadd_rn(d, (double)cur);
+    return __double2float_rn(d);
+}
+__device__ float ref_tau(float v, float dv) {
+    return __double2float_rn(__dmul_rn(__ddiv_rn((double)dv, __dadd_rn(__dsub_rn(30.0, (double)v),
+                                                                         (double)dv)), 0.1));
+}
+__device__ float ref_voltage(float v, float drive, float sum_c) {
+    return __double2float_rn(__ddiv_rn(__dadd_rn((double)v, __dmul_rn(0.1, (double)drive)),
+                                       __dadd_rn(1.0, __dmul_rn(0.1, (double)sum_c))));
+}
+
+// random Izhikevich substeps (operands as in the host check)
+__global__ void k_iz_random(unsigned long long n, unsigned long long seed, Result* dv, Result* vr,
+                            Result* tr) {
+    unsigned long long checked = 0, fb_dv = 0, fb_v = 0, fb_t = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint64_t z0 = mix(seed * 0x100000001B3ull + i), z1 = mix(z0), z2 = mix(z1),
+                       z3 = mix(z2);
+        const uint32_t sel = (uint32_t)(z0 >> 58);
+        const float v = sel < 4 ? -65.0f : sel < 6 ? -50.0f
+                        : -100.0f + 130.0f * ((float)((z0 >> 11) & 0xFFFFFF) * (1.0f / 16777216.0f));
+        const float rec = -30.0f + 60.0f * ((float)((z1 >> 11) & 0xFFFFFF) * (1.0f / 16777216.0f));
+        const float cur = draw(z2, 100.0f);
+        const float sum_c = fabsf(draw(z3, 10.0f));
+        float out;
+        ++checked;
+        if (!sg::ff::iz_delta_v(v, rec, cur, out)) ++fb_dv;
+        else record(dv, !same(out, ref_dv(v, rec, cur)), i);
+        float d1, d2;
+        sg::ff::iz_denominator(sum_c, d1, d2);
+        if (!sg::ff::iz_voltage(v, cur, d1, d2, 1.0f / d1, out)) ++fb_v;
+        else record(vr, !same(out, ref_voltage(v, cur, sum_c)), i);
+        // the threshold-crossing substep: dv in [1, 1024), v past 30 by up to dv / 10
+        const float dvs = ldexpf(1.0f + (v + 100.0f) / 130.0f, (int)(sum_c * 1e6f) % 10);
+        const float vs = 30.0f + 0.1f * dvs * ((rec + 30.0f) / 60.0f) + 1e-3f;
+        if (!sg::ff::iz_adjusted_tau(vs, dvs, out)) ++fb_t;
+        else record(tr, !same(out, ref_tau(vs, dvs)), i);
+    }
+    atomicAdd(&tr->checked, checked);
+    atomicAdd(&tr->fallbacks, fb_t);
+    atomicAdd(&dv->checked, checked);
+    atomicAdd(&dv->fallbacks, fb_dv);
+    atomicAdd(&vr->checked, checked);
+    atomicAdd(&vr->fallbacks, fb_v);
+}
+
 int run(void (*launch)(Result*), unsigned long long* out) {
     Result* d = nullptr;
-    if (cudaMalloc(&d, sizeof(Result)) != cudaSuccess) return 1;
-    Result h{0, 0, 0, ~0ull};
-    cudaMemcpy(d, &h, sizeof(h), cudaMemcpyHostToDevice);
+    if (cudaMalloc(&d, 3 * sizeof(Result)) != cudaSuccess) return 1;
+    Result h[3] = {{0, 0, 0, ~0ull}, {0, 0, 0, ~0ull}, {0, 0, 0, ~0ull}};
+    cudaMemcpy(d, h, sizeof(h), cudaMemcpyHostToDevice);
     launch(d);
     cudaError_t e = cudaDeviceSynchronize();
-    cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
     cudaFree(d);
-    out[0] = h.mismatches;
-    out[1] = h.checked;
-    out[2] = h.fallbacks;
-    out[3] = h.first;
+    for (int k = 0; k < 3; ++k) {
+        out[4 * k + 0] = h[k].mismatches;
+        out[4 * k + 1] = h[k].checked;
+        out[4 * k + 2] = h[k].fallbacks;
+        out[4 * k + 3] = h[k].first;
+    }
     return e == cudaSuccess ? 0 : 2;
 }
 
@@ -147,6 +203,14 @@ int check_wd_random(unsigned long long n, unsigned long long seed, unsigned long
     sn = n;
     ss = seed;
     return run([](Result* d) { k_wd_random<<<152 * 8, 256>>>(sn, ss, d); }, out);
+}
+
+int check_iz_random(unsigned long long n, unsigned long long seed, unsigned long long* out) {
+    static unsigned long long sn, ss;
+    sn = n;
+    ss = seed;
+    // three results: delta_v in out[0..3], voltage in out[4..7], tau in out[8..11]
+    return run([](Result* d) { k_iz_random<<<152 * 8, 256>>>(sn, ss, d, d + 1, d + 2); }, out);
 }
 
 }  // extern "C"

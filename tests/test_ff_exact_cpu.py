@@ -1,8 +1,10 @@
-"""Host checks of the float-float evaluations of the STDP updater's double
-expressions (synaptogenesis_gb300/csrc/ff_exact.cuh): wherever the rounding
-test accepts, the float result equals the reference's double expression
-evaluated by the host compiler, bit for bit.  Strided over the float bit
-patterns here (every one of them on the GPU), random with spike terms."""
+"""Host checks of the float-float evaluations of the Izhikevich model's
+double expressions (synaptogenesis_gb300/csrc/ff_exact.cuh): wherever the
+rounding test accepts, the float result equals the reference's double
+expression evaluated by the host compiler, bit for bit.  The STDP updater's
+expressions strided over the float bit patterns here (every one of them on
+the GPU) and random with spike terms; the neuron substep's two expressions
+on random operands."""
 import ctypes
 import os
 import subprocess
@@ -54,3 +56,13 @@ def test_weight_derivative_random_spike_terms(lib):
     lib.check_wd_random(ctypes.c_ulonglong(20_000_000), ctypes.c_ulonglong(5), ctypes.byref(r))
     assert r.checked == 20_000_000
     _check(r, 1e-3)
+
+
+def test_izhikevich_substep_random(lib):
+    dv, vr, tr = Result(), Result(), Result()
+    lib.check_iz_random(ctypes.c_ulonglong(20_000_000), ctypes.c_ulonglong(7), ctypes.byref(dv),
+                        ctypes.byref(vr), ctypes.byref(tr))
+    assert dv.checked == vr.checked == tr.checked == 20_000_000
+    _check(dv, 0.05)
+    _check(vr, 1e-3)
+    _check(tr, 1e-3)

@@ -1,9 +1,11 @@
-"""The float-float evaluations of the STDP updater's double expressions
+"""The float-float evaluations of the Izhikevich model's double expressions
 (synaptogenesis_gb300/csrc/ff_exact.cuh) against the same expressions on the
 GPU's FP64 pipe: bit for bit wherever the rounding test accepts, over every
-float bit pattern for the weight derivative without spike terms and for
-short-term w (both opcodes, with and without a source spike), and on 2^32
-random operand triples with spike terms.  The test rejects non-finite
+float bit pattern for the STDP weight derivative without spike terms and for
+short-term w (both opcodes, with and without a source spike), on 2^32
+random operand triples with spike terms, and on 2^32 random neuron substeps
+(the voltage derivative, the implicit voltage update and the recovery time
+constant of a threshold-crossing substep).  The test rejects non-finite
 operands, results below 2^-101 and values within the error bound of a
 rounding boundary; the rest must be a small fraction."""
 import ctypes
@@ -30,7 +32,7 @@ def lib(tmp_path_factory):
 
 
 def _out():
-    return (ctypes.c_ulonglong * 4)()
+    return (ctypes.c_ulonglong * 12)()
 
 
 def _ok(out, max_fallback):
@@ -59,3 +61,12 @@ def test_weight_derivative_random_spike_terms(lib):
     assert lib.check_wd_random(ctypes.c_ulonglong(1 << 32), ctypes.c_ulonglong(3), out) == 0
     assert out[1] == 1 << 32
     _ok(out, 1e-3)
+
+
+def test_izhikevich_substep_random(lib):
+    out = _out()
+    assert lib.check_iz_random(ctypes.c_ulonglong(1 << 32), ctypes.c_ulonglong(9), out) == 0
+    assert out[1] == out[5] == out[9] == 1 << 32
+    _ok(out[:4], 0.05)
+    _ok(out[4:8], 1e-3)
+    _ok(out[8:], 1e-3)
