@@ -1,13 +1,22 @@
 """Benchmark of the GB300 simulation cycle (one JSON line on rank 0).
 
-Default workload: game of life on a 2048x2048 toroidal grid (3x3 convergent
-wrap connection, B3/S23, cells alive with p=0.3 from seed 1); one bench step is
-the full 10,000-timestep run of that grid.  Metric: synapse updates per second
-(a synapse update is one (destination, weight) visit in one timestep: 9 per
-cell, as the reference computes the zero centre weight too).
+Default workload (``iz_plastic``): three 256x256 Izhikevich layers (80%
+regular / 20% fast spiking), L1->L2 convergent 9x9 with STDP, L2->L3
+divergent 3x3 stride 2, L3->L1 one-to-one, a 4096x4096 subset projection,
+delays U{0..3}, a 5 Hz Poisson drive generated on the device; one bench step
+is 1000 timesteps.  Metric: synapse updates per second (one (destination,
+weight) visit in an activator or updater in one timestep).  The network and
+its injected weights, delays and per-neuron parameters are those of the
+parity case at the same size (tests/golden/configs.py).
+
+On one GPU the line also nests the other measured configurations under
+"configs" (each from its own child run of this script): ``iz_c0`` (32x32
+Izhikevich), ``gol`` (game of life 2048x2048, 10,000 timesteps per step),
+``batched`` (256 instances) and ``rate_adjoint`` (differentiable rate
+network), each with its roofline, CPU baseline and end-to-end figure.
 
   python bench.py [--gpus N] [--steps K] [--warmup W]
-                  [--workload gol|iz_plastic|batched|rate_adjoint|spnet_sparse]
+                  [--workload iz_plastic|iz_c0|gol|batched|rate_adjoint|spnet_sparse]
   python bench.py --impl reference ...   # the reference's own CPU path
 
 Timing: each step is bracketed by CUDA events recorded on the stream the
@@ -69,6 +78,7 @@ def gol_workload(side=2048):
         # timestep and cell a step reads the newest and the oldest history bit
         # and writes one new bit (3 bits); the word layout would move 8 B.
         "kernel": "k_gol_planes_steps (16 timesteps per launch)",
+        "profile_group": "game_of_life.advance",
         "steps_per_launch": 16,
         "timestep_bytes": 3 * n // 8,
         "word_layout_timestep_bytes": 8 * n,
@@ -79,54 +89,50 @@ def gol_workload(side=2048):
     }
 
 
-def iz_plastic_workload(side=256):
+def _inject_case(net_obj, inject, sizes_of):
+    """Applies a parity case's injections (tests/golden/configs.py) to a
+    built network; delays go in through the delay callback at build time."""
+    for key, arr in inject.items():
+        if key[2] == "delays":
+            continue
+        if key[0] == "neuron":
+            dst = net_obj.get_neuron_data(key[1], key[2], key[3]).to_np_array()
+        else:
+            dst = net_obj.get_weight_matrix(key[1], key[2]).to_np_array()
+        dst.view(arr.dtype)[:] = arr
+
+
+def _case_network(net, inject_fn, seed):
+    """(network dict with delay callbacks, injections, delays, sizes) of a
+    parity case's network, for the bench's builds of the same configuration."""
+    import numpy as np
+    from tests.golden.cases import Case, callback_injections
+    from tests.harness import case_sizes
+    sizes = case_sizes(Case("bench", net, 1, seed))
+    inj = inject_fn(np.random.default_rng(seed), sizes)
+    delays = {k: v for k, v in inj.items() if k[2] == "delays"}
+    net_dict, _, _, delay_arrays = callback_injections(net, delays)
+    return net_dict, inj, delay_arrays, sizes
+
+
+def _delay_callback(sg, delay_arrays):
+    def delay_cb(ID, size, weights, delays):
+        sg.IntArray(size, delays).to_np_array()[:] = delay_arrays[ID]
+    if not hasattr(sg, "_delay_weight_callbacks"):
+        sg._delay_weight_callbacks = {}
+    sg.create_delay_weight_callback("golden_delay", delay_cb)
+
+
+def iz_plastic_workload():
     """Large plastic Izhikevich network: three 256x256 Izhikevich layers with STDP on the convergent
     connection, a 4096x4096 subset projection and a 5 Hz Poisson drive."""
-    import numpy as np
-    n = side * side
-
-    def layer(name, drive=False):
-        d = {"name": name, "neural model": "izhikevich", "rows": side, "columns": side}
-        if drive:   # 5 Hz at 1 ms per step, seeded, generated on the device
-            d["init config"] = {"type": "poisson", "rate": 5, "value": 20, "seed": 11}
-        return d
-    lo, hi = side * 3 // 8, side * 3 // 8 + 64
-    net = {"structures": [{"name": "s", "type": "parallel", "layers": [
-        layer("L1", drive=True), layer("L2"), layer("L3")]}],
-        "connections": [
-            {"name": "c12", "from layer": "L1", "to layer": "L2", "type": "convergent",
-             "opcode": "add", "plastic": True, "learning rate": 0.004, "myelinated": True,
-             "arborized config": {"field size": 9, "wrap": True},
-             "weight config": {"type": "random", "min weight": 0.0, "max weight": 0.3, "seed": 21}},
-            {"name": "c23", "from layer": "L2", "to layer": "L3", "type": "divergent",
-             "opcode": "add", "plastic": False, "myelinated": True,
-             "arborized config": {"field size": 3, "stride": 2},
-             "weight config": {"type": "random", "min weight": 0.0, "max weight": 0.3, "seed": 22}},
-            {"name": "c31", "from layer": "L3", "to layer": "L1", "type": "one to one",
-             "opcode": "sub", "plastic": False, "myelinated": True,
-             "weight config": {"type": "flat", "weight": 0.5}},
-            {"name": "c23s", "from layer": "L2", "to layer": "L3", "type": "subset",
-             "opcode": "add", "plastic": False, "myelinated": True,
-             "subset config": {"from row start": lo, "from row end": hi, "from column start": lo,
-                               "from column end": hi, "to row start": lo, "to row end": hi,
-                               "to column start": lo, "to column end": hi},
-             "weight config": {"type": "gaussian", "mean": 0.0, "std dev": 0.05, "seed": 23}}]}
+    from tests.golden import configs
+    n = configs.C2_SIDE ** 2
+    net = configs.c2_net(device_drive=11)
+    net_dict, inj, delay_arrays, sizes = _case_network(net, configs.c2_inject, 221)
 
     def inject(net_obj):
-        rng = np.random.default_rng(2)
-        for lname in ("L1", "L2", "L3"):
-            fast = rng.random(n) < 0.2           # 80% regular, 20% fast spiking
-            vals = {"a": np.where(fast, 0.1, 0.02), "b": np.full(n, 0.2),
-                    "c": np.full(n, -65.0), "d": np.where(fast, 2.0, 8.0)}
-            for k, v in vals.items():
-                net_obj.get_neuron_data("s", lname, k).to_np_array()[:] = v.astype(np.float32)
-            net_obj.get_neuron_data("s", lname, "voltage").to_np_array()[:] = -65.0
-            net_obj.get_neuron_data("s", lname, "recovery").to_np_array()[:] = (
-                np.float32(0.2) * np.float32(-65.0))
-        # short-term w of convergent / divergent / one-to-one connections is 0 in
-        # the reference (type compared with opcodes); give them the ADD value.
-        for cname in ("c12", "c23", "c31"):
-            net_obj.get_weight_matrix(cname, "short term w").to_np_array()[:] = 0.5
+        _inject_case(net_obj, inj, sizes)
 
     def result(net_obj):
         return net_obj.get_neuron_data("s", "L3", "output").to_np_array()
@@ -137,18 +143,64 @@ def iz_plastic_workload(side=256):
         "name": "iz_plastic",
         "desc": "3x 256x256 Izhikevich (80% RS / 20% FS), L1->L2 convergent 9x9 STDP, "
                 "L2->L3 divergent 3x3 stride 2, L3->L1 one-to-one, L2->L3 subset 4096x4096, "
-                "5 Hz Poisson drive",
-        "net": net, "inject": inject, "result": result,
+                "delays U{0..3}, 5 Hz Poisson drive of value 20 generated on the device",
+        "net": net_dict, "inject": inject, "result": result,
+        "prepare": lambda sg: _delay_callback(sg, delay_arrays),
         "timesteps": 1000,
         "units_per_timestep": activate + conv,          # activator visits + updater visits
         "unit": "synapse-updates/s",
         "dtype": "f32",
-        "kernel": "izhikevich.activate.subset",
-        "bytes_per_launch": 32 * sub,                   # w, stp r/w, delay, 2 traces r+w
+        # algorithmic bytes per launch of each profiled kernel group
+        "group_bytes": {"izhikevich.activate.subset": 32 * sub,         # w, stp r/w, delay, traces r+w
+                        "izhikevich.learn.convergent": 40 * conv,       # w, presyn, wd, stp r/w r+w
+                        "izhikevich.activate.convergent": 32 * conv,
+                        "izhikevich.activate.divergent": 32 * div,
+                        "izhikevich.activate.one to one": 32 * one,
+                        "izhikevich.update": 124 * 3 * n},
         "bytes_per_timestep": 32 * activate + 40 * conv + 3 * n * 124,
         "state_bytes": None,                            # taken from the run report
         "cpu_seconds": 15.0,
         "learning": True,
+    }
+
+
+def iz_c0_workload():
+    """The 32x32 plain Izhikevich network (no plasticity): relay input driven
+    at 10 Hz on the device, convergent 5x5 wrap excitatory, recurrent fully
+    connected inhibitory at 20% density, delays U{0..3}."""
+    from tests.golden import configs
+    net = configs.c0_net()
+    net["structures"][0]["layers"][0]["init config"] = {"type": "poisson", "rate": 10,
+                                                         "value": 1.0, "seed": 12}
+    net_dict, inj, delay_arrays, sizes = _case_network(net, configs.c0_inject, 201)
+    n = 32 * 32
+
+    def inject(net_obj):
+        _inject_case(net_obj, inj, sizes)
+
+    def result(net_obj):
+        return net_obj.get_neuron_data("s", "iz", "output").to_np_array()
+
+    conv, fc = n * 25, n * n
+    return {
+        "name": "iz_c0",
+        "desc": "32x32 relay (10 Hz Poisson drive generated on the device) -> 32x32 Izhikevich "
+                "regular spiking, convergent 5x5 wrap U(0,0.5), recurrent fully connected 20% "
+                "density U(0,0.2), delays U{0..3}, no plasticity",
+        "net": net_dict, "inject": inject, "result": result,
+        "prepare": lambda sg: _delay_callback(sg, delay_arrays),
+        "timesteps": 1000,
+        "units_per_timestep": conv + fc,
+        "unit": "synapse-updates/s",
+        "dtype": "f32",
+        "group_bytes": {"izhikevich.activate.fully connected": 32 * fc,
+                        "izhikevich.activate.convergent": 28 * conv,    # FLOAT source: no delay read
+                        "izhikevich.update": 124 * n},
+        "bytes_per_timestep": 32 * fc + 28 * conv + 124 * n,
+        "l2_note": "34 MB per timestep: L2-resident within a bench step; flushed between steps",
+        "state_bytes": None,
+        "cpu_seconds": 10.0,
+        "learning": False,
     }
 
 
@@ -265,8 +317,12 @@ def rate_inputs(batch=64, seed=4):
             "target": rng.uniform(0, 1, (batch, c["outputs"])).astype(np.float32)}
 
 
-WORKLOADS = {"gol": gol_workload, "iz_plastic": iz_plastic_workload, "batched": batched_workload,
-             "rate_adjoint": rate_workload, "spnet_sparse": spnet_sparse_workload}
+WORKLOADS = {"gol": gol_workload, "iz_plastic": iz_plastic_workload, "iz_c0": iz_c0_workload,
+             "batched": batched_workload, "rate_adjoint": rate_workload,
+             "spnet_sparse": spnet_sparse_workload}
+# the configurations nested in the default line, and their child-run arguments
+SUB_RECORDS = (("iz_c0", []), ("gol", []), ("batched", ["--steps", "3", "--warmup", "3"]),
+               ("rate_adjoint", []))
 
 # Sides of the instances timed one at a time (plain GPU path / reference CPU
 # path); the per-timestep time is fitted as alpha + beta * (recurrent synapses)
@@ -430,6 +486,8 @@ def cpu_worker(args):
         print(json.dumps({"value": len(insts) / secs, "seconds": total_s, "timesteps": total_steps,
                           "samples": samples, "alpha": alpha, "beta": beta}))
         return
+    if wl.get("prepare"):
+        wl["prepare"](sg)
     net = sg.Network(wl["net"])
     net.build_state()
     wl["inject"](net)
@@ -503,6 +561,8 @@ def run_gb300(args, rank, world, local):
     sg.set_warnings(False)
     wl = WORKLOADS[args.workload]()
     T = args.timesteps or wl["timesteps"]
+    if wl.get("prepare"):
+        wl["prepare"](sg)
     net = sg.Network(wl["net"])
     net.build_state()
     wl["inject"](net)
@@ -551,13 +611,25 @@ def run_gb300(args, rank, world, local):
         print("# %-36s groups %7s  mean %9.2f us  share %5.1f%%"
               % (name, k["groups"], float(k["mean us"]), 100.0 * float(k["total ms"]) / total_ms),
               file=sys.stderr)
-    dom = kern.get(wl["kernel"])
-    mean_us = float(dom["mean us"]) if dom else None
-    profiled_us = mean_us
+    mean_us = profiled_us = None
+    dominant = wl.get("kernel")
+    if wl.get("group_bytes"):
+        # the kernel group with the largest share of the profiled pass
+        ranked = sorted(kern.items(), key=lambda kv: -float(kv[1]["total ms"]))
+        named = [(n, k) for n, k in ranked if n in wl["group_bytes"]]
+        if named:
+            dominant = named[0][0]
+            wl["bytes_per_launch"] = wl["group_bytes"][dominant]
+            mean_us = profiled_us = float(named[0][1]["mean us"])
+        wl["shares"] = {n: round(float(k["total ms"]) / total_ms, 4) for n, k in ranked}
     if wl.get("timestep_bytes"):
         # every timed launch but two format conversions per run is the
         # multi-step kernel: its mean duration from the timed region
         mean_us = dev_ms * 1000.0 / (T * args.steps) * wl["steps_per_launch"]
+        adv = kern.get(wl.get("profile_group", ""))
+        if adv and int(adv["launches"]) > 0:
+            profiled_us = 1000.0 * float(adv["total ms"]) / int(adv["launches"])
+    wl["dominant"] = dominant
 
     # -- end to end through the public API with host buffers ----------------
     env = sg.Environment({"modules": []})
@@ -685,14 +757,19 @@ def run_batched(args, rank, world, local):
 
 def batched_line(args, world, r, wl, cb):
     peak, peak_kind = measured_peak()
-    achieved = r["step_bytes"] / (r["mean_us"] * 1e-6) / 1e9
+    p = r["props"]
+    # algorithmic bytes: the non-zero recurrent synapses (read 16, write 8),
+    # the convergent synapses (read 12, write 8) and the neurons (24); the
+    # kernel also moves the ELL padding and the idle lanes of partial groups
+    algo_bytes = (int(p["fc synapses"]) * 24 + int(p["conv synapses"]) * 20
+                  + int(p["neurons"]) * 24)
+    achieved = algo_bytes / (r["mean_us"] * 1e-6) / 1e9
     traffic = None
     try:
         with open(TRAFFIC) as f:
             traffic = json.load(f).get(args.workload)
     except Exception:
         pass
-    p = r["props"]
     value = r["units"] / r["dev_s"]
     return {
         "metric": "instance-timesteps/s (batched)", "value": value, "unit": wl["unit"],
@@ -714,7 +791,8 @@ def batched_line(args, world, r, wl, cb):
                    "parallelism": "instances sharded over ranks" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": wl["kernel"], "bytes_per_launch": r["step_bytes"],
+                     "kernel": wl["kernel"], "bytes_per_launch": algo_bytes,
+                     "moved_bytes_per_launch": r["step_bytes"],
                      "mean_launch_us": r["mean_us"]},
         "plain_gpu_one_at_a_time": r["plain"],
         "cpu_baseline": cb,
@@ -853,13 +931,37 @@ def rate_line(args, world, r, wl, cb):
     }
 
 
+def sub_records(args):
+    """The other measured configurations, each from a child run of this
+    script on the same GPU (one JSON line each)."""
+    out = {}
+    for name, extra in SUB_RECORDS:
+        cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--workload", name,
+               "--steps", str(min(args.steps, 10)), "--warmup", str(max(3, min(args.warmup, 3)))]
+        cmd += extra
+        if args.no_cpu_baseline:
+            cmd.append("--no-cpu-baseline")
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=1200)
+            lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+            if r.returncode != 0 or not lines:
+                out[name] = {"failed": (r.stderr or r.stdout)[-400:]}
+                continue
+            out[name] = json.loads(lines[-1])
+        except Exception as e:                              # noqa: BLE001
+            out[name] = {"failed": repr(e)[:400]}
+    return out
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="gol", choices=sorted(WORKLOADS))
+    p.add_argument("--workload", default="iz_plastic", choices=sorted(WORKLOADS))
+    p.add_argument("--no-sub", action="store_true",
+                   help="default workload: leave out the nested configurations")
     p.add_argument("--timesteps", type=int, default=0, help="timesteps per bench step")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--instances", type=int, default=0,
@@ -946,6 +1048,24 @@ def main():
     if not args.no_cpu_baseline:
         cb = cpu_baseline(args.workload, wl["cpu_seconds"])
     value = r["units"] / r["dev_s"]
+    ms_per_timestep = 1000.0 * r["dev_s"] / (args.steps * r["T"])
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None,
+                "traffic": traffic.get(wl["dominant"]) if isinstance(traffic, dict) else traffic,
+                "peak_kind": peak_kind,
+                "kernel": wl["dominant"], "bytes_per_launch": wl.get("bytes_per_launch"),
+                "mean_launch_us": r["mean_us"],
+                "profiled_launch_us": r["profiled_us"],
+                "word_layout_bytes_per_timestep": wl.get("word_layout_timestep_bytes")}
+    if wl.get("shares"):
+        roofline["profiled_shares"] = wl["shares"]
+    if wl.get("bytes_per_timestep"):
+        # the whole timestep: every kernel's algorithmic bytes over the
+        # device time per timestep
+        step_gbs = wl["bytes_per_timestep"] / (ms_per_timestep * 1e-3) / 1e9
+        roofline["step"] = {"bytes_per_timestep": wl["bytes_per_timestep"],
+                            "ms_per_timestep": ms_per_timestep, "achieved": step_gbs,
+                            "frac": step_gbs / peak}
     line = {
         "metric": metric, "value": value, "unit": wl["unit"], "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
@@ -953,16 +1073,11 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": wl["dtype"], "data": "synthetic",
         "config": {"workload": wl["desc"], "timesteps_per_step": r["T"],
-                   "ms_per_timestep": 1000.0 * r["dev_s"] / (args.steps * r["T"]),
-                   "l2": "flushed between steps (256 MiB write outside the timed events)",
+                   "ms_per_timestep": ms_per_timestep,
+                   "l2": wl.get("l2_note", "flushed between steps (256 MiB write outside the "
+                                           "timed events)"),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None,
-                     "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": wl["kernel"], "bytes_per_launch": wl["bytes_per_launch"],
-                     "mean_launch_us": r["mean_us"],
-                     "profiled_launch_us": r["profiled_us"],
-                     "word_layout_bytes_per_timestep": wl.get("word_layout_timestep_bytes")},
+        "roofline": roofline,
         "cpu_baseline": cb,
         "e2e": {"value": r["e2e_value"], "unit": wl["unit"],
                 "h2d_bytes_per_step": r["state_bytes"], "d2h_bytes_per_step": r["state_bytes"],
@@ -970,6 +1085,8 @@ def main():
         "clocks": r["clocks"],
         "gpu_launches": r["launches"],
     }
+    if world == 1 and args.workload == "iz_plastic" and not args.no_sub:
+        line["configs"] = sub_records(args)
     print(json.dumps(line))
 
 

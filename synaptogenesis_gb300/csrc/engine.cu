@@ -102,11 +102,13 @@ Engine::Engine(Network* net, Environment* env, State* state, const Props& args)
         profile_ = args.get_bool("profile", false);
         use_graphs_ = args.get_bool("graphs", true) && !profile_;
         // Learning overlapped with the next step's activations, for networks
-        // whose learned connections are large (at least 2^20 synapses), with
-        // plain launches: measured on the 3 x 256^2 plastic network, 288 us
-        // per step against 342 us for graphs without overlap (graph replay
-        // did not run the two branches concurrently, 332 us).  One stream
-        // when profiling, so that the per-group timings stay separate.
+        // whose learned connections are large (at least 2^20 synapses): the
+        // learning kernels go to a low-priority side stream, with plain
+        // launches.  Measured on the 3 x 256^2 plastic network: 237 us per
+        // step, against 254 us for graphs of the same two branches
+        // (instantiated to honour the node priorities copied from the
+        // streams at capture) and 266 us for graphs without overlap.  One
+        // stream when profiling, so that the per-group timings stay separate.
         if (learning_)
             for (auto& lp : net_->layers)
                 for (Connection* c : lp->inputs)
@@ -122,7 +124,7 @@ Engine::Engine(Network* net, Environment* env, State* state, const Props& args)
         for (auto& sp : net_->structures) ordered_ = ordered_ || !sp->parallel();
         overlap_ = learning_ && !profile_ && !ordered_ &&
                    args.get_bool("overlap learning", learned >= (1LL << 20));
-        if (overlap_) use_graphs_ = false;
+        if (overlap_) use_graphs_ = args.get_bool("graphs", false);
         if (overlap_) {
             side_ = engine_side_stream();
             SG_CUDA(cudaEventCreateWithFlags(&fork_ev_, cudaEventDisableTiming));
@@ -591,7 +593,7 @@ long Engine::step(long n) {
                 for (int k = 0; k < graph_steps_; ++k) enqueue_step(false);
                 join_side();                 // the side stream rejoins inside the graph
                 SG_CUDA(cudaStreamEndCapture(stream_, &g));
-                SG_CUDA(cudaGraphInstantiate(&ng.exec, g, 0));
+                SG_CUDA(cudaGraphInstantiate(&ng.exec, g, cudaGraphInstantiateFlagUseNodePriority));
                 SG_CUDA(cudaGraphDestroy(g));
                 ng.launches = launches_ - before;
                 launches_ = before;

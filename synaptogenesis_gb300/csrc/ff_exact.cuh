@@ -109,9 +109,10 @@ SG_FF void two_prod(float a, float b, float& p, float& e) {
 SG_FF bool rounds_to(float f, float g, float B) {
     const uint32_t u = bits(f) & 0x7FFFFFFFu;
     const uint32_t E = u >> 23;
-    if (E < 26u || E > 253u) return false;
-    const bool toward_zero = ((bits(f) ^ bits(g)) >> 31) != 0u && absf(g) != 0.0f;
-    const uint32_t hE = (toward_zero && (u & 0x7FFFFFu) == 0u) ? E - 25u : E - 24u;
+    if (E - 26u > 227u) return false;                  // E outside [26, 253]
+    // a power of two: the boundary below is a quarter of its ulp away (taken
+    // on both sides)
+    const uint32_t hE = (u & 0x7FFFFFu) == 0u ? E - 25u : E - 24u;
     const float lim = mul(from_bits(hE << 23), 0.99999904632568359375f);   // 1 - 2^-20
     return add(absf(g), B) <= lim;
 }
@@ -119,6 +120,28 @@ SG_FF bool rounds_to(float f, float g, float B) {
 constexpr float kBound = 9.094947017729282379e-13f;   // 2^-40
 constexpr float kBound4 = 2.273736754432320595e-13f;  // 2^-42
 constexpr float kBound5 = 1.136868377216160297e-13f;  // 2^-43
+
+// (float)((double)p * c) for a double constant c ~ c1 + c2 (two floats, c2
+// the rounded remainder): Dekker's product plus the remainder's, error below
+// 2^-45 |p c| in all, bound 2^-40 |f|.  Operands below 2^-50 are scaled by
+// 2^64 first (exact, as are both roundings of a result in the normal float
+// range); results below 2^-126 return false.
+SG_FF bool product(float p, float c1, float c2, float& out) {
+    const bool small = absf(p) < 8.881784197001252323e-16f;             // 2^-50
+    const float ps = small ? mul(p, 18446744073709551616.0f) : p;       // 2^64
+    float h, l;
+    two_prod(ps, c1, h, l);
+    l = add(l, mul(ps, c2));
+    float f, g;
+    two_sum(h, l, f, g);
+    if (!rounds_to(f, g, mul(absf(f), kBound))) return false;
+    if (small) {
+        if (absf(f) < 2.168404344971008868e-19f) return false;          // 2^-62: result below 2^-126
+        f = mul(f, 5.421010862427522170e-20f);                          // 2^-64, exact for normal results
+    }
+    out = f;
+    return true;
+}
 
 // Weight derivative of the STDP updater: (float)(x - c) with
 //   c = ((x - 1e-6) * 1e-4 [+ p] [- q])

@@ -59,8 +59,8 @@ struct IzLut { float src[33]; float dst[33]; };
 //    evaluation (wd_double, sw_double), kept out of line;
 //  * a spike product that is zero (no destination / source spike) adds or
 //    subtracts +0.0 to a partial sum that is never zero, so it is skipped;
-//  * the presynaptic trace decay product runs in integer arithmetic
-//    (exact_convert.cuh).
+//  * the presynaptic trace decay product is a float-float product with the
+//    same rounding test (integer arithmetic where it fails, exact_convert.cuh).
 // iz_learn_load reads a synapse's variables and iz_learn_apply updates them,
 // so that a thread can have several synapses' loads in flight at once.
 struct LearnVals {
@@ -79,6 +79,9 @@ __device__ __forceinline__ LearnVals iz_learn_load(size_t wi, int stp_flag, cons
     v.sw = stp_flag ? stp_w[wi] : 0.0f;
     return v;
 }
+
+// presyn * 0.933 in double, rounded to float.
+static __device__ __noinline__ float presyn_decay_exact(float p) { return mul_fd_rn(p, 0.933); }
 
 // wd - ((wd - 1e-6) * 1e-4 [+ p] [- q]) in double, rounded to float.
 static __device__ __noinline__ float wd_double(float x, float p, bool has_p, float q, bool has_q) {
@@ -115,7 +118,10 @@ __device__ __forceinline__ void iz_learn_apply(size_t wi, const LearnVals& v, in
     float src_trace, dest_trace;
     if (!SUB) {
         // presyn = src_spike ? 0.004 : presyn * 0.933, stored as float
-        src_trace = src_spike ? (float)0.004 : mul_fd_rn(v.presyn, 0.933);
+        constexpr float C1 = (float)0.933;
+        constexpr float C2 = (float)(0.933 - (double)C1);
+        if (src_spike) src_trace = (float)0.004;
+        else if (!ff::product(v.presyn, C1, C2, src_trace)) src_trace = presyn_decay_exact(v.presyn);
         presyn[wi] = src_trace;
         dest_trace = dest_exc_trace;
     } else {
@@ -221,6 +227,30 @@ __device__ __forceinline__ int conv_source(const DGeom& g, int d, int k) {
     return fr * g.from_cols + fc;
 }
 
+// The same through a per-CTA table of kernel-position offsets: `koff[k]` =
+// (kr * row spacing, kc * column spacing), filled by conv_offsets, and the
+// destination's base coordinates from conv_base.
+__device__ __forceinline__ int2 conv_base(const DGeom& g, int d) {
+    const int tr = d / g.to_cols, tc = d - tr * g.to_cols;
+    return make_int2(tr * g.rs + g.rsp * g.ro, tc * g.cs + g.csp * g.co);
+}
+__device__ __forceinline__ void conv_offsets(const DGeom& g, int K, int2* koff) {
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        const int kr = k / g.cf;
+        koff[k] = make_int2(kr * g.rsp, (k - kr * g.cf) * g.csp);
+    }
+}
+__device__ __forceinline__ int conv_source_at(const DGeom& g, int2 base, int2 off) {
+    int fr = base.x + off.x, fc = base.y + off.y;
+    if (g.wrap) {
+        fr = wrap_coord(g, fr, g.from_rows);
+        fc = wrap_coord(g, fc, g.from_cols);
+    } else if (fr < 0 || fr >= g.from_rows || fc < 0 || fc >= g.from_cols) {
+        return -1;
+    }
+    return fr * g.from_cols + fc;
+}
+
 // Trace activator for non-convolutional convergent connections.  A CTA owns
 // 32 consecutive destinations; its 8 warps take the kernel positions k in
 // turn (warp w: k = w, w+8, ...), one lane per destination, so every load is a
@@ -238,9 +268,13 @@ __global__ void __launch_bounds__(256) k_iz_activate_conv_tile(
     float long_tau, float* __restrict__ short_cond, float* __restrict__ long_cond) {
     __shared__ float s_st[kConvMaxK][32];
     __shared__ float s_lt[LONG ? kConvMaxK : 1][32];
+    __shared__ int2 koff[kConvMaxK];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int d = blockIdx.x * 32 + lane;
     const bool ok = d < g.to_size;
+    conv_offsets(g, K, koff);
+    __syncthreads();
+    const int2 base = conv_base(g, ok ? d : 0);
     constexpr int B = 4;                 // kernel positions whose loads are in flight together
     for (int k0 = warp; k0 < K; k0 += 8 * B) {
         uint32_t word[B];
@@ -250,7 +284,7 @@ __global__ void __launch_bounds__(256) k_iz_activate_conv_tile(
 #pragma unroll
         for (int b = 0; b < B; ++b) {
             const int k = k0 + 8 * b;
-            const int from = (ok && k < K) ? conv_source(g, d, k) : -1;
+            const int from = (ok && k < K) ? conv_source_at(g, base, koff[k]) : -1;
             on[b] = from >= 0;
             if (on[b]) {
                 const size_t wi = (size_t)k * g.to_size + d;
@@ -288,20 +322,23 @@ __global__ void __launch_bounds__(256) k_iz_activate_conv_tile(
     if (warp == 0) {
         float sum = 0.0f;
         for (int k = 0; k < K; ++k)
-            if (g.wrap || conv_source(g, d, k) >= 0) sum += s_st[k][lane];
+            if (g.wrap || conv_source_at(g, base, koff[k]) >= 0) sum += s_st[k][lane];
         short_cond[d] += sum;
     } else if (LONG && warp == 1) {
         float sum = 0.0f;
         for (int k = 0; k < K; ++k)
-            if (g.wrap || conv_source(g, d, k) >= 0) sum += s_lt[k][lane];
+            if (g.wrap || conv_source_at(g, base, koff[k]) >= 0) sum += s_lt[k][lane];
         long_cond[d] += sum;
     }
 }
 
 // Updater for non-convolutional convergent connections: one thread per
 // synapse (kernel position, destination), coalesced along destinations.  A
-// thread takes its kernel positions kLearnBatch at a time and loads all of
-// their variables before updating any (distinct synapses: no overlap).
+// CTA owns 32 consecutive destinations; its 8 warps take the kernel
+// positions in turn (warp w: k = w, w+8, ...), kLearnBatch at a time, loading
+// all of their variables before updating any (distinct synapses: no
+// overlap).  Source coordinates come from a per-CTA table of kernel-position
+// offsets.
 constexpr int kLearnBatch = 4;
 
 template <int SR, bool SUB>
@@ -310,20 +347,23 @@ __global__ void __launch_bounds__(256) k_iz_learn_conv_tile(
     const int* __restrict__ to_tss, const int* __restrict__ from_tss, float lr, int stp_flag,
     float max_weight, float* __restrict__ w, float* __restrict__ presyn, float* __restrict__ wd,
     float* __restrict__ stp_r, float* __restrict__ stp_w, IzLut lut) {
+    __shared__ int2 koff[kConvMaxK];
+    conv_offsets(g, K, koff);
+    __syncthreads();
     const int d = blockIdx.x * 32 + (threadIdx.x & 31);
     if (d >= g.to_size) return;
     const float dest_exc_trace = __ldg(to_exc + d);
     const int dest_tss = __ldg(to_tss + d);
     const float dest_spike = extract<SR>(__ldg(dest_out + d), 0);
-    const int kstep = 8 * gridDim.y;
-    for (int k0 = (threadIdx.x >> 5) + blockIdx.y * 8; k0 < K; k0 += kstep * kLearnBatch) {
+    const int2 base = conv_base(g, d);
+    for (int k0 = threadIdx.x >> 5; k0 < K; k0 += 8 * kLearnBatch) {
         LearnVals v[kLearnBatch];
         int src_tss[kLearnBatch];
         bool ok[kLearnBatch];
 #pragma unroll
         for (int b = 0; b < kLearnBatch; ++b) {
-            const int k = k0 + b * kstep;
-            const int from = k < K ? conv_source(g, d, k) : -1;
+            const int k = k0 + 8 * b;
+            const int from = k < K ? conv_source_at(g, base, koff[k]) : -1;
             ok[b] = from >= 0;
             if (ok[b]) {
                 v[b] = iz_learn_load<SUB>((size_t)k * g.to_size + d, stp_flag, w, presyn, wd,
@@ -334,7 +374,7 @@ __global__ void __launch_bounds__(256) k_iz_learn_conv_tile(
 #pragma unroll
         for (int b = 0; b < kLearnBatch; ++b)
             if (ok[b])
-                iz_learn_apply<SUB>((size_t)(k0 + b * kstep) * g.to_size + d, v[b], src_tss[b],
+                iz_learn_apply<SUB>((size_t)(k0 + 8 * b) * g.to_size + d, v[b], src_tss[b],
                                     dest_spike, dest_exc_trace, dest_tss, lr, stp_flag, max_weight,
                                     w, presyn, wd, stp_r, stp_w, lut);
     }
@@ -372,13 +412,20 @@ __global__ void k_iz_gap(DGeom g, const float* __restrict__ voltage, const float
 // Time since the presynaptic spike, per source (CALC_VAL_PREAMBLE,
 // izhikevich_attributes.cpp:257-262).  The reference updates it once per
 // visit in serial order: t = spike ? 0 : min(32, t + 1).  The result depends
-// only on the last visit that saw a spike and on how many visits follow it,
-// so each source scans its last (at most 32) visits backwards.
-// A source whose last visits all read the same delay (uniform[f] >= 0, the
-// usual case) either sees a spike at every one of them (0) or at none.
+// only on the last visit that saw a spike and on how many visits follow it.
+// Every visit with the same delay reads the same spike bit, so a source's
+// last (at most 32) visits are summarised after each upload
+// (k_iz_delay_summary) as, per distinct delay, the position of its last
+// visit: the latest position whose delay shows a spike decides.  A source
+// with more than kSummary distinct delays among those visits scans them.
+//
+// Summary word: bits 0-2 the number of entries (7: scan), entry i in bits
+// 3 + 10 i: delay (5 bits), then position (5 bits).
+constexpr int kSummary = 6;
+
 __global__ void k_iz_time_since_spike(int n_src, const int* __restrict__ counts,
                                       const int* __restrict__ last, const int* __restrict__ delays,
-                                      const int* __restrict__ uniform,
+                                      const unsigned long long* __restrict__ summary,
                                       const uint32_t* __restrict__ src, int src_type,
                                       int* __restrict__ tss) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
@@ -386,17 +433,24 @@ __global__ void k_iz_time_since_spike(int n_src, const int* __restrict__ counts,
     int n = counts[f];
     if (n == 0) return;
     uint32_t word = src[f];
-    const int du = uniform[f];
-    if (du >= 0) {
-        if (extract_rt(word, du, src_type) > 0.0f) {
-            tss[f] = 0;
+    const int m = n < 32 ? n : 32;
+    const unsigned long long sm = summary[f];
+    const int ne = (int)(sm & 7);
+    if (ne != 7) {
+        int best = -1;
+        for (int i = 0; i < ne; ++i) {
+            const int e = (int)(sm >> (3 + 10 * i)) & 1023;
+            const int pos = e >> 5;
+            if (pos > best && extract_rt(word, e & 31, src_type) > 0.0f) best = pos;
+        }
+        if (best >= 0) {
+            tss[f] = m - 1 - best;
         } else {
             const int t = tss[f] + n;
             tss[f] = t < 32 ? t : 32;
         }
         return;
     }
-    int m = n < 32 ? n : 32;
     const int* L = last + (size_t)f * 32;
     for (int j = m - 1; j >= 0; --j) {
         float spike = extract_rt(word, delays[L[j]], src_type);
@@ -405,19 +459,25 @@ __global__ void k_iz_time_since_spike(int n_src, const int* __restrict__ counts,
     int t = tss[f] + n;
     tss[f] = t < 32 ? t : 32;
 }
-
-// The delay shared by all of a source's last (at most 32) visits, or -1.
-__global__ void k_iz_uniform_delay(int n_src, const int* __restrict__ counts,
+__global__ void k_iz_delay_summary(int n_src, const int* __restrict__ counts,
                                    const int* __restrict__ last, const int* __restrict__ delays,
-                                   int* __restrict__ uniform) {
+                                   unsigned long long* __restrict__ summary) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= n_src) return;
     const int m = min(counts[f], 32);
     const int* L = last + (size_t)f * 32;
-    int d = m > 0 ? delays[L[0]] : -1;
-    for (int j = 1; j < m && d >= 0; ++j)
-        if (delays[L[j]] != d) d = -1;
-    uniform[f] = d;
+    unsigned long long sm = 0;
+    unsigned seen = 0;
+    int ne = 0;
+    for (int j = m - 1; j >= 0 && ne <= kSummary; --j) {
+        const int d = delays[L[j]];
+        if (d < 0 || d > 31) { ne = kSummary + 1; break; }
+        if (seen & (1u << d)) continue;
+        seen |= 1u << d;
+        if (ne < kSummary) sm |= (unsigned long long)(d | (j << 5)) << (3 + 10 * ne);
+        ++ne;
+    }
+    summary[f] = ne > kSummary ? 7ull : (sm | (unsigned long long)ne);
 }
 
 // Neuron update (izhikevich_attributes.cpp:102-213).  One launch updates the
@@ -608,8 +668,8 @@ static void iz_delays_and_visits(State& st, ConnState& cs) {
     int nsrc = c.from->size;
     cs.visit_counts = st.add_array("visit counts", 'i', nsrc);
     cs.last_visits = st.add_array("last visits", 'i', (size_t)nsrc * 32);
-    cs.uniform_delay = st.add_array("uniform delay", 'i', nsrc);
-    cs.uniform_delay->scratch = true;
+    cs.delay_summary = st.add_array("delay summary", 'i', 0, LAYOUT_PLAIN, 1, 1, (size_t)nsrc * 2);
+    cs.delay_summary->scratch = true;
     int32_t* cnt = cs.visit_counts->hi();
     int32_t* last = cs.last_visits->hi();
     enumerate_visits(c, [&](int, int, int from, long wi, int, int) {
@@ -636,11 +696,11 @@ class IzhikevichModel : public Model {
     // After every upload (delays may have changed): which sources' last
     // visits share one delay.
     void prepare_device(State&, ConnState& cs, cudaStream_t s) const override {
-        if (!cs.uniform_delay) return;
+        if (!cs.delay_summary) return;
         const int n = cs.conn->from->size;
-        k_iz_uniform_delay<<<blocks_for(n, 256), 256, 0, s>>>(n, cs.visit_counts->di(),
-                                                              cs.last_visits->di(),
-                                                              cs.delays->di(), cs.uniform_delay->di());
+        k_iz_delay_summary<<<blocks_for(n, 256), 256, 0, s>>>(
+            n, cs.visit_counts->di(), cs.last_visits->di(), cs.delays->di(),
+            reinterpret_cast<unsigned long long*>(cs.delay_summary->di()));
         SG_LAUNCH_CHECK();
     }
 
@@ -730,7 +790,7 @@ class IzhikevichModel : public Model {
         // time since spike, from the same (pre-update) source words
         k_iz_time_since_spike<<<blocks_for(c.from->size, 256), 256, 0, ctx.stream>>>(
             c.from->size, cs.visit_counts->di(), cs.last_visits->di(), cs.delays->di(),
-            cs.uniform_delay->di(), src, (int)c.from->output_type,
+            reinterpret_cast<const unsigned long long*>(cs.delay_summary->di()), src, (int)c.from->output_type,
             cs.var("time since spike")->di());
         SG_LAUNCH_CHECK();
         ctx.count();
@@ -843,9 +903,9 @@ class IzhikevichModel : public Model {
         const int threads = 128;
         unsigned blocks = blocks_for(cs.geom.n_dest, threads);
         bool sub = c.opcode == OP_SUB;
-        if (c.type == CONVERGENT) {
+        if (c.type == CONVERGENT && c.arbor.kernel() <= kConvMaxK) {
             const int K = c.arbor.kernel();
-            dim3 grid(blocks_for(c.to->size, 32), std::max(1, (K + 23) / 24));
+            dim3 grid(blocks_for(c.to->size, 32));
             int sr = (int)c.from->output_type;
 #define SG_CONV_LEARN(SRV, SUBV)                                                                  \
     k_iz_learn_conv_tile<SRV, SUBV><<<grid, 256, 0, ctx.stream>>>(                                \
@@ -1063,11 +1123,11 @@ class SpnetModel : public Model {
     OutputType output_type() const override { return OUT_BIT; }
 
     void prepare_device(State&, ConnState& cs, cudaStream_t s) const override {
-        if (!cs.uniform_delay) return;
+        if (!cs.delay_summary) return;
         const int n = cs.conn->from->size;
-        k_iz_uniform_delay<<<blocks_for(n, 256), 256, 0, s>>>(n, cs.visit_counts->di(),
-                                                              cs.last_visits->di(),
-                                                              cs.delays->di(), cs.uniform_delay->di());
+        k_iz_delay_summary<<<blocks_for(n, 256), 256, 0, s>>>(
+            n, cs.visit_counts->di(), cs.last_visits->di(), cs.delays->di(),
+            reinterpret_cast<unsigned long long*>(cs.delay_summary->di()));
         SG_LAUNCH_CHECK();
     }
 
@@ -1104,7 +1164,7 @@ class SpnetModel : public Model {
         const uint32_t* src = st.dev_output(c.from, word_index(c.delay, c.from->output_type));
         k_iz_time_since_spike<<<blocks_for(c.from->size, 256), 256, 0, ctx.stream>>>(
             c.from->size, cs.visit_counts->di(), cs.last_visits->di(), cs.delays->di(),
-            cs.uniform_delay->di(), src, (int)c.from->output_type, cs.var("time since spike")->di());
+            reinterpret_cast<const unsigned long long*>(cs.delay_summary->di()), src, (int)c.from->output_type, cs.var("time since spike")->di());
         SG_LAUNCH_CHECK();
         const unsigned blocks = blocks_for(cs.geom.n_dest, 128);
         float* inputs = input_register(st, cs);

@@ -75,9 +75,9 @@ struct ConnState {
     // weight indices, plus the visit count per source (time-since-spike rule).
     Array* last_visits = nullptr;
     Array* visit_counts = nullptr;
-    // Per source: the delay all of its last visits read, or -1 (device only,
-    // recomputed after every upload).
-    Array* uniform_delay = nullptr;
+    // Per source: a summary of the delays its last visits read (device only,
+    // recomputed after every upload; see k_iz_delay_summary).
+    Array* delay_summary = nullptr;
     // Distances computed for a distance callback, reused by distance-based
     // delays like the reference's cached distances (weight_matrix.cpp:1372-1374).
     std::vector<float> cached_distances;

@@ -172,6 +172,33 @@ int check_wd_strided(unsigned long long stride, unsigned long long offset, Resul
     return 0;
 }
 
+// Every float p with (bits - offset) % stride == 0: (float)((double)p * 0.933).
+int check_product_strided(unsigned long long stride, unsigned long long offset, Result* r) {
+    r->mismatches = r->checked = r->fallbacks = 0;
+    r->first = ~0ull;
+    const float c1 = (float)0.933, c2 = (float)(0.933 - (double)c1);
+#pragma omp parallel
+    {
+        Result l{0, 0, 0, ~0ull};
+#pragma omp for schedule(static)
+        for (long long i = (long long)offset; i < (1ll << 32); i += (long long)stride) {
+            const float p = ffrom((uint32_t)i);
+            float out;
+            ++l.checked;
+            if (!sg::ff::product(p, c1, c2, out)) {
+                ++l.fallbacks;
+                continue;
+            }
+            if (!same(out, (float)((double)p * 0.933))) {
+                ++l.mismatches;
+                if ((unsigned long long)i < l.first) l.first = (unsigned long long)i;
+            }
+        }
+        merge(r, l);
+    }
+    return 0;
+}
+
 // Every float w with (bits - offset) % stride == 0, with and without a spike.
 int check_sw_strided(int sub, int spike, unsigned long long stride, unsigned long long offset,
                      Result* r) {

@@ -76,6 +76,22 @@ __global__ void k_wd_all(Result* r) {
     atomicAdd(&r->fallbacks, fallbacks);
 }
 
+// every float bit pattern: (float)((double)p * 0.933)
+__global__ void k_product_all(Result* r) {
+    const float c1 = (float)0.933, c2 = (float)(0.933 - (double)c1);
+    unsigned long long checked = 0, fallbacks = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+         i < (1ull << 32); i += (unsigned long long)gridDim.x * blockDim.x) {
+        const float p = __uint_as_float((uint32_t)i);
+        float out;
+        ++checked;
+        if (!sg::ff::product(p, c1, c2, out)) { ++fallbacks; continue; }
+        record(r, !same(out, __double2float_rn(__dmul_rn((double)p, 0.933))), i);
+    }
+    atomicAdd(&r->checked, checked);
+    atomicAdd(&r->fallbacks, fallbacks);
+}
+
 template <bool SUB>
 __global__ void k_sw_all(bool spike, Result* r) {
     unsigned long long checked = 0, fallbacks = 0;
@@ -189,6 +205,10 @@ extern "C" {
 
 int check_wd_all(unsigned long long* out) {
     return run([](Result* d) { k_wd_all<<<152 * 8, 256>>>(d); }, out);
+}
+
+int check_product_all(unsigned long long* out) {
+    return run([](Result* d) { k_product_all<<<152 * 8, 256>>>(d); }, out);
 }
 
 int check_sw_all(int sub, int spike, unsigned long long* out) {

@@ -42,6 +42,12 @@ def test_weight_derivative_strided(lib):
     _check(r, 0.6)
 
 
+def test_trace_decay_product_strided(lib):
+    r = Result()
+    lib.check_product_strided(ctypes.c_ulonglong(61), ctypes.c_ulonglong(5), ctypes.byref(r))
+    _check(r, 0.16)       # non-finite and huge operands, results below 2^-126
+
+
 @pytest.mark.parametrize("sub", [0, 1])
 @pytest.mark.parametrize("spike", [0, 1])
 def test_short_term_w_strided(lib, sub, spike):

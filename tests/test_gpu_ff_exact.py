@@ -1,8 +1,8 @@
 """The float-float evaluations of the Izhikevich model's double expressions
 (synaptogenesis_gb300/csrc/ff_exact.cuh) against the same expressions on the
 GPU's FP64 pipe: bit for bit wherever the rounding test accepts, over every
-float bit pattern for the STDP weight derivative without spike terms and for
-short-term w (both opcodes, with and without a source spike), on 2^32
+float bit pattern for the STDP weight derivative without spike terms, the
+presynaptic trace decay product and short-term w (both opcodes, with and without a source spike), on 2^32
 random operand triples with spike terms, and on 2^32 random neuron substeps
 (the voltage derivative, the implicit voltage update and the recovery time
 constant of a threshold-crossing substep).  The test rejects non-finite
@@ -45,6 +45,13 @@ def test_weight_derivative_every_float(lib):
     assert lib.check_wd_all(out) == 0
     assert out[1] == 1 << 32
     _ok(out, 0.12)        # non-finite and |x| >= 2^100 (11%), results below 2^-101
+
+
+def test_trace_decay_product_every_float(lib):
+    out = _out()
+    assert lib.check_product_all(out) == 0
+    assert out[1] == 1 << 32
+    _ok(out, 0.16)        # non-finite and huge operands, results below 2^-126
 
 
 @pytest.mark.parametrize("sub", [0, 1])
