@@ -166,10 +166,12 @@ int sg_version(void);
  * Allocates nothing: its only working memory is a static device array of
  * SG_GOL_NOALLOC_MAX_CELLS words that every GPU loading the library holds until
  * exit.  Boards larger than that are rejected (SG_NOALLOC_ETOOBIG).  The first
- * call on a device looks up that array's device address; make that first call
- * before any stream capture.  All calls share the array, so calls that overlap
- * on the GPU race.  Returns 0, or a negative SG_NOALLOC_* code.  The work is
- * asynchronous on `stream`. */
+ * call on a device (and the first after a cudaDeviceReset gave the device a new
+ * context) looks up that array's device address; make that first call before
+ * any stream capture.  All calls share the array, so calls that overlap on the
+ * GPU race.  Returns 0, or a negative SG_NOALLOC_* code; a launch that fails
+ * returns SG_NOALLOC_ECUDA without touching errors the caller's earlier work
+ * left pending.  The work is asynchronous on `stream`. */
 #define SG_GOL_NOALLOC_MAX_CELLS (1 << 20)
 #define SG_NOALLOC_EINVAL (-1)
 #define SG_NOALLOC_ETOOBIG (-2)

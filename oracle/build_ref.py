@@ -21,8 +21,8 @@ Steps
      (``__GUI__``/``__MPI__`` undefined so their stubs compile in), then link
      ``libsyngen.so``.
 
-The reference checkout is read from ``$SYNGEN_REFERENCE`` (default
-``/root/reference``).  When it is absent but a staged copy already exists in
+The reference checkout is read from ``$SYNGEN_REFERENCE`` (default: a
+``reference`` folder beside this repository's).  When it is absent but a staged copy already exists in
 ``oracle/_ref/src`` (a machine that received the build folder but not the
 checkout), the staged copy is compiled.
 """
@@ -62,7 +62,11 @@ CXXFLAGS = ["-std=c++11", "-O2", "-fopenmp", "-fPIC", "-pthread", "-w",
 
 
 def reference_root():
-    return os.environ.get("SYNGEN_REFERENCE", "/root/reference")
+    """The reference checkout: $SYNGEN_REFERENCE, else a ``reference`` folder
+    beside this repository's."""
+    repo = os.path.dirname(HERE)
+    return os.environ.get("SYNGEN_REFERENCE",
+                          os.path.join(os.path.dirname(repo), "reference"))
 
 
 def stage():

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 
+#include "gol_step.cuh"
 #include "cuda_check.h"
 #include "history.cuh"
 #include "models.h"
@@ -192,18 +193,7 @@ __global__ void __launch_bounds__(256) k_gol_fused(DGeom g, int delay, const uin
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     int r = blockIdx.y * blockDim.y + threadIdx.y;
     if (c >= g.to_cols || r >= g.to_rows) return;
-    int d = r * g.to_cols + c;
-    float sum = 0.0f;
-    for_each_source<T_CONV>(g, d, [&](int from, int wi) {
-        float val = extract<S_BIT>(__ldg(cur + from), delay) * __ldg(w + wi);
-        sum += val;
-    });
-    float input = 0.0f + sum;
-    if (input_out) input_out[d] = input;
-    int n = (int)input;
-    uint32_t word = cur[d];
-    bool live = (word & 1u) ? (n >= smin && n <= smax) : (n >= bmin && n <= bmax);
-    next[d] = (word >> 1) | ((live ? 1u : 0u) << 31);
+    gol_cell_step(g, delay, r, c, cur, next, w, input_out, smin, smax, bmin, bmax);
 }
 
 // Bit-sliced game_of_life step (same semantics as k_gol_fused) for a 3x3

@@ -14,7 +14,7 @@
 #include <mutex>
 
 #include "../../include/syngen.h"
-#include "synapse.cuh"
+#include "gol_step.cuh"
 
 namespace {
 
@@ -24,9 +24,8 @@ namespace {
 // overlap on the GPU share this array and race.
 __device__ __align__(256) uint32_t g_gol_scratch[SG_GOL_NOALLOC_MAX_CELLS];
 
-// One game_of_life step on a toroidal board: sequential weighted count of the
-// neighbours' newest bits (as the base activator sums it, prior 0, "add"),
-// the survival / birth rule on the cell's bit 0, and the history shift.
+// One game_of_life step on a toroidal board (the engine's fused step with
+// delay 0).
 __global__ void __launch_bounds__(256) k_gol_step_noalloc(
     sg::DGeom g, const uint32_t* __restrict__ cur, uint32_t* __restrict__ next,
     const float* __restrict__ w, float* __restrict__ input_out, int smin, int smax, int bmin,
@@ -34,38 +33,60 @@ __global__ void __launch_bounds__(256) k_gol_step_noalloc(
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     int r = blockIdx.y * blockDim.y + threadIdx.y;
     if (c >= g.to_cols || r >= g.to_rows) return;
-    int d = r * g.to_cols + c;
-    float sum = 0.0f;
-    sg::for_each_source<sg::T_CONV>(g, d, [&](int from, int wi) {
-        float val = sg::extract<sg::S_BIT>(__ldg(cur + from), 0) * __ldg(w + wi);
-        sum += val;
+    sg::gol_cell_step(g, 0, r, c, cur, next, w, input_out, smin, smax, bmin, bmax);
+}
+
+// The current context's identity, through the driver entry points the
+// runtime hands out (no link to the driver library): a cudaDeviceReset
+// replaces the device's context, and with it the array's address.
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+
+bool current_context_id(unsigned long long* id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(f);
     });
-    float input = 0.0f + sum;
-    if (input_out) input_out[d] = input;
-    int n = (int)input;
-    uint32_t word = cur[d];
-    bool live = (word & 1u) ? (n >= smin && n <= smax) : (n >= bmin && n <= bmax);
-    next[d] = (word >> 1) | ((live ? 1u : 0u) << 31);
+    void* ctx = nullptr;
+    if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx) return false;
+    return get_id(ctx, id) == 0;
 }
 
 std::mutex g_setup_mutex;
-uint32_t* g_scratch_addr[256] = {nullptr};   // per device ordinal
+struct ScratchAddr {
+    unsigned long long ctx = 0;
+    uint32_t* addr = nullptr;
+};
+ScratchAddr g_scratch_addr[256];   // per device ordinal
 
-// Device address of the scratch array on the current device, looked up once
-// per device (host code cannot use the symbol's name as a device address).
+// Device address of the scratch array on the current device (host code cannot
+// use the symbol's name as a device address).  Looked up once per device
+// context: again after a cudaDeviceReset gave the device a new context.
 uint32_t* scratch_on_current_device() {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return nullptr;
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[dev]) {
+    ScratchAddr& a = g_scratch_addr[dev];
+    unsigned long long ctx = 0;
+    // no current context (none made yet, or reset) also means a new lookup
+    const bool known = current_context_id(&ctx);
+    if (!a.addr || !known || a.ctx != ctx) {
         void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_gol_scratch) != cudaSuccess) {
-            cudaGetLastError();
-            return nullptr;
-        }
-        g_scratch_addr[dev] = static_cast<uint32_t*>(p);
+        if (cudaGetSymbolAddress(&p, g_gol_scratch) != cudaSuccess) return nullptr;
+        a.addr = static_cast<uint32_t*>(p);
+        // the lookup made the device's context current
+        a.ctx = current_context_id(&ctx) ? ctx : 0;
     }
-    return g_scratch_addr[dev];
+    return a.addr;
 }
 
 }  // namespace
@@ -100,17 +121,21 @@ extern "C" int sg_gol_steps_noalloc(unsigned int* words, float* input_out, int r
     dim3 block(32, 8);
     dim3 grid((cols + 31) / 32, (rows + 7) / 8);
     uint32_t* bufs[2] = {reinterpret_cast<uint32_t*>(words), scratch};
+    // each launch's own status (an error the caller's earlier work left
+    // pending is neither read nor cleared here)
     for (int t = 0; t < steps; ++t) {
-        k_gol_step_noalloc<<<grid, block, 0, s>>>(g, bufs[t & 1], bufs[(t + 1) & 1], weights,
-                                                  t == steps - 1 ? input_out : nullptr,
-                                                  survival_min, survival_max, birth_min, birth_max);
+        const uint32_t* cur = bufs[t & 1];
+        uint32_t* next = bufs[(t + 1) & 1];
+        float* in_out = t == steps - 1 ? input_out : nullptr;
+        void* args[] = {&g, &cur, &next, const_cast<float**>(&weights), &in_out, &survival_min,
+                        &survival_max, &birth_min, &birth_max};
+        if (cudaLaunchKernel((const void*)k_gol_step_noalloc, grid, block, args, 0, s) !=
+            cudaSuccess)
+            return SG_NOALLOC_ECUDA;
     }
     if (steps & 1)
         if (cudaMemcpyAsync(words, scratch, (size_t)rows * cols * 4, cudaMemcpyDeviceToDevice, s) !=
-            cudaSuccess) {
-            cudaGetLastError();
+            cudaSuccess)
             return SG_NOALLOC_ECUDA;
-        }
-    if (cudaGetLastError() != cudaSuccess) return SG_NOALLOC_ECUDA;
     return 0;
 }

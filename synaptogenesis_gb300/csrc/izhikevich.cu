@@ -261,7 +261,7 @@ __device__ __forceinline__ int conv_source_at(const DGeom& g, int2 base, int2 of
 constexpr int kConvMaxK = 128;
 
 template <int SR, bool LONG>
-__global__ void __launch_bounds__(256) k_iz_activate_conv_tile(
+__global__ void __launch_bounds__(256, 4) k_iz_activate_conv_tile(
     DGeom g, int K, const uint32_t* __restrict__ src, const float* __restrict__ w,
     const float* __restrict__ stp_r, const float* __restrict__ stp_w, const int* __restrict__ delays,
     float* __restrict__ short_tr, float* __restrict__ long_tr, float gcond, float short_tau,
@@ -334,15 +334,15 @@ __global__ void __launch_bounds__(256) k_iz_activate_conv_tile(
 
 // Updater for non-convolutional convergent connections: one thread per
 // synapse (kernel position, destination), coalesced along destinations.  A
-// CTA owns 32 consecutive destinations; its 8 warps take the kernel
-// positions in turn (warp w: k = w, w+8, ...), kLearnBatch at a time, loading
-// all of their variables before updating any (distinct synapses: no
-// overlap).  Source coordinates come from a per-CTA table of kernel-position
-// offsets.
+// CTA owns 32 consecutive destinations and a share of the kernel positions
+// (grid.y shares of 24); its 8 warps take those positions in turn,
+// kLearnBatch at a time, loading all of their variables before updating any
+// (distinct synapses: no overlap).  Source coordinates come from a per-CTA
+// table of kernel-position offsets.
 constexpr int kLearnBatch = 4;
 
 template <int SR, bool SUB>
-__global__ void __launch_bounds__(256) k_iz_learn_conv_tile(
+__global__ void __launch_bounds__(256, 4) k_iz_learn_conv_tile(
     DGeom g, int K, const uint32_t* __restrict__ dest_out, const float* __restrict__ to_exc,
     const int* __restrict__ to_tss, const int* __restrict__ from_tss, float lr, int stp_flag,
     float max_weight, float* __restrict__ w, float* __restrict__ presyn, float* __restrict__ wd,
@@ -356,13 +356,14 @@ __global__ void __launch_bounds__(256) k_iz_learn_conv_tile(
     const int dest_tss = __ldg(to_tss + d);
     const float dest_spike = extract<SR>(__ldg(dest_out + d), 0);
     const int2 base = conv_base(g, d);
-    for (int k0 = threadIdx.x >> 5; k0 < K; k0 += 8 * kLearnBatch) {
+    const int kstep = 8 * gridDim.y;
+    for (int k0 = (threadIdx.x >> 5) + 8 * blockIdx.y; k0 < K; k0 += kstep * kLearnBatch) {
         LearnVals v[kLearnBatch];
         int src_tss[kLearnBatch];
         bool ok[kLearnBatch];
 #pragma unroll
         for (int b = 0; b < kLearnBatch; ++b) {
-            const int k = k0 + 8 * b;
+            const int k = k0 + kstep * b;
             const int from = k < K ? conv_source_at(g, base, koff[k]) : -1;
             ok[b] = from >= 0;
             if (ok[b]) {
@@ -374,7 +375,7 @@ __global__ void __launch_bounds__(256) k_iz_learn_conv_tile(
 #pragma unroll
         for (int b = 0; b < kLearnBatch; ++b)
             if (ok[b])
-                iz_learn_apply<SUB>((size_t)(k0 + 8 * b) * g.to_size + d, v[b], src_tss[b],
+                iz_learn_apply<SUB>((size_t)(k0 + kstep * b) * g.to_size + d, v[b], src_tss[b],
                                     dest_spike, dest_exc_trace, dest_tss, lr, stp_flag, max_weight,
                                     w, presyn, wd, stp_r, stp_w, lut);
     }
@@ -905,7 +906,7 @@ class IzhikevichModel : public Model {
         bool sub = c.opcode == OP_SUB;
         if (c.type == CONVERGENT && c.arbor.kernel() <= kConvMaxK) {
             const int K = c.arbor.kernel();
-            dim3 grid(blocks_for(c.to->size, 32));
+            dim3 grid(blocks_for(c.to->size, 32), std::max(1, (K + 23) / 24));
             int sr = (int)c.from->output_type;
 #define SG_CONV_LEARN(SRV, SUBV)                                                                  \
     k_iz_learn_conv_tile<SRV, SUBV><<<grid, 256, 0, ctx.stream>>>(                                \
