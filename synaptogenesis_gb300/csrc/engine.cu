@@ -430,6 +430,29 @@ void Engine::enqueue_step(bool last) {
                 for (Layer* l : sp->layers) update_layer(l);
     } else {
     std::vector<Layer*> deferred;
+    {
+        // prologues of the connections whose activation waits on nothing,
+        // grouped by the model of their destination layer
+        std::vector<std::pair<const Model*, std::vector<ConnState*>>> pro;
+        for (auto& lp : net_->layers) {
+            const Model* m = find_model(lp->model);
+            for (Connection* c : lp->inputs) {
+                if (c->second_order_slave || (overlap_ && learn_pending_[c->index]) ||
+                    m->fuses_input(*state_, *c, ctx))
+                    continue;
+                auto it = std::find_if(pro.begin(), pro.end(),
+                                       [&](const auto& p) { return p.first == m; });
+                if (it == pro.end()) {
+                    pro.push_back({m, {}});
+                    it = pro.end() - 1;
+                }
+                it->second.push_back(state_->conn_state(c));
+            }
+        }
+        for (auto& p : pro)
+            timed(std::string(p.first->name()) + ".prologue", 1,
+                  [&] { p.first->activate_prologue(*state_, p.second, ctx); });
+    }
     for (auto& lp : net_->layers) {
         bool waits = false;
         if (overlap_)

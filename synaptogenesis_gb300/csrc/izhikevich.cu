@@ -424,13 +424,12 @@ __global__ void k_iz_gap(DGeom g, const float* __restrict__ voltage, const float
 // 3 + 10 i: delay (5 bits), then position (5 bits).
 constexpr int kSummary = 6;
 
-__global__ void k_iz_time_since_spike(int n_src, const int* __restrict__ counts,
-                                      const int* __restrict__ last, const int* __restrict__ delays,
-                                      const unsigned long long* __restrict__ summary,
-                                      const uint32_t* __restrict__ src, int src_type,
-                                      int* __restrict__ tss) {
-    int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= n_src) return;
+__device__ __forceinline__ void tss_update(int f, const int* __restrict__ counts,
+                                           const int* __restrict__ last,
+                                           const int* __restrict__ delays,
+                                           const unsigned long long* __restrict__ summary,
+                                           const uint32_t* __restrict__ src, int src_type,
+                                           int* __restrict__ tss) {
     int n = counts[f];
     if (n == 0) return;
     uint32_t word = src[f];
@@ -459,6 +458,41 @@ __global__ void k_iz_time_since_spike(int n_src, const int* __restrict__ counts,
     }
     int t = tss[f] + n;
     tss[f] = t < 32 ? t : 32;
+}
+
+__global__ void k_iz_time_since_spike(int n_src, const int* __restrict__ counts,
+                                      const int* __restrict__ last, const int* __restrict__ delays,
+                                      const unsigned long long* __restrict__ summary,
+                                      const uint32_t* __restrict__ src, int src_type,
+                                      int* __restrict__ tss) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_src) return;
+    tss_update(f, counts, last, delays, summary, src, src_type, tss);
+}
+
+// The same for several connections in one launch (their sources concatenated):
+// the connections of a step whose activation waits on nothing.
+struct TssArgs {
+    int n_src, src_type;
+    const int *counts, *last, *delays;
+    const unsigned long long* summary;
+    const uint32_t* src;
+    int* tss;
+};
+constexpr int kTssGroup = 8;
+struct TssGroup {
+    int n;
+    int start[kTssGroup + 1];
+    TssArgs C[kTssGroup];
+};
+
+__global__ void k_iz_time_since_spike_group(TssGroup G) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= G.start[G.n]) return;
+    int c = 0;
+    while (c + 1 < G.n && g >= G.start[c + 1]) ++c;
+    const TssArgs& A = G.C[c];
+    tss_update(g - G.start[c], A.counts, A.last, A.delays, A.summary, A.src, A.src_type, A.tss);
 }
 __global__ void k_iz_delay_summary(int n_src, const int* __restrict__ counts,
                                    const int* __restrict__ last, const int* __restrict__ delays,
@@ -754,6 +788,44 @@ class IzhikevichModel : public Model {
             throw SgError(c.str() + ": Unimplemented connection type!");
     }
 
+    // The time-since-spike updates of trace connections (the ones activate
+    // makes) whose activation waits on nothing, in launches of up to
+    // kTssGroup connections.
+    static bool trace_connection(const Connection& c) {
+        return c.parameter("direct", "false") != "true" &&
+               (c.opcode == OP_ADD || c.opcode == OP_SUB || c.opcode == OP_MULT ||
+                c.opcode == OP_REWARD);
+    }
+    bool activate_prologue(State& st, const std::vector<ConnState*>& conns,
+                           const StepCtx& ctx) const override {
+        std::vector<ConnState*> todo;
+        for (ConnState* cs : conns)
+            if (trace_connection(*cs->conn) && cs->delay_summary) todo.push_back(cs);
+        if (todo.size() < 2) return false;
+        for (size_t first = 0; first < todo.size(); first += kTssGroup) {
+            TssGroup G{};
+            G.n = (int)std::min<size_t>(kTssGroup, todo.size() - first);
+            int total = 0;
+            for (int i = 0; i < G.n; ++i) {
+                ConnState& cs = *todo[first + i];
+                const Connection& c = *cs.conn;
+                G.start[i] = total;
+                G.C[i] = TssArgs{c.from->size, (int)c.from->output_type, cs.visit_counts->di(),
+                                 cs.last_visits->di(), cs.delays->di(),
+                                 reinterpret_cast<const unsigned long long*>(cs.delay_summary->di()),
+                                 st.dev_output(c.from, word_index(c.delay, c.from->output_type)),
+                                 cs.var("time since spike")->di()};
+                total += c.from->size;
+                cs.prologue_done = true;
+            }
+            G.start[G.n] = total;
+            k_iz_time_since_spike_group<<<blocks_for(total, 256), 256, 0, ctx.stream>>>(G);
+            SG_LAUNCH_CHECK();
+            ctx.count();
+        }
+        return true;
+    }
+
     void activate(State& st, ConnState& cs, const StepCtx& ctx) const override {
         Connection& c = *cs.conn;
         LayerState& to = *st.layer_state(c.to);
@@ -788,13 +860,18 @@ class IzhikevichModel : public Model {
             default: throw SgError(c.str() + ": Unimplemented connection type!");
         }
         const uint32_t* src = st.dev_output(c.from, word_index(c.delay, c.from->output_type));
-        // time since spike, from the same (pre-update) source words
-        k_iz_time_since_spike<<<blocks_for(c.from->size, 256), 256, 0, ctx.stream>>>(
-            c.from->size, cs.visit_counts->di(), cs.last_visits->di(), cs.delays->di(),
-            reinterpret_cast<const unsigned long long*>(cs.delay_summary->di()), src, (int)c.from->output_type,
-            cs.var("time since spike")->di());
-        SG_LAUNCH_CHECK();
-        ctx.count();
+        // time since spike, from the same (pre-update) source words, unless
+        // activate_prologue did it with other connections of the step
+        if (cs.prologue_done) {
+            cs.prologue_done = false;
+        } else {
+            k_iz_time_since_spike<<<blocks_for(c.from->size, 256), 256, 0, ctx.stream>>>(
+                c.from->size, cs.visit_counts->di(), cs.last_visits->di(), cs.delays->di(),
+                reinterpret_cast<const unsigned long long*>(cs.delay_summary->di()), src,
+                (int)c.from->output_type, cs.var("time since spike")->di());
+            SG_LAUNCH_CHECK();
+            ctx.count();
+        }
         int serial = c.convolutional ? 1 : 0;
         if (serial) blocks = 1;
         float* sc = to.var(sname)->df();

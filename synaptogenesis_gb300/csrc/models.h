@@ -52,6 +52,14 @@ class Model {
     virtual bool fuses_input(State& st, const Connection& c, const StepCtx& ctx) const {
         return false;
     }
+    // Before a step's synaptic input: work of several of the step's
+    // connections into this model's layers that activate() would otherwise
+    // launch one connection at a time.  A model that takes a connection's
+    // share sets its ConnState::prologue_done (activate() clears it).
+    virtual bool activate_prologue(State& st, const std::vector<ConnState*>& conns,
+                                   const StepCtx& ctx) const {
+        return false;
+    }
     // Start of a step, before any synaptic input: per-layer buffers the
     // reference re-initialises every step (get_init_keys, cluster_node.cpp:46-50).
     virtual void begin_step(State& st, LayerState& ls, const StepCtx& ctx) const {}

@@ -87,6 +87,9 @@ struct ConnState {
     bool device_plan_tried = false;
     // Input register of the dendritic node the connection feeds.
     int reg = 0;
+    // This step's per-connection prologue ran with other connections'
+    // (Model::activate_prologue); the connection's activation clears it.
+    bool prologue_done = false;
     // Second-order host: the per-step copy of its weights that the slaves
     // modulate and the host's activation reads (device only, same layout as
     // the weights; weight_matrix.cpp:79-80).
