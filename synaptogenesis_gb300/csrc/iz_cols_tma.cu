@@ -41,7 +41,7 @@ namespace {
 #define SG_COLS_ROWS 32                  // kR * 8 floats per TMA box row: at most 256
 #endif
 #ifndef SG_COLS_STAGES
-#define SG_COLS_STAGES 8
+#define SG_COLS_STAGES 6
 #endif
 constexpr int kR = SG_COLS_ROWS;         // source rows per chunk
 constexpr int kStages = SG_COLS_STAGES;

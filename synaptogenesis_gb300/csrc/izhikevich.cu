@@ -6,7 +6,9 @@
 // what the reference's optimised build computes.
 #include <cmath>
 #include <cstdlib>
+#include <mutex>
 #include <random>
+#include <set>
 
 #include "cuda_check.h"
 #include "exact_convert.cuh"
@@ -379,6 +381,17 @@ __global__ void __launch_bounds__(256, 4) k_iz_learn_conv_tile(
                                     dest_spike, dest_exc_trace, dest_tss, lr, stp_flag, max_weight,
                                     w, presyn, wd, stp_r, stp_w, lut);
     }
+}
+
+// The largest shared-memory carveout for a kernel that runs beside the
+// TMA activator (which needs it): SMs configured alike can hold both.
+static void prefer_max_shared(const void* fn) {
+    static std::mutex m;
+    static std::set<const void*> done;
+    std::lock_guard<std::mutex> lock(m);
+    if (done.insert(fn).second)
+        SG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     (int)cudaSharedmemCarveoutMaxShared));
 }
 
 // Rows (sources) and columns (destinations) of a fully connected or subset
@@ -986,12 +999,15 @@ class IzhikevichModel : public Model {
             dim3 grid(blocks_for(c.to->size, 32), std::max(1, (K + 23) / 24));
             int sr = (int)c.from->output_type;
 #define SG_CONV_LEARN(SRV, SUBV)                                                                  \
-    k_iz_learn_conv_tile<SRV, SUBV><<<grid, 256, 0, ctx.stream>>>(                                \
-        cs.geom, K, st.dev_output(c.to, 0), to.var("post trace")->df(),                         \
-        to.var("time since spike")->di(), cs.var("time since spike")->di(),                     \
-        cs.params.at("learning rate"), (int)cs.params.at("stp"), c.max_weight,                  \
-        cs.weights->df(), cs.var("presyn trace")->df(), cs.var("weight derivatives")->df(),     \
-        cs.var("short term R")->df(), cs.var("short term w")->df(), lut)
+    do {                                                                                         \
+        prefer_max_shared((const void*)k_iz_learn_conv_tile<SRV, SUBV>);                        \
+        k_iz_learn_conv_tile<SRV, SUBV><<<grid, 256, 0, ctx.stream>>>(                            \
+            cs.geom, K, st.dev_output(c.to, 0), to.var("post trace")->df(),                     \
+            to.var("time since spike")->di(), cs.var("time since spike")->di(),                 \
+            cs.params.at("learning rate"), (int)cs.params.at("stp"), c.max_weight,              \
+            cs.weights->df(), cs.var("presyn trace")->df(), cs.var("weight derivatives")->df(), \
+            cs.var("short term R")->df(), cs.var("short term w")->df(), lut);                   \
+    } while (0)
             if (sub) {
                 if (sr == S_FLOAT) SG_CONV_LEARN(S_FLOAT, true);
                 else if (sr == S_BIT) SG_CONV_LEARN(S_BIT, true);
