@@ -62,6 +62,91 @@ def rng_below(seed, stream, index, n):
     return (rng_bits(seed, stream, index) >> 32) % n
 
 
+def _rng_bits_np(seed, stream, index):
+    """rng_bits over an array of indices (uint64)."""
+    m = (1 << 64) - 1
+    z = (seed * 0x9E3779B97F4A7C15 + stream * 0xD1B54A32D192ED03) & m
+    z = (np.uint64(z) + np.asarray(index, np.uint64))
+    with np.errstate(over="ignore"):
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return z
+
+
+RNG_NOISE, RNG_NOISE_RATE = 6, 7
+F32 = np.float32
+
+
+def rng_open01(seed, stream, index):
+    """Uniform draws in (0, 1): (24 random bits + 1) times the float nearest
+    1 / (2^24 + 1)."""
+    bits = _rng_bits_np(seed, stream, index) >> np.uint64(40)
+    return (bits + np.uint64(1)).astype(np.float32) * F32(1.0 / 16777217.0)
+
+
+def noise_log(x):
+    """log x for x in (0, 1], float32 step by step: x = m 2^e, m in
+    [sqrt(1/2), sqrt(2)), log m = 2 atanh((m - 1) / (m + 1)) by its series to
+    the ninth power."""
+    x = np.asarray(x, np.float32)
+    u = x.view(np.uint32)
+    e = ((u >> np.uint32(23)) & np.uint32(0xFF)).astype(np.int32) - 127
+    m = ((u & np.uint32(0x7FFFFF)) | np.uint32(0x3F800000)).view(np.float32)
+    big = m > F32(1.41421354)
+    m = np.where(big, m * F32(0.5), m).astype(np.float32)
+    e = np.where(big, e + 1, e)
+    s = (m - F32(1.0)) / (m + F32(1.0))
+    z = s * s
+    p = F32(0.222222224) * z + F32(0.285714298)
+    p = p * z + F32(0.400000006)
+    p = p * z + F32(0.666666687)
+    p = p * z + F32(2.0)
+    return s * p + e.astype(np.float32) * F32(0.693147182)
+
+
+def noise_cospi(x):
+    """cos(pi x) for x in [0, 2], float32: folded onto [0, 1/4], then the
+    Taylor series of cos (to t^10) or sin (to t^9)."""
+    x = np.asarray(x, np.float32)
+    x = np.where(x > F32(1.0), F32(2.0) - x, x).astype(np.float32)
+    neg = x > F32(0.5)
+    x = np.where(neg, F32(1.0) - x, x).astype(np.float32)
+    sign = np.where(neg, F32(-1.0), F32(1.0)).astype(np.float32)
+    t = (F32(0.5) - x) * F32(3.14159274)
+    z = t * t
+    p = F32(2.75573188e-06) * z - F32(1.98412701e-04)
+    p = p * z + F32(8.33333377e-03)
+    p = p * z - F32(0.166666672)
+    p = p * z + F32(1.0)
+    r_sin = t * p
+    t = x * F32(3.14159274)
+    z = t * t
+    p = F32(-2.75573188e-07) * z + F32(2.48015876e-05)
+    p = p * z - F32(1.38888892e-03)
+    p = p * z + F32(4.16666679e-02)
+    p = p * z - F32(0.5)
+    r_cos = p * z + F32(1.0)
+    return sign * np.where(x > F32(0.25), r_sin, r_cos).astype(np.float32)
+
+
+def noise_draw(kind, seed, step, n, a, b, rates=None):
+    """One step of init-config noise for n neurons (the library's k_noise):
+    kind "uniform" (min a, max b), "normal" (mean a, std b), "poisson"
+    (probability a or per-neuron rates; value b, returned as a mask and b)."""
+    idx = (np.uint64(step) << np.uint64(32)) | np.arange(n, dtype=np.uint64)
+    u = rng_open01(seed, RNG_NOISE * 4, idx)
+    a, b = F32(a), F32(b)
+    if kind == "uniform":
+        return u * (b - a) + a
+    if kind == "normal":
+        u2 = rng_open01(seed, RNG_NOISE * 4 + 1, idx)
+        normal = np.sqrt(F32(-2.0) * noise_log(u)) * noise_cospi(F32(2.0) * u2)
+        return normal * b + a
+    prob = rates if rates is not None else a
+    return u < prob
+
+
 def rng_uniform(seed, stream, index):
     """Counter-based uniform draw in [0, 1) (SplitMix64 finaliser of a
     linear mix of seed, stream and index), as the library's generators use."""
@@ -725,6 +810,46 @@ class OracleNetwork:
             raise ValueError("BIT delays cannot be greater than 31")
         return delays
 
+    # -- init-config noise (instruction.h:200-282, kernel.cpp:42-158) --------
+    def _noise_seed(self, l):
+        init = l.p.child("init config")
+        if init.has("seed"):
+            return int(init.get("seed"))
+        return (GLOBAL_SEED ^ (0xA5A5 * (self.layers.index(l) + 1))) & ((1 << 64) - 1)
+
+    def _noise(self, l, init, kind, reg0, is_input):
+        """The layer's noise of this step, drawn like the library's
+        counter-based generator from (seed, the layer's step, neuron);
+        overwrites a layer without input, adds onto an input layer's."""
+        if not hasattr(self, "noise_step"):
+            self.noise_step = {}
+        t = self.noise_step.get(l.name, 0)
+        seed = self._noise_seed(l)
+        if kind == "uniform":
+            v = noise_draw(kind, seed, t, l.size, init.get_float("min", 0.0),
+                           init.get_float("max", 1.0))
+        elif kind == "normal":
+            v = noise_draw(kind, seed, t, l.size, init.get_float("mean", 1.0),
+                           init.get_float("std dev", 0.1))
+        else:
+            rate = np.float32(0.001) * np.float32(init.get_float("rate", 1.0))
+            rates = None
+            if init.get("random", "false") == "true":
+                rates = rng_uniform(seed, RNG_NOISE_RATE, np.arange(l.size)) * rate
+            fire = noise_draw(kind, seed, t, l.size, rate, 0.0, rates)
+            value = np.float32(init.get_float("value", 20.0))
+            if is_input:
+                reg0[fire] += value
+            else:
+                reg0[:] = np.where(fire, value, np.float32(0.0))
+            self.noise_step[l.name] = t + 1
+            return
+        if is_input:
+            reg0 += v
+        else:
+            reg0[:] = v
+        self.noise_step[l.name] = t + 1
+
     # -- accessors mirroring the reference's getters -------------------------
     def layer(self, name):
         return self._find(name, None)
@@ -785,13 +910,17 @@ class OracleNetwork:
             if is_input:
                 reg0[:] = np.asarray(inputs[l.name], np.float32)
             if init is not None:
-                if init.get("type", "normal") != "flat":
-                    raise ValueError("oracle: only flat init configs are restated")
-                v = np.float32(init.get_float("value", 1.0))
-                if is_input:
-                    reg0 += v
+                kind = init.get("type", "normal")
+                if kind == "flat":
+                    v = np.float32(init.get_float("value", 1.0))
+                    if is_input:
+                        reg0 += v
+                    else:
+                        reg0[:] = v
+                elif kind in ("uniform", "normal", "poisson"):
+                    self._noise(l, init, kind, reg0, is_input)
                 else:
-                    reg0[:] = v
+                    raise ValueError("Unrecognized init type: " + kind)
             elif not is_input:
                 reg0[:] = 0.0
         if not self.order:

@@ -1,3 +1,4 @@
+#include "counter_rng.h"
 #include "engine.h"
 #include "iz_cols_tma.cuh"
 
@@ -40,49 +41,53 @@ static cudaStream_t engine_side_stream() {
 
 // ---------------------------------------------------------------------------
 // Input-register initialisation (engine/kernel/kernel.cpp:14-158).  Noise is
-// drawn from a seeded counter-based generator keyed by (seed, step, neuron);
-// the step comes from a device counter so captured graphs stay valid.
+// drawn from the seeded counter-based generator (counter_rng.h), keyed by
+// (seed, step, neuron); the step is the layer's own counter in the state.
 // ---------------------------------------------------------------------------
 __global__ void k_set_value(float* p, int n, float v, int overwrite) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) p[i] = overwrite ? v : p[i] + v;
 }
 
-__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
-    x += 0x9E3779B97F4A7C15ULL;
-    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
-    x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
-    return x ^ (x >> 31);
-}
-
-__device__ __forceinline__ float uniform01(unsigned long long seed, long long step, int i, int draw) {
-    unsigned long long h =
-        mix64(seed ^ mix64((unsigned long long)step * 0x100000001B3ULL + draw) ^ ((unsigned long long)i << 20));
-    return ((h >> 40) + 1) * (1.0f / 16777217.0f);   // (0, 1)
-}
-
-// kind 0 uniform(a, b), 1 normal(mean a, std b), 2 poisson(probability a, value b)
+// kind 0 uniform(a, b), 1 normal(mean a, std b), 2 Poisson (probability a, or
+// rates[i] when given; value b).  Overwrite for a layer without input, add
+// onto an input layer's input (kernel.cpp:42-158).  Every thread reads the
+// step from ctr[0]; the last block to finish advances it (ctr[1] counts the
+// finished blocks), so one launch per step keeps graphs valid.
 __global__ void k_noise(float* p, int n, int kind, float a, float b, int overwrite,
-                        unsigned long long seed, const long long* step) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    long long t = *step;
-    float u = uniform01(seed, t, i, 0);
-    float v;
-    if (kind == 0) {
-        v = u * (b - a) + a;
-    } else if (kind == 1) {
-        float u2 = uniform01(seed, t, i, 1);
-        v = sqrtf(-2.0f * logf(u)) * cospif(2.0f * u2) * b + a;
-    } else {
-        if (overwrite) { p[i] = u < a ? b : 0.0f; return; }
-        if (u < a) p[i] += b;
-        return;
+                        unsigned long long seed, unsigned long long* ctr,
+                        const float* __restrict__ rates) {
+    const unsigned long long t = *(volatile unsigned long long*)ctr;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const unsigned long long idx = (t << 32) | (unsigned)i;
+        const float u = rng_open01(seed, RNG_NOISE * 4 + 0, idx);
+        if (kind == 2) {
+            const float prob = rates ? rates[i] : a;
+            if (overwrite) p[i] = u < prob ? b : 0.0f;
+            else if (u < prob) p[i] += b;
+        } else {
+            float v;
+            if (kind == 0) {
+                v = (u * (b - a)) + a;
+            } else {
+                const float u2 = rng_open01(seed, RNG_NOISE * 4 + 1, idx);
+                v = (noise_normal(u, u2) * b) + a;
+            }
+            p[i] = overwrite ? v : p[i] + v;
+        }
     }
-    p[i] = overwrite ? v : p[i] + v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(ctr + 1, 1ull) == (unsigned long long)gridDim.x - 1) {
+            ctr[0] = t + 1;
+            ctr[1] = 0;
+            __threadfence();
+        }
+    }
 }
 
-__global__ void k_step_counter(long long* step) { *step += 1; }
 
 // ---------------------------------------------------------------------------
 Engine::Engine(Network* net, Environment* env, State* state, const Props& args)
@@ -136,10 +141,6 @@ Engine::Engine(Network* net, Environment* env, State* state, const Props& args)
         graph_steps_ = std::max(2, args.get_int("graph steps", 16) / 2 * 2);
         build_modules();
         if (!modules_.empty()) use_graphs_ = false;
-        for (auto& lp : net_->layers) {
-            Props* init = lp->config.child("init config");
-            if (init && init->get("type", "normal") != "flat") step_counter_ = true;
-        }
         // dendritic trees: activation order, and the internal registers set
         // to their init values (cluster_node.cpp:116-129; second-order nodes
         // and the root are not set)
@@ -183,14 +184,11 @@ Engine::Engine(Network* net, Environment* env, State* state, const Props& args)
             SG_CUDA(cudaMallocHost(&h, (size_t)l->size * 4));
             out_pinned_.push_back((uint32_t*)h);
         }
-        SG_CUDA(cudaMalloc(&d_step_, sizeof(long long)));
-        SG_CUDA(cudaMemsetAsync(d_step_, 0, sizeof(long long), stream_));
         SG_CUDA(cudaStreamSynchronize(stream_));
     } catch (...) {
         for (float* p : in_pinned_) cudaFreeHost(p);
         for (float* p : in_staging_) cudaFree(p);
         for (uint32_t* p : out_pinned_) cudaFreeHost(p);
-        if (d_step_) cudaFree(d_step_);
         running = false;
         throw;
     }
@@ -209,7 +207,6 @@ Engine::~Engine() {
     for (float* p : in_pinned_) cudaFreeHost(p);
     for (float* p : in_staging_) cudaFree(p);
     for (uint32_t* p : out_pinned_) cudaFreeHost(p);
-    if (d_step_) cudaFree(d_step_);
     for (auto& g : graphs_) cudaGraphExecDestroy(g.exec);
     for (auto& kv : prof_)
         for (auto& e : kv.second.events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
@@ -319,24 +316,31 @@ void Engine::enqueue_step(bool last) {
         if (init) {
             std::string t = init->get("type", "normal");
             int ow = is_input ? 0 : 1;
-            unsigned long long seed = init->has("seed") ? std::stoull(init->get("seed"))
-                                                        : (global_seed() ^ (0xA5A5ULL * (l->index + 1)));
+            const unsigned long long seed = noise_seed(*l);
             unsigned blocks = blocks_for(l->size, 256);
+            unsigned long long* ctr = nullptr;
+            const float* rates = nullptr;
+            if (t != "flat") {
+                ctr = reinterpret_cast<unsigned long long*>(ls->internal.at("noise step")->du());
+                auto r = ls->internal.find("noise rates");
+                if (r != ls->internal.end()) rates = r->second->df();
+            }
             timed("init", 1, [&] {
                 if (t == "flat") {
                     k_set_value<<<blocks, 256, 0, stream_>>>(in, l->size, init->get_float("value", 1.0f), ow);
                 } else if (t == "uniform") {
                     k_noise<<<blocks, 256, 0, stream_>>>(in, l->size, 0, init->get_float("min", 0.0f),
-                                                         init->get_float("max", 1.0f), ow, seed, d_step_);
+                                                         init->get_float("max", 1.0f), ow, seed, ctr,
+                                                         nullptr);
                 } else if (t == "normal") {
                     k_noise<<<blocks, 256, 0, stream_>>>(in, l->size, 1, init->get_float("mean", 1.0f),
-                                                         init->get_float("std dev", 0.1f), ow, seed, d_step_);
+                                                         init->get_float("std dev", 0.1f), ow, seed, ctr,
+                                                         nullptr);
                 } else if (t == "poisson") {
-                    if (init->get_bool("random", false))
-                        throw SgError("random per-neuron Poisson rates are not supported");
                     k_noise<<<blocks, 256, 0, stream_>>>(in, l->size, 2,
                                                          0.001f * init->get_float("rate", 1.0f),
-                                                         init->get_float("value", 20.0f), ow, seed, d_step_);
+                                                         init->get_float("value", 20.0f), ow, seed, ctr,
+                                                         rates);
                 } else {
                     throw SgError("Error building cluster node for " + l->str() +
                                   ":\n  Unrecognized init type: " + t);
@@ -522,11 +526,6 @@ void Engine::enqueue_step(bool last) {
                     }
                 }
         }
-    }
-    if (step_counter_) {
-        k_step_counter<<<1, 1, 0, stream_>>>(d_step_);
-        SG_LAUNCH_CHECK();
-        ++launches_;
     }
 }
 

@@ -117,7 +117,6 @@ class Engine {
     std::vector<float*> in_pinned_, in_staging_;
     std::vector<char> in_dirty_;
     std::vector<uint32_t*> out_pinned_;
-    long long* d_step_ = nullptr;        // device step counter (noise generators)
     struct Graph {
         std::vector<void*> sig;          // output buffers the graph was captured with
         cudaGraphExec_t exec = nullptr;
@@ -125,7 +124,6 @@ class Engine {
     };
     std::vector<Graph> graphs_;          // one per ping-pong placement
     int graph_steps_ = 16;               // steps per captured graph (even)
-    bool step_counter_ = false;          // a noise generator reads the step counter
     bool alone_ = false;                 // every layer advances whole runs on its own
     bool ordered_ = false;               // a sequential or feedforward structure sets the step order
     long launches_ = 0, steps_ = 0;

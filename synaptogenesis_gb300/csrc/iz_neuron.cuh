@@ -102,7 +102,7 @@ __device__ __forceinline__ void iz_integrate_ff(float& voltage, float& recovery,
     const float rd = 1.0f / d1;
     for (int i = 0; (i < 10) && (voltage < 30.0f); ++i) {
         float current = -ampa_c * voltage;
-        float q = (voltage + 80) / 60;
+        float q = ff::div_int<60>(voltage + 80);
         float temp = q * q;
         current -= nmda_c * (temp / (1 + temp)) * voltage;
         current -= gabaa_c * (voltage + 70);

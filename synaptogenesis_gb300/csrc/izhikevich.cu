@@ -145,7 +145,7 @@ __device__ __forceinline__ void iz_learn_apply(size_t wi, const LearnVals& v, in
         // Without a source spike, R = 1 and w = U are fixed points: the
         // increments are +0.0 and the stored values would not change.
         if (src_spike || r != 1.0f || !isfinite(sw))
-            stp_r[wi] = r + (((1 - r) / D) - (r * sw * src_spike));
+            stp_r[wi] = r + (ff::div_int<D>(1 - r) - (r * sw * src_spike));
         if (src_spike || !(U == (double)(float)U && sw == (float)U)) {
             // stp_w += (U - sw) / F + U * (1 - sw) * src_spike
             float nsw;

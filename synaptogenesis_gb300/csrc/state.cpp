@@ -1,3 +1,4 @@
+#include "counter_rng.h"
 #include "state.h"
 #include "iz_cols_tma.cuh"
 
@@ -107,6 +108,12 @@ Array* State::add_array(const std::string& name, char dtype, size_t count, Array
     return arrays_.back().get();
 }
 
+uint64_t noise_seed(const Layer& l) {
+    Props* init = l.config.child("init config");
+    return (init && init->has("seed")) ? std::stoull(init->get("seed"))
+                                       : (global_seed() ^ (0xA5A5ULL * (uint64_t)(l.index + 1)));
+}
+
 void State::build() {
     // a sparse connection is compacted anew from this state's weights
     for (auto& cp : network->connections) {
@@ -126,6 +133,23 @@ void State::build() {
         // (attributes.cpp:21-26); get_neuron_data("input") returns them all
         ls->input = add_array("input", 'f', (size_t)l->registers * l->size);
         ls->output = add_array("output", 'u', (size_t)l->history() * l->size);
+        // init-config noise: the layer's step counter and dispatch ticket
+        // (two 64-bit words, kept with the state so that a later run continues
+        // the draws) and the per-neuron Poisson rates of "random": rates
+        // uniform in [0, rate) like the reference's fRand
+        // (instruction.h:255-268), drawn from the layer's noise seed
+        if (Props* init = l->config.child("init config")) {
+            const std::string t = init->get("type", "normal");
+            if (t != "flat") ls->internal["noise step"] = add_array("noise step", 'i', 4);
+            if (t == "poisson" && init->get_bool("random", false)) {
+                Array* rates = add_array("noise rates", 'f', l->size);
+                const float rate = 0.001f * init->get_float("rate", 1.0f);
+                const uint64_t seed = noise_seed(*l);
+                for (int i = 0; i < l->size; ++i)
+                    rates->hf()[i] = rng_uniform(seed, RNG_NOISE_RATE, (uint64_t)i) * rate;
+                ls->internal["noise rates"] = rates;
+            }
+        }
         find_model(l->model)->build_layer(*this, *ls);
         layers.push_back(std::move(ls));
     }

@@ -163,6 +163,10 @@ void launch_transpose(const uint32_t* in, uint32_t* out, int rows, int cols, cud
 
 DGeom make_geom(const Connection& c);
 
+// Seed of a layer's init-config noise: its "seed", else derived from the
+// global seed and the layer's index.
+uint64_t noise_seed(const Layer& l);
+
 // Serial-order enumeration of a connection's visits, host layout weight
 // indices: f(row, to_index, from_index, weight_index, pre_wrap_row, pre_wrap_col).
 // Shared by the index/distance/delay initialisers and the visit tables.

@@ -199,6 +199,29 @@ int check_product_strided(unsigned long long stride, unsigned long long offset, 
     return 0;
 }
 
+// Every float a with (bits - offset) % stride == 0: div_int<D>(a) == a / D.
+int check_div_strided(int D, unsigned long long stride, unsigned long long offset, Result* r) {
+    r->mismatches = r->checked = r->fallbacks = 0;
+    r->first = ~0ull;
+#pragma omp parallel
+    {
+        Result l{0, 0, 0, ~0ull};
+#pragma omp for schedule(static)
+        for (long long i = (long long)offset; i < (1ll << 32); i += (long long)stride) {
+            const float a = ffrom((uint32_t)i);
+            const float got = D == 60 ? sg::ff::div_int<60>(a)
+                              : D == 700 ? sg::ff::div_int<700>(a) : sg::ff::div_int<800>(a);
+            ++l.checked;
+            if (!same(got, a / (float)D)) {
+                ++l.mismatches;
+                if ((unsigned long long)i < l.first) l.first = (unsigned long long)i;
+            }
+        }
+        merge(r, l);
+    }
+    return 0;
+}
+
 // Every float w with (bits - offset) % stride == 0, with and without a spike.
 int check_sw_strided(int sub, int spike, unsigned long long stride, unsigned long long offset,
                      Result* r) {

@@ -92,6 +92,19 @@ __global__ void k_product_all(Result* r) {
     atomicAdd(&r->fallbacks, fallbacks);
 }
 
+// every float bit pattern: div_int<D>(a) == a / D (IEEE)
+template <int D>
+__global__ void k_div_all(Result* r) {
+    unsigned long long checked = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+         i < (1ull << 32); i += (unsigned long long)gridDim.x * blockDim.x) {
+        const float a = __uint_as_float((uint32_t)i);
+        ++checked;
+        record(r, !same(sg::ff::div_int<D>(a), __fdiv_rn(a, (float)D)), i);
+    }
+    atomicAdd(&r->checked, checked);
+}
+
 template <bool SUB>
 __global__ void k_sw_all(bool spike, Result* r) {
     unsigned long long checked = 0, fallbacks = 0;
@@ -209,6 +222,13 @@ int check_wd_all(unsigned long long* out) {
 
 int check_product_all(unsigned long long* out) {
     return run([](Result* d) { k_product_all<<<152 * 8, 256>>>(d); }, out);
+}
+
+int check_div_all(int D, unsigned long long* out) {
+    if (D == 60) return run([](Result* d) { k_div_all<60><<<152 * 8, 256>>>(d); }, out);
+    if (D == 700) return run([](Result* d) { k_div_all<700><<<152 * 8, 256>>>(d); }, out);
+    if (D == 800) return run([](Result* d) { k_div_all<800><<<152 * 8, 256>>>(d); }, out);
+    return 1;
 }
 
 int check_sw_all(int sub, int spike, unsigned long long* out) {

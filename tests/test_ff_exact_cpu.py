@@ -48,6 +48,13 @@ def test_trace_decay_product_strided(lib):
     _check(r, 0.16)       # non-finite and huge operands, results below 2^-126
 
 
+@pytest.mark.parametrize("divisor", [60, 700, 800])
+def test_division_by_integer_strided(lib, divisor):
+    r = Result()
+    lib.check_div_strided(divisor, ctypes.c_ulonglong(61), ctypes.c_ulonglong(3), ctypes.byref(r))
+    _check(r, 0.0)
+
+
 @pytest.mark.parametrize("sub", [0, 1])
 @pytest.mark.parametrize("spike", [0, 1])
 def test_short_term_w_strided(lib, sub, spike):

@@ -2,7 +2,8 @@
 (synaptogenesis_gb300/csrc/ff_exact.cuh) against the same expressions on the
 GPU's FP64 pipe: bit for bit wherever the rounding test accepts, over every
 float bit pattern for the STDP weight derivative without spike terms, the
-presynaptic trace decay product and short-term w (both opcodes, with and without a source spike), on 2^32
+presynaptic trace decay product, the float divisions by the integer
+constants 60, 700 and 800 (reciprocal and one correction) and short-term w (both opcodes, with and without a source spike), on 2^32
 random operand triples with spike terms, and on 2^32 random neuron substeps
 (the voltage derivative, the implicit voltage update and the recovery time
 constant of a threshold-crossing substep).  The test rejects non-finite
@@ -52,6 +53,14 @@ def test_trace_decay_product_every_float(lib):
     assert lib.check_product_all(out) == 0
     assert out[1] == 1 << 32
     _ok(out, 0.16)        # non-finite and huge operands, results below 2^-126
+
+
+@pytest.mark.parametrize("divisor", [60, 700, 800])
+def test_division_by_integer_every_float(lib, divisor):
+    out = _out()
+    assert lib.check_div_all(divisor, out) == 0
+    assert out[1] == 1 << 32
+    assert out[0] == 0, "mismatch at %#x" % out[3]
 
 
 @pytest.mark.parametrize("sub", [0, 1])
