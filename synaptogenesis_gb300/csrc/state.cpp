@@ -361,15 +361,25 @@ void State::load(const std::string& path) {
     for (;;) {
         size_t key[3];
         if (!f.read(reinterpret_cast<char*>(key), sizeof(key))) break;
-        Array* target = nullptr;
+        // records are matched on (owner, variable) like the reference's
+        // PointerKey; ones this state does not hold (a transposed weight
+        // copy, distances, sparse index arrays) are skipped, as the
+        // reference skips unknown ones
+        const Rec* target = nullptr;
         for (auto& r : recs)
-            if (r.hash == key[0] && r.type == key[1] && r.bytes == key[2]) target = r.arr;
-        if (target) {
-            if (!f.read(reinterpret_cast<char*>(target->host.data()), key[2]))
-                throw SgError("Error reading data from file!");
-        } else {
+            if (r.hash == key[0] && r.type == key[1]) target = &r;
+        if (!target) {
             f.ignore(key[2]);
+            continue;
         }
+        // the reference resizes such an array (sparse matrices); every array
+        // here has the size its network fixes
+        if (target->bytes != key[2])
+            throw SgError("State record '" + target->arr->name + "' holds " +
+                          std::to_string(key[2]) + " bytes; the network's array has " +
+                          std::to_string(target->bytes));
+        if (!f.read(reinterpret_cast<char*>(target->arr->host.data()), key[2]))
+            throw SgError("Error reading data from file!");
     }
     on_host_ = true;
 }

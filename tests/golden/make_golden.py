@@ -155,9 +155,31 @@ def scale_fixture(sg, name):
 SCALE = ("c0_1000", "c1_10000", "c2_1000")
 
 
+def state_fixture(name):
+    """``<case>_state<steps>``: the state file the reference saves after
+    running the case for that many steps (bytes), for the GPU test that
+    continues it here."""
+    import subprocess
+    import tempfile
+    case, steps = name.rsplit("_state", 1)
+    with tempfile.TemporaryDirectory() as d:
+        state, dumped = os.path.join(d, "s.state"), os.path.join(d, "s.npz")
+        env = dict(os.environ, OMP_NUM_THREADS="1")
+        subprocess.run([sys.executable, os.path.join(HERE, "ref_state.py"), "save", case, steps,
+                        state, dumped], env=env, check=True)
+        with open(state, "rb") as f:
+            return {"state": np.frombuffer(f.read(), np.uint8)}
+
+
 def main(names):
     sg = load_reference_syngen()
     for name in names or sorted(CASES):
+        if "_state" in name:
+            out = state_fixture(name)
+            path = os.path.join(HERE, name + ".npz")
+            np.savez_compressed(path, **out)
+            print("wrote", path)
+            continue
         if name in SCALE:
             out = scale_fixture(sg, name)
             path = os.path.join(HERE, name + ".npz")

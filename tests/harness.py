@@ -119,14 +119,18 @@ def run_oracle_digest(case, steps, checkpoints=()):
     return out
 
 
-def run_library(case, syngen, steps=None, extra_args=None):
+def run_library(case, syngen, steps=None, extra_args=None, state_file=None, start=0):
     """Runs ``case`` through the drop-in front-end ``syngen`` (either library);
-    ``extra_args`` are added to the run arguments."""
+    ``extra_args`` are added to the run arguments.  With ``state_file`` the
+    network starts from that saved state (in place of the injections) and
+    takes the case's inputs from step ``start`` on."""
     from tests.golden.cases import callback_injections
     steps = case.steps if steps is None else steps
     sizes = case_sizes(case)
     net_dict, injections, weight_arrays, delay_arrays = callback_injections(
         case.net, case.injections(sizes))
+    if state_file is not None:
+        net_dict, injections = case.net, {}
 
     def weight_cb(ID, size, weights):
         syngen.FloatArray(size, weights).to_np_array()[:] = weight_arrays[ID]
@@ -138,6 +142,8 @@ def run_library(case, syngen, steps=None, extra_args=None):
     syngen.create_delay_weight_callback("golden_delay", delay_cb)
     net = syngen.Network(net_dict)
     net.build_state()
+    if state_file is not None:
+        net.load_state(state_file)
     for key, arr in injections.items():
         if key[0] == "neuron":
             dst = net.get_neuron_data(key[1], key[2], key[3]).to_np_array()
@@ -145,7 +151,7 @@ def run_library(case, syngen, steps=None, extra_args=None):
             dst = net.get_weight_matrix(key[1], key[2]).to_np_array()
         assert dst.size == arr.size, (key, dst.size, arr.size)
         dst.view(arr.dtype)[:] = arr
-    inputs = case.input_arrays(sizes, steps)
+    inputs = case.input_arrays(sizes, start + steps)[start:]
     step = {"in": 0}
     in_layers = sorted(case.inputs)
     rec = {k: [] for k in case.record}

@@ -120,3 +120,22 @@ def test_cases_without_environment(syngen, name, graphs):
                        float_keys=("neuron/d/rtree/output", "neuron/p/sdiv/output"),
                        nan_keys=float_like_keys(case))
     assert not problems, problems
+
+
+def test_reference_state_continues_here(syngen, tmp_path):
+    """State interchange on the GPU: the plastic case's state saved by the
+    reference's library after 75 of the fixture's 150 steps (a state file in
+    the reference's record format), loaded here and run for the remaining 75
+    steps, gives the reference's spike records of those steps and its final
+    state, bit for bit."""
+    import numpy as np
+    from tests.harness import GOLDEN
+    case = CASES["iz_plastic"]
+    with np.load(GOLDEN + "/iz_plastic_state75.npz") as z:
+        path = tmp_path / "reference.state"
+        path.write_bytes(z["state"].tobytes())
+    got = run_library(case, syngen, steps=75, state_file=str(path), start=75)
+    want = load_fixture("iz_plastic")
+    want = {k: (v[75:] if k.startswith("rec/") else v) for k, v in want.items()}
+    problems = compare(got, want, nan_keys=float_like_keys(case))
+    assert not problems, problems
