@@ -62,7 +62,7 @@ def build(force=False, verbose=False):
         objs = list(ex.map(one, _sources()))
     newest = max(os.path.getmtime(o) for o in objs)
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
-        cmd = ["g++", "-shared", "-o", LIB] + objs + [
+        cmd = ["g++", "-shared", "-Wl,-soname,libsyngen.so", "-o", LIB] + objs + [
             "-L" + os.path.join(CUDA, "lib64"), "-lcudart", "-Wl,-rpath," + os.path.join(CUDA, "lib64")]
         subprocess.run(cmd, check=True)
     return LIB
