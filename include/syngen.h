@@ -150,6 +150,14 @@ void sg_set_seed(unsigned long long seed);
 /* ABI version of this header. */
 int sg_version(void);
 
+/* Testing hook, no counterpart in the reference: from now on the TMA
+ * activator of fully connected / subset Izhikevich connections issues no
+ * loads for chunk `chunk` of its source rows (-1: back to normal), so that its
+ * consumers' bounded wait runs out and the run reports the timeout as an
+ * error.  The state of a network run meanwhile is not meaningful.  Returns
+ * false on a CUDA error. */
+bool sg_test_cols_skip_chunk(int chunk);
+
 /* Allocation-free game_of_life stepping.  No counterpart in the reference.
  *
  * For callers that cannot call cudaMalloc: a host program whose device memory

@@ -41,7 +41,7 @@ MODELS = {"izhikevich": BIT, "relay": FLOAT, "game_of_life": BIT, "rate_encoding
           "hebbian_rate_encoding": FLOAT, "perceptron": FLOAT, "sine generator": FLOAT,
           "poisson generator": BIT, "spnet": BIT, "oscillator": FLOAT, "som": FLOAT,
           "nvm": FLOAT, "nvm_heaviside": FLOAT, "nvm_compare": FLOAT, "vp_max": FLOAT,
-          "sample": FLOAT}
+          "sample": FLOAT, "debug": FLOAT}
 GLOBAL_SEED = 0x5EED5EED     # the library's default sg_set_seed value
 # Which sine the reference's sine generator evaluates: its unqualified
 # sin(float) resolves to the C library's double sin (pinned by the fixture).
@@ -339,7 +339,7 @@ class Conn:
         self.randomized = p.get_bool("randomized projection", False)
         if self.sparse and self.second_order:
             raise ValueError("Sparse second order connections are not supported!")
-        if self.randomized and (self.convolutional or self.type in (0, 1, 4)):
+        if self.randomized and (self.convolutional or self.type in (0, 1)):
             raise ValueError("Cannot randomize projection on this weight matrix!")
         c = _Conn()
         c.type, c.opcode, c.convolutional = self.type, self.opcode, int(self.convolutional)
@@ -419,6 +419,49 @@ class Conn:
         self.rows = rows.value
         self.nvisits = n
 
+    def _randomized_divergent(self, seed, n):
+        """weight_matrix.cpp:443-504: the inverted convergent connection
+        (layers swapped, same arborized config) randomized -- each source's
+        window shifted so its first position is a random destination, indexed
+        with the destination layer's row count as the row pitch -- and
+        adjusted (wrapped or clipped), then every kept pair flipped into the
+        divergent matrix at the destination's next free position."""
+        c = self.c
+        S, D = self.frm, self.to
+        K = c.row_field * c.col_field
+        fr = np.full(n, -1, np.int64)
+        fc = np.full(n, -1, np.int64)
+        fi = np.full(n, -1, np.int64)
+        tr = np.full(n, -1, np.int64)
+        tc = np.full(n, -1, np.int64)
+        used = np.zeros(n, bool)
+        count = np.zeros(D.size, np.int64)
+        for s in range(S.size):
+            sr, sc = divmod(s, S.cols)
+            r0 = sr * c.row_stride + c.row_spacing * c.row_offset
+            c0 = sc * c.col_stride + c.col_spacing * c.col_offset
+            nr = rng_below(seed, 2 * s, 0, D.rows)
+            nc = rng_below(seed, 2 * s + 1, 0, D.cols)
+            for kr in range(c.row_field):
+                for kc in range(c.col_field):
+                    r = nr + kr * c.row_spacing
+                    q = nc + kc * c.col_spacing
+                    idx = r * D.rows + q
+                    if c.wrap:
+                        r, q = r % D.rows, q % D.cols
+                        idx = r * D.cols + q
+                    elif r < 0 or r >= D.rows or q < 0 or q >= D.cols:
+                        continue
+                    if idx < 0 or idx >= D.size:
+                        raise ValueError("randomized projection indexes outside the layer")
+                    slot = count[idx]
+                    count[idx] += 1
+                    if slot >= K:
+                        raise ValueError("randomized divergent projection: more than K sources")
+                    j = idx * K + slot
+                    fr[j], fc[j], fi[j], tr[j], tc[j], used[j] = sr, sc, s, r, q, True
+        return fr, fc, fi, tr, tc, used
+
     def sparsify(self, w):
         """WeightMatrix::sparsify + adjust_sparse_indices (weight_matrix.cpp:
         510-651, 253-338): keeps each matrix row's nonzero synapses, in order,
@@ -441,10 +484,12 @@ class Conn:
         tr[wi], tc[wi] = dst_of_visit // self.to.cols, dst_of_visit % self.to.cols
         used[wi] = True
         fi = np.where(used, fr * self.frm.cols + fc, -1)
-        if self.randomized:   # weight_matrix.cpp:377-437, seeded draws
-            wc = self.p.child("weight config")
-            seed = int(wc.get("seed")) if (wc is not None and wc.has("seed")) else \
-                GLOBAL_SEED ^ ((0xA11CE5 * (self.index + 1)) & ((1 << 64) - 1))
+        wc = self.p.child("weight config")
+        seed = int(wc.get("seed")) if (wc is not None and wc.has("seed")) else \
+            GLOBAL_SEED ^ ((0xA11CE5 * (self.index + 1)) & ((1 << 64) - 1))
+        if self.randomized and self.type == 4:
+            fr, fc, fi, tr, tc, used = self._randomized_divergent(seed, n_dense)
+        elif self.randomized:   # weight_matrix.cpp:377-437, seeded draws
             for d in range(self.to.size):
                 nr = rng_below(seed, 2 * d, 0, self.frm.rows)
                 nc = rng_below(seed, 2 * d + 1, 0, self.frm.cols)
@@ -638,6 +683,8 @@ class OracleNetwork:
                 st["error deltas"] = np.zeros(l.size, np.float32)
             if l.model == "sample":
                 st["neuron_var"] = np.zeros(l.size, np.float32)
+            elif l.model == "debug":   # debug_attributes.cpp:140-146: DUMMY_VAL
+                st["neuron_var"] = np.ones(l.size, np.float32)
             elif l.model == "perceptron":
                 st["expected"] = np.zeros(l.size, np.float32)
             elif l.model == "oscillator":   # oscillator_attributes.cpp:12-22
@@ -1013,6 +1060,8 @@ class OracleNetwork:
         return out[w * c.frm.size:(w + 1) * c.frm.size]
 
     def _activate(self, L, c):
+        if c.to.model == "debug":   # debug activators only check indices
+            return
         st, m = self.neuron[c.to], self.matrix[c]
         src = self._src_words(c)
         geo = (c.rows, _p(c.dst), _p(c.ptr), _p(c.from_idx), _p(c.w_idx))

@@ -665,6 +665,7 @@ void Engine::synchronize() {
     join_side();
     SG_CUDA(cudaStreamSynchronize(stream_));
     check_iz_cols_errors();
+    check_debug_errors();
 }
 
 Props* Engine::report() {

@@ -13,6 +13,7 @@
 #include "callbacks.h"
 #include "cuda_check.h"
 #include "engine.h"
+#include "iz_cols_tma.cuh"
 #include "models.h"
 #include "weight_init.h"
 
@@ -322,5 +323,12 @@ void sg_engine_destroy(SG_ENGINE eng) {
 void sg_set_seed(unsigned long long seed) { set_global_seed(seed); }
 
 int sg_version(void) { return SG_ABI_VERSION; }
+
+bool sg_test_cols_skip_chunk(int chunk) {
+    SG_TRY(false)
+    set_iz_cols_skip_chunk(chunk);
+    return true;
+    SG_CATCH(false)
+}
 
 }  // extern "C"

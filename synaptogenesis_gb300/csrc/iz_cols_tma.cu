@@ -73,6 +73,9 @@ struct ColsParams {
 };
 
 __device__ int g_cols_error = 0;
+// Testing hook (sg_test_cols_skip_chunk): the producer issues no load for this
+// chunk, so the consumers' bounded wait for it runs out; -1 in normal use.
+__device__ int g_cols_skip_chunk = -1;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -184,7 +187,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (tid >= kProducer) {
         // ---- producer warp: loads into free stages, stores of finished ones
         if (tid == kProducer) {
+            const int skip = g_cols_skip_chunk;
             auto issue = [&](int ch) {
+                if (ch == skip) return;
                 const int s = ch % kStages;
                 const uint32_t bar = smem_u32(&full[s]);
                 // the full box is counted, rows past the end included (zero-filled)
@@ -439,6 +444,10 @@ void launch_iz_cols_tma(const IzColsPlan& plan, const DGeom& g, int src_type, bo
     else if (src_type == S_FLOAT) { SG_COLS(S_FLOAT) }
     else { SG_COLS(S_INT) }
 #undef SG_COLS
+}
+
+void set_iz_cols_skip_chunk(int chunk) {
+    SG_CUDA(cudaMemcpyToSymbol(g_cols_skip_chunk, &chunk, sizeof(int)));
 }
 
 void check_iz_cols_errors() {

@@ -31,5 +31,8 @@ void launch_iz_cols_tma(const IzColsPlan& plan, const DGeom& g, int src_type, bo
 // Throws if a pipeline wait of the kernel ran out (reads a device flag; call
 // after the stream has synchronised).
 void check_iz_cols_errors();
+// Testing hook: the producer skips the loads of chunk `chunk` of every launch
+// (-1: none), so that a bounded wait runs out and the error path is taken.
+void set_iz_cols_skip_chunk(int chunk);
 
 }  // namespace sg

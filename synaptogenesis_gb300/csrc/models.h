@@ -92,6 +92,10 @@ const Model* find_model(const std::string& name);
 bool register_model(const Model* m);
 std::vector<std::string> model_names();
 
+// Failed checks of the debug model's kernels since the last call, as an error
+// (debug_model.cu).
+void check_debug_errors();
+
 // Register in the model's translation unit: SG_REGISTER_MODEL(MyModel);
 #define SG_REGISTER_MODEL(CLS) \
     static const bool sg_registered_##CLS = ::sg::register_model(new CLS())

@@ -381,8 +381,6 @@ void Network::add_connection(const Props& p) {
         if (c->type == SUBSET)
             throw SgError("Error intializing weight matrix for " + c->str() +
                           "\n   Cannot randomize projection on subset weight matrix!");
-        if (c->type == DIVERGENT)
-            throw SgError(c->str() + ": randomized divergent projections are not supported");
     }
     c->dense_type = c->type;
     c->dense_num_weights = c->num_weights;

@@ -286,6 +286,7 @@ void State::to_host(cudaStream_t stream) {
     if (on_host_) return;
     SG_CUDA(cudaStreamSynchronize(stream));
     check_iz_cols_errors();
+    check_debug_errors();
     for (auto& a : arrays_) {
         if (a->dev_count == 0 || a->scratch) continue;
         const size_t n = std::min(a->dev_count, a->count);

@@ -243,6 +243,77 @@ void init_weights(State& st, ConnState& cs) {
     if (!cfg.get_bool("diagonal", true)) clear_diagonal(c, w);
 }
 
+// Seed of a randomized projection's draws: the weight config's "seed", else
+// derived from the global seed and the connection's index (the reference's
+// generator is unseeded).
+static uint64_t randomized_seed(const Connection& c) {
+    const Props* wc = c.config.child("weight config");
+    return (wc && wc->has("seed")) ? std::stoull(wc->get("seed"))
+                                   : (g_seed ^ (0xA11CE5ULL * (uint64_t)(c.index + 1)));
+}
+
+// Randomized divergent projection (weight_matrix.cpp:443-504): the inverted,
+// convergent connection (destination and source layers swapped, the same
+// arborized config; Connection::invert, connection.cpp:108-124) is built and
+// randomized as a convergent one -- each source's field shifted so that its
+// first position lands on a random destination (seeded draws), indexed with
+// the destination layer's row count as the row pitch -- and its indices are
+// adjusted (wrapped, or positions outside the layer dropped); then every kept
+// (source, destination) pair is flipped into the divergent matrix, in the
+// inverse's order, at the destination's next free position.  Where a
+// destination would receive more sources than the kernel has positions the
+// reference writes past that destination's row; that is refused here, as is
+// a pitch-quirk index outside the destination layer.  (The reference also
+// drops the inverse's zero weights, drawn from the same weight config and
+// unseeded; here every kept pair of the inverse is flipped.)
+static Indices randomized_divergent(const Connection& c, uint64_t seed) {
+    const Layer& S = *c.from;
+    const Layer& D = *c.to;
+    const Arbor& a = c.arbor;
+    const int K = a.kernel();
+    const size_t n = (size_t)D.size * K;
+    Indices ix;
+    ix.from_row.assign(n, -1); ix.from_col.assign(n, -1); ix.from_index.assign(n, -1);
+    ix.to_row.assign(n, -1); ix.to_col.assign(n, -1); ix.to_index.assign(n, -1);
+    ix.used.assign(n, 0);
+    std::vector<int> count(D.size, 0);
+    for (int s = 0; s < S.size; ++s) {
+        const int sr = s / S.cols, sc = s % S.cols;
+        // the inverse's window of s in D starts at s * stride + spacing * offset
+        const int r0 = sr * a.row_stride + a.row_spacing * a.row_offset;
+        const int c0 = sc * a.col_stride + a.col_spacing * a.col_offset;
+        const int nr = (int)rng_below(seed, 2 * (uint64_t)s, 0, (uint32_t)D.rows);
+        const int nc = (int)rng_below(seed, 2 * (uint64_t)s + 1, 0, (uint32_t)D.cols);
+        for (int kr = 0; kr < a.row_field; ++kr)
+            for (int kc = 0; kc < a.col_field; ++kc) {
+                int r = r0 + kr * a.row_spacing + (nr - r0);
+                int q = c0 + kc * a.col_spacing + (nc - c0);
+                int idx = r * D.rows + q;
+                if (a.wrap) {
+                    r = (r % D.rows + D.rows) % D.rows;
+                    q = (q % D.cols + D.cols) % D.cols;
+                    idx = r * D.cols + q;
+                } else if (r < 0 || r >= D.rows || q < 0 || q >= D.cols) {
+                    continue;
+                }
+                if (idx < 0 || idx >= D.size)
+                    throw SgError(c.str() + ": randomized projection indexes outside the "
+                                  "destination layer (the row pitch is its row count; use a "
+                                  "square layer)");
+                const int slot = count[idx]++;
+                if (slot >= K)
+                    throw SgError(c.str() + ": randomized divergent projection gives destination " +
+                                  std::to_string(idx) + " more than " + std::to_string(K) +
+                                  " sources");
+                const size_t j = (size_t)idx * K + slot;
+                ix.from_row[j] = sr; ix.from_col[j] = sc; ix.from_index[j] = s;
+                ix.to_row[j] = r; ix.to_col[j] = q; ix.to_index[j] = idx;
+                ix.used[j] = 1;
+            }
+    }
+    return ix;
+}
+
 // ---------------------------------------------------------------------------
 // WeightMatrix::sparsify and adjust_sparse_indices (weight_matrix.cpp:510-651,
 // 253-338), run when the dense weights (and any callback delays or
@@ -257,16 +328,16 @@ void sparsify(State& st, ConnState& cs) {
     const float* w = cs.weights->hf();
     Indices ix = compute_indices(c);
     const int frows = c.from->rows, fcols = c.from->cols;
-    if (c.randomized) {
+    if (c.randomized && c.type == DIVERGENT) {
+        ix = randomized_divergent(c, randomized_seed(c));
+    } else if (c.randomized) {
         // randomize_projection (weight_matrix.cpp:377-437), with seeded draws
         // (the reference's generator is unseeded): one to one takes a random
         // source per destination; convergent shifts each destination's field
         // so that its first position lands on a random source, and -- as the
         // reference -- indexes the shifted sources with the source layer's
         // row count as the row pitch.
-        const Props* wc = c.config.child("weight config");
-        const uint64_t seed = (wc && wc->has("seed")) ? std::stoull(wc->get("seed"))
-                                                      : (g_seed ^ (0xA11CE5ULL * (uint64_t)(c.index + 1)));
+        const uint64_t seed = randomized_seed(c);
         for (int d = 0; d < to_size; ++d) {
             const int nr = (int)rng_below(seed, 2 * (uint64_t)d, 0, (uint32_t)frows);
             const int nc = (int)rng_below(seed, 2 * (uint64_t)d + 1, 0, (uint32_t)fcols);

@@ -785,4 +785,47 @@ def cases():
     return out
 
 
-CASES = {c.name: c for c in cases()}
+def _debug_case():
+    """The debug model (a checker): every connection type into debug layers,
+    plastic ones too, and a relay layer reading a debug layer.  Its layers'
+    outputs stay zero and its neuron variable the dummy value."""
+    net = {"structures": [{"name": "g", "type": "parallel", "layers": [
+        _layer("src", "relay", 6, 8),
+        _layer("d", "debug", 6, 8),
+        _layer("e", "debug", 4, 5),
+        _layer("out", "relay", 6, 8)]}],
+        "connections": [
+            {"name": "g_fc", "from layer": "src", "to layer": "e", "type": "fully connected",
+             "plastic": True, "opcode": "add"},
+            {"name": "g_sub", "from layer": "src", "to layer": "e", "type": "subset", "opcode": "add",
+             "plastic": True,
+             "subset config": {"from row start": 1, "from row end": 4, "from column start": 2,
+                               "from column end": 6, "to row start": 0, "to row end": 2,
+                               "to column start": 1, "to column end": 4}},
+            {"name": "g_one", "from layer": "src", "to layer": "d", "type": "one to one",
+             "plastic": False, "opcode": "add"},
+            {"name": "g_conv", "from layer": "src", "to layer": "d", "type": "convergent",
+             "plastic": True, "opcode": "add", "arborized config": {"field size": 3, "wrap": True}},
+            {"name": "g_conv_clip", "from layer": "src", "to layer": "d", "type": "convergent",
+             "plastic": False, "opcode": "add",
+             "arborized config": {"field size": 3, "wrap": False}},
+            {"name": "g_cnv", "from layer": "src", "to layer": "d", "type": "convergent",
+             "convolutional": True, "plastic": True, "opcode": "add",
+             "arborized config": {"field size": 3, "wrap": True}},
+            {"name": "g_div", "from layer": "e", "to layer": "d", "type": "divergent",
+             "plastic": True, "opcode": "add", "arborized config": {"field size": 3, "stride": 2}},
+            {"name": "g_read", "from layer": "d", "to layer": "out", "type": "one to one",
+             "plastic": False, "opcode": "add"}]}
+
+    def inj(rng, sizes):
+        return {("matrix", c, "weights"): rng.uniform(-1, 1, sizes["conn:" + c]).astype(np.float32)
+                for c in ("g_fc", "g_sub", "g_one", "g_conv", "g_conv_clip", "g_cnv", "g_div",
+                          "g_read")}
+    return Case("debug", net, 10, 151, inject=inj,
+                inputs={"src": lambda rng, t, n: rng.normal(0.0, 1.0, n)},
+                record=[("g", "d"), ("g", "e"), ("g", "out")],
+                final=[("neuron", "g", l, k) for l in ("d", "e") for k in ("neuron_var", "input")]
+                + [("neuron", "g", "out", "input")])
+
+
+CASES = {c.name: c for c in cases() + [_debug_case()]}

@@ -61,14 +61,39 @@ def test_perceptron_learning_is_refused(syngen):
 
 
 def test_randomized_projection_matches_oracle(syngen):
-    """Randomized one-to-one and convergent projections (seeded draws,
-    clipped and wrapping fields, relay and Izhikevich targets): bit-exact
-    against the oracle's restatement of the same draws and compaction."""
+    """Randomized one-to-one, convergent and divergent projections (seeded
+    draws, clipped and wrapping fields, relay and Izhikevich targets):
+    bit-exact against the oracle's restatement of the same draws and
+    compaction."""
     from tests.test_host_cpu import _randomized_net
     case = Case("randomized", _randomized_net(), 40, 9,
-                inputs={"a": lambda rng, t, n: rng.normal(0.0, 5.0, n)},
+                inputs={"a": lambda rng, t, n: rng.normal(0.0, 5.0, n),
+                        "c": lambda rng, t, n: rng.normal(0.0, 5.0, n)},
                 record=[("s", "b"), ("s", "iz")],
                 final=[("neuron", "s", "b", "input"), ("neuron", "s", "iz", "voltage")])
     got = run_library(case, syngen)
     want = run_oracle(case)
     assert not compare(got, want, nan_keys={"rec/s/b", "neuron/s/b/input", "neuron/s/iz/voltage"})
+
+
+def test_debug_model_reports_failed_checks(syngen):
+    """The debug model's checks (device asserts in the reference) count
+    failures on the device; the host reports them as the run's error, and the
+    next run, with the dummy value restored, succeeds."""
+    from tests.golden.cases import CASES
+    case = CASES["debug"]
+    net = syngen.Network(case.net)
+    net.build_state()
+    env = syngen.Environment({"modules": []})
+    rep = net.run(env, {"iterations": 3})
+    assert rep is not None and rep.obj is not None, syngen.last_error()
+    var = net.get_neuron_data("g", "d", "neuron_var").to_np_array()
+    assert np.all(var == 1.0)
+    var[5] = 2.0
+    rep = net.run(env, {"iterations": 2})
+    assert rep is None or rep.obj is None
+    assert "neuron_var differs" in syngen.last_error() and "index 5" in syngen.last_error()
+    var = net.get_neuron_data("g", "d", "neuron_var").to_np_array()
+    var[5] = 1.0
+    rep = net.run(env, {"iterations": 2})
+    assert rep is not None and rep.obj is not None, syngen.last_error()

@@ -96,12 +96,13 @@ def test_sparse_compaction_matches_oracle(sg):
 
 
 def _randomized_net():
-    """A one-to-one and two convergent randomized projections (relay and
+    """One-to-one, convergent and divergent randomized projections (relay and
     Izhikevich targets, clipped and wrapping fields), seeded."""
     return {"structures": [{"name": "s", "layers": [
         {"name": "a", "neural model": "relay", "rows": 6, "columns": 6},
         {"name": "b", "neural model": "relay", "rows": 6, "columns": 6},
-        {"name": "iz", "neural model": "izhikevich", "rows": 6, "columns": 6}]}],
+        {"name": "iz", "neural model": "izhikevich", "rows": 6, "columns": 6},
+        {"name": "c", "neural model": "relay", "rows": 3, "columns": 3}]}],
         "connections": [
             {"name": "r1", "from layer": "a", "to layer": "b", "type": "one to one",
              "randomized projection": True, "plastic": False,
@@ -113,7 +114,15 @@ def _randomized_net():
             {"name": "r3", "from layer": "a", "to layer": "iz", "type": "convergent",
              "randomized projection": True, "plastic": False,
              "arborized config": {"field size": 3, "wrap": True},
-             "weight config": {"type": "flat", "weight": 0.5, "seed": 7}}]}
+             "weight config": {"type": "flat", "weight": 0.5, "seed": 7}},
+            {"name": "r4", "from layer": "c", "to layer": "b", "type": "divergent",
+             "randomized projection": True, "plastic": False,
+             "arborized config": {"field size": 3, "stride": 2, "wrap": True},
+             "weight config": {"type": "flat", "weight": 0.75, "seed": 8}},
+            {"name": "r5", "from layer": "c", "to layer": "iz", "type": "divergent",
+             "randomized projection": True, "plastic": False,
+             "arborized config": {"field size": 3, "stride": 2, "wrap": False},
+             "weight config": {"type": "flat", "weight": 0.5, "seed": 9}}]}
 
 
 def test_randomized_projection_state_matches_oracle(sg):
@@ -413,3 +422,20 @@ def test_state_save_load_roundtrip(sg, tmp_path):
     m.build_state(path)
     assert np.array_equal(m.get_neuron_data("s", "e", "voltage").to_np_array(), v)
     assert np.array_equal(m.get_weight_matrix("p_ee").to_np_array(), w)
+
+
+def test_randomized_divergent_overflow_is_refused(sg):
+    """A randomized divergent projection whose flipped pairs give a
+    destination more sources than the kernel has positions (where the
+    reference writes past that destination's row) is refused at build."""
+    net = {"structures": [{"name": "s", "layers": [
+        {"name": "a", "neural model": "relay", "rows": 8, "columns": 8},
+        {"name": "b", "neural model": "relay", "rows": 8, "columns": 8}]}],
+        "connections": [{"name": "d", "from layer": "a", "to layer": "b", "type": "divergent",
+                         "randomized projection": True, "plastic": False,
+                         "arborized config": {"field size": 3, "stride": 1, "wrap": True},
+                         "weight config": {"type": "flat", "weight": 1.0, "seed": 1}}]}
+    n = sg.Network(net)
+    n.build_state()
+    assert not n.state
+    assert "more than 9 sources" in sg.last_error()
