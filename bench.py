@@ -46,6 +46,11 @@ FALLBACK_HBM_GBS = 6800.0
 # ---------------------------------------------------------------------------
 # Workloads (synthetic, seeded)
 # ---------------------------------------------------------------------------
+# Timesteps per launch of the whole-run game_of_life kernel (the library's
+# default, or its SG_GOL_STEPS_PER_LAUNCH override).
+GOL_STEPS_PER_LAUNCH = int(os.environ.get("SG_GOL_STEPS_PER_LAUNCH", "12"))
+
+
 def gol_workload(side=2048):
     import numpy as np
     net = {"structures": [{"name": "g", "type": "parallel", "layers": [
@@ -74,15 +79,16 @@ def gol_workload(side=2048):
         "units_per_timestep": 9 * n,
         "unit": "synapse-updates/s",
         "dtype": "u32",
-        # Whole runs on bit planes: one launch advances 16 timesteps; per
-        # timestep and cell a step reads the newest and the oldest history bit
-        # and writes one new bit (3 bits); the word layout would move 8 B.
-        "kernel": "k_gol_planes_steps (16 timesteps per launch)",
+        # Whole runs on bit planes: one launch advances GOL_STEPS_PER_LAUNCH
+        # timesteps; per timestep and cell a step reads the newest and the
+        # oldest history bit and writes one new bit (3 bits); the word layout
+        # would move 8 B.
+        "kernel": "k_gol_strips_steps (%d timesteps per launch)" % GOL_STEPS_PER_LAUNCH,
         "profile_group": "game_of_life.advance",
-        "steps_per_launch": 16,
+        "steps_per_launch": GOL_STEPS_PER_LAUNCH,
         "timestep_bytes": 3 * n // 8,
         "word_layout_timestep_bytes": 8 * n,
-        "bytes_per_launch": 16 * 3 * n // 8,
+        "bytes_per_launch": GOL_STEPS_PER_LAUNCH * 3 * n // 8,
         "state_bytes": 8 * n + 36,           # input + output + weights moved per e2e step
         "cpu_seconds": 12.0,
         "learning": False,

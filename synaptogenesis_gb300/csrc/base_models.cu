@@ -575,6 +575,287 @@ __global__ void __launch_bounds__(kPlaneThreads) k_gol_planes_steps(int rows, in
     }
 }
 
+// ---------------------------------------------------------------------------
+// game_of_life on bit planes, full-width strips: boards whose rows are 32, 64
+// or 128 words (1024, 2048 or 4096 cells) wide, counting the 8 outer cells or
+// all 9 cells of the 3x3 block.
+//
+// A CTA advances K steps (K <= 31) of a band of ty board rows plus K halo rows
+// above and below, one band per SM.  Each warp holds R consecutive band rows
+// across the whole width in registers -- lane l holds words l*WPL .. l*WPL +
+// WPL - 1 of a row -- so the wrap across the width is a lane rotation, and the
+// words west and east of a lane's run come from shuffles.  Per row a warp
+// keeps the bit-sliced horizontal sums of each cell's three-cell row (ones s3,
+// twos c3) and, for the 8-cell count, of the two cells beside it (s2, c2); a
+// new row is the sum of the row above's and below's (s3, c3) with its own
+// (s2, c2): six three-input logic operations per word with the B3/S23 rule,
+// and six more for the new row's sums.  Warps hand their top and bottom rows'
+// (s3, c3) to the warps above and below through shared memory, double
+// buffered, with one barrier per step.  The plane holding the cells' oldest
+// bits is copied (cp.async) into a shared-memory ring kStripDepth steps ahead.
+// Rows outside the tile are recomputed halo: after step s only band rows
+// within K - 1 - s of the tile must be right, and a warp whose rows all lie
+// outside that range stops computing.  Consecutive launches are programmatic
+// dependents, so that one is scheduled while the previous one drains.
+// Band rows per warp: 2 for rows of 32 or 64 words (up to 32 warps, so that
+// enough warps stay busy while the band shrinks), 4 for 128-word rows (up to
+// 16 warps, registers permitting).
+__host__ __device__ constexpr int strip_rows(int wpl) { return wpl >= 4 ? 4 : 2; }
+__host__ __device__ constexpr int strip_max_warps(int rpw) { return rpw >= 4 ? 16 : 32; }
+constexpr int kStripDepth = 4;       // steps ahead the oldest-bit plane is copied
+
+template <int WPL>
+__device__ __forceinline__ void strip_ld(const uint32_t* p, uint32_t (&v)[WPL]) {
+    if constexpr (WPL == 4) {
+        const uint4 t = __ldcg(reinterpret_cast<const uint4*>(p));
+        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    } else if constexpr (WPL == 2) {
+        const uint2 t = __ldcg(reinterpret_cast<const uint2*>(p));
+        v[0] = t.x; v[1] = t.y;
+    } else {
+        v[0] = __ldcg(p);
+    }
+}
+
+template <int WPL>
+__device__ __forceinline__ void strip_cp_async(uint32_t* dst, const uint32_t* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(
+                     (unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src), "n"(4 * WPL)
+                 : "memory");
+}
+
+template <int WPL>
+__device__ __forceinline__ void strip_lds(const uint32_t* p, uint32_t (&v)[WPL]) {
+    if constexpr (WPL == 4) {
+        const uint4 t = *reinterpret_cast<const uint4*>(p);
+        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    } else if constexpr (WPL == 2) {
+        const uint2 t = *reinterpret_cast<const uint2*>(p);
+        v[0] = t.x; v[1] = t.y;
+    } else {
+        v[0] = *p;
+    }
+}
+
+template <int WPL>
+__device__ __forceinline__ void strip_st(uint32_t* p, const uint32_t (&v)[WPL]) {
+    if constexpr (WPL == 4) __stcg(reinterpret_cast<uint4*>(p), make_uint4(v[0], v[1], v[2], v[3]));
+    else if constexpr (WPL == 2) __stcg(reinterpret_cast<uint2*>(p), make_uint2(v[0], v[1]));
+    else __stcg(p, v[0]);
+}
+
+// One exchange slot of a lane: N = 2 * WPL words, s3 then c3.
+template <int N>
+__device__ __forceinline__ void xch_put(uint32_t* p, const uint32_t (&t)[N]) {
+    if constexpr (N % 4 == 0) {
+#pragma unroll
+        for (int k = 0; k < N; k += 4)
+            reinterpret_cast<uint4*>(p)[k / 4] = make_uint4(t[k], t[k + 1], t[k + 2], t[k + 3]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < N; k += 2) reinterpret_cast<uint2*>(p)[k / 2] = make_uint2(t[k], t[k + 1]);
+    }
+}
+
+template <int N>
+__device__ __forceinline__ void xch_get(const uint32_t* p, uint32_t (&t)[N]) {
+    if constexpr (N % 4 == 0) {
+#pragma unroll
+        for (int k = 0; k < N; k += 4) {
+            const uint4 u = reinterpret_cast<const uint4*>(p)[k / 4];
+            t[k] = u.x; t[k + 1] = u.y; t[k + 2] = u.z; t[k + 3] = u.w;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < N; k += 2) {
+            const uint2 u = reinterpret_cast<const uint2*>(p)[k / 2];
+            t[k] = u.x; t[k + 1] = u.y;
+        }
+    }
+}
+
+template <int WPL>
+struct StripRow {
+    uint32_t s3[WPL], c3[WPL], s2[WPL], c2[WPL];
+};
+
+// Horizontal sums of one row held across the warp.
+template <int MODE, int WPL>
+__device__ __forceinline__ void strip_sums(const uint32_t (&v)[WPL], int lane, StripRow<WPL>& r) {
+    const uint32_t wi = __shfl_sync(0xFFFFFFFFu, v[WPL - 1], (lane + 31) & 31);
+    const uint32_t ei = __shfl_sync(0xFFFFFFFFu, v[0], (lane + 1) & 31);
+#pragma unroll
+    for (int j = 0; j < WPL; ++j) {
+        const uint32_t west = j == 0 ? wi : v[j > 0 ? j - 1 : 0];
+        const uint32_t east = j == WPL - 1 ? ei : v[j < WPL - 1 ? j + 1 : 0];
+        const uint32_t a = __funnelshift_l(west, v[j], 1);   // west neighbours: (v << 1) | (west >> 31)
+        const uint32_t b = __funnelshift_r(v[j], east, 1);   // east neighbours: (v >> 1) | (east << 31)
+        r.s3[j] = a ^ v[j] ^ b;
+        r.c3[j] = maj3(a, v[j], b);
+        if (MODE == 1) {
+            r.s2[j] = a ^ b;
+            r.c2[j] = a & b;
+        }
+    }
+}
+
+template <int MODE, bool CONWAY, int WPL, int R>
+__global__ void __launch_bounds__(strip_max_warps(R) * 32) k_gol_strips_steps(
+    int rows, int ty, long long T0, int K, uint32_t* __restrict__ planes, unsigned smask,
+    unsigned bmask) {
+    constexpr int W = 32 * WPL, XN = 2 * WPL;
+    extern __shared__ uint4 strip_smem[];
+    // [2][warps + 2][2][32][XN]: warp w publishes in slot w + 1; slots 0 and
+    // warps + 1 stay zero (nothing above the first warp or below the last)
+    uint32_t* xch = reinterpret_cast<uint32_t*>(strip_smem);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const size_t slots = (size_t)(nw + 2) * 2 * 32 * XN;       // words of one buffer
+    // launched as a programmatic dependent of the previous advance: nothing
+    // global is read before it has completed; the next advance may be
+    // scheduled from here on
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+        if (e == 0 ? warp != 0 : warp != nw - 1) continue;
+        const int slot = e == 0 ? 0 : nw + 1;
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+#pragma unroll
+            for (int k = 0; k < 2 * XN; ++k)
+                xch[b * slots + (size_t)slot * 2 * 32 * XN + (size_t)k * 32 + lane] = 0u;
+    }
+    const size_t plane_words = (size_t)rows * W;
+    const int r0 = blockIdx.x * ty, tile_n = min(ty, rows - r0);
+    const int hb0 = warp * R;                 // first band row of this warp; band row K is board row r0
+    const int t0 = (int)(T0 & (kPlaneRing - 1));
+    // word offsets of the warp's rows within a plane (a plane holds fewer
+    // than 2^26 words), and which of them are tile rows
+    uint32_t off[R];
+    unsigned tile_rows = 0;
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+        int g = (r0 - K + hb0 + q) % rows;
+        if (g < 0) g += rows;
+        off[q] = (uint32_t)g * W + (uint32_t)lane * WPL;
+        if (hb0 + q >= K && hb0 + q < K + tile_n) tile_rows |= 1u << q;
+    }
+    StripRow<WPL> cur[R];
+    {
+        const uint32_t* newest = planes + (size_t)((t0 + 31) & (kPlaneRing - 1)) * plane_words;
+        uint32_t v[R][WPL];
+#pragma unroll
+        for (int q = 0; q < R; ++q) strip_ld<WPL>(newest + off[q], v[q]);
+#pragma unroll
+        for (int q = 0; q < R; ++q) strip_sums<MODE, WPL>(v[q], lane, cur[q]);
+    }
+    // the cells' oldest bits: plane T0 + s at step s
+    // The cells' oldest bits, plane T0 + s at step s, come through a ring of
+    // kStripDepth slots in shared memory filled by cp.async kStripDepth steps
+    // ahead: a lane copies and reads only its own words, and the copies stay
+    // in flight across the per-step barriers.
+    uint32_t* oring = xch + 2 * slots + (size_t)lane * WPL;       // [depth][warps * R][32][WPL]
+    const size_t oslot = (size_t)nw * R * 32 * WPL;
+    auto fetch_oldest = [&](int s) {
+        if (s < K) {
+            const uint32_t* p = planes + (size_t)((t0 + s) & (kPlaneRing - 1)) * plane_words;
+            uint32_t* d = oring + (size_t)(s % kStripDepth) * oslot + (size_t)hb0 * 32 * WPL;
+#pragma unroll
+            for (int q = 0; q < R; ++q) strip_cp_async<WPL>(d + (size_t)q * 32 * WPL, p + off[q]);
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+#pragma unroll
+    for (int d = 0; d < kStripDepth; ++d) fetch_oldest(d);
+    // the warp's top and bottom rows' (s3, c3) for the step that reads
+    // exchange buffer b; a warp publishes after every step it computed, and
+    // a warp that stopped computing holds no row a later step still needs
+    auto publish = [&](int b) {
+        uint32_t* xp = xch + (size_t)b * slots + (size_t)32 * 2 * XN;
+        uint32_t t[XN];
+#pragma unroll
+        for (int j = 0; j < WPL; ++j) { t[j] = cur[0].s3[j]; t[WPL + j] = cur[0].c3[j]; }
+        xch_put<XN>(xp + ((size_t)(warp * 2 + 0) * 32 + lane) * XN, t);
+#pragma unroll
+        for (int j = 0; j < WPL; ++j) { t[j] = cur[R - 1].s3[j]; t[WPL + j] = cur[R - 1].c3[j]; }
+        xch_put<XN>(xp + ((size_t)(warp * 2 + 1) * 32 + lane) * XN, t);
+    };
+    publish(0);
+    // the last step that still needs one of this warp's rows: after step s
+    // the band rows [s + 1, 2K + ty - 2 - s] must be right
+    const int s_last = min(hb0 + R - 2, 2 * K + ty - 2 - hb0);
+    auto step = [&](int s) {
+        const uint32_t* xb = xch + (size_t)(s & 1) * slots;
+        __syncthreads();
+        if (s > s_last) return;
+        // this step's copies (the group committed kStripDepth groups ago)
+        asm volatile("cp.async.wait_group %0;\n" ::"n"(kStripDepth - 1) : "memory");
+        uint32_t Od[R][WPL];
+        {
+            const uint32_t* o = oring + (size_t)(s % kStripDepth) * oslot + (size_t)hb0 * 32 * WPL;
+#pragma unroll
+            for (int q = 0; q < R; ++q) strip_lds<WPL>(o + (size_t)q * 32 * WPL, Od[q]);
+        }
+        uint32_t ab[XN], be[XN];              // sums of the row above the warp's first and below its last
+        xch_get<XN>(xb + ((size_t)(warp * 2 + 1) * 32 + lane) * XN, ab);
+        xch_get<XN>(xb + ((size_t)((warp + 2) * 2 + 0) * 32 + lane) * XN, be);
+        uint32_t* out = planes + (size_t)((t0 + s + 32) & (kPlaneRing - 1)) * plane_words;
+        uint32_t prev[WPL];
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            uint32_t nl[WPL];
+#pragma unroll
+            for (int j = 0; j < WPL; ++j) {
+                const uint32_t as = q == 0 ? ab[j] : cur[q > 0 ? q - 1 : 0].s3[j];
+                const uint32_t ac = q == 0 ? ab[WPL + j] : cur[q > 0 ? q - 1 : 0].c3[j];
+                const uint32_t bs = q == R - 1 ? be[j] : cur[q < R - 1 ? q + 1 : 0].s3[j];
+                const uint32_t bc = q == R - 1 ? be[WPL + j] : cur[q < R - 1 ? q + 1 : 0].c3[j];
+                const uint32_t ms = MODE == 1 ? cur[q].s2[j] : cur[q].s3[j];
+                const uint32_t mc = MODE == 1 ? cur[q].c2[j] : cur[q].c3[j];
+                // count = c0 + 2 (k1 + x) + 4 y
+                const uint32_t c0 = as ^ ms ^ bs, k1 = maj3(as, ms, bs);
+                const uint32_t x = ac ^ mc ^ bc, y = maj3(ac, mc, bc);
+                if (CONWAY) {
+                    // count 2 or 3: exactly one of x, k1 and no y; 3 also needs c0
+                    nl[j] = (x ^ k1) & ~y & (c0 | Od[q][j]);
+                } else {
+                    const uint32_t c1 = x ^ k1, k2 = x & k1, c2 = y ^ k2, c3 = y & k2;
+                    uint32_t S = 0, B = 0;
+#pragma unroll
+                    for (int v = 0; v < 10; ++v) {
+                        if (!(((smask | bmask) >> v) & 1u)) continue;
+                        const uint32_t eq = ~((c0 ^ ((v & 1) ? ~0u : 0u)) | (c1 ^ ((v & 2) ? ~0u : 0u)) |
+                                              (c2 ^ ((v & 4) ? ~0u : 0u)) | (c3 ^ ((v & 8) ? ~0u : 0u)));
+                        if ((smask >> v) & 1u) S |= eq;
+                        if ((bmask >> v) & 1u) B |= eq;
+                    }
+                    nl[j] = (Od[q][j] & S) | (~Od[q][j] & B);
+                }
+            }
+            // the new row q - 1 is no longer read as an old row: store it and
+            // take its sums
+            if (q > 0) {
+                if (tile_rows & (1u << (q - 1))) strip_st<WPL>(out + off[q - 1], prev);
+                strip_sums<MODE, WPL>(prev, lane, cur[q - 1]);
+            }
+#pragma unroll
+            for (int j = 0; j < WPL; ++j) prev[j] = nl[j];
+        }
+        {
+            if (tile_rows & (1u << (R - 1))) strip_st<WPL>(out + off[R - 1], prev);
+            strip_sums<MODE, WPL>(prev, lane, cur[R - 1]);
+        }
+        // buffer (s + 1) & 1 was last read before this step's barrier
+        publish((s + 1) & 1);
+        // the slot just read takes the plane kStripDepth steps ahead
+        fetch_oldest(s + kStripDepth);
+    };
+    for (int s = 0; s < K; ++s) step(s);
+    // no copy may land in shared memory after the block ends
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 static int num_sms() {
     int dev = 0, n = 0;
     SG_CUDA(cudaGetDevice(&dev));
@@ -652,6 +933,75 @@ class GameOfLifeModel : public Model {
             }
         }
     }
+    // Steps of the full-width strip kernel per launch (at most 31: a step
+    // reads the plane written 32 steps earlier, which must come from an
+    // earlier launch).
+    static int strip_steps_per_launch() {
+        static const int k = [] {
+            const char* e = std::getenv("SG_GOL_STEPS_PER_LAUNCH");
+            const int v = e ? std::atoi(e) : 12;
+            return v < 1 ? 1 : (v > 31 ? 31 : v);
+        }();
+        return k;
+    }
+    // exchange buffers: 2 x (warps + 2) slots of 2 rows x 32 lanes x 2 * wpl
+    // words; ring of the oldest-bit planes: kStripDepth x warps x rpw rows x
+    // 32 lanes x wpl words
+    static size_t strip_smem_bytes(int warps, int rpw, int wpl) {
+        return ((size_t)(warps + 2) * 256 + (size_t)kStripDepth * warps * rpw * 32) * wpl * 4;
+    }
+    static long advance_strips(int rows, int W, int mode, bool conway, long n, uint32_t* planes,
+                               unsigned smask, unsigned bmask, cudaStream_t s) {
+        using Kernel = void (*)(int, int, long long, int, uint32_t*, unsigned, unsigned);
+        const int wpl = W / 32;
+        const int rpw = strip_rows(wpl), max_warps = strip_max_warps(rpw);
+        const int wi = wpl == 1 ? 0 : (wpl == 2 ? 1 : 2);
+#define SG_STRIPS(M, C)                                                                  \
+    {k_gol_strips_steps<M, C, 1, strip_rows(1)>, k_gol_strips_steps<M, C, 2, strip_rows(2)>, \
+     k_gol_strips_steps<M, C, 4, strip_rows(4)>}
+        static const Kernel kernels[2][2][3] = {{SG_STRIPS(1, false), SG_STRIPS(1, true)},
+                                                {SG_STRIPS(2, false), SG_STRIPS(2, true)}};
+#undef SG_STRIPS
+        const Kernel kernel = kernels[mode - 1][conway ? 1 : 0][wi];
+        const size_t max_smem = strip_smem_bytes(max_warps, rpw, wpl);
+        static bool configured[2][2][3] = {};
+        bool& cfg = configured[mode - 1][conway ? 1 : 0][wi];
+        if (!cfg) {
+            SG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)max_smem));
+            cfg = true;
+        }
+        const int sms = num_sms();
+        long launches = 0;
+        long long T = 0;
+        while (T < n) {
+            const int K = (int)std::min<long long>(strip_steps_per_launch(), n - T);
+            // one band of ty rows per SM, within max_warps warps of rpw rows
+            // holding the band and its 2K halo rows
+            int ty = (rows + sms - 1) / sms;
+            ty = std::min(ty, max_warps * rpw - 2 * K);
+            const int nw = (ty + 2 * K + rpw - 1) / rpw;
+            const int grid = (rows + ty - 1) / ty;
+            const size_t smem = strip_smem_bytes(nw, rpw, wpl);
+            // programmatic dependent launch: each launch may be scheduled
+            // while the previous one drains; it waits for it to complete
+            // (griddepcontrol.wait) before touching the planes
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3((unsigned)grid);
+            cfg.blockDim = dim3((unsigned)(nw * 32));
+            cfg.dynamicSmemBytes = smem;
+            cfg.stream = s;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            attr[0].val.programmaticStreamSerializationAllowed = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            SG_CUDA(cudaLaunchKernelEx(&cfg, kernel, rows, ty, (long long)T, K, planes, smask, bmask));
+            ++launches;
+            T += K;
+        }
+        return launches;
+    }
     // Whole-run path on bit planes: a toroidal board whose only input is its
     // own 0/1-weight 3x3 connection with delay 0.
     bool can_advance_alone(State& st, const LayerState& ls) const override {
@@ -679,6 +1029,13 @@ class GameOfLifeModel : public Model {
         // mask; the B3/S23 rule as its own instance
         const int mode = (mask9 & 0x1EFu) == 0x1EFu ? ((mask9 & 0x10u) ? 2 : 1) : 0;
         const bool conway = smask == count_mask(2, 3) && bmask == count_mask(3, 3);
+        if (mode != 0 && (W == 32 || W == 64 || W == 128)) {
+            launches += advance_strips(l.rows, W, mode, conway, n, planes, smask, bmask, s);
+            k_gol_planes_to_words<<<blocks_for(segs * 32, 256), 256, 0, s>>>(
+                l.rows, W, n, planes, words, ls.input->df(), mask9);
+            SG_LAUNCH_CHECK();
+            return launches + 1;
+        }
         using Kernel = void (*)(int, int, int, long long, int, uint32_t*, unsigned, unsigned,
                                 unsigned);
         static const Kernel kernels[6] = {k_gol_planes_steps<0, false>, k_gol_planes_steps<1, false>,

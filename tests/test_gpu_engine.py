@@ -112,7 +112,13 @@ def test_izhikevich_graph_replay_equals_stepwise(sg):
     (96, 160, dict(survival_min=2, survival_max=3, birth_min=3, birth_max=3)),
     (20, 32, dict(survival_min=2, survival_max=4, birth_min=3, birth_max=3)),
     (130, 288, dict(diagonal=True, survival_min=3, survival_max=4, birth_min=3, birth_max=5)),
-    (257, 64, dict(survival_min=1, survival_max=5, birth_min=2, birth_max=3))])
+    (257, 64, dict(survival_min=1, survival_max=5, birth_min=2, birth_max=3)),
+    # boards 1024, 2048 and 4096 cells wide take the full-width strip kernel
+    (40, 1024, dict(survival_min=2, survival_max=3, birth_min=3, birth_max=3)),
+    (70, 2048, dict(diagonal=True, survival_min=3, survival_max=4, birth_min=3, birth_max=5)),
+    (17, 2048, dict(survival_min=1, survival_max=5, birth_min=2, birth_max=3)),
+    (33, 4096, dict(survival_min=2, survival_max=3, birth_min=3, birth_max=3)),
+    (24, 4096, dict(diagonal=True, survival_min=2, survival_max=6, birth_min=4, birth_max=4))])
 def test_gol_whole_runs_equal_per_step_path(sg, rows, cols, rule):
     """Without an environment a toroidal game_of_life board advances whole runs
     on bit planes (many steps per launch); words and the input register equal
