@@ -556,6 +556,11 @@ __global__ void __launch_bounds__(kBlock) k_rate_lambda(
     const int b0 = blockIdx.z * D.bg, b1 = min(D.B, b0 + D.bg);
     const float* ln = last ? nullptr : lam_next + (long long)(l + 1) * D.B * D.N;
     const W halo(D, ty0, tx0);
+    // launched as a programmatic dependent of the previous step's adjoint:
+    // the weights above are loaded while it drains; nothing it writes is
+    // read before it has completed
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
     float pre[W::PER];
     if (!last) halo.fetch(ln + (long long)b0 * D.N, a1, pre);
     for (int b = b0, buf = 0; b < b1; ++b, buf ^= 1) {
@@ -863,12 +868,25 @@ void step(const Dims& D, const float* x_t, const float* wo, const float* tau, co
     SG_LAUNCH_CHECK();
 }
 
+// One timestep of the adjoint, launched as a programmatic dependent of the
+// launch before it (the next step's adjoint, or any kernel, which then simply
+// completes first): each step's weight loads overlap the previous step's tail.
 void lambda_step(const Dims& D, const float* wo, const float* tau, const Work& W,
                  const float* gy_t, const float* r_t, const float* lam_next, float* lam, float* dx_t,
                  cudaStream_t st) {
-    SG_RATE_FIELD(D.field, (k_rate_lambda<F><<<tile_grid(D), kBlock, 0, st>>>(
-                               D, W.wt, wo, tau, gy_t, r_t, lam_next, lam, dx_t)));
-    SG_LAUNCH_CHECK();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = tile_grid(D);
+    cfg.blockDim = dim3(kBlock);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const float* wt = W.wt;
+    SG_RATE_FIELD(D.field, SG_CUDA(cudaLaunchKernelEx(&cfg, k_rate_lambda<F>, D, wt, wo, tau, gy_t,
+                                                      r_t, lam_next, lam, dx_t)));
 }
 
 // Shared memory of the multi-step kernel, or 0 where it does not fit (the
