@@ -10,7 +10,10 @@
 //   * a producer warp issues, per chunk, one 2-D tensor TMA load per array
 //     (weights, short-term R and w, delays, short and long traces) whose box
 //     rows are the CTA's bands' contiguous chunks, into a shared-memory ring,
-//     completing on the stage's mbarrier;
+//     completing on the stage's mbarrier.  A connection that never learns
+//     has its weights and short-term factors fixed for a whole run: it reads
+//     one array of w * (R * w) instead of the three (EFF), computed after
+//     each upload with the activator's own float operations;
 //   * 8 compute warps compute the chunk's synapses, write the pre-decay traces
 //     to a ring of sums tiles and the decayed traces back into the stage, and
 //     arrive on the stage's "consumed" mbarrier (they synchronise only among
@@ -57,7 +60,7 @@ constexpr int kBlockFloats = kR * kBand; // one band's chunk: 32 rows x 8 destin
 // of the producer warp, which takes no part in the compute warps' barriers.
 constexpr int kProducer = kCompute + 32 * kSumWarps;
 
-constexpr int kArrays = 6;               // w, R, w_stp, [delay], short, [long]
+constexpr int kArrays = 6;               // w, R, w_stp (or w * (R * w_stp)), [delay], short, [long]
 
 struct ColsMaps {
     CUtensorMap m[2][kArrays];           // [bands of the wider CTAs, narrower][array]
@@ -121,12 +124,13 @@ __device__ __forceinline__ int source_of_row(const DGeom& g, int row) {
     return (row / fkc + g.fr0) * g.from_cols + (row % fkc + g.fc0);
 }
 
-template <int SR, bool LONG, bool SUBSET>
+template <int SR, bool LONG, bool SUBSET, bool EFF>
 __global__ void __launch_bounds__(kThreads, 1)
     k_iz_cols_bulk(const __grid_constant__ ColsMaps maps, const ColsParams p) {
     constexpr int HAS_D = SR == S_BIT ? 1 : 0;
-    constexpr int NA = 4 + HAS_D + (LONG ? 1 : 0);
-    constexpr int A_ST = 3 + HAS_D, A_LT = 4 + HAS_D;
+    constexpr int NW = EFF ? 1 : 3;                        // weight arrays
+    constexpr int NA = NW + 1 + HAS_D + (LONG ? 1 : 0);
+    constexpr int A_D = NW, A_ST = NW + HAS_D, A_LT = NW + 1 + HAS_D;
     constexpr int kTile = kMaxBands * kBlockFloats;        // floats per array per stage
     constexpr int kSumBuf = 2 * kR * kSumPitch;            // one chunk's short + long sums
     extern __shared__ unsigned char smem_raw[];
@@ -208,10 +212,11 @@ __global__ void __launch_bounds__(kThreads, 1)
                 tma_store2(&mp[A_ST], ch * kBlockFloats, band0, smem_u32(tile(s, A_ST)));
                 if (LONG) tma_store2(&mp[A_LT], ch * kBlockFloats, band0, smem_u32(tile(s, A_LT)));
                 asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-                if (ch + kStages < nchunks) {
-                    // the stage is refilled once its traces have been read out
-                    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-                    issue(ch + kStages);
+                // the previous chunk's stage is refilled once its traces have
+                // been read out (this chunk's store may still be reading)
+                if (ch >= 1 && ch - 1 + kStages < nchunks) {
+                    asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+                    issue(ch - 1 + kStages);
                     ++issued;
                 }
             }
@@ -280,17 +285,17 @@ __global__ void __launch_bounds__(kThreads, 1)
                 s_abort = 1;
             float* sb = sums + q * kSumBuf;
             const float* tw = tile(s, 0);
-            const float* tr = tile(s, 1);
-            const float* tsw = tile(s, 2);
+            const float* tr = tile(s, EFF ? 0 : 1);
+            const float* tsw = tile(s, EFF ? 0 : 2);
             float* tst = tile(s, A_ST);
 #pragma unroll
             for (int k = 0; k < kPer; ++k) {
                 const int o = eo[k];
                 if (o < 0) continue;
                 const uint32_t word = s_words[s][ej[k]];
-                const int delay = HAS_D ? __float_as_int(tile(s, 3)[o]) : 0;
+                const int delay = HAS_D ? __float_as_int(tile(s, A_D)[o]) : 0;
                 const float spike = extract<SR>(word, delay);
-                const float weight = tw[o] * (tr[o] * tsw[o]);
+                const float weight = EFF ? tw[o] : tw[o] * (tr[o] * tsw[o]);
                 const float st = tst[o] + (spike * weight * p.gcond);
                 const int so = ej[k] * kSumPitch + ecol[k];
                 sb[so] = st;
@@ -349,14 +354,29 @@ struct IzColsPlan {
     ColsMaps maps;
     ColsParams base;
     int n_cta = 0, na = 0;
-    bool has_delay = false, long_trace = false;
+    bool has_delay = false, long_trace = false, eff = false;
     size_t smem = 0;
 };
+
+// w * (R * w_stp), the activator's weight of a synapse, over the whole banded
+// array (padding included)
+__global__ void k_iz_effective_weights(size_t n, const float* __restrict__ w,
+                                       const float* __restrict__ stp_r,
+                                       const float* __restrict__ stp_w, float* __restrict__ eff) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) eff[i] = w[i] * (stp_r[i] * stp_w[i]);
+}
+
+void fill_iz_effective_weights(size_t n, const float* w, const float* stp_r, const float* stp_w,
+                               float* eff, cudaStream_t s) {
+    k_iz_effective_weights<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, w, stp_r, stp_w, eff);
+    SG_LAUNCH_CHECK();
+}
 
 std::shared_ptr<IzColsPlan> make_iz_cols_plan(int nrows, int ncols, const float* w,
                                               const float* stp_r, const float* stp_w,
                                               const int* delays, float* short_tr,
-                                              float* long_tr, int ctas) {
+                                              float* long_tr, const float* eff, int ctas) {
     if (nrows < 1 || ncols < 1) return nullptr;
     auto encode = encode_fn();
     if (!encode) return nullptr;
@@ -370,7 +390,8 @@ std::shared_ptr<IzColsPlan> make_iz_cols_plan(int nrows, int ncols, const float*
                            (bands + kMaxBands - 1) / kMaxBands);
     plan->has_delay = delays != nullptr;
     plan->long_trace = long_tr != nullptr;
-    plan->na = 4 + (plan->has_delay ? 1 : 0) + (plan->long_trace ? 1 : 0);
+    plan->eff = eff != nullptr;
+    plan->na = (plan->eff ? 2 : 4) + (plan->has_delay ? 1 : 0) + (plan->long_trace ? 1 : 0);
     plan->smem = cols_smem_bytes(plan->na);
     if ((long long)plan->smem > optin) return nullptr;
     ColsParams& p = plan->base;
@@ -381,9 +402,13 @@ std::shared_ptr<IzColsPlan> make_iz_cols_plan(int nrows, int ncols, const float*
     p.extra = bands % plan->n_cta;
     const void* arrays[kArrays];
     int a = 0;
-    arrays[a++] = w;
-    arrays[a++] = stp_r;
-    arrays[a++] = stp_w;
+    if (plan->eff) {
+        arrays[a++] = eff;
+    } else {
+        arrays[a++] = w;
+        arrays[a++] = stp_r;
+        arrays[a++] = stp_w;
+    }
     if (plan->has_delay) arrays[a++] = delays;
     arrays[a++] = short_tr;
     if (plan->long_trace) arrays[a++] = long_tr;
@@ -407,15 +432,15 @@ std::shared_ptr<IzColsPlan> make_iz_cols_plan(int nrows, int ncols, const float*
     return plan;
 }
 
-template <int SR, bool LONG, bool SUBSET>
+template <int SR, bool LONG, bool SUBSET, bool EFF>
 static void launch_t(const IzColsPlan& plan, const ColsParams& p, cudaStream_t s) {
     static int configured = 0;
     if (configured < (int)plan.smem) {
-        SG_CUDA(cudaFuncSetAttribute(k_iz_cols_bulk<SR, LONG, SUBSET>,
+        SG_CUDA(cudaFuncSetAttribute(k_iz_cols_bulk<SR, LONG, SUBSET, EFF>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem));
         configured = (int)plan.smem;
     }
-    k_iz_cols_bulk<SR, LONG, SUBSET><<<plan.n_cta, kThreads, plan.smem, s>>>(plan.maps, p);
+    k_iz_cols_bulk<SR, LONG, SUBSET, EFF><<<plan.n_cta, kThreads, plan.smem, s>>>(plan.maps, p);
     SG_LAUNCH_CHECK();
 }
 
@@ -432,17 +457,23 @@ void launch_iz_cols_tma(const IzColsPlan& plan, const DGeom& g, int src_type, bo
     p.short_cond = short_cond;
     p.long_cond = long_cond;
     const bool lng = plan.long_trace;
-#define SG_COLS(SRV)                                                         \
+#define SG_COLS(SRV, EF)                                                     \
     if (lng) {                                                               \
-        if (subset) launch_t<SRV, true, true>(plan, p, stream);              \
-        else launch_t<SRV, true, false>(plan, p, stream);                    \
+        if (subset) launch_t<SRV, true, true, EF>(plan, p, stream);          \
+        else launch_t<SRV, true, false, EF>(plan, p, stream);                \
     } else {                                                                 \
-        if (subset) launch_t<SRV, false, true>(plan, p, stream);             \
-        else launch_t<SRV, false, false>(plan, p, stream);                   \
+        if (subset) launch_t<SRV, false, true, EF>(plan, p, stream);         \
+        else launch_t<SRV, false, false, EF>(plan, p, stream);               \
     }
-    if (src_type == S_BIT) { SG_COLS(S_BIT) }
-    else if (src_type == S_FLOAT) { SG_COLS(S_FLOAT) }
-    else { SG_COLS(S_INT) }
+    if (plan.eff) {
+        if (src_type == S_BIT) { SG_COLS(S_BIT, true) }
+        else if (src_type == S_FLOAT) { SG_COLS(S_FLOAT, true) }
+        else { SG_COLS(S_INT, true) }
+    } else {
+        if (src_type == S_BIT) { SG_COLS(S_BIT, false) }
+        else if (src_type == S_FLOAT) { SG_COLS(S_FLOAT, false) }
+        else { SG_COLS(S_INT, false) }
+    }
 #undef SG_COLS
 }
 

@@ -15,14 +15,21 @@ struct IzColsPlan;
 
 // nrows sources x ncols destinations, every array banded
 // (banded_index(destination, source, nrows)); delays may be null (FLOAT / INT
-// sources), long_tr null for single-trace opcodes.  bands_per_cta_max limits
-// each CTA to that many bands of kBand destinations; ctas = 0 spreads the
-// bands over every SM.  Returns null if the kernel cannot run this shape
-// (the caller then uses the per-destination activator).
+// sources), long_tr null for single-trace opcodes.  eff, if not null, holds
+// w * (R * w_stp) for a connection whose weights and short-term factors do
+// not change during a run (fill_iz_effective_weights after each upload); the
+// kernel then reads it instead of w, stp_r and stp_w.  ctas = 0 spreads the
+// bands over every SM.  Returns null if the kernel cannot run this shape (the
+// caller then uses the per-destination activator).
 std::shared_ptr<IzColsPlan> make_iz_cols_plan(int nrows, int ncols, const float* w,
                                               const float* stp_r, const float* stp_w,
                                               const int* delays, float* short_tr,
-                                              float* long_tr, int ctas = 0);
+                                              float* long_tr, const float* eff = nullptr,
+                                              int ctas = 0);
+
+// eff[i] = w[i] * (stp_r[i] * stp_w[i]) for i < n (the activator's weight).
+void fill_iz_effective_weights(size_t n, const float* w, const float* stp_r, const float* stp_w,
+                               float* eff, cudaStream_t s);
 
 void launch_iz_cols_tma(const IzColsPlan& plan, const DGeom& g, int src_type, bool subset,
                         const uint32_t* src, float gcond, float short_tau, float long_tau,

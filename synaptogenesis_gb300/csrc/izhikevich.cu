@@ -741,9 +741,14 @@ class IzhikevichModel : public Model {
     const char* name() const override { return "izhikevich"; }
     OutputType output_type() const override { return OUT_BIT; }
 
-    // After every upload (delays may have changed): which sources' last
-    // visits share one delay.
+    // After every upload (delays, weights or short-term factors may have
+    // changed): which sources' last visits share one delay, and the
+    // effective weights of a connection that never learns.
     void prepare_device(State&, ConnState& cs, cudaStream_t s) const override {
+        if (cs.eff_weights)
+            fill_iz_effective_weights(cs.weights->dev_count, cs.weights->df(),
+                                      cs.var("short term R")->df(), cs.var("short term w")->df(),
+                                      cs.eff_weights->df(), s);
         if (!cs.delay_summary) return;
         const int n = cs.conn->from->size;
         k_iz_delay_summary<<<blocks_for(n, 256), 256, 0, s>>>(
@@ -794,6 +799,15 @@ class IzhikevichModel : public Model {
         if (c.parameter("direct", "false") != "true" && c.opcode != OP_ADD && c.opcode != OP_SUB &&
             c.opcode != OP_MULT && c.opcode != OP_REWARD && c.opcode != OP_GAP)
             throw SgError(c.str() + ": Unimplemented connection type!");
+        // A fully connected or subset trace connection that never learns
+        // keeps w, R and w_stp for a whole run: the TMA activator reads their
+        // product, w * (R * w_stp), from one array (8 bytes less per synapse
+        // and step), refilled after every upload.
+        if ((c.type == FULLY_CONNECTED || c.type == SUBSET) && !c.plastic &&
+            c.parameter("direct", "false") != "true" && c.opcode != OP_GAP) {
+            cs.eff_weights = st.add_array("effective weights", 'f', n, matrix_layout(c), R, C);
+            cs.eff_weights->scratch = true;
+        }
         // trace activators write conductances, not a register, and keep no
         // weight copy: second order only through the base activator
         // (izhikevich_attributes.cpp:371-379)
@@ -921,7 +935,8 @@ class IzhikevichModel : public Model {
                 cs.device_plan = make_iz_cols_plan(
                     nrows, ncols, cs.weights->df(), cs.var("short term R")->df(),
                     cs.var("short term w")->df(), bit ? cs.delays->di() : nullptr,
-                    cs.var("short trace")->df(), lname ? cs.var("long trace")->df() : nullptr);
+                    cs.var("short trace")->df(), lname ? cs.var("long trace")->df() : nullptr,
+                    cs.eff_weights ? cs.eff_weights->df() : nullptr);
             }
             if (cs.device_plan) {
                 launch_iz_cols_tma(*static_cast<IzColsPlan*>(cs.device_plan.get()), cs.geom,

@@ -90,6 +90,11 @@ struct ConnState {
     // This step's per-connection prologue ran with other connections'
     // (Model::activate_prologue); the connection's activation clears it.
     bool prologue_done = false;
+    // Fully connected or subset trace connection that never learns: the
+    // activator's per-synapse weight w * (R * w_stp), constant during a run
+    // and refilled after every upload (device only, same layout as the
+    // weights).
+    Array* eff_weights = nullptr;
     // Second-order host: the per-step copy of its weights that the slaves
     // modulate and the host's activation reads (device only, same layout as
     // the weights; weight_matrix.cpp:79-80).
