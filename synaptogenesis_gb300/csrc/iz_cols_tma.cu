@@ -288,23 +288,35 @@ __global__ void __launch_bounds__(kThreads, 1)
             const float* tr = tile(s, EFF ? 0 : 1);
             const float* tsw = tile(s, EFF ? 0 : 2);
             float* tst = tile(s, A_ST);
+            float* tlt = tile(s, LONG ? A_LT : A_ST);
+            // every load of the thread's synapses first, then the arithmetic
+            // and the stores (a store into the stage would otherwise hold
+            // back the next synapse's loads: the compiler cannot tell them
+            // apart)
+            float term[kPer], st[kPer], lt[kPer];
+#pragma unroll
+            for (int k = 0; k < kPer; ++k) {
+                const int o = eo[k] < 0 ? 0 : eo[k];
+                const uint32_t word = s_words[s][ej[k]];
+                const int delay = HAS_D ? __float_as_int(tile(s, A_D)[o]) : 0;
+                const float weight = EFF ? tw[o] : tw[o] * (tr[o] * tsw[o]);
+                term[k] = extract<SR>(word, delay) * weight;
+                st[k] = tst[o];
+                lt[k] = LONG ? tlt[o] : 0.0f;
+            }
 #pragma unroll
             for (int k = 0; k < kPer; ++k) {
                 const int o = eo[k];
                 if (o < 0) continue;
-                const uint32_t word = s_words[s][ej[k]];
-                const int delay = HAS_D ? __float_as_int(tile(s, A_D)[o]) : 0;
-                const float spike = extract<SR>(word, delay);
-                const float weight = EFF ? tw[o] : tw[o] * (tr[o] * tsw[o]);
-                const float st = tst[o] + (spike * weight * p.gcond);
+                const float add = term[k] * p.gcond;
+                const float sv = st[k] + add;
                 const int so = ej[k] * kSumPitch + ecol[k];
-                sb[so] = st;
-                tst[o] = st * p.short_tau;
+                sb[so] = sv;
+                tst[o] = sv * p.short_tau;
                 if (LONG) {
-                    float* tlt = tile(s, A_LT);
-                    const float lt = tlt[o] + (spike * weight * p.gcond);
-                    sb[kR * kSumPitch + so] = lt;
-                    tlt[o] = lt * p.long_tau;
+                    const float lv = lt[k] + add;
+                    sb[kR * kSumPitch + so] = lv;
+                    tlt[o] = lv * p.long_tau;
                 }
             }
             asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&sums_full[q]))
