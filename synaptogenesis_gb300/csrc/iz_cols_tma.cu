@@ -14,18 +14,21 @@
 //     has its weights and short-term factors fixed for a whole run: it reads
 //     one array of w * (R * w) instead of the three (EFF), computed after
 //     each upload with the activator's own float operations;
-//   * 8 compute warps compute the chunk's synapses, write the pre-decay traces
-//     to a ring of sums tiles and the decayed traces back into the stage, and
-//     arrive on the stage's "consumed" mbarrier (they synchronise only among
-//     themselves; warp 0 also prefetches the chunks' source words);
-//   * the producer writes the decayed traces back with TMA tensor stores and
-//     refills the stage once the stores have read it;
+//   * 8 compute warps compute the chunk's synapses (every shared-memory load
+//     of a thread first, then its arithmetic), write the pre-decay traces to
+//     a ring of sums tiles and arrive on the stage's "consumed" mbarrier
+//     (they synchronise only among themselves; warp 0 also prefetches the
+//     chunks' source words);
+//   * the producer refills a stage as soon as it is consumed;
 //   * two sum warps, one lane per destination, add each chunk's pre-decay
-//     traces in source order (the reference's sequential fp32 sum) while the
-//     compute warps go on with the next chunks.
+//     traces in source order (the reference's sequential fp32 sum) and write
+//     the decayed traces back to HBM (streaming stores, 32-byte sectors), while
+//     the compute warps go on with the next chunks.  Nothing is written into
+//     the stages, so they need no store to drain before a refill, and the
+//     shared-memory pipe carries the loads, the sums and nothing else.
 // Every mbarrier wait is bounded: if one runs out, the kernel records the
-// fact in a device flag, waits (bounded) for its loads in flight, drains its
-// stores and returns; check_iz_cols_errors reports it on the host.
+// fact in a device flag, waits (bounded) for its loads in flight and returns;
+// check_iz_cols_errors reports it on the host.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_pipeline.h>
@@ -56,7 +59,7 @@ constexpr int kThreads = kCompute + 32 * kSumWarps + 32;   // plus one producer 
 constexpr int kSumPitch = 40;            // sums row pitch: conflict-free writes and reads
 constexpr int kWaitLimit = 1 << 20;
 constexpr int kBlockFloats = kR * kBand; // one band's chunk: 32 rows x 8 destinations
-// The thread that issues the TMA copies and waits on its store groups: lane 0
+// The thread that issues the TMA copies: lane 0
 // of the producer warp, which takes no part in the compute warps' barriers.
 constexpr int kProducer = kCompute + 32 * kSumWarps;
 
@@ -73,6 +76,8 @@ struct ColsParams {
     float gcond, short_tau, long_tau;
     float* short_cond;
     float* long_cond;
+    float* short_tr;                     // the banded trace arrays (decayed traces written back)
+    float* long_tr;
 };
 
 __device__ int g_cols_error = 0;
@@ -85,6 +90,17 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
 }
 
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    {
+        // a phase that has already completed: no suspending wait
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
     for (int it = 0; it < kWaitLimit; ++it) {
         uint32_t ok;
         asm volatile(
@@ -108,13 +124,6 @@ __device__ __forceinline__ void tma_load2(uint32_t dst, const CUtensorMap* map, 
         :
         : "r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
         : "memory");
-}
-
-__device__ __forceinline__ void tma_store2(const CUtensorMap* map, int x, int y, uint32_t src) {
-    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];"
-                 :
-                 : "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(src)
-                 : "memory");
 }
 
 template <bool SUBSET>
@@ -189,7 +198,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncthreads();
 
     if (tid >= kProducer) {
-        // ---- producer warp: loads into free stages, stores of finished ones
+        // ---- producer warp: loads into free stages
         if (tid == kProducer) {
             const int skip = g_cols_skip_chunk;
             auto issue = [&](int ch) {
@@ -209,14 +218,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (; ch < nchunks; ++ch) {
                 const int s = ch % kStages;
                 if (!mbar_wait(smem_u32(&consumed[s]), parity(ch))) break;
-                tma_store2(&mp[A_ST], ch * kBlockFloats, band0, smem_u32(tile(s, A_ST)));
-                if (LONG) tma_store2(&mp[A_LT], ch * kBlockFloats, band0, smem_u32(tile(s, A_LT)));
-                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-                // the previous chunk's stage is refilled once its traces have
-                // been read out (this chunk's store may still be reading)
-                if (ch >= 1 && ch - 1 + kStages < nchunks) {
-                    asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
-                    issue(ch - 1 + kStages);
+                // the compute warps are done with the stage: refill it
+                if (ch + kStages < nchunks) {
+                    issue(ch + kStages);
                     ++issued;
                 }
             }
@@ -226,13 +230,16 @@ __global__ void __launch_bounds__(kThreads, 1)
                 atomicExch(&g_cols_error, 1);
                 for (int c = ch; c < issued; ++c) mbar_wait(smem_u32(&full[c % kStages]), parity(c));
             }
-            asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
         }
     } else if (tid >= kCompute) {
         // ---- sum warps: warp kCompute/32 adds the short traces, the next the
         // long ones; one lane per destination, each chunk's rows in order
         const int kind = (tid - kCompute) / 32, c = (tid - kCompute) % 32;
         const bool owner = c < ncol && (kind == 0 || LONG);
+        const float tau = kind == 0 ? p.short_tau : p.long_tau;
+        // this lane's column of the banded trace array, row 0
+        float* trace = (kind == 0 ? p.short_tr : p.long_tr) +
+                       (size_t)(band0 + c / kBand) * p.nrows * kBand + c % kBand;
         float acc = 0.0f;
         int ch = 0;
         for (; ch < nchunks; ++ch) {
@@ -241,14 +248,23 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (owner) {
                 const float* col = sums + q * kSumBuf + kind * kR * kSumPitch + c;
                 const int nr = chunk_rows(ch);
+                float* tr = trace + (size_t)ch * kR * kBand;
                 if (nr == kR) {
                     float v[kR];
 #pragma unroll
                     for (int j = 0; j < kR; ++j) v[j] = col[j * kSumPitch];
 #pragma unroll
                     for (int j = 0; j < kR; ++j) acc += v[j];
+                    // the decayed traces go back to HBM from here (the sums
+                    // hold every pre-decay trace of the chunk)
+#pragma unroll
+                    for (int j = 0; j < kR; ++j) __stcs(tr + j * kBand, v[j] * tau);
                 } else {
-                    for (int j = 0; j < nr; ++j) acc += col[j * kSumPitch];
+                    for (int j = 0; j < nr; ++j) {
+                        const float v = col[j * kSumPitch];
+                        acc += v;
+                        __stcs(tr + j * kBand, v * tau);
+                    }
                 }
             }
             asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&sums_empty[q]))
@@ -287,12 +303,11 @@ __global__ void __launch_bounds__(kThreads, 1)
             const float* tw = tile(s, 0);
             const float* tr = tile(s, EFF ? 0 : 1);
             const float* tsw = tile(s, EFF ? 0 : 2);
-            float* tst = tile(s, A_ST);
-            float* tlt = tile(s, LONG ? A_LT : A_ST);
+            const float* tst = tile(s, A_ST);
+            const float* tlt = tile(s, LONG ? A_LT : A_ST);
             // every load of the thread's synapses first, then the arithmetic
-            // and the stores (a store into the stage would otherwise hold
-            // back the next synapse's loads: the compiler cannot tell them
-            // apart)
+            // and the stores (a store into the sums would otherwise hold back
+            // the next synapse's loads: the compiler cannot tell them apart)
             float term[kPer], st[kPer], lt[kPer];
 #pragma unroll
             for (int k = 0; k < kPer; ++k) {
@@ -312,12 +327,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const float sv = st[k] + add;
                 const int so = ej[k] * kSumPitch + ecol[k];
                 sb[so] = sv;
-                tst[o] = sv * p.short_tau;
-                if (LONG) {
-                    const float lv = lt[k] + add;
-                    sb[kR * kSumPitch + so] = lv;
-                    tlt[o] = lv * p.long_tau;
-                }
+                if (LONG) sb[kR * kSumPitch + so] = lt[k] + add;
             }
             asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&sums_full[q]))
                          : "memory");
@@ -325,9 +335,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 fetch_words(ch + kStages - 1);
                 __pipeline_wait_prior(kStages - 2);        // chunk ch+1 landed
             }
-            // the decayed traces are read by the TMA store: generic-proxy
-            // writes become visible to the async proxy before the arrival
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            // the stage is refilled (TMA) once every compute thread has read it
             asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&consumed[s]))
                          : "memory");
             asm volatile("bar.sync 1, %0;" ::"n"(kCompute) : "memory");
@@ -412,6 +420,8 @@ std::shared_ptr<IzColsPlan> make_iz_cols_plan(int nrows, int ncols, const float*
     p.ncols = ncols;
     p.base_bands = bands / plan->n_cta;
     p.extra = bands % plan->n_cta;
+    p.short_tr = short_tr;
+    p.long_tr = long_tr;
     const void* arrays[kArrays];
     int a = 0;
     if (plan->eff) {
