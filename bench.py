@@ -158,14 +158,15 @@ def iz_plastic_workload():
         "dtype": "f32",
         # algorithmic bytes per launch of each profiled kernel group
         # (the subset connection never learns: its activator reads the
-        # product w * (R * w_stp), fixed during a run, instead of the three)
-        "group_bytes": {"izhikevich.activate.subset": 24 * sub,         # w R w_stp, delay, traces r+w
+        # product w * (R * w_stp), fixed during a run, instead of the three,
+        # and its delays as bytes)
+        "group_bytes": {"izhikevich.activate.subset": 21 * sub,         # w R w_stp, delay, traces r+w
                         "izhikevich.learn.convergent": 40 * conv,       # w, presyn, wd, stp r/w r+w
                         "izhikevich.activate.convergent": 32 * conv,
                         "izhikevich.activate.divergent": 32 * div,
                         "izhikevich.activate.one to one": 32 * one,
                         "izhikevich.update": 124 * 3 * n},
-        "bytes_per_timestep": 24 * sub + 32 * (conv + div + one) + 40 * conv + 3 * n * 124,
+        "bytes_per_timestep": 21 * sub + 32 * (conv + div + one) + 40 * conv + 3 * n * 124,
         "state_bytes": None,                            # taken from the run report
         "cpu_seconds": 15.0,
         "learning": True,
@@ -201,11 +202,12 @@ def iz_c0_workload():
         "units_per_timestep": conv + fc,
         "unit": "synapse-updates/s",
         "dtype": "f32",
-        # the recurrent connection never learns: w * (R * w_stp) in one array
-        "group_bytes": {"izhikevich.activate.fully connected": 24 * fc,
+        # the recurrent connection never learns: w * (R * w_stp) in one
+        # array, delays as bytes
+        "group_bytes": {"izhikevich.activate.fully connected": 21 * fc,
                         "izhikevich.activate.convergent": 28 * conv,    # FLOAT source: no delay read
                         "izhikevich.update": 124 * n},
-        "bytes_per_timestep": 24 * fc + 28 * conv + 124 * n,
+        "bytes_per_timestep": 21 * fc + 28 * conv + 124 * n,
         "l2_note": "34 MB per timestep: L2-resident within a bench step; flushed between steps",
         "state_bytes": None,
         "cpu_seconds": 10.0,

@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const uint32_t bar = smem_u32(&full[s]);
                 // the full box is counted, rows past the end included (zero-filled)
                 asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
-                             "r"((uint32_t)(NA * nb * kBlockFloats * 4))
+                             "r"((uint32_t)(((NA - HAS_D) * 4 + HAS_D) * nb * kBlockFloats))
                              : "memory");
                 for (int a = 0; a < NA; ++a)
                     tma_load2(smem_u32(tile(s, a)), &mp[a], ch * kBlockFloats, band0, bar);
@@ -313,7 +313,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int k = 0; k < kPer; ++k) {
                 const int o = eo[k] < 0 ? 0 : eo[k];
                 const uint32_t word = s_words[s][ej[k]];
-                const int delay = HAS_D ? __float_as_int(tile(s, A_D)[o]) : 0;
+                const int delay =
+                    HAS_D ? (int)reinterpret_cast<const uint8_t*>(tile(s, A_D))[o] : 0;
                 const float weight = EFF ? tw[o] : tw[o] * (tr[o] * tsw[o]);
                 term[k] = extract<SR>(word, delay) * weight;
                 st[k] = tst[o];
@@ -393,9 +394,29 @@ void fill_iz_effective_weights(size_t n, const float* w, const float* stp_r, con
     SG_LAUNCH_CHECK();
 }
 
+size_t iz_delay_bytes_pitch(int nrows) { return ((size_t)nrows * kBand + 15) / 16 * 16; }
+
+// d8[band][row * 8 + lane] (band pitch iz_delay_bytes_pitch) = delays[banded]
+__global__ void k_iz_delays_to_bytes(int nrows, int bands, size_t pitch,
+                                     const int* __restrict__ delays, uint8_t* __restrict__ d8) {
+    const size_t per = (size_t)nrows * kBand;
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= per * bands) return;
+    const size_t band = i / per, e = i - band * per;
+    d8[band * pitch + e] = (uint8_t)delays[i];
+}
+
+void fill_iz_delay_bytes(int nrows, int ncols, const int* delays, uint8_t* d8, cudaStream_t s) {
+    const int bands = (ncols + kBand - 1) / kBand;
+    const size_t n = (size_t)nrows * kBand * bands;
+    k_iz_delays_to_bytes<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+        nrows, bands, iz_delay_bytes_pitch(nrows), delays, d8);
+    SG_LAUNCH_CHECK();
+}
+
 std::shared_ptr<IzColsPlan> make_iz_cols_plan(int nrows, int ncols, const float* w,
                                               const float* stp_r, const float* stp_w,
-                                              const int* delays, float* short_tr,
+                                              const uint8_t* delays, float* short_tr,
                                               float* long_tr, const float* eff, int ctas) {
     if (nrows < 1 || ncols < 1) return nullptr;
     auto encode = encode_fn();
@@ -443,7 +464,11 @@ std::shared_ptr<IzColsPlan> make_iz_cols_plan(int nrows, int ncols, const float*
             cuuint64_t strides[1] = {(cuuint64_t)nrows * kBand * 4};
             cuuint32_t box[2] = {(cuuint32_t)kBlockFloats, (cuuint32_t)nb};
             cuuint32_t estr[2] = {1, 1};
-            CUresult r = encode(&plan->maps.m[wide][i], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+            // the delays are bytes, each band's rows padded to 16 bytes
+            const bool bytes = plan->has_delay && i == (plan->eff ? 1 : 3);
+            if (bytes) strides[0] = (cuuint64_t)iz_delay_bytes_pitch(nrows);
+            CUresult r = encode(&plan->maps.m[wide][i],
+                                bytes ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
                                 const_cast<void*>(arrays[i]), dims, strides, box, estr,
                                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B,

@@ -749,6 +749,10 @@ class IzhikevichModel : public Model {
             fill_iz_effective_weights(cs.weights->dev_count, cs.weights->df(),
                                       cs.var("short term R")->df(), cs.var("short term w")->df(),
                                       cs.eff_weights->df(), s);
+        int nrows = 0, ncols = 0;
+        if (cs.delays8 && matrix_shape(*cs.conn, nrows, ncols))
+            fill_iz_delay_bytes(nrows, ncols, cs.delays->di(),
+                                reinterpret_cast<uint8_t*>(cs.delays8->du()), s);
         if (!cs.delay_summary) return;
         const int n = cs.conn->from->size;
         k_iz_delay_summary<<<blocks_for(n, 256), 256, 0, s>>>(
@@ -803,10 +807,18 @@ class IzhikevichModel : public Model {
         // keeps w, R and w_stp for a whole run: the TMA activator reads their
         // product, w * (R * w_stp), from one array (8 bytes less per synapse
         // and step), refilled after every upload.
-        if ((c.type == FULLY_CONNECTED || c.type == SUBSET) && !c.plastic &&
-            c.parameter("direct", "false") != "true" && c.opcode != OP_GAP) {
+        const bool trace_cols = (c.type == FULLY_CONNECTED || c.type == SUBSET) &&
+                                c.parameter("direct", "false") != "true" && c.opcode != OP_GAP;
+        if (trace_cols && !c.plastic) {
             cs.eff_weights = st.add_array("effective weights", 'f', n, matrix_layout(c), R, C);
             cs.eff_weights->scratch = true;
+        }
+        // ... and reads its delays (below 32) as bytes
+        int nrows = 0, ncols = 0;
+        if (trace_cols && c.from->output_type == OUT_BIT && matrix_shape(c, nrows, ncols)) {
+            const size_t bytes = (size_t)((ncols + kBand - 1) / kBand) * iz_delay_bytes_pitch(nrows);
+            cs.delays8 = st.add_array("delay bytes", 'u', 0, LAYOUT_PLAIN, 1, 1, (bytes + 3) / 4);
+            cs.delays8->scratch = true;
         }
         // trace activators write conductances, not a register, and keep no
         // weight copy: second order only through the base activator
@@ -934,7 +946,8 @@ class IzhikevichModel : public Model {
                 const bool bit = c.from->output_type == OUT_BIT;
                 cs.device_plan = make_iz_cols_plan(
                     nrows, ncols, cs.weights->df(), cs.var("short term R")->df(),
-                    cs.var("short term w")->df(), bit ? cs.delays->di() : nullptr,
+                    cs.var("short term w")->df(),
+                    bit ? reinterpret_cast<const uint8_t*>(cs.delays8->du()) : nullptr,
                     cs.var("short trace")->df(), lname ? cs.var("long trace")->df() : nullptr,
                     cs.eff_weights ? cs.eff_weights->df() : nullptr);
             }

@@ -95,6 +95,11 @@ struct ConnState {
     // and refilled after every upload (device only, same layout as the
     // weights).
     Array* eff_weights = nullptr;
+    // Fully connected or subset trace connection from a BIT layer: its
+    // delays as bytes for the TMA activator, [band][row * 8 + lane] with each
+    // band's rows padded to 16 bytes (device only, refilled after every
+    // upload).
+    Array* delays8 = nullptr;
     // Second-order host: the per-step copy of its weights that the slaves
     // modulate and the host's activation reads (device only, same layout as
     // the weights; weight_matrix.cpp:79-80).
