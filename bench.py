@@ -162,11 +162,11 @@ def iz_plastic_workload():
         # and its delays as bytes)
         "group_bytes": {"izhikevich.activate.subset": 21 * sub,         # w R w_stp, delay, traces r+w
                         "izhikevich.learn.convergent": 40 * conv,       # w, presyn, wd, stp r/w r+w
-                        "izhikevich.activate.convergent": 32 * conv,
+                        "izhikevich.activate.convergent": 29 * conv,    # delays as bytes
                         "izhikevich.activate.divergent": 32 * div,
                         "izhikevich.activate.one to one": 32 * one,
                         "izhikevich.update": 124 * 3 * n},
-        "bytes_per_timestep": 21 * sub + 32 * (conv + div + one) + 40 * conv + 3 * n * 124,
+        "bytes_per_timestep": 21 * sub + 29 * conv + 32 * (div + one) + 40 * conv + 3 * n * 124,
         "state_bytes": None,                            # taken from the run report
         "cpu_seconds": 15.0,
         "learning": True,

@@ -265,7 +265,7 @@ constexpr int kConvMaxK = 128;
 template <int SR, bool LONG>
 __global__ void __launch_bounds__(256, 4) k_iz_activate_conv_tile(
     DGeom g, int K, const uint32_t* __restrict__ src, const float* __restrict__ w,
-    const float* __restrict__ stp_r, const float* __restrict__ stp_w, const int* __restrict__ delays,
+    const float* __restrict__ stp_r, const float* __restrict__ stp_w, const uint8_t* __restrict__ delays,
     float* __restrict__ short_tr, float* __restrict__ long_tr, float gcond, float short_tau,
     float long_tau, float* __restrict__ short_cond, float* __restrict__ long_cond) {
     __shared__ float s_st[kConvMaxK][32];
@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(256, 4) k_iz_activate_conv_tile(
             if (on[b]) {
                 const size_t wi = (size_t)k * g.to_size + d;
                 word[b] = __ldg(src + from);
-                dl[b] = SR == S_BIT ? __ldg(delays + wi) : 0;
+                dl[b] = SR == S_BIT ? (int)__ldg(delays + wi) : 0;
                 wv[b] = __ldg(w + wi);
                 rv[b] = __ldg(stp_r + wi);
                 sv[b] = __ldg(stp_w + wi);
@@ -736,6 +736,13 @@ static void iz_delays_and_visits(State& st, ConnState& cs) {
     }
 }
 
+// The delays (below 32) as bytes, element for element.
+__global__ void k_iz_delay_bytes_plain(size_t n, const int* __restrict__ delays,
+                                       uint8_t* __restrict__ d8) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) d8[i] = (uint8_t)delays[i];
+}
+
 class IzhikevichModel : public Model {
   public:
     const char* name() const override { return "izhikevich"; }
@@ -753,6 +760,10 @@ class IzhikevichModel : public Model {
         if (cs.delays8 && matrix_shape(*cs.conn, nrows, ncols))
             fill_iz_delay_bytes(nrows, ncols, cs.delays->di(),
                                 reinterpret_cast<uint8_t*>(cs.delays8->du()), s);
+        else if (cs.delays8)
+            k_iz_delay_bytes_plain<<<blocks_for((long)cs.delays->dev_count, 256), 256, 0, s>>>(
+                cs.delays->dev_count, cs.delays->di(),
+                reinterpret_cast<uint8_t*>(cs.delays8->du()));
         if (!cs.delay_summary) return;
         const int n = cs.conn->from->size;
         k_iz_delay_summary<<<blocks_for(n, 256), 256, 0, s>>>(
@@ -813,11 +824,17 @@ class IzhikevichModel : public Model {
             cs.eff_weights = st.add_array("effective weights", 'f', n, matrix_layout(c), R, C);
             cs.eff_weights->scratch = true;
         }
-        // ... and reads its delays (below 32) as bytes
+        // ... and reads its delays (below 32) as bytes, as does the
+        // convergent tile activator (same layout as the delays there)
         int nrows = 0, ncols = 0;
         if (trace_cols && c.from->output_type == OUT_BIT && matrix_shape(c, nrows, ncols)) {
             const size_t bytes = (size_t)((ncols + kBand - 1) / kBand) * iz_delay_bytes_pitch(nrows);
             cs.delays8 = st.add_array("delay bytes", 'u', 0, LAYOUT_PLAIN, 1, 1, (bytes + 3) / 4);
+            cs.delays8->scratch = true;
+        } else if (c.type == CONVERGENT && !c.convolutional && c.arbor.kernel() <= kConvMaxK &&
+                   c.parameter("direct", "false") != "true" && c.opcode != OP_GAP) {
+            cs.delays8 = st.add_array("delay bytes", 'u', 0, LAYOUT_PLAIN, 1, 1,
+                                      (cs.delays->dev_count + 3) / 4);
             cs.delays8->scratch = true;
         }
         // trace activators write conductances, not a register, and keep no
@@ -923,7 +940,8 @@ class IzhikevichModel : public Model {
 #define SG_CONV_TILE(SRV, LV)                                                                     \
     k_iz_activate_conv_tile<SRV, LV><<<nb, 256, 0, ctx.stream>>>(                                 \
         cs.geom, K, src, cs.weights->df(), cs.var("short term R")->df(),                        \
-        cs.var("short term w")->df(), cs.delays->di(), cs.var("short trace")->df(),             \
+        cs.var("short term w")->df(), reinterpret_cast<const uint8_t*>(cs.delays8->du()),        \
+        cs.var("short trace")->df(),                                                            \
         cs.var("long trace")->df(), g, stau, ltau, sc, lc)
             if (lname) {
                 if (sr == S_FLOAT) SG_CONV_TILE(S_FLOAT, true);
