@@ -34,6 +34,8 @@
 #include <cuda_pipeline.h>
 
 #include <algorithm>
+#include <cstdlib>
+#include <string>
 #include <mutex>
 
 #include "cuda_check.h"
@@ -377,7 +379,82 @@ struct IzColsPlan {
     int n_cta = 0, na = 0;
     bool has_delay = false, long_trace = false, eff = false;
     size_t smem = 0;
+    // few source rows: one CTA per band, no pipeline (k_iz_cols_small)
+    bool small = false;
+    const float *w = nullptr, *stp_r = nullptr, *stp_w = nullptr;
+    const uint8_t* delays = nullptr;
 };
+
+// Source rows up to which a band's pre-decay traces fit in shared memory
+// (2 x rows x 8 floats) and the one-pass kernel beats the TMA pipeline.
+constexpr int kSmallRows = 1536;
+
+// One-pass activator for matrices of at most kSmallRows source rows: one CTA
+// per band of 8 destinations reads the band's synapses with plain coalesced
+// loads (every synapse of the band in flight across the CTA), writes the
+// decayed traces back and the pre-decay traces to shared memory, then 8 (16
+// for two traces) threads add each destination's terms in source order.  The
+// float operations are the pipelined kernel's, in the same order.
+template <int SR, bool LONG, bool SUBSET, bool EFF>
+__global__ void __launch_bounds__(512) k_iz_cols_small(const ColsParams p, const float* __restrict__ w,
+                                                       const float* __restrict__ stp_r,
+                                                       const float* __restrict__ stp_w,
+                                                       const uint8_t* __restrict__ d8, size_t pitch) {
+    extern __shared__ float pre[];                         // [2][nrows * 8]
+    constexpr int U = 8;                                   // synapses a thread has in flight
+    const int band = blockIdx.x, n = p.nrows * kBand;
+    const size_t base = (size_t)band * n;
+    for (int e0 = threadIdx.x; e0 < n; e0 += U * blockDim.x) {
+        uint32_t word[U];
+        int delay[U];
+        float weight[U], st[U], lt[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int e = min(e0 + u * (int)blockDim.x, n - 1);
+            const size_t i = base + e;
+            word[u] = __ldg(p.src + source_of_row<SUBSET>(p.g, e >> 3));
+            delay[u] = SR == S_BIT ? (int)__ldg(d8 + (size_t)band * pitch + e) : 0;
+            weight[u] = EFF ? __ldg(w + i) : __ldg(w + i) * (__ldg(stp_r + i) * __ldg(stp_w + i));
+            st[u] = __ldcs(p.short_tr + i);
+            lt[u] = LONG ? __ldcs(p.long_tr + i) : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int e = e0 + u * (int)blockDim.x;
+            if (e >= n) break;
+            const size_t i = base + e;
+            const float add = (extract<SR>(word[u], delay[u]) * weight[u]) * p.gcond;
+            const float sv = st[u] + add;
+            pre[e] = sv;
+            __stcs(p.short_tr + i, sv * p.short_tau);
+            if (LONG) {
+                const float lv = lt[u] + add;
+                pre[n + e] = lv;
+                __stcs(p.long_tr + i, lv * p.long_tau);
+            }
+        }
+    }
+    __syncthreads();
+    const int kind = threadIdx.x >> 3, lane = threadIdx.x & 7;
+    if (threadIdx.x >= 16 || (kind == 1 && !LONG)) return;
+    const float* col = pre + kind * n + lane;
+    float acc = 0.0f;
+    int r = 0;
+    for (; r + 8 <= p.nrows; r += 8) {
+        float v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = col[(r + j) * kBand];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc += v[j];
+    }
+    for (; r < p.nrows; ++r) acc += col[r * kBand];
+    const int c = band * kBand + lane;
+    if (c < p.ncols) {
+        const int to = dest_of<SUBSET ? T_SUBSET : T_FC>(p.g, c);
+        if (kind == 0) p.short_cond[to] += acc;
+        else p.long_cond[to] += acc;
+    }
+}
 
 // w * (R * w_stp), the activator's weight of a synapse, over the whole banded
 // array (padding included)
@@ -432,6 +509,17 @@ std::shared_ptr<IzColsPlan> make_iz_cols_plan(int nrows, int ncols, const float*
     plan->has_delay = delays != nullptr;
     plan->long_trace = long_tr != nullptr;
     plan->eff = eff != nullptr;
+    plan->w = eff ? eff : w;
+    plan->stp_r = stp_r;
+    plan->stp_w = stp_w;
+    plan->delays = delays;
+    {
+        // SG_IZ_COLS_PATH=tma or small forces a path (tests run both)
+        const char* e = std::getenv("SG_IZ_COLS_PATH");
+        const std::string path = e ? e : "";
+        plan->small = path == "small" || (path != "tma" && nrows <= kSmallRows);
+        if (plan->small && nrows > kSmallRows) plan->small = false;
+    }
     plan->na = (plan->eff ? 2 : 4) + (plan->has_delay ? 1 : 0) + (plan->long_trace ? 1 : 0);
     plan->smem = cols_smem_bytes(plan->na);
     if ((long long)plan->smem > optin) return nullptr;
@@ -481,6 +569,20 @@ std::shared_ptr<IzColsPlan> make_iz_cols_plan(int nrows, int ncols, const float*
 
 template <int SR, bool LONG, bool SUBSET, bool EFF>
 static void launch_t(const IzColsPlan& plan, const ColsParams& p, cudaStream_t s) {
+    if (plan.small) {
+        const size_t bytes = (size_t)2 * p.nrows * kBand * sizeof(float);
+        static size_t small_configured = 0;
+        if (bytes > 48 * 1024 && small_configured < bytes) {
+            SG_CUDA(cudaFuncSetAttribute(k_iz_cols_small<SR, LONG, SUBSET, EFF>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+            small_configured = bytes;
+        }
+        const int bands = (p.ncols + kBand - 1) / kBand;
+        k_iz_cols_small<SR, LONG, SUBSET, EFF><<<bands, 512, bytes, s>>>(
+            p, plan.w, plan.stp_r, plan.stp_w, plan.delays, iz_delay_bytes_pitch(p.nrows));
+        SG_LAUNCH_CHECK();
+        return;
+    }
     static int configured = 0;
     if (configured < (int)plan.smem) {
         SG_CUDA(cudaFuncSetAttribute(k_iz_cols_bulk<SR, LONG, SUBSET, EFF>,

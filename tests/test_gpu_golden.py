@@ -42,6 +42,20 @@ def test_library_matches_reference_fixture(syngen, name):
     assert not problems, problems
 
 
+@pytest.mark.parametrize("path", ["tma", "small"])
+@pytest.mark.parametrize("name", ["iz_c0_8", "iz_c0_32", "iz_opcodes", "iz_plastic",
+                                  "iz_subset_columns"])
+def test_izhikevich_matrix_activator_paths(syngen, name, path, monkeypatch):
+    """Fully connected and subset Izhikevich connections take the TMA pipeline
+    or, for few source rows, the one-pass kernel; each path alone matches the
+    reference's fixture."""
+    monkeypatch.setenv("SG_IZ_COLS_PATH", path)
+    case = CASES[name]
+    got = run_library(case, syngen)
+    problems = compare(got, load_fixture(name), nan_keys=float_like_keys(case))
+    assert not problems, problems
+
+
 @pytest.mark.parametrize("name", ["iz_c0_32", "iz_plastic", "gol_16x16"])
 def test_library_matches_oracle_longer(syngen, name):
     case = CASES[name]

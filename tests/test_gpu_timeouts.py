@@ -23,7 +23,8 @@ def sg():
     return syngen
 
 
-def test_tma_wait_timeout_is_reported(sg):
+def test_tma_wait_timeout_is_reported(sg, monkeypatch):
+    monkeypatch.setenv("SG_IZ_COLS_PATH", "tma")     # this case's rows would take the one-pass kernel
     lib = ctypes.CDLL(sg.LIB_PATH)
     lib.sg_test_cols_skip_chunk.argtypes = (ctypes.c_int,)
     lib.sg_test_cols_skip_chunk.restype = ctypes.c_bool
