@@ -357,6 +357,17 @@ __global__ void __launch_bounds__(kBlock) k_rate_fused(
 #pragma unroll
         for (int k = 0; k < (kRegLast ? K : 1); ++k) wlast[k] = wl[k * kTileSide * kTileSide];
     }
+    // Layer 1, when it is not the last: the weights of the thread's first
+    // position (p = tid) in registers too, the other positions' from shared
+    // memory.
+    constexpr bool kRegMid = F <= 5;
+    float wmid[kRegMid ? K : 1];
+    if (kRegMid && D.L >= 3) {
+        const int sd1 = R.side(1);
+        const float* wl = ws + R.woff(1, K) + tid;
+#pragma unroll
+        for (int k = 0; k < (kRegMid ? K : 1); ++k) wmid[k] = wl[k * sd1 * sd1];
+    }
     const int lane = tid & 31, warp = tid >> 5;
     for (int tt = 1; tt <= nt; ++tt) {
         const int t = c + tt, cur = (tt - 1) & 1;
@@ -395,6 +406,15 @@ __global__ void __launch_bounds__(kBlock) k_rate_fused(
 #pragma unroll
                             for (int kc = 0; kc < F; ++kc)
                                 part[kr] = __fmaf_rn(wlast[kRegLast ? kr * F + kc : 0],
+                                                     src[kr * sp + kc], part[kr]);
+                        }
+                    } else if (kRegMid && l == 1 && p == tid) {
+#pragma unroll
+                        for (int kr = 0; kr < F; ++kr) {
+                            part[kr] = 0.0f;
+#pragma unroll
+                            for (int kc = 0; kc < F; ++kc)
+                                part[kr] = __fmaf_rn(wmid[kRegMid ? kr * F + kc : 0],
                                                      src[kr * sp + kc], part[kr]);
                         }
                     } else {
