@@ -157,16 +157,24 @@ def iz_plastic_workload():
         "unit": "synapse-updates/s",
         "dtype": "f32",
         # algorithmic bytes per launch of each profiled kernel group
-        # (the subset connection never learns: its activator reads the
-        # product w * (R * w_stp), fixed during a run, instead of the three,
-        # and its delays as bytes)
-        "group_bytes": {"izhikevich.activate.subset": 21 * sub,         # w R w_stp, delay, traces r+w
-                        "izhikevich.learn.convergent": 40 * conv,       # w, presyn, wd, stp r/w r+w
-                        "izhikevich.activate.convergent": 29 * conv,    # delays as bytes
+        # algorithmic bytes per launch of each profiled kernel group, the
+        # per-synapse and per-neuron figures of the reference's data:
+        # activator 32 B (w, stp r, stp w, delay, short and long trace r+w),
+        # updater 40 B (w, presyn, wd, stp r/w, each read and written),
+        # neuron 124 B
+        "group_bytes": {"izhikevich.activate.subset": 32 * sub,
+                        "izhikevich.learn.convergent": 40 * conv,
+                        "izhikevich.activate.convergent": 32 * conv,
                         "izhikevich.activate.divergent": 32 * div,
                         "izhikevich.activate.one to one": 32 * one,
                         "izhikevich.update": 124 * 3 * n},
-        "bytes_per_timestep": 21 * sub + 29 * conv + 32 * (div + one) + 40 * conv + 3 * n * 124,
+        "bytes_per_timestep": 32 * activate + 40 * conv + 3 * n * 124,
+        # what this design moves: the subset connection never learns, so its
+        # activator reads the product w * (R * w_stp), fixed during a run,
+        # instead of the three arrays, and every activator here reads its
+        # delays from a byte copy (21 and 29 B per synapse)
+        "moved_bytes": {"izhikevich.activate.subset": 21 * sub,
+                        "izhikevich.activate.convergent": 29 * conv},
         "state_bytes": None,                            # taken from the run report
         "cpu_seconds": 15.0,
         "learning": True,
@@ -202,12 +210,13 @@ def iz_c0_workload():
         "units_per_timestep": conv + fc,
         "unit": "synapse-updates/s",
         "dtype": "f32",
-        # the recurrent connection never learns: w * (R * w_stp) in one
-        # array, delays as bytes
-        "group_bytes": {"izhikevich.activate.fully connected": 21 * fc,
+        "group_bytes": {"izhikevich.activate.fully connected": 32 * fc,
                         "izhikevich.activate.convergent": 28 * conv,    # FLOAT source: no delay read
                         "izhikevich.update": 124 * n},
-        "bytes_per_timestep": 21 * fc + 28 * conv + 124 * n,
+        "bytes_per_timestep": 32 * fc + 28 * conv + 124 * n,
+        # the recurrent connection never learns: w * (R * w_stp) in one
+        # array, delays as bytes
+        "moved_bytes": {"izhikevich.activate.fully connected": 21 * fc},
         "l2_note": "34 MB per timestep: L2-resident within a bench step; flushed between steps",
         "state_bytes": None,
         "cpu_seconds": 10.0,
@@ -1070,6 +1079,12 @@ def main():
                 "word_layout_bytes_per_timestep": wl.get("word_layout_timestep_bytes")}
     if wl.get("shares"):
         roofline["profiled_shares"] = wl["shares"]
+    moved = (wl.get("moved_bytes") or {}).get(wl["dominant"])
+    if moved and r["mean_us"]:
+        # the bytes this design's kernel must move (fewer than the
+        # reference's data holds), over the same launch time
+        roofline["moved_bytes_per_launch"] = moved
+        roofline["moved_frac"] = moved / (r["mean_us"] * 1e-6) / 1e9 / peak
     if wl.get("bytes_per_timestep"):
         # the whole timestep: every kernel's algorithmic bytes over the
         # device time per timestep
