@@ -264,6 +264,11 @@ def spnet_sparse_workload(side=256):
         wl["synapses"] = counts
         wl["units_per_timestep"] = sum(counts.values()) + counts["ee"]   # activations + STDP
         wl["bytes_per_launch"] = 28 * counts["ee"]
+        # the profiled groups this line can name: the STDP kernel (weight,
+        # presynaptic trace and weight derivative read and written, source
+        # index) and the three activations (weight, delay, source index)
+        wl["group_bytes"] = {"spnet.learn.sparse": 28 * counts["ee"],
+                             "spnet.activate.sparse": 12 * sum(counts.values()) // 3}
 
     def result(net_obj):
         return net_obj.get_neuron_data("s", "exc", "output").to_np_array()

@@ -159,6 +159,23 @@ SG_FF bool product(float p, float c1, float c2, float& out) {
     return true;
 }
 
+// (float)((double)x + k) for a double constant k ~ k1 + k2 (two floats, k2
+// the rounded remainder): the exact sum of x and k1 plus the remainder's,
+// which errs by at most 2^-24 (|e| + |k2|) <= 2^-48 (|s| + |k1|), s = RN(x +
+// k1); the double addition it stands for errs by at most 2^-53 |x + k| and
+// the split of k by 2^-48 |k1|: the bound 2^-43 (|s| + |k1|) covers all three
+// with a factor of 10 to spare.
+SG_FF bool add_const(float x, float k1, float k2, float& out) {
+    float s, e;
+    two_sum(x, k1, s, e);
+    e = add(e, k2);
+    float f, g;
+    two_sum(s, e, f, g);
+    if (!rounds_to(f, g, mul(add(absf(s), absf(k1)), kBound5))) return false;
+    out = f;
+    return true;
+}
+
 // Weight derivative of the STDP updater: (float)(x - c) with
 //   c = ((x - 1e-6) * 1e-4 [+ p] [- q])
 // in double, x = wd, p = dest_spike * src_trace and q = src_spike *

@@ -1209,9 +1209,11 @@ static __device__ __noinline__ float spnet_dw_full(float dw0, float f1, float f2
 
 // Sparse connections: one thread per compacted synapse (blockIdx.y is the
 // synapse's rank within its destination, x the destination), since each
-// synapse's update is independent.  The products with 0.9 / 0.95 go through
-// the integer helpers; the double sums stay double.  Bit-identical to
-// k_spnet_learn.
+// synapse's update is independent.  The products with 0.9 / 0.95 and the
+// sums with 0.1 / 0.01 are float-float evaluations with a rounding test
+// (ff_exact.cuh), falling back to the integer helpers and double sums where
+// the test rejects; the full weight-derivative sum with spike terms stays
+// double.  Bit-identical to k_spnet_learn.
 template <int SR, bool SUB>
 __global__ void __launch_bounds__(256) k_spnet_learn_sparse(DGeom g, const uint32_t* __restrict__ dest_out,
                                                             const float* __restrict__ post,
@@ -1233,8 +1235,13 @@ __global__ void __launch_bounds__(256) k_spnet_learn_sparse(DGeom g, const uint3
     if (!SUB) {
         const float p = presyn[wi];
         float np;
-        if (src_spike) np = spnet_trace_step(p);
-        else np = mul_fd_rn(p, 0.95);
+        constexpr float T1 = (float)0.1, T2 = (float)(0.1 - (double)T1);
+        constexpr float D1 = (float)0.95, D2 = (float)(0.95 - (double)D1);
+        if (src_spike) {
+            if (!ff::add_const(p, T1, T2, np)) np = spnet_trace_step(p);
+        } else if (!ff::product(p, D1, D2, np)) {
+            np = mul_fd_rn(p, 0.95);
+        }
         src_trace = presyn[wi] = np;
         dest_trace = post[d];
     } else {
@@ -1248,10 +1255,16 @@ __global__ void __launch_bounds__(256) k_spnet_learn_sparse(DGeom g, const uint3
     // 0.9 dw + f1 - f2 in double: with f1, f2 zero and dw nonzero it is the
     // rounded product alone
     float dw;
-    if (f1 == 0.0f && f2 == 0.0f && dw0 != 0.0f) dw = mul_fd_rn(dw0, 0.9);
-    else dw = spnet_dw_full(dw0, f1, f2);
+    constexpr float N1 = (float)0.9, N2 = (float)(0.9 - (double)N1);
+    constexpr float S1 = (float)0.01, S2 = (float)(0.01 - (double)S1);
+    if (f1 == 0.0f && f2 == 0.0f && dw0 != 0.0f) {
+        if (!ff::product(dw0, N1, N2, dw)) dw = mul_fd_rn(dw0, 0.9);
+    } else {
+        dw = spnet_dw_full(dw0, f1, f2);
+    }
     dws[wi] = dw;
-    const float weight_delta = d2f_rn(__dadd_rn(f2d_exact(dw), 0.01));
+    float weight_delta;
+    if (!ff::add_const(dw, S1, S2, weight_delta)) weight_delta = d2f_rn(__dadd_rn(f2d_exact(dw), 0.01));
     weight += lr * weight_delta;
     const float capped = (max_weight < weight) ? max_weight : weight;
     w[wi] = (0.0001f > capped) ? 0.0001f : capped;

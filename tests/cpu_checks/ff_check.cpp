@@ -199,6 +199,62 @@ int check_product_strided(unsigned long long stride, unsigned long long offset, 
     return 0;
 }
 
+// Every float p with (bits - offset) % stride == 0: (float)((double)p * c).
+int check_product_c_strided(double c, unsigned long long stride, unsigned long long offset,
+                            Result* r) {
+    r->mismatches = r->checked = r->fallbacks = 0;
+    r->first = ~0ull;
+    const float c1 = (float)c, c2 = (float)(c - (double)c1);
+#pragma omp parallel
+    {
+        Result l{0, 0, 0, ~0ull};
+#pragma omp for schedule(static)
+        for (long long i = (long long)offset; i < (1ll << 32); i += (long long)stride) {
+            const float p = ffrom((uint32_t)i);
+            float out;
+            ++l.checked;
+            if (!sg::ff::product(p, c1, c2, out)) {
+                ++l.fallbacks;
+                continue;
+            }
+            if (!same(out, (float)((double)p * c))) {
+                ++l.mismatches;
+                if ((unsigned long long)i < l.first) l.first = (unsigned long long)i;
+            }
+        }
+        merge(r, l);
+    }
+    return 0;
+}
+
+// Every float x with (bits - offset) % stride == 0: (float)((double)x + k).
+int check_add_const_strided(double k, unsigned long long stride, unsigned long long offset,
+                            Result* r) {
+    r->mismatches = r->checked = r->fallbacks = 0;
+    r->first = ~0ull;
+    const float k1 = (float)k, k2 = (float)(k - (double)k1);
+#pragma omp parallel
+    {
+        Result l{0, 0, 0, ~0ull};
+#pragma omp for schedule(static)
+        for (long long i = (long long)offset; i < (1ll << 32); i += (long long)stride) {
+            const float x = ffrom((uint32_t)i);
+            float out;
+            ++l.checked;
+            if (!sg::ff::add_const(x, k1, k2, out)) {
+                ++l.fallbacks;
+                continue;
+            }
+            if (!same(out, (float)((double)x + k))) {
+                ++l.mismatches;
+                if ((unsigned long long)i < l.first) l.first = (unsigned long long)i;
+            }
+        }
+        merge(r, l);
+    }
+    return 0;
+}
+
 // Every float a with (bits - offset) % stride == 0: div_int<D>(a) == a / D.
 int check_div_strided(int D, unsigned long long stride, unsigned long long offset, Result* r) {
     r->mismatches = r->checked = r->fallbacks = 0;

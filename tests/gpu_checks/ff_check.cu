@@ -92,6 +92,37 @@ __global__ void k_product_all(Result* r) {
     atomicAdd(&r->fallbacks, fallbacks);
 }
 
+// every float bit pattern: (float)((double)p * c) and (float)((double)x + k)
+__global__ void k_product_c_all(double c, Result* r) {
+    const float c1 = (float)c, c2 = (float)(c - (double)c1);
+    unsigned long long checked = 0, fallbacks = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+         i < (1ull << 32); i += (unsigned long long)gridDim.x * blockDim.x) {
+        const float p = __uint_as_float((uint32_t)i);
+        float out;
+        ++checked;
+        if (!sg::ff::product(p, c1, c2, out)) { ++fallbacks; continue; }
+        record(r, !same(out, __double2float_rn(__dmul_rn((double)p, c))), i);
+    }
+    atomicAdd(&r->checked, checked);
+    atomicAdd(&r->fallbacks, fallbacks);
+}
+
+__global__ void k_add_const_all(double k, Result* r) {
+    const float k1 = (float)k, k2 = (float)(k - (double)k1);
+    unsigned long long checked = 0, fallbacks = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+         i < (1ull << 32); i += (unsigned long long)gridDim.x * blockDim.x) {
+        const float x = __uint_as_float((uint32_t)i);
+        float out;
+        ++checked;
+        if (!sg::ff::add_const(x, k1, k2, out)) { ++fallbacks; continue; }
+        record(r, !same(out, __double2float_rn(__dadd_rn((double)x, k))), i);
+    }
+    atomicAdd(&r->checked, checked);
+    atomicAdd(&r->fallbacks, fallbacks);
+}
+
 // every float bit pattern: div_int<D>(a) == a / D (IEEE)
 template <int D>
 __global__ void k_div_all(Result* r) {
@@ -222,6 +253,18 @@ int check_wd_all(unsigned long long* out) {
 
 int check_product_all(unsigned long long* out) {
     return run([](Result* d) { k_product_all<<<152 * 8, 256>>>(d); }, out);
+}
+
+int check_product_c_all(double c, unsigned long long* out) {
+    static double cc;
+    cc = c;
+    return run([](Result* d) { k_product_c_all<<<152 * 8, 256>>>(cc, d); }, out);
+}
+
+int check_add_const_all(double k, unsigned long long* out) {
+    static double kk;
+    kk = k;
+    return run([](Result* d) { k_add_const_all<<<152 * 8, 256>>>(kk, d); }, out);
 }
 
 int check_div_all(int D, unsigned long long* out) {

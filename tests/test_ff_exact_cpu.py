@@ -48,6 +48,24 @@ def test_trace_decay_product_strided(lib):
     _check(r, 0.16)       # non-finite and huge operands, results below 2^-126
 
 
+@pytest.mark.parametrize("c", [0.95, 0.9])
+def test_spnet_decay_products_strided(lib, c):
+    """spnet's presynaptic trace and weight derivative decays."""
+    r = Result()
+    lib.check_product_c_strided(ctypes.c_double(c), ctypes.c_ulonglong(61), ctypes.c_ulonglong(11),
+                                ctypes.byref(r))
+    _check(r, 0.16)
+
+
+@pytest.mark.parametrize("k", [0.01, 0.1])
+def test_sum_with_double_constant_strided(lib, k):
+    """spnet's weight step (dw + 0.01) and trace step (p + 0.1)."""
+    r = Result()
+    lib.check_add_const_strided(ctypes.c_double(k), ctypes.c_ulonglong(61), ctypes.c_ulonglong(13),
+                                ctypes.byref(r))
+    _check(r, 0.16)       # non-finite operands and results outside the normal range
+
+
 @pytest.mark.parametrize("divisor", [60, 700, 800])
 def test_division_by_integer_strided(lib, divisor):
     r = Result()

@@ -55,6 +55,22 @@ def test_trace_decay_product_every_float(lib):
     _ok(out, 0.16)        # non-finite and huge operands, results below 2^-126
 
 
+@pytest.mark.parametrize("c", [0.95, 0.9])
+def test_spnet_decay_products_every_float(lib, c):
+    out = _out()
+    assert lib.check_product_c_all(ctypes.c_double(c), out) == 0
+    assert out[1] == 1 << 32
+    _ok(out, 0.16)
+
+
+@pytest.mark.parametrize("k", [0.01, 0.1])
+def test_sum_with_double_constant_every_float(lib, k):
+    out = _out()
+    assert lib.check_add_const_all(ctypes.c_double(k), out) == 0
+    assert out[1] == 1 << 32
+    _ok(out, 0.16)
+
+
 @pytest.mark.parametrize("divisor", [60, 700, 800])
 def test_division_by_integer_every_float(lib, divisor):
     out = _out()
