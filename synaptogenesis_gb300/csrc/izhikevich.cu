@@ -1125,10 +1125,34 @@ __global__ void __launch_bounds__(128) k_spnet_activate(DGeom g, const uint32_t*
     const int d = blockIdx.x * blockDim.x + threadIdx.x;
     if (d >= g.n_dest) return;
     float sum = 0.0f;
-    for_each_source<TY>(g, d, [&](int from, int wi) {
-        const float spike = extract<SR>(src[from], delays[wi]);
-        sum += spike * w[wi] * gc;
-    });
+    if constexpr (TY == T_SPARSE) {
+        // 8 synapses' loads in flight, then their terms in order
+        constexpr int U = 8;
+        const int n = g.nz[d];
+        int i = 0, wi = d;
+        for (; i + U <= n; i += U, wi += U * g.to_size) {
+            int fr[U], dl[U];
+            float wv[U];
+            uint32_t word[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int j = wi + u * g.to_size;
+                fr[u] = g.sfrom[j];
+                dl[u] = delays[j];
+                wv[u] = w[j];
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) word[u] = src[fr[u]];
+#pragma unroll
+            for (int u = 0; u < U; ++u) sum += extract<SR>(word[u], dl[u]) * wv[u] * gc;
+        }
+        for (; i < n; ++i, wi += g.to_size) sum += extract<SR>(src[g.sfrom[wi]], delays[wi]) * w[wi] * gc;
+    } else {
+        for_each_source<TY>(g, d, [&](int from, int wi) {
+            const float spike = extract<SR>(src[from], delays[wi]);
+            sum += spike * w[wi] * gc;
+        });
+    }
     const int to = dest_of<TY>(g, d);
     inputs[to] = aggregate(inputs[to], sum, opcode);
 }
@@ -1224,16 +1248,25 @@ __global__ void __launch_bounds__(256) k_spnet_learn_sparse(DGeom g, const uint3
                                                             float* __restrict__ dws, IzLut lut) {
     const int d = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y;
-    if (d >= g.to_size || i >= g.nz[d]) return;
+    if (d >= g.to_size) return;
+    // every load that depends on nothing but the synapse's position first
+    // (the [kmax][to] arrays are allocated for the padding too), then the
+    // checks, then the source's time since spike
     const int wi = i * g.to_size + d;
+    const int n = g.nz[d];
     float weight = w[wi];
-    if (!(weight >= 0.0001f)) return;
-    const int stss = from_tss[g.sfrom[wi]];
+    const int from = g.sfrom[wi];
+    const float p = SUB ? 0.0f : presyn[wi];
+    const float dw0 = dws[wi];
+    const uint32_t dword = dest_out[d];
+    const float dest_exc = SUB ? 0.0f : post[d];
+    const int dtss = SUB ? to_tss[d] : 0;
+    if (i >= n || !(weight >= 0.0001f)) return;
+    const int stss = from_tss[from];
     const bool src_spike = stss == 0;
-    const float dest_spike = extract<SR>(dest_out[d], 0);    // the source's extractor
+    const float dest_spike = extract<SR>(dword, 0);          // the source's extractor
     float src_trace, dest_trace;
     if (!SUB) {
-        const float p = presyn[wi];
         float np;
         constexpr float T1 = (float)0.1, T2 = (float)(0.1 - (double)T1);
         constexpr float D1 = (float)0.95, D2 = (float)(0.95 - (double)D1);
@@ -1243,15 +1276,13 @@ __global__ void __launch_bounds__(256) k_spnet_learn_sparse(DGeom g, const uint3
             np = mul_fd_rn(p, 0.95);
         }
         src_trace = presyn[wi] = np;
-        dest_trace = post[d];
+        dest_trace = dest_exc;
     } else {
-        const int dtss = to_tss[d];
         src_trace = (dest_spike > 0.0f && stss > 0 && stss < 32) ? lut.src[stss] : 0.0f;
         dest_trace = (src_spike && dtss > 0 && dtss < 32) ? lut.dst[dtss] : 0.0f;
     }
     const float f1 = dest_spike * src_trace;
     const float f2 = (src_spike ? 1.0f : 0.0f) * dest_trace;
-    const float dw0 = dws[wi];
     // 0.9 dw + f1 - f2 in double: with f1, f2 zero and dw nonzero it is the
     // rounded product alone
     float dw;
